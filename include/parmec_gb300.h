@@ -1,0 +1,243 @@
+/*
+ * parmec_gb300.h -- C ABI of the GB300 (sm_103a) implementation of Parmec's
+ * explicit DEM time step.
+ *
+ * Two surfaces are exported by libparmec_gb300.so:
+ *
+ *  (1) Compat entry points with the exact names and argument lists of the ISPC
+ *      exports that Parmec's host loop calls (parmec.cpp:2386-2517).  Each takes
+ *      host structure-of-arrays pointers, copies them to a device mirror, runs
+ *      the CUDA kernels and copies the results back, so an unmodified parmec.cpp
+ *      can link against this library instead of the ISPC objects.  They are
+ *      declared inside namespace ispc for C++ callers, as ISPC's generated
+ *      headers do (parmec.cpp:46-55).
+ *
+ *  (2) A device-resident session API (pg_session_*): the whole scene lives in
+ *      HBM, one call advances many steps.  This is what the Python DEM()
+ *      command and the benchmarks use.
+ *
+ * All REAL arguments are double (the reference's -DREAL=8 build, macros.h:60).
+ * Every function returns an int status (PG_OK, or a negative PG_ERR_*) where the
+ * reference would have called ASSERT/exit.  No function falls back to the CPU:
+ * without a CUDA device they return PG_ERR_CUDA.
+ */
+#ifndef PARMEC_GB300_H
+#define PARMEC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define PG_OK                 0
+#define PG_ERR_CUDA         (-1)  /* a CUDA runtime call failed */
+#define PG_ERR_CAPACITY     (-2)  /* a per-particle list overflowed; the session re-sizes and re-runs */
+#define PG_ERR_ARGUMENT     (-3)  /* invalid argument (size, index, null pointer) */
+#define PG_ERR_UNSUPPORTED  (-4)  /* a case the reference asserts on (ellipsoids, USER_FORCE) */
+#define PG_ERR_TIMEOUT      (-5)  /* a bounded device wait gave up */
+
+/* ---- constants shared with the reference (constants.h:33-64) ------------- */
+#define PG_NIPARAM 7              /* SPRING, DAMPER, FRISTAT, FRIDYN, FRIROL, FRIDRIL, KSKN */
+#define PG_SPRING_NONLINEAR_ELASTIC 0
+#define PG_SPRING_GENERAL_NONLINEAR 1
+#define PG_SPRING_YIELDED   1
+#define PG_SPRING_UNLOADING 2
+#define PG_SPRDIR_CONSTANT  4
+#define PG_SPRDIR_PLANAR    8
+#define PG_SPRDIR_FOLLOWER  16
+#define PG_SPRDIR_PROJECT   32
+#define PG_FLAG_ANALYTICAL  1
+#define PG_FLAG_OUTREST     2
+#define PG_FLAG_SKIP        4
+
+/* ---- reference-defect switches (pg_scene.compat bits) -------------------- */
+/* expmap's v02 = Omega2*Omega3 typo (macros.h:1505); ON reproduces it.        */
+#define PG_COMPAT_EXPMAP    1
+/* moving obstacle k's contacts read obstacle k+1's point and velocity
+ * (input.cpp:1391,1433 vs forces.ispc:265); ON reproduces it.                 */
+#define PG_COMPAT_OBSIDX    2
+/* triangle_sphere's region s >= 0, t < 0, s+t >= det, a+d <= b+e takes the
+ * ac-edge parameter -e/c for s (condet.ispc:371-375, 597-601), so a centre
+ * beyond vertex b is matched to vertex a; ON reproduces it, OFF uses the
+ * ab-edge parameter -d/a.                                                     */
+#define PG_COMPAT_TRIEDGE   4
+
+/*
+ * Host description of one scene: the reference's global SoA buffers
+ * (parmec.cpp:61-285) as plain pointers.  One pointer per vector component,
+ * exactly like the reference (e.g. position[0..2] current, [3..5] reference;
+ * rotation is a column-major 3x3, macros.h:945).  Arrays a scene does not use
+ * may be NULL when their count is zero.
+ */
+typedef struct pg_scene {
+  /* particles (parmec.cpp:95-114) */
+  int parnum;
+  double *angular[6];   /* [0..2] referential Omega, [3..5] spatial omega */
+  double *linear[3];
+  double *rotation[9];
+  double *position[6];
+  double *inertia[9];
+  double *inverse[9];
+  double *mass;
+  double *invm;
+  double *force[3];
+  double *torque[3];
+  int *flags;
+  int *parmat;
+
+  /* spheres (parmec.cpp:86-93); radii[1] < 0 marks a sphere */
+  int ellnum;
+  double *center[6];
+  double *radii[3];
+  int *ellcol;
+  int *part;
+
+  /* triangles (parmec.cpp:116-121): tri[vertex][coord][index] */
+  int trinum;
+  double *tri[3][3];
+  int *tricol;
+  int *triobs;          /* -1 static, -k-2 moving obstacle k, >=0 mesh particle */
+
+  /* moving obstacles */
+  int obsnum;
+  int *trirng;          /* [2*obsnum] triangle ranges */
+  double *obspnt;       /* [3*obsnum] rotation points (updated by obstacles) */
+  double *obsang;       /* [3*obsnum] current angular velocities (last obstaclev) */
+  double *obslin;       /* [3*obsnum] current linear velocities (last obstaclev) */
+
+  /* surface pairing (sorted by sort_materials, parmec.cpp:1636) */
+  int pairnum;
+  int *pairs;           /* [2*pairnum] colour pairs */
+  int *ikind;           /* [pairnum] GRANULAR_FORCE = 0 */
+  double *iparam[PG_NIPARAM];
+
+  /* meshed particles: nodes and faces (parmec.cpp nodes/facnod/factri) */
+  int nodnum;
+  double *nodes[6];     /* [0..2] current, [3..5] reference */
+  int *nodpart;
+  int facnum;
+  int *facnod[3];
+  int *factri;
+
+  /* translational springs, sorted by (part0, part1) (parmec.cpp:151-178) */
+  int sprnum;
+  int *sprtype;
+  int *unspring;
+  int *sprpart[2];
+  double *sprpnt[2][6];
+  double *spring[2];  int *spridx;
+  double *dashpot[2]; int *dashidx;
+  double *unload[2];  int *unidx;
+  double *yield[2];
+  double *sprdir[6];
+  int *sprflg;
+  int *sproffset;
+  double *sprfric;
+  double *sprkskn;
+  double *sprsdsp[3];
+  double *stroke0;
+  double *stroke[3];
+  double *sprfrc[3];
+  double *lcurve[2];  int *lcidx;
+
+  /* prescribed motion (input.cpp:2647-2795); values come per step */
+  int prsnum;
+  int *prspart;
+  int *prslin;          /* 1 when the linear motion is prescribed */
+  int *prsang;          /* 1 when the angular motion is prescribed */
+  int *linkind;         /* 0 velocity, 1 acceleration */
+  int *angkind;
+
+  int compat;           /* PG_COMPAT_* bits */
+} pg_scene;
+
+/*
+ * Per-step host inputs of the time loop.  The reference evaluates these through
+ * Python callbacks or TSERIES inside the loop (input.cpp:4199-4503); the host
+ * samples them at the same times before the steps run.  Row s belongs to step
+ * s of this call.  NULL means "zero for every step".
+ */
+typedef struct pg_steptab {
+  int nsteps;
+  const double *curtime;   /* [n]  time at the start of each step */
+  const double *gravity;   /* [n][3] at curtime */
+  const double *damping;   /* [n][6] at curtime */
+  const double *prs_lin;   /* [n][prsnum][3] at curtime */
+  const double *prs_ang;   /* [n][prsnum][3] at curtime */
+  const double *obs_ang;   /* [n][obsnum][3] at curtime+step */
+  const double *obs_lin;   /* [n][obsnum][3] at curtime+step */
+} pg_steptab;
+
+/* ======================================================================== */
+/* (2) Device-resident session API                                          */
+/* ======================================================================== */
+typedef struct pg_session pg_session;
+
+/* Numeric form of a session. */
+#define PG_FORM_FP64   0   /* plain FP64, bit-exact with the oracle */
+#define PG_FORM_MIXED  1   /* FP32 contact geometry and forces, FP64 positions/rotations */
+
+/* Create a session on the current CUDA device and upload the scene.
+ * Replaces the buffer set-up of init()/input() (parmec.cpp:2227) plus the
+ * per-DEM partitioning_create (partition.ispc:663). */
+int pg_session_create(const pg_scene *scene, int form, pg_session **out);
+
+/* Release all device memory of the session. */
+int pg_session_destroy(pg_session *s);
+
+/* The curtime == 0 block of dem() (parmec.cpp:2397-2405): euler(0.5*step),
+ * full shapes, obstacle velocities at 0.5*step and obstacles(step). */
+int pg_session_first_half_step(pg_session *s, double step,
+                               const double *obs_ang, const double *obs_lin);
+
+/* invert_inertia (parmec.ispc:90), called by dem() at every DEM call. */
+int pg_session_invert_inertia(pg_session *s);
+
+/* Advance tab->nsteps steps of the loop body of dem() (parmec.cpp:2418-2517)
+ * with a fixed step (adaptive == 0).  Asynchronous on the session stream. */
+int pg_session_run(pg_session *s, const pg_steptab *tab, double step);
+
+/* Wait for the session stream; returns the first device error seen. */
+int pg_session_sync(pg_session *s);
+
+/* Copy the dynamic state back into the host arrays of 'scene' (the same
+ * layout that was uploaded): particles, spheres, triangles, obstacles,
+ * nodes and spring state. */
+int pg_session_download(pg_session *s, pg_scene *scene);
+
+/* Re-upload every dynamic array from the host (after host edits between DEM calls). */
+int pg_session_upload(pg_session *s, const pg_scene *scene);
+
+/* Number of active contact points (master side). */
+int pg_session_contact_count(pg_session *s, int *count);
+
+/* Export the active contacts in the canonical order (master particle, then
+ * partner code).  code >= 0 is the slave ellipsoid, code < 0 is -(triangle+1).
+ * Arrays hold 'cap' entries; *count returns the number written. */
+int pg_session_contacts(pg_session *s, int cap, int *count,
+                        int *master_particle, int *code,
+                        double *point, double *normal, double *depth,
+                        double *force, double *state);
+
+/* CUDA stream used by the session (cudaStream_t as void*). */
+int pg_session_stream(pg_session *s, void **stream);
+
+/* Number of kernels the last pg_session_run launched (for bench accounting). */
+int pg_session_kernel_launches(pg_session *s, long long *count);
+
+/* Set the skin (Verlet margin) used by contact detection, in length units.
+ * A negative value selects the automatic choice. */
+int pg_session_set_skin(pg_session *s, double skin);
+
+/* Record contact normals and depths as well (for parity exports; costs
+ * bandwidth, off by default). */
+int pg_session_record_geometry(pg_session *s, int on);
+
+/* Library version string. */
+const char *pg_version(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* PARMEC_GB300_H */

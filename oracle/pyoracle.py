@@ -1,0 +1,125 @@
+"""ctypes wrapper of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Exposes the oracle's restated dem() loop body as an engine with the same
+interface as parmec_gb300.engine.GpuEngine, so that a Model can be stepped by
+either.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+import this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from parmec_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build():
+    """Compile the oracle with make (g++, -ffp-contract=off, OpenMP)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "oracle.cpp")):
+        build()
+    lib = ctypes.CDLL(LIB)
+    P = ctypes.c_void_p
+    S = ctypes.POINTER(abi.PgScene)
+    D = abi.D
+    sig = {
+        "or_create": (P, [S]),
+        "or_destroy": (None, [P]),
+        "or_set_threads": (None, [P, ctypes.c_int]),
+        "or_invert_inertia": (None, [P, S]),
+        "or_first_half_step": (None, [P, S, ctypes.c_double, D, D]),
+        "or_condet_forces": (None, [P, S, ctypes.c_double, ctypes.c_double, D, D, D]),
+        "or_run": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double]),
+        "or_dynamics": (None, [P, S, D, ctypes.c_double, ctypes.c_double]),
+        "or_shapes": (None, [P, S]),
+        "or_obstacles": (None, [P, S, ctypes.c_double]),
+        "or_expmap": (None, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, D]),
+        "or_triangle_sphere": (ctypes.c_double, [D, D, D, D, ctypes.c_double, D, D, ctypes.c_int]),
+        "or_eqm": (ctypes.c_double, [S, ctypes.c_int, D, ctypes.c_int, D, D]),
+        "or_contact_count": (ctypes.c_int, [P]),
+        "or_contacts": (ctypes.c_int, [P, ctypes.c_int, abi.I, abi.I, D, D, D, D, D]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class OracleEngine:
+    """Steps a Model with the oracle, in place on the model's host arrays."""
+
+    def __init__(self, threads=1):
+        self.lib = load()
+        self.threads = threads
+        self.model = None
+        self.ctx = None
+        self.counts = None
+
+    def attach(self, m):
+        from parmec_gb300.engine import _counts
+        self.close()
+        self.model = m
+        self.scene = m.scene()
+        self.counts = _counts(m)
+        self.ctx = self.lib.or_create(ctypes.byref(self.scene))
+        self.lib.or_set_threads(self.ctx, self.threads)
+
+    def stale(self):
+        from parmec_gb300.engine import _counts
+        return self.model is None or _counts(self.model) != self.counts
+
+    def upload(self):
+        self.scene = self.model.scene()
+
+    def first_half_step(self, step, ang, lin):
+        ang = np.ascontiguousarray(ang, dtype=np.float64)
+        lin = np.ascontiguousarray(lin, dtype=np.float64)
+        self.lib.or_first_half_step(self.ctx, ctypes.byref(self.scene), step, abi.dptr(ang), abi.dptr(lin))
+
+    def invert_inertia(self):
+        self.lib.or_invert_inertia(self.ctx, ctypes.byref(self.scene))
+
+    def run(self, tab, step):
+        self.lib.or_run(self.ctx, ctypes.byref(self.scene), ctypes.byref(tab), step)
+
+    def sync(self):
+        pass
+
+    def download(self):
+        self.model.pull_obstacles()
+
+    def contacts(self):
+        n = self.lib.or_contact_count(self.ctx)
+        cap = max(1, n)
+        out = {"mpart": np.zeros(cap, np.int32), "code": np.zeros(cap, np.int32),
+               "point": np.zeros((cap, 3)), "normal": np.zeros((cap, 3)), "depth": np.zeros(cap),
+               "force": np.zeros((cap, 3)), "state": np.zeros((cap, 3))}
+        cnt = self.lib.or_contacts(self.ctx, cap, abi.iptr(out["mpart"]), abi.iptr(out["code"]),
+                                   abi.dptr(out["point"]), abi.dptr(out["normal"]), abi.dptr(out["depth"]),
+                                   abi.dptr(out["force"]), abi.dptr(out["state"]))
+        return {k: v[:cnt] for k, v in out.items()}
+
+    def close(self):
+        if self.ctx is not None:
+            self.lib.or_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,241 @@
+// pg_math.cuh -- FP64 small-vector algebra for the DEM kernels.
+//
+// Every helper evaluates the same expression tree as the corresponding macro of
+// the reference (macros.h:97-1050, expmap macros.h:1453-1535).  The library is
+// compiled with -fmad=false, so no multiply-add is contracted and the FP64 form
+// reproduces the CPU restatement bit for bit.
+#pragma once
+
+#define PG_DEV __device__ __forceinline__
+
+namespace pg {
+
+PG_DEV double dot3(const double *a, const double *b) { return a[0]*b[0] + a[1]*b[1] + a[2]*b[2]; }
+
+// NVMUL: C = A*B, A column-major 3x3
+PG_DEV void nvmul(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[3]*B[1]+A[6]*B[2];
+  C[1] = A[1]*B[0]+A[4]*B[1]+A[7]*B[2];
+  C[2] = A[2]*B[0]+A[5]*B[1]+A[8]*B[2];
+}
+// TVMUL: C = A^T*B
+PG_DEV void tvmul(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[1]*B[1]+A[2]*B[2];
+  C[1] = A[3]*B[0]+A[4]*B[1]+A[5]*B[2];
+  C[2] = A[6]*B[0]+A[7]*B[1]+A[8]*B[2];
+}
+// NVADDMUL: D = C + A*B
+PG_DEV void nvaddmul(const double *C, const double *A, const double *B, double *D)
+{
+  D[0] = C[0] + (A[0]*B[0]+A[3]*B[1]+A[6]*B[2]);
+  D[1] = C[1] + (A[1]*B[0]+A[4]*B[1]+A[7]*B[2]);
+  D[2] = C[2] + (A[2]*B[0]+A[5]*B[1]+A[8]*B[2]);
+}
+// NNMUL: C = A*B
+PG_DEV void nnmul(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[3]*B[1]+A[6]*B[2];
+  C[1] = A[1]*B[0]+A[4]*B[1]+A[7]*B[2];
+  C[2] = A[2]*B[0]+A[5]*B[1]+A[8]*B[2];
+  C[3] = A[0]*B[3]+A[3]*B[4]+A[6]*B[5];
+  C[4] = A[1]*B[3]+A[4]*B[4]+A[7]*B[5];
+  C[5] = A[2]*B[3]+A[5]*B[4]+A[8]*B[5];
+  C[6] = A[0]*B[6]+A[3]*B[7]+A[6]*B[8];
+  C[7] = A[1]*B[6]+A[4]*B[7]+A[7]*B[8];
+  C[8] = A[2]*B[6]+A[5]*B[7]+A[8]*B[8];
+}
+// TNMUL: C = A^T*B
+PG_DEV void tnmul(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[1]*B[1]+A[2]*B[2];
+  C[1] = A[3]*B[0]+A[4]*B[1]+A[5]*B[2];
+  C[2] = A[6]*B[0]+A[7]*B[1]+A[8]*B[2];
+  C[3] = A[0]*B[3]+A[1]*B[4]+A[2]*B[5];
+  C[4] = A[3]*B[3]+A[4]*B[4]+A[5]*B[5];
+  C[5] = A[6]*B[3]+A[7]*B[4]+A[8]*B[5];
+  C[6] = A[0]*B[6]+A[1]*B[7]+A[2]*B[8];
+  C[7] = A[3]*B[6]+A[4]*B[7]+A[5]*B[8];
+  C[8] = A[6]*B[6]+A[7]*B[7]+A[8]*B[8];
+}
+
+// Rotation matrix of a rotation vector (Lie-group exponential map).  Below ten
+// degrees it uses the truncated series sin(x)/x and (1-cos(x))/x^2 in x^2; the
+// coefficients are the Taylor coefficients 1/(2k+1)! and 1/(2k+2)!.
+// 'typo' reproduces the reference's v02 = O2*O3 (macros.h:1505).
+PG_DEV void expmap(double O1, double O2, double O3, double *L, bool typo)
+{
+  double angsq, sx, cx, v0, v1, v2, v01, v02, v12, s0, s1, s2;
+  v0 = O1 * O1;
+  v1 = O2 * O2;
+  v2 = O3 * O3;
+  angsq = v0 + v1 + v2;
+  if (angsq < 3.0461741978671E-02)
+  {
+    sx = 1.0 +
+      (-1.666666666666667E-1 +
+       (8.333333333333333E-3 +
+        (-1.984126984126984E-4 +
+         (2.755731922398589E-6 +
+          (-2.505210838544172E-8 +
+           1.605904383682161E-10 * angsq
+          )*angsq
+         )*angsq
+        )*angsq
+       )*angsq
+      )*angsq;
+    cx = 0.5 +
+      (-4.166666666666667E-2 +
+       (1.388888888888889E-3 +
+        (-2.480158730158730E-5 +
+         (2.755731922398589E-7 +
+          (-2.087675698786810E-9 +
+           1.147074559772972E-11 * angsq
+          )*angsq
+         )*angsq
+        )*angsq
+       )*angsq
+      )*angsq;
+  }
+  else
+  {
+    double t = angsq;
+    angsq = sqrt(angsq);
+    double s, c;
+    sincos(angsq, &s, &c);
+    sx = s / angsq;
+    cx = (1.0 - c) / t;
+  }
+  v01 = O1 * O2;
+  v02 = typo ? O2 * O3 : O1 * O3;
+  v12 = O2 * O3;
+  s0 = sx * O1;
+  s1 = sx * O2;
+  s2 = sx * O3;
+  L[0] = -cx*(v2+v1);
+  L[1] = cx*v01;
+  L[2] = cx*v02;
+  L[3] = L[1];
+  L[4] = -cx*(v2+v0);
+  L[5] = cx*v12;
+  L[6] = L[2];
+  L[7] = L[5];
+  L[8] = -cx*(v1+v0);
+  L[0] += 1.0;
+  L[1] += s2;
+  L[2] -= s1;
+  L[3] -= s2;
+  L[4] += 1.0;
+  L[5] += s0;
+  L[6] += s1;
+  L[7] -= s0;
+  L[8] += 1.0;
+}
+
+PG_DEV double clampd(double a, double b, double c) { return a < b ? b : a > c ? c : a; }
+
+// Closest point of triangle (a,b,c) to sphere centre p, by Voronoi regions of
+// the (s,t) parameter plane (condet.ispc:294-400).  Writes the point and the
+// unit normal from the point to the centre; returns r - distance.
+// 'edge_typo' reproduces the reference's -e/c in the s >= 0, t < 0 region
+// beyond edge bc (condet.ispc:373); otherwise the ab-edge parameter -d/a.
+PG_DEV double triangle_sphere(const double *A, const double *Bv, const double *Cv, const double *p, double r,
+                              double *point, double *normal, bool edge_typo)
+{
+  double edge0[3] = {Bv[0]-A[0], Bv[1]-A[1], Bv[2]-A[2]};
+  double edge1[3] = {Cv[0]-A[0], Cv[1]-A[1], Cv[2]-A[2]};
+  double v0[3] = {A[0]-p[0], A[1]-p[1], A[2]-p[2]};
+  double a = dot3(edge0, edge0);
+  double b = dot3(edge0, edge1);
+  double c = dot3(edge1, edge1);
+  double d = dot3(edge0, v0);
+  double e = dot3(edge1, v0);
+  double det = a*c - b*b;
+  double s = b*e - c*d;
+  double t = b*d - a*e;
+  if (s + t < det)
+  {
+    if (s < 0.0)
+    {
+      if (t < 0.0)
+      {
+        if (d < 0.0) { s = clampd(-d/a, 0.0, 1.0); t = 0.0; }
+        else { s = 0.0; t = clampd(-e/c, 0.0, 1.0); }
+      }
+      else { s = 0.0; t = clampd(-e/c, 0.0, 1.0); }
+    }
+    else if (t < 0.0) { s = clampd(-d/a, 0.0, 1.0); t = 0.0; }
+    else
+    {
+      double invDet = 1.0 / det;
+      s *= invDet;
+      t *= invDet;
+    }
+  }
+  else
+  {
+    if (s < 0.0)
+    {
+      double tmp0 = b+d;
+      double tmp1 = c+e;
+      if (tmp1 > tmp0)
+      {
+        double numer = tmp1 - tmp0;
+        double denom = a-2*b+c;
+        s = clampd(numer/denom, 0.0, 1.0);
+        t = 1-s;
+      }
+      else { t = clampd(-e/c, 0.0, 1.0); s = 0.0; }
+    }
+    else if (t < 0.0)
+    {
+      if (a+d > b+e)
+      {
+        double numer = c+e-b-d;
+        double denom = a-2*b+c;
+        s = clampd(numer/denom, 0.0, 1.0);
+        t = 1-s;
+      }
+      else { s = edge_typo ? clampd(-e/c, 0.0, 1.0) : clampd(-d/a, 0.0, 1.0); t = 0.0; }
+    }
+    else
+    {
+      double numer = c+e-b-d;
+      double denom = a-2*b+c;
+      s = clampd(numer/denom, 0.0, 1.0);
+      t = 1.0 - s;
+    }
+  }
+  point[0] = A[0] + s*edge0[0] + t*edge1[0];
+  point[1] = A[1] + s*edge0[1] + t*edge1[1];
+  point[2] = A[2] + s*edge0[2] + t*edge1[2];
+  double q[3] = {p[0]-point[0], p[1]-point[1], p[2]-point[2]};
+  double len = sqrt(dot3(q, q));
+  double ilen = 1.0/len;
+  normal[0] = ilen*q[0];
+  normal[1] = ilen*q[1];
+  normal[2] = ilen*q[2];
+  return r - len;
+}
+
+// INVERT (macros.h:1033): leaves INV untouched when singular
+PG_DEV void invert3(const double *F, double *INV)
+{
+  double det = F[0]*(F[4]*F[8]-F[5]*F[7]) + F[3]*(F[2]*F[7]-F[1]*F[8]) + (F[1]*F[5]-F[2]*F[4])*F[6];
+  if (det != 0.0)
+  {
+    det = 1.0 / det;
+    INV[0] = (F[4]*F[8]-F[5]*F[7])*det;
+    INV[1] = (F[2]*F[7]-F[1]*F[8])*det;
+    INV[2] = (F[1]*F[5]-F[2]*F[4])*det;
+    INV[3] = (F[5]*F[6]-F[3]*F[8])*det;
+    INV[4] = (F[0]*F[8]-F[2]*F[6])*det;
+    INV[5] = (F[2]*F[3]-F[0]*F[5])*det;
+    INV[6] = (F[3]*F[7]-F[4]*F[6])*det;
+    INV[7] = (F[1]*F[6]-F[0]*F[7])*det;
+    INV[8] = (F[0]*F[4]-F[1]*F[3])*det;
+  }
+}
+
+} // namespace pg

@@ -1,0 +1,468 @@
+// pg_rebuild.cu -- contact candidate lists (replaces partition.ispc's kd-tree).
+//
+// The reference re-drops every sphere into a frozen kd-tree each step and
+// searches it per sphere and per triangle (partition.ispc:600-764,
+// condet.ispc:98-516).  Here candidate lists are rebuilt only when a sphere
+// or triangle vertex has moved more than 0.45*skin since the last rebuild:
+//
+//   1. Morton key of each sphere's cell (cell >= 2*rmax + skin)
+//   2. stable LSD radix sort of (key, sphere) pairs, 8-bit digits
+//   3. cell start/end ranges over the sorted keys
+//   4. per sphere: the spheres of the 27 neighbouring cells and the triangles
+//      within r + skin (the master side only: partner particle index larger),
+//      sorted in partner order and merged with the previous list so that the
+//      contact flag and tangential state follow their contact
+//   5. per particle: slave list of master entries that point at it, sorted by
+//      master particle then master slot
+//
+// Every kernel returns at once unless the rebuild flag is set, so the whole
+// sequence can be enqueued (or captured) every step at the cost of a few
+// empty launches.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include "pg_state.h"
+#include "pg_math.cuh"
+#include "pg_launch.h"
+#include "../../include/parmec_gb300.h"
+
+namespace {
+
+constexpr int TPB = 128;
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // keys per block per pass
+constexpr int MAXKN = 96;                               // upper bound of slots per sphere
+constexpr int TRI_TILE = 256;
+
+inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+
+__device__ __forceinline__ void set_err(const PgDev &d, int code) { atomicCAS(d.err, 0, code); }
+
+__device__ __forceinline__ unsigned spread3(unsigned x)
+{
+  x &= 0x3ff;
+  x = (x | (x << 16)) & 0x030000FF;
+  x = (x | (x << 8)) & 0x0300F00F;
+  x = (x | (x << 4)) & 0x030C30C3;
+  x = (x | (x << 2)) & 0x09249249;
+  return x;
+}
+
+__device__ __forceinline__ void cell_of(const PgDev &d, const double *c, int *u)
+{
+  for (int k = 0; k < 3; k ++)
+  {
+    double f = floor((c[k] - d.org[k]) / d.cell);
+    if (!(f >= 0.0)) f = 0.0;                 // also catches NaN
+    if (f > (double)(d.dim[k] - 1)) f = (double)(d.dim[k] - 1);
+    u[k] = (int)f;
+  }
+}
+
+__device__ __forceinline__ unsigned morton(int x, int y, int z)
+{
+  return spread3((unsigned)x) | (spread3((unsigned)y) << 1) | (spread3((unsigned)z) << 2);
+}
+
+// ---- 0. clear the cell ranges of the previous sort
+__global__ void k_rb_clear(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.ellnum) return;
+  unsigned key = d.keys[0][s];
+  d.cstart[key] = 0;
+  d.cend[key] = 0;
+}
+
+// ---- 1. keys, reference centres
+__global__ void k_rb_keys(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ellnum) return;
+  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
+  int u[3];
+  cell_of(d, c, u);
+  d.keys[0][i] = morton(u[0], u[1], u[2]);
+  d.vals[0][i] = i;
+  d.cref[0][i] = c[0]; d.cref[1][i] = c[1]; d.cref[2][i] = c[2];
+}
+
+// ---- triangle reference vertices and widened float AABBs
+__global__ void k_rb_tref(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.trinum) return;
+  for (int k = 0; k < 9; k ++) d.tref[k][t] = d.tri[k][t];
+  for (int c = 0; c < 3; c ++)
+  {
+    double lo = fmin(fmin(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
+    double hi = fmax(fmax(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
+    d.tbox[(size_t)c * d.trinum + t] = __double2float_rd(lo);
+    d.tbox[(size_t)(3+c) * d.trinum + t] = __double2float_ru(hi);
+  }
+}
+
+// ---- 2. radix sort: per-block digit histograms
+__global__ void __launch_bounds__(SORT_THREADS) k_rb_hist(PgDev d, int src, int shift)
+{
+  if (!*d.rebuild) return;
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int n = d.ellnum;
+  const int base = blockIdx.x * SORT_TILE;
+  for (int it = 0; it < SORT_ITEMS; it ++)
+  {
+    int s = base + it * SORT_THREADS + threadIdx.x;
+    if (s < n) atomicAdd(&h[(d.keys[src][s] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  d.hist[threadIdx.x * d.nsortblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan of hist[digit][block] (digit-major), one block
+__global__ void __launch_bounds__(1024) k_rb_scan(PgDev d)
+{
+  if (!*d.rebuild) return;
+  __shared__ unsigned part[1024];
+  const int total = 256 * d.nsortblocks;
+  const int per = (total + 1023) / 1024;
+  const int b = threadIdx.x * per;
+  const int e = min(b + per, total);
+  unsigned sum = 0;
+  for (int k = b; k < e; k ++) sum += d.hist[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1)
+  {
+    unsigned v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (int k = b; k < e; k ++)
+  {
+    unsigned v = d.hist[k];
+    d.hist[k] = run;
+    run += v;
+  }
+}
+
+// stable scatter: each warp ranks its contiguous sub-tile round by round
+__global__ void __launch_bounds__(SORT_THREADS) k_rb_scatter(PgDev d, int src, int shift)
+{
+  if (!*d.rebuild) return;
+  constexpr int WARPS = SORT_THREADS / 32;
+  constexpr int SUB = SORT_TILE / WARPS;              // keys per warp
+  __shared__ unsigned wcnt[WARPS][256];
+  __shared__ unsigned goff[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = threadIdx.x; k < WARPS * 256; k += SORT_THREADS) (&wcnt[0][0])[k] = 0;
+  goff[threadIdx.x] = d.hist[threadIdx.x * d.nsortblocks + blockIdx.x];
+  __syncthreads();
+
+  const int n = d.ellnum;
+  const int base = blockIdx.x * SORT_TILE + warp * SUB;
+  unsigned keyv[SUB / 32];
+  int valv[SUB / 32];
+  unsigned rank[SUB / 32];
+  const unsigned lt = (1u << lane) - 1u;
+  for (int r = 0; r < SUB / 32; r ++)
+  {
+    int s = base + r * 32 + lane;
+    bool ok = s < n;
+    unsigned key = ok ? d.keys[src][s] : 0xffffffffu;
+    int val = ok ? d.vals[src][s] : -1;
+    unsigned dig = ok ? (key >> shift) & 255u : 256u;      // 256: padding, never written
+    unsigned peers = __match_any_sync(0xffffffffu, dig);
+    unsigned before = __popc(peers & lt);
+    unsigned prev = ok ? wcnt[warp][dig] : 0u;
+    __syncwarp();
+    if (ok && before == 0) wcnt[warp][dig] = prev + __popc(peers);
+    __syncwarp();
+    keyv[r] = key;
+    valv[r] = val;
+    rank[r] = prev + before;
+  }
+  __syncthreads();
+  // exclusive prefix over warps for every digit
+  {
+    unsigned run = 0;
+    for (int w = 0; w < WARPS; w ++)
+    {
+      unsigned c = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  const int dst = src ^ 1;
+  for (int r = 0; r < SUB / 32; r ++)
+  {
+    if (valv[r] < 0) continue;
+    unsigned dig = (keyv[r] >> shift) & 255u;
+    unsigned pos = goff[dig] + wcnt[warp][dig] + rank[r];
+    d.keys[dst][pos] = keyv[r];
+    d.vals[dst][pos] = valv[r];
+  }
+}
+
+// ---- 3. cell ranges
+__global__ void k_rb_ranges(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = d.ellnum;
+  if (s >= n) return;
+  unsigned key = d.keys[0][s];
+  if (s == 0 || d.keys[0][s-1] != key) d.cstart[key] = s;
+  if (s == n-1 || d.keys[0][s+1] != key) d.cend[key] = s + 1;
+}
+
+__device__ __forceinline__ unsigned order_key(int code)
+{
+  return code >= 0 ? (unsigned)code : 0x80000000u + (unsigned)(-code - 1);
+}
+
+// ---- 4. candidate lists with carried contact state
+__global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
+{
+  if (!*d.rebuild) return;
+  __shared__ float sbox[6][TRI_TILE];
+  const int E = d.ellnum;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < E;
+  int codes[MAXKN];
+  int n = 0, nsph = 0;
+  bool over = false;
+  double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
+  int pi = 0;
+  if (live)
+  {
+    c[0] = d.center[0][i]; c[1] = d.center[1][i]; c[2] = d.center[2][i];
+    ri = d.radii[0][i];
+    pi = d.part[i];
+    int u[3];
+    cell_of(d, c, u);
+    for (int dz = -1; dz <= 1; dz ++)
+      for (int dy = -1; dy <= 1; dy ++)
+        for (int dx = -1; dx <= 1; dx ++)
+        {
+          int x = u[0]+dx, y = u[1]+dy, z = u[2]+dz;
+          if (x < 0 || y < 0 || z < 0 || x >= d.dim[0] || y >= d.dim[1] || z >= d.dim[2]) continue;
+          unsigned key = morton(x, y, z);
+          int b = d.cstart[key], e = d.cend[key];
+          for (int s = b; s < e; s ++)
+          {
+            int j = d.vals[0][s];
+            if (d.part[j] <= pi) continue;
+            double q0 = c[0] - d.center[0][j], q1 = c[1] - d.center[1][j], q2 = c[2] - d.center[2][j];
+            double lim = ri + d.radii[0][j] + d.skin;
+            if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
+            {
+              if (n < d.kn) codes[n ++] = j;
+              else over = true;
+            }
+          }
+        }
+    // insertion sort of the sphere partners
+    for (int a = 1; a < n; a ++)
+    {
+      int v = codes[a], b = a - 1;
+      while (b >= 0 && codes[b] > v) { codes[b+1] = codes[b]; b --; }
+      codes[b+1] = v;
+    }
+    nsph = n;
+  }
+  // triangles within r + skin, tiled through shared memory
+  const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
+  const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
+  const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
+  for (int t0 = 0; t0 < d.trinum; t0 += TRI_TILE)
+  {
+    __syncthreads();
+    for (int k = threadIdx.x; k < TRI_TILE; k += blockDim.x)
+    {
+      int t = t0 + k;
+      for (int q = 0; q < 6; q ++) sbox[q][k] = t < d.trinum ? d.tbox[(size_t)q * d.trinum + t] : 0.0f;
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int tn = min(TRI_TILE, d.trinum - t0);
+    for (int k = 0; k < tn; k ++)
+    {
+      if (sbox[0][k] > chi[0] || sbox[3][k] < clo[0] ||
+          sbox[1][k] > chi[1] || sbox[4][k] < clo[1] ||
+          sbox[2][k] > chi[2] || sbox[5][k] < clo[2]) continue;
+      int t = t0 + k;
+      double A[3], B[3], C[3], pnt[3], nrm[3];
+      for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
+      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+      if (!(depth > -d.skin) && !(depth != depth)) continue;
+      if (n < d.kn) codes[n ++] = -(t + 1);
+      else over = true;
+    }
+  }
+  if (!live) return;
+  if (over) set_err(d, PG_ERR_CAPACITY);
+
+  // merge with the previous list (both in partner order)
+  const int nold = d.ncnt[i];
+  int ocode[MAXKN];
+  unsigned char oflag[MAXKN];
+  double ost[3][MAXKN];
+  for (int k = 0; k < nold; k ++)
+  {
+    size_t idx = (size_t)k * E + i;
+    ocode[k] = d.ncode[idx];
+    oflag[k] = d.nflag[idx];
+    ost[0][k] = d.nstate[0][idx]; ost[1][k] = d.nstate[1][idx]; ost[2][k] = d.nstate[2][idx];
+  }
+  int o = 0;
+  for (int k = 0; k < n; k ++)
+  {
+    unsigned key = order_key(codes[k]);
+    while (o < nold && order_key(ocode[o]) < key) o ++;
+    size_t idx = (size_t)k * E + i;
+    d.ncode[idx] = codes[k];
+    if (o < nold && ocode[o] == codes[k])
+    {
+      d.nflag[idx] = oflag[o];
+      d.nstate[0][idx] = ost[0][o]; d.nstate[1][idx] = ost[1][o]; d.nstate[2][idx] = ost[2][o];
+    }
+    else
+    {
+      d.nflag[idx] = 0;
+      d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+    }
+  }
+  d.ncnt[i] = n;
+  (void)nsph;
+}
+
+// ---- 5. slave lists
+__global__ void k_rb_rzero(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < d.parnum) d.rcnt[p] = 0;
+}
+
+__global__ void k_rb_rfill(PgDev d)
+{
+  if (!*d.rebuild) return;
+  const int E = d.ellnum;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const int n = d.ncnt[i];
+  for (int k = 0; k < n; k ++)
+  {
+    int code = d.ncode[(size_t)k * E + i];
+    int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
+    if (pj < 0) continue;
+    int r = atomicAdd(&d.rcnt[pj], 1);
+    if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
+    else set_err(d, PG_ERR_CAPACITY);
+  }
+}
+
+__global__ void k_rb_rsort(PgDev d)
+{
+  if (!*d.rebuild) return;
+  const int P = d.parnum, E = d.ellnum;
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  int n = d.rcnt[p];
+  if (n > d.kr) { n = d.kr; d.rcnt[p] = n; }
+  unsigned long long key[MAXKN];
+  int ref[MAXKN];
+  for (int r = 0; r < n; r ++)
+  {
+    int v = d.rref[(size_t)r * P + p];
+    int i = v % E, k = v / E;
+    key[r] = ((unsigned long long)(unsigned)d.part[i] << 32) | (unsigned)k;
+    ref[r] = v;
+  }
+  for (int a = 1; a < n; a ++)
+  {
+    unsigned long long kv = key[a];
+    int rv = ref[a], b = a - 1;
+    while (b >= 0 && key[b] > kv) { key[b+1] = key[b]; ref[b+1] = ref[b]; b --; }
+    key[b+1] = kv;
+    ref[b+1] = rv;
+  }
+  for (int r = 0; r < n; r ++) d.rref[(size_t)r * P + p] = ref[r];
+}
+
+__global__ void k_rb_done(PgDev d)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0) *d.rebuild = 0;
+}
+
+int sort_passes(const PgDev &d)
+{
+  int bits = 3 * d.bits;
+  int p = (bits + 7) / 8;
+  if (p & 1) p ++;             // even, so the result lands in buffer 0
+  return p;
+}
+
+} // namespace
+
+void pg_rebuild_grid_params(PgDev &d, const double *lo, const double *hi, double rmax, double rmin)
+{
+  if (!(d.skin > 0.0)) d.skin = 0.3 * rmin;
+  d.half_skin_sq = (0.45 * d.skin) * (0.45 * d.skin);
+  double cell = 2.0 * rmax + d.skin;
+  double ext = 0.0;
+  for (int k = 0; k < 3; k ++) ext = fmax(ext, hi[k] - lo[k]);
+  ext += 8.0 * cell;
+  const int maxdim = 512;
+  if (ext / cell > maxdim - 4) cell = ext / (maxdim - 4);
+  d.cell = cell;
+  int need = 1;
+  for (int k = 0; k < 3; k ++)
+  {
+    d.org[k] = lo[k] - 4.0 * cell;
+    int n = (int)ceil((hi[k] - lo[k]) / cell) + 9;
+    if (n > maxdim) n = maxdim;
+    if (n < 1) n = 1;
+    d.dim[k] = n;
+    while ((1 << need) < n) need ++;
+  }
+  d.bits = need;
+}
+
+void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
+{
+  const int E = d.ellnum;
+  if (!E) return;
+  k_rb_clear<<<nblk(E), TPB, 0, s>>>(d);
+  k_rb_keys<<<nblk(E), TPB, 0, s>>>(d);
+  if (d.trinum) k_rb_tref<<<nblk(d.trinum), TPB, 0, s>>>(d);
+  const int passes = sort_passes(d);
+  for (int p = 0; p < passes; p ++)
+  {
+    int src = p & 1;
+    k_rb_hist<<<d.nsortblocks, SORT_THREADS, 0, s>>>(d, src, 8 * p);
+    k_rb_scan<<<1, 1024, 0, s>>>(d);
+    k_rb_scatter<<<d.nsortblocks, SORT_THREADS, 0, s>>>(d, src, 8 * p);
+  }
+  k_rb_ranges<<<nblk(E), TPB, 0, s>>>(d);
+  k_rb_verlet<<<nblk(E), TPB, 0, s>>>(d);
+  k_rb_rzero<<<nblk(d.parnum), TPB, 0, s>>>(d);
+  k_rb_rfill<<<nblk(E), TPB, 0, s>>>(d);
+  k_rb_rsort<<<nblk(d.parnum), TPB, 0, s>>>(d);
+  k_rb_done<<<1, 32, 0, s>>>(d);
+}
+
+int pg_rebuild_kernel_count(const PgDev &d)
+{
+  if (!d.ellnum) return 0;
+  return 2 + (d.trinum ? 1 : 0) + 3 * sort_passes(d) + 6;
+}

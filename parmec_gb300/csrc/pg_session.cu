@@ -1,0 +1,698 @@
+// pg_session.cu -- device-resident session: the C ABI of include/parmec_gb300.h.
+//
+// A session owns one scene in HBM.  pg_session_run enqueues, for every step,
+// the rebuild kernels (they return at once unless a rebuild is due) and the
+// step kernels on the session stream; host inputs of each step come from a
+// device copy of the per-step table.  Nothing falls back to the CPU.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <cmath>
+#include "pg_state.h"
+#include "pg_launch.h"
+#include "../../include/parmec_gb300.h"
+
+struct pg_session
+{
+  PgDev d;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  int tab_cap = 0;
+  long long launches = 0;
+  double lo[3], hi[3], rmax = 0.0, rmin = 0.0;
+  size_t ncells = 0;
+  int prs_stride = 3, obs_stride = 3;
+  std::vector<int> h_pell;
+};
+
+namespace {
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
+  std::fprintf(stderr, "parmec_gb300: %s failed: %s (%s:%d)\n", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  return PG_ERR_CUDA; } } while (0)
+
+template <typename T>
+int dalloc(pg_session *s, T **p, size_t n)
+{
+  if (n == 0) n = 1;
+  void *q = nullptr;
+  CK(cudaMalloc(&q, n * sizeof(T)));
+  CK(cudaMemsetAsync(q, 0, n * sizeof(T), s->stream));
+  s->allocs.push_back(q);
+  *p = (T *)q;
+  return PG_OK;
+}
+
+template <typename T>
+int h2d(pg_session *s, T *dst, const T *src, size_t n)
+{
+  if (n == 0 || src == nullptr) return PG_OK;
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s->stream));
+  return PG_OK;
+}
+
+template <typename T>
+int d2h(pg_session *s, T *dst, const T *src, size_t n)
+{
+  if (n == 0 || dst == nullptr) return PG_OK;
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, s->stream));
+  return PG_OK;
+}
+
+#define TRY(x) do { int r_ = (x); if (r_ != PG_OK) return r_; } while (0)
+
+int table_len(const int *idx, int n) { return n > 0 && idx ? idx[n] : 0; }
+
+// allocate every device array for the counts of 'sc'
+int allocate(pg_session *s, const pg_scene *sc)
+{
+  PgDev &d = s->d;
+  const size_t P = sc->parnum, E = sc->ellnum, T = sc->trinum, O = sc->obsnum;
+  const size_t N = sc->nodnum, F = sc->facnum, S = sc->sprnum;
+  for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.angular[k], P));
+  for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.linear[k], P));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.rotation[k], P));
+  for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.position[k], P));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.inertia[k], P));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.inverse[k], P));
+  TRY(dalloc(s, &d.mass, P));
+  TRY(dalloc(s, &d.invm, P));
+  for (int k = 0; k < 3; k ++) { TRY(dalloc(s, &d.force[k], P)); TRY(dalloc(s, &d.torque[k], P)); }
+  TRY(dalloc(s, &d.flags, P));
+  TRY(dalloc(s, &d.parmat, P));
+  TRY(dalloc(s, &d.pell, P));
+  for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.center[k], E));
+  for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.radii[k], E));
+  TRY(dalloc(s, &d.ellcol, E));
+  TRY(dalloc(s, &d.part, E));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.tri[k], T));
+  TRY(dalloc(s, &d.tricol, T));
+  TRY(dalloc(s, &d.triobs, T));
+  TRY(dalloc(s, &d.triown, T));
+  TRY(dalloc(s, &d.trirng, 2*O));
+  TRY(dalloc(s, &d.obspnt, 3*O));
+  TRY(dalloc(s, &d.obsang, 3*O));
+  TRY(dalloc(s, &d.obslin, 3*O));
+  TRY(dalloc(s, &d.pairs, 2*(size_t)sc->pairnum));
+  TRY(dalloc(s, &d.ikind, (size_t)sc->pairnum));
+  for (int k = 0; k < 7; k ++) TRY(dalloc(s, &d.iparam[k], (size_t)sc->pairnum));
+  for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.nodes[k], N));
+  TRY(dalloc(s, &d.nodpart, N));
+  for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.facnod[k], F));
+  TRY(dalloc(s, &d.factri, F));
+  // springs
+  TRY(dalloc(s, &d.sprtype, S));
+  TRY(dalloc(s, &d.unspring, S));
+  for (int k = 0; k < 2; k ++) TRY(dalloc(s, &d.sprpart[k], S));
+  for (int k = 0; k < 12; k ++) TRY(dalloc(s, &d.sprpnt[k], S));
+  const size_t ns = table_len(sc->spridx, sc->sprnum), nd = table_len(sc->dashidx, sc->sprnum);
+  const size_t nu = table_len(sc->unidx, sc->sprnum);
+  for (int k = 0; k < 2; k ++)
+  {
+    TRY(dalloc(s, &d.spring[k], ns));
+    TRY(dalloc(s, &d.dashpot[k], nd));
+    TRY(dalloc(s, &d.unload[k], nu));
+    TRY(dalloc(s, &d.yield[k], S));
+  }
+  TRY(dalloc(s, &d.spridx, S + 1));
+  TRY(dalloc(s, &d.dashidx, S + 1));
+  TRY(dalloc(s, &d.unidx, S + 1));
+  for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.sprdir[k], S));
+  TRY(dalloc(s, &d.sprflg, S));
+  TRY(dalloc(s, &d.sproffset, S));
+  TRY(dalloc(s, &d.sprfric, S));
+  TRY(dalloc(s, &d.sprkskn, S));
+  for (int k = 0; k < 3; k ++)
+  {
+    TRY(dalloc(s, &d.sprsdsp[k], S));
+    TRY(dalloc(s, &d.stroke[k], S));
+    TRY(dalloc(s, &d.sprfrc[k], S));
+  }
+  TRY(dalloc(s, &d.stroke0, S));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.spr_out[k], S));
+  return PG_OK;
+}
+
+// arrays that depend on counts only and never change during a session
+int upload_static(pg_session *s, const pg_scene *sc)
+{
+  PgDev &d = s->d;
+  const int P = sc->parnum, E = sc->ellnum, T = sc->trinum, O = sc->obsnum;
+  // particle -> sphere
+  s->h_pell.assign(P, -1);
+  for (int e = 0; e < E; e ++)
+  {
+    int p = sc->part[e];
+    if (p < 0 || p >= P) return PG_ERR_ARGUMENT;
+    if (s->h_pell[p] >= 0) return PG_ERR_UNSUPPORTED;   // more than one sphere per particle
+    if (!(sc->radii[1][e] < 0.0)) return PG_ERR_UNSUPPORTED;  // ellipsoids: assert(0) in the reference
+    s->h_pell[p] = e;
+  }
+  TRY(h2d(s, d.pell, s->h_pell.data(), P));
+  // triangle -> moving obstacle
+  std::vector<int> own(T, -1);
+  for (int o = 0; o < O; o ++)
+    for (int t = sc->trirng[2*o]; t < sc->trirng[2*o+1]; t ++)
+      if (t >= 0 && t < T) own[t] = o;
+  TRY(h2d(s, d.triown, own.data(), T));
+  // prescriptions per particle, in input order
+  {
+    std::vector<int> first(P + 1, 0), list(std::max(1, sc->prsnum));
+    for (int q = 0; q < sc->prsnum; q ++) first[sc->prspart[q] + 1] ++;
+    for (int p = 0; p < P; p ++) first[p+1] += first[p];
+    std::vector<int> fill(first.begin(), first.end() - 1);
+    for (int q = 0; q < sc->prsnum; q ++) list[fill[sc->prspart[q]] ++] = q;
+    TRY(dalloc(s, &d.prs_first, P + 1));
+    TRY(dalloc(s, &d.prs_list, list.size()));
+    TRY(dalloc(s, &d.prslin, std::max(1, sc->prsnum)));
+    TRY(dalloc(s, &d.prsang, std::max(1, sc->prsnum)));
+    TRY(dalloc(s, &d.linkind, std::max(1, sc->prsnum)));
+    TRY(dalloc(s, &d.angkind, std::max(1, sc->prsnum)));
+    TRY(h2d(s, d.prs_first, first.data(), P + 1));
+    TRY(h2d(s, d.prs_list, list.data(), list.size()));
+    TRY(h2d(s, d.prslin, sc->prslin, sc->prsnum));
+    TRY(h2d(s, d.prsang, sc->prsang, sc->prsnum));
+    TRY(h2d(s, d.linkind, sc->linkind, sc->prsnum));
+    TRY(h2d(s, d.angkind, sc->angkind, sc->prsnum));
+  }
+  // spring flush events: the single-task springs_task order (forces.ispc:1207-1412)
+  {
+    struct Ev { int part; long long pos; int4 v; };
+    std::vector<Ev> ev;
+    const int S = sc->sprnum;
+    int j0 = -1, k0 = -1, jb = 0, kb = 0;
+    bool firstj = true, firstk = true;
+    for (int i = 0; i < S; i ++)
+    {
+      int j = sc->sprpart[0][i], k = sc->sprpart[1][i];
+      if (j0 != j && j0 >= 0)
+      {
+        ev.push_back({j0, 2LL*i, make_int4(0, jb, i, firstj ? 1 : 0)});
+        firstj = false;
+        jb = i;
+      }
+      if (j0 < 0) jb = i;
+      if (k >= 0)
+      {
+        if (k0 != k && k0 >= 0)
+        {
+          ev.push_back({k0, 2LL*i + 1, make_int4(1, kb, i, firstk ? 1 : 0)});
+          firstk = false;
+          kb = i;
+        }
+        if (k0 < 0) kb = i;
+        k0 = k;
+      }
+      j0 = j;
+    }
+    if (j0 >= 0) ev.push_back({j0, 2LL*S, make_int4(0, jb, S, firstj ? 1 : 0)});
+    if (k0 >= 0) ev.push_back({k0, 2LL*S + 1, make_int4(1, kb, S, firstk ? 1 : 0)});
+    std::stable_sort(ev.begin(), ev.end(), [](const Ev &a, const Ev &b) {
+      return a.part != b.part ? a.part < b.part : a.pos < b.pos; });
+    std::vector<int> first(P + 1, 0);
+    std::vector<int4> evv(std::max<size_t>(1, ev.size()));
+    for (size_t q = 0; q < ev.size(); q ++) { first[ev[q].part + 1] ++; evv[q] = ev[q].v; }
+    for (int p = 0; p < P; p ++) first[p+1] += first[p];
+    TRY(dalloc(s, &d.sev_first, P + 1));
+    TRY(dalloc(s, &d.sev, evv.size()));
+    TRY(h2d(s, d.sev_first, first.data(), P + 1));
+    TRY(h2d(s, d.sev, evv.data(), evv.size()));
+  }
+  return PG_OK;
+}
+
+// every array the host may have edited (the dynamic state and the parameters)
+int upload_all(pg_session *s, const pg_scene *sc)
+{
+  PgDev &d = s->d;
+  const size_t P = sc->parnum, E = sc->ellnum, T = sc->trinum, O = sc->obsnum;
+  const size_t N = sc->nodnum, F = sc->facnum, S = sc->sprnum;
+  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.angular[k], sc->angular[k], P));
+  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.linear[k], sc->linear[k], P));
+  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.rotation[k], sc->rotation[k], P));
+  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.position[k], sc->position[k], P));
+  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.inertia[k], sc->inertia[k], P));
+  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.inverse[k], sc->inverse[k], P));
+  TRY(h2d(s, d.mass, sc->mass, P));
+  TRY(h2d(s, d.invm, sc->invm, P));
+  for (int k = 0; k < 3; k ++) { TRY(h2d(s, d.force[k], sc->force[k], P)); TRY(h2d(s, d.torque[k], sc->torque[k], P)); }
+  TRY(h2d(s, d.flags, sc->flags, P));
+  TRY(h2d(s, d.parmat, sc->parmat, P));
+  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.center[k], sc->center[k], E));
+  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.radii[k], sc->radii[k], E));
+  TRY(h2d(s, d.ellcol, sc->ellcol, E));
+  TRY(h2d(s, d.part, sc->part, E));
+  for (int v = 0; v < 3; v ++)
+    for (int c = 0; c < 3; c ++) TRY(h2d(s, d.tri[3*v+c], sc->tri[v][c], T));
+  TRY(h2d(s, d.tricol, sc->tricol, T));
+  TRY(h2d(s, d.triobs, sc->triobs, T));
+  TRY(h2d(s, d.trirng, sc->trirng, 2*O));
+  TRY(h2d(s, d.obspnt, sc->obspnt, 3*O));
+  TRY(h2d(s, d.obsang, sc->obsang, 3*O));
+  TRY(h2d(s, d.obslin, sc->obslin, 3*O));
+  TRY(h2d(s, d.pairs, sc->pairs, 2*(size_t)sc->pairnum));
+  TRY(h2d(s, d.ikind, sc->ikind, (size_t)sc->pairnum));
+  for (int k = 0; k < 7; k ++) TRY(h2d(s, d.iparam[k], sc->iparam[k], (size_t)sc->pairnum));
+  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.nodes[k], sc->nodes[k], N));
+  TRY(h2d(s, d.nodpart, sc->nodpart, N));
+  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.facnod[k], sc->facnod[k], F));
+  TRY(h2d(s, d.factri, sc->factri, F));
+  TRY(h2d(s, d.sprtype, sc->sprtype, S));
+  TRY(h2d(s, d.unspring, sc->unspring, S));
+  for (int k = 0; k < 2; k ++) TRY(h2d(s, d.sprpart[k], sc->sprpart[k], S));
+  for (int a = 0; a < 2; a ++)
+    for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprpnt[6*a+k], sc->sprpnt[a][k], S));
+  const size_t ns = table_len(sc->spridx, sc->sprnum), nd = table_len(sc->dashidx, sc->sprnum);
+  const size_t nu = table_len(sc->unidx, sc->sprnum);
+  for (int k = 0; k < 2; k ++)
+  {
+    TRY(h2d(s, d.spring[k], sc->spring[k], ns));
+    TRY(h2d(s, d.dashpot[k], sc->dashpot[k], nd));
+    TRY(h2d(s, d.unload[k], sc->unload[k], nu));
+    TRY(h2d(s, d.yield[k], sc->yield[k], S));
+  }
+  if (S)
+  {
+    TRY(h2d(s, d.spridx, sc->spridx, S + 1));
+    TRY(h2d(s, d.dashidx, sc->dashidx, S + 1));
+    TRY(h2d(s, d.unidx, sc->unidx, S + 1));
+  }
+  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprdir[k], sc->sprdir[k], S));
+  TRY(h2d(s, d.sprflg, sc->sprflg, S));
+  TRY(h2d(s, d.sproffset, sc->sproffset, S));
+  TRY(h2d(s, d.sprfric, sc->sprfric, S));
+  TRY(h2d(s, d.sprkskn, sc->sprkskn, S));
+  for (int k = 0; k < 3; k ++)
+  {
+    TRY(h2d(s, d.sprsdsp[k], sc->sprsdsp[k], S));
+    TRY(h2d(s, d.stroke[k], sc->stroke[k], S));
+    TRY(h2d(s, d.sprfrc[k], sc->sprfrc[k], S));
+  }
+  TRY(h2d(s, d.stroke0, sc->stroke0, S));
+  // lookup curves for stroke offsets
+  {
+    int nlc = 0;
+    if (sc->sproffset)
+      for (size_t i = 0; i < S; i ++) nlc = std::max(nlc, sc->sproffset[i] + 1);
+    size_t nl = (nlc > 0 && sc->lcidx) ? (size_t)sc->lcidx[nlc] : 0;
+    if (!d.lcidx)
+    {
+      TRY(dalloc(s, &d.lcidx, nlc + 1));
+      for (int k = 0; k < 2; k ++) TRY(dalloc(s, &d.lcurve[k], nl));
+    }
+    if (nlc > 0)
+    {
+      TRY(h2d(s, d.lcidx, sc->lcidx, nlc + 1));
+      for (int k = 0; k < 2; k ++) TRY(h2d(s, d.lcurve[k], sc->lcurve[k], nl));
+    }
+  }
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
+  return PG_OK;
+}
+
+int ensure_tables(pg_session *s, int n)
+{
+  PgDev &d = s->d;
+  if (n <= s->tab_cap) return PG_OK;
+  int cap = std::max(n, 2 * s->tab_cap);
+  double **arrs[7] = {&d.t_curtime, &d.t_gravity, &d.t_damping, &d.t_prs_lin, &d.t_prs_ang, &d.t_obs_ang, &d.t_obs_lin};
+  size_t widths[7] = {1, 3, 6, (size_t)s->prs_stride, (size_t)s->prs_stride, (size_t)s->obs_stride, (size_t)s->obs_stride};
+  for (int k = 0; k < 7; k ++)
+  {
+    if (*arrs[k])
+    {
+      CK(cudaStreamSynchronize(s->stream));
+      auto it = std::find(s->allocs.begin(), s->allocs.end(), (void *)*arrs[k]);
+      if (it != s->allocs.end()) s->allocs.erase(it);
+      CK(cudaFree(*arrs[k]));
+      *arrs[k] = nullptr;
+    }
+    TRY(dalloc(s, arrs[k], (size_t)cap * widths[k]));
+  }
+  s->tab_cap = cap;
+  return PG_OK;
+}
+
+int contact_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  const size_t E = d.ellnum, P = d.parnum, T = d.trinum;
+  const size_t slots = (size_t)d.kn * std::max<size_t>(E, 1);
+  TRY(dalloc(s, &d.ncnt, E));
+  TRY(dalloc(s, &d.ncode, slots));
+  TRY(dalloc(s, &d.nflag, slots));
+  for (int k = 0; k < 3; k ++)
+  {
+    TRY(dalloc(s, &d.nstate[k], slots));
+    TRY(dalloc(s, &d.nfrc[k], slots));
+    TRY(dalloc(s, &d.npnt[k], slots));
+    TRY(dalloc(s, &d.nnrm[k], slots));
+    TRY(dalloc(s, &d.fm[k], P));
+    TRY(dalloc(s, &d.tm[k], P));
+    TRY(dalloc(s, &d.cref[k], E));
+  }
+  TRY(dalloc(s, &d.ndep, slots));
+  TRY(dalloc(s, &d.rcnt, P));
+  TRY(dalloc(s, &d.rref, (size_t)d.kr * std::max<size_t>(P, 1)));
+  for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.tref[k], T));
+  TRY(dalloc(s, &d.tbox, 6 * std::max<size_t>(T, 1)));
+  for (int k = 0; k < 2; k ++)
+  {
+    TRY(dalloc(s, &d.keys[k], E));
+    TRY(dalloc(s, &d.vals[k], E));
+  }
+  d.nsortblocks = (int)((E + 2047) / 2048);
+  if (d.nsortblocks < 1) d.nsortblocks = 1;
+  TRY(dalloc(s, &d.hist, 256 * (size_t)d.nsortblocks));
+  return PG_OK;
+}
+
+int grid_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  pg_rebuild_grid_params(d, s->lo, s->hi, s->rmax, s->rmin);
+  size_t cells = (size_t)1 << (3 * d.bits);
+  if (cells != s->ncells)
+  {
+    for (int *p : {d.cstart, d.cend})
+      if (p)
+      {
+        auto it = std::find(s->allocs.begin(), s->allocs.end(), (void *)p);
+        if (it != s->allocs.end()) s->allocs.erase(it);
+        CK(cudaFree(p));
+      }
+    TRY(dalloc(s, &d.cstart, cells));
+    TRY(dalloc(s, &d.cend, cells));
+    s->ncells = cells;
+  }
+  else
+  {
+    CK(cudaMemsetAsync(d.cstart, 0, cells * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(d.cend, 0, cells * sizeof(int), s->stream));
+  }
+  if (d.keys[0]) CK(cudaMemsetAsync(d.keys[0], 0, (size_t)std::max(1, d.ellnum) * sizeof(unsigned), s->stream));
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
+  return PG_OK;
+}
+
+int read_err(pg_session *s)
+{
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, s->d.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return e;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *pg_version(void) { return "parmec_gb300 0.1.0 (sm_103a)"; }
+
+int pg_session_create(const pg_scene *sc, int form, pg_session **out)
+{
+  if (!sc || !out || sc->parnum < 0 || sc->ellnum < 0) return PG_ERR_ARGUMENT;
+  if (form != PG_FORM_FP64) return PG_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PG_ERR_CUDA;
+  pg_session *s = new pg_session();
+  std::memset(&s->d, 0, sizeof(PgDev));
+  PgDev &d = s->d;
+  int r = PG_OK;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return PG_ERR_CUDA; }
+  d.parnum = sc->parnum; d.ellnum = sc->ellnum; d.trinum = sc->trinum; d.obsnum = sc->obsnum;
+  d.nodnum = sc->nodnum; d.facnum = sc->facnum; d.sprnum = sc->sprnum; d.pairnum = sc->pairnum;
+  d.prsnum = sc->prsnum; d.compat = sc->compat; d.form = form;
+  d.kn = 64; d.kr = 64;
+  s->prs_stride = 3 * std::max(1, sc->prsnum);
+  s->obs_stride = 3 * std::max(1, sc->obsnum);
+  d.tab_prs_stride = s->prs_stride;
+  d.tab_obs_stride = s->obs_stride;
+  if ((r = allocate(s, sc)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.stepno, 1)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.rebuild, 1)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.err, 1)) != PG_OK) goto fail;
+  if ((r = upload_static(s, sc)) != PG_OK) goto fail;
+  if ((r = upload_all(s, sc)) != PG_OK) goto fail;
+  if ((r = contact_buffers(s)) != PG_OK) goto fail;
+  for (int k = 0; k < 3; k ++) { s->lo[k] = 1e300; s->hi[k] = -1e300; }
+  s->rmax = 0.0; s->rmin = 1e300;
+  for (int e = 0; e < sc->ellnum; e ++)
+  {
+    for (int k = 0; k < 3; k ++)
+    {
+      s->lo[k] = std::min(s->lo[k], sc->center[k][e]);
+      s->hi[k] = std::max(s->hi[k], sc->center[k][e]);
+    }
+    s->rmax = std::max(s->rmax, sc->radii[0][e]);
+    s->rmin = std::min(s->rmin, sc->radii[0][e]);
+  }
+  if (sc->ellnum == 0) { for (int k = 0; k < 3; k ++) { s->lo[k] = 0; s->hi[k] = 1; } s->rmax = s->rmin = 1.0; }
+  if ((r = grid_buffers(s)) != PG_OK) goto fail;
+  if ((r = ensure_tables(s, 64)) != PG_OK) goto fail;
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) { r = PG_ERR_CUDA; goto fail; }
+  *out = s;
+  return PG_OK;
+fail:
+  pg_session_destroy(s);
+  return r;
+}
+
+int pg_session_destroy(pg_session *s)
+{
+  if (!s) return PG_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void *p : s->allocs) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return PG_OK;
+}
+
+int pg_session_set_skin(pg_session *s, double skin)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  s->d.skin = skin > 0.0 ? skin : 0.0;
+  return grid_buffers(s);
+}
+
+int pg_session_record_geometry(pg_session *s, int on)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  s->d.record_geometry = on ? 1 : 0;
+  return PG_OK;
+}
+
+int pg_session_upload(pg_session *s, const pg_scene *sc)
+{
+  if (!s || !sc) return PG_ERR_ARGUMENT;
+  if (sc->parnum != s->d.parnum || sc->ellnum != s->d.ellnum || sc->trinum != s->d.trinum ||
+      sc->sprnum != s->d.sprnum || sc->obsnum != s->d.obsnum || sc->prsnum != s->d.prsnum)
+    return PG_ERR_ARGUMENT;
+  s->d.compat = sc->compat;
+  TRY(upload_all(s, sc));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_invert_inertia(pg_session *s)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  pg_launch_invert(s->d, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_session_first_half_step(pg_session *s, double step, const double *obs_ang, const double *obs_lin)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  pg_launch_euler(d, s->stream, 0.5 * step);
+  pg_launch_shapes(d, s->stream, false);
+  if (d.obsnum)
+  {
+    TRY(h2d(s, d.obsang, obs_ang, 3 * (size_t)d.obsnum));
+    TRY(h2d(s, d.obslin, obs_lin, 3 * (size_t)d.obsnum));
+  }
+  pg_launch_obstacles_state(d, s->stream, step);
+  s->launches += 5;
+  CK(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
+{
+  if (!s || !tab || tab->nsteps < 0) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  const int n = tab->nsteps;
+  if (n == 0) return PG_OK;
+  TRY(ensure_tables(s, n));
+  // host tables -> device (rows of this call)
+  std::vector<double> zeros;
+  auto put = [&](double *dst, const double *src, size_t width) -> int {
+    if (src) return h2d(s, dst, src, (size_t)n * width);
+    zeros.assign((size_t)n * width, 0.0);
+    int r = h2d(s, dst, zeros.data(), (size_t)n * width);
+    if (r == PG_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) return PG_ERR_CUDA;
+    return r;
+  };
+  TRY(put(d.t_curtime, tab->curtime, 1));
+  TRY(put(d.t_gravity, tab->gravity, 3));
+  TRY(put(d.t_damping, tab->damping, 6));
+  TRY(put(d.t_prs_lin, tab->prs_lin, s->prs_stride));
+  TRY(put(d.t_prs_ang, tab->prs_ang, s->prs_stride));
+  TRY(put(d.t_obs_ang, tab->obs_ang, s->obs_stride));
+  TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
+  CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
+  const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d);
+  for (int k = 0; k < n; k ++)
+  {
+    pg_launch_rebuild(d, s->stream);
+    pg_launch_contacts(d, s->stream, step);
+    pg_launch_springs(d, s->stream, step);
+    pg_launch_integrate(d, s->stream, step);
+    pg_launch_mesh(d, s->stream);
+    pg_launch_obstacles_row(d, s->stream, step);
+    pg_launch_tail(d, s->stream, step);
+  }
+  s->launches += (long long)per_step * n;
+  CK(cudaGetLastError());
+  // the host tables are pageable: keep them alive until the copies finished
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_sync(pg_session *s)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  CK(cudaStreamSynchronize(s->stream));
+  int e = read_err(s);
+  return e ? e : PG_OK;
+}
+
+int pg_session_download(pg_session *s, pg_scene *sc)
+{
+  if (!s || !sc) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  const size_t P = d.parnum, E = d.ellnum, T = d.trinum, O = d.obsnum, N = d.nodnum, S = d.sprnum;
+  for (int k = 0; k < 6; k ++) TRY(d2h(s, sc->angular[k], d.angular[k], P));
+  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->linear[k], d.linear[k], P));
+  for (int k = 0; k < 9; k ++) TRY(d2h(s, sc->rotation[k], d.rotation[k], P));
+  for (int k = 0; k < 6; k ++) TRY(d2h(s, sc->position[k], d.position[k], P));
+  for (int k = 0; k < 9; k ++) TRY(d2h(s, sc->inverse[k], d.inverse[k], P));
+  TRY(d2h(s, sc->invm, d.invm, P));
+  for (int k = 0; k < 3; k ++) { TRY(d2h(s, sc->force[k], d.force[k], P)); TRY(d2h(s, sc->torque[k], d.torque[k], P)); }
+  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->center[k], d.center[k], E));
+  for (int v = 0; v < 3; v ++)
+    for (int c = 0; c < 3; c ++) TRY(d2h(s, sc->tri[v][c], d.tri[3*v+c], T));
+  TRY(d2h(s, sc->obspnt, d.obspnt, 3*O));
+  TRY(d2h(s, sc->obsang, d.obsang, 3*O));
+  TRY(d2h(s, sc->obslin, d.obslin, 3*O));
+  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->nodes[k], d.nodes[k], N));
+  TRY(d2h(s, sc->unspring, d.unspring, S));
+  for (int a = 0; a < 2; a ++)
+    for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->sprpnt[a][k], d.sprpnt[6*a+k], S));
+  for (int k = 0; k < 2; k ++) TRY(d2h(s, sc->yield[k], d.yield[k], S));
+  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->sprdir[k], d.sprdir[k], S));
+  TRY(d2h(s, sc->sprflg, d.sprflg, S));
+  for (int k = 0; k < 3; k ++)
+  {
+    TRY(d2h(s, sc->sprsdsp[k], d.sprsdsp[k], S));
+    TRY(d2h(s, sc->stroke[k], d.stroke[k], S));
+    TRY(d2h(s, sc->sprfrc[k], d.sprfrc[k], S));
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  int e = read_err(s);
+  return e ? e : PG_OK;
+}
+
+int pg_session_contact_count(pg_session *s, int *count)
+{
+  if (!s || !count) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  const size_t E = d.ellnum;
+  *count = 0;
+  if (!E) return PG_OK;
+  std::vector<int> cnt(E);
+  std::vector<unsigned char> flag((size_t)d.kn * E);
+  TRY(d2h(s, cnt.data(), d.ncnt, E));
+  TRY(d2h(s, flag.data(), d.nflag, (size_t)d.kn * E));
+  CK(cudaStreamSynchronize(s->stream));
+  int n = 0;
+  for (size_t i = 0; i < E; i ++)
+    for (int k = 0; k < cnt[i]; k ++) n += flag[(size_t)k * E + i] ? 1 : 0;
+  *count = n;
+  return PG_OK;
+}
+
+int pg_session_contacts(pg_session *s, int cap, int *count, int *master_particle, int *code,
+                        double *point, double *normal, double *depth, double *force, double *state)
+{
+  if (!s || !count) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  const size_t E = d.ellnum, slots = (size_t)d.kn * E;
+  *count = 0;
+  if (!E) return PG_OK;
+  std::vector<int> cnt(E), cod(slots);
+  std::vector<unsigned char> flag(slots);
+  std::vector<double> st[3], fr[3], pt[3], nr[3], dp(slots);
+  TRY(d2h(s, cnt.data(), d.ncnt, E));
+  TRY(d2h(s, cod.data(), d.ncode, slots));
+  TRY(d2h(s, flag.data(), d.nflag, slots));
+  for (int k = 0; k < 3; k ++)
+  {
+    st[k].resize(slots); fr[k].resize(slots); pt[k].resize(slots); nr[k].resize(slots);
+    TRY(d2h(s, st[k].data(), d.nstate[k], slots));
+    TRY(d2h(s, fr[k].data(), d.nfrc[k], slots));
+    TRY(d2h(s, pt[k].data(), d.npnt[k], slots));
+    TRY(d2h(s, nr[k].data(), d.nnrm[k], slots));
+  }
+  TRY(d2h(s, dp.data(), d.ndep, slots));
+  CK(cudaStreamSynchronize(s->stream));
+  int n = 0;
+  for (int p = 0; p < d.parnum; p ++)
+  {
+    int i = s->h_pell[p];
+    if (i < 0) continue;
+    for (int k = 0; k < cnt[i]; k ++)
+    {
+      size_t idx = (size_t)k * E + i;
+      if (!flag[idx]) continue;
+      if (n >= cap) { *count = n; return PG_OK; }
+      if (master_particle) master_particle[n] = p;
+      if (code) code[n] = cod[idx];
+      for (int c = 0; c < 3; c ++)
+      {
+        if (point) point[3*n+c] = pt[c][idx];
+        if (normal) normal[3*n+c] = nr[c][idx];
+        if (force) force[3*n+c] = fr[c][idx];
+        if (state) state[3*n+c] = st[c][idx];
+      }
+      if (depth) depth[n] = dp[idx];
+      n ++;
+    }
+  }
+  *count = n;
+  return PG_OK;
+}
+
+int pg_session_stream(pg_session *s, void **stream)
+{
+  if (!s || !stream) return PG_ERR_ARGUMENT;
+  *stream = (void *)s->stream;
+  return PG_OK;
+}
+
+int pg_session_kernel_launches(pg_session *s, long long *count)
+{
+  if (!s || !count) return PG_ERR_ARGUMENT;
+  *count = s->launches;
+  return PG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,100 @@
+// pg_state.h -- device-resident scene of one session.
+//
+// Layout in HBM: structure of arrays, one contiguous array per vector
+// component (as the reference's host buffers, parmec.cpp:61-285), so a warp
+// reading component k of 32 consecutive particles reads 256 contiguous bytes.
+// Contact candidate lists are slot-major ([slot][sphere]) so that slot k of a
+// warp's 32 spheres is one coalesced segment.
+#pragma once
+#include <cstdint>
+
+#define PG_MAX_OBS_ROW 64   // obstacles per scene handled by the per-step kernels
+
+struct PgDev
+{
+  int parnum, ellnum, trinum, obsnum, nodnum, facnum, sprnum, pairnum, prsnum;
+  int compat;
+  int form;                 // PG_FORM_FP64 / PG_FORM_MIXED
+
+  // ---- particles (parmec.cpp:95-114)
+  double *angular[6], *linear[3], *rotation[9], *position[6];
+  double *inertia[9], *inverse[9], *mass, *invm, *force[3], *torque[3];
+  int *flags, *parmat;
+  int *pell;                // particle -> its sphere, or -1
+
+  // ---- spheres (parmec.cpp:86-93)
+  double *center[6], *radii[3];
+  int *ellcol, *part;
+
+  // ---- triangles and obstacles
+  double *tri[9];           // tri[3*vertex + coord]
+  int *tricol, *triobs;
+  int *trirng;              // [2*obsnum]
+  int *triown;              // triangle -> moving obstacle index, or -1
+  double *obspnt, *obsang, *obslin;   // [3*obsnum]
+
+  // ---- surface pairing
+  int *pairs, *ikind;
+  double *iparam[7];
+
+  // ---- mesh nodes and faces
+  double *nodes[6];
+  int *nodpart;
+  int *facnod[3], *factri;
+
+  // ---- springs (parmec.cpp:151-178)
+  int *sprtype, *unspring, *sprpart[2];
+  double *sprpnt[12];       // sprpnt[6*side + k]
+  double *spring[2]; int *spridx;
+  double *dashpot[2]; int *dashidx;
+  double *unload[2]; int *unidx;
+  double *yield[2], *sprdir[6];
+  int *sprflg, *sproffset;
+  double *sprfric, *sprkskn, *sprsdsp[3], *stroke0, *stroke[3], *sprfrc[3];
+  double *lcurve[2]; int *lcidx;
+  double *spr_out[9];       // per spring: frc[3], trq_j[3], trq_k[3]
+  int *sev_first;           // [parnum+1] CSR of spring force events per particle
+  int4 *sev;                // (type, begin, end, first): type 0 = j-run (+=), 1 = k-run (-=)
+
+  // ---- prescribed motion
+  int *prs_first;           // [parnum+1] CSR of prescriptions per particle
+  int *prs_list;            // prescription indices in input order
+  int *prslin, *prsang, *linkind, *angkind;
+
+  // ---- per-step host tables on the device
+  double *t_curtime, *t_gravity, *t_damping, *t_prs_lin, *t_prs_ang, *t_obs_ang, *t_obs_lin;
+  int tab_prs_stride, tab_obs_stride;   // rows: prsnum*3, obsnum*3 (at least 3)
+  int *stepno;              // device step counter (row of the tables)
+
+  // ---- contact candidates (Verlet lists), master side, slot-major
+  int kn;                   // slots per sphere
+  int *ncnt;                // [ellnum]
+  int *ncode;               // [kn][ellnum]: sphere j >= 0, or -(triangle+1)
+  unsigned char *nflag;     // [kn][ellnum]: contact active
+  double *nstate[3];        // [kn][ellnum]: tangential spring state
+  double *nfrc[3];          // [kn][ellnum]: contact force on the master
+  double *npnt[3];          // [kn][ellnum]: contact point
+  double *nnrm[3], *ndep;   // optional: normal and depth (parity exports only)
+  int record_geometry;
+  double *fm[3], *tm[3];    // [parnum] master-side partial force and torque sums
+  int kr;                   // slave slots per particle
+  int *rcnt;                // [parnum]
+  int *rref;                // [kr][parnum]: entry index slot*ellnum + sphere
+
+  // ---- rebuild machinery
+  int *rebuild;             // 1 when the candidate lists must be rebuilt
+  int *err;                 // first device error (PG_ERR_*), 0 when fine
+  double skin, cell, half_skin_sq;
+  double org[3];
+  int dim[3], bits;
+  double *cref[3];          // sphere centres at the last rebuild
+  double *tref[9];          // triangle vertices at the last rebuild
+  unsigned *keys[2];        // radix-sort ping-pong buffers
+  int *vals[2];
+  unsigned *hist;           // radix-sort block histograms
+  int nsortblocks;
+  int *cstart, *cend;       // [2^(3*bits)] cell ranges in sorted order
+  int *ncnt_new;            // scratch candidate lists of a rebuild
+  int *ncode_new;
+  float *tbox;              // [6][trinum] triangle AABBs at rebuild (float, widened)
+};

@@ -1,0 +1,1065 @@
+// pg_step.cu -- the per-step DEM kernels (FP64 form).
+//
+// One step of the reference loop (parmec.cpp:2418-2517) runs as
+//   [rebuild of candidate lists, only when some sphere moved > skin/2]
+//   k_contacts   per sphere: narrow phase of its candidates, granular force,
+//                contact state, master-side partial sums  (condet + contacts_task)
+//   k_springs    per spring: nonlinear spring/dashpot/friction force (springs_task)
+//   k_integrate  per particle: slave-side sums + gravity + spring flushes,
+//                prescribed motion, Lie-group integration, sphere centres
+//                (contacts_acc_task + prescribe_* + dynamics_task + ellipsoids_task)
+//   k_nodes/k_faces, k_obstacles, k_tail
+// All sums run in a fixed order (master list in partner order, then slave
+// list in master order), so results repeat bit for bit from run to run.
+#include <cuda_runtime.h>
+#include "pg_state.h"
+#include "pg_math.cuh"
+#include "pg_launch.h"
+#include "../../include/parmec_gb300.h"
+
+using namespace pg;
+
+namespace {
+
+constexpr int TPB = 128;
+
+inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+
+__device__ __forceinline__ void set_err(const PgDev &d, int code) { atomicCAS(d.err, 0, code); }
+
+__device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
+{
+  unsigned m = __ballot_sync(__activemask(), need);
+  if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
+}
+
+// ---------------------------------------------------------------- invert (parmec.ispc:62-99)
+__global__ void k_invert(PgDev d)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.parnum) return;
+  double a[9], x[9];
+  for (int j = 0; j < 9; j ++) a[j] = d.inertia[j][i];
+  for (int j = 0; j < 9; j ++) x[j] = 0.0;
+  invert3(a, x);
+  for (int j = 0; j < 9; j ++) d.inverse[j][i] = x[j];
+  d.invm[i] = 1.0 / d.mass[i];
+}
+
+// ---------------------------------------------------------------- euler (parmec.ispc:224-272)
+__global__ void k_euler(PgDev d, double step)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.parnum) return;
+  const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+  double O[3], L1[9], DL[9], L2[9], o[3];
+  O[0] = step*d.angular[0][i];
+  O[1] = step*d.angular[1][i];
+  O[2] = step*d.angular[2][i];
+  expmap(O[0], O[1], O[2], DL, typo);
+  for (int k = 0; k < 9; k ++) L1[k] = d.rotation[k][i];
+  nnmul(L1, DL, L2);
+  for (int k = 0; k < 9; k ++) d.rotation[k][i] = L2[k];
+  nvmul(L2, O, o);
+  d.angular[3][i] = o[0];
+  d.angular[4][i] = o[1];
+  d.angular[5][i] = o[2];
+  d.position[0][i] += step * d.linear[0][i];
+  d.position[1][i] += step * d.linear[1][i];
+  d.position[2][i] += step * d.linear[2][i];
+}
+
+// ---------------------------------------------------------------- shapes (shapes.ispc:29-211)
+__device__ __forceinline__ void body_point(const double *x, const double *L, const double *X,
+                                           const double *C0, double *c)
+{
+  double C[3] = {C0[0], C0[1], C0[2]};
+  C[0] -= X[0]; C[1] -= X[1]; C[2] -= X[2];     // SCC (X, C)
+  nvaddmul(x, L, C, c);
+}
+
+__global__ void k_spheres(PgDev d)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ellnum) return;
+  int j = d.part[e];
+  double L[9], X[3], x[3], C[3], c[3];
+  for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][j];
+  for (int k = 0; k < 3; k ++) { X[k] = d.position[3+k][j]; x[k] = d.position[k][j]; C[k] = d.center[3+k][e]; }
+  body_point(x, L, X, C, c);
+  for (int k = 0; k < 3; k ++) d.center[k][e] = c[k];
+}
+
+__global__ void k_nodes(PgDev d, int skip_analytical)
+{
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= d.nodnum) return;
+  int j = d.nodpart[n];
+  if (skip_analytical && (d.flags[j] & PG_FLAG_ANALYTICAL)) return;
+  double L[9], X[3], x[3], C[3], c[3];
+  for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][j];
+  for (int k = 0; k < 3; k ++) { X[k] = d.position[3+k][j]; x[k] = d.position[k][j]; C[k] = d.nodes[3+k][n]; }
+  body_point(x, L, X, C, c);
+  for (int k = 0; k < 3; k ++) d.nodes[k][n] = c[k];
+}
+
+__global__ void k_faces(PgDev d)
+{
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (f < d.facnum)
+  {
+    int t = d.factri[f];
+    for (int v = 0; v < 3; v ++)
+    {
+      int n = d.facnod[v][f];
+      double dd = 0.0;
+      for (int c = 0; c < 3; c ++)
+      {
+        double val = d.nodes[c][n];
+        d.tri[3*v+c][t] = val;
+        double r = val - d.tref[3*v+c][t];
+        dd += r*r;
+      }
+      need |= dd > d.half_skin_sq;
+    }
+  }
+  if (d.ellnum) flag_rebuild(d, need);
+}
+
+// ---------------------------------------------------------------- obstacles (obstacles.ispc:28-78)
+// velocities: row of the step table (use_row) or the current obsang/obslin state
+__global__ void k_obstacles(PgDev d, double step, int use_row)
+{
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (t < d.trinum)
+  {
+    int o = d.triown[t];
+    if (o >= 0)
+    {
+      const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+      const double *ang, *lin;
+      if (use_row)
+      {
+        int row = *d.stepno;
+        ang = d.t_obs_ang + (size_t)row * d.tab_obs_stride + 3*o;
+        lin = d.t_obs_lin + (size_t)row * d.tab_obs_stride + 3*o;
+      }
+      else
+      {
+        ang = d.obsang + 3*o;
+        lin = d.obslin + 3*o;
+      }
+      const double *x = d.obspnt + 3*o;
+      double y[3], DL[9], z[3];
+      y[0] = x[0] + step*lin[0];
+      y[1] = x[1] + step*lin[1];
+      y[2] = x[2] + step*lin[2];
+      expmap(step*ang[0], step*ang[1], step*ang[2], DL, typo);
+      for (int v = 0; v < 3; v ++)
+      {
+        z[0] = d.tri[3*v+0][t] - x[0];
+        z[1] = d.tri[3*v+1][t] - x[1];
+        z[2] = d.tri[3*v+2][t] - x[2];
+        double n0 = DL[0]*z[0]+DL[3]*z[1]+DL[6]*z[2] + y[0];
+        double n1 = DL[1]*z[0]+DL[4]*z[1]+DL[7]*z[2] + y[1];
+        double n2 = DL[2]*z[0]+DL[5]*z[1]+DL[8]*z[2] + y[2];
+        d.tri[3*v+0][t] = n0;
+        d.tri[3*v+1][t] = n1;
+        d.tri[3*v+2][t] = n2;
+        double r0 = n0 - d.tref[3*v+0][t], r1 = n1 - d.tref[3*v+1][t], r2 = n2 - d.tref[3*v+2][t];
+        need |= (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
+      }
+    }
+  }
+  if (d.ellnum) flag_rebuild(d, need);
+}
+
+// obstacle points (after every triangle used the old point), obstacle
+// velocity state, and the step counter
+__global__ void k_tail(PgDev d, double step, int use_row)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int row = use_row ? *d.stepno : 0;
+  for (int o = 0; o < d.obsnum; o ++)
+  {
+    if (use_row)
+      for (int k = 0; k < 3; k ++)
+      {
+        d.obsang[3*o+k] = d.t_obs_ang[(size_t)row * d.tab_obs_stride + 3*o + k];
+        d.obslin[3*o+k] = d.t_obs_lin[(size_t)row * d.tab_obs_stride + 3*o + k];
+      }
+    double *x = d.obspnt + 3*o;
+    const double *v = d.obslin + 3*o;
+    double y0 = x[0] + step*v[0], y1 = x[1] + step*v[1], y2 = x[2] + step*v[2];
+    x[0] = y0; x[1] = y1; x[2] = y2;
+  }
+  if (use_row) *d.stepno = row + 1;
+}
+
+// ---------------------------------------------------------------- pairing (forces.ispc:98-122)
+__device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
+{
+  int p0 = i, p1 = j, start = 1, end = d.pairnum;
+  if (i > j) { p0 = j; p1 = i; }
+  while (start < end)
+  {
+    int mid = ((end-start)>>1) + start;
+    int a = d.pairs[2*mid], b = d.pairs[2*mid+1];
+    if (p0 > a) { if (start == mid) break; start = mid; }
+    else if (p0 == a)
+    {
+      if (p1 > b) { if (start == mid) break; start = mid; }
+      else if (p1 == b) return mid;
+      else end = mid;
+    }
+    else end = mid;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- contacts
+// One thread per sphere (master side).  For every candidate in its list the
+// exact FP64 narrow phase decides whether the contact exists this step:
+// a contact persists while depth >= 0 (forces.ispc:191, removal 327-365) and
+// is created when depth > 0 (condet.ispc:183); existing sphere pairs use the
+// unguarded 1/len (condet.ispc:667), new ones the guarded one (137).
+template <bool GEOM>
+__global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
+{
+  const int E = d.ellnum;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const int pi = d.part[i];
+  const int cnt = d.ncnt[i];
+  double fs[3] = {0.0, 0.0, 0.0}, ts[3] = {0.0, 0.0, 0.0};
+  if (cnt > 0)
+  {
+    const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
+    double x[3], v[3], oi[3], c[3];
+    for (int k = 0; k < 3; k ++)
+    {
+      x[k] = d.position[k][pi];
+      v[k] = d.linear[k][pi];
+      oi[k] = d.angular[3+k][pi];
+      c[k] = d.center[k][i];
+    }
+    const double ri = d.radii[0][i];
+    const int coli = d.ellcol[i];
+    const double invmi = d.invm[pi], massi = d.mass[pi];
+
+    for (int k = 0; k < cnt; k ++)
+    {
+      const size_t idx = (size_t)k * E + i;
+      const int code = d.ncode[idx];
+      const bool existing = d.nflag[idx] != 0;
+      double point[3], normal[3], depth;
+      int pj, colj;
+      if (code >= 0)
+      {
+        const int j = code;
+        pj = d.part[j];
+        colj = d.ellcol[j];
+        double q[3], cj[3];
+        cj[0] = d.center[0][j]; cj[1] = d.center[1][j]; cj[2] = d.center[2][j];
+        q[0] = c[0]-cj[0];
+        q[1] = c[1]-cj[1];
+        q[2] = c[2]-cj[2];
+        double len = sqrt(dot3(q, q));
+        double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
+        point[0] = 0.5*(c[0]+cj[0]);
+        point[1] = 0.5*(c[1]+cj[1]);
+        point[2] = 0.5*(c[2]+cj[2]);
+        normal[0] = ilen*q[0];
+        normal[1] = ilen*q[1];
+        normal[2] = ilen*q[2];
+        depth = ri+d.radii[0][j] - len;
+      }
+      else
+      {
+        const int t = -code-1;
+        double A[3], B[3], C[3];
+        for (int kk = 0; kk < 3; kk ++) { A[kk] = d.tri[kk][t]; B[kk] = d.tri[3+kk][t]; C[kk] = d.tri[6+kk][t]; }
+        depth = triangle_sphere(A, B, C, c, ri, point, normal, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+        pj = d.triobs[t];
+        colj = d.tricol[t];
+      }
+      const bool active = existing ? !(depth < 0.0) : (depth > 0.0);
+      if (!active)
+      {
+        if (existing)
+        {
+          d.nflag[idx] = 0;
+          d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+        }
+        continue;
+      }
+
+      // contact point velocities (forces.ispc:226-279)
+      double z[3], vi[3], vj[3], oj[3], vij[3];
+      z[0] = point[0]-x[0]; z[1] = point[1]-x[1]; z[2] = point[2]-x[2];
+      vi[0] = oi[1]*z[2]-oi[2]*z[1] + v[0];
+      vi[1] = oi[2]*z[0]-oi[0]*z[2] + v[1];
+      vi[2] = oi[0]*z[1]-oi[1]*z[0] + v[2];
+      if (pj >= 0)
+      {
+        z[0] = point[0]-d.position[0][pj];
+        z[1] = point[1]-d.position[1][pj];
+        z[2] = point[2]-d.position[2][pj];
+        oj[0] = d.angular[3][pj]; oj[1] = d.angular[4][pj]; oj[2] = d.angular[5][pj];
+        vj[0] = oj[1]*z[2]-oj[2]*z[1] + d.linear[0][pj];
+        vj[1] = oj[2]*z[0]-oj[0]*z[2] + d.linear[1][pj];
+        vj[2] = oj[0]*z[1]-oj[1]*z[0] + d.linear[2][pj];
+      }
+      else
+      {
+        int l = -pj-2;
+        if (obsc && l >= 0) l = l+1;
+        if (l >= 0 && l < d.obsnum)
+        {
+          z[0] = point[0]-d.obspnt[3*l];
+          z[1] = point[1]-d.obspnt[3*l+1];
+          z[2] = point[2]-d.obspnt[3*l+2];
+          oj[0] = d.obsang[3*l]; oj[1] = d.obsang[3*l+1]; oj[2] = d.obsang[3*l+2];
+          vj[0] = oj[1]*z[2]-oj[2]*z[1] + d.obslin[3*l];
+          vj[1] = oj[2]*z[0]-oj[0]*z[2] + d.obslin[3*l+1];
+          vj[2] = oj[0]*z[1]-oj[1]*z[0] + d.obslin[3*l+2];
+        }
+        else
+        {
+          vj[0] = vj[1] = vj[2] = 0.0;
+        }
+      }
+      vij[0] = vj[0] - vi[0];
+      vij[1] = vj[1] - vi[1];
+      vij[2] = vj[2] - vi[2];
+
+      const int ij = pairing(d, coli, colj);
+      if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED);
+
+      // granular force (forces.ispc:125-192)
+      double state[3];
+      if (existing) { state[0] = d.nstate[0][idx]; state[1] = d.nstate[1][idx]; state[2] = d.nstate[2][idx]; }
+      else { state[0] = 0.0; state[1] = 0.0; state[2] = 0.0; }
+      double ma = pj >= 0 ? 1.0 / (invmi + d.invm[pj]) : massi;
+      double kn = d.iparam[0][ij];
+      double en = d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+      double vn = dot3(vij, normal);
+      double fn = kn*depth + en*vn;
+      double f[3];
+      f[0] = fn*normal[0];
+      f[1] = fn*normal[1];
+      f[2] = fn*normal[2];
+      double kskn = d.iparam[6][ij];
+      double kt = kn * kskn;
+      double et = en * kskn;
+      double mus = d.iparam[2][ij];
+      double mud = d.iparam[3][ij];
+      double vt[3], ft[3];
+      vt[0] = vij[0] - vn*normal[0];
+      vt[1] = vij[1] - vn*normal[1];
+      vt[2] = vij[2] - vn*normal[2];
+      state[0] += step*vt[0];
+      state[1] += step*vt[1];
+      state[2] += step*vt[2];
+      ft[0] = kt*state[0] + et*vt[0];
+      ft[1] = kt*state[1] + et*vt[1];
+      ft[2] = kt*state[2] + et*vt[2];
+      double flen = sqrt(dot3(ft, ft));
+      double lim = mus*fn;
+      if (flen > lim)
+      {
+        lim = mud*fn/flen;
+        ft[0] *= lim;
+        ft[1] *= lim;
+        ft[2] *= lim;
+      }
+      f[0] += ft[0];
+      f[1] += ft[1];
+      f[2] += ft[2];
+
+      d.nflag[idx] = 1;
+      d.nstate[0][idx] = state[0]; d.nstate[1][idx] = state[1]; d.nstate[2][idx] = state[2];
+      d.nfrc[0][idx] = f[0]; d.nfrc[1][idx] = f[1]; d.nfrc[2][idx] = f[2];
+      d.npnt[0][idx] = point[0]; d.npnt[1][idx] = point[1]; d.npnt[2][idx] = point[2];
+      if (GEOM)
+      {
+        d.nnrm[0][idx] = normal[0]; d.nnrm[1][idx] = normal[1]; d.nnrm[2][idx] = normal[2];
+        d.ndep[idx] = depth;
+      }
+
+      // master-side accumulation (contacts_acc_task, forces.ispc:490-510)
+      double a[3] = {point[0]-x[0], point[1]-x[1], point[2]-x[2]};
+      fs[0] += f[0]; fs[1] += f[1]; fs[2] += f[2];
+      ts[0] += a[1]*f[2] - a[2]*f[1];
+      ts[1] += a[2]*f[0] - a[0]*f[2];
+      ts[2] += a[0]*f[1] - a[1]*f[0];
+    }
+  }
+  d.fm[0][pi] = fs[0]; d.fm[1][pi] = fs[1]; d.fm[2][pi] = fs[2];
+  d.tm[0][pi] = ts[0]; d.tm[1][pi] = ts[1]; d.tm[2][pi] = ts[2];
+}
+
+// ---------------------------------------------------------------- springs (forces.ispc:641-1412)
+__device__ double look_up(const double *t0, const double *t1, int lo, int hi, double arg, double *slope)
+{
+  int h0 = hi;
+  while (hi > lo+1)
+  {
+    int mid = lo + (hi-lo)/2;
+    if (arg > t0[mid]) lo = mid;
+    else hi = mid;
+  }
+  if (lo+1 == h0) lo --;
+  *slope = (t1[lo+1]-t1[lo])/(t0[lo+1]-t0[lo]);
+  return t1[lo] + (*slope)*(arg-t0[lo]);
+}
+
+__device__ double look_up_slope(int i, const double *t0, const double *t1, int lo, int hi, double arg, double *at)
+{
+  const double *ti = i == 0 ? t0 : t1;
+  const double *tj = i == 0 ? t1 : t0;
+  int h0 = hi;
+  while (hi > lo+1)
+  {
+    int mid = lo + (hi-lo)/2;
+    if (arg > ti[mid]) lo = mid;
+    else hi = mid;
+  }
+  if (lo+1 == h0) lo --;
+  if (at) at[0] = tj[lo] + (tj[lo+1]-tj[lo])*(arg-ti[lo])/(ti[lo+1]-ti[lo]);
+  return (t1[lo+1]-t1[lo])/(t0[lo+1]-t0[lo]);
+}
+
+__device__ double extremum_eigenvalue_min(const double *A)
+{
+  double p1 = A[3]*A[3] + A[6]*A[6] + A[7]*A[7];
+  if (p1 == 0.0)
+  {
+    double r = fmax(A[0], A[4]);
+    return fmax(r, A[8]);
+  }
+  double q = (A[0]+A[4]+A[8])/3.0;
+  double p2 = (A[0]-q)*(A[0]-q) + (A[4]-q)*(A[4]-q) + (A[8]-q)*(A[8]-q) + 2*p1;
+  double p = sqrt(p2 / 6.0);
+  double invp = 1.0 / p;
+  double B[9] = {invp*(A[0]-q), invp*A[1], invp*A[2], invp*A[3], invp*(A[4]-q), invp*A[5],
+                 invp*A[6], invp*A[7], invp*(A[8]-q)};
+  double r = 0.5 * (B[0]*(B[4]*B[8]-B[5]*B[7]) + B[3]*(B[2]*B[7]-B[1]*B[8]) + B[6]*(B[1]*B[5]-B[2]*B[4]));
+  double phi;
+  if (r <= -1.0) phi = 3.14159265358979323846 / 3.0;
+  else if (r >= 1.0) phi = 0.0;
+  else phi = acos(r) / 3.0;
+  return q + 2.0 * p * cos(phi + (2*3.14159265358979323846/3));
+}
+
+// equivalent relative point mass (parmec.ispc:423-482)
+__device__ double eqm(const PgDev &d, int part1, const double *point1, int part2, const double *point2,
+                      const double *direction)
+{
+  double Jiv[9], im, A[3], Ask[9], tmp[9], Miv[9];
+  for (int k = 0; k < 9; k ++) Jiv[k] = d.inverse[k][part1];
+  im = d.invm[part1];
+  A[0] = d.position[3][part1] - point1[0];
+  A[1] = d.position[4][part1] - point1[1];
+  A[2] = d.position[5][part1] - point1[2];
+  Ask[0] = 0; Ask[1] = A[2]; Ask[2] = -A[1]; Ask[3] = -A[2]; Ask[4] = 0; Ask[5] = A[0];
+  Ask[6] = A[1]; Ask[7] = -A[0]; Ask[8] = 0;
+  tnmul(Ask, Jiv, tmp);
+  nnmul(tmp, Ask, Miv);
+  Miv[0] += im; Miv[4] += im; Miv[8] += im;
+  if (part2 >= 0)
+  {
+    for (int k = 0; k < 9; k ++) Jiv[k] = d.inverse[k][part2];
+    im = d.invm[part2];
+    A[0] = d.position[3][part2] - point2[0];
+    A[1] = d.position[4][part2] - point2[1];
+    A[2] = d.position[5][part2] - point2[2];
+    Ask[0] = 0; Ask[1] = A[2]; Ask[2] = -A[1]; Ask[3] = -A[2]; Ask[4] = 0; Ask[5] = A[0];
+    Ask[6] = A[1]; Ask[7] = -A[0]; Ask[8] = 0;
+    tnmul(Ask, Jiv, tmp);
+    nnmul(tmp, Ask, Jiv);
+    for (int k = 0; k < 9; k ++) Miv[k] = Miv[k] + Jiv[k];
+    Miv[0] += im; Miv[4] += im; Miv[8] += im;
+  }
+  if (direction && dot3(direction, direction) > 0.0)
+  {
+    nvmul(Miv, direction, tmp);
+    return 1.0/dot3(tmp, direction);
+  }
+  return 1.0/extremum_eigenvalue_min(Miv);
+}
+
+__global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.sprnum) return;
+  const double time = d.t_curtime[*d.stepno];
+  const int j = d.sprpart[0][i], k = d.sprpart[1][i];
+  double len = 0.0, inv, velocity, spring_force = 0.0, dashpot_force, total_force;
+  double Yj[3], Yk[3] = {0.0, 0.0, 0.0}, p[3], q[3], z[3] = {0.0, 0.0, 0.0}, w[3], frc[3], u[3], a[3], b[3] = {0.0, 0.0, 0.0};
+  double stiffness = 0.0, damping = 0.0;
+  double oj[3], vj[3], xj[3], Xj[3], Lj[9];
+  for (int m = 0; m < 3; m ++)
+  {
+    oj[m] = d.angular[3+m][j]; vj[m] = d.linear[m][j]; xj[m] = d.position[m][j]; Xj[m] = d.position[3+m][j];
+  }
+  for (int m = 0; m < 9; m ++) Lj[m] = d.rotation[m][j];
+  const int flg0 = d.sprflg[i];
+  int flg = flg0;
+
+  Yj[0] = d.sprpnt[3][i]; Yj[1] = d.sprpnt[4][i]; Yj[2] = d.sprpnt[5][i];
+  Yj[0] = Yj[0] - Xj[0]; Yj[1] = Yj[1] - Xj[1]; Yj[2] = Yj[2] - Xj[2];
+  nvaddmul(xj, Lj, Yj, p);
+  d.sprpnt[0][i] = p[0]; d.sprpnt[1][i] = p[1]; d.sprpnt[2][i] = p[2];
+  u[0] = vj[0]; u[1] = vj[1]; u[2] = vj[2];
+  u[0] *= -1.0; u[1] *= -1.0; u[2] *= -1.0;
+  a[0] = p[0] - xj[0]; a[1] = p[1] - xj[1]; a[2] = p[2] - xj[2];
+  u[0] -= oj[1]*a[2] - oj[2]*a[1];
+  u[1] -= oj[2]*a[0] - oj[0]*a[2];
+  u[2] -= oj[0]*a[1] - oj[1]*a[0];
+
+  if (k >= 0)
+  {
+    double ok[3], vk[3], xk[3], Xk[3], Lk[9];
+    for (int m = 0; m < 3; m ++)
+    {
+      ok[m] = d.angular[3+m][k]; vk[m] = d.linear[m][k]; xk[m] = d.position[m][k]; Xk[m] = d.position[3+m][k];
+    }
+    for (int m = 0; m < 9; m ++) Lk[m] = d.rotation[m][k];
+    if (flg & PG_SPRDIR_PROJECT)
+    {
+      w[0] = d.sprdir[3][i]; w[1] = d.sprdir[4][i]; w[2] = d.sprdir[5][i];
+      nvmul(Lk, w, z);
+      d.sprdir[0][i] = z[0]; d.sprdir[1][i] = z[1]; d.sprdir[2][i] = z[2];
+    }
+    Yk[0] = d.sprpnt[9][i]; Yk[1] = d.sprpnt[10][i]; Yk[2] = d.sprpnt[11][i];
+    Yk[0] = Yk[0] - Xk[0]; Yk[1] = Yk[1] - Xk[1]; Yk[2] = Yk[2] - Xk[2];
+    nvaddmul(xk, Lk, Yk, q);
+    d.sprpnt[6][i] = q[0]; d.sprpnt[7][i] = q[1]; d.sprpnt[8][i] = q[2];
+    u[0] += vk[0]; u[1] += vk[1]; u[2] += vk[2];
+    b[0] = q[0] - xk[0]; b[1] = q[1] - xk[1]; b[2] = q[2] - xk[2];
+    u[0] += ok[1]*b[2] - ok[2]*b[1];
+    u[1] += ok[2]*b[0] - ok[0]*b[2];
+    u[2] += ok[0]*b[1] - ok[1]*b[0];
+  }
+  else
+  {
+    q[0] = d.sprpnt[6][i]; q[1] = d.sprpnt[7][i]; q[2] = d.sprpnt[8][i];
+    if (flg & PG_SPRDIR_PROJECT) { z[0] = d.sprdir[0][i]; z[1] = d.sprdir[1][i]; z[2] = d.sprdir[2][i]; }
+  }
+
+  switch (flg & (PG_SPRDIR_FOLLOWER|PG_SPRDIR_CONSTANT|PG_SPRDIR_PLANAR|PG_SPRDIR_PROJECT))
+  {
+    case PG_SPRDIR_FOLLOWER:
+      w[0] = q[0] - p[0]; w[1] = q[1] - p[1]; w[2] = q[2] - p[2];
+      len = sqrt(dot3(w, w));
+      inv = len > 0.0 ? 1.0/len : 0.0;
+      z[0] = inv*w[0]; z[1] = inv*w[1]; z[2] = inv*w[2];
+      d.sprdir[0][i] = z[0]; d.sprdir[1][i] = z[1]; d.sprdir[2][i] = z[2];
+      break;
+    case PG_SPRDIR_CONSTANT:
+      w[0] = q[0] - p[0]; w[1] = q[1] - p[1]; w[2] = q[2] - p[2];
+      z[0] = d.sprdir[0][i]; z[1] = d.sprdir[1][i]; z[2] = d.sprdir[2][i];
+      len = dot3(w, z);
+      break;
+    case PG_SPRDIR_PLANAR:
+      w[0] = q[0] - p[0]; w[1] = q[1] - p[1]; w[2] = q[2] - p[2];
+      inv = w[0]*d.sprdir[3][i]+w[1]*d.sprdir[4][i]+w[2]*d.sprdir[5][i];
+      w[0] -= inv*d.sprdir[3][i];
+      w[1] -= inv*d.sprdir[4][i];
+      w[2] -= inv*d.sprdir[5][i];
+      len = sqrt(dot3(w, w));
+      inv = len > 0.0 ? 1.0/len : 0.0;
+      z[0] = inv*w[0]; z[1] = inv*w[1]; z[2] = inv*w[2];
+      d.sprdir[0][i] = z[0]; d.sprdir[1][i] = z[1]; d.sprdir[2][i] = z[2];
+      break;
+    case PG_SPRDIR_PROJECT:
+      w[0] = p[0] - q[0]; w[1] = p[1] - q[1]; w[2] = p[2] - q[2];
+      len = dot3(w, z);
+      break;
+  }
+
+  double offset = 0.0, slope;
+  const int ilc = d.sproffset[i];
+  if (ilc >= 0) offset = look_up(d.lcurve[0], d.lcurve[1], d.lcidx[ilc], d.lcidx[ilc+1], time, &slope);
+
+  const int unspr = d.unspring[i];
+  const double *S0 = d.spring[0], *S1 = d.spring[1];
+  const double *U0 = d.unload[0], *U1 = d.unload[1];
+  if (unspr <= -2)
+  {
+    if (d.sprtype[i] == PG_SPRING_NONLINEAR_ELASTIC)
+    {
+      d.stroke[0][i] = len - d.stroke0[i];
+      spring_force = look_up(S0, S1, d.spridx[i], d.spridx[i+1], d.stroke[0][i] - offset, &stiffness);
+    }
+    else if (d.sprtype[i] == PG_SPRING_GENERAL_NONLINEAR)
+    {
+      if ((flg & PG_SPRING_YIELDED) == 0)
+      {
+        d.stroke[0][i] = len - d.stroke0[i];
+        spring_force = look_up(S0, S1, d.spridx[i], d.spridx[i+1], d.stroke[0][i] - offset, &stiffness);
+        if (spring_force < d.yield[0][i] || spring_force > d.yield[1][i])
+        {
+          flg |= PG_SPRING_YIELDED;
+          if (spring_force < 0)
+          {
+            d.stroke[1][i] = d.stroke[0][i];
+            d.stroke[2][i] = 0.0;
+            d.yield[1][i] = 0.0;
+          }
+          else
+          {
+            d.stroke[1][i] = 0.0;
+            d.stroke[2][i] = d.stroke[0][i];
+            d.yield[0][i] = 0.0;
+          }
+        }
+      }
+      else
+      {
+        double s0 = d.stroke[0][i];
+        double s1 = len - d.stroke0[i];
+        double ds = s1 - s0;
+        double f0 = d.sprfrc[1][i];
+        d.stroke[0][i] = s1;
+        bool loading = false;
+        if (f0 * ds > 0)
+        {
+          if (flg & PG_SPRING_UNLOADING)
+          {
+            double dfds = look_up_slope(1, U0, U1, d.unidx[i], d.unidx[i+1], f0, nullptr);
+            spring_force = f0 + dfds*ds;
+            if (spring_force < d.yield[0][i] || spring_force > d.yield[1][i])
+            {
+              flg &= ~PG_SPRING_UNLOADING;
+              loading = true;
+            }
+          }
+          else loading = true;
+        }
+        else
+        {
+          double at;
+          double dfds = look_up_slope(1, U0, U1, d.unidx[i], d.unidx[i+1], f0, &at);
+          stiffness = dfds;
+          spring_force = f0 + dfds*ds;
+          if (spring_force * f0 < 0.0)
+            spring_force = look_up(U0, U1, d.unidx[i], d.unidx[i+1], ds+at, &stiffness);
+          if (spring_force < d.yield[0][i] || spring_force > d.yield[1][i])
+          {
+            flg &= ~PG_SPRING_UNLOADING;
+            loading = true;
+          }
+          else flg |= PG_SPRING_UNLOADING;
+        }
+        if (loading)
+        {
+          if (ds < 0) d.stroke[1][i] += ds;
+          else d.stroke[2][i] += ds;
+          spring_force = look_up(S0, S1, d.spridx[i], d.spridx[i+1], ds < 0 ? d.stroke[1][i] : d.stroke[2][i], &stiffness);
+          if (ds < 0) d.yield[0][i] = spring_force;
+          else d.yield[1][i] = spring_force;
+        }
+      }
+    }
+    velocity = dot3(z, u);
+    if (d.dashidx[i]+1 == d.dashidx[i+1])
+    {
+      double mass = eqm(d, j, Yj, k, Yk, z);
+      double ratio = d.dashpot[0][d.dashidx[i]];
+      damping = ratio * 2.0 * sqrt(fabs(stiffness) * mass);
+      dashpot_force = velocity * damping;
+    }
+    else
+    {
+      dashpot_force = look_up(d.dashpot[0], d.dashpot[1], d.dashidx[i], d.dashidx[i+1], velocity, &damping);
+    }
+    total_force = spring_force + (spring_force == 0.0 ? 0.0 : dashpot_force);
+  }
+  else if (unspr == -1)
+  {
+    d.stroke[0][i] = len - d.stroke0[i];
+    stiffness = 0.; damping = 0.;
+    spring_force = dashpot_force = total_force = 0.;
+    velocity = dot3(z, u);
+  }
+  else
+  {
+    double s0 = d.stroke[0][i];
+    double s1 = len - d.stroke0[i];
+    double ds = s1 - s0;
+    double f0 = d.sprfrc[1][i];
+    double sgn = f0 > 0. ? 1. : -1.;
+    d.stroke[0][i] = s1;
+    double at;
+    double dfds = look_up_slope(1, d.lcurve[0], d.lcurve[1], d.lcidx[unspr], d.lcidx[unspr+1], f0, &at);
+    stiffness = dfds;
+    spring_force = f0 - sgn*fabs(dfds*ds);
+    if (spring_force * f0 < 0.0)
+    {
+      d.unspring[i] = -1;
+      spring_force = 0.;
+    }
+    damping = 0.; dashpot_force = 0.;
+    total_force = spring_force;
+    velocity = dot3(z, u);
+  }
+
+  frc[0] = z[0] * total_force;
+  frc[1] = z[1] * total_force;
+  frc[2] = z[2] * total_force;
+  d.sprfrc[0][i] = total_force;
+  d.sprfrc[1][i] = spring_force;
+
+  const double fric = d.sprfric[i];
+  if (fric > 0.0)
+  {
+    double us[3] = {u[0] - velocity*z[0], u[1] - velocity*z[1], u[2] - velocity*z[2]};
+    double flim = fric*fabs(total_force);
+    double fsv[3] = {0.0, 0.0, 0.0};
+    double kskn = d.sprkskn[i];
+    if (kskn == 0.0)
+    {
+      double ulen = sqrt(dot3(us, us));
+      if (ulen > 0.0)
+      {
+        double coef = flim/ulen;
+        fsv[0] = coef*us[0]; fsv[1] = coef*us[1]; fsv[2] = coef*us[2];
+      }
+    }
+    else
+    {
+      if (spring_force == 0.0) { d.sprsdsp[0][i] = 0.0; d.sprsdsp[1][i] = 0.0; d.sprsdsp[2][i] = 0.0; }
+      double ds[3] = {d.sprsdsp[0][i] + us[0]*step, d.sprsdsp[1][i] + us[1]*step, d.sprsdsp[2][i] + us[2]*step};
+      double c0 = kskn * fabs(stiffness);
+      double c1 = spring_force == 0.0 ? 0.0 : kskn * fabs(damping);
+      fsv[0] = c0 * ds[0] + c1 * us[0];
+      fsv[1] = c0 * ds[1] + c1 * us[1];
+      fsv[2] = c0 * ds[2] + c1 * us[2];
+      double flen = sqrt(dot3(fsv, fsv));
+      if (flen > flim)
+      {
+        double coef = flim/flen;
+        fsv[0] *= coef; fsv[1] *= coef; fsv[2] *= coef;
+        double dl0 = sqrt(dot3(ds, ds));
+        coef = flim/(c0*dl0);
+        d.sprsdsp[0][i] = coef*ds[0]; d.sprsdsp[1][i] = coef*ds[1]; d.sprsdsp[2][i] = coef*ds[2];
+      }
+      else
+      {
+        d.sprsdsp[0][i] = ds[0]; d.sprsdsp[1][i] = ds[1]; d.sprsdsp[2][i] = ds[2];
+      }
+    }
+    d.sprfrc[2][i] = sqrt(dot3(fsv, fsv));
+    frc[0] += fsv[0]; frc[1] += fsv[1]; frc[2] += fsv[2];
+  }
+  if (flg != flg0) d.sprflg[i] = flg;
+
+  d.spr_out[0][i] = frc[0]; d.spr_out[1][i] = frc[1]; d.spr_out[2][i] = frc[2];
+  d.spr_out[3][i] = a[1]*frc[2] - a[2]*frc[1];
+  d.spr_out[4][i] = a[2]*frc[0] - a[0]*frc[2];
+  d.spr_out[5][i] = a[0]*frc[1] - a[1]*frc[0];
+  d.spr_out[6][i] = b[1]*frc[2] - b[2]*frc[1];
+  d.spr_out[7][i] = b[2]*frc[0] - b[0]*frc[2];
+  d.spr_out[8][i] = b[0]*frc[1] - b[1]*frc[0];
+}
+
+// ---------------------------------------------------------------- integrate
+// contacts_acc_task (slave side) + gravity + spring flushes (single-task order
+// of springs_task) + prescribe_acceleration + dynamics_task +
+// prescribe_velocity + ellipsoids_task, one thread per particle.
+__global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < d.parnum)
+  {
+    const int row = *d.stepno;
+    const double *grav = d.t_gravity + 3*(size_t)row;
+    const double *damping = d.t_damping + 6*(size_t)row;
+    const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+    const int E = d.ellnum;
+    double po[3] = {d.position[0][i], d.position[1][i], d.position[2][i]};
+    double F[3], T[3];
+    const int e = d.pell ? d.pell[i] : -1;
+    if (e >= 0)
+    {
+      F[0] = d.fm[0][i]; F[1] = d.fm[1][i]; F[2] = d.fm[2][i];
+      T[0] = d.tm[0][i]; T[1] = d.tm[1][i]; T[2] = d.tm[2][i];
+    }
+    else { F[0] = F[1] = F[2] = 0.0; T[0] = T[1] = T[2] = 0.0; }
+
+    // slave contacts, in master order (forces.ispc:539-569)
+    if (E)
+    {
+      const int nr = d.rcnt[i];
+      for (int r = 0; r < nr; r ++)
+      {
+        const int ref = d.rref[(size_t)r * d.parnum + i];
+        if (!d.nflag[ref]) continue;
+        double f[3] = {-d.nfrc[0][ref], -d.nfrc[1][ref], -d.nfrc[2][ref]};
+        double a[3] = {d.npnt[0][ref]-po[0], d.npnt[1][ref]-po[1], d.npnt[2][ref]-po[2]};
+        F[0] += f[0]; F[1] += f[1]; F[2] += f[2];
+        T[0] += a[1]*f[2] - a[2]*f[1];
+        T[1] += a[2]*f[0] - a[0]*f[2];
+        T[2] += a[0]*f[1] - a[1]*f[0];
+      }
+    }
+    const double ma = d.mass[i];
+    F[0] = F[0] + ma * grav[0];
+    F[1] = F[1] + ma * grav[1];
+    F[2] = F[2] + ma * grav[2];
+
+    // spring force flushes, in the order a single springs_task applies them
+    if (d.sprnum)
+    {
+      for (int ev = d.sev_first[i]; ev < d.sev_first[i+1]; ev ++)
+      {
+        const int4 v = d.sev[ev];
+        const int off = v.x == 0 ? 3 : 6;
+        double af[3] = {0.0, 0.0, 0.0}, at[3] = {0.0, 0.0, 0.0};
+        bool started = false;
+        for (int s = v.y; s < v.z; s ++)
+        {
+          if (v.x == 1 && d.sprpart[1][s] < 0) continue;
+          double fr[3] = {d.spr_out[0][s], d.spr_out[1][s], d.spr_out[2][s]};
+          double tq[3] = {d.spr_out[off][s], d.spr_out[off+1][s], d.spr_out[off+2][s]};
+          if (!started && !v.w)
+          {
+            af[0] = fr[0]; af[1] = fr[1]; af[2] = fr[2];
+            at[0] = tq[0]; at[1] = tq[1]; at[2] = tq[2];
+          }
+          else
+          {
+            af[0] += fr[0]; af[1] += fr[1]; af[2] += fr[2];
+            at[0] += tq[0]; at[1] += tq[1]; at[2] += tq[2];
+          }
+          started = true;
+        }
+        if (v.x == 0)
+        {
+          F[0] += af[0]; F[1] += af[1]; F[2] += af[2];
+          T[0] += at[0]; T[1] += at[1]; T[2] += at[2];
+        }
+        else
+        {
+          F[0] -= af[0]; F[1] -= af[1]; F[2] -= af[2];
+          T[0] -= at[0]; T[1] -= at[1]; T[2] -= at[2];
+        }
+      }
+    }
+
+    // prescribe_acceleration (input.cpp:4247-4341)
+    const int pb = d.prsnum ? d.prs_first[i] : 0, pe = d.prsnum ? d.prs_first[i+1] : 0;
+    for (int pp = pb; pp < pe; pp ++)
+    {
+      const int q = d.prs_list[pp];
+      const double *lin = d.t_prs_lin + (size_t)row * d.tab_prs_stride + 3*q;
+      const double *ang = d.t_prs_ang + (size_t)row * d.tab_prs_stride + 3*q;
+      if (d.prslin[q] && d.linkind[q] == 1)
+      {
+        F[0] = ma * lin[0]; F[1] = ma * lin[1]; F[2] = ma * lin[2];
+      }
+      else if (d.prslin[q] && d.linkind[q] == 0)
+      {
+        F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
+      }
+      if (d.prsang[q] && d.angkind[q] == 1)
+      {
+        double in[9], acc[3] = {ang[0], ang[1], ang[2]};
+        for (int k = 0; k < 9; k ++) in[k] = d.inertia[k][i];
+        nvmul(in, acc, T);
+      }
+      else if (d.prsang[q] && d.angkind[q] == 0)
+      {
+        T[0] = 0.0; T[1] = 0.0; T[2] = 0.0;
+      }
+    }
+
+    // dynamics_task (dynamics.ispc:30-169)
+    double O[3], o[3], v[3], L1[9], J[9], I[9], im, f[3], t[3], Tb[3], DL[9], L2[9], A[3], B[3];
+    double x[3] = {po[0], po[1], po[2]};
+    if (!(d.flags[i] & PG_FLAG_SKIP))
+    {
+      const double half = 0.5*step;
+      const double hstep = 0.5*(step+step);
+      for (int k = 0; k < 3; k ++) { O[k] = d.angular[k][i]; v[k] = d.linear[k][i]; }
+      for (int k = 0; k < 9; k ++) { L1[k] = d.rotation[k][i]; J[k] = d.inertia[k][i]; I[k] = d.inverse[k][i]; }
+      im = d.invm[i];
+      if (damping[0] != 0.0 || damping[1] != 0.0 || damping[2] != 0.0)
+      {
+        F[0] -= ma * damping[0] * v[0];
+        F[1] -= ma * damping[1] * v[1];
+        F[2] -= ma * damping[2] * v[2];
+      }
+      if (damping[3] != 0.0 || damping[4] != 0.0 || damping[5] != 0.0)
+      {
+        o[0] = damping[3]*d.angular[3][i];
+        o[1] = damping[4]*d.angular[4][i];
+        o[2] = damping[5]*d.angular[5][i];
+        tvmul(L1, o, t);
+        nvmul(J, t, Tb);
+        nvmul(L1, Tb, t);
+        T[0] -= t[0]; T[1] -= t[1]; T[2] -= t[2];
+      }
+      f[0] = F[0]; f[1] = F[1]; f[2] = F[2];
+      t[0] = T[0]; t[1] = T[1]; t[2] = T[2];
+      tvmul(L1, t, Tb);
+      expmap(-half*O[0], -half*O[1], -half*O[2], DL, typo);
+      nvmul(J, O, A);
+      nvmul(DL, A, B);
+      B[0] = B[0] + half*Tb[0];
+      B[1] = B[1] + half*Tb[1];
+      B[2] = B[2] + half*Tb[2];
+      nvmul(I, B, A);
+      nvmul(J, A, B);
+      Tb[0] -= A[1]*B[2] - A[2]*B[1];
+      Tb[1] -= A[2]*B[0] - A[0]*B[2];
+      Tb[2] -= A[0]*B[1] - A[1]*B[0];
+      Tb[0] *= step; Tb[1] *= step; Tb[2] *= step;
+      nvaddmul(O, I, Tb, O);
+      im *= step;
+      v[0] = v[0] + im*f[0];
+      v[1] = v[1] + im*f[1];
+      v[2] = v[2] + im*f[2];
+      expmap(hstep*O[0], hstep*O[1], hstep*O[2], DL, typo);
+      nnmul(L1, DL, L2);
+      nvmul(L2, O, o);
+      x[0] += hstep*v[0];
+      x[1] += hstep*v[1];
+      x[2] += hstep*v[2];
+
+      // prescribe_velocity (input.cpp:4344-4421)
+      for (int pp = pb; pp < pe; pp ++)
+      {
+        const int q = d.prs_list[pp];
+        const double *lin = d.t_prs_lin + (size_t)row * d.tab_prs_stride + 3*q;
+        const double *ang = d.t_prs_ang + (size_t)row * d.tab_prs_stride + 3*q;
+        if (d.prslin[q] && d.linkind[q] == 0) { v[0] = lin[0]; v[1] = lin[1]; v[2] = lin[2]; }
+        if (d.prsang[q] && d.angkind[q] == 0)
+        {
+          double oo[3] = {ang[0], ang[1], ang[2]};
+          tvmul(L2, oo, O);
+          o[0] = oo[0]; o[1] = oo[1]; o[2] = oo[2];
+        }
+      }
+
+      for (int k = 0; k < 9; k ++) d.rotation[k][i] = L2[k];
+      for (int k = 0; k < 3; k ++)
+      {
+        d.position[k][i] = x[k];
+        d.angular[k][i] = O[k];
+        d.angular[3+k][i] = o[k];
+        d.linear[k][i] = v[k];
+      }
+    }
+    else
+    {
+      // skipped particle: prescribe_velocity still applies (it runs after dynamics)
+      for (int pp = pb; pp < pe; pp ++)
+      {
+        const int q = d.prs_list[pp];
+        const double *lin = d.t_prs_lin + (size_t)row * d.tab_prs_stride + 3*q;
+        const double *ang = d.t_prs_ang + (size_t)row * d.tab_prs_stride + 3*q;
+        if (d.prslin[q] && d.linkind[q] == 0)
+          for (int k = 0; k < 3; k ++) d.linear[k][i] = lin[k];
+        if (d.prsang[q] && d.angkind[q] == 0)
+        {
+          double Lc[9], oo[3] = {ang[0], ang[1], ang[2]}, Oc[3];
+          for (int k = 0; k < 9; k ++) Lc[k] = d.rotation[k][i];
+          tvmul(Lc, oo, Oc);
+          for (int k = 0; k < 3; k ++) { d.angular[k][i] = Oc[k]; d.angular[3+k][i] = oo[k]; }
+        }
+      }
+      for (int k = 0; k < 9; k ++) L2[k] = d.rotation[k][i];
+    }
+    d.force[0][i] = F[0]; d.force[1][i] = F[1]; d.force[2][i] = F[2];
+    d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
+
+    // ellipsoids_task for this particle's sphere (shapes.ispc:29-98)
+    if (e >= 0)
+    {
+      double X[3] = {d.position[3][i], d.position[4][i], d.position[5][i]};
+      double C[3] = {d.center[3][e], d.center[4][e], d.center[5][e]}, c[3];
+      body_point(x, L2, X, C, c);
+      d.center[0][e] = c[0]; d.center[1][e] = c[1]; d.center[2][e] = c[2];
+      double r0 = c[0] - d.cref[0][e], r1 = c[1] - d.cref[1][e], r2 = c[2] - d.cref[2][e];
+      need = (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
+    }
+  }
+  if (d.ellnum) flag_rebuild(d, need);
+}
+
+} // namespace
+
+// ================================================================ launchers
+void pg_launch_invert(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_invert<<<nblk(d.parnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_euler(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.parnum) k_euler<<<nblk(d.parnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_shapes(const PgDev &d, cudaStream_t s, bool skip_analytical)
+{
+  if (d.ellnum) k_spheres<<<nblk(d.ellnum), TPB, 0, s>>>(d);
+  if (d.nodnum) k_nodes<<<nblk(d.nodnum), TPB, 0, s>>>(d, skip_analytical ? 1 : 0);
+  if (d.facnum) k_faces<<<nblk(d.facnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.obsnum && d.trinum) k_obstacles<<<nblk(d.trinum), TPB, 0, s>>>(d, step, 0);
+  if (d.obsnum) k_tail<<<1, 32, 0, s>>>(d, step, 0);
+}
+
+void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
+{
+  if (!d.ellnum) return;
+  if (d.record_geometry) k_contacts<true><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  else k_contacts<false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.sprnum) k_springs<<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.parnum) k_integrate<<<nblk(d.parnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_mesh(const PgDev &d, cudaStream_t s)
+{
+  if (d.nodnum) k_nodes<<<nblk(d.nodnum), TPB, 0, s>>>(d, 1);
+  if (d.facnum) k_faces<<<nblk(d.facnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.obsnum && d.trinum) k_obstacles<<<nblk(d.trinum), TPB, 0, s>>>(d, step, 1);
+}
+
+void pg_launch_tail(const PgDev &d, cudaStream_t s, double step)
+{
+  k_tail<<<1, 32, 0, s>>>(d, step, 1);
+}
+
+int pg_step_kernel_count(const PgDev &d)
+{
+  int n = 1;                                   // tail
+  if (d.ellnum) n += 1;                        // contacts
+  if (d.sprnum) n += 1;
+  if (d.parnum) n += 1;                        // integrate
+  if (d.nodnum) n += 1;
+  if (d.facnum) n += 1;
+  if (d.obsnum && d.trinum) n += 1;
+  return n;
+}

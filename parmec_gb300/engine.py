@@ -1,0 +1,96 @@
+"""Compute engine over the device-resident session API of libparmec_gb300.so."""
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+
+def _counts(m):
+    return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
+            len(m.prescribe), len(m.pairs), len(m.lcurves))
+
+
+class GpuEngine:
+    """Runs DEM steps of one Model in a pg_session on the current CUDA device."""
+
+    def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False):
+        self.lib = abi.load_library()
+        self.form = form
+        self.skin = skin
+        self.record_geometry = record_geometry
+        self.model = None
+        self.sess = None
+        self.scene = None
+        self.counts = None
+
+    def attach(self, m):
+        self.close()
+        self.model = m
+        self.scene = m.scene()
+        self.counts = _counts(m)
+        h = ctypes.c_void_p()
+        abi.check(self.lib.pg_session_create(ctypes.byref(self.scene), self.form, ctypes.byref(h)),
+                  "pg_session_create")
+        self.sess = h
+        if self.skin is not None:
+            abi.check(self.lib.pg_session_set_skin(self.sess, float(self.skin)), "pg_session_set_skin")
+        if self.record_geometry:
+            abi.check(self.lib.pg_session_record_geometry(self.sess, 1), "pg_session_record_geometry")
+
+    def stale(self):
+        return self.model is None or _counts(self.model) != self.counts
+
+    def upload(self):
+        self.scene = self.model.scene()
+        abi.check(self.lib.pg_session_upload(self.sess, ctypes.byref(self.scene)), "pg_session_upload")
+
+    def first_half_step(self, step, ang, lin):
+        ang = np.ascontiguousarray(ang, dtype=np.float64)
+        lin = np.ascontiguousarray(lin, dtype=np.float64)
+        abi.check(self.lib.pg_session_first_half_step(self.sess, step, abi.dptr(ang), abi.dptr(lin)),
+                  "pg_session_first_half_step")
+
+    def invert_inertia(self):
+        abi.check(self.lib.pg_session_invert_inertia(self.sess), "pg_session_invert_inertia")
+
+    def run(self, tab, step):
+        abi.check(self.lib.pg_session_run(self.sess, ctypes.byref(tab), step), "pg_session_run")
+
+    def sync(self):
+        abi.check(self.lib.pg_session_sync(self.sess), "pg_session_sync")
+
+    def download(self):
+        abi.check(self.lib.pg_session_download(self.sess, ctypes.byref(self.scene)), "pg_session_download")
+        self.model.pull_obstacles()
+
+    def kernel_launches(self):
+        n = ctypes.c_longlong()
+        abi.check(self.lib.pg_session_kernel_launches(self.sess, ctypes.byref(n)), "kernel_launches")
+        return n.value
+
+    def contacts(self):
+        """Active contacts in canonical order as a dict of numpy arrays."""
+        n = ctypes.c_int()
+        abi.check(self.lib.pg_session_contact_count(self.sess, ctypes.byref(n)), "contact_count")
+        cap = max(1, n.value)
+        out = {"mpart": np.zeros(cap, np.int32), "code": np.zeros(cap, np.int32),
+               "point": np.zeros((cap, 3)), "normal": np.zeros((cap, 3)), "depth": np.zeros(cap),
+               "force": np.zeros((cap, 3)), "state": np.zeros((cap, 3))}
+        cnt = ctypes.c_int()
+        abi.check(self.lib.pg_session_contacts(
+            self.sess, cap, ctypes.byref(cnt), abi.iptr(out["mpart"]), abi.iptr(out["code"]),
+            abi.dptr(out["point"]), abi.dptr(out["normal"]), abi.dptr(out["depth"]),
+            abi.dptr(out["force"]), abi.dptr(out["state"])), "contacts")
+        return {k: v[:cnt.value] for k, v in out.items()}
+
+    def close(self):
+        if self.sess is not None:
+            self.lib.pg_session_destroy(self.sess)
+            self.sess = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

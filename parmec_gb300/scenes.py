@@ -1,0 +1,140 @@
+"""Seeded synthetic scenes with the shapes, sizes and value distributions of the
+benchmark configurations (the reference publishes no benchmark decks).
+
+hopper_fill  4,096 spheres on a jittered 16^3 lattice in a 1 m box of 12
+             triangles; GRANULAR spring 1e6, damping 0.2, friction 0.5;
+             dt = 0.1 of the single-contact critical step (CPU-runnable case).
+drum         N spheres (1,048,576 for the full case), radii log-uniform in
+             [0.5, 2] mm, a bed in the lower part of a rotating cylinder of
+             4,096 triangles (R = 0.5 m, L = 0.3 m, 2 rad/s about x);
+             friction 0.3.
+"""
+import math
+
+import numpy as np
+
+from .model import Model
+
+
+def critical_step(kn, m_min, xi):
+    """Single-contact critical step h = (2/w)(sqrt(1+xi^2) - xi), w = sqrt(kn/m)
+    (the LS-DYNA form used by parmec.ispc:300-379)."""
+    w = math.sqrt(kn / m_min)
+    return (2.0 / w) * (math.sqrt(1.0 + xi * xi) - xi)
+
+
+def box_triangles(lo, hi):
+    """12 triangles of an axis-aligned box."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0),
+         (x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]
+    quads = [(0, 1, 2, 3), (4, 5, 6, 7), (0, 1, 5, 4), (3, 2, 6, 7), (0, 3, 7, 4), (1, 2, 6, 5)]
+    tris = []
+    for a, b, c, d in quads:
+        tris.append(v[a] + v[b] + v[c])
+        tris.append(v[a] + v[c] + v[d])
+    return [tuple(float(x) for x in t) for t in tris]
+
+
+def hopper_fill(n_side=16, seed=0, spacing=0.045, jitter=0.005, rmin=0.01, rmax=0.02, density=2500.0,
+                kn=1e6, damper=0.2, friction=0.5, box=1.0):
+    """Config 0: returns (model, dt)."""
+    rng = np.random.default_rng(seed)
+    m = Model()
+    mat = m.material(density, 1e9, 0.25)
+    n = n_side ** 3
+    g = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), np.arange(n_side), indexing="ij"), -1)
+    g = g.reshape(-1, 3)[:, ::-1].astype(np.float64)          # x fastest
+    extent = (n_side - 1) * spacing
+    org = 0.5 * (box - extent)
+    centers = org + g * spacing + rng.uniform(-jitter, jitter, size=(n, 3))
+    radii = rng.uniform(rmin, rmax, size=n)
+    parts = m.spheres(centers, radii, mat, 1)
+    v0 = rng.normal(0.0, 0.05, size=(n, 3))
+    m.P.linear[:, parts[0]:parts[-1] + 1] = v0.T
+    m.obstacle(box_triangles((0.0, 0.0, 0.0), (box, box, box)), 2)
+    m.granular(0, 0, kn, damper, friction)
+    m.set_gravity(0.0, 0.0, -9.81)
+    m_min = (4.0 / 3.0) * math.pi * rmin ** 3 * density
+    dt = 0.1 * critical_step(kn, m_min, damper)
+    return m, dt
+
+
+def cylinder_triangles(radius=0.5, length=0.3, n_theta=128, n_x=13):
+    """Cylinder along x with capped ends: 2*n_theta*n_x side triangles plus two
+    caps of n_theta fan + 2*n_theta ring triangles (4,096 for the defaults)."""
+    tris = []
+    th = np.linspace(0.0, 2.0 * math.pi, n_theta + 1)
+    xs = np.linspace(-0.5 * length, 0.5 * length, n_x + 1)
+    def p(x, r, t):
+        return (float(x), float(r * math.cos(t)), float(r * math.sin(t)))
+    for a in range(n_x):
+        for b in range(n_theta):
+            p0, p1 = p(xs[a], radius, th[b]), p(xs[a + 1], radius, th[b])
+            p2, p3 = p(xs[a + 1], radius, th[b + 1]), p(xs[a], radius, th[b + 1])
+            tris.append(p0 + p1 + p2)
+            tris.append(p0 + p2 + p3)
+    for x in (-0.5 * length, 0.5 * length):
+        rin = 0.5 * radius
+        for b in range(n_theta):
+            tris.append((float(x), 0.0, 0.0) + p(x, rin, th[b]) + p(x, rin, th[b + 1]))
+            q0, q1 = p(x, rin, th[b]), p(x, radius, th[b])
+            q2, q3 = p(x, radius, th[b + 1]), p(x, rin, th[b + 1])
+            tris.append(q0 + q1 + q2)
+            tris.append(q0 + q2 + q3)
+    return tris
+
+
+def drum(n=1048576, seed=1, radius=0.5, length=0.3, rmin=0.5e-3, rmax=2e-3, density=2500.0,
+         kn=1e6, damper=0.2, friction=0.3, omega=2.0, overlap=0.002):
+    """Config 1: returns (model, dt, info).
+
+    Placement: radii are drawn log-uniform and sorted; spheres fill slabs from
+    the bottom of the drum upwards on square lattices whose pitch is the
+    slab's largest diameter times (1 - overlap), so neighbours of similar size
+    start in light contact.  The achieved solid fraction of the bed is
+    reported in `info`.
+    """
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(math.log(rmin), math.log(rmax), size=n))
+    r = np.sort(r)[::-1]
+    centers = np.zeros((n, 3))
+    filled = 0
+    z = -radius + rmax * 1.5
+    half = 0.5 * length - rmax
+    bed_volume = 0.0
+    while filled < n:
+        rl = r[filled]
+        pitch = 2.0 * rl * (1.0 - overlap)
+        zc = z + rl
+        if zc + rl > radius:
+            raise ValueError("drum is too small for the requested sphere count")
+        ychord = math.sqrt(max(0.0, (radius - rmax) ** 2 - zc ** 2))
+        nx = int(2 * half / pitch) + 1
+        ny = int(2 * ychord / pitch) + 1
+        xs = -half + pitch * np.arange(nx)
+        ys = -ychord + pitch * np.arange(ny)
+        X, Y = np.meshgrid(xs, ys, indexing="ij")
+        layer = np.stack([X.ravel(), Y.ravel(), np.full(X.size, zc)], -1)
+        take = min(len(layer), n - filled)
+        sel = layer[:take]
+        jit = rng.uniform(-0.02, 0.02, size=(take, 3)) * rl
+        centers[filled:filled + take] = sel + jit
+        bed_volume += 2 * half * 2 * ychord * pitch
+        filled += take
+        z += pitch
+    m = Model()
+    mat = m.material(density, 1e9, 0.25)
+    m.spheres(centers, r, mat, 1)
+    m.obstacle(cylinder_triangles(radius, length), 2, point=(0.0, 0.0, 0.0),
+               angular=lambda t: (omega, 0.0, 0.0))
+    m.granular(0, 0, kn, damper, friction)
+    m.set_gravity(0.0, 0.0, -9.81)
+    m_min = (4.0 / 3.0) * math.pi * rmin ** 3 * density
+    dt = 0.1 * critical_step(kn, m_min, damper)
+    solid = float(np.sum((4.0 / 3.0) * math.pi * r ** 3))
+    info = {"spheres": n, "solid_volume": solid, "bed_volume": bed_volume,
+            "solid_fraction": solid / bed_volume if bed_volume > 0 else 0.0,
+            "drum_fill_fraction": solid / (math.pi * radius ** 2 * length), "dt": dt}
+    return m, dt, info

@@ -1,0 +1,257 @@
+"""SPRING command, spring ordering and spring tables (host side).
+
+Restates input.cpp:1440-1788 (SPRING), parmec.cpp:1683-1965 (sort_springs),
+parmec.cpp:1239-1269 (lcurve_from_time_series) and parmec.ispc:485-544
+(critical_perspring) for the host.  The per-step spring force itself runs on
+the device.
+"""
+import math
+
+import numpy as np
+
+from .model import (REAL_MAX, SPRDIR_CONSTANT, SPRDIR_FOLLOWER, SPRDIR_PLANAR, SPRDIR_PROJECT,
+                    SPRING_GENERAL_NONLINEAR, SPRING_NONLINEAR_ELASTIC)
+
+
+def _pairs(lst, what):
+    if not isinstance(lst, list) or len(lst) < 4 or len(lst) % 2:
+        raise ValueError(f"Invalid {what} lookup table list length")
+    return [(float(lst[2 * j]), float(lst[2 * j + 1])) for j in range(len(lst) // 2)]
+
+
+def spring_command(m, part1, point1, part2, geom2, spring, dashpot, direction, planar,
+                   unload, ylim, inactive, offset, friction, kskn):
+    if part1 < 0:
+        raise ValueError("'part1' must be non-negative")
+    if not (isinstance(point1, tuple) and len(point1) == 3):
+        raise TypeError("'point1' must be a tuple of size 3")
+    if friction < 0 or kskn < 0:
+        raise ValueError("'friction' and 'kskn' must be non-negative")
+    if offset < -1 or offset >= len(m.tms):
+        raise ValueError("offset TSERIES index is out of range")
+    if part2 < -1:
+        raise ValueError("Particle two index is out of range [-1, 0, ...]")
+    sp = _pairs(spring, "spring")
+    for j in range(1, len(sp)):
+        if sp[j][0] <= sp[j - 1][0]:
+            raise ValueError("Spring stroke values must increase")
+    if isinstance(dashpot, list):
+        dp = _pairs(dashpot, "dashpot")
+        for j in range(1, len(dp)):
+            if dp[j][0] <= dp[j - 1][0]:
+                raise ValueError("Dashpot velocity values must increase")
+    elif dashpot is not None:
+        ratio = float(dashpot)
+        if ratio < 0.0:
+            raise ValueError("Critical damping ratio not in [0.0, +Inf) interval")
+        dp = [(ratio, ratio)]
+    else:
+        dp = [(-REAL_MAX, 0.0), (REAL_MAX, 0.0)]
+    ul = None
+    if unload is not None:
+        ul = _pairs(unload, "unload")
+        for j in range(1, len(ul)):
+            slope = (ul[j][1] - ul[j - 1][1]) / (ul[j][0] - ul[j - 1][0])
+            if slope <= 0.0:
+                raise ValueError("Unloading curve must be monotonically increasing")
+
+    S = m.S
+    i = m.sprnum
+    S.ensure(i + 1)
+    m.sprnum += 1
+    S.sprid[i] = i
+    S.sprmap[i] = i
+    S.sprpart[:, i] = (part1, part2)
+    p1 = [float(x) for x in point1]
+    S.sprpnt[0:3, i] = p1
+    S.sprpnt[3:6, i] = p1
+    S.sprdir[:, i] = 0.0
+    if isinstance(geom2, tuple):
+        if len(geom2) != 3:
+            raise TypeError("'geom2' must be a tuple of size 3 or a [point, normal] list")
+        q = [float(x) for x in geom2]
+        S.sprpnt[6:9, i] = q
+        S.sprpnt[9:12, i] = q
+    else:
+        point, normal = geom2[0], geom2[1]
+        q = [float(x) for x in point]
+        d = [float(x) for x in normal]
+        ln = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])     # NORMALIZE (macros.h:427)
+        d = [d[0] / ln, d[1] / ln, d[2] / ln]
+        S.sprdir[0:3, i] = d
+        S.sprdir[3:6, i] = d
+        w = [p1[0] - q[0], p1[1] - q[1], p1[2] - q[2]]
+        ln = d[0] * w[0] + d[1] * w[1] + d[2] * w[2]
+        q = [p1[0] - ln * d[0], p1[1] - ln * d[1], p1[2] - ln * d[2]]   # SUBMUL
+        S.sprpnt[6:9, i] = q
+        S.sprpnt[9:12, i] = q
+    S.sprflg[i] = 0
+    S.sproffset[i] = -1 if offset < 0 else _lcurve_from_time_series(m, offset)
+    S.sprfric[i] = float(friction)
+    S.sprkskn[i] = float(kskn)
+    S.sprsdsp[:, i] = 0.0
+    S.stroke[:, i] = 0.0
+    S.sprfrc[:, i] = 0.0
+    m.spring_tab.append(sp)
+    m.dashpot_tab.append(dp)
+    m.unload_tab.append(ul)
+    S.sprtype[i] = SPRING_GENERAL_NONLINEAR if ul is not None else SPRING_NONLINEAR_ELASTIC
+    S.unspring[i] = -1 if inactive is True else -3
+    if not isinstance(geom2, tuple):
+        S.sprflg[i] |= SPRDIR_PROJECT
+        S.stroke0[i] = 0.0
+    else:
+        if direction is not None:
+            d = [float(x) for x in direction]
+            ln = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+            if ln == 0.0:
+                raise ValueError("Invalid zero direction")
+            inv = 1.0 / ln
+            d = [d[0] * inv, d[1] * inv, d[2] * inv]
+            S.sprdir[0:3, i] = d
+            S.sprdir[3:6, i] = d
+            if planar is not None:
+                if planar == "ON":
+                    S.sprflg[i] |= SPRDIR_PLANAR
+                elif planar == "OFF":
+                    S.sprflg[i] |= SPRDIR_CONSTANT
+                else:
+                    raise ValueError("Invalid planar switch")
+            else:
+                S.sprflg[i] |= SPRDIR_CONSTANT
+            dif = [q[0] - p1[0], q[1] - p1[1], q[2] - p1[2]]
+            if S.sprflg[i] & SPRDIR_CONSTANT:
+                S.stroke0[i] = dif[0] * d[0] + dif[1] * d[1] + dif[2] * d[2]
+            else:
+                dot = dif[0] * d[0] + dif[1] * d[1] + dif[2] * d[2]
+                dif = [dif[0] - dot * d[0], dif[1] - dot * d[1], dif[2] - dot * d[2]]
+                S.stroke0[i] = math.sqrt(dif[0] * dif[0] + dif[1] * dif[1] + dif[2] * dif[2])
+        else:
+            S.sprflg[i] |= SPRDIR_FOLLOWER
+            dif = [q[0] - p1[0], q[1] - p1[1], q[2] - p1[2]]
+            S.stroke0[i] = math.sqrt(dif[0] * dif[0] + dif[1] * dif[1] + dif[2] * dif[2])
+    if ylim is not None:
+        y0, y1 = float(ylim[0]), float(ylim[1])
+        if y0 > 0.0:
+            raise ValueError("Compressive yield limit must be <= 0.0")
+        if y1 < 0.0:
+            raise ValueError("Tensile yield limit must be >= 0.0")
+        S.yield_[:, i] = (y0, y1)
+    else:
+        S.yield_[:, i] = (0.0, 0.0)
+    return i
+
+
+def _lcurve_from_time_series(m, ts):
+    """lcurve_from_time_series (parmec.cpp:1239-1269): copy a TSERIES into the lookup curves once."""
+    for k, t in enumerate(m.lcurves):
+        if t == ts:
+            return k
+    m.lcurves.append(ts)
+    return len(m.lcurves) - 1
+
+
+def sort_springs(m):
+    """sort_springs (parmec.cpp:1683-1965): order springs by (part0, part1).
+
+    Springs with equal keys keep their creation order (stable sort)."""
+    n = m.sprnum
+    if n == 0:
+        return
+    S = m.S
+    order = sorted(range(n), key=lambda i: (int(S.sprpart[0, i]), int(S.sprpart[1, i])))
+    for name, (ncomp, _) in S.spec.items():
+        arr = getattr(S, name)
+        if ncomp:
+            arr[:, :n] = arr[:, order]
+        else:
+            arr[:n] = arr[order]
+    m.spring_tab = [m.spring_tab[i] for i in order]
+    m.dashpot_tab = [m.dashpot_tab[i] for i in order]
+    m.unload_tab = [m.unload_tab[i] for i in order]
+    for i in range(n):
+        S.sprmap[S.sprid[i]] = i
+
+
+def spring_tables(m):
+    """Flat lookup tables (spring[2][*], spridx, ...) in the current spring order."""
+    n = m.sprnum
+
+    def flat(tabs):
+        idx = np.zeros(n + 1, dtype=np.int32)
+        xs, ys = [], []
+        for i, t in enumerate(tabs):
+            t = t or []
+            idx[i + 1] = idx[i] + len(t)
+            xs += [p[0] for p in t]
+            ys += [p[1] for p in t]
+        arr = np.zeros((2, max(1, len(xs))), dtype=np.float64)
+        arr[0, :len(xs)] = xs
+        arr[1, :len(ys)] = ys
+        return arr, idx
+
+    spring, spridx = flat(m.spring_tab)
+    dashpot, dashidx = flat(m.dashpot_tab)
+    unload, unidx = flat(m.unload_tab)
+    lcidx = np.zeros(len(m.lcurves) + 1, dtype=np.int32)
+    xs, ys = [], []
+    for k, ts in enumerate(m.lcurves):
+        pts = m.tms[ts].points
+        lcidx[k + 1] = lcidx[k] + len(pts)
+        xs += [p[0] for p in pts]
+        ys += [p[1] for p in pts]
+    lcurve = np.zeros((2, max(1, len(xs))), dtype=np.float64)
+    lcurve[0, :len(xs)] = xs
+    lcurve[1, :len(ys)] = ys
+    return {"spring": spring, "spridx": spridx, "dashpot": dashpot, "dashidx": dashidx,
+            "unload": unload, "unidx": unidx, "lcurve": lcurve, "lcidx": lcidx}
+
+
+def _eqm(m, part1, point1, part2, point2, direction):
+    """eqm (parmec.ispc:423-482) on the host model."""
+    P = m.P
+
+    def block(part, point):
+        Jiv = P.inverse[:, part]
+        A = [P.position[3, part] - point[0], P.position[4, part] - point[1], P.position[5, part] - point[2]]
+        Ask = np.array([0, A[2], -A[1], -A[2], 0, A[0], A[1], -A[0], 0], dtype=float).reshape(3, 3).T
+        J = np.array(Jiv, dtype=float).reshape(3, 3).T
+        return Ask.T @ J @ Ask + P.invm[part] * np.eye(3)
+
+    Miv = block(part1, point1)
+    if part2 >= 0:
+        Miv = Miv + block(part2, point2)
+    d = np.array(direction, dtype=float)
+    if d @ d > 0.0:
+        return 1.0 / float(d @ (Miv @ d))
+    return 1.0 / float(np.linalg.eigvalsh(Miv)[0])
+
+
+def critical_perspring(m):
+    """critical_perspring (parmec.ispc:485-544): per-spring critical step, omega, damping ratio."""
+    S = m.S
+    h, o, r = [], [], []
+    for j in range(m.sprnum):
+        i, k = int(S.sprpart[0, j]), int(S.sprpart[1, j])
+        sp = m.spring_tab[j]
+        kspr = 0.0
+        for a in range(len(sp) - 1):
+            kk = (sp[a + 1][1] - sp[a][1]) / (sp[a + 1][0] - sp[a][0])
+            kspr = max(abs(kk), kspr)
+        mspr = _eqm(m, i, S.sprpnt[3:6, j], k, S.sprpnt[9:12, j], S.sprdir[0:3, j])
+        omega = math.sqrt(kspr / mspr)
+        ksi = 0.0
+        dp = m.dashpot_tab[j]
+        if len(dp) == 1:
+            ksi = dp[0][0]
+        else:
+            espr = 0.0
+            for a in range(len(dp) - 1):
+                e = (dp[a + 1][1] - dp[a][1]) / (dp[a + 1][0] - dp[a][0])
+                espr = max(abs(e), espr)
+            if omega > 0.0:
+                ksi = espr / (2 * mspr * omega)
+        h.append((2.0 / omega) * (math.sqrt(1.0 + ksi * ksi) - ksi) if omega > 0.0 else 1.0)
+        o.append(omega)
+        r.append(ksi)
+    return h, o, r
