@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Throughput of the plain FP64 DEM step on the rotating-drum scene.
+
+Workload: 1,048,576 spheres, radii log-uniform in [0.5, 2] mm, in a cylinder
+of 4,096 triangles (R = 0.5 m, L = 0.3 m) rotating at 2 rad/s about x;
+GRANULAR spring 1e6 N/m, damping 0.2, friction 0.3; dt = 0.1 of the critical
+step.  One bench step = one DEM time step of the whole scene.  The scene
+state (~0.6 GB) is larger than L2 (129 MB), so no flush is needed between
+steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 (under torchrun) runs independent replicas, one per GPU ("replicas
+only": scenes do not exchange data), and reports the aggregate.
+--impl reference times the CPU restatement of the reference's ISPC path
+(the reference itself cannot be built: no ispc) on all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = ("rotating drum: 1,048,576 spheres, radii log-uniform [0.5,2] mm, 4,096-triangle cylinder "
+            "R=0.5 m L=0.3 m at 2 rad/s, GRANULAR kn=1e6 damping 0.2 friction 0.3, dt=0.1 critical")
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def state_bytes(m):
+    """Bytes the session uploads / downloads for a scene (the arrays copied)."""
+    P, E, T = m.parnum, m.ellnum, m.trinum
+    up = P * 8 * (6 + 3 + 9 + 6 + 9 + 9 + 2 + 3 + 3) + P * 4 * 2 + E * (8 * 9 + 4 * 2) + T * (8 * 9 + 8)
+    down = P * 8 * (6 + 3 + 9 + 6 + 9 + 1 + 3 + 3) + E * 8 * 3 + T * 8 * 9
+    return up, down
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(n_spheres, threads, steps=3):
+    """The oracle (restatement of the reference's ISPC path) on a bounded sample:
+    the same drum scene, one untimed step, then `steps` timed steps."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.scenes import drum
+    m, dt, _ = drum(n_spheres)
+    eng = OracleEngine(threads=threads)
+    m.dem(0.5 * dt, dt, interval=1e9, engine=eng)
+    t0 = time.perf_counter()
+    m.dem(steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    el = time.perf_counter() - t0
+    return {"value": m.parnum * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} DEM steps of the full {m.parnum}-sphere drum after one untimed step, "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU restatement on all host cores, rank 0 only."""
+    if rank != 0:
+        return 0
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.scenes import drum
+    threads = os.cpu_count() or 1
+    m, dt, info = drum(args.spheres)
+    eng = OracleEngine(threads=threads)
+    m.dem(0.5 * dt, dt, interval=1e9, engine=eng)
+    if args.warmup > 1:
+        m.dem((args.warmup - 1) * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    t0 = time.perf_counter()
+    m.dem(args.steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    el = time.perf_counter() - t0
+    v = m.parnum * args.steps / el
+    line = {"impl": "reference", "metric": "particle-steps/s", "value": v, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "spheres": m.parnum},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} DEM steps of the full drum (the reference's ISPC build "
+                                       "cannot be compiled here: no ispc, no HDF5)"},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--spheres", type=int, default=1048576)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = env_int("RANK", 0)
+    world = env_int("WORLD_SIZE", 1)
+    local = env_int("LOCAL_RANK", 0)
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    import __graft_entry__
+    if not os.path.exists(os.path.join(HERE, "parmec_gb300", "_build", "libparmec_gb300.so")):
+        __graft_entry__.build()
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import drum
+    from parmec_gb300 import driver
+
+    m, dt, info = drum(args.spheres)
+    eng = GpuEngine()
+    eng.attach(m)
+    m.engine = eng
+    m._dirty = False
+    # warm-up: the first DEM call (half step, inverse inertia) and W steps
+    try:
+        m.dem(args.warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    except RuntimeError:
+        print(json.dumps({"warmup_failure_diagnostics": eng.diagnostics()}), file=sys.stderr)
+        raise
+
+    # timed region: K steps, device resident, CUDA events on the session stream
+    times, end_time = driver.step_times(m.curtime, args.steps * dt - 0.5 * dt, dt)
+    tabs = driver.StepTables(m, times, dt, [1e9, 1e9], [None, None], [-1, -1])
+    ctab = tabs.ctab(0, len(times))
+    stream = torch.cuda.ExternalStream(eng.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    eng.profile(True)
+    launches0 = eng.kernel_launches()
+    clocks.start()
+    ev0.record(stream)
+    eng.run(ctab, dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = eng.kernel_launches() - launches0
+    prof = eng.profile_read()
+    eng.profile(False)
+    m.curtime = end_time
+    el_ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([el_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_ms = float(t.item())
+        dist.barrier()
+    eng.download()
+    contacts = eng.contacts()
+    nc = len(contacts["mpart"])
+    c_pair = nc / m.parnum
+
+    # end to end through the public DEM command: host arrays -> device, K steps, device -> host
+    m._dirty = True
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    try:
+        m.dem(args.steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    except RuntimeError:
+        print(json.dumps({"e2e_failure_diagnostics": eng.diagnostics()}), file=sys.stderr)
+        raise
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    up, down = state_bytes(m)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    total_ps = m.parnum * args.steps * world
+    value = total_ps / (el_ms * 1e-3)
+    hbm, peak_kind = peaks()
+    # roofline of the dominant kernel group (algorithmic bytes: each datum the
+    # kernel must read or write, counted once; formulas in the design doc)
+    groups = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(groups, key=lambda k: groups[k][0])
+    P = m.parnum
+    cand = None
+    per_launch = {
+        "integrate": P * (696.0 + 53.0 * c_pair),
+        "contacts": P * (172.0 + 96.0 * c_pair),
+    }
+    ms_dom, n_dom = groups[dom]
+    launches_dom = max(1, n_dom)
+    bytes_dom = per_launch.get(dom)
+    if bytes_dom is not None:
+        avg_s = ms_dom * 1e-3 / args.steps
+        achieved = bytes_dom / avg_s / 1e9
+    else:
+        achieved = None
+    step_bytes = P * (420.0 + 56.0 * c_pair)
+    step_gbs = step_bytes / (el_ms * 1e-3 / args.steps) / 1e9
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "plain FP64 (bit-exact with the oracle)",
+                   "spheres": m.parnum, "triangles": m.trinum, "parallelism": f"replicas x{world}",
+                   "l2": "state ~0.6 GB per replica, larger than L2; no flush",
+                   "bed_solid_fraction": round(info["solid_fraction"], 3),
+                   "contacts_per_particle": round(c_pair, 3)},
+        "e2e": {"value": m.parnum * args.steps * world / e2e_s, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": up // args.steps, "d2h_bytes_per_step": down // args.steps,
+                "path": "Model.dem() through the pg_session C ABI: full host->device upload, K steps, "
+                        "device->host download (pageable host arrays)"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind,
+                     "step_algorithmic_gbs": step_gbs, "step_frac": step_gbs / hbm,
+                     "note": "FP64-ALU bound on GB300 (2 DFMA/clk/SM); see profiles/"},
+        "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in groups.items()},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(args.spheres, os.cpu_count() or 1)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -233,6 +233,22 @@ int pg_session_set_skin(pg_session *s, double skin);
  * bandwidth, off by default). */
 int pg_session_record_geometry(pg_session *s, int on);
 
+/* Time kernel groups with CUDA events on the session stream during
+ * pg_session_run (on != 0) and reset the accumulators.  Groups: 0 rebuild of
+ * candidate lists, 1 contacts, 2 springs, 3 integrate, 4 mesh nodes/faces,
+ * 5 obstacles and step tail. */
+int pg_session_profile(pg_session *s, int on);
+
+/* Accumulated milliseconds and kernel launches per group (8 entries each). */
+int pg_session_profile_read(pg_session *s, double *ms, long long *launches);
+
+/* Diagnostics (16 ints): [0..3] first device error (status, site, index,
+ * value; site 1 = candidate list, 3 = slave list, 4 = pairing kind),
+ * [4] rebuilds so far, [5] largest candidate count seen, [6] largest slave
+ * count, [7] largest triangle candidate count, [12..14] grid cells per axis,
+ * [15] Morton bits per axis. */
+int pg_session_diagnostics(pg_session *s, int *out16);
+
 /* Library version string. */
 const char *pg_version(void);
 

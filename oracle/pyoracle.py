@@ -19,8 +19,11 @@ _lib = None
 
 
 def build():
-    """Compile the oracle with make (g++, -ffp-contract=off, OpenMP)."""
-    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile the oracle (g++, -ffp-contract=off so no multiply-add is fused, OpenMP);
+    the same command as oracle/Makefile."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    subprocess.run(["g++", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-std=c++17",
+                    "-Wall", "-shared", "-o", LIB, os.path.join(HERE, "oracle.cpp")], check=True)
     return LIB
 
 

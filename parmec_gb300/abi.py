@@ -149,6 +149,9 @@ def load_library():
         "pg_session_kernel_launches": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_set_skin": (ctypes.c_int, [P, ctypes.c_double]),
         "pg_session_record_geometry": (ctypes.c_int, [P, ctypes.c_int]),
+        "pg_session_profile": (ctypes.c_int, [P, ctypes.c_int]),
+        "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
+        "pg_session_diagnostics": (ctypes.c_int, [P, I]),
         "pg_version": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -37,7 +37,16 @@ constexpr int TRI_TILE = 256;
 
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
-__device__ __forceinline__ void set_err(const PgDev &d, int code) { atomicCAS(d.err, 0, code); }
+// record the first error with where it happened (site), the index and a value
+__device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
+{
+  if (atomicCAS(d.err, 0, code) == 0)
+  {
+    d.err[1] = site;
+    d.err[2] = index;
+    d.err[3] = value;
+  }
+}
 
 __device__ __forceinline__ unsigned spread3(unsigned x)
 {
@@ -238,7 +247,7 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = i < E;
   int codes[MAXKN];
-  int n = 0, nsph = 0;
+  int n = 0, nsph = 0, nover = 0, ntri = 0;
   bool over = false;
   double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
   int pi = 0;
@@ -266,7 +275,7 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
             if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
             {
               if (n < d.kn) codes[n ++] = j;
-              else over = true;
+              else { over = true; nover ++; }
             }
           }
         }
@@ -302,14 +311,19 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
       int t = t0 + k;
       double A[3], B[3], C[3], pnt[3], nrm[3];
       for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
-      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+      // the candidate test uses the true closest point: the reference's region
+      // formula can only report a larger distance, so this set stays a superset
+      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, false);
       if (!(depth > -d.skin) && !(depth != depth)) continue;
+      ntri ++;
       if (n < d.kn) codes[n ++] = -(t + 1);
-      else over = true;
+      else { over = true; nover ++; }
     }
   }
   if (!live) return;
-  if (over) set_err(d, PG_ERR_CAPACITY);
+  if (over) set_err(d, PG_ERR_CAPACITY, 1, i, n + nover);
+  atomicMax(&d.stats[1], n + nover);
+  atomicMax(&d.stats[3], ntri);
 
   // merge with the previous list (both in partner order)
   const int nold = d.ncnt[i];
@@ -367,7 +381,7 @@ __global__ void k_rb_rfill(PgDev d)
     if (pj < 0) continue;
     int r = atomicAdd(&d.rcnt[pj], 1);
     if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
-    else set_err(d, PG_ERR_CAPACITY);
+    else set_err(d, PG_ERR_CAPACITY, 3, pj, r + 1);
   }
 }
 
@@ -378,6 +392,7 @@ __global__ void k_rb_rsort(PgDev d)
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   int n = d.rcnt[p];
+  atomicMax(&d.stats[2], n);
   if (n > d.kr) { n = d.kr; d.rcnt[p] = n; }
   unsigned long long key[MAXKN];
   int ref[MAXKN];
@@ -401,7 +416,11 @@ __global__ void k_rb_rsort(PgDev d)
 
 __global__ void k_rb_done(PgDev d)
 {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *d.rebuild = 0;
+  if (threadIdx.x == 0 && blockIdx.x == 0 && *d.rebuild)
+  {
+    *d.rebuild = 0;
+    d.stats[0] += 1;
+  }
 }
 
 int sort_passes(const PgDev &d)

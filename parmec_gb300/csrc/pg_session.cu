@@ -26,6 +26,12 @@ struct pg_session
   size_t ncells = 0;
   int prs_stride = 3, obs_stride = 3;
   std::vector<int> h_pell;
+  // per kernel group timing with CUDA events on the session stream
+  int profile = 0;
+  cudaEvent_t ev[8] = {};
+  double group_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long group_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<cudaEvent_t> ring;
 };
 
 namespace {
@@ -436,7 +442,8 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if ((r = allocate(s, sc)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.stepno, 1)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.rebuild, 1)) != PG_OK) goto fail;
-  if ((r = dalloc(s, &d.err, 1)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.err, 4)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.stats, 8)) != PG_OK) goto fail;
   if ((r = upload_static(s, sc)) != PG_OK) goto fail;
   if ((r = upload_all(s, sc)) != PG_OK) goto fail;
   if ((r = contact_buffers(s)) != PG_OK) goto fail;
@@ -468,6 +475,7 @@ int pg_session_destroy(pg_session *s)
   if (!s) return PG_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (void *p : s->allocs) cudaFree(p);
+  for (auto &e : s->ring) if (e) cudaEventDestroy(e);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return PG_OK;
@@ -550,15 +558,57 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
   CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
   const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d);
-  for (int k = 0; k < n; k ++)
+  if (!s->profile)
   {
-    pg_launch_rebuild(d, s->stream);
-    pg_launch_contacts(d, s->stream, step);
-    pg_launch_springs(d, s->stream, step);
-    pg_launch_integrate(d, s->stream, step);
-    pg_launch_mesh(d, s->stream);
-    pg_launch_obstacles_row(d, s->stream, step);
-    pg_launch_tail(d, s->stream, step);
+    for (int k = 0; k < n; k ++)
+    {
+      pg_launch_rebuild(d, s->stream);
+      pg_launch_contacts(d, s->stream, step);
+      pg_launch_springs(d, s->stream, step);
+      pg_launch_integrate(d, s->stream, step);
+      pg_launch_mesh(d, s->stream);
+      pg_launch_obstacles_row(d, s->stream, step);
+      pg_launch_tail(d, s->stream, step);
+    }
+  }
+  else
+  {
+    // groups: 0 rebuild, 1 contacts, 2 springs, 3 integrate, 4 mesh, 5 obstacles + tail
+    const int G = 6;
+    s->ring.resize((size_t)n * (G + 1));
+    for (auto &e : s->ring) if (!e) CK(cudaEventCreate(&e));
+    for (int k = 0; k < n; k ++)
+    {
+      cudaEvent_t *ev = &s->ring[(size_t)k * (G + 1)];
+      CK(cudaEventRecord(ev[0], s->stream));
+      pg_launch_rebuild(d, s->stream);
+      CK(cudaEventRecord(ev[1], s->stream));
+      pg_launch_contacts(d, s->stream, step);
+      CK(cudaEventRecord(ev[2], s->stream));
+      pg_launch_springs(d, s->stream, step);
+      CK(cudaEventRecord(ev[3], s->stream));
+      pg_launch_integrate(d, s->stream, step);
+      CK(cudaEventRecord(ev[4], s->stream));
+      pg_launch_mesh(d, s->stream);
+      CK(cudaEventRecord(ev[5], s->stream));
+      pg_launch_obstacles_row(d, s->stream, step);
+      pg_launch_tail(d, s->stream, step);
+      CK(cudaEventRecord(ev[6], s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    const int counts[6] = {pg_rebuild_kernel_count(d), d.ellnum ? 1 : 0, d.sprnum ? 1 : 0, d.parnum ? 1 : 0,
+                           (d.nodnum ? 1 : 0) + (d.facnum ? 1 : 0), 1 + ((d.obsnum && d.trinum) ? 1 : 0)};
+    for (int k = 0; k < n; k ++)
+    {
+      cudaEvent_t *ev = &s->ring[(size_t)k * (G + 1)];
+      for (int g = 0; g < G; g ++)
+      {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, ev[g], ev[g + 1]));
+        s->group_ms[g] += ms;
+        s->group_launches[g] += counts[g];
+      }
+    }
   }
   s->launches += (long long)per_step * n;
   CK(cudaGetLastError());
@@ -685,6 +735,38 @@ int pg_session_stream(pg_session *s, void **stream)
 {
   if (!s || !stream) return PG_ERR_ARGUMENT;
   *stream = (void *)s->stream;
+  return PG_OK;
+}
+
+int pg_session_profile(pg_session *s, int on)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  s->profile = on ? 1 : 0;
+  for (int g = 0; g < 8; g ++) { s->group_ms[g] = 0.0; s->group_launches[g] = 0; }
+  return PG_OK;
+}
+
+int pg_session_profile_read(pg_session *s, double *ms, long long *launches)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  for (int g = 0; g < 8; g ++)
+  {
+    if (ms) ms[g] = s->group_ms[g];
+    if (launches) launches[g] = s->group_launches[g];
+  }
+  return PG_OK;
+}
+
+int pg_session_diagnostics(pg_session *s, int *out16)
+{
+  if (!s || !out16) return PG_ERR_ARGUMENT;
+  int e[4], st[8];
+  TRY(d2h(s, e, s->d.err, 4));
+  TRY(d2h(s, st, s->d.stats, 8));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int k = 0; k < 4; k ++) out16[k] = e[k];
+  for (int k = 0; k < 8; k ++) out16[4 + k] = st[k];
+  out16[12] = s->d.dim[0]; out16[13] = s->d.dim[1]; out16[14] = s->d.dim[2]; out16[15] = s->d.bits;
   return PG_OK;
 }
 

@@ -83,7 +83,8 @@ struct PgDev
 
   // ---- rebuild machinery
   int *rebuild;             // 1 when the candidate lists must be rebuilt
-  int *err;                 // first device error (PG_ERR_*), 0 when fine
+  int *err;                 // [4]: first device error (PG_ERR_*), site, index, value; 0 when fine
+  int *stats;               // [8]: rebuilds, max candidates, max slave entries, max triangles per sphere
   double skin, cell, half_skin_sq;
   double org[3];
   int dim[3], bits;

@@ -25,7 +25,16 @@ constexpr int TPB = 128;
 
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
-__device__ __forceinline__ void set_err(const PgDev &d, int code) { atomicCAS(d.err, 0, code); }
+// record the first error with where it happened (site), the index and a value
+__device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
+{
+  if (atomicCAS(d.err, 0, code) == 0)
+  {
+    d.err[1] = site;
+    d.err[2] = index;
+    d.err[3] = value;
+  }
+}
 
 __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
 {
@@ -336,7 +345,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       vij[2] = vj[2] - vi[2];
 
       const int ij = pairing(d, coli, colj);
-      if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED);
+      if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED, 4, i, ij);
 
       // granular force (forces.ispc:125-192)
       double state[3];

@@ -69,6 +69,28 @@ class GpuEngine:
         abi.check(self.lib.pg_session_kernel_launches(self.sess, ctypes.byref(n)), "kernel_launches")
         return n.value
 
+    def profile(self, on=True):
+        abi.check(self.lib.pg_session_profile(self.sess, 1 if on else 0), "pg_session_profile")
+
+    def profile_read(self):
+        ms = (ctypes.c_double * 8)()
+        n = (ctypes.c_longlong * 8)()
+        abi.check(self.lib.pg_session_profile_read(self.sess, ms, n), "pg_session_profile_read")
+        names = ["rebuild", "contacts", "springs", "integrate", "mesh", "obstacles"]
+        return {names[g]: (ms[g], n[g]) for g in range(6)}
+
+    def diagnostics(self):
+        out = (ctypes.c_int * 16)()
+        abi.check(self.lib.pg_session_diagnostics(self.sess, out), "pg_session_diagnostics")
+        v = list(out)
+        return {"error": v[0:4], "rebuilds": v[4], "max_candidates": v[5], "max_slave": v[6],
+                "max_triangles": v[7], "grid": v[12:15], "bits": v[15]}
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        abi.check(self.lib.pg_session_stream(self.sess, ctypes.byref(p)), "pg_session_stream")
+        return p.value
+
     def contacts(self):
         """Active contacts in canonical order as a dict of numpy arrays."""
         n = ctypes.c_int()

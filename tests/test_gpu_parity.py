@@ -76,3 +76,19 @@ def test_repeatable(gpu_lib):
         m.dem(60 * dt, dt, interval=1e9, engine=GpuEngine())
         out.append(m)
     assert_bitwise(out[0], out[1])
+
+
+def test_state_edit_between_dem_calls(gpu_lib, oracle_lib):
+    """VELOCITY between two DEM calls: the host edit is uploaded, contacts persist."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.engine import GpuEngine
+    out = []
+    for eng in (GpuEngine(record_geometry=True), OracleEngine()):
+        m, dt = make_collision_scene(n_side=5, seed=21)
+        m.dem(40 * dt, dt, interval=1e9, engine=eng)
+        for i in range(0, m.parnum, 7):
+            m.velocity(i, linear=(0.2, -0.1, 0.3), angular=(1.0, 0.0, -2.0))
+        m.dem(40 * dt, dt, interval=1e9, engine=eng)
+        out.append((m, eng))
+    assert_bitwise(out[0][0], out[1][0])
+    assert_contacts_equal(out[0][1].contacts(), out[1][1].contacts())
