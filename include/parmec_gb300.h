@@ -249,6 +249,22 @@ int pg_session_profile_read(pg_session *s, double *ms, long long *launches);
  * [15] Morton bits per axis. */
 int pg_session_diagnostics(pg_session *s, int *out16);
 
+/* ======================================================================== */
+/* (3) Building blocks on caller-owned device memory                         */
+/* ======================================================================== */
+
+/* Morton-ordered cell list of n sphere centres (device arrays x, y, z):
+ * replaces partitioning_create (partition.ispc:663).  Cells of size 'cell'
+ * from 'origin' with dim[k] cells per axis (1..1024; positions outside are
+ * clamped to the border cells).  Writes, to device arrays of n entries, the
+ * Morton key of every sphere's cell in ascending order (keys_out) and the
+ * sphere indices in that order (order_out; stable, so equal keys keep index
+ * order).  Enqueued on 'stream' (a cudaStream_t, or NULL); scratch memory is
+ * taken with cudaMallocAsync and released on the same stream. */
+int pg_cell_order(const double *x, const double *y, const double *z, int n,
+                  const double origin[3], double cell, const int dim[3],
+                  unsigned *keys_out, int *order_out, void *stream);
+
 /* Library version string. */
 const char *pg_version(void);
 

@@ -11,7 +11,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["pg_step.cu", "pg_rebuild.cu", "pg_session.cu"]
+SOURCES = ["pg_step.cu", "pg_rebuild.cu", "pg_sort.cu", "pg_partition.cu", "pg_session.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

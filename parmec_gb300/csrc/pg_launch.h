@@ -16,6 +16,15 @@ void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     /
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
 int  pg_step_kernel_count(const PgDev &d);
 
+// pg_sort.cu
+int  pg_sort_blocks(int n);
+int  pg_sort_passes(int bits_per_axis);
+void pg_launch_cell_keys(const double *x, const double *y, const double *z, int n, const double org[3],
+                         double cell, const int dim[3], unsigned *keys, int *vals,
+                         double *rx, double *ry, double *rz, const int *gate, cudaStream_t s);
+void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned *hist, int n, int passes,
+                          const int *gate, cudaStream_t s);
+
 // pg_rebuild.cu
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
 int  pg_rebuild_kernel_count(const PgDev &d);

@@ -5,8 +5,8 @@
 // condet.ispc:98-516).  Here candidate lists are rebuilt only when a sphere
 // or triangle vertex has moved more than 0.45*skin since the last rebuild:
 //
-//   1. Morton key of each sphere's cell (cell >= 2*rmax + skin)
-//   2. stable LSD radix sort of (key, sphere) pairs, 8-bit digits
+//   1. Morton key of each sphere's cell (cell >= 2*rmax + skin)   [pg_sort.cu]
+//   2. stable LSD radix sort of (key, sphere) pairs, 8-bit digits  [pg_sort.cu]
 //   3. cell start/end ranges over the sorted keys
 //   4. per sphere: the spheres of the 27 neighbouring cells and the triangles
 //      within r + skin (the master side only: partner particle index larger),
@@ -29,9 +29,6 @@
 namespace {
 
 constexpr int TPB = 128;
-constexpr int SORT_THREADS = 256;
-constexpr int SORT_ITEMS = 8;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // keys per block per pass
 constexpr int MAXKN = 96;                               // upper bound of slots per sphere
 constexpr int TRI_TILE = 256;
 
@@ -85,20 +82,6 @@ __global__ void k_rb_clear(PgDev d)
   d.cend[key] = 0;
 }
 
-// ---- 1. keys, reference centres
-__global__ void k_rb_keys(PgDev d)
-{
-  if (!*d.rebuild) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ellnum) return;
-  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
-  int u[3];
-  cell_of(d, c, u);
-  d.keys[0][i] = morton(u[0], u[1], u[2]);
-  d.vals[0][i] = i;
-  d.cref[0][i] = c[0]; d.cref[1][i] = c[1]; d.cref[2][i] = c[2];
-}
-
 // ---- triangle reference vertices and widened float AABBs
 __global__ void k_rb_tref(PgDev d)
 {
@@ -112,112 +95,6 @@ __global__ void k_rb_tref(PgDev d)
     double hi = fmax(fmax(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
     d.tbox[(size_t)c * d.trinum + t] = __double2float_rd(lo);
     d.tbox[(size_t)(3+c) * d.trinum + t] = __double2float_ru(hi);
-  }
-}
-
-// ---- 2. radix sort: per-block digit histograms
-__global__ void __launch_bounds__(SORT_THREADS) k_rb_hist(PgDev d, int src, int shift)
-{
-  if (!*d.rebuild) return;
-  __shared__ unsigned h[256];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  const int n = d.ellnum;
-  const int base = blockIdx.x * SORT_TILE;
-  for (int it = 0; it < SORT_ITEMS; it ++)
-  {
-    int s = base + it * SORT_THREADS + threadIdx.x;
-    if (s < n) atomicAdd(&h[(d.keys[src][s] >> shift) & 255u], 1u);
-  }
-  __syncthreads();
-  d.hist[threadIdx.x * d.nsortblocks + blockIdx.x] = h[threadIdx.x];
-}
-
-// exclusive scan of hist[digit][block] (digit-major), one block
-__global__ void __launch_bounds__(1024) k_rb_scan(PgDev d)
-{
-  if (!*d.rebuild) return;
-  __shared__ unsigned part[1024];
-  const int total = 256 * d.nsortblocks;
-  const int per = (total + 1023) / 1024;
-  const int b = threadIdx.x * per;
-  const int e = min(b + per, total);
-  unsigned sum = 0;
-  for (int k = b; k < e; k ++) sum += d.hist[k];
-  part[threadIdx.x] = sum;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1)
-  {
-    unsigned v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
-  }
-  unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-  for (int k = b; k < e; k ++)
-  {
-    unsigned v = d.hist[k];
-    d.hist[k] = run;
-    run += v;
-  }
-}
-
-// stable scatter: each warp ranks its contiguous sub-tile round by round
-__global__ void __launch_bounds__(SORT_THREADS) k_rb_scatter(PgDev d, int src, int shift)
-{
-  if (!*d.rebuild) return;
-  constexpr int WARPS = SORT_THREADS / 32;
-  constexpr int SUB = SORT_TILE / WARPS;              // keys per warp
-  __shared__ unsigned wcnt[WARPS][256];
-  __shared__ unsigned goff[256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int k = threadIdx.x; k < WARPS * 256; k += SORT_THREADS) (&wcnt[0][0])[k] = 0;
-  goff[threadIdx.x] = d.hist[threadIdx.x * d.nsortblocks + blockIdx.x];
-  __syncthreads();
-
-  const int n = d.ellnum;
-  const int base = blockIdx.x * SORT_TILE + warp * SUB;
-  unsigned keyv[SUB / 32];
-  int valv[SUB / 32];
-  unsigned rank[SUB / 32];
-  const unsigned lt = (1u << lane) - 1u;
-  for (int r = 0; r < SUB / 32; r ++)
-  {
-    int s = base + r * 32 + lane;
-    bool ok = s < n;
-    unsigned key = ok ? d.keys[src][s] : 0xffffffffu;
-    int val = ok ? d.vals[src][s] : -1;
-    unsigned dig = ok ? (key >> shift) & 255u : 256u;      // 256: padding, never written
-    unsigned peers = __match_any_sync(0xffffffffu, dig);
-    unsigned before = __popc(peers & lt);
-    unsigned prev = ok ? wcnt[warp][dig] : 0u;
-    __syncwarp();
-    if (ok && before == 0) wcnt[warp][dig] = prev + __popc(peers);
-    __syncwarp();
-    keyv[r] = key;
-    valv[r] = val;
-    rank[r] = prev + before;
-  }
-  __syncthreads();
-  // exclusive prefix over warps for every digit
-  {
-    unsigned run = 0;
-    for (int w = 0; w < WARPS; w ++)
-    {
-      unsigned c = wcnt[w][threadIdx.x];
-      wcnt[w][threadIdx.x] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-  const int dst = src ^ 1;
-  for (int r = 0; r < SUB / 32; r ++)
-  {
-    if (valv[r] < 0) continue;
-    unsigned dig = (keyv[r] >> shift) & 255u;
-    unsigned pos = goff[dig] + wcnt[warp][dig] + rank[r];
-    d.keys[dst][pos] = keyv[r];
-    d.vals[dst][pos] = valv[r];
   }
 }
 
@@ -423,14 +300,6 @@ __global__ void k_rb_done(PgDev d)
   }
 }
 
-int sort_passes(const PgDev &d)
-{
-  int bits = 3 * d.bits;
-  int p = (bits + 7) / 8;
-  if (p & 1) p ++;             // even, so the result lands in buffer 0
-  return p;
-}
-
 } // namespace
 
 void pg_rebuild_grid_params(PgDev &d, const double *lo, const double *hi, double rmax, double rmin)
@@ -462,16 +331,10 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
   const int E = d.ellnum;
   if (!E) return;
   k_rb_clear<<<nblk(E), TPB, 0, s>>>(d);
-  k_rb_keys<<<nblk(E), TPB, 0, s>>>(d);
+  pg_launch_cell_keys(d.center[0], d.center[1], d.center[2], E, d.org, d.cell, d.dim, d.keys[0], d.vals[0],
+                      d.cref[0], d.cref[1], d.cref[2], d.rebuild, s);
   if (d.trinum) k_rb_tref<<<nblk(d.trinum), TPB, 0, s>>>(d);
-  const int passes = sort_passes(d);
-  for (int p = 0; p < passes; p ++)
-  {
-    int src = p & 1;
-    k_rb_hist<<<d.nsortblocks, SORT_THREADS, 0, s>>>(d, src, 8 * p);
-    k_rb_scan<<<1, 1024, 0, s>>>(d);
-    k_rb_scatter<<<d.nsortblocks, SORT_THREADS, 0, s>>>(d, src, 8 * p);
-  }
+  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes(d.bits), d.rebuild, s);
   k_rb_ranges<<<nblk(E), TPB, 0, s>>>(d);
   k_rb_verlet<<<nblk(E), TPB, 0, s>>>(d);
   k_rb_rzero<<<nblk(d.parnum), TPB, 0, s>>>(d);
@@ -483,5 +346,5 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 int pg_rebuild_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
-  return 2 + (d.trinum ? 1 : 0) + 3 * sort_passes(d) + 6;
+  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes(d.bits) + 6;
 }

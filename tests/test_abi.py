@@ -1,0 +1,74 @@
+"""The C ABI: ctypes mirrors match the header's layout, and the library
+exports every function include/parmec_gb300.h declares (CPU only: nothing is
+computed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "parmec_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(pg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_session_api():
+    names = declared_functions()
+    for n in ("pg_session_create", "pg_session_run", "pg_session_download", "pg_cell_order", "pg_version"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    import __graft_entry__
+    __graft_entry__.build()
+    from parmec_gb300 import abi
+    lib = abi.load_library()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.library_path()], capture_output=True, text=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    assert not [n for n in declared_functions() if n not in exported]
+    assert lib.pg_version().decode().startswith("parmec_gb300")
+
+
+def c_layout(tmp_path):
+    src = tmp_path / "layout.c"
+    fields = ["parnum", "angular", "mass", "ellnum", "center", "trinum", "tri", "obsnum", "obslin", "pairnum",
+              "iparam", "nodnum", "facnum", "factri", "sprnum", "sprpnt", "lcidx", "prsnum", "angkind", "compat"]
+    body = "".join(f'  printf("{f} %zu\\n", offsetof(pg_scene, {f}));\n' for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "parmec_gb300.h"\nint main(void){\n'
+                   '  printf("size %zu\\n", sizeof(pg_scene));\n  printf("tabsize %zu\\n", sizeof(pg_steptab));\n'
+                   + body + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    return {l.split()[0]: int(l.split()[1]) for l in out.splitlines()}
+
+
+def test_ctypes_scene_layout_matches_c(tmp_path):
+    from parmec_gb300 import abi
+    lay = c_layout(tmp_path)
+    assert lay["size"] == ctypes.sizeof(abi.PgScene)
+    assert lay["tabsize"] == ctypes.sizeof(abi.PgStepTab)
+    for name, off in lay.items():
+        if name in ("size", "tabsize"):
+            continue
+        assert getattr(abi.PgScene, name).offset == off, name
+
+
+def test_session_create_without_gpu_fails_loudly():
+    """No CPU fallback: without a device the session cannot be created."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import hopper_fill
+    m, dt = hopper_fill(n_side=2)
+    with pytest.raises(RuntimeError):
+        m.dem(dt, dt, engine=GpuEngine())
