@@ -265,6 +265,20 @@ int pg_cell_order(const double *x, const double *y, const double *z, int n,
                   const double origin[3], double cell, const int dim[3],
                   unsigned *keys_out, int *order_out, void *stream);
 
+/* pg_cell_order without any device allocation (no counterpart in the
+ * reference).  For callers that cannot allocate device memory -- coupling
+ * codes whose own pool owns the device memory, and hosts that cannot afford
+ * the device synchronisation cudaMalloc/cudaFree may cause.  Scratch lives in
+ * a static device array of the library, sized for at most 65,536 spheres
+ * (about 0.55 MB, held by every GPU that loads the library until exit);
+ * larger n returns PG_ERR_CAPACITY.  Calls share that array: calls that
+ * overlap on the GPU race.  The first call on a device sets up the array's
+ * address and should come before any stream capture.  Same arguments and
+ * results as pg_cell_order. */
+int pg_cell_order_static(const double *x, const double *y, const double *z, int n,
+                         const double origin[3], double cell, const int dim[3],
+                         unsigned *keys_out, int *order_out, void *stream);
+
 /* Library version string. */
 const char *pg_version(void);
 

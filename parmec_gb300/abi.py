@@ -153,6 +153,7 @@ def load_library():
         "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_diagnostics": (ctypes.c_int, [P, I]),
         "pg_cell_order": (ctypes.c_int, [P, P, P, ctypes.c_int, D, ctypes.c_double, I, P, P, P]),
+        "pg_cell_order_static": (ctypes.c_int, [P, P, P, ctypes.c_int, D, ctypes.c_double, I, P, P, P]),
         "pg_version": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -7,6 +7,7 @@
 // with a stable LSD radix sort; sorted cell keys give each cell's range of
 // spheres (a cell list).
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdio>
 #include "pg_launch.h"
 #include "../../include/parmec_gb300.h"
@@ -60,6 +61,95 @@ extern "C" int pg_cell_order(const double *x, const double *y, const double *z, 
   if (e != cudaSuccess)
   {
     std::fprintf(stderr, "parmec_gb300: pg_cell_order: %s\n", cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pg_cell_order_static: the same ordering, with no device allocation.
+//
+// Some callers of this library cannot allocate device memory: coupling codes
+// that give the whole device to their own memory pool (so a cudaMalloc here
+// would fail or fragment it), and hosts that must not let cudaMalloc/cudaFree
+// synchronise the device while their other streams run.  This entry point
+// takes its scratch from a file-scope __device__ array instead.  That array is
+// part of the library image: every GPU that loads the library holds its
+// PG_CELL_ORDER_STATIC_MAX-sized scratch (about 0.55 MB) until the process
+// exits.  Every call on a device shares the one array, so calls that overlap
+// on the GPU (from different streams or threads) race and must not be made.
+// Nothing in the array needs to start at zero: each sort pass writes every
+// histogram entry and every key before it reads them.  The first call on a
+// device looks up the array's device address (cudaGetSymbolAddress); make
+// that first call before any stream capture on the device.
+// ---------------------------------------------------------------------------
+
+#define PG_CELL_ORDER_STATIC_MAX 65536
+#define PG_CELL_ORDER_STATIC_BLOCKS ((PG_CELL_ORDER_STATIC_MAX + 2047) / 2048)
+
+namespace {
+
+constexpr size_t STATIC_KEYS_OFF = 0;
+constexpr size_t STATIC_VALS_OFF = STATIC_KEYS_OFF + sizeof(unsigned) * PG_CELL_ORDER_STATIC_MAX;
+constexpr size_t STATIC_HIST_OFF = STATIC_VALS_OFF + sizeof(int) * PG_CELL_ORDER_STATIC_MAX;
+constexpr size_t STATIC_BYTES = STATIC_HIST_OFF + sizeof(unsigned) * 256 * PG_CELL_ORDER_STATIC_BLOCKS;
+
+__device__ __align__(256) unsigned char g_cell_order_scratch[STATIC_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+std::atomic<unsigned char *> g_scratch_addr[MAX_DEVICES];
+
+// The host-side name g_cell_order_scratch is not a device address; ask the
+// runtime for the device address once per device, with that device current.
+int scratch_address(unsigned char **out)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return PG_ERR_CUDA;
+  unsigned char *p = g_scratch_addr[dev].load();
+  if (!p)
+  {
+    void *q = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&q, g_cell_order_scratch);
+    if (e != cudaSuccess || !q)
+    {
+      std::fprintf(stderr, "parmec_gb300: pg_cell_order_static: cudaGetSymbolAddress failed: %s\n",
+                   cudaGetErrorString(e));
+      return PG_ERR_CUDA;
+    }
+    p = (unsigned char *)q;
+    g_scratch_addr[dev].store(p);
+  }
+  *out = p;
+  return PG_OK;
+}
+
+} // namespace
+
+extern "C" int pg_cell_order_static(const double *x, const double *y, const double *z, int n,
+                                    const double origin[3], double cell, const int dim[3],
+                                    unsigned *keys_out, int *order_out, void *stream)
+{
+  if (!valid(x, y, z, n, origin, cell, dim, keys_out, order_out)) return PG_ERR_ARGUMENT;
+  if (n > PG_CELL_ORDER_STATIC_MAX)
+  {
+    std::fprintf(stderr, "parmec_gb300: pg_cell_order_static: n = %d exceeds the static scratch limit of %d "
+                         "spheres; use pg_cell_order\n", n, PG_CELL_ORDER_STATIC_MAX);
+    return PG_ERR_CAPACITY;
+  }
+  if (n == 0) return PG_OK;
+  unsigned char *base = nullptr;
+  int r = scratch_address(&base);
+  if (r != PG_OK) return r;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned *k1 = (unsigned *)(base + STATIC_KEYS_OFF);
+  int *v1 = (int *)(base + STATIC_VALS_OFF);
+  unsigned *hist = (unsigned *)(base + STATIC_HIST_OFF);
+  pg_launch_cell_keys(x, y, z, n, origin, cell, dim, keys_out, order_out, nullptr, nullptr, nullptr, nullptr, s);
+  pg_launch_radix_sort(keys_out, order_out, k1, v1, hist, n, pg_sort_passes(bits_for(dim)), nullptr, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+  {
+    std::fprintf(stderr, "parmec_gb300: pg_cell_order_static: %s\n", cudaGetErrorString(e));
     return PG_ERR_CUDA;
   }
   return PG_OK;
