@@ -208,18 +208,15 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    eng.profile(True)
     launches0 = eng.kernel_launches()
     clocks.start()
     ev0.record(stream)
-    eng.run(ctab, dt)
+    eng.run(ctab, dt)                       # K steps, one captured CUDA graph per step
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = eng.kernel_launches() - launches0
-    prof = eng.profile_read()
-    eng.profile(False)
     m.curtime = end_time
     el_ms = ev0.elapsed_time(ev1)
     if dist:
@@ -227,6 +224,16 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         el_ms = float(t.item())
         dist.barrier()
+    # the same K steps again with CUDA events around every kernel group, for the
+    # per-kernel durations behind the roofline
+    times2, end2 = driver.step_times(m.curtime, args.steps * dt - 0.5 * dt, dt)
+    tabs2 = driver.StepTables(m, times2, dt, [1e9, 1e9], [None, None], [-1, -1])
+    eng.profile(True)
+    eng.run(tabs2.ctab(0, len(times2)), dt)
+    torch.cuda.synchronize()
+    prof = eng.profile_read()
+    eng.profile(False)
+    m.curtime = end2
     eng.download()
     contacts = eng.contacts()
     nc = len(contacts["mpart"])
@@ -263,14 +270,16 @@ def main():
     groups = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(groups, key=lambda k: groups[k][0])
     P = m.parnum
-    cand = None
     per_launch = {
         "integrate": P * (696.0 + 53.0 * c_pair),
         "contacts": P * (172.0 + 96.0 * c_pair),
     }
     ms_dom, n_dom = groups[dom]
-    launches_dom = max(1, n_dom)
     bytes_dom = per_launch.get(dom)
+    # DRAM bytes per launch: ncu capture of the 262,144-sphere case
+    # (profiles/k_integrate_k_contacts_drum_fp64.md) scaled by the units processed
+    traffic_per_unit = {"integrate": 611.0, "contacts": 188.0}
+    traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     if bytes_dom is not None:
         avg_s = ms_dom * 1e-3 / args.steps
         achieved = bytes_dom / avg_s / 1e9
@@ -294,7 +303,8 @@ def main():
                         "device->host download (pageable host arrays)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None,
+                     "traffic": traffic, "traffic_source": "ncu 262,144-sphere capture scaled per unit",
                      "peak_source": peak_kind,
                      "step_algorithmic_gbs": step_gbs, "step_frac": step_gbs / hbm,
                      "note": "FP64-ALU bound on GB300 (2 DFMA/clk/SM); see profiles/"},

@@ -233,6 +233,10 @@ int pg_session_set_skin(pg_session *s, double skin);
  * bandwidth, off by default). */
 int pg_session_record_geometry(pg_session *s, int on);
 
+/* Run steps as one captured CUDA graph per step (on, the default) or as
+ * individual stream launches (off).  Results are identical. */
+int pg_session_use_graph(pg_session *s, int on);
+
 /* Time kernel groups with CUDA events on the session stream during
  * pg_session_run (on != 0) and reset the accumulators.  Groups: 0 rebuild of
  * candidate lists, 1 contacts, 2 springs, 3 integrate, 4 mesh nodes/faces,

@@ -150,6 +150,7 @@ def load_library():
         "pg_session_set_skin": (ctypes.c_int, [P, ctypes.c_double]),
         "pg_session_record_geometry": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_profile": (ctypes.c_int, [P, ctypes.c_int]),
+        "pg_session_use_graph": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_diagnostics": (ctypes.c_int, [P, I]),
         "pg_cell_order": (ctypes.c_int, [P, P, P, ctypes.c_int, D, ctypes.c_double, I, P, P, P]),

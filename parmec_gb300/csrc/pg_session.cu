@@ -32,6 +32,11 @@ struct pg_session
   double group_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   long long group_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   std::vector<cudaEvent_t> ring;
+  // one captured step (re-captured when kernel arguments change)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  double graph_step = 0.0;
+  int use_graph = 1;
 };
 
 namespace {
@@ -69,6 +74,8 @@ int d2h(pg_session *s, T *dst, const T *src, size_t n)
 }
 
 #define TRY(x) do { int r_ = (x); if (r_ != PG_OK) return r_; } while (0)
+
+void drop_graph(pg_session *s);
 
 int table_len(const int *idx, int n) { return n > 0 && idx ? idx[n] : 0; }
 
@@ -325,6 +332,7 @@ int ensure_tables(pg_session *s, int n)
   PgDev &d = s->d;
   if (n <= s->tab_cap) return PG_OK;
   int cap = std::max(n, 2 * s->tab_cap);
+  drop_graph(s);
   double **arrs[7] = {&d.t_curtime, &d.t_gravity, &d.t_damping, &d.t_prs_lin, &d.t_prs_ang, &d.t_obs_ang, &d.t_obs_lin};
   size_t widths[7] = {1, 3, 6, (size_t)s->prs_stride, (size_t)s->prs_stride, (size_t)s->obs_stride, (size_t)s->obs_stride};
   for (int k = 0; k < 7; k ++)
@@ -380,6 +388,7 @@ int contact_buffers(pg_session *s)
 int grid_buffers(pg_session *s)
 {
   PgDev &d = s->d;
+  drop_graph(s);
   pg_rebuild_grid_params(d, s->lo, s->hi, s->rmax, s->rmin);
   size_t cells = (size_t)1 << (3 * d.bits);
   if (cells != s->ncells)
@@ -403,6 +412,40 @@ int grid_buffers(pg_session *s)
   if (d.keys[0]) CK(cudaMemsetAsync(d.keys[0], 0, (size_t)std::max(1, d.ellnum) * sizeof(unsigned), s->stream));
   int one = 1;
   TRY(h2d(s, d.rebuild, &one, 1));
+  return PG_OK;
+}
+
+void drop_graph(pg_session *s)
+{
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->graph_exec = nullptr;
+  s->graph = nullptr;
+}
+
+void enqueue_step(pg_session *s, double step)
+{
+  const PgDev &d = s->d;
+  pg_launch_rebuild(d, s->stream);
+  pg_launch_contacts(d, s->stream, step);
+  pg_launch_springs(d, s->stream, step);
+  pg_launch_integrate(d, s->stream, step);
+  pg_launch_mesh(d, s->stream);
+  pg_launch_obstacles_row(d, s->stream, step);
+  pg_launch_tail(d, s->stream, step);
+}
+
+// capture one step into a CUDA graph (kernel arguments are baked in: the
+// graph is re-captured when a buffer is reallocated or the step changes)
+int capture_step(pg_session *s, double step)
+{
+  if (s->graph_exec && s->graph_step == step) return PG_OK;
+  drop_graph(s);
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(s, step);
+  CK(cudaStreamEndCapture(s->stream, &s->graph));
+  CK(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
+  s->graph_step = step;
   return PG_OK;
 }
 
@@ -474,6 +517,7 @@ int pg_session_destroy(pg_session *s)
 {
   if (!s) return PG_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
+  drop_graph(s);
   for (void *p : s->allocs) cudaFree(p);
   for (auto &e : s->ring) if (e) cudaEventDestroy(e);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -492,6 +536,7 @@ int pg_session_record_geometry(pg_session *s, int on)
 {
   if (!s) return PG_ERR_ARGUMENT;
   s->d.record_geometry = on ? 1 : 0;
+  drop_graph(s);
   return PG_OK;
 }
 
@@ -501,6 +546,7 @@ int pg_session_upload(pg_session *s, const pg_scene *sc)
   if (sc->parnum != s->d.parnum || sc->ellnum != s->d.ellnum || sc->trinum != s->d.trinum ||
       sc->sprnum != s->d.sprnum || sc->obsnum != s->d.obsnum || sc->prsnum != s->d.prsnum)
     return PG_ERR_ARGUMENT;
+  if (s->d.compat != sc->compat) drop_graph(s);
   s->d.compat = sc->compat;
   TRY(upload_all(s, sc));
   CK(cudaStreamSynchronize(s->stream));
@@ -558,18 +604,14 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
   CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
   const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d);
-  if (!s->profile)
+  if (!s->profile && s->use_graph)
   {
-    for (int k = 0; k < n; k ++)
-    {
-      pg_launch_rebuild(d, s->stream);
-      pg_launch_contacts(d, s->stream, step);
-      pg_launch_springs(d, s->stream, step);
-      pg_launch_integrate(d, s->stream, step);
-      pg_launch_mesh(d, s->stream);
-      pg_launch_obstacles_row(d, s->stream, step);
-      pg_launch_tail(d, s->stream, step);
-    }
+    TRY(capture_step(s, step));
+    for (int k = 0; k < n; k ++) CK(cudaGraphLaunch(s->graph_exec, s->stream));
+  }
+  else if (!s->profile)
+  {
+    for (int k = 0; k < n; k ++) enqueue_step(s, step);
   }
   else
   {
@@ -735,6 +777,13 @@ int pg_session_stream(pg_session *s, void **stream)
 {
   if (!s || !stream) return PG_ERR_ARGUMENT;
   *stream = (void *)s->stream;
+  return PG_OK;
+}
+
+int pg_session_use_graph(pg_session *s, int on)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  s->use_graph = on ? 1 : 0;
   return PG_OK;
 }
 

@@ -14,8 +14,9 @@ def _counts(m):
 class GpuEngine:
     """Runs DEM steps of one Model in a pg_session on the current CUDA device."""
 
-    def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False):
+    def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False, graph=True):
         self.lib = abi.load_library()
+        self.graph = graph
         self.form = form
         self.skin = skin
         self.record_geometry = record_geometry
@@ -37,6 +38,8 @@ class GpuEngine:
             abi.check(self.lib.pg_session_set_skin(self.sess, float(self.skin)), "pg_session_set_skin")
         if self.record_geometry:
             abi.check(self.lib.pg_session_record_geometry(self.sess, 1), "pg_session_record_geometry")
+        if not self.graph:
+            abi.check(self.lib.pg_session_use_graph(self.sess, 0), "pg_session_use_graph")
 
     def stale(self):
         return self.model is None or _counts(self.model) != self.counts

@@ -92,3 +92,14 @@ def test_state_edit_between_dem_calls(gpu_lib, oracle_lib):
         out.append((m, eng))
     assert_bitwise(out[0][0], out[1][0])
     assert_contacts_equal(out[0][1].contacts(), out[1][1].contacts())
+
+
+def test_graph_and_stream_launches_identical(gpu_lib):
+    """A captured CUDA graph per step gives the same bits as stream launches."""
+    from parmec_gb300.engine import GpuEngine
+    out = []
+    for graph in (True, False):
+        m, dt = make_collision_scene(n_side=5, seed=31, moving=True)
+        m.dem(80 * dt, dt, interval=1e9, engine=GpuEngine(graph=graph))
+        out.append(m)
+    assert_bitwise(out[0], out[1])
