@@ -126,6 +126,49 @@ def cpu_baseline(n_spheres, threads, steps=3):
                       f"{el:.1f} s"}
 
 
+def mixed_form(args, ref64):
+    """The mixed-precision form on the same drum: W warm-up and K timed steps,
+    then its state against the FP64 form's after the same W + K steps."""
+    import torch
+    from parmec_gb300 import abi, driver, energy
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import drum
+    m, dt, _ = drum(args.spheres)
+    eng = GpuEngine(form=abi.PG_FORM_MIXED)
+    eng.attach(m)
+    m.engine = eng
+    m._dirty = False
+    m.dem(args.warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    times, end_time = driver.step_times(m.curtime, args.steps * dt - 0.5 * dt, dt)
+    tabs = driver.StepTables(m, times, dt, [1e9, 1e9], [None, None], [-1, -1])
+    ctab = tabs.ctab(0, len(times))
+    stream = torch.cuda.ExternalStream(eng.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    eng.run(ctab, dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    el_ms = ev0.elapsed_time(ev1)
+    m.curtime = end_time
+    eng.download()
+    n = m.parnum
+    dx = float(np.max(np.abs(m.P.position[0:3, :n] - ref64["x"])))
+    fmax = float(np.max(np.abs(ref64["f"])))
+    df = float(np.max(np.abs(m.P.force[:, :n] - ref64["f"]))) / fmax
+    E = energy.total(m)
+    out = {"form": "mixed: FP32 contact geometry and forces, compensated FP32 pairs for x, v, L, radii and gaps",
+           "value": n * args.steps / (el_ms * 1e-3), "unit": "particle-steps/s",
+           "ms_per_step": el_ms / args.steps,
+           "errors_vs_fp64": {"steps": args.warmup + args.steps, "position_max_abs_m": dx,
+                              "force_max_abs_rel_to_max": df,
+                              "energy_rel": abs(E - ref64["E"]) / abs(ref64["E"]),
+                              "kinetic_energy_rel": abs(energy.kinetic(m) - ref64["K"]) / abs(ref64["K"]),
+                              "energy_definition": "kinetic + rotational + gravity potential (parmec_gb300/energy.py)"}}
+    eng.close()
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU restatement on all host cores, rank 0 only."""
     if rank != 0:
@@ -224,6 +267,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         el_ms = float(t.item())
         dist.barrier()
+    # FP64 reference state after W + K steps, for the mixed form's error report
+    eng.download()
+    ref64 = {"x": m.P.position[0:3, :m.parnum].copy(), "f": m.P.force[:, :m.parnum].copy()}
+    from parmec_gb300 import energy as _energy
+    ref64["E"] = _energy.total(m)
+    ref64["K"] = _energy.kinetic(m)
     # the same K steps again with CUDA events around every kernel group, for the
     # per-kernel durations behind the roofline
     times2, end2 = driver.step_times(m.curtime, args.steps * dt - 0.5 * dt, dt)
@@ -311,6 +360,8 @@ def main():
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in groups.items()},
         "clocks": clk,
     }
+    line["mixed"] = mixed_form(args, ref64)
+    line["mixed"]["speedup_vs_plain"] = line["mixed"]["value"] / (value / world)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(args.spheres, os.cpu_count() or 1)
     print(json.dumps(line))

@@ -11,7 +11,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["pg_step.cu", "pg_rebuild.cu", "pg_sort.cu", "pg_partition.cu", "pg_session.cu"]
+SOURCES = ["pg_step.cu", "pg_rebuild.cu", "pg_sort.cu", "pg_partition.cu", "pg_mixed.cu", "pg_session.cu"]
+# the FP64 form must not contract multiply-adds (bit parity with the oracle);
+# the mixed form is FP32 arithmetic with explicit error-free transformations
+FMAD = {"pg_mixed.cu": "true"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -24,7 +27,7 @@ def nvcc():
 
 def build(verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-div=true", "--prec-sqrt=true",
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--prec-div=true", "--prec-sqrt=true",
                     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"] + list(extra)
     if verbose:
         flags += ["-Xptxas", "-v"]
@@ -32,7 +35,7 @@ def build(verbose=False, extra=()):
     for src in SOURCES:
         obj = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmd = [nvcc()] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc()] + flags + ["-fmad=" + FMAD.get(src, "false"), "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     failed = False
     for src, p in procs:

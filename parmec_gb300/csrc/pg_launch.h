@@ -16,6 +16,13 @@ void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     /
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
 int  pg_step_kernel_count(const PgDev &d);
 
+// pg_mixed.cu
+void pg_launch_mx_from64(const PgDev &d, cudaStream_t s);
+void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s);
+void pg_launch_mx_to64(const PgDev &d, cudaStream_t s);
+void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step);
+void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step);
+
 // pg_sort.cu
 int  pg_sort_blocks(int n);
 int  pg_sort_passes(int bits_per_axis);

@@ -1,0 +1,496 @@
+// pg_mixed.cu -- the mixed-precision step (PG_FORM_MIXED).
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, so this form keeps everything on
+// the FP32 pipe:
+//   * positions, linear velocities, rotations and sphere radii are compensated
+//     FP32 pairs (pg_df.cuh, ~48 significant bits), so that positions are
+//     accumulated with FP64-class accuracy and the near-touching gap
+//     r_i + r_j - |x_i - x_j| is evaluated without cancellation;
+//   * contact normals, velocities, forces, torques, tangential state and the
+//     angular dynamics run in FP32.
+// Sums keep the FP64 form's order (master list, then slave list), so results
+// are reproducible run to run.  The FP64 arrays of the session remain the
+// interchange format: uploads convert FP64 -> pairs (k_mx_from64), downloads
+// convert back (k_mx_to64).  Scope: sphere particles whose sphere centre is the
+// particle's reference point (SPHERE), triangles of obstacles, analytical
+// particles; no springs or meshes.
+#include <cuda_runtime.h>
+#include "pg_state.h"
+#include "pg_math.cuh"
+#include "pg_df.cuh"
+#include "pg_launch.h"
+#include "../../include/parmec_gb300.h"
+
+using namespace pg;
+
+namespace {
+
+constexpr int TPB = 128;
+inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+
+__device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
+{
+  if (atomicCAS(d.err, 0, code) == 0) { d.err[1] = site; d.err[2] = index; d.err[3] = value; }
+}
+
+__device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
+{
+  unsigned m = __ballot_sync(__activemask(), need);
+  if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
+}
+
+// FP32 expmap: the FP64 form's expression tree in single precision
+__device__ __forceinline__ void expmap_f(float O1, float O2, float O3, float *L, bool typo)
+{
+  float v0 = O1 * O1, v1 = O2 * O2, v2 = O3 * O3;
+  float angsq = v0 + v1 + v2, sx, cx;
+  if (angsq < 3.0461741978671E-02f)
+  {
+    sx = 1.0f + (-1.666666666666667E-1f + (8.333333333333333E-3f + (-1.984126984126984E-4f +
+         (2.755731922398589E-6f + (-2.505210838544172E-8f + 1.605904383682161E-10f * angsq) * angsq) * angsq)
+         * angsq) * angsq) * angsq;
+    cx = 0.5f + (-4.166666666666667E-2f + (1.388888888888889E-3f + (-2.480158730158730E-5f +
+         (2.755731922398589E-7f + (-2.087675698786810E-9f + 1.147074559772972E-11f * angsq) * angsq) * angsq)
+         * angsq) * angsq) * angsq;
+  }
+  else
+  {
+    float t = angsq, a = sqrtf(angsq), s, c;
+    sincosf(a, &s, &c);
+    sx = s / a;
+    cx = (1.0f - c) / t;
+  }
+  float v01 = O1 * O2, v02 = typo ? O2 * O3 : O1 * O3, v12 = O2 * O3;
+  float s0 = sx * O1, s1 = sx * O2, s2 = sx * O3;
+  L[0] = 1.0f - cx*(v2+v1); L[1] = cx*v01 + s2;  L[2] = cx*v02 - s1;
+  L[3] = cx*v01 - s2;       L[4] = 1.0f - cx*(v2+v0); L[5] = cx*v12 + s0;
+  L[6] = cx*v02 + s1;       L[7] = cx*v12 - s0;  L[8] = 1.0f - cx*(v1+v0);
+}
+
+__device__ __forceinline__ void nvmul_f(const float *A, const float *B, float *C)
+{
+  C[0] = A[0]*B[0]+A[3]*B[1]+A[6]*B[2];
+  C[1] = A[1]*B[0]+A[4]*B[1]+A[7]*B[2];
+  C[2] = A[2]*B[0]+A[5]*B[1]+A[8]*B[2];
+}
+
+__device__ __forceinline__ void tvmul_f(const float *A, const float *B, float *C)
+{
+  C[0] = A[0]*B[0]+A[1]*B[1]+A[2]*B[2];
+  C[1] = A[3]*B[0]+A[4]*B[1]+A[5]*B[2];
+  C[2] = A[6]*B[0]+A[7]*B[1]+A[8]*B[2];
+}
+
+__device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
+{
+  int p0 = i, p1 = j, start = 1, end = d.pairnum;
+  if (i > j) { p0 = j; p1 = i; }
+  while (start < end)
+  {
+    int mid = ((end-start)>>1) + start;
+    int a = d.pairs[2*mid], b = d.pairs[2*mid+1];
+    if (p0 > a) { if (start == mid) break; start = mid; }
+    else if (p0 == a)
+    {
+      if (p1 > b) { if (start == mid) break; start = mid; }
+      else if (p1 == b) return mid;
+      else end = mid;
+    }
+    else end = mid;
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------ conversions
+__global__ void k_mx_from64(PgDev d)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.parnum)
+  {
+    for (int k = 0; k < 3; k ++)
+    {
+      df x = df_from(d.position[k][i]); d.xh[k][i] = x.hi; d.xl[k][i] = x.lo;
+      df v = df_from(d.linear[k][i]); d.vh[k][i] = v.hi; d.vl[k][i] = v.lo;
+      d.Om[k][i] = (float)d.angular[k][i];
+      d.om[k][i] = (float)d.angular[3+k][i];
+      d.F_f[k][i] = (float)d.force[k][i];
+      d.T_f[k][i] = (float)d.torque[k][i];
+    }
+    for (int k = 0; k < 9; k ++)
+    {
+      df l = df_from(d.rotation[k][i]); d.Lh[k][i] = l.hi; d.Ll[k][i] = l.lo;
+      d.J_f[k][i] = (float)d.inertia[k][i];
+      d.I_f[k][i] = (float)d.inverse[k][i];
+    }
+    d.mass_f[i] = (float)d.mass[i];
+    d.invm_f[i] = (float)d.invm[i];
+  }
+  if (i < d.ellnum)
+  {
+    df r = df_from(d.radii[0][i]);
+    d.rh[i] = r.hi; d.rl[i] = r.lo;
+  }
+}
+
+__global__ void k_mx_inertia(PgDev d)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.parnum) return;
+  for (int k = 0; k < 9; k ++) { d.J_f[k][i] = (float)d.inertia[k][i]; d.I_f[k][i] = (float)d.inverse[k][i]; }
+  d.mass_f[i] = (float)d.mass[i];
+  d.invm_f[i] = (float)d.invm[i];
+}
+
+__global__ void k_mx_to64(PgDev d)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.parnum) return;
+  for (int k = 0; k < 3; k ++)
+  {
+    d.position[k][i] = df_to({d.xh[k][i], d.xl[k][i]});
+    d.linear[k][i] = df_to({d.vh[k][i], d.vl[k][i]});
+    d.angular[k][i] = (double)d.Om[k][i];
+    d.angular[3+k][i] = (double)d.om[k][i];
+    d.force[k][i] = (double)d.F_f[k][i];
+    d.torque[k][i] = (double)d.T_f[k][i];
+  }
+  for (int k = 0; k < 9; k ++) d.rotation[k][i] = df_to({d.Lh[k][i], d.Ll[k][i]});
+  int e = d.pell[i];
+  if (e >= 0) for (int k = 0; k < 3; k ++) d.center[k][e] = d.position[k][i];
+}
+
+// ------------------------------------------------------------ contacts
+__global__ void __launch_bounds__(TPB) k_contacts_mx(PgDev d, double step_d)
+{
+  const int E = d.ellnum;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const int pi = d.part[i];
+  const int cnt = d.ncnt[i];
+  float fs[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
+  if (cnt > 0)
+  {
+    const float step = (float)step_d;
+    const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
+    const bool etypo = (d.compat & PG_COMPAT_TRIEDGE) != 0;
+    df x[3];
+    float v[3], oi[3];
+    for (int k = 0; k < 3; k ++)
+    {
+      x[k] = {d.xh[k][pi], d.xl[k][pi]};
+      v[k] = d.vh[k][pi];
+      oi[k] = d.om[k][pi];
+    }
+    const df ri = {d.rh[i], d.rl[i]};
+    const int coli = d.ellcol[i];
+    const float invmi = d.invm_f[pi], massi = d.mass_f[pi];
+    for (int k = 0; k < cnt; k ++)
+    {
+      const size_t idx = (size_t)k * E + i;
+      const int code = d.ncode[idx];
+      const bool existing = d.nflag[idx] != 0;
+      float normal[3], armi[3], armj[3] = {0.0f, 0.0f, 0.0f}, depth;
+      bool pos, neg;
+      int pj, colj;
+      double pnt[3] = {0.0, 0.0, 0.0};
+      if (code >= 0)
+      {
+        const int j = code;
+        pj = d.part[j];
+        colj = d.ellcol[j];
+        df q[3];
+        for (int c = 0; c < 3; c ++) q[c] = df_sub(x[c], {d.xh[c][pj], d.xl[c][pj]});
+        df d2 = df_add(df_add(df_mul(q[0], q[0]), df_mul(q[1], q[1])), df_mul(q[2], q[2]));
+        df len = df_sqrt(d2);
+        df dep = df_sub(df_add(ri, {d.rh[j], d.rl[j]}), len);
+        depth = df_f(dep);
+        pos = df_pos(dep);
+        neg = df_neg_(dep);
+        float qf[3] = {df_f(q[0]), df_f(q[1]), df_f(q[2])};
+        float lenf = df_f(len);
+        float ilen = existing ? 1.0f / lenf : (lenf > 0.0f ? 1.0f / lenf : 1.0f);
+        for (int c = 0; c < 3; c ++)
+        {
+          normal[c] = ilen * qf[c];
+          armi[c] = -0.5f * qf[c];
+          armj[c] = 0.5f * qf[c];
+        }
+      }
+      else
+      {
+        const int t = -code-1;
+        double A[3], B[3], C[3], cd[3], nd[3];
+        for (int c = 0; c < 3; c ++)
+        {
+          A[c] = d.tri[c][t]; B[c] = d.tri[3+c][t]; C[c] = d.tri[6+c][t];
+          cd[c] = df_to(x[c]);
+        }
+        double dd = triangle_sphere(A, B, C, cd, df_to(ri), pnt, nd, etypo);
+        depth = (float)dd;
+        pos = dd > 0.0;
+        neg = dd < 0.0;
+        for (int c = 0; c < 3; c ++) { normal[c] = (float)nd[c]; armi[c] = (float)(pnt[c] - cd[c]); }
+        pj = d.triobs[t];
+        colj = d.tricol[t];
+      }
+      const bool active = existing ? !neg : pos;
+      if (!active)
+      {
+        if (existing)
+        {
+          d.nflag[idx] = 0;
+          d.nstate_f[0][idx] = 0.0f; d.nstate_f[1][idx] = 0.0f; d.nstate_f[2][idx] = 0.0f;
+        }
+        continue;
+      }
+      float vi[3], vj[3], vij[3];
+      vi[0] = oi[1]*armi[2]-oi[2]*armi[1] + v[0];
+      vi[1] = oi[2]*armi[0]-oi[0]*armi[2] + v[1];
+      vi[2] = oi[0]*armi[1]-oi[1]*armi[0] + v[2];
+      if (pj >= 0)
+      {
+        float oj[3] = {d.om[0][pj], d.om[1][pj], d.om[2][pj]};
+        vj[0] = oj[1]*armj[2]-oj[2]*armj[1] + d.vh[0][pj];
+        vj[1] = oj[2]*armj[0]-oj[0]*armj[2] + d.vh[1][pj];
+        vj[2] = oj[0]*armj[1]-oj[1]*armj[0] + d.vh[2][pj];
+      }
+      else
+      {
+        int l = -pj-2;
+        if (obsc && l >= 0) l = l+1;
+        if (l >= 0 && l < d.obsnum)
+        {
+          float z[3], oj[3];
+          for (int c = 0; c < 3; c ++)
+          {
+            z[c] = (float)(pnt[c] - d.obspnt[3*l+c]);
+            oj[c] = (float)d.obsang[3*l+c];
+          }
+          vj[0] = oj[1]*z[2]-oj[2]*z[1] + (float)d.obslin[3*l];
+          vj[1] = oj[2]*z[0]-oj[0]*z[2] + (float)d.obslin[3*l+1];
+          vj[2] = oj[0]*z[1]-oj[1]*z[0] + (float)d.obslin[3*l+2];
+        }
+        else { vj[0] = vj[1] = vj[2] = 0.0f; }
+      }
+      for (int c = 0; c < 3; c ++) vij[c] = vj[c] - vi[c];
+      const int ij = pairing(d, coli, colj);
+      if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED, 4, i, ij);
+      float state[3];
+      if (existing) { state[0] = d.nstate_f[0][idx]; state[1] = d.nstate_f[1][idx]; state[2] = d.nstate_f[2][idx]; }
+      else { state[0] = state[1] = state[2] = 0.0f; }
+      float ma = pj >= 0 ? 1.0f / (invmi + d.invm_f[pj]) : massi;
+      float kn = (float)d.iparam[0][ij];
+      float en = (float)d.iparam[1][ij] * 2.0f * sqrtf(kn*ma);
+      float vn = vij[0]*normal[0] + vij[1]*normal[1] + vij[2]*normal[2];
+      float fn = kn*depth + en*vn;
+      float kskn = (float)d.iparam[6][ij];
+      float kt = kn * kskn, et = en * kskn;
+      float mus = (float)d.iparam[2][ij], mud = (float)d.iparam[3][ij];
+      float f[3], vt[3], ft[3];
+      for (int c = 0; c < 3; c ++)
+      {
+        f[c] = fn*normal[c];
+        vt[c] = vij[c] - vn*normal[c];
+        state[c] += step*vt[c];
+        ft[c] = kt*state[c] + et*vt[c];
+      }
+      float flen = sqrtf(ft[0]*ft[0] + ft[1]*ft[1] + ft[2]*ft[2]);
+      float lim = mus*fn;
+      if (flen > lim)
+      {
+        lim = mud*fn/flen;
+        ft[0] *= lim; ft[1] *= lim; ft[2] *= lim;
+      }
+      for (int c = 0; c < 3; c ++) f[c] += ft[c];
+      d.nflag[idx] = 1;
+      for (int c = 0; c < 3; c ++)
+      {
+        d.nstate_f[c][idx] = state[c];
+        d.nfrc_f[c][idx] = f[c];
+        d.narm_f[c][idx] = armj[c];
+      }
+      fs[0] += f[0]; fs[1] += f[1]; fs[2] += f[2];
+      ts[0] += armi[1]*f[2] - armi[2]*f[1];
+      ts[1] += armi[2]*f[0] - armi[0]*f[2];
+      ts[2] += armi[0]*f[1] - armi[1]*f[0];
+    }
+  }
+  for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
+}
+
+// ------------------------------------------------------------ integrate
+__global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < d.parnum)
+  {
+    const int row = *d.stepno;
+    const double *grav = d.t_gravity + 3*(size_t)row;
+    const double *damping = d.t_damping + 6*(size_t)row;
+    const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+    const float step = (float)step_d;
+    const int e = d.pell[i];
+    float F[3] = {0.0f, 0.0f, 0.0f}, T[3] = {0.0f, 0.0f, 0.0f};
+    if (e >= 0) for (int c = 0; c < 3; c ++) { F[c] = d.fm_f[c][i]; T[c] = d.tm_f[c][i]; }
+    if (d.ellnum)
+    {
+      const int nr = d.rcnt[i];
+      for (int r = 0; r < nr; r ++)
+      {
+        const int ref = d.rref[(size_t)r * d.parnum + i];
+        if (!d.nflag[ref]) continue;
+        float f[3] = {-d.nfrc_f[0][ref], -d.nfrc_f[1][ref], -d.nfrc_f[2][ref]};
+        float a[3] = {d.narm_f[0][ref], d.narm_f[1][ref], d.narm_f[2][ref]};
+        F[0] += f[0]; F[1] += f[1]; F[2] += f[2];
+        T[0] += a[1]*f[2] - a[2]*f[1];
+        T[1] += a[2]*f[0] - a[0]*f[2];
+        T[2] += a[0]*f[1] - a[1]*f[0];
+      }
+    }
+    const float ma = d.mass_f[i];
+    for (int c = 0; c < 3; c ++) F[c] = F[c] + ma * (float)grav[c];
+
+    const int pb = d.prsnum ? d.prs_first[i] : 0, pe = d.prsnum ? d.prs_first[i+1] : 0;
+    for (int pp = pb; pp < pe; pp ++)
+    {
+      const int q = d.prs_list[pp];
+      const double *lin = d.t_prs_lin + (size_t)row * d.tab_prs_stride + 3*q;
+      const double *ang = d.t_prs_ang + (size_t)row * d.tab_prs_stride + 3*q;
+      if (d.prslin[q] && d.linkind[q] == 1) for (int c = 0; c < 3; c ++) F[c] = ma * (float)lin[c];
+      else if (d.prslin[q] && d.linkind[q] == 0) F[0] = F[1] = F[2] = 0.0f;
+      if (d.prsang[q] && d.angkind[q] == 1)
+      {
+        float in[9], acc[3] = {(float)ang[0], (float)ang[1], (float)ang[2]};
+        for (int k = 0; k < 9; k ++) in[k] = d.J_f[k][i];
+        nvmul_f(in, acc, T);
+      }
+      else if (d.prsang[q] && d.angkind[q] == 0) T[0] = T[1] = T[2] = 0.0f;
+    }
+
+    df x[3], v[3], L[9];
+    float O[3], o[3], Lf[9], J[9], I[9];
+    for (int c = 0; c < 3; c ++)
+    {
+      x[c] = {d.xh[c][i], d.xl[c][i]};
+      v[c] = {d.vh[c][i], d.vl[c][i]};
+      O[c] = d.Om[c][i];
+      o[c] = d.om[c][i];
+    }
+    for (int k = 0; k < 9; k ++)
+    {
+      L[k] = {d.Lh[k][i], d.Ll[k][i]};
+      Lf[k] = L[k].hi;
+      J[k] = d.J_f[k][i];
+      I[k] = d.I_f[k][i];
+    }
+    if (!(d.flags[i] & PG_FLAG_SKIP))
+    {
+      const float half = 0.5f * step, hstep = step;
+      if (damping[0] != 0.0 || damping[1] != 0.0 || damping[2] != 0.0)
+        for (int c = 0; c < 3; c ++) F[c] -= ma * (float)damping[c] * v[c].hi;
+      if (damping[3] != 0.0 || damping[4] != 0.0 || damping[5] != 0.0)
+      {
+        float w[3], t[3], Tb[3];
+        for (int c = 0; c < 3; c ++) w[c] = (float)damping[3+c] * o[c];
+        tvmul_f(Lf, w, t);
+        nvmul_f(J, t, Tb);
+        nvmul_f(Lf, Tb, t);
+        for (int c = 0; c < 3; c ++) T[c] -= t[c];
+      }
+      float Tb[3], DL[9], A[3], B[3];
+      tvmul_f(Lf, T, Tb);
+      expmap_f(-half*O[0], -half*O[1], -half*O[2], DL, typo);
+      nvmul_f(J, O, A);
+      nvmul_f(DL, A, B);
+      for (int c = 0; c < 3; c ++) B[c] = B[c] + half*Tb[c];
+      nvmul_f(I, B, A);
+      nvmul_f(J, A, B);
+      Tb[0] -= A[1]*B[2] - A[2]*B[1];
+      Tb[1] -= A[2]*B[0] - A[0]*B[2];
+      Tb[2] -= A[0]*B[1] - A[1]*B[0];
+      for (int c = 0; c < 3; c ++) Tb[c] *= step;
+      float IT[3];
+      nvmul_f(I, Tb, IT);
+      for (int c = 0; c < 3; c ++) O[c] = O[c] + IT[c];
+      const float im = d.invm_f[i] * step;
+      for (int c = 0; c < 3; c ++) v[c] = df_add_f(v[c], im * F[c]);
+      expmap_f(hstep*O[0], hstep*O[1], hstep*O[2], DL, typo);
+      df L2[9];
+      for (int col = 0; col < 3; col ++)
+        for (int row3 = 0; row3 < 3; row3 ++)
+        {
+          df acc = df_mul_f(L[row3], DL[3*col]);
+          acc = df_add(acc, df_mul_f(L[3+row3], DL[3*col+1]));
+          acc = df_add(acc, df_mul_f(L[6+row3], DL[3*col+2]));
+          L2[3*col+row3] = acc;
+        }
+      for (int k = 0; k < 9; k ++) { L[k] = L2[k]; Lf[k] = L2[k].hi; }
+      nvmul_f(Lf, O, o);
+      for (int c = 0; c < 3; c ++) x[c] = df_add(x[c], df_mul_f(v[c], hstep));
+      for (int pp = pb; pp < pe; pp ++)
+      {
+        const int q = d.prs_list[pp];
+        const double *lin = d.t_prs_lin + (size_t)row * d.tab_prs_stride + 3*q;
+        const double *ang = d.t_prs_ang + (size_t)row * d.tab_prs_stride + 3*q;
+        if (d.prslin[q] && d.linkind[q] == 0) for (int c = 0; c < 3; c ++) v[c] = df_from(lin[c]);
+        if (d.prsang[q] && d.angkind[q] == 0)
+        {
+          float oo[3] = {(float)ang[0], (float)ang[1], (float)ang[2]};
+          tvmul_f(Lf, oo, O);
+          o[0] = oo[0]; o[1] = oo[1]; o[2] = oo[2];
+        }
+      }
+      for (int c = 0; c < 3; c ++)
+      {
+        d.xh[c][i] = x[c].hi; d.xl[c][i] = x[c].lo;
+        d.vh[c][i] = v[c].hi; d.vl[c][i] = v[c].lo;
+        d.Om[c][i] = O[c];
+        d.om[c][i] = o[c];
+      }
+      for (int k = 0; k < 9; k ++) { d.Lh[k][i] = L[k].hi; d.Ll[k][i] = L[k].lo; }
+    }
+    for (int c = 0; c < 3; c ++) { d.F_f[c][i] = F[c]; d.T_f[c][i] = T[c]; }
+    if (e >= 0)
+    {
+      float dd = 0.0f;
+      for (int c = 0; c < 3; c ++)
+      {
+        double cc = df_to(x[c]);
+        d.center[c][e] = cc;
+        float r = (float)(cc - d.cref[c][e]);
+        dd += r*r;
+      }
+      need = dd > (float)d.half_skin_sq;
+    }
+  }
+  if (d.ellnum) flag_rebuild(d, need);
+}
+
+} // namespace
+
+void pg_launch_mx_from64(const PgDev &d, cudaStream_t s)
+{
+  int n = d.parnum > d.ellnum ? d.parnum : d.ellnum;
+  if (n) k_mx_from64<<<nblk(n), TPB, 0, s>>>(d);
+}
+
+void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_mx_inertia<<<nblk(d.parnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_mx_to64(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_mx_to64<<<nblk(d.parnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.ellnum) k_contacts_mx<<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.parnum) k_integrate_mx<<<nblk(d.parnum), TPB, 0, s>>>(d, step);
+}

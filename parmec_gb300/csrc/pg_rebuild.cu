@@ -207,12 +207,15 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
   int ocode[MAXKN];
   unsigned char oflag[MAXKN];
   double ost[3][MAXKN];
+  // the tangential state lives in the FP64 arrays (FP64 form) or the FP32
+  // arrays (mixed form); it moves with its contact either way
+  const bool mixed = d.form == PG_FORM_MIXED;
   for (int k = 0; k < nold; k ++)
   {
     size_t idx = (size_t)k * E + i;
     ocode[k] = d.ncode[idx];
     oflag[k] = d.nflag[idx];
-    ost[0][k] = d.nstate[0][idx]; ost[1][k] = d.nstate[1][idx]; ost[2][k] = d.nstate[2][idx];
+    for (int c = 0; c < 3; c ++) ost[c][k] = mixed ? (double)d.nstate_f[c][idx] : d.nstate[c][idx];
   }
   int o = 0;
   for (int k = 0; k < n; k ++)
@@ -221,15 +224,13 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
     while (o < nold && order_key(ocode[o]) < key) o ++;
     size_t idx = (size_t)k * E + i;
     d.ncode[idx] = codes[k];
-    if (o < nold && ocode[o] == codes[k])
+    const bool kept = o < nold && ocode[o] == codes[k];
+    d.nflag[idx] = kept ? oflag[o] : 0;
+    for (int c = 0; c < 3; c ++)
     {
-      d.nflag[idx] = oflag[o];
-      d.nstate[0][idx] = ost[0][o]; d.nstate[1][idx] = ost[1][o]; d.nstate[2][idx] = ost[2][o];
-    }
-    else
-    {
-      d.nflag[idx] = 0;
-      d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+      double st = kept ? ost[c][o] : 0.0;
+      if (mixed) d.nstate_f[c][idx] = (float)st;
+      else d.nstate[c][idx] = st;
     }
   }
   d.ncnt[i] = n;

@@ -385,6 +385,30 @@ int contact_buffers(pg_session *s)
   return PG_OK;
 }
 
+int mixed_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  const size_t P = d.parnum, E = d.ellnum;
+  const size_t slots = (size_t)d.kn * std::max<size_t>(E, 1);
+  for (int k = 0; k < 3; k ++)
+  {
+    TRY(dalloc(s, &d.xh[k], P)); TRY(dalloc(s, &d.xl[k], P));
+    TRY(dalloc(s, &d.vh[k], P)); TRY(dalloc(s, &d.vl[k], P));
+    TRY(dalloc(s, &d.Om[k], P)); TRY(dalloc(s, &d.om[k], P));
+    TRY(dalloc(s, &d.F_f[k], P)); TRY(dalloc(s, &d.T_f[k], P));
+    TRY(dalloc(s, &d.fm_f[k], P)); TRY(dalloc(s, &d.tm_f[k], P));
+    TRY(dalloc(s, &d.nstate_f[k], slots)); TRY(dalloc(s, &d.nfrc_f[k], slots)); TRY(dalloc(s, &d.narm_f[k], slots));
+  }
+  for (int k = 0; k < 9; k ++)
+  {
+    TRY(dalloc(s, &d.Lh[k], P)); TRY(dalloc(s, &d.Ll[k], P));
+    TRY(dalloc(s, &d.J_f[k], P)); TRY(dalloc(s, &d.I_f[k], P));
+  }
+  TRY(dalloc(s, &d.mass_f, P)); TRY(dalloc(s, &d.invm_f, P));
+  TRY(dalloc(s, &d.rh, E)); TRY(dalloc(s, &d.rl, E));
+  return PG_OK;
+}
+
 int grid_buffers(pg_session *s)
 {
   PgDev &d = s->d;
@@ -427,6 +451,14 @@ void enqueue_step(pg_session *s, double step)
 {
   const PgDev &d = s->d;
   pg_launch_rebuild(d, s->stream);
+  if (d.form == PG_FORM_MIXED)
+  {
+    pg_launch_contacts_mx(d, s->stream, step);
+    pg_launch_integrate_mx(d, s->stream, step);
+    pg_launch_obstacles_row(d, s->stream, step);
+    pg_launch_tail(d, s->stream, step);
+    return;
+  }
   pg_launch_contacts(d, s->stream, step);
   pg_launch_springs(d, s->stream, step);
   pg_launch_integrate(d, s->stream, step);
@@ -466,7 +498,18 @@ const char *pg_version(void) { return "parmec_gb300 0.1.0 (sm_103a)"; }
 int pg_session_create(const pg_scene *sc, int form, pg_session **out)
 {
   if (!sc || !out || sc->parnum < 0 || sc->ellnum < 0) return PG_ERR_ARGUMENT;
-  if (form != PG_FORM_FP64) return PG_ERR_UNSUPPORTED;
+  if (form != PG_FORM_FP64 && form != PG_FORM_MIXED) return PG_ERR_ARGUMENT;
+  if (form == PG_FORM_MIXED)
+  {
+    // scope of the mixed form: spheres centred on their particle, obstacles, analytical particles
+    if (sc->sprnum || sc->nodnum || sc->facnum) return PG_ERR_UNSUPPORTED;
+    for (int e = 0; e < sc->ellnum; e ++)
+    {
+      int p = sc->part[e];
+      for (int k = 0; k < 3; k ++)
+        if (sc->center[3+k][e] != sc->position[3+k][p]) return PG_ERR_UNSUPPORTED;
+    }
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PG_ERR_CUDA;
   pg_session *s = new pg_session();
@@ -490,6 +533,11 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if ((r = upload_static(s, sc)) != PG_OK) goto fail;
   if ((r = upload_all(s, sc)) != PG_OK) goto fail;
   if ((r = contact_buffers(s)) != PG_OK) goto fail;
+  if (form == PG_FORM_MIXED)
+  {
+    if ((r = mixed_buffers(s)) != PG_OK) goto fail;
+    pg_launch_mx_from64(d, s->stream);
+  }
   for (int k = 0; k < 3; k ++) { s->lo[k] = 1e300; s->hi[k] = -1e300; }
   s->rmax = 0.0; s->rmin = 1e300;
   for (int e = 0; e < sc->ellnum; e ++)
@@ -549,6 +597,7 @@ int pg_session_upload(pg_session *s, const pg_scene *sc)
   if (s->d.compat != sc->compat) drop_graph(s);
   s->d.compat = sc->compat;
   TRY(upload_all(s, sc));
+  if (s->d.form == PG_FORM_MIXED) pg_launch_mx_from64(s->d, s->stream);
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
@@ -558,6 +607,7 @@ int pg_session_invert_inertia(pg_session *s)
   if (!s) return PG_ERR_ARGUMENT;
   pg_launch_invert(s->d, s->stream);
   s->launches += 1;
+  if (s->d.form == PG_FORM_MIXED) { pg_launch_mx_inertia(s->d, s->stream); s->launches += 1; }
   CK(cudaGetLastError());
   return PG_OK;
 }
@@ -566,6 +616,7 @@ int pg_session_first_half_step(pg_session *s, double step, const double *obs_ang
 {
   if (!s) return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream);
   pg_launch_euler(d, s->stream, 0.5 * step);
   pg_launch_shapes(d, s->stream, false);
   if (d.obsnum)
@@ -575,6 +626,7 @@ int pg_session_first_half_step(pg_session *s, double step, const double *obs_ang
   }
   pg_launch_obstacles_state(d, s->stream, step);
   s->launches += 5;
+  if (d.form == PG_FORM_MIXED) { pg_launch_mx_from64(d, s->stream); s->launches += 2; }
   CK(cudaGetLastError());
   return PG_OK;
 }
@@ -625,11 +677,13 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       CK(cudaEventRecord(ev[0], s->stream));
       pg_launch_rebuild(d, s->stream);
       CK(cudaEventRecord(ev[1], s->stream));
-      pg_launch_contacts(d, s->stream, step);
+      if (d.form == PG_FORM_MIXED) pg_launch_contacts_mx(d, s->stream, step);
+      else pg_launch_contacts(d, s->stream, step);
       CK(cudaEventRecord(ev[2], s->stream));
-      pg_launch_springs(d, s->stream, step);
+      if (d.form != PG_FORM_MIXED) pg_launch_springs(d, s->stream, step);
       CK(cudaEventRecord(ev[3], s->stream));
-      pg_launch_integrate(d, s->stream, step);
+      if (d.form == PG_FORM_MIXED) pg_launch_integrate_mx(d, s->stream, step);
+      else pg_launch_integrate(d, s->stream, step);
       CK(cudaEventRecord(ev[4], s->stream));
       pg_launch_mesh(d, s->stream);
       CK(cudaEventRecord(ev[5], s->stream));
@@ -672,6 +726,7 @@ int pg_session_download(pg_session *s, pg_scene *sc)
   if (!s || !sc) return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
   const size_t P = d.parnum, E = d.ellnum, T = d.trinum, O = d.obsnum, N = d.nodnum, S = d.sprnum;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream);
   for (int k = 0; k < 6; k ++) TRY(d2h(s, sc->angular[k], d.angular[k], P));
   for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->linear[k], d.linear[k], P));
   for (int k = 0; k < 9; k ++) TRY(d2h(s, sc->rotation[k], d.rotation[k], P));
@@ -739,6 +794,15 @@ int pg_session_contacts(pg_session *s, int cap, int *count, int *master_particle
   for (int k = 0; k < 3; k ++)
   {
     st[k].resize(slots); fr[k].resize(slots); pt[k].resize(slots); nr[k].resize(slots);
+    if (d.form == PG_FORM_MIXED)
+    {
+      std::vector<float> a(slots), b(slots);
+      TRY(d2h(s, a.data(), d.nstate_f[k], slots));
+      TRY(d2h(s, b.data(), d.nfrc_f[k], slots));
+      CK(cudaStreamSynchronize(s->stream));
+      for (size_t q = 0; q < slots; q ++) { st[k][q] = a[q]; fr[k][q] = b[q]; pt[k][q] = nr[k][q] = NAN; }
+      continue;
+    }
     TRY(d2h(s, st[k].data(), d.nstate[k], slots));
     TRY(d2h(s, fr[k].data(), d.nfrc[k], slots));
     TRY(d2h(s, pt[k].data(), d.npnt[k], slots));

@@ -98,4 +98,14 @@ struct PgDev
   int *ncnt_new;            // scratch candidate lists of a rebuild
   int *ncode_new;
   float *tbox;              // [6][trinum] triangle AABBs at rebuild (float, widened)
+
+  // ---- mixed form (PG_FORM_MIXED): compensated FP32 pairs for positions,
+  // linear velocities, rotations and radii; FP32 for everything else
+  float *xh[3], *xl[3], *vh[3], *vl[3], *Lh[9], *Ll[9];
+  float *Om[3], *om[3];     // referential and spatial angular velocity
+  float *rh, *rl;           // sphere radius pairs
+  float *mass_f, *invm_f, *J_f[9], *I_f[9];
+  float *F_f[3], *T_f[3];
+  float *nstate_f[3], *nfrc_f[3], *narm_f[3];   // per candidate entry; arm = point - slave position
+  float *fm_f[3], *tm_f[3];
 };
