@@ -169,6 +169,46 @@ def mixed_form(args, ref64):
     return out
 
 
+def batched_form(args, scenes):
+    """Config 3: 512 shaken boxes (sphere counts log-uniform in [2048, 65536])
+    stepped together in one session, mixed form against the plain FP64 form on
+    the same GPU.  One step = one time step of every scene."""
+    import torch
+    from parmec_gb300 import abi, batch, driver
+    from parmec_gb300.engine import GpuEngine
+    steps = min(args.steps, 100)
+    out = {"workload": f"{len(scenes)} shaken boxes, sphere counts log-uniform [2048,65536], "
+                       "base excitation f~U[1,20] Hz, a~U[0.1,1] g", "steps": steps}
+    for form, key in ((abi.PG_FORM_MIXED, "mixed"), (abi.PG_FORM_FP64, "fp64")):
+        models = [sc[0] for sc in scenes]
+        P, _ = batch.pool(models)
+        dt = scenes[0][1]
+        eng = GpuEngine(form=form, capacity=(32, 32))
+        eng.attach(P)
+        for k, sc in enumerate(scenes):
+            eng.set_scene(k, True, excitation=sc[2], start=0)
+        P.engine = eng
+        P._dirty = False
+        P.dem(args.warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        times, end_time = driver.step_times(P.curtime, steps * dt - 0.5 * dt, dt)
+        tabs = driver.StepTables(P, times, dt, [1e9, 1e9], [None, None], [-1, -1])
+        ctab = tabs.ctab(0, len(times))
+        stream = torch.cuda.ExternalStream(eng.stream())
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        eng.run(ctab, dt)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        out[key] = {"value": P.parnum * steps / (ms * 1e-3), "unit": "particle-steps/s",
+                    "ms_per_step": ms / steps, "spheres": P.parnum}
+        eng.close()
+        del P
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU restatement on all host cores, rank 0 only."""
     if rank != 0:
@@ -205,6 +245,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--spheres", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -360,6 +401,9 @@ def main():
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in groups.items()},
         "clocks": clk,
     }
+    if not args.no_batched:
+        from parmec_gb300.scenes import batch_scenes
+        line["batched"] = batched_form(args, batch_scenes(512))
     line["mixed"] = mixed_form(args, ref64)
     line["mixed"]["speedup_vs_plain"] = line["mixed"]["value"] / (value / world)
     if not args.no_cpu_baseline and world == 1:

@@ -149,6 +149,14 @@ typedef struct pg_scene {
   int *angkind;
 
   int compat;           /* PG_COMPAT_* bits */
+
+  /* independent scenes sharing one session (batching and serving pools);
+   * nscene == 0 means a single scene and the arrays below may be NULL */
+  int nscene;
+  int *pscene;          /* [parnum] scene of each particle */
+  int *tscene;          /* [trinum] scene of each triangle (a scene's triangles are contiguous) */
+  int *oscene;          /* [obsnum] scene of each obstacle */
+  int *sactive;         /* [nscene] 1 when the scene steps */
 } pg_scene;
 
 /*
@@ -236,6 +244,38 @@ int pg_session_record_geometry(pg_session *s, int on);
 /* Run steps as one captured CUDA graph per step (on, the default) or as
  * individual stream launches (off).  Results are identical. */
 int pg_session_use_graph(pg_session *s, int on);
+
+/* ---- scenes sharing a session -------------------------------------------
+ * Every scene has its own grid origin (cells of a common size), its own
+ * triangles, an active flag, a local time origin and optionally a base
+ * excitation evaluated on the device, g(t) = g0 + a*sin(2*pi*f*t + phase)
+ * with t = (global step - start step) * step.  Scenes never interact, and a
+ * scene's arithmetic is the same whichever other scenes share the session. */
+
+/* Candidate-list capacity: kn slots per sphere and kr slave slots per
+ * particle (1..96, default 32).  Contact lists restart empty. */
+int pg_session_set_capacity(pg_session *s, int kn, int kr);
+
+/* Common grid of every scene: cell size and cells per axis (1..512); the
+ * cell tables are reallocated for nscene << (3*bits) cells. */
+int pg_session_set_grid(pg_session *s, double cell, const int dim[3]);
+
+/* Scene control: active flag; grid origin (NULL keeps it); excitation
+ * [g0x,g0y,g0z,ax,ay,az,f,phase] (NULL: gravity from the step table);
+ * start_step < 0 takes the current global step. */
+int pg_session_scene(pg_session *s, int scene, int active, const double origin[3],
+                     const double excitation[8], long long start_step);
+
+/* Copy the ranges [p0,p1) particles, [e0,e1) spheres, [t0,t1) triangles,
+ * [o0,o1) obstacles of a pooled host scene to the device (range = {p0,p1,e0,
+ * e1,t0,t1,o0,o1}); candidate lists of those spheres restart empty. */
+int pg_session_upload_range(pg_session *s, const pg_scene *scene, const int range[8]);
+
+/* Copy the same ranges of the dynamic state back to the host scene. */
+int pg_session_download_range(pg_session *s, pg_scene *scene, const int range[8]);
+
+/* Steps the session has run so far. */
+int pg_session_global_step(pg_session *s, long long *step);
 
 /* Time kernel groups with CUDA events on the session stream during
  * pg_session_run (on != 0) and reset the accumulators.  Groups: 0 rebuild of

@@ -66,6 +66,8 @@ class PgScene(ctypes.Structure):
         ("prsnum", ctypes.c_int),
         ("prspart", I), ("prslin", I), ("prsang", I), ("linkind", I), ("angkind", I),
         ("compat", ctypes.c_int),
+        ("nscene", ctypes.c_int),
+        ("pscene", I), ("tscene", I), ("oscene", I), ("sactive", I),
     ]
 
 
@@ -150,6 +152,12 @@ def load_library():
         "pg_session_set_skin": (ctypes.c_int, [P, ctypes.c_double]),
         "pg_session_record_geometry": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_profile": (ctypes.c_int, [P, ctypes.c_int]),
+        "pg_session_set_grid": (ctypes.c_int, [P, ctypes.c_double, I]),
+        "pg_session_set_capacity": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "pg_session_scene": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, D, D, ctypes.c_longlong]),
+        "pg_session_upload_range": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I]),
+        "pg_session_download_range": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I]),
+        "pg_session_global_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_use_graph": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_diagnostics": (ctypes.c_int, [P, I]),

@@ -17,22 +17,25 @@ void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
 int  pg_step_kernel_count(const PgDev &d);
 
 // pg_mixed.cu
-void pg_launch_mx_from64(const PgDev &d, cudaStream_t s);
+void pg_launch_mx_from64(const PgDev &d, cudaStream_t s, int p0 = 0, int p1 = -1, int e0 = 0, int e1 = -1);
 void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s);
-void pg_launch_mx_to64(const PgDev &d, cudaStream_t s);
+void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0 = 0, int p1 = -1);
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step);
 
 // pg_sort.cu
 int  pg_sort_blocks(int n);
 int  pg_sort_passes(int bits_per_axis);
+int  pg_sort_passes_bits(int key_bits);
 void pg_launch_cell_keys(const double *x, const double *y, const double *z, int n, const double org[3],
                          double cell, const int dim[3], unsigned *keys, int *vals,
-                         double *rx, double *ry, double *rz, const int *gate, cudaStream_t s);
+                         double *rx, double *ry, double *rz, const int *gate, cudaStream_t s,
+                         const int *scene = nullptr, double *const sorg[3] = nullptr, int shift = 0);
 void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned *hist, int n, int passes,
                           const int *gate, cudaStream_t s);
 
 // pg_rebuild.cu
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
 int  pg_rebuild_kernel_count(const PgDev &d);
-void pg_rebuild_grid_params(PgDev &d, const double *lo, const double *hi, double rmax, double rmin);
+void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin);
+void pg_rebuild_key_bits(PgDev &d);

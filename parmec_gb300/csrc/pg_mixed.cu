@@ -39,6 +39,25 @@ __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
   if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
 }
 
+// gravity of a particle's scene: the device excitation g0 + a*sin(2*pi*f*t + phase)
+// at the scene's local time, or the step table's value
+__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double step, const double *table, double g[3])
+{
+  if (d.sexc_on[sc])
+  {
+    const double *e = d.sexc + 8 * (size_t)sc;
+    const double t = (double)(*d.gstep - d.sstart[sc]) * step;
+    const double sn = sin(2.0 * 3.14159265358979323846 * e[6] * t + e[7]);
+    g[0] = e[0] + e[3] * sn;
+    g[1] = e[1] + e[4] * sn;
+    g[2] = e[2] + e[5] * sn;
+  }
+  else
+  {
+    g[0] = table[0]; g[1] = table[1]; g[2] = table[2];
+  }
+}
+
 // FP32 expmap: the FP64 form's expression tree in single precision
 __device__ __forceinline__ void expmap_f(float O1, float O2, float O3, float *L, bool typo)
 {
@@ -102,10 +121,11 @@ __device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
 }
 
 // ------------------------------------------------------------ conversions
-__global__ void k_mx_from64(PgDev d)
+__global__ void k_mx_from64(PgDev d, int p0, int p1, int e0, int e1)
 {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.parnum)
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = p0 + t;
+  if (i < p1)
   {
     for (int k = 0; k < 3; k ++)
     {
@@ -125,10 +145,11 @@ __global__ void k_mx_from64(PgDev d)
     d.mass_f[i] = (float)d.mass[i];
     d.invm_f[i] = (float)d.invm[i];
   }
-  if (i < d.ellnum)
+  int e = e0 + t;
+  if (e < e1)
   {
-    df r = df_from(d.radii[0][i]);
-    d.rh[i] = r.hi; d.rl[i] = r.lo;
+    df r = df_from(d.radii[0][e]);
+    d.rh[e] = r.hi; d.rl[e] = r.lo;
   }
 }
 
@@ -141,10 +162,10 @@ __global__ void k_mx_inertia(PgDev d)
   d.invm_f[i] = (float)d.invm[i];
 }
 
-__global__ void k_mx_to64(PgDev d)
+__global__ void k_mx_to64(PgDev d, int p0, int p1)
 {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.parnum) return;
+  int i = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p1) return;
   for (int k = 0; k < 3; k ++)
   {
     d.position[k][i] = df_to({d.xh[k][i], d.xl[k][i]});
@@ -323,10 +344,11 @@ __global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
-  if (i < d.parnum)
+  if (i < d.parnum && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
-    const double *grav = d.t_gravity + 3*(size_t)row;
+    double grav[3];
+    scene_gravity(d, d.pscene[i], step_d, d.t_gravity + 3*(size_t)row, grav);
     const double *damping = d.t_damping + 6*(size_t)row;
     const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
     const float step = (float)step_d;
@@ -469,10 +491,12 @@ __global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
 
 } // namespace
 
-void pg_launch_mx_from64(const PgDev &d, cudaStream_t s)
+void pg_launch_mx_from64(const PgDev &d, cudaStream_t s, int p0, int p1, int e0, int e1)
 {
-  int n = d.parnum > d.ellnum ? d.parnum : d.ellnum;
-  if (n) k_mx_from64<<<nblk(n), TPB, 0, s>>>(d);
+  if (p1 < 0) p1 = d.parnum;
+  if (e1 < 0) e1 = d.ellnum;
+  int n = (p1 - p0) > (e1 - e0) ? (p1 - p0) : (e1 - e0);
+  if (n > 0) k_mx_from64<<<nblk(n), TPB, 0, s>>>(d, p0, p1, e0, e1);
 }
 
 void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s)
@@ -480,9 +504,10 @@ void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s)
   if (d.parnum) k_mx_inertia<<<nblk(d.parnum), TPB, 0, s>>>(d);
 }
 
-void pg_launch_mx_to64(const PgDev &d, cudaStream_t s)
+void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0, int p1)
 {
-  if (d.parnum) k_mx_to64<<<nblk(d.parnum), TPB, 0, s>>>(d);
+  if (p1 < 0) p1 = d.parnum;
+  if (p1 > p0) k_mx_to64<<<nblk(p1 - p0), TPB, 0, s>>>(d, p0, p1);
 }
 
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)

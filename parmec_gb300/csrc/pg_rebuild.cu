@@ -30,7 +30,6 @@ namespace {
 
 constexpr int TPB = 128;
 constexpr int MAXKN = 96;                               // upper bound of slots per sphere
-constexpr int TRI_TILE = 256;
 
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
@@ -55,11 +54,11 @@ __device__ __forceinline__ unsigned spread3(unsigned x)
   return x;
 }
 
-__device__ __forceinline__ void cell_of(const PgDev &d, const double *c, int *u)
+__device__ __forceinline__ void cell_of(const PgDev &d, int scene, const double *c, int *u)
 {
   for (int k = 0; k < 3; k ++)
   {
-    double f = floor((c[k] - d.org[k]) / d.cell);
+    double f = floor((c[k] - d.sorg[k][scene]) / d.cell);
     if (!(f >= 0.0)) f = 0.0;                 // also catches NaN
     if (f > (double)(d.dim[k] - 1)) f = (double)(d.dim[k] - 1);
     u[k] = (int)f;
@@ -119,29 +118,29 @@ __device__ __forceinline__ unsigned order_key(int code)
 __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
 {
   if (!*d.rebuild) return;
-  __shared__ float sbox[6][TRI_TILE];
   const int E = d.ellnum;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = i < E;
+  if (i >= E) return;
   int codes[MAXKN];
   int n = 0, nsph = 0, nover = 0, ntri = 0;
   bool over = false;
-  double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
-  int pi = 0;
+  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
+  const double ri = d.radii[0][i];
+  const int pi = d.part[i];
+  const int sc = d.escene[i];
+  const bool live = d.sactive[sc] != 0;
   if (live)
   {
-    c[0] = d.center[0][i]; c[1] = d.center[1][i]; c[2] = d.center[2][i];
-    ri = d.radii[0][i];
-    pi = d.part[i];
+    const unsigned prefix = (unsigned)sc << (3 * d.bits);
     int u[3];
-    cell_of(d, c, u);
+    cell_of(d, sc, c, u);
     for (int dz = -1; dz <= 1; dz ++)
       for (int dy = -1; dy <= 1; dy ++)
         for (int dx = -1; dx <= 1; dx ++)
         {
           int x = u[0]+dx, y = u[1]+dy, z = u[2]+dz;
           if (x < 0 || y < 0 || z < 0 || x >= d.dim[0] || y >= d.dim[1] || z >= d.dim[2]) continue;
-          unsigned key = morton(x, y, z);
+          unsigned key = prefix | morton(x, y, z);
           int b = d.cstart[key], e = d.cend[key];
           for (int s = b; s < e; s ++)
           {
@@ -164,28 +163,17 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
       codes[b+1] = v;
     }
     nsph = n;
-  }
-  // triangles within r + skin, tiled through shared memory
-  const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
-  const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
-  const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
-  for (int t0 = 0; t0 < d.trinum; t0 += TRI_TILE)
-  {
-    __syncthreads();
-    for (int k = threadIdx.x; k < TRI_TILE; k += blockDim.x)
+    // triangles of the sphere's scene within r + skin (AABB in float, then the
+    // true closest-point distance)
+    const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
+    const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
+    const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
+    const int T = d.trinum;
+    for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++)
     {
-      int t = t0 + k;
-      for (int q = 0; q < 6; q ++) sbox[q][k] = t < d.trinum ? d.tbox[(size_t)q * d.trinum + t] : 0.0f;
-    }
-    __syncthreads();
-    if (!live) continue;
-    const int tn = min(TRI_TILE, d.trinum - t0);
-    for (int k = 0; k < tn; k ++)
-    {
-      if (sbox[0][k] > chi[0] || sbox[3][k] < clo[0] ||
-          sbox[1][k] > chi[1] || sbox[4][k] < clo[1] ||
-          sbox[2][k] > chi[2] || sbox[5][k] < clo[2]) continue;
-      int t = t0 + k;
+      if (d.tbox[t] > chi[0] || d.tbox[(size_t)3 * T + t] < clo[0] ||
+          d.tbox[(size_t)T + t] > chi[1] || d.tbox[(size_t)4 * T + t] < clo[1] ||
+          d.tbox[(size_t)2 * T + t] > chi[2] || d.tbox[(size_t)5 * T + t] < clo[2]) continue;
       double A[3], B[3], C[3], pnt[3], nrm[3];
       for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
       // the candidate test uses the true closest point: the reference's region
@@ -303,28 +291,35 @@ __global__ void k_rb_done(PgDev d)
 
 } // namespace
 
-void pg_rebuild_grid_params(PgDev &d, const double *lo, const double *hi, double rmax, double rmin)
+void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin)
 {
   if (!(d.skin > 0.0)) d.skin = 0.3 * rmin;
   d.half_skin_sq = (0.45 * d.skin) * (0.45 * d.skin);
   double cell = 2.0 * rmax + d.skin;
-  double ext = 0.0;
-  for (int k = 0; k < 3; k ++) ext = fmax(ext, hi[k] - lo[k]);
-  ext += 8.0 * cell;
+  double e = 0.0;
+  for (int k = 0; k < 3; k ++) e = fmax(e, ext[k]);
+  e += 8.0 * cell;
   const int maxdim = 512;
-  if (ext / cell > maxdim - 4) cell = ext / (maxdim - 4);
+  if (e / cell > maxdim - 4) cell = e / (maxdim - 4);
   d.cell = cell;
-  int need = 1;
   for (int k = 0; k < 3; k ++)
   {
-    d.org[k] = lo[k] - 4.0 * cell;
-    int n = (int)ceil((hi[k] - lo[k]) / cell) + 9;
+    int n = (int)ceil(ext[k] / cell) + 9;
     if (n > maxdim) n = maxdim;
     if (n < 1) n = 1;
     d.dim[k] = n;
-    while ((1 << need) < n) need ++;
   }
+  pg_rebuild_key_bits(d);
+}
+
+void pg_rebuild_key_bits(PgDev &d)
+{
+  int need = 1;
+  for (int k = 0; k < 3; k ++) while ((1 << need) < d.dim[k]) need ++;
   d.bits = need;
+  int sb = 0;
+  while ((1 << sb) < d.nscene) sb ++;
+  d.keybits = 3 * need + sb;
 }
 
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
@@ -332,10 +327,11 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
   const int E = d.ellnum;
   if (!E) return;
   k_rb_clear<<<nblk(E), TPB, 0, s>>>(d);
-  pg_launch_cell_keys(d.center[0], d.center[1], d.center[2], E, d.org, d.cell, d.dim, d.keys[0], d.vals[0],
-                      d.cref[0], d.cref[1], d.cref[2], d.rebuild, s);
+  pg_launch_cell_keys(d.center[0], d.center[1], d.center[2], E, nullptr, d.cell, d.dim, d.keys[0], d.vals[0],
+                      d.cref[0], d.cref[1], d.cref[2], d.rebuild, s, d.escene, d.sorg, 3 * d.bits);
   if (d.trinum) k_rb_tref<<<nblk(d.trinum), TPB, 0, s>>>(d);
-  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes(d.bits), d.rebuild, s);
+  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes_bits(d.keybits),
+                       d.rebuild, s);
   k_rb_ranges<<<nblk(E), TPB, 0, s>>>(d);
   k_rb_verlet<<<nblk(E), TPB, 0, s>>>(d);
   k_rb_rzero<<<nblk(d.parnum), TPB, 0, s>>>(d);
@@ -347,5 +343,5 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 int pg_rebuild_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
-  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes(d.bits) + 6;
+  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes_bits(d.keybits) + 6;
 }

@@ -22,7 +22,9 @@ struct pg_session
   std::vector<void *> allocs;
   int tab_cap = 0;
   long long launches = 0;
-  double lo[3], hi[3], rmax = 0.0, rmin = 0.0;
+  double ext[3] = {1.0, 1.0, 1.0}, rmax = 0.0, rmin = 0.0;
+  std::vector<double> sorg_h;              // [3][nscene] grid origins
+  std::vector<int> stbeg_h, stend_h;
   size_t ncells = 0;
   int prs_stride = 3, obs_stride = 3;
   std::vector<int> h_pell;
@@ -146,6 +148,20 @@ int allocate(pg_session *s, const pg_scene *sc)
   }
   TRY(dalloc(s, &d.stroke0, S));
   for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.spr_out[k], S));
+  // scenes
+  const size_t NS = d.nscene;
+  TRY(dalloc(s, &d.pscene, P));
+  TRY(dalloc(s, &d.escene, E));
+  TRY(dalloc(s, &d.tscene, T));
+  TRY(dalloc(s, &d.oscene, O));
+  TRY(dalloc(s, &d.sactive, NS));
+  TRY(dalloc(s, &d.stbeg, NS));
+  TRY(dalloc(s, &d.stend, NS));
+  for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.sorg[k], NS));
+  TRY(dalloc(s, &d.sexc_on, NS));
+  TRY(dalloc(s, &d.sexc, 8 * NS));
+  TRY(dalloc(s, &d.sstart, NS));
+  TRY(dalloc(s, &d.gstep, 1));
   return PG_OK;
 }
 
@@ -154,23 +170,7 @@ int upload_static(pg_session *s, const pg_scene *sc)
 {
   PgDev &d = s->d;
   const int P = sc->parnum, E = sc->ellnum, T = sc->trinum, O = sc->obsnum;
-  // particle -> sphere
-  s->h_pell.assign(P, -1);
-  for (int e = 0; e < E; e ++)
-  {
-    int p = sc->part[e];
-    if (p < 0 || p >= P) return PG_ERR_ARGUMENT;
-    if (s->h_pell[p] >= 0) return PG_ERR_UNSUPPORTED;   // more than one sphere per particle
-    if (!(sc->radii[1][e] < 0.0)) return PG_ERR_UNSUPPORTED;  // ellipsoids: assert(0) in the reference
-    s->h_pell[p] = e;
-  }
-  TRY(h2d(s, d.pell, s->h_pell.data(), P));
-  // triangle -> moving obstacle
-  std::vector<int> own(T, -1);
-  for (int o = 0; o < O; o ++)
-    for (int t = sc->trirng[2*o]; t < sc->trirng[2*o+1]; t ++)
-      if (t >= 0 && t < T) own[t] = o;
-  TRY(h2d(s, d.triown, own.data(), T));
+  (void)E; (void)T; (void)O;
   // prescriptions per particle, in input order
   {
     std::vector<int> first(P + 1, 0), list(std::max(1, sc->prsnum));
@@ -237,76 +237,163 @@ int upload_static(pg_session *s, const pg_scene *sc)
   return PG_OK;
 }
 
-// every array the host may have edited (the dynamic state and the parameters)
-int upload_all(pg_session *s, const pg_scene *sc)
+struct Ranges { size_t p0, p1, e0, e1, t0, t1, o0, o1; };
+
+Ranges full_ranges(const PgDev &d)
+{
+  return {0, (size_t)d.parnum, 0, (size_t)d.ellnum, 0, (size_t)d.trinum, 0, (size_t)d.obsnum};
+}
+
+template <typename T>
+int h2dr(pg_session *s, T *dst, const T *src, size_t b, size_t e, size_t w = 1)
+{
+  if (e <= b || !src) return PG_OK;
+  return h2d(s, dst + w * b, src + w * b, w * (e - b));
+}
+
+template <typename T>
+int d2hr(pg_session *s, T *dst, const T *src, size_t b, size_t e, size_t w = 1)
+{
+  if (e <= b || !dst) return PG_OK;
+  return d2h(s, dst + w * b, src + w * b, w * (e - b));
+}
+
+// triangle ranges of every scene from the host's triangle -> scene map
+int scene_triangle_ranges(pg_session *s, const pg_scene *sc)
 {
   PgDev &d = s->d;
-  const size_t P = sc->parnum, E = sc->ellnum, T = sc->trinum, O = sc->obsnum;
-  const size_t N = sc->nodnum, F = sc->facnum, S = sc->sprnum;
-  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.angular[k], sc->angular[k], P));
-  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.linear[k], sc->linear[k], P));
-  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.rotation[k], sc->rotation[k], P));
-  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.position[k], sc->position[k], P));
-  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.inertia[k], sc->inertia[k], P));
-  for (int k = 0; k < 9; k ++) TRY(h2d(s, d.inverse[k], sc->inverse[k], P));
-  TRY(h2d(s, d.mass, sc->mass, P));
-  TRY(h2d(s, d.invm, sc->invm, P));
-  for (int k = 0; k < 3; k ++) { TRY(h2d(s, d.force[k], sc->force[k], P)); TRY(h2d(s, d.torque[k], sc->torque[k], P)); }
-  TRY(h2d(s, d.flags, sc->flags, P));
-  TRY(h2d(s, d.parmat, sc->parmat, P));
-  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.center[k], sc->center[k], E));
-  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.radii[k], sc->radii[k], E));
-  TRY(h2d(s, d.ellcol, sc->ellcol, E));
-  TRY(h2d(s, d.part, sc->part, E));
+  s->stbeg_h.assign(d.nscene, 0);
+  s->stend_h.assign(d.nscene, 0);
+  std::vector<int> seen(d.nscene, 0);
+  for (int t = 0; t < d.trinum; t ++)
+  {
+    int k = (sc->nscene && sc->tscene) ? sc->tscene[t] : 0;
+    if (k < 0 || k >= d.nscene) return PG_ERR_ARGUMENT;
+    if (!seen[k]) { s->stbeg_h[k] = t; seen[k] = 1; }
+    else if (s->stend_h[k] != t) return PG_ERR_ARGUMENT;   // a scene's triangles must be contiguous
+    s->stend_h[k] = t + 1;
+  }
+  TRY(h2d(s, d.stbeg, s->stbeg_h.data(), d.nscene));
+  TRY(h2d(s, d.stend, s->stend_h.data(), d.nscene));
+  return PG_OK;
+}
+
+// copy the given ranges of every per-particle, per-sphere, per-triangle and
+// per-obstacle array; 'global' also copies pairs, springs, meshes and curves
+int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool restart_lists)
+{
+  PgDev &d = s->d;
+  const size_t p0 = r.p0, p1 = r.p1, e0 = r.e0, e1 = r.e1, t0 = r.t0, t1 = r.t1, o0 = r.o0, o1 = r.o1;
+  for (int k = 0; k < 6; k ++) TRY(h2dr(s, d.angular[k], sc->angular[k], p0, p1));
+  for (int k = 0; k < 3; k ++) TRY(h2dr(s, d.linear[k], sc->linear[k], p0, p1));
+  for (int k = 0; k < 9; k ++) TRY(h2dr(s, d.rotation[k], sc->rotation[k], p0, p1));
+  for (int k = 0; k < 6; k ++) TRY(h2dr(s, d.position[k], sc->position[k], p0, p1));
+  for (int k = 0; k < 9; k ++) TRY(h2dr(s, d.inertia[k], sc->inertia[k], p0, p1));
+  for (int k = 0; k < 9; k ++) TRY(h2dr(s, d.inverse[k], sc->inverse[k], p0, p1));
+  TRY(h2dr(s, d.mass, sc->mass, p0, p1));
+  TRY(h2dr(s, d.invm, sc->invm, p0, p1));
+  for (int k = 0; k < 3; k ++) { TRY(h2dr(s, d.force[k], sc->force[k], p0, p1)); TRY(h2dr(s, d.torque[k], sc->torque[k], p0, p1)); }
+  TRY(h2dr(s, d.flags, sc->flags, p0, p1));
+  TRY(h2dr(s, d.parmat, sc->parmat, p0, p1));
+  for (int k = 0; k < 6; k ++) TRY(h2dr(s, d.center[k], sc->center[k], e0, e1));
+  for (int k = 0; k < 3; k ++) TRY(h2dr(s, d.radii[k], sc->radii[k], e0, e1));
+  TRY(h2dr(s, d.ellcol, sc->ellcol, e0, e1));
+  TRY(h2dr(s, d.part, sc->part, e0, e1));
   for (int v = 0; v < 3; v ++)
-    for (int c = 0; c < 3; c ++) TRY(h2d(s, d.tri[3*v+c], sc->tri[v][c], T));
-  TRY(h2d(s, d.tricol, sc->tricol, T));
-  TRY(h2d(s, d.triobs, sc->triobs, T));
-  TRY(h2d(s, d.trirng, sc->trirng, 2*O));
-  TRY(h2d(s, d.obspnt, sc->obspnt, 3*O));
-  TRY(h2d(s, d.obsang, sc->obsang, 3*O));
-  TRY(h2d(s, d.obslin, sc->obslin, 3*O));
-  TRY(h2d(s, d.pairs, sc->pairs, 2*(size_t)sc->pairnum));
-  TRY(h2d(s, d.ikind, sc->ikind, (size_t)sc->pairnum));
-  for (int k = 0; k < 7; k ++) TRY(h2d(s, d.iparam[k], sc->iparam[k], (size_t)sc->pairnum));
-  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.nodes[k], sc->nodes[k], N));
-  TRY(h2d(s, d.nodpart, sc->nodpart, N));
-  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.facnod[k], sc->facnod[k], F));
-  TRY(h2d(s, d.factri, sc->factri, F));
-  TRY(h2d(s, d.sprtype, sc->sprtype, S));
-  TRY(h2d(s, d.unspring, sc->unspring, S));
-  for (int k = 0; k < 2; k ++) TRY(h2d(s, d.sprpart[k], sc->sprpart[k], S));
-  for (int a = 0; a < 2; a ++)
-    for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprpnt[6*a+k], sc->sprpnt[a][k], S));
-  const size_t ns = table_len(sc->spridx, sc->sprnum), nd = table_len(sc->dashidx, sc->sprnum);
-  const size_t nu = table_len(sc->unidx, sc->sprnum);
-  for (int k = 0; k < 2; k ++)
+    for (int c = 0; c < 3; c ++) TRY(h2dr(s, d.tri[3*v+c], sc->tri[v][c], t0, t1));
+  TRY(h2dr(s, d.tricol, sc->tricol, t0, t1));
+  TRY(h2dr(s, d.triobs, sc->triobs, t0, t1));
+  TRY(h2dr(s, d.trirng, sc->trirng, o0, o1, 2));
+  TRY(h2dr(s, d.obspnt, sc->obspnt, o0, o1, 3));
+  TRY(h2dr(s, d.obsang, sc->obsang, o0, o1, 3));
+  TRY(h2dr(s, d.obslin, sc->obslin, o0, o1, 3));
+
+  // particle -> sphere for the particles of the range
   {
-    TRY(h2d(s, d.spring[k], sc->spring[k], ns));
-    TRY(h2d(s, d.dashpot[k], sc->dashpot[k], nd));
-    TRY(h2d(s, d.unload[k], sc->unload[k], nu));
-    TRY(h2d(s, d.yield[k], sc->yield[k], S));
+    std::vector<int> pell(p1 - p0, -1);
+    for (size_t e = e0; e < e1; e ++)
+    {
+      int p = sc->part[e];
+      if (p < 0 || p >= d.parnum) return PG_ERR_ARGUMENT;
+      if (!(sc->radii[1][e] < 0.0)) return PG_ERR_UNSUPPORTED;   // ellipsoids: assert(0) in the reference
+      if ((size_t)p >= p0 && (size_t)p < p1)
+      {
+        if (pell[p - p0] >= 0) return PG_ERR_UNSUPPORTED;       // more than one sphere per particle
+        pell[p - p0] = (int)e;
+      }
+    }
+    if (s->h_pell.size() != (size_t)d.parnum) s->h_pell.assign(d.parnum, -1);
+    for (size_t p = p0; p < p1; p ++) s->h_pell[p] = pell[p - p0];
+    TRY(h2dr(s, d.pell, s->h_pell.data(), p0, p1));
   }
-  if (S)
+  // triangle -> moving obstacle for the triangles of the range
   {
-    TRY(h2d(s, d.spridx, sc->spridx, S + 1));
-    TRY(h2d(s, d.dashidx, sc->dashidx, S + 1));
-    TRY(h2d(s, d.unidx, sc->unidx, S + 1));
+    std::vector<int> own(d.trinum, -1);
+    for (int o = 0; o < d.obsnum; o ++)
+      for (int t = sc->trirng[2*o]; t < sc->trirng[2*o+1]; t ++)
+        if (t >= 0 && t < d.trinum) own[t] = o;
+    TRY(h2dr(s, d.triown, own.data(), t0, t1));
   }
-  for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprdir[k], sc->sprdir[k], S));
-  TRY(h2d(s, d.sprflg, sc->sprflg, S));
-  TRY(h2d(s, d.sproffset, sc->sproffset, S));
-  TRY(h2d(s, d.sprfric, sc->sprfric, S));
-  TRY(h2d(s, d.sprkskn, sc->sprkskn, S));
-  for (int k = 0; k < 3; k ++)
+  // scenes
   {
-    TRY(h2d(s, d.sprsdsp[k], sc->sprsdsp[k], S));
-    TRY(h2d(s, d.stroke[k], sc->stroke[k], S));
-    TRY(h2d(s, d.sprfrc[k], sc->sprfrc[k], S));
+    std::vector<int> ps(d.parnum, 0), es(d.ellnum, 0), ts(d.trinum, 0), os(d.obsnum, 0);
+    const bool many = sc->nscene > 0;
+    for (size_t p = p0; p < p1; p ++) ps[p] = many ? sc->pscene[p] : 0;
+    for (size_t e = e0; e < e1; e ++) es[e] = many ? sc->pscene[sc->part[e]] : 0;
+    for (size_t t = t0; t < t1; t ++) ts[t] = many ? sc->tscene[t] : 0;
+    for (size_t o = o0; o < o1; o ++) os[o] = many ? sc->oscene[o] : 0;
+    TRY(h2dr(s, d.pscene, ps.data(), p0, p1));
+    TRY(h2dr(s, d.escene, es.data(), e0, e1));
+    TRY(h2dr(s, d.tscene, ts.data(), t0, t1));
+    TRY(h2dr(s, d.oscene, os.data(), o0, o1));
+    TRY(scene_triangle_ranges(s, sc));
   }
-  TRY(h2d(s, d.stroke0, sc->stroke0, S));
-  // lookup curves for stroke offsets
+  // a newly loaded scene's spheres start with empty candidate lists; a
+  // re-upload of the same scene keeps its contacts and their state
+  if (restart_lists && e1 > e0) CK(cudaMemsetAsync(d.ncnt + e0, 0, (e1 - e0) * sizeof(int), s->stream));
+
+  if (global)
   {
+    const size_t N = sc->nodnum, F = sc->facnum, S = sc->sprnum;
+    TRY(h2d(s, d.pairs, sc->pairs, 2*(size_t)sc->pairnum));
+    TRY(h2d(s, d.ikind, sc->ikind, (size_t)sc->pairnum));
+    for (int k = 0; k < 7; k ++) TRY(h2d(s, d.iparam[k], sc->iparam[k], (size_t)sc->pairnum));
+    for (int k = 0; k < 6; k ++) TRY(h2d(s, d.nodes[k], sc->nodes[k], N));
+    TRY(h2d(s, d.nodpart, sc->nodpart, N));
+    for (int k = 0; k < 3; k ++) TRY(h2d(s, d.facnod[k], sc->facnod[k], F));
+    TRY(h2d(s, d.factri, sc->factri, F));
+    TRY(h2d(s, d.sprtype, sc->sprtype, S));
+    TRY(h2d(s, d.unspring, sc->unspring, S));
+    for (int k = 0; k < 2; k ++) TRY(h2d(s, d.sprpart[k], sc->sprpart[k], S));
+    for (int a = 0; a < 2; a ++)
+      for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprpnt[6*a+k], sc->sprpnt[a][k], S));
+    const size_t ns = table_len(sc->spridx, sc->sprnum), nd = table_len(sc->dashidx, sc->sprnum);
+    const size_t nu = table_len(sc->unidx, sc->sprnum);
+    for (int k = 0; k < 2; k ++)
+    {
+      TRY(h2d(s, d.spring[k], sc->spring[k], ns));
+      TRY(h2d(s, d.dashpot[k], sc->dashpot[k], nd));
+      TRY(h2d(s, d.unload[k], sc->unload[k], nu));
+      TRY(h2d(s, d.yield[k], sc->yield[k], S));
+    }
+    if (S)
+    {
+      TRY(h2d(s, d.spridx, sc->spridx, S + 1));
+      TRY(h2d(s, d.dashidx, sc->dashidx, S + 1));
+      TRY(h2d(s, d.unidx, sc->unidx, S + 1));
+    }
+    for (int k = 0; k < 6; k ++) TRY(h2d(s, d.sprdir[k], sc->sprdir[k], S));
+    TRY(h2d(s, d.sprflg, sc->sprflg, S));
+    TRY(h2d(s, d.sproffset, sc->sproffset, S));
+    TRY(h2d(s, d.sprfric, sc->sprfric, S));
+    TRY(h2d(s, d.sprkskn, sc->sprkskn, S));
+    for (int k = 0; k < 3; k ++)
+    {
+      TRY(h2d(s, d.sprsdsp[k], sc->sprsdsp[k], S));
+      TRY(h2d(s, d.stroke[k], sc->stroke[k], S));
+      TRY(h2d(s, d.sprfrc[k], sc->sprfrc[k], S));
+    }
+    TRY(h2d(s, d.stroke0, sc->stroke0, S));
     int nlc = 0;
     if (sc->sproffset)
       for (size_t i = 0; i < S; i ++) nlc = std::max(nlc, sc->sproffset[i] + 1);
@@ -321,9 +408,36 @@ int upload_all(pg_session *s, const pg_scene *sc)
       TRY(h2d(s, d.lcidx, sc->lcidx, nlc + 1));
       for (int k = 0; k < 2; k ++) TRY(h2d(s, d.lcurve[k], sc->lcurve[k], nl));
     }
+    std::vector<int> act(d.nscene, 1);
+    if (sc->nscene && sc->sactive) for (int k = 0; k < d.nscene; k ++) act[k] = sc->sactive[k] ? 1 : 0;
+    TRY(h2d(s, d.sactive, act.data(), d.nscene));
   }
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_from64(d, s->stream, (int)p0, (int)p1, (int)e0, (int)e1);
   int one = 1;
   TRY(h2d(s, d.rebuild, &one, 1));
+  return PG_OK;
+}
+
+int upload_all(pg_session *s, const pg_scene *sc) { return upload_ranges(s, sc, full_ranges(s->d), true, false); }
+
+int download_ranges(pg_session *s, pg_scene *sc, Ranges r)
+{
+  PgDev &d = s->d;
+  const size_t p0 = r.p0, p1 = r.p1, e0 = r.e0, e1 = r.e1, t0 = r.t0, t1 = r.t1, o0 = r.o0, o1 = r.o1;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream, (int)p0, (int)p1);
+  for (int k = 0; k < 6; k ++) TRY(d2hr(s, sc->angular[k], d.angular[k], p0, p1));
+  for (int k = 0; k < 3; k ++) TRY(d2hr(s, sc->linear[k], d.linear[k], p0, p1));
+  for (int k = 0; k < 9; k ++) TRY(d2hr(s, sc->rotation[k], d.rotation[k], p0, p1));
+  for (int k = 0; k < 6; k ++) TRY(d2hr(s, sc->position[k], d.position[k], p0, p1));
+  for (int k = 0; k < 9; k ++) TRY(d2hr(s, sc->inverse[k], d.inverse[k], p0, p1));
+  TRY(d2hr(s, sc->invm, d.invm, p0, p1));
+  for (int k = 0; k < 3; k ++) { TRY(d2hr(s, sc->force[k], d.force[k], p0, p1)); TRY(d2hr(s, sc->torque[k], d.torque[k], p0, p1)); }
+  for (int k = 0; k < 3; k ++) TRY(d2hr(s, sc->center[k], d.center[k], e0, e1));
+  for (int v = 0; v < 3; v ++)
+    for (int c = 0; c < 3; c ++) TRY(d2hr(s, sc->tri[v][c], d.tri[3*v+c], t0, t1));
+  TRY(d2hr(s, sc->obspnt, d.obspnt, o0, o1, 3));
+  TRY(d2hr(s, sc->obsang, d.obsang, o0, o1, 3));
+  TRY(d2hr(s, sc->obslin, d.obslin, o0, o1, 3));
   return PG_OK;
 }
 
@@ -351,27 +465,73 @@ int ensure_tables(pg_session *s, int n)
   return PG_OK;
 }
 
+void release(pg_session *s, void *p)
+{
+  if (!p) return;
+  auto it = std::find(s->allocs.begin(), s->allocs.end(), p);
+  if (it != s->allocs.end()) s->allocs.erase(it);
+  cudaFree(p);
+}
+
+// candidate-list storage: kn slots per sphere, kr slave slots per particle;
+// the per-slot FP64 arrays exist only in the FP64 form
+int slot_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  const size_t E = d.ellnum, P = d.parnum;
+  const size_t slots = (size_t)d.kn * std::max<size_t>(E, 1);
+  TRY(dalloc(s, &d.ncode, slots));
+  TRY(dalloc(s, &d.nflag, slots));
+  if (d.form == PG_FORM_FP64)
+  {
+    for (int k = 0; k < 3; k ++)
+    {
+      TRY(dalloc(s, &d.nstate[k], slots));
+      TRY(dalloc(s, &d.nfrc[k], slots));
+      TRY(dalloc(s, &d.npnt[k], slots));
+      TRY(dalloc(s, &d.nnrm[k], slots));
+    }
+    TRY(dalloc(s, &d.ndep, slots));
+  }
+  else
+  {
+    for (int k = 0; k < 3; k ++)
+    {
+      TRY(dalloc(s, &d.nstate_f[k], slots));
+      TRY(dalloc(s, &d.nfrc_f[k], slots));
+      TRY(dalloc(s, &d.narm_f[k], slots));
+    }
+  }
+  TRY(dalloc(s, &d.rref, (size_t)d.kr * std::max<size_t>(P, 1)));
+  return PG_OK;
+}
+
+void release_slot_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  release(s, d.ncode); release(s, d.nflag); release(s, d.ndep); release(s, d.rref);
+  d.ncode = nullptr; d.nflag = nullptr; d.ndep = nullptr; d.rref = nullptr;
+  for (int k = 0; k < 3; k ++)
+  {
+    release(s, d.nstate[k]); release(s, d.nfrc[k]); release(s, d.npnt[k]); release(s, d.nnrm[k]);
+    release(s, d.nstate_f[k]); release(s, d.nfrc_f[k]); release(s, d.narm_f[k]);
+    d.nstate[k] = d.nfrc[k] = d.npnt[k] = d.nnrm[k] = nullptr;
+    d.nstate_f[k] = d.nfrc_f[k] = d.narm_f[k] = nullptr;
+  }
+}
+
 int contact_buffers(pg_session *s)
 {
   PgDev &d = s->d;
   const size_t E = d.ellnum, P = d.parnum, T = d.trinum;
-  const size_t slots = (size_t)d.kn * std::max<size_t>(E, 1);
   TRY(dalloc(s, &d.ncnt, E));
-  TRY(dalloc(s, &d.ncode, slots));
-  TRY(dalloc(s, &d.nflag, slots));
   for (int k = 0; k < 3; k ++)
   {
-    TRY(dalloc(s, &d.nstate[k], slots));
-    TRY(dalloc(s, &d.nfrc[k], slots));
-    TRY(dalloc(s, &d.npnt[k], slots));
-    TRY(dalloc(s, &d.nnrm[k], slots));
     TRY(dalloc(s, &d.fm[k], P));
     TRY(dalloc(s, &d.tm[k], P));
     TRY(dalloc(s, &d.cref[k], E));
   }
-  TRY(dalloc(s, &d.ndep, slots));
   TRY(dalloc(s, &d.rcnt, P));
-  TRY(dalloc(s, &d.rref, (size_t)d.kr * std::max<size_t>(P, 1)));
   for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.tref[k], T));
   TRY(dalloc(s, &d.tbox, 6 * std::max<size_t>(T, 1)));
   for (int k = 0; k < 2; k ++)
@@ -379,17 +539,15 @@ int contact_buffers(pg_session *s)
     TRY(dalloc(s, &d.keys[k], E));
     TRY(dalloc(s, &d.vals[k], E));
   }
-  d.nsortblocks = (int)((E + 2047) / 2048);
-  if (d.nsortblocks < 1) d.nsortblocks = 1;
+  d.nsortblocks = pg_sort_blocks((int)E);
   TRY(dalloc(s, &d.hist, 256 * (size_t)d.nsortblocks));
-  return PG_OK;
+  return slot_buffers(s);
 }
 
 int mixed_buffers(pg_session *s)
 {
   PgDev &d = s->d;
   const size_t P = d.parnum, E = d.ellnum;
-  const size_t slots = (size_t)d.kn * std::max<size_t>(E, 1);
   for (int k = 0; k < 3; k ++)
   {
     TRY(dalloc(s, &d.xh[k], P)); TRY(dalloc(s, &d.xl[k], P));
@@ -397,7 +555,6 @@ int mixed_buffers(pg_session *s)
     TRY(dalloc(s, &d.Om[k], P)); TRY(dalloc(s, &d.om[k], P));
     TRY(dalloc(s, &d.F_f[k], P)); TRY(dalloc(s, &d.T_f[k], P));
     TRY(dalloc(s, &d.fm_f[k], P)); TRY(dalloc(s, &d.tm_f[k], P));
-    TRY(dalloc(s, &d.nstate_f[k], slots)); TRY(dalloc(s, &d.nfrc_f[k], slots)); TRY(dalloc(s, &d.narm_f[k], slots));
   }
   for (int k = 0; k < 9; k ++)
   {
@@ -413,8 +570,7 @@ int grid_buffers(pg_session *s)
 {
   PgDev &d = s->d;
   drop_graph(s);
-  pg_rebuild_grid_params(d, s->lo, s->hi, s->rmax, s->rmin);
-  size_t cells = (size_t)1 << (3 * d.bits);
+  size_t cells = (size_t)d.nscene << (3 * d.bits);
   if (cells != s->ncells)
   {
     for (int *p : {d.cstart, d.cend})
@@ -434,9 +590,41 @@ int grid_buffers(pg_session *s)
     CK(cudaMemsetAsync(d.cend, 0, cells * sizeof(int), s->stream));
   }
   if (d.keys[0]) CK(cudaMemsetAsync(d.keys[0], 0, (size_t)std::max(1, d.ellnum) * sizeof(unsigned), s->stream));
+  for (int k = 0; k < 3; k ++) TRY(h2d(s, d.sorg[k], s->sorg_h.data() + (size_t)k * d.nscene, d.nscene));
   int one = 1;
   TRY(h2d(s, d.rebuild, &one, 1));
   return PG_OK;
+}
+
+// per-scene sphere bounding boxes -> common cell size and dims, per-scene origins
+int grid_from_scene(pg_session *s, const pg_scene *sc)
+{
+  PgDev &d = s->d;
+  const int NS = d.nscene;
+  std::vector<double> lo(3 * NS, 1e300), hi(3 * NS, -1e300);
+  s->rmax = 0.0; s->rmin = 1e300;
+  for (int e = 0; e < sc->ellnum; e ++)
+  {
+    int k = sc->nscene ? sc->pscene[sc->part[e]] : 0;
+    for (int c = 0; c < 3; c ++)
+    {
+      lo[3*k+c] = std::min(lo[3*k+c], sc->center[c][e]);
+      hi[3*k+c] = std::max(hi[3*k+c], sc->center[c][e]);
+    }
+    s->rmax = std::max(s->rmax, sc->radii[0][e]);
+    s->rmin = std::min(s->rmin, sc->radii[0][e]);
+  }
+  if (sc->ellnum == 0) s->rmax = s->rmin = 1.0;
+  for (int c = 0; c < 3; c ++) s->ext[c] = 1e-300;
+  for (int k = 0; k < NS; k ++)
+    for (int c = 0; c < 3; c ++)
+      if (hi[3*k+c] >= lo[3*k+c]) s->ext[c] = std::max(s->ext[c], hi[3*k+c] - lo[3*k+c]);
+  pg_rebuild_grid_params(d, s->ext, s->rmax, s->rmin);
+  s->sorg_h.assign(3 * (size_t)NS, 0.0);
+  for (int k = 0; k < NS; k ++)
+    for (int c = 0; c < 3; c ++)
+      s->sorg_h[(size_t)c * NS + k] = hi[3*k+c] >= lo[3*k+c] ? lo[3*k+c] - 4.0 * d.cell : 0.0;
+  return grid_buffers(s);
 }
 
 void drop_graph(pg_session *s)
@@ -520,7 +708,8 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   d.parnum = sc->parnum; d.ellnum = sc->ellnum; d.trinum = sc->trinum; d.obsnum = sc->obsnum;
   d.nodnum = sc->nodnum; d.facnum = sc->facnum; d.sprnum = sc->sprnum; d.pairnum = sc->pairnum;
   d.prsnum = sc->prsnum; d.compat = sc->compat; d.form = form;
-  d.kn = 64; d.kr = 64;
+  d.nscene = sc->nscene > 0 ? sc->nscene : 1;
+  d.kn = 32; d.kr = 32;
   s->prs_stride = 3 * std::max(1, sc->prsnum);
   s->obs_stride = 3 * std::max(1, sc->obsnum);
   d.tab_prs_stride = s->prs_stride;
@@ -530,28 +719,11 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if ((r = dalloc(s, &d.rebuild, 1)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.err, 4)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.stats, 8)) != PG_OK) goto fail;
+  if ((r = contact_buffers(s)) != PG_OK) goto fail;
+  if (form == PG_FORM_MIXED && (r = mixed_buffers(s)) != PG_OK) goto fail;
   if ((r = upload_static(s, sc)) != PG_OK) goto fail;
   if ((r = upload_all(s, sc)) != PG_OK) goto fail;
-  if ((r = contact_buffers(s)) != PG_OK) goto fail;
-  if (form == PG_FORM_MIXED)
-  {
-    if ((r = mixed_buffers(s)) != PG_OK) goto fail;
-    pg_launch_mx_from64(d, s->stream);
-  }
-  for (int k = 0; k < 3; k ++) { s->lo[k] = 1e300; s->hi[k] = -1e300; }
-  s->rmax = 0.0; s->rmin = 1e300;
-  for (int e = 0; e < sc->ellnum; e ++)
-  {
-    for (int k = 0; k < 3; k ++)
-    {
-      s->lo[k] = std::min(s->lo[k], sc->center[k][e]);
-      s->hi[k] = std::max(s->hi[k], sc->center[k][e]);
-    }
-    s->rmax = std::max(s->rmax, sc->radii[0][e]);
-    s->rmin = std::min(s->rmin, sc->radii[0][e]);
-  }
-  if (sc->ellnum == 0) { for (int k = 0; k < 3; k ++) { s->lo[k] = 0; s->hi[k] = 1; } s->rmax = s->rmin = 1.0; }
-  if ((r = grid_buffers(s)) != PG_OK) goto fail;
+  if ((r = grid_from_scene(s, sc)) != PG_OK) goto fail;
   if ((r = ensure_tables(s, 64)) != PG_OK) goto fail;
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) { r = PG_ERR_CUDA; goto fail; }
   *out = s;
@@ -577,6 +749,9 @@ int pg_session_set_skin(pg_session *s, double skin)
 {
   if (!s) return PG_ERR_ARGUMENT;
   s->d.skin = skin > 0.0 ? skin : 0.0;
+  const double cell_old = s->d.cell;
+  pg_rebuild_grid_params(s->d, s->ext, s->rmax, s->rmin);
+  for (auto &o : s->sorg_h) o += 4.0 * (cell_old - s->d.cell);
   return grid_buffers(s);
 }
 
@@ -597,7 +772,6 @@ int pg_session_upload(pg_session *s, const pg_scene *sc)
   if (s->d.compat != sc->compat) drop_graph(s);
   s->d.compat = sc->compat;
   TRY(upload_all(s, sc));
-  if (s->d.form == PG_FORM_MIXED) pg_launch_mx_from64(s->d, s->stream);
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
@@ -725,21 +899,8 @@ int pg_session_download(pg_session *s, pg_scene *sc)
 {
   if (!s || !sc) return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
-  const size_t P = d.parnum, E = d.ellnum, T = d.trinum, O = d.obsnum, N = d.nodnum, S = d.sprnum;
-  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream);
-  for (int k = 0; k < 6; k ++) TRY(d2h(s, sc->angular[k], d.angular[k], P));
-  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->linear[k], d.linear[k], P));
-  for (int k = 0; k < 9; k ++) TRY(d2h(s, sc->rotation[k], d.rotation[k], P));
-  for (int k = 0; k < 6; k ++) TRY(d2h(s, sc->position[k], d.position[k], P));
-  for (int k = 0; k < 9; k ++) TRY(d2h(s, sc->inverse[k], d.inverse[k], P));
-  TRY(d2h(s, sc->invm, d.invm, P));
-  for (int k = 0; k < 3; k ++) { TRY(d2h(s, sc->force[k], d.force[k], P)); TRY(d2h(s, sc->torque[k], d.torque[k], P)); }
-  for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->center[k], d.center[k], E));
-  for (int v = 0; v < 3; v ++)
-    for (int c = 0; c < 3; c ++) TRY(d2h(s, sc->tri[v][c], d.tri[3*v+c], T));
-  TRY(d2h(s, sc->obspnt, d.obspnt, 3*O));
-  TRY(d2h(s, sc->obsang, d.obsang, 3*O));
-  TRY(d2h(s, sc->obslin, d.obslin, 3*O));
+  const size_t N = d.nodnum, S = d.sprnum;
+  TRY(download_ranges(s, sc, full_ranges(d)));
   for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->nodes[k], d.nodes[k], N));
   TRY(d2h(s, sc->unspring, d.unspring, S));
   for (int a = 0; a < 2; a ++)
@@ -756,6 +917,99 @@ int pg_session_download(pg_session *s, pg_scene *sc)
   CK(cudaStreamSynchronize(s->stream));
   int e = read_err(s);
   return e ? e : PG_OK;
+}
+
+int pg_session_set_capacity(pg_session *s, int kn, int kr)
+{
+  if (!s || kn < 1 || kr < 1 || kn > 96 || kr > 96) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  CK(cudaStreamSynchronize(s->stream));
+  drop_graph(s);
+  release_slot_buffers(s);
+  d.kn = kn;
+  d.kr = kr;
+  TRY(slot_buffers(s));
+  if (d.ellnum) CK(cudaMemsetAsync(d.ncnt, 0, (size_t)d.ellnum * sizeof(int), s->stream));
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_set_grid(pg_session *s, double cell, const int dim[3])
+{
+  if (!s || !dim || !(cell > 0.0)) return PG_ERR_ARGUMENT;
+  for (int k = 0; k < 3; k ++) if (dim[k] < 1 || dim[k] > 512) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (cell < 2.0 * s->rmax + d.skin) return PG_ERR_ARGUMENT;   // neighbours must lie in adjacent cells
+  d.cell = cell;
+  for (int k = 0; k < 3; k ++) d.dim[k] = dim[k];
+  pg_rebuild_key_bits(d);
+  if (d.keybits > 32) return PG_ERR_ARGUMENT;
+  return grid_buffers(s);
+}
+
+int pg_session_scene(pg_session *s, int scene, int active, const double origin[3], const double exc[8],
+                     long long start_step)
+{
+  if (!s || scene < 0 || scene >= s->d.nscene) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  int a = active ? 1 : 0, on = exc ? 1 : 0;
+  TRY(h2d(s, d.sactive + scene, &a, 1));
+  TRY(h2d(s, d.sexc_on + scene, &on, 1));
+  if (exc) TRY(h2d(s, d.sexc + 8 * (size_t)scene, exc, 8));
+  if (origin)
+    for (int k = 0; k < 3; k ++)
+    {
+      s->sorg_h[(size_t)k * d.nscene + scene] = origin[k];
+      TRY(h2d(s, d.sorg[k] + scene, &origin[k], 1));
+    }
+  long long st = start_step;
+  if (st < 0) CK(cudaMemcpyAsync(d.sstart + scene, d.gstep, sizeof(long long), cudaMemcpyDeviceToDevice, s->stream));
+  else TRY(h2d(s, d.sstart + scene, &st, 1));
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+static int ranges_of(const PgDev &d, const int *r, Ranges *out)
+{
+  if (!r) return PG_ERR_ARGUMENT;
+  const int lim[4] = {d.parnum, d.ellnum, d.trinum, d.obsnum};
+  for (int k = 0; k < 4; k ++)
+    if (r[2*k] < 0 || r[2*k+1] < r[2*k] || r[2*k+1] > lim[k]) return PG_ERR_ARGUMENT;
+  *out = {(size_t)r[0], (size_t)r[1], (size_t)r[2], (size_t)r[3], (size_t)r[4], (size_t)r[5], (size_t)r[6], (size_t)r[7]};
+  return PG_OK;
+}
+
+int pg_session_upload_range(pg_session *s, const pg_scene *sc, const int range[8])
+{
+  if (!s || !sc) return PG_ERR_ARGUMENT;
+  Ranges r;
+  TRY(ranges_of(s->d, range, &r));
+  TRY(upload_ranges(s, sc, r, false, true));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_download_range(pg_session *s, pg_scene *sc, const int range[8])
+{
+  if (!s || !sc) return PG_ERR_ARGUMENT;
+  Ranges r;
+  TRY(ranges_of(s->d, range, &r));
+  TRY(download_ranges(s, sc, r));
+  CK(cudaStreamSynchronize(s->stream));
+  int e = read_err(s);
+  return e ? e : PG_OK;
+}
+
+int pg_session_global_step(pg_session *s, long long *step)
+{
+  if (!s || !step) return PG_ERR_ARGUMENT;
+  TRY(d2h(s, step, s->d.gstep, 1));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
 }
 
 int pg_session_contact_count(pg_session *s, int *count)
@@ -808,7 +1062,8 @@ int pg_session_contacts(pg_session *s, int cap, int *count, int *master_particle
     TRY(d2h(s, pt[k].data(), d.npnt[k], slots));
     TRY(d2h(s, nr[k].data(), d.nnrm[k], slots));
   }
-  TRY(d2h(s, dp.data(), d.ndep, slots));
+  if (d.ndep) TRY(d2h(s, dp.data(), d.ndep, slots));
+  else std::fill(dp.begin(), dp.end(), NAN);
   CK(cudaStreamSynchronize(s->stream));
   int n = 0;
   for (int p = 0; p < d.parnum; p ++)

@@ -30,22 +30,32 @@ __device__ __forceinline__ unsigned spread3(unsigned x)
 
 struct Grid { double org[3]; double cell; int dim[3]; };
 
+// key = (scene << shift) | Morton(cell); the cell is taken from the scene's
+// own origin when 'scene' is given, else from g.org
 __global__ void k_cell_keys(const double *x, const double *y, const double *z, int n, Grid g,
+                            const int *scene, const double *sox, const double *soy, const double *soz, int shift,
                             unsigned *keys, int *vals, double *rx, double *ry, double *rz, const int *gate)
 {
   if (closed(gate)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double c[3] = {x[i], y[i], z[i]};
+  double o[3] = {g.org[0], g.org[1], g.org[2]};
+  unsigned sc = 0;
+  if (scene)
+  {
+    sc = (unsigned)scene[i];
+    o[0] = sox[sc]; o[1] = soy[sc]; o[2] = soz[sc];
+  }
   unsigned u[3];
   for (int k = 0; k < 3; k ++)
   {
-    double f = floor((c[k] - g.org[k]) / g.cell);
+    double f = floor((c[k] - o[k]) / g.cell);
     if (!(f >= 0.0)) f = 0.0;
     if (f > (double)(g.dim[k] - 1)) f = (double)(g.dim[k] - 1);
     u[k] = (unsigned)f;
   }
-  keys[i] = spread3(u[0]) | (spread3(u[1]) << 1) | (spread3(u[2]) << 2);
+  keys[i] = (scene ? (sc << shift) : 0u) | spread3(u[0]) | (spread3(u[1]) << 1) | (spread3(u[2]) << 2);
   vals[i] = i;
   if (rx) { rx[i] = c[0]; ry[i] = c[1]; rz[i] = c[2]; }
 }
@@ -161,9 +171,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const unsigned *k
 
 int pg_sort_blocks(int n) { return n > 0 ? (n + SORT_TILE - 1) / SORT_TILE : 1; }
 
-int pg_sort_passes(int bits_per_axis)
+int pg_sort_passes(int bits_per_axis) { return pg_sort_passes_bits(3 * bits_per_axis); }
+
+int pg_sort_passes_bits(int key_bits)
 {
-  int p = (3 * bits_per_axis + 7) / 8;
+  int p = (key_bits + 7) / 8;
   if (p < 2) p = 2;
   if (p & 1) p ++;             // even: the result lands back in the first buffer pair
   return p;
@@ -171,13 +183,16 @@ int pg_sort_passes(int bits_per_axis)
 
 void pg_launch_cell_keys(const double *x, const double *y, const double *z, int n, const double org[3],
                          double cell, const int dim[3], unsigned *keys, int *vals,
-                         double *rx, double *ry, double *rz, const int *gate, cudaStream_t s)
+                         double *rx, double *ry, double *rz, const int *gate, cudaStream_t s,
+                         const int *scene, double *const sorg[3], int shift)
 {
   if (n <= 0) return;
   Grid g;
-  for (int k = 0; k < 3; k ++) { g.org[k] = org[k]; g.dim[k] = dim[k]; }
+  for (int k = 0; k < 3; k ++) { g.org[k] = org ? org[k] : 0.0; g.dim[k] = dim[k]; }
   g.cell = cell;
-  k_cell_keys<<<(n + 127) / 128, 128, 0, s>>>(x, y, z, n, g, keys, vals, rx, ry, rz, gate);
+  k_cell_keys<<<(n + 127) / 128, 128, 0, s>>>(x, y, z, n, g, scene, scene ? sorg[0] : nullptr,
+                                              scene ? sorg[1] : nullptr, scene ? sorg[2] : nullptr, shift,
+                                              keys, vals, rx, ry, rz, gate);
 }
 
 void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned *hist, int n, int passes,

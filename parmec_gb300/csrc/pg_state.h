@@ -87,7 +87,7 @@ struct PgDev
   int *stats;               // [8]: rebuilds, max candidates, max slave entries, max triangles per sphere
   double skin, cell, half_skin_sq;
   double org[3];
-  int dim[3], bits;
+  int dim[3], bits, keybits;   // cells per axis, Morton bits per axis, bits of (scene, cell) keys
   double *cref[3];          // sphere centres at the last rebuild
   double *tref[9];          // triangle vertices at the last rebuild
   unsigned *keys[2];        // radix-sort ping-pong buffers
@@ -98,6 +98,20 @@ struct PgDev
   int *ncnt_new;            // scratch candidate lists of a rebuild
   int *ncode_new;
   float *tbox;              // [6][trinum] triangle AABBs at rebuild (float, widened)
+
+  // ---- independent scenes in one session (batching / serving pool)
+  int nscene;
+  int *pscene;              // [parnum] scene of each particle
+  int *escene;              // [ellnum] scene of each sphere
+  int *tscene;              // [trinum] scene of each triangle
+  int *oscene;              // [obsnum] scene of each obstacle
+  int *sactive;             // [nscene] 1 when the scene steps
+  int *stbeg, *stend;       // [nscene] triangle range of each scene
+  double *sorg[3];          // [nscene] grid origin of each scene (common cell and dims)
+  int *sexc_on;             // [nscene] 1: gravity from the device excitation, 0: from the step table
+  double *sexc;             // [nscene][8] g0 (3), amplitude (3), frequency, phase
+  long long *sstart;        // [nscene] global step at which the scene's local time is 0
+  long long *gstep;         // global step counter
 
   // ---- mixed form (PG_FORM_MIXED): compensated FP32 pairs for positions,
   // linear velocities, rotations and radii; FP32 for everything else

@@ -42,6 +42,26 @@ __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
   if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
 }
 
+
+// gravity of a particle's scene: the device excitation g0 + a*sin(2*pi*f*t + phase)
+// at the scene's local time, or the step table's value
+__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double step, const double *table, double g[3])
+{
+  if (d.sexc_on[sc])
+  {
+    const double *e = d.sexc + 8 * (size_t)sc;
+    const double t = (double)(*d.gstep - d.sstart[sc]) * step;
+    const double sn = sin(2.0 * 3.14159265358979323846 * e[6] * t + e[7]);
+    g[0] = e[0] + e[3] * sn;
+    g[1] = e[1] + e[4] * sn;
+    g[2] = e[2] + e[5] * sn;
+  }
+  else
+  {
+    g[0] = table[0]; g[1] = table[1]; g[2] = table[2];
+  }
+}
+
 // ---------------------------------------------------------------- invert (parmec.ispc:62-99)
 __global__ void k_invert(PgDev d)
 {
@@ -145,7 +165,7 @@ __global__ void k_obstacles(PgDev d, double step, int use_row)
   if (t < d.trinum)
   {
     int o = d.triown[t];
-    if (o >= 0)
+    if (o >= 0 && d.sactive[d.tscene[t]])
     {
       const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
       const double *ang, *lin;
@@ -193,6 +213,7 @@ __global__ void k_tail(PgDev d, double step, int use_row)
   int row = use_row ? *d.stepno : 0;
   for (int o = 0; o < d.obsnum; o ++)
   {
+    if (!d.sactive[d.oscene[o]]) continue;
     if (use_row)
       for (int k = 0; k < 3; k ++)
       {
@@ -204,7 +225,11 @@ __global__ void k_tail(PgDev d, double step, int use_row)
     double y0 = x[0] + step*v[0], y1 = x[1] + step*v[1], y2 = x[2] + step*v[2];
     x[0] = y0; x[1] = y1; x[2] = y2;
   }
-  if (use_row) *d.stepno = row + 1;
+  if (use_row)
+  {
+    *d.stepno = row + 1;
+    *d.gstep += 1;
+  }
 }
 
 // ---------------------------------------------------------------- pairing (forces.ispc:98-122)
@@ -784,10 +809,11 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
-  if (i < d.parnum)
+  if (i < d.parnum && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
-    const double *grav = d.t_gravity + 3*(size_t)row;
+    double grav[3];
+    scene_gravity(d, d.pscene[i], step, d.t_gravity + 3*(size_t)row, grav);
     const double *damping = d.t_damping + 6*(size_t)row;
     const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
     const int E = d.ellnum;

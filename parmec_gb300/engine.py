@@ -14,9 +14,11 @@ def _counts(m):
 class GpuEngine:
     """Runs DEM steps of one Model in a pg_session on the current CUDA device."""
 
-    def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False, graph=True):
+    def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False, graph=True,
+                 capacity=None):
         self.lib = abi.load_library()
         self.graph = graph
+        self.capacity = capacity
         self.form = form
         self.skin = skin
         self.record_geometry = record_geometry
@@ -40,6 +42,9 @@ class GpuEngine:
             abi.check(self.lib.pg_session_record_geometry(self.sess, 1), "pg_session_record_geometry")
         if not self.graph:
             abi.check(self.lib.pg_session_use_graph(self.sess, 0), "pg_session_use_graph")
+        if self.capacity is not None:
+            abi.check(self.lib.pg_session_set_capacity(self.sess, int(self.capacity[0]), int(self.capacity[1])),
+                      "pg_session_set_capacity")
 
     def stale(self):
         return self.model is None or _counts(self.model) != self.counts
@@ -70,6 +75,38 @@ class GpuEngine:
     def kernel_launches(self):
         n = ctypes.c_longlong()
         abi.check(self.lib.pg_session_kernel_launches(self.sess, ctypes.byref(n)), "kernel_launches")
+        return n.value
+
+    # ---- scenes sharing the session
+    def set_scene(self, k, active=True, origin=None, excitation=None, start=-1):
+        o = None if origin is None else np.ascontiguousarray(origin, dtype=np.float64)
+        e = None if excitation is None else np.ascontiguousarray(excitation, dtype=np.float64)
+        abi.check(self.lib.pg_session_scene(self.sess, int(k), 1 if active else 0, abi.dptr(o), abi.dptr(e),
+                                            int(start)), "pg_session_scene")
+
+    def set_grid(self, cell, dims):
+        d = np.ascontiguousarray(dims, dtype=np.int32)
+        abi.check(self.lib.pg_session_set_grid(self.sess, float(cell), abi.iptr(d)), "pg_session_set_grid")
+
+    def upload_range(self, r):
+        self.scene_refresh()
+        rr = np.ascontiguousarray(r, dtype=np.int32)
+        abi.check(self.lib.pg_session_upload_range(self.sess, ctypes.byref(self.scene), abi.iptr(rr)),
+                  "pg_session_upload_range")
+
+    def download_range(self, r):
+        rr = np.ascontiguousarray(r, dtype=np.int32)
+        abi.check(self.lib.pg_session_download_range(self.sess, ctypes.byref(self.scene), abi.iptr(rr)),
+                  "pg_session_download_range")
+        self.model.pull_obstacles()
+
+    def scene_refresh(self):
+        """Re-point the ctypes scene at the model's arrays (after host edits)."""
+        self.scene = self.model.scene()
+
+    def global_step(self):
+        n = ctypes.c_longlong()
+        abi.check(self.lib.pg_session_global_step(self.sess, ctypes.byref(n)), "pg_session_global_step")
         return n.value
 
     def profile(self, on=True):

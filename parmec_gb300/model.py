@@ -641,6 +641,13 @@ class Model:
         s.linkind = abi.iptr(linkind)
         s.angkind = abi.iptr(angkind)
         s.compat = self.compat
+        nscene = getattr(self, "nscene", 0)
+        if nscene:
+            s.nscene = nscene
+            s.pscene = abi.iptr(self.pscene)
+            s.tscene = abi.iptr(self.tscene)
+            s.oscene = abi.iptr(self.oscene)
+            s.sactive = abi.iptr(self.sactive)
         s._keep = keep
         return s
 

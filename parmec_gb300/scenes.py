@@ -148,3 +148,27 @@ def drum(n=1048576, seed=1, radius=0.5, length=0.3, rmin=0.5e-3, rmax=2e-3, dens
             "solid_fraction": solid / bed_volume if bed_volume > 0 else 0.0,
             "drum_fill_fraction": solid / (math.pi * radius ** 2 * length), "dt": dt}
     return m, dt, info
+
+
+def shaken_box(n, seed, frequency, amplitude_g):
+    """A config-0 scene scaled to about n spheres (lattice side round(n^(1/3)),
+    box side 1 m per 16 lattice sites) with its base excitation:
+    g(t) = (A sin(2 pi f t), 0, -9.81).  Returns (model, dt, excitation)."""
+    from .batch import excitation
+    side = max(2, int(round(n ** (1.0 / 3.0))))
+    m, dt = hopper_fill(n_side=side, seed=seed, box=max(1.0, side / 16.0))
+    exc = excitation((0.0, 0.0, -9.81), (amplitude_g * 9.81, 0.0, 0.0), frequency)
+    return m, dt, exc
+
+
+def batch_scenes(count=512, seed=3, nmin=2048, nmax=65536):
+    """Config 3: `count` shaken boxes with sphere counts log-uniform in
+    [nmin, nmax], base excitation f ~ U[1,20] Hz, amplitude ~ U[0.1,1] g."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=count))
+    fs = rng.uniform(1.0, 20.0, size=count)
+    amps = rng.uniform(0.1, 1.0, size=count)
+    out = []
+    for k in range(count):
+        out.append(shaken_box(int(ns[k]), seed * 100003 + k, float(fs[k]), float(amps[k])))
+    return out
