@@ -209,6 +209,50 @@ def batched_form(args, scenes):
     return out
 
 
+def serving_form(args, count):
+    """Config 4: a Poisson stream (200 req/s) of excitation-sweep requests
+    (sphere counts log-uniform [1024, 262144], 200-5000 steps, sinusoid or
+    band-limited noise), served by the continuous-batching pool (mixed and
+    FP64 forms, 150 GB HBM budget) and, for comparison, by the plain FP64
+    drop-in path one request at a time (a DEM() call per request)."""
+    import torch
+    from parmec_gb300 import abi
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.serving import Server, request_stream
+    reqs = request_stream(count)
+    out = {"workload": f"{count} requests, Poisson 200 req/s, spheres log-uniform [1024,262144], "
+                       "steps U[200,5000], sinusoid or band-limited noise base excitation", "hbm_budget_gb": 150}
+    big = max(q.model.parnum for q in reqs)
+    for form, key in ((abi.PG_FORM_MIXED, "mixed_pool"), (abi.PG_FORM_FP64, "fp64_pool")):
+        srv = Server(reqs[0].model, reqs[0].dt, form=form, budget_bytes=150e9, max_scenes=256,
+                     max_spheres=max(big, sum(q.model.parnum for q in reqs)), max_scene_extent=4.0)
+        torch.cuda.synchronize()
+        res, st = srv.serve(reqs, realtime=True)
+        srv.close()
+        out[key] = {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "throughput": st["throughput"],
+                    "unit": "particle-steps/s", "wall_s": st["wall_s"], "requests": st["requests"]}
+    # the plain FP64 drop-in: each request alone through DEM(), in arrival order
+    t0 = time.perf_counter()
+    lat, ps = [], 0
+    for q in reqs:
+        now = time.perf_counter() - t0
+        if now < q.arrival:
+            time.sleep(q.arrival - now)
+        m = q.model
+        m.set_gravity(0.0, 0.0, -9.81)
+        eng = GpuEngine()
+        m.dem(q.steps * q.dt - 0.5 * q.dt, q.dt, interval=1e9, engine=eng)
+        eng.close()
+        lat.append(time.perf_counter() - t0 - q.arrival)
+        ps += m.parnum * q.steps
+    wall = time.perf_counter() - t0
+    out["fp64_dropin"] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                          "throughput": ps / wall, "unit": "particle-steps/s", "wall_s": wall,
+                          "note": "sinusoid excitation replaced by constant gravity; one DEM() per request"}
+    out["mixed_pool_over_fp64_dropin"] = out["mixed_pool"]["throughput"] / out["fp64_dropin"]["throughput"]
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU restatement on all host cores, rank 0 only."""
     if rank != 0:
@@ -246,6 +290,7 @@ def main():
     ap.add_argument("--spheres", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--serving", type=int, default=48, help="requests in the serving stream (0: skip)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -405,6 +450,8 @@ def main():
         from parmec_gb300.scenes import batch_scenes
         line["batched"] = batched_form(args, batch_scenes(512))
     line["mixed"] = mixed_form(args, ref64)
+    if args.serving > 0:
+        line["serving"] = serving_form(args, args.serving)
     line["mixed"]["speedup_vs_plain"] = line["mixed"]["value"] / (value / world)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(args.spheres, os.cpu_count() or 1)

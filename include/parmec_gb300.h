@@ -248,9 +248,13 @@ int pg_session_use_graph(pg_session *s, int on);
 /* ---- scenes sharing a session -------------------------------------------
  * Every scene has its own grid origin (cells of a common size), its own
  * triangles, an active flag, a local time origin and optionally a base
- * excitation evaluated on the device, g(t) = g0 + a*sin(2*pi*f*t + phase)
- * with t = (global step - start step) * step.  Scenes never interact, and a
- * scene's arithmetic is the same whichever other scenes share the session. */
+ * excitation evaluated on the device at t = (global step - start step)*step:
+ *   g(t) = g0 + dir * sum_k amp_k * sin(2*pi*freq_k*t + phase_k),  k < ncomp <= 8,
+ * stored as PG_EXC_LEN doubles {g0x,g0y,g0z, dirx,diry,dirz, ncomp, 0,
+ * amp_0,freq_0,phase_0, ..., amp_7,freq_7,phase_7}.  Scenes never interact,
+ * and a scene's arithmetic is the same whichever other scenes share the
+ * session. */
+#define PG_EXC_LEN 32
 
 /* Candidate-list capacity: kn slots per sphere and kr slave slots per
  * particle (1..96, default 32).  Contact lists restart empty. */
@@ -261,10 +265,10 @@ int pg_session_set_capacity(pg_session *s, int kn, int kr);
 int pg_session_set_grid(pg_session *s, double cell, const int dim[3]);
 
 /* Scene control: active flag; grid origin (NULL keeps it); excitation
- * [g0x,g0y,g0z,ax,ay,az,f,phase] (NULL: gravity from the step table);
+ * record of PG_EXC_LEN doubles (NULL: gravity from the step table);
  * start_step < 0 takes the current global step. */
 int pg_session_scene(pg_session *s, int scene, int active, const double origin[3],
-                     const double excitation[8], long long start_step);
+                     const double excitation[PG_EXC_LEN], long long start_step);
 
 /* Copy the ranges [p0,p1) particles, [e0,e1) spheres, [t0,t1) triangles,
  * [o0,o1) obstacles of a pooled host scene to the device (range = {p0,p1,e0,

@@ -95,9 +95,41 @@ def reserve(P, particles, spheres, triangles, obstacles):
         setattr(P, name, new)
 
 
-def excitation(g0, amplitude, frequency, phase=0.0):
-    """[g0x, g0y, g0z, ax, ay, az, f, phase]: g(t) = g0 + a*sin(2*pi*f*t + phase)."""
-    return np.array(list(g0) + list(amplitude) + [frequency, phase], dtype=np.float64)
+EXC_LEN = 32
+
+
+def excitation(g0, direction, components):
+    """Excitation record: g(t) = g0 + direction * sum_k amp_k sin(2 pi freq_k t + phase_k).
+
+    components: up to 8 (amp, freq, phase) triples."""
+    comps = list(components)
+    if len(comps) > 8:
+        raise ValueError("at most 8 sinusoid components")
+    rec = np.zeros(EXC_LEN, dtype=np.float64)
+    rec[0:3] = g0
+    rec[3:6] = direction
+    rec[6] = len(comps)
+    for k, (a, f, ph) in enumerate(comps):
+        rec[8 + 3 * k:11 + 3 * k] = (a, f, ph)
+    return rec
+
+
+def sinusoid(g0, amplitude_vector, frequency, phase=0.0):
+    """A single sinusoid a*sin(2 pi f t + phase) added to g0."""
+    a = np.asarray(amplitude_vector, dtype=np.float64)
+    n = float(np.linalg.norm(a))
+    d = a / n if n > 0 else np.array([1.0, 0.0, 0.0])
+    return excitation(g0, d, [(n, frequency, phase)])
+
+
+def band_noise(g0, direction, rms, fmin, fmax, seed, ncomp=8):
+    """Seeded band-limited noise: ncomp sinusoids with random frequencies in
+    [fmin, fmax] and phases, scaled to the given RMS acceleration."""
+    rng = np.random.default_rng(seed)
+    f = rng.uniform(fmin, fmax, size=ncomp)
+    ph = rng.uniform(0.0, 2.0 * np.pi, size=ncomp)
+    a = np.full(ncomp, rms * np.sqrt(2.0 / ncomp))
+    return excitation(g0, direction, list(zip(a, f, ph)))
 
 
 def extract(P, k, m):

@@ -14,6 +14,7 @@ void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_mesh(const PgDev &d, cudaStream_t s);
 void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     // velocities from the step table
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
+void pg_launch_excite(const PgDev &d, cudaStream_t s, double step);
 int  pg_step_kernel_count(const PgDev &d);
 
 // pg_mixed.cu
@@ -39,3 +40,4 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
 int  pg_rebuild_kernel_count(const PgDev &d);
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin);
 void pg_rebuild_key_bits(PgDev &d);
+int  pg_rebuild_sort_bits(const PgDev &d);

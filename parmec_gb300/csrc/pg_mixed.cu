@@ -39,23 +39,10 @@ __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
   if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
 }
 
-// gravity of a particle's scene: the device excitation g0 + a*sin(2*pi*f*t + phase)
-// at the scene's local time, or the step table's value
-__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double step, const double *table, double g[3])
+// gravity of a particle's scene for this step (written by k_excite)
+__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double, const double *, double g[3])
 {
-  if (d.sexc_on[sc])
-  {
-    const double *e = d.sexc + 8 * (size_t)sc;
-    const double t = (double)(*d.gstep - d.sstart[sc]) * step;
-    const double sn = sin(2.0 * 3.14159265358979323846 * e[6] * t + e[7]);
-    g[0] = e[0] + e[3] * sn;
-    g[1] = e[1] + e[4] * sn;
-    g[2] = e[2] + e[5] * sn;
-  }
-  else
-  {
-    g[0] = table[0]; g[1] = table[1]; g[2] = table[2];
-  }
+  g[0] = d.sgrav[3*sc]; g[1] = d.sgrav[3*sc+1]; g[2] = d.sgrav[3*sc+2];
 }
 
 // FP32 expmap: the FP64 form's expression tree in single precision
@@ -344,7 +331,7 @@ __global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
-  if (i < d.parnum && d.sactive[d.pscene[i]])
+  if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
     double grav[3];

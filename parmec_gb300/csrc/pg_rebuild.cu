@@ -77,6 +77,7 @@ __global__ void k_rb_clear(PgDev d)
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.ellnum) return;
   unsigned key = d.keys[0][s];
+  if (key == 0xffffffffu) return;          // entries of no scene own no cell
   d.cstart[key] = 0;
   d.cend[key] = 0;
 }
@@ -105,6 +106,7 @@ __global__ void k_rb_ranges(PgDev d)
   const int n = d.ellnum;
   if (s >= n) return;
   unsigned key = d.keys[0][s];
+  if (key == 0xffffffffu) return;
   if (s == 0 || d.keys[0][s-1] != key) d.cstart[key] = s;
   if (s == n-1 || d.keys[0][s+1] != key) d.cend[key] = s + 1;
 }
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
   const double ri = d.radii[0][i];
   const int pi = d.part[i];
   const int sc = d.escene[i];
-  const bool live = d.sactive[sc] != 0;
+  const bool live = sc >= 0 && d.sactive[sc] != 0;
   if (live)
   {
     const unsigned prefix = (unsigned)sc << (3 * d.bits);
@@ -322,6 +324,11 @@ void pg_rebuild_key_bits(PgDev &d)
   d.keybits = 3 * need + sb;
 }
 
+// bits the radix sort orders: with scene ids one more than the valid keys
+// use, so that the 0xffffffff key of a free entry sorts strictly after every
+// valid key (a valid key of all ones in the sorted bits would tie with it)
+int pg_rebuild_sort_bits(const PgDev &d) { return d.keybits + (d.escene ? 1 : 0); }
+
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 {
   const int E = d.ellnum;
@@ -330,7 +337,7 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
   pg_launch_cell_keys(d.center[0], d.center[1], d.center[2], E, nullptr, d.cell, d.dim, d.keys[0], d.vals[0],
                       d.cref[0], d.cref[1], d.cref[2], d.rebuild, s, d.escene, d.sorg, 3 * d.bits);
   if (d.trinum) k_rb_tref<<<nblk(d.trinum), TPB, 0, s>>>(d);
-  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes_bits(d.keybits),
+  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes_bits(pg_rebuild_sort_bits(d)),
                        d.rebuild, s);
   k_rb_ranges<<<nblk(E), TPB, 0, s>>>(d);
   k_rb_verlet<<<nblk(E), TPB, 0, s>>>(d);
@@ -343,5 +350,5 @@ void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 int pg_rebuild_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
-  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes_bits(d.keybits) + 6;
+  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes_bits(pg_rebuild_sort_bits(d)) + 6;
 }

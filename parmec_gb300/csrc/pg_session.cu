@@ -159,7 +159,8 @@ int allocate(pg_session *s, const pg_scene *sc)
   TRY(dalloc(s, &d.stend, NS));
   for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.sorg[k], NS));
   TRY(dalloc(s, &d.sexc_on, NS));
-  TRY(dalloc(s, &d.sexc, 8 * NS));
+  TRY(dalloc(s, &d.sexc, (size_t)PG_EXC_LEN * NS));
+  TRY(dalloc(s, &d.sgrav, 3 * NS));
   TRY(dalloc(s, &d.sstart, NS));
   TRY(dalloc(s, &d.gstep, 1));
   return PG_OK;
@@ -268,7 +269,8 @@ int scene_triangle_ranges(pg_session *s, const pg_scene *sc)
   for (int t = 0; t < d.trinum; t ++)
   {
     int k = (sc->nscene && sc->tscene) ? sc->tscene[t] : 0;
-    if (k < 0 || k >= d.nscene) return PG_ERR_ARGUMENT;
+    if (k < 0) continue;                                   // a triangle of no scene
+    if (k >= d.nscene) return PG_ERR_ARGUMENT;
     if (!seen[k]) { s->stbeg_h[k] = t; seen[k] = 1; }
     else if (s->stend_h[k] != t) return PG_ERR_ARGUMENT;   // a scene's triangles must be contiguous
     s->stend_h[k] = t + 1;
@@ -339,7 +341,7 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     std::vector<int> ps(d.parnum, 0), es(d.ellnum, 0), ts(d.trinum, 0), os(d.obsnum, 0);
     const bool many = sc->nscene > 0;
     for (size_t p = p0; p < p1; p ++) ps[p] = many ? sc->pscene[p] : 0;
-    for (size_t e = e0; e < e1; e ++) es[e] = many ? sc->pscene[sc->part[e]] : 0;
+    for (size_t e = e0; e < e1; e ++) es[e] = many ? sc->pscene[sc->part[e]] : 0;   // -1: no scene
     for (size_t t = t0; t < t1; t ++) ts[t] = many ? sc->tscene[t] : 0;
     for (size_t o = o0; o < o1; o ++) os[o] = many ? sc->oscene[o] : 0;
     TRY(h2dr(s, d.pscene, ps.data(), p0, p1));
@@ -569,6 +571,7 @@ int mixed_buffers(pg_session *s)
 int grid_buffers(pg_session *s)
 {
   PgDev &d = s->d;
+  if (pg_rebuild_sort_bits(d) > 32) return PG_ERR_ARGUMENT;   // (scene, cell) keys must fit 32 bits
   drop_graph(s);
   size_t cells = (size_t)d.nscene << (3 * d.bits);
   if (cells != s->ncells)
@@ -606,6 +609,7 @@ int grid_from_scene(pg_session *s, const pg_scene *sc)
   for (int e = 0; e < sc->ellnum; e ++)
   {
     int k = sc->nscene ? sc->pscene[sc->part[e]] : 0;
+    if (k < 0) continue;
     for (int c = 0; c < 3; c ++)
     {
       lo[3*k+c] = std::min(lo[3*k+c], sc->center[c][e]);
@@ -614,7 +618,8 @@ int grid_from_scene(pg_session *s, const pg_scene *sc)
     s->rmax = std::max(s->rmax, sc->radii[0][e]);
     s->rmin = std::min(s->rmin, sc->radii[0][e]);
   }
-  if (sc->ellnum == 0) s->rmax = s->rmin = 1.0;
+  if (!(s->rmax > 0.0)) s->rmax = s->rmin = 1e-3;   // no sphere in any scene yet (an empty pool):
+                                                    // the host sets the skin and grid before loading
   for (int c = 0; c < 3; c ++) s->ext[c] = 1e-300;
   for (int k = 0; k < NS; k ++)
     for (int c = 0; c < 3; c ++)
@@ -639,6 +644,7 @@ void enqueue_step(pg_session *s, double step)
 {
   const PgDev &d = s->d;
   pg_launch_rebuild(d, s->stream);
+  pg_launch_excite(d, s->stream, step);
   if (d.form == PG_FORM_MIXED)
   {
     pg_launch_contacts_mx(d, s->stream, step);
@@ -850,6 +856,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       cudaEvent_t *ev = &s->ring[(size_t)k * (G + 1)];
       CK(cudaEventRecord(ev[0], s->stream));
       pg_launch_rebuild(d, s->stream);
+      pg_launch_excite(d, s->stream, step);
       CK(cudaEventRecord(ev[1], s->stream));
       if (d.form == PG_FORM_MIXED) pg_launch_contacts_mx(d, s->stream, step);
       else pg_launch_contacts(d, s->stream, step);
@@ -945,11 +952,10 @@ int pg_session_set_grid(pg_session *s, double cell, const int dim[3])
   d.cell = cell;
   for (int k = 0; k < 3; k ++) d.dim[k] = dim[k];
   pg_rebuild_key_bits(d);
-  if (d.keybits > 32) return PG_ERR_ARGUMENT;
   return grid_buffers(s);
 }
 
-int pg_session_scene(pg_session *s, int scene, int active, const double origin[3], const double exc[8],
+int pg_session_scene(pg_session *s, int scene, int active, const double origin[3], const double exc[PG_EXC_LEN],
                      long long start_step)
 {
   if (!s || scene < 0 || scene >= s->d.nscene) return PG_ERR_ARGUMENT;
@@ -957,7 +963,7 @@ int pg_session_scene(pg_session *s, int scene, int active, const double origin[3
   int a = active ? 1 : 0, on = exc ? 1 : 0;
   TRY(h2d(s, d.sactive + scene, &a, 1));
   TRY(h2d(s, d.sexc_on + scene, &on, 1));
-  if (exc) TRY(h2d(s, d.sexc + 8 * (size_t)scene, exc, 8));
+  if (exc) TRY(h2d(s, d.sexc + (size_t)PG_EXC_LEN * scene, exc, PG_EXC_LEN));
   if (origin)
     for (int k = 0; k < 3; k ++)
     {

@@ -44,6 +44,13 @@ __global__ void k_cell_keys(const double *x, const double *y, const double *z, i
   unsigned sc = 0;
   if (scene)
   {
+    if (scene[i] < 0)                // an entry of no scene: sorts last, owns no cell
+    {
+      keys[i] = 0xffffffffu;
+      vals[i] = i;
+      if (rx) { rx[i] = c[0]; ry[i] = c[1]; rz[i] = c[2]; }
+      return;
+    }
     sc = (unsigned)scene[i];
     o[0] = sox[sc]; o[1] = soy[sc]; o[2] = soz[sc];
   }

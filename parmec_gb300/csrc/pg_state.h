@@ -8,7 +8,7 @@
 #pragma once
 #include <cstdint>
 
-#define PG_MAX_OBS_ROW 64   // obstacles per scene handled by the per-step kernels
+#define PG_EXC_LEN 32       // doubles per excitation record: g0[3], dir[3], ncomp, pad, 8 x (amp, freq, phase)
 
 struct PgDev
 {
@@ -109,7 +109,8 @@ struct PgDev
   int *stbeg, *stend;       // [nscene] triangle range of each scene
   double *sorg[3];          // [nscene] grid origin of each scene (common cell and dims)
   int *sexc_on;             // [nscene] 1: gravity from the device excitation, 0: from the step table
-  double *sexc;             // [nscene][8] g0 (3), amplitude (3), frequency, phase
+  double *sexc;             // [nscene][PG_EXC_LEN] excitation records (see pg_session_scene)
+  double *sgrav;            // [nscene][3] gravity of this step (k_excite)
   long long *sstart;        // [nscene] global step at which the scene's local time is 0
   long long *gstep;         // global step counter
 

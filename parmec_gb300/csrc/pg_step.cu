@@ -43,23 +43,35 @@ __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
 }
 
 
-// gravity of a particle's scene: the device excitation g0 + a*sin(2*pi*f*t + phase)
-// at the scene's local time, or the step table's value
-__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double step, const double *table, double g[3])
+// gravity of a particle's scene for this step (written by k_excite)
+__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double, const double *, double g[3])
 {
-  if (d.sexc_on[sc])
+  g[0] = d.sgrav[3*sc]; g[1] = d.sgrav[3*sc+1]; g[2] = d.sgrav[3*sc+2];
+}
+
+// ---------------------------------------------------------------- excitation
+// gravity of every scene for this step: the step table's row, or the scene's
+// base excitation g0 + dir * sum_k amp_k sin(2 pi freq_k t + phase_k) at its
+// local time t = (global step - start step) * step
+__global__ void k_excite(PgDev d, double step)
+{
+  const int sc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sc >= d.nscene) return;
+  const double *tab = d.t_gravity + 3*(size_t)(*d.stepno);
+  if (!d.sexc_on[sc])
   {
-    const double *e = d.sexc + 8 * (size_t)sc;
-    const double t = (double)(*d.gstep - d.sstart[sc]) * step;
-    const double sn = sin(2.0 * 3.14159265358979323846 * e[6] * t + e[7]);
-    g[0] = e[0] + e[3] * sn;
-    g[1] = e[1] + e[4] * sn;
-    g[2] = e[2] + e[5] * sn;
+    d.sgrav[3*sc] = tab[0]; d.sgrav[3*sc+1] = tab[1]; d.sgrav[3*sc+2] = tab[2];
+    return;
   }
-  else
-  {
-    g[0] = table[0]; g[1] = table[1]; g[2] = table[2];
-  }
+  const double *e = d.sexc + (size_t)PG_EXC_LEN * sc;
+  const double t = (double)(*d.gstep - d.sstart[sc]) * step;
+  int nk = (int)e[6];
+  if (nk > 8) nk = 8;
+  double sum = 0.0;
+  for (int k = 0; k < nk; k ++) sum += e[8+3*k] * sin(2.0 * 3.14159265358979323846 * e[9+3*k] * t + e[10+3*k]);
+  d.sgrav[3*sc] = e[0] + e[3] * sum;
+  d.sgrav[3*sc+1] = e[1] + e[4] * sum;
+  d.sgrav[3*sc+2] = e[2] + e[5] * sum;
 }
 
 // ---------------------------------------------------------------- invert (parmec.ispc:62-99)
@@ -165,7 +177,7 @@ __global__ void k_obstacles(PgDev d, double step, int use_row)
   if (t < d.trinum)
   {
     int o = d.triown[t];
-    if (o >= 0 && d.sactive[d.tscene[t]])
+    if (o >= 0 && d.tscene[t] >= 0 && d.sactive[d.tscene[t]])
     {
       const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
       const double *ang, *lin;
@@ -213,7 +225,7 @@ __global__ void k_tail(PgDev d, double step, int use_row)
   int row = use_row ? *d.stepno : 0;
   for (int o = 0; o < d.obsnum; o ++)
   {
-    if (!d.sactive[d.oscene[o]]) continue;
+    if (d.oscene[o] < 0 || !d.sactive[d.oscene[o]]) continue;
     if (use_row)
       for (int k = 0; k < 3; k ++)
       {
@@ -809,7 +821,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
-  if (i < d.parnum && d.sactive[d.pscene[i]])
+  if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
     double grav[3];
@@ -1082,6 +1094,11 @@ void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step)
   if (d.obsnum && d.trinum) k_obstacles<<<nblk(d.trinum), TPB, 0, s>>>(d, step, 1);
 }
 
+void pg_launch_excite(const PgDev &d, cudaStream_t s, double step)
+{
+  k_excite<<<nblk(d.nscene), TPB, 0, s>>>(d, step);
+}
+
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step)
 {
   k_tail<<<1, 32, 0, s>>>(d, step, 1);
@@ -1089,7 +1106,7 @@ void pg_launch_tail(const PgDev &d, cudaStream_t s, double step)
 
 int pg_step_kernel_count(const PgDev &d)
 {
-  int n = 1;                                   // tail
+  int n = 2;                                   // excite, tail
   if (d.ellnum) n += 1;                        // contacts
   if (d.sprnum) n += 1;
   if (d.parnum) n += 1;                        // integrate

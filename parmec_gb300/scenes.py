@@ -154,10 +154,10 @@ def shaken_box(n, seed, frequency, amplitude_g):
     """A config-0 scene scaled to about n spheres (lattice side round(n^(1/3)),
     box side 1 m per 16 lattice sites) with its base excitation:
     g(t) = (A sin(2 pi f t), 0, -9.81).  Returns (model, dt, excitation)."""
-    from .batch import excitation
+    from .batch import sinusoid
     side = max(2, int(round(n ** (1.0 / 3.0))))
     m, dt = hopper_fill(n_side=side, seed=seed, box=max(1.0, side / 16.0))
-    exc = excitation((0.0, 0.0, -9.81), (amplitude_g * 9.81, 0.0, 0.0), frequency)
+    exc = sinusoid((0.0, 0.0, -9.81), (amplitude_g * 9.81, 0.0, 0.0), frequency)
     return m, dt, exc
 
 

@@ -1,0 +1,307 @@
+"""Continuous-batching service for excitation-sweep requests.
+
+Each request is a sphere scene (SPHERE particles in a box of OBSTACLE
+triangles), a number of steps and a base excitation evaluated on the device.
+The server keeps one pooled session resident in HBM: its arrays hold every
+admitted scene in its own ranges, with its own grid, triangles, local time and
+excitation.  Requests are admitted, in arrival order, as soon as a scene slot
+and room in the pool (sized from an HBM budget) are free; all admitted scenes
+advance together, one launch per kernel per step, so their work overlaps on
+the device.  When a request's steps are done its state is read back, its
+ranges are freed and a waiting request can take them.
+
+A scene's arithmetic does not depend on the other scenes in the pool, so a
+request's result is bitwise the same alone and in the mix
+(tests/test_gpu_serving.py).  Each request runs `steps` steps from its initial
+state (no initial half step: the half step of the reference's first DEM call
+is a property of a standalone run).
+"""
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi, batch
+from .engine import GpuEngine
+from .model import Model
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float            # seconds after the stream starts
+    model: Model              # a sphere scene (particles == spheres)
+    steps: int
+    excitation: np.ndarray    # batch.excitation record
+    dt: float
+
+
+@dataclass
+class Result:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    steps: int
+    spheres: int
+    position: np.ndarray = field(repr=False)
+    linear: np.ndarray = field(repr=False)
+    error: str = None
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+class _Ranges:
+    """First-fit allocator over [0, n)."""
+
+    def __init__(self, n):
+        self.free = [(0, n)]
+
+    def take(self, size):
+        if size == 0:
+            return 0
+        for k, (b, e) in enumerate(self.free):
+            if e - b >= size:
+                if e - b == size:
+                    del self.free[k]
+                else:
+                    self.free[k] = (b + size, e)
+                return b
+        return None
+
+    def give(self, b, size):
+        if size == 0:
+            return
+        self.free.append((b, b + size))
+        self.free.sort()
+        merged = []
+        for r in self.free:
+            if merged and merged[-1][1] == r[0]:
+                merged[-1] = (merged[-1][0], r[1])
+            else:
+                merged.append(r)
+        self.free = merged
+
+
+def bytes_per_sphere(form, kn=32, kr=32):
+    """Device bytes one pooled sphere particle needs (state, candidate and slave lists)."""
+    state = 8 * (6 + 3 + 9 + 6 + 9 + 9 + 2 + 3 + 3) + 8 * (6 + 3) + 4 * 12 + 8 * 6 + 8 * 3
+    if form == abi.PG_FORM_MIXED:
+        state += 4 * (6 + 6 + 18 + 6 + 2 + 2 + 18 + 6 + 6 + 6)
+        slots = kn * (4 + 1 + 12 + 12 + 12)
+    else:
+        slots = kn * (4 + 1 + 24 + 24 + 24 + 24 + 8)
+    return state + slots + kr * 4 + 16
+
+
+class Server:
+    """One pooled session; serves requests with continuous batching."""
+
+    def __init__(self, template, dt, form=abi.PG_FORM_MIXED, budget_bytes=150e9, max_scenes=256,
+                 max_spheres=None, max_triangles=None, max_scene_extent=4.0, kn=32, kr=32, chunk=250):
+        self.form = form
+        self.dt = dt
+        self.chunk = chunk
+        cap = int(budget_bytes // bytes_per_sphere(form, kn, kr))
+        if max_spheres is not None:
+            cap = min(cap, int(max_spheres))
+        self.cap = cap
+        self.tcap = int(max_triangles if max_triangles is not None else 12 * max_scenes)
+        self.max_scenes = max_scenes
+        self.P = self._empty_pool(template, cap, self.tcap, max_scenes)
+        self.eng = GpuEngine(form=form, capacity=(kn, kr))
+        self.eng.attach(self.P)
+        self.P.engine = self.eng
+        rmax = float(template.E.radii[0, :template.ellnum].max())
+        rmin = float(template.E.radii[0, :template.ellnum].min())
+        skin = 0.3 * rmin
+        self.cell = 2.0 * rmax + skin
+        n = min(512, int(np.ceil(max_scene_extent / self.cell)) + 9)
+        abi.check(self.eng.lib.pg_session_set_skin(self.eng.sess, skin), "pg_session_set_skin")
+        self.eng.set_grid(self.cell, (n, n, n))
+        self.spheres = _Ranges(cap)
+        self.tris = _Ranges(self.tcap)
+        self.slots = list(range(max_scenes))
+        self.active = {}         # scene slot -> (request, ranges, remaining, admitted)
+        self._zero_tab = None
+
+    @staticmethod
+    def _empty_pool(template, cap, tcap, nscene):
+        P = Model()
+        P.mparam = [list(x) for x in template.mparam]
+        P.pairs, P.ikind, P.iparam = list(template.pairs), list(template.ikind), [list(x) for x in template.iparam]
+        P.compat = template.compat
+        P.P.ensure(cap)
+        P.E.ensure(cap)
+        P.Tr.ensure(tcap)
+        P.parnum = P.ellnum = cap
+        P.trinum = tcap
+        P.P.mass[:cap] = 1.0
+        P.P.invm[:cap] = 1.0
+        P.P.rotation[0, :cap] = P.P.rotation[4, :cap] = P.P.rotation[8, :cap] = 1.0
+        P.E.part[:cap] = np.arange(cap, dtype=np.int32)
+        P.E.radii[0, :cap] = 1e-6
+        P.E.radii[1:3, :cap] = -1.0
+        P.E.ellcol[:cap] = 1
+        P.Tr.triobs[:tcap] = -1
+        P.Tr.tricol[:tcap] = 2
+        P.nscene = nscene
+        P.pscene = np.full(P.P.cap, -1, dtype=np.int32)
+        P.tscene = np.full(P.Tr.cap, -1, dtype=np.int32)
+        P.oscene = np.full(max(1, P.O.cap), -1, dtype=np.int32)
+        P.sactive = np.zeros(nscene, dtype=np.int32)
+        return P
+
+    # ---------------------------------------------------------------- load
+    def _load(self, req, slot):
+        m = req.model
+        n, nt = m.parnum, m.trinum
+        if m.ellnum != n or m.obsnum or m.sprnum or m.prescribe:
+            raise ValueError("a request must be a sphere scene with static obstacles")
+        e0 = self.spheres.take(n)
+        if e0 is None:
+            return None
+        t0 = self.tris.take(nt)
+        if t0 is None:
+            self.spheres.give(e0, n)
+            return None
+        P = self.P
+        for name in P.P.spec:
+            getattr(P.P, name)[..., e0:e0 + n] = getattr(m.P, name)[..., :n]
+        for name in P.E.spec:
+            getattr(P.E, name)[..., e0:e0 + n] = getattr(m.E, name)[..., :n]
+        P.E.part[e0:e0 + n] = np.arange(e0, e0 + n, dtype=np.int32)
+        for name in P.Tr.spec:
+            getattr(P.Tr, name)[..., t0:t0 + nt] = getattr(m.Tr, name)[..., :nt]
+        P.pscene[e0:e0 + n] = slot
+        P.tscene[t0:t0 + nt] = slot
+        r = (e0, e0 + n, e0, e0 + n, t0, t0 + nt, 0, 0)
+        self.eng.upload_range(r)
+        lo = m.E.center[0:3, :n].min(axis=1)
+        self.eng.set_scene(slot, True, origin=lo - 4.0 * self.cell, excitation=req.excitation, start=-1)
+        return r
+
+    def _unload(self, slot):
+        req, r, _, _ = self.active.pop(slot)
+        e0, e1, _, _, t0, t1, _, _ = r
+        self.eng.download_range(r)
+        P = self.P
+        pos = P.P.position[0:3, e0:e1].copy()
+        lin = P.P.linear[:, e0:e1].copy()
+        self.eng.set_scene(slot, False)
+        P.pscene[e0:e1] = -1
+        P.tscene[t0:t1] = -1
+        self.eng.upload_range(r)
+        self.spheres.give(e0, e1 - e0)
+        self.tris.give(t0, t1 - t0)
+        self.slots.append(slot)
+        return pos, lin
+
+    # ---------------------------------------------------------------- loop
+    def _tab(self, n):
+        from .driver import StepTables
+        if self._zero_tab is None or self._zero_tab[0] < n:
+            t = StepTables.__new__(StepTables)
+            t.curtime = np.zeros(n)
+            t.gravity = np.zeros((n, 3))
+            t.damping = np.zeros((n, 6))
+            t.prs_lin = np.zeros((n, 1, 3))
+            t.prs_ang = np.zeros((n, 1, 3))
+            t.obs_ang = np.zeros((n, 1, 3))
+            t.obs_lin = np.zeros((n, 1, 3))
+            self._zero_tab = (n, t)
+        return self._zero_tab[1].ctab(0, n)
+
+    def check(self, req):
+        """Why a request cannot be served by this pool (None when it can)."""
+        m = req.model
+        if m.ellnum != m.parnum or m.obsnum or m.sprnum or m.prescribe:
+            return "not a sphere scene with static obstacles"
+        if m.parnum > self.cap or m.trinum > self.tcap:
+            return "larger than the pool"
+        if abs(req.dt - self.dt) > 1e-12 * self.dt:
+            return "time step differs from the pool's"
+        if req.steps <= 0:
+            return "no steps"
+        return None
+
+    def serve(self, requests, realtime=True):
+        """Serve `requests` (sorted by arrival).  Returns (results, stats);
+        rejected requests come back with `error` set."""
+        pending = []
+        results = []
+        for q in sorted(requests, key=lambda q: q.arrival):
+            why = self.check(q)
+            if why is None:
+                pending.append(q)
+            else:
+                results.append(Result(q.rid, q.arrival, q.arrival, q.arrival, q.steps, q.model.parnum,
+                                      np.zeros((3, 0)), np.zeros((3, 0)), error=why))
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        steps_done = 0
+        psteps = 0
+        while pending or self.active:
+            # admit in arrival order while there is room
+            while pending and (not realtime or pending[0].arrival <= now()) and self.slots:
+                req = pending[0]
+                slot = self.slots.pop(0)
+                r = self._load(req, slot)
+                if r is None:
+                    self.slots.insert(0, slot)
+                    break
+                pending.pop(0)
+                self.active[slot] = (req, r, req.steps, now())
+            if not self.active:
+                if pending and realtime:
+                    time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
+                continue
+            c = min(self.chunk, min(v[2] for v in self.active.values()))
+            self.eng.run(self._tab(c), self.dt)
+            steps_done += c
+            for slot in list(self.active):
+                req, r, rem, adm = self.active[slot]
+                psteps += (r[1] - r[0]) * c
+                rem -= c
+                self.active[slot] = (req, r, rem, adm)
+                if rem == 0:
+                    pos, lin = self._unload(slot)
+                    results.append(Result(req.rid, req.arrival, adm, now(), req.steps, r[1] - r[0], pos, lin))
+        wall = now()
+        lat = np.array([x.latency for x in results if x.error is None])
+        stats = {"requests": len(lat), "rejected": sum(1 for x in results if x.error), "wall_s": wall,
+                 "particle_steps": psteps,
+                 "throughput": psteps / wall if wall > 0 else 0.0,
+                 "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                 "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                 "steps_launched": steps_done}
+        return results, stats
+
+    def close(self):
+        self.eng.close()
+
+
+def request_stream(count, rate=200.0, seed=4, nmin=1024, nmax=262144, smin=200, smax=5000):
+    """Config 4: Poisson arrivals at `rate` req/s; sphere counts log-uniform in
+    [nmin, nmax]; steps uniform in [smin, smax]; half the requests a random
+    sinusoid, half seeded band-limited noise."""
+    import math
+    from .scenes import hopper_fill
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    out = []
+    for k in range(count):
+        n = int(np.exp(rng.uniform(math.log(nmin), math.log(nmax))))
+        side = max(2, int(round(n ** (1.0 / 3.0))))
+        m, dt = hopper_fill(n_side=side, seed=seed * 1000003 + k, box=max(1.0, side / 16.0))
+        steps = int(rng.integers(smin, smax + 1))
+        if rng.random() < 0.5:
+            exc = batch.sinusoid((0.0, 0.0, -9.81), (rng.uniform(0.1, 1.0) * 9.81, 0.0, 0.0),
+                                 rng.uniform(1.0, 20.0))
+        else:
+            exc = batch.band_noise((0.0, 0.0, -9.81), (1.0, 0.0, 0.0), rng.uniform(0.1, 1.0) * 9.81,
+                                   1.0, 20.0, seed=int(rng.integers(1 << 30)))
+        out.append(Request(k, float(t[k]), m, steps, exc, dt))
+    return out
