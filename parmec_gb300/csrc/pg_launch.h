@@ -1,6 +1,7 @@
 // pg_launch.h -- host-side launchers of the device kernels.
 #pragma once
 #include <cuda_runtime.h>
+#include <vector>
 #include "pg_state.h"
 
 // pg_step.cu
@@ -11,6 +12,8 @@ void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step);   /
 void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step);
+void pg_launch_force_sums(const PgDev &d, cudaStream_t s);                          // forces() tail
+void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1); // dynamics()
 void pg_launch_mesh(const PgDev &d, cudaStream_t s);
 void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     // velocities from the step table
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
@@ -23,6 +26,9 @@ void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s);
 void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0 = 0, int p1 = -1);
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step);
+
+// pg_session.cu
+void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &ev);
 
 // pg_sort.cu
 int  pg_sort_blocks(int n);
@@ -37,6 +43,7 @@ void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned
 
 // pg_rebuild.cu
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
+void pg_launch_rebuild_gate(const PgDev &d, cudaStream_t s);   // sets *rebuild when a sphere or vertex moved
 int  pg_rebuild_kernel_count(const PgDev &d);
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin);
 void pg_rebuild_key_bits(PgDev &d);

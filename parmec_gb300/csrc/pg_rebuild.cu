@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
           for (int s = b; s < e; s ++)
           {
             int j = d.vals[0][s];
-            if (d.part[j] <= pi) continue;
+            if ((unsigned)j >= (unsigned)E || d.part[j] <= pi) continue;
             double q0 = c[0] - d.center[0][j], q1 = c[1] - d.center[1][j], q2 = c[2] - d.center[2][j];
             double lim = ri + d.radii[0][j] + d.skin;
             if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
@@ -246,7 +246,7 @@ __global__ void k_rb_rfill(PgDev d)
   {
     int code = d.ncode[(size_t)k * E + i];
     int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
-    if (pj < 0) continue;
+    if (pj < 0 || pj >= d.parnum) continue;
     int r = atomicAdd(&d.rcnt[pj], 1);
     if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
     else set_err(d, PG_ERR_CAPACITY, 3, pj, r + 1);
@@ -291,7 +291,35 @@ __global__ void k_rb_done(PgDev d)
   }
 }
 
+// ---- gate of the drop-in condet(): a rebuild is due when a sphere centre or
+// a triangle vertex moved more than 0.45*skin since the last rebuild (in the
+// session the step kernels raise the same flag as they move things)
+__global__ void k_rb_gate(PgDev d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < d.ellnum)
+  {
+    double r0 = d.center[0][i] - d.cref[0][i], r1 = d.center[1][i] - d.cref[1][i], r2 = d.center[2][i] - d.cref[2][i];
+    need = !((r0*r0 + r1*r1 + r2*r2) <= d.half_skin_sq);
+  }
+  if (i < d.trinum)
+    for (int v = 0; v < 3; v ++)
+    {
+      double r0 = d.tri[3*v][i] - d.tref[3*v][i], r1 = d.tri[3*v+1][i] - d.tref[3*v+1][i];
+      double r2 = d.tri[3*v+2][i] - d.tref[3*v+2][i];
+      need |= !((r0*r0 + r1*r1 + r2*r2) <= d.half_skin_sq);
+    }
+  if (__syncthreads_or(need) && threadIdx.x == 0) atomicExch(d.rebuild, 1);
+}
+
 } // namespace
+
+void pg_launch_rebuild_gate(const PgDev &d, cudaStream_t s)
+{
+  const int n = d.ellnum > d.trinum ? d.ellnum : d.trinum;
+  if (n > 0) k_rb_gate<<<nblk(n), TPB, 0, s>>>(d);
+}
 
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin)
 {

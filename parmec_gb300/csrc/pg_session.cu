@@ -41,6 +41,49 @@ struct pg_session
   int use_graph = 1;
 };
 
+// spring force flush events per particle (CSR 'first' over particles), in
+// the order one springs_task applies them (forces.ispc:1207-1412): springs
+// sorted by (part0, part1) flush a run of equal part0 with += and a run of
+// equal part1 with -=; 'w' marks the first run of its kind, which assigns
+void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &evv)
+{
+  struct Ev { int part; long long pos; int4 v; };
+  std::vector<Ev> ev;
+  int j0 = -1, k0 = -1, jb = 0, kb = 0;
+  bool firstj = true, firstk = true;
+  for (int i = 0; i < S; i ++)
+  {
+    int j = sj[i], k = sk[i];
+    if (j0 != j && j0 >= 0)
+    {
+      ev.push_back({j0, 2LL*i, make_int4(0, jb, i, firstj ? 1 : 0)});
+      firstj = false;
+      jb = i;
+    }
+    if (j0 < 0) jb = i;
+    if (k >= 0)
+    {
+      if (k0 != k && k0 >= 0)
+      {
+        ev.push_back({k0, 2LL*i + 1, make_int4(1, kb, i, firstk ? 1 : 0)});
+        firstk = false;
+        kb = i;
+      }
+      if (k0 < 0) kb = i;
+      k0 = k;
+    }
+    j0 = j;
+  }
+  if (j0 >= 0) ev.push_back({j0, 2LL*S, make_int4(0, jb, S, firstj ? 1 : 0)});
+  if (k0 >= 0) ev.push_back({k0, 2LL*S + 1, make_int4(1, kb, S, firstk ? 1 : 0)});
+  std::stable_sort(ev.begin(), ev.end(), [](const Ev &a, const Ev &b) {
+    return a.part != b.part ? a.part < b.part : a.pos < b.pos; });
+  first.assign(P + 1, 0);
+  evv.assign(std::max<size_t>(1, ev.size()), make_int4(0, 0, 0, 0));
+  for (size_t q = 0; q < ev.size(); q ++) { first[ev[q].part + 1] ++; evv[q] = ev[q].v; }
+  for (int p = 0; p < P; p ++) first[p+1] += first[p];
+}
+
 namespace {
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
@@ -194,42 +237,9 @@ int upload_static(pg_session *s, const pg_scene *sc)
   }
   // spring flush events: the single-task springs_task order (forces.ispc:1207-1412)
   {
-    struct Ev { int part; long long pos; int4 v; };
-    std::vector<Ev> ev;
-    const int S = sc->sprnum;
-    int j0 = -1, k0 = -1, jb = 0, kb = 0;
-    bool firstj = true, firstk = true;
-    for (int i = 0; i < S; i ++)
-    {
-      int j = sc->sprpart[0][i], k = sc->sprpart[1][i];
-      if (j0 != j && j0 >= 0)
-      {
-        ev.push_back({j0, 2LL*i, make_int4(0, jb, i, firstj ? 1 : 0)});
-        firstj = false;
-        jb = i;
-      }
-      if (j0 < 0) jb = i;
-      if (k >= 0)
-      {
-        if (k0 != k && k0 >= 0)
-        {
-          ev.push_back({k0, 2LL*i + 1, make_int4(1, kb, i, firstk ? 1 : 0)});
-          firstk = false;
-          kb = i;
-        }
-        if (k0 < 0) kb = i;
-        k0 = k;
-      }
-      j0 = j;
-    }
-    if (j0 >= 0) ev.push_back({j0, 2LL*S, make_int4(0, jb, S, firstj ? 1 : 0)});
-    if (k0 >= 0) ev.push_back({k0, 2LL*S + 1, make_int4(1, kb, S, firstk ? 1 : 0)});
-    std::stable_sort(ev.begin(), ev.end(), [](const Ev &a, const Ev &b) {
-      return a.part != b.part ? a.part < b.part : a.pos < b.pos; });
-    std::vector<int> first(P + 1, 0);
-    std::vector<int4> evv(std::max<size_t>(1, ev.size()));
-    for (size_t q = 0; q < ev.size(); q ++) { first[ev[q].part + 1] ++; evv[q] = ev[q].v; }
-    for (int p = 0; p < P; p ++) first[p+1] += first[p];
+    std::vector<int> first;
+    std::vector<int4> evv;
+    pg_spring_events(P, sc->sprnum, sc->sprpart[0], sc->sprpart[1], first, evv);
     TRY(dalloc(s, &d.sev_first, P + 1));
     TRY(dalloc(s, &d.sev, evv.size()));
     TRY(h2d(s, d.sev_first, first.data(), P + 1));

@@ -817,21 +817,37 @@ __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
 // contacts_acc_task (slave side) + gravity + spring flushes (single-task order
 // of springs_task) + prescribe_acceleration + dynamics_task +
 // prescribe_velocity + ellipsoids_task, one thread per particle.
-__global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
+// MODE: INT_FUSED runs the whole particle update of one step; the drop-in
+// entry points split it as the reference does: INT_FORCES ends with the
+// force and torque sums (the tail of forces(), forces.ispc:453-596) and
+// INT_DYNAMICS starts from the force and torque arrays (dynamics(),
+// dynamics.ispc:30-169, with h = step and h-bar = (step + step1)/2).
+enum { INT_FUSED = 0, INT_FORCES = 1, INT_DYNAMICS = 2 };
+
+template <int MODE>
+__global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double step1)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
   if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
-    double grav[3];
-    scene_gravity(d, d.pscene[i], step, d.t_gravity + 3*(size_t)row, grav);
     const double *damping = d.t_damping + 6*(size_t)row;
     const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
     const int E = d.ellnum;
     double po[3] = {d.position[0][i], d.position[1][i], d.position[2][i]};
     double F[3], T[3];
     const int e = d.pell ? d.pell[i] : -1;
+    const double ma = d.mass[i];
+    if (MODE == INT_DYNAMICS)
+    {
+      F[0] = d.force[0][i]; F[1] = d.force[1][i]; F[2] = d.force[2][i];
+      T[0] = d.torque[0][i]; T[1] = d.torque[1][i]; T[2] = d.torque[2][i];
+    }
+    else
+    {
+    double grav[3];
+    scene_gravity(d, d.pscene[i], step, d.t_gravity + 3*(size_t)row, grav);
     if (e >= 0)
     {
       F[0] = d.fm[0][i]; F[1] = d.fm[1][i]; F[2] = d.fm[2][i];
@@ -855,7 +871,6 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
         T[2] += a[0]*f[1] - a[1]*f[0];
       }
     }
-    const double ma = d.mass[i];
     F[0] = F[0] + ma * grav[0];
     F[1] = F[1] + ma * grav[1];
     F[2] = F[2] + ma * grav[2];
@@ -899,8 +914,18 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
       }
     }
 
-    // prescribe_acceleration (input.cpp:4247-4341)
-    const int pb = d.prsnum ? d.prs_first[i] : 0, pe = d.prsnum ? d.prs_first[i+1] : 0;
+    }
+    if (MODE == INT_FORCES)
+    {
+      d.force[0][i] = F[0]; d.force[1][i] = F[1]; d.force[2][i] = F[2];
+      d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
+      return;
+    }
+
+    // prescribe_acceleration (input.cpp:4247-4341); the drop-in entry points
+    // leave prescribed motion to the host, as parmec.cpp does
+    const bool prs = MODE == INT_FUSED && d.prsnum;
+    const int pb = prs ? d.prs_first[i] : 0, pe = prs ? d.prs_first[i+1] : 0;
     for (int pp = pb; pp < pe; pp ++)
     {
       const int q = d.prs_list[pp];
@@ -932,7 +957,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
     if (!(d.flags[i] & PG_FLAG_SKIP))
     {
       const double half = 0.5*step;
-      const double hstep = 0.5*(step+step);
+      const double hstep = 0.5*(step+step1);
       for (int k = 0; k < 3; k ++) { O[k] = d.angular[k][i]; v[k] = d.linear[k][i]; }
       for (int k = 0; k < 9; k ++) { L1[k] = d.rotation[k][i]; J[k] = d.inertia[k][i]; I[k] = d.inverse[k][i]; }
       im = d.invm[i];
@@ -1027,7 +1052,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
     d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
 
     // ellipsoids_task for this particle's sphere (shapes.ispc:29-98)
-    if (e >= 0)
+    if (MODE == INT_FUSED && e >= 0)
     {
       double X[3] = {d.position[3][i], d.position[4][i], d.position[5][i]};
       double C[3] = {d.center[3][e], d.center[4][e], d.center[5][e]}, c[3];
@@ -1037,7 +1062,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step)
       need = (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
     }
   }
-  if (d.ellnum) flag_rebuild(d, need);
+  if (MODE == INT_FUSED && d.ellnum) flag_rebuild(d, need);
 }
 
 } // namespace
@@ -1080,7 +1105,17 @@ void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
 
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.parnum) k_integrate<<<nblk(d.parnum), TPB, 0, s>>>(d, step);
+  if (d.parnum) k_integrate<INT_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, step, step);
+}
+
+void pg_launch_force_sums(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_integrate<INT_FORCES><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+}
+
+void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1)
+{
+  if (d.parnum) k_integrate<INT_DYNAMICS><<<nblk(d.parnum), TPB, 0, s>>>(d, step0, step1);
 }
 
 void pg_launch_mesh(const PgDev &d, cudaStream_t s)

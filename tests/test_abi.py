@@ -72,3 +72,71 @@ def test_session_create_without_gpu_fails_loudly():
     m, dt = hopper_fill(n_side=2)
     with pytest.raises(RuntimeError):
         m.dem(dt, dt, engine=GpuEngine())
+
+
+# ---------------------------------------------------------------- drop-in ISPC surface
+ISPC_HEADER = os.path.join(ROOT, "include", "parmec_ispc.h")
+
+
+def ispc_functions():
+    text = open(ISPC_HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"#.*", "", text)
+    return sorted(set(re.findall(r"(?:^|;|\})\s*(?:struct\s+)?\w+\s*\*?\s*(\w+)\s*\(", text)))
+
+
+def test_ispc_header_declares_the_reference_exports():
+    names = ispc_functions()
+    for n in ("condet", "forces", "dynamics", "euler", "invert_inertia", "shapes", "obstacles",
+              "partitioning_create", "partitioning_store", "partitioning_destroy", "master_alloc", "master_free",
+              "slave_alloc", "slave_free", "aligned_real_alloc", "aligned_int_alloc", "ispc_num_cores"):
+        assert n in names, n
+
+
+def test_library_exports_every_ispc_symbol():
+    from parmec_gb300 import abi
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.library_path()], capture_output=True, text=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    assert not [n for n in ispc_functions() if n not in exported]
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_ispc_header_compiles(tmp_path, lang):
+    """parmec.cpp includes the header as C++ (namespace ispc); C hosts can use it too."""
+    src = tmp_path / ("use.cpp" if lang == "c++" else "use.c")
+    pre = "using namespace ispc;\n" if lang == "c++" else ""
+    src.write_text('#include "parmec_ispc.h"\n' + pre +
+                   "int main(void){ return (int)sizeof(struct master_conpnt) - 1464 + "
+                   "(int)sizeof(struct slave_conpnt) - 600; }\n")
+    exe = tmp_path / "use"
+    cc = "g++" if lang == "c++" else "gcc"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0
+
+
+def test_ispc_host_side_functions_without_gpu():
+    """Allocation, grid handles and the no-op restraint paths need no device."""
+    from parmec_gb300 import abi
+    lib = abi.load_library()
+    lib.aligned_real_alloc.restype = ctypes.POINTER(ctypes.c_double)
+    lib.partitioning_create.restype = ctypes.c_void_p
+    lib.master_alloc.restype = ctypes.c_void_p
+    lib.master_alloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.master_free.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    p = lib.aligned_real_alloc(1000)
+    assert all(p[i] == 0.0 for i in range(1000))
+    lib.aligned_real_free(p)
+    assert lib.ispc_num_cores() >= 1
+    assert lib.partitioning_create(1, 0, None) is None
+    t = lib.partitioning_create(1, 10, None)
+    assert t and lib.partitioning_store(1, ctypes.c_void_p(t), 10, None, None, None, None, None) == 0
+    lib.partitioning_destroy(ctypes.c_void_p(t))
+    m = lib.master_alloc(None, 0, 16)
+    m2 = lib.master_alloc(m, 16, 32)
+    lib.master_free(m2, 32)
+    lib.pg_compat_exit_on_error(0)
+    lib.restrain_forces(1, 0, None, None, None, None, None)
+    assert lib.pg_compat_status() == 0
+    lib.restrain_forces(1, 2, None, None, None, None, None)
+    assert lib.pg_compat_status() == abi.PG_ERR_UNSUPPORTED
+    lib.pg_compat_exit_on_error(1)

@@ -1,0 +1,124 @@
+"""The drop-in ISPC entry points (include/parmec_ispc.h) on the GPU.
+
+parmec.cpp's dem() loop over condet/forces/dynamics/shapes/obstacles/euler/
+invert_inertia (tests/ispc_loop.py) must give the oracle's state bit for bit,
+as the session does: the entry points run the same kernels, with host arrays
+copied in and out at every call.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import ispc_loop
+from helpers import assert_bitwise, assert_spheres_bitwise, bits, make_collision_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(make, steps, calls=1, skin=0.0):
+    from oracle.pyoracle import OracleEngine
+    lib = ispc_loop.library()
+    lib.pg_compat_exit_on_error(0)
+    lib.pg_compat_set_skin(ctypes.c_double(skin))
+    mc, dt = make()
+    mo, _ = make()
+    host = ispc_loop.Host(lib, mc)
+    eo = OracleEngine()
+    for c in range(calls):
+        mo.dem(steps * dt - 0.5 * dt, dt, interval=1e9, engine=eo)
+        ispc_loop.dem(lib, host, steps * dt - 0.5 * dt, dt)
+        assert_bitwise(mc, mo, where=f"after DEM call {c + 1}: ")
+    return lib, host, mc, mo, eo
+
+
+def materialized(lib, host):
+    """Contacts written into the reference's list layout, as (particle, code, force) rows."""
+    P = host.m.parnum
+
+    class Master(ctypes.Structure):
+        pass
+    Master._fields_ = [("master", ctypes.c_int * 8), ("slave", (ctypes.c_int * 8) * 2),
+                       ("color", (ctypes.c_int * 8) * 2), ("point", (ctypes.c_double * 8) * 3),
+                       ("normal", (ctypes.c_double * 8) * 3), ("depth", ctypes.c_double * 8),
+                       ("force", (ctypes.c_double * 8) * 3), ("kcur", ctypes.c_double * 8),
+                       ("ecur", ctypes.c_double * 8), ("state", (ctypes.c_double * 8) * 8),
+                       ("size", ctypes.c_int), ("next", ctypes.POINTER(Master)), ("lock", ctypes.c_int)]
+    n = lib.pg_compat_materialize(ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), P)
+    assert n >= 0
+    arr = (Master * P).from_address(host.master)
+    rows = []
+    for p in range(P):
+        b = arr[p]
+        while True:
+            for k in range(b.size):
+                rows.append((p, b.slave[1][k], b.force[0][k], b.force[1][k], b.force[2][k], b.depth[k]))
+            if not b.next:
+                break
+            b = b.next.contents
+    assert len(rows) == n
+    return rows
+
+
+def test_dropin_collisions_bitwise(gpu_lib, oracle_lib):
+    """Sphere-sphere and sphere-triangle contacts through condet/forces/dynamics."""
+    lib, host, mc, mo, eo = run_both(lambda: make_collision_scene(n_side=5), 120)
+    assert_bitwise(mc, mo)
+    assert_spheres_bitwise(mc, mo)
+    rows = materialized(lib, host)
+    co = eo.contacts()
+    assert len(rows) == len(co["mpart"]) > 10
+    got = sorted((r[0], r[1]) for r in rows)
+    want = sorted(zip(co["mpart"].tolist(), co["code"].tolist()))
+    assert got == want
+    fg = np.array(sorted((r[0], r[1], r[2], r[3], r[4]) for r in rows))[:, 2:]
+    f = co["force"]
+    fo = np.array(sorted(zip(co["mpart"].tolist(), co["code"].tolist(), f[:, 0], f[:, 1], f[:, 2])))[:, 2:]
+    assert np.array_equal(bits(fg), bits(fo))
+    assert lib.pg_compat_kernel_launches() > 0
+    host.close()
+
+
+def test_dropin_moving_obstacle_two_calls(gpu_lib, oracle_lib):
+    """A rotating wall, two DEM() calls: contact state survives between calls."""
+    lib, host, mc, mo, eo = run_both(lambda: make_collision_scene(n_side=4, moving=True, seed=11), 70, calls=2)
+    assert_bitwise(mc, mo)
+    a = mc.Tr.tri[:, :mc.trinum]
+    b = mo.Tr.tri[:, :mo.trinum]
+    assert np.array_equal(bits(a), bits(b))
+    host.close()
+
+
+def test_dropin_small_skin(gpu_lib, oracle_lib):
+    """A tiny skin: condet() rebuilds the candidate lists nearly every step."""
+    lib, host, mc, mo, eo = run_both(lambda: make_collision_scene(n_side=4, seed=5), 60, skin=1e-5)
+    assert_bitwise(mc, mo)
+    host.close()
+    lib.pg_compat_set_skin(ctypes.c_double(0.0))
+
+
+def test_dropin_springs_and_prescribe(gpu_lib, oracle_lib):
+    """The spring lattice with a prescribed base: springs in forces(), the
+    prescribed motion on the host between forces() and dynamics()."""
+    from test_gpu_springs import lattice, spring_state_equal
+    step = 2e-5
+    lib, host, mc, mo, eo = run_both(lambda: (lattice(), step), 200)
+    assert_bitwise(mc, mo)
+    spring_state_equal(mc, mo)
+    host.close()
+
+
+def test_dropin_unsupported_cases_report(gpu_lib):
+    """Ellipsoids and restraints report PG_ERR_UNSUPPORTED instead of running."""
+    from parmec_gb300 import abi
+    lib = ispc_loop.library()
+    lib.pg_compat_exit_on_error(0)
+    m, dt = make_collision_scene(n_side=2)
+    m.E.radii[1, 0] = 0.01                     # an ellipsoid
+    host = ispc_loop.Host(lib, m)
+    with pytest.raises(RuntimeError):
+        ispc_loop.dem(lib, host, 2.5 * dt, dt)
+    host.close()
+    lib.restrain_velocities(1, 1, None, None, None, None, None, None)
+    assert lib.pg_compat_status() == abi.PG_ERR_UNSUPPORTED
+    lib.pg_compat_exit_on_error(1)
