@@ -179,17 +179,22 @@ def batched_form(args, scenes):
     steps = min(args.steps, 100)
     out = {"workload": f"{len(scenes)} shaken boxes, sphere counts log-uniform [2048,65536], "
                        "base excitation f~U[1,20] Hz, a~U[0.1,1] g", "steps": steps}
-    for form, key in ((abi.PG_FORM_MIXED, "mixed"), (abi.PG_FORM_FP64, "fp64")):
+    legs = ((abi.PG_FORM_MIXED, "mixed", True), (abi.PG_FORM_MIXED, "mixed_per_phase_kernels", False),
+            (abi.PG_FORM_FP64, "fp64", False))
+    for form, key, fused in legs:
         models = [sc[0] for sc in scenes]
         P, _ = batch.pool(models)
         dt = scenes[0][1]
-        eng = GpuEngine(form=form, capacity=(32, 32))
+        # the persistent fused step kernel picks its launch shape during the
+        # warm-up steps (real steps; the result does not depend on the shape)
+        eng = GpuEngine(form=form, capacity=(32, 32), fused=fused, autotune=fused)
         eng.attach(P)
         for k, sc in enumerate(scenes):
             eng.set_scene(k, True, excitation=sc[2], start=0)
         P.engine = eng
         P._dirty = False
-        P.dem(args.warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        warm = max(args.warmup, 64) if fused else args.warmup
+        P.dem(warm * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
         times, end_time = driver.step_times(P.curtime, steps * dt - 0.5 * dt, dt)
         tabs = driver.StepTables(P, times, dt, [1e9, 1e9], [None, None], [-1, -1])
         ctab = tabs.ctab(0, len(times))
@@ -203,6 +208,10 @@ def batched_form(args, scenes):
         ms = ev0.elapsed_time(ev1)
         out[key] = {"value": P.parnum * steps / (ms * 1e-3), "unit": "particle-steps/s",
                     "ms_per_step": ms / steps, "spheres": P.parnum}
+        if fused:
+            threads, blocks, tuned, graph = eng.fused_config()
+            out[key]["kernel"] = {"persistent_fused": True, "threads": threads, "blocks": blocks,
+                                  "autotuned": bool(tuned), "cuda_graph": bool(graph)}
         eng.close()
         del P
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]

@@ -245,6 +245,22 @@ int pg_session_record_geometry(pg_session *s, int on);
  * individual stream launches (off).  Results are identical. */
 int pg_session_use_graph(pg_session *s, int on);
 
+/* Mixed form only: run steps in one persistent, cooperatively launched step
+ * kernel (rebuild, radix sort, contacts, integration, obstacles and scene
+ * excitation between grid barriers), captured as a CUDA graph of 16 steps per
+ * replay.  Results are bit-identical to the per-phase kernels for any launch
+ * shape.  A grid barrier that waits more than 2 s gives PG_ERR_TIMEOUT in
+ * the diagnostics instead of hanging.  PG_ERR_UNSUPPORTED in the FP64 form. */
+int pg_session_use_fused(pg_session *s, int on);
+
+/* Let the next runs pick the fused kernel's launch shape (threads per block,
+ * blocks per SM) by timing the candidates on the session's own first steps;
+ * the steps are real steps of the run. */
+int pg_session_autotune(pg_session *s, int on);
+
+/* out4 = {threads per block, blocks, 1 if tuned, 1 if running as a graph}. */
+int pg_session_fused_config(pg_session *s, int *out4);
+
 /* ---- scenes sharing a session -------------------------------------------
  * Every scene has its own grid origin (cells of a common size), its own
  * triangles, an active flag, a local time origin and optionally a base

@@ -1,0 +1,510 @@
+// pg_items.cuh -- per-item bodies of the step phases that both the one-kernel-
+// per-phase path (pg_step.cu, pg_rebuild.cu, pg_sort.cu) and the persistent
+// fused step kernel (pg_mixed.cu) run.  A kernel launches one thread per item
+// and calls the body; the persistent kernel walks the same items in
+// grid-stride loops between grid barriers.  The bodies are the only copy of
+// this code.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "pg_state.h"
+#include "pg_math.cuh"
+#include "../../include/parmec_gb300.h"
+
+namespace pgk {
+
+constexpr int MAXKN = 96;                       // upper bound of candidate slots per sphere
+constexpr int SORT_THREADS = 256;               // radix sort: threads and keys of one tile
+constexpr int SORT_ITEMS = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+
+// record the first error with where it happened (site), the index and a value
+__device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
+{
+  if (atomicCAS(d.err, 0, code) == 0)
+  {
+    d.err[1] = site;
+    d.err[2] = index;
+    d.err[3] = value;
+  }
+}
+
+__device__ __forceinline__ unsigned spread3(unsigned x)
+{
+  x &= 0x3ff;
+  x = (x | (x << 16)) & 0x030000FF;
+  x = (x | (x << 8)) & 0x0300F00F;
+  x = (x | (x << 4)) & 0x030C30C3;
+  x = (x | (x << 2)) & 0x09249249;
+  return x;
+}
+
+__device__ __forceinline__ unsigned morton(int x, int y, int z)
+{
+  return spread3((unsigned)x) | (spread3((unsigned)y) << 1) | (spread3((unsigned)z) << 2);
+}
+
+__device__ __forceinline__ void cell_of(const PgDev &d, int scene, const double *c, int *u)
+{
+  for (int k = 0; k < 3; k ++)
+  {
+    double f = floor((c[k] - d.sorg[k][scene]) / d.cell);
+    if (!(f >= 0.0)) f = 0.0;                 // also catches NaN
+    if (f > (double)(d.dim[k] - 1)) f = (double)(d.dim[k] - 1);
+    u[k] = (int)f;
+  }
+}
+
+__device__ __forceinline__ unsigned order_key(int code)
+{
+  return code >= 0 ? (unsigned)code : 0x80000000u + (unsigned)(-code - 1);
+}
+
+// ================================================================ cell keys and radix sort
+struct Grid { double org[3]; double cell; int dim[3]; };
+
+// key = (scene << shift) | Morton(cell); the cell is taken from the scene's
+// own origin when 'scene' is given, else from g.org
+__device__ __forceinline__ void cell_keys_item(int i, const double *x, const double *y, const double *z, const Grid &g,
+                                               const int *scene, const double *sox, const double *soy,
+                                               const double *soz, int shift, unsigned *keys, int *vals,
+                                               double *rx, double *ry, double *rz)
+{
+  double c[3] = {x[i], y[i], z[i]};
+  double o[3] = {g.org[0], g.org[1], g.org[2]};
+  unsigned sc = 0;
+  if (scene)
+  {
+    if (scene[i] < 0)                // an entry of no scene: sorts last, owns no cell
+    {
+      keys[i] = 0xffffffffu;
+      vals[i] = i;
+      if (rx) { rx[i] = c[0]; ry[i] = c[1]; rz[i] = c[2]; }
+      return;
+    }
+    sc = (unsigned)scene[i];
+    o[0] = sox[sc]; o[1] = soy[sc]; o[2] = soz[sc];
+  }
+  unsigned u[3];
+  for (int k = 0; k < 3; k ++)
+  {
+    double f = floor((c[k] - o[k]) / g.cell);
+    if (!(f >= 0.0)) f = 0.0;
+    if (f > (double)(g.dim[k] - 1)) f = (double)(g.dim[k] - 1);
+    u[k] = (unsigned)f;
+  }
+  keys[i] = (scene ? (sc << shift) : 0u) | spread3(u[0]) | (spread3(u[1]) << 1) | (spread3(u[2]) << 2);
+  vals[i] = i;
+  if (rx) { rx[i] = c[0]; ry[i] = c[1]; rz[i] = c[2]; }
+}
+
+// per-tile digit histogram, stored digit-major: hist[digit*nb + tile].  The
+// first 256 threads of the block do the work; every thread must call.
+__device__ __forceinline__ void sort_hist_tile(const unsigned *keys, int n, unsigned *hist, int nb, int shift,
+                                               int tile, unsigned *h)
+{
+  const int t = threadIdx.x;
+  if (t < 256) h[t] = 0;
+  __syncthreads();
+  if (t < SORT_THREADS)
+  {
+    const int base = tile * SORT_TILE;
+    for (int it = 0; it < SORT_ITEMS; it ++)
+    {
+      int s = base + it * SORT_THREADS + t;
+      if (s < n) atomicAdd(&h[(keys[s] >> shift) & 255u], 1u);
+    }
+  }
+  __syncthreads();
+  if (t < 256) hist[t * nb + tile] = h[t];
+  __syncthreads();
+}
+
+// exclusive scan of the digit-major histogram by one block (any size >= 32);
+// part[] holds blockDim.x entries
+__device__ __forceinline__ void sort_scan_block(unsigned *hist, int nb, unsigned *part)
+{
+  const int T = blockDim.x, t = threadIdx.x;
+  const int total = 256 * nb;
+  const int per = (total + T - 1) / T;
+  const int b = t * per;
+  const int e = min(b + per, total);
+  unsigned sum = 0;
+  for (int k = b; k < e; k ++) sum += hist[k];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1)
+  {
+    unsigned v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  unsigned run = t ? part[t - 1] : 0u;
+  for (int k = b; k < e; k ++)
+  {
+    unsigned v = hist[k];
+    hist[k] = run;
+    run += v;
+  }
+  __syncthreads();
+}
+
+// stable scatter of one tile: each of the first 8 warps ranks its contiguous
+// sub-tile 32 keys at a time (__match_any_sync groups equal digits, popc of
+// lower peers gives the rank).  wcnt is [8][256], goff [256]; every thread
+// of the block must call.
+__device__ __forceinline__ void sort_scatter_tile(const unsigned *ksrc, const int *vsrc, unsigned *kdst, int *vdst,
+                                                  int n, const unsigned *hist, int nb, int shift, int tile,
+                                                  unsigned (*wcnt)[256], unsigned *goff)
+{
+  constexpr int WARPS = SORT_THREADS / 32;
+  constexpr int SUB = SORT_TILE / WARPS;
+  const int t = threadIdx.x;
+  const int lane = t & 31, warp = t >> 5;
+  if (t < SORT_THREADS)
+  {
+    for (int k = t; k < WARPS * 256; k += SORT_THREADS) (&wcnt[0][0])[k] = 0;
+    goff[t] = hist[t * nb + tile];
+  }
+  __syncthreads();
+  const int base = tile * SORT_TILE + warp * SUB;
+  unsigned keyv[SUB / 32];
+  int valv[SUB / 32];
+  unsigned rank[SUB / 32];
+  const unsigned lt = (1u << lane) - 1u;
+  if (warp < WARPS)
+    for (int r = 0; r < SUB / 32; r ++)
+    {
+      int s = base + r * 32 + lane;
+      bool ok = s < n;
+      unsigned key = ok ? ksrc[s] : 0xffffffffu;
+      int val = ok ? vsrc[s] : -1;
+      unsigned dig = ok ? (key >> shift) & 255u : 256u;      // 256: padding lane, never stored
+      unsigned peers = __match_any_sync(0xffffffffu, dig);
+      unsigned before = __popc(peers & lt);
+      unsigned prev = ok ? wcnt[warp][dig] : 0u;
+      __syncwarp();
+      if (ok && before == 0) wcnt[warp][dig] = prev + __popc(peers);
+      __syncwarp();
+      keyv[r] = key;
+      valv[r] = ok ? val : -1;
+      rank[r] = prev + before;
+    }
+  __syncthreads();
+  if (t < SORT_THREADS)
+  {
+    unsigned run = 0;
+    for (int w = 0; w < WARPS; w ++)
+    {
+      unsigned c = wcnt[w][t];
+      wcnt[w][t] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  if (warp < WARPS)
+    for (int r = 0; r < SUB / 32; r ++)
+    {
+      int s = base + r * 32 + lane;
+      if (s >= n) continue;
+      unsigned dig = (keyv[r] >> shift) & 255u;
+      unsigned pos = goff[dig] + wcnt[warp][dig] + rank[r];
+      kdst[pos] = keyv[r];
+      vdst[pos] = valv[r];
+    }
+  __syncthreads();
+}
+
+// ================================================================ candidate-list rebuild
+// 0. clear the cell ranges of the previous sort
+__device__ __forceinline__ void rb_clear_item(const PgDev &d, int s)
+{
+  unsigned key = d.keys[0][s];
+  if (key == 0xffffffffu) return;          // entries of no scene own no cell
+  d.cstart[key] = 0;
+  d.cend[key] = 0;
+}
+
+// triangle reference vertices and widened float AABBs
+__device__ __forceinline__ void rb_tref_item(const PgDev &d, int t)
+{
+  for (int k = 0; k < 9; k ++) d.tref[k][t] = d.tri[k][t];
+  for (int c = 0; c < 3; c ++)
+  {
+    double lo = fmin(fmin(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
+    double hi = fmax(fmax(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
+    d.tbox[(size_t)c * d.trinum + t] = __double2float_rd(lo);
+    d.tbox[(size_t)(3+c) * d.trinum + t] = __double2float_ru(hi);
+  }
+}
+
+// 3. cell ranges
+__device__ __forceinline__ void rb_ranges_item(const PgDev &d, int s)
+{
+  const int n = d.ellnum;
+  unsigned key = d.keys[0][s];
+  if (key == 0xffffffffu) return;
+  if (s == 0 || d.keys[0][s-1] != key) d.cstart[key] = s;
+  if (s == n-1 || d.keys[0][s+1] != key) d.cend[key] = s + 1;
+}
+
+// 4. candidate list of sphere i with carried contact state
+__device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
+{
+  const int E = d.ellnum;
+  int codes[MAXKN];
+  int n = 0, nover = 0, ntri = 0;
+  bool over = false;
+  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
+  const double ri = d.radii[0][i];
+  const int pi = d.part[i];
+  const int sc = d.escene[i];
+  const bool live = sc >= 0 && d.sactive[sc] != 0;
+  if (!live) return;
+  {
+    const unsigned prefix = (unsigned)sc << (3 * d.bits);
+    int u[3];
+    cell_of(d, sc, c, u);
+    for (int dz = -1; dz <= 1; dz ++)
+      for (int dy = -1; dy <= 1; dy ++)
+        for (int dx = -1; dx <= 1; dx ++)
+        {
+          int x = u[0]+dx, y = u[1]+dy, z = u[2]+dz;
+          if (x < 0 || y < 0 || z < 0 || x >= d.dim[0] || y >= d.dim[1] || z >= d.dim[2]) continue;
+          unsigned key = prefix | morton(x, y, z);
+          int b = d.cstart[key], e = d.cend[key];
+          for (int s = b; s < e; s ++)
+          {
+            int j = d.vals[0][s];
+            if ((unsigned)j >= (unsigned)E || d.part[j] <= pi) continue;
+            double q0 = c[0] - d.center[0][j], q1 = c[1] - d.center[1][j], q2 = c[2] - d.center[2][j];
+            double lim = ri + d.radii[0][j] + d.skin;
+            if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
+            {
+              if (n < d.kn) codes[n ++] = j;
+              else { over = true; nover ++; }
+            }
+          }
+        }
+    // insertion sort of the sphere partners
+    for (int a = 1; a < n; a ++)
+    {
+      int v = codes[a], b = a - 1;
+      while (b >= 0 && codes[b] > v) { codes[b+1] = codes[b]; b --; }
+      codes[b+1] = v;
+    }
+    // triangles of the sphere's scene within r + skin (AABB in float, then the
+    // true closest-point distance)
+    const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
+    const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
+    const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
+    const int T = d.trinum;
+    for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++)
+    {
+      if (d.tbox[t] > chi[0] || d.tbox[(size_t)3 * T + t] < clo[0] ||
+          d.tbox[(size_t)T + t] > chi[1] || d.tbox[(size_t)4 * T + t] < clo[1] ||
+          d.tbox[(size_t)2 * T + t] > chi[2] || d.tbox[(size_t)5 * T + t] < clo[2]) continue;
+      double A[3], B[3], C[3], pnt[3], nrm[3];
+      for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
+      // the candidate test uses the true closest point: the reference's region
+      // formula can only report a larger distance, so this set stays a superset
+      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, false);
+      if (!(depth > -d.skin) && !(depth != depth)) continue;
+      ntri ++;
+      if (n < d.kn) codes[n ++] = -(t + 1);
+      else { over = true; nover ++; }
+    }
+  }
+  if (over) set_err(d, PG_ERR_CAPACITY, 1, i, n + nover);
+  atomicMax(&d.stats[1], n + nover);
+  atomicMax(&d.stats[3], ntri);
+
+  // merge with the previous list (both in partner order)
+  const int nold = d.ncnt[i];
+  int ocode[MAXKN];
+  unsigned char oflag[MAXKN];
+  double ost[3][MAXKN];
+  // the tangential state lives in the FP64 arrays (FP64 form) or the FP32
+  // arrays (mixed form); it moves with its contact either way
+  const bool mixed = d.form == PG_FORM_MIXED;
+  for (int k = 0; k < nold; k ++)
+  {
+    size_t idx = (size_t)k * E + i;
+    ocode[k] = d.ncode[idx];
+    oflag[k] = d.nflag[idx];
+    for (int c = 0; c < 3; c ++) ost[c][k] = mixed ? (double)d.nstate_f[c][idx] : d.nstate[c][idx];
+  }
+  int o = 0;
+  for (int k = 0; k < n; k ++)
+  {
+    unsigned key = order_key(codes[k]);
+    while (o < nold && order_key(ocode[o]) < key) o ++;
+    size_t idx = (size_t)k * E + i;
+    d.ncode[idx] = codes[k];
+    const bool kept = o < nold && ocode[o] == codes[k];
+    d.nflag[idx] = kept ? oflag[o] : 0;
+    for (int c = 0; c < 3; c ++)
+    {
+      double st = kept ? ost[c][o] : 0.0;
+      if (mixed) d.nstate_f[c][idx] = (float)st;
+      else d.nstate[c][idx] = st;
+    }
+  }
+  d.ncnt[i] = n;
+}
+
+// 5. slave lists: clear, fill, sort by (master particle, master slot)
+__device__ __forceinline__ void rb_rzero_item(const PgDev &d, int p) { d.rcnt[p] = 0; }
+
+__device__ __forceinline__ void rb_rfill_item(const PgDev &d, int i)
+{
+  const int E = d.ellnum;
+  const int n = d.ncnt[i];
+  for (int k = 0; k < n; k ++)
+  {
+    int code = d.ncode[(size_t)k * E + i];
+    int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
+    if (pj < 0 || pj >= d.parnum) continue;
+    int r = atomicAdd(&d.rcnt[pj], 1);
+    if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
+    else set_err(d, PG_ERR_CAPACITY, 3, pj, r + 1);
+  }
+}
+
+__device__ __forceinline__ void rb_rsort_item(const PgDev &d, int p)
+{
+  const int P = d.parnum, E = d.ellnum;
+  int n = d.rcnt[p];
+  atomicMax(&d.stats[2], n);
+  if (n > d.kr) { n = d.kr; d.rcnt[p] = n; }
+  unsigned long long key[MAXKN];
+  int ref[MAXKN];
+  for (int r = 0; r < n; r ++)
+  {
+    int v = d.rref[(size_t)r * P + p];
+    int i = v % E, k = v / E;
+    key[r] = ((unsigned long long)(unsigned)d.part[i] << 32) | (unsigned)k;
+    ref[r] = v;
+  }
+  for (int a = 1; a < n; a ++)
+  {
+    unsigned long long kv = key[a];
+    int rv = ref[a], b = a - 1;
+    while (b >= 0 && key[b] > kv) { key[b+1] = key[b]; ref[b+1] = ref[b]; b --; }
+    key[b+1] = kv;
+    ref[b+1] = rv;
+  }
+  for (int r = 0; r < n; r ++) d.rref[(size_t)r * P + p] = ref[r];
+}
+
+// end of a rebuild (one thread)
+__device__ __forceinline__ void rb_done_item(const PgDev &d)
+{
+  if (*d.rebuild)
+  {
+    *d.rebuild = 0;
+    d.stats[0] += 1;
+  }
+}
+
+// ================================================================ per-step scene state
+// gravity of scene sc for this step: the step table's row, or the scene's
+// base excitation g0 + dir * sum_k amp_k sin(2 pi freq_k t + phase_k) at its
+// local time t = (global step - start step) * step.  Written with explicit
+// round-to-nearest operations: the same bits whether or not the compiler
+// contracts multiply-adds.
+__device__ __forceinline__ void excite_item(const PgDev &d, int sc, double step)
+{
+  const double *tab = d.t_gravity + 3*(size_t)(*d.stepno);
+  if (!d.sexc_on[sc])
+  {
+    d.sgrav[3*sc] = tab[0]; d.sgrav[3*sc+1] = tab[1]; d.sgrav[3*sc+2] = tab[2];
+    return;
+  }
+  const double *e = d.sexc + (size_t)PG_EXC_LEN * sc;
+  const double t = __dmul_rn((double)(*d.gstep - d.sstart[sc]), step);
+  int nk = (int)e[6];
+  if (nk > 8) nk = 8;
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  double sum = 0.0;
+  for (int k = 0; k < nk; k ++)
+    sum = __dadd_rn(sum, __dmul_rn(e[8+3*k], sin(__dadd_rn(__dmul_rn(__dmul_rn(two_pi, e[9+3*k]), t), e[10+3*k]))));
+  d.sgrav[3*sc] = __dadd_rn(e[0], __dmul_rn(e[3], sum));
+  d.sgrav[3*sc+1] = __dadd_rn(e[1], __dmul_rn(e[4], sum));
+  d.sgrav[3*sc+2] = __dadd_rn(e[2], __dmul_rn(e[5], sum));
+}
+
+// obstacle triangle t moved by its obstacle's velocities (obstacles.ispc:28-78):
+// the row of the step table (use_row) or the current obsang/obslin state.
+// Returns whether a vertex left its rebuild neighbourhood.
+__device__ __forceinline__ bool obstacles_item(const PgDev &d, int t, double step, int use_row)
+{
+  bool need = false;
+  int o = d.triown[t];
+  if (o >= 0 && d.tscene[t] >= 0 && d.sactive[d.tscene[t]])
+  {
+    const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+    const double *ang, *lin;
+    if (use_row)
+    {
+      int row = *d.stepno;
+      ang = d.t_obs_ang + (size_t)row * d.tab_obs_stride + 3*o;
+      lin = d.t_obs_lin + (size_t)row * d.tab_obs_stride + 3*o;
+    }
+    else
+    {
+      ang = d.obsang + 3*o;
+      lin = d.obslin + 3*o;
+    }
+    const double *x = d.obspnt + 3*o;
+    double y[3], DL[9], z[3];
+    y[0] = x[0] + step*lin[0];
+    y[1] = x[1] + step*lin[1];
+    y[2] = x[2] + step*lin[2];
+    pg::expmap(step*ang[0], step*ang[1], step*ang[2], DL, typo);
+    for (int v = 0; v < 3; v ++)
+    {
+      z[0] = d.tri[3*v+0][t] - x[0];
+      z[1] = d.tri[3*v+1][t] - x[1];
+      z[2] = d.tri[3*v+2][t] - x[2];
+      double n0 = DL[0]*z[0]+DL[3]*z[1]+DL[6]*z[2] + y[0];
+      double n1 = DL[1]*z[0]+DL[4]*z[1]+DL[7]*z[2] + y[1];
+      double n2 = DL[2]*z[0]+DL[5]*z[1]+DL[8]*z[2] + y[2];
+      d.tri[3*v+0][t] = n0;
+      d.tri[3*v+1][t] = n1;
+      d.tri[3*v+2][t] = n2;
+      double r0 = n0 - d.tref[3*v+0][t], r1 = n1 - d.tref[3*v+1][t], r2 = n2 - d.tref[3*v+2][t];
+      need |= (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
+    }
+  }
+  return need;
+}
+
+// obstacle points (after every triangle used the old point), obstacle
+// velocity state, and the step counters (one thread)
+__device__ __forceinline__ void tail_item(const PgDev &d, double step, int use_row)
+{
+  int row = use_row ? *d.stepno : 0;
+  for (int o = 0; o < d.obsnum; o ++)
+  {
+    if (d.oscene[o] < 0 || !d.sactive[d.oscene[o]]) continue;
+    if (use_row)
+      for (int k = 0; k < 3; k ++)
+      {
+        d.obsang[3*o+k] = d.t_obs_ang[(size_t)row * d.tab_obs_stride + 3*o + k];
+        d.obslin[3*o+k] = d.t_obs_lin[(size_t)row * d.tab_obs_stride + 3*o + k];
+      }
+    double *x = d.obspnt + 3*o;
+    const double *v = d.obslin + 3*o;
+    double y0 = x[0] + step*v[0], y1 = x[1] + step*v[1], y2 = x[2] + step*v[2];
+    x[0] = y0; x[1] = y1; x[2] = y2;
+  }
+  if (use_row)
+  {
+    *d.stepno = row + 1;
+    *d.gstep += 1;
+  }
+}
+
+} // namespace pgk

@@ -26,6 +26,11 @@ void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s);
 void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0 = 0, int p1 = -1);
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step);
+// the persistent fused step of the mixed form: shape index into the kernel
+// table, threads per block and blocks of the cooperative grid
+struct PgFusedCfg { int shape, threads, blocks; };
+int  pg_fused_candidates(PgFusedCfg *out, int cap);
+cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int nsteps, const PgFusedCfg &c);
 
 // pg_session.cu
 void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &ev);

@@ -19,6 +19,7 @@
 #include "pg_math.cuh"
 #include "pg_df.cuh"
 #include "pg_launch.h"
+#include "pg_items.cuh"
 #include "../../include/parmec_gb300.h"
 
 using namespace pg;
@@ -168,11 +169,9 @@ __global__ void k_mx_to64(PgDev d, int p0, int p1)
 }
 
 // ------------------------------------------------------------ contacts
-__global__ void __launch_bounds__(TPB) k_contacts_mx(PgDev d, double step_d)
+__device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double step_d)
 {
   const int E = d.ellnum;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
   const int pi = d.part[i];
   const int cnt = d.ncnt[i];
   float fs[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
@@ -326,12 +325,18 @@ __global__ void __launch_bounds__(TPB) k_contacts_mx(PgDev d, double step_d)
   for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
 }
 
-// ------------------------------------------------------------ integrate
-__global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
+__global__ void __launch_bounds__(TPB) k_contacts_mx(PgDev d, double step_d)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.ellnum) mx_contacts_item(d, i, step_d);
+}
+
+// ------------------------------------------------------------ integrate
+// returns whether the particle's sphere left its rebuild neighbourhood
+__device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double step_d)
+{
   bool need = false;
-  if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
+  if (d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
     double grav[3];
@@ -473,10 +478,198 @@ __global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
       need = dd > (float)d.half_skin_sq;
     }
   }
+  return need;
+}
+
+__global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < d.parnum) need = mx_integrate_item(d, i, step_d);
   if (d.ellnum) flag_rebuild(d, need);
 }
 
+// ------------------------------------------------------------ persistent fused step
+// One cooperatively launched grid runs whole steps of the mixed form:
+//   [rebuild, when flagged: clear | keys | radix sort passes | ranges |
+//    candidate lists | slave lists]
+//   excitation + contacts | integration + obstacles | tail
+// with a grid barrier at each '|'.  Every block walks the items of a phase in
+// a grid-stride loop; the item bodies are the ones the per-phase kernels run,
+// so the results do not depend on the launch shape.
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// barrier of all blocks of a cooperative grid.  d.gbar = {arrivals,
+// generation, abort}.  A block that waits more than 2 s records
+// PG_ERR_TIMEOUT and raises abort; every block then leaves the kernel.
+__device__ bool grid_barrier(const PgDev &d)
+{
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    volatile unsigned *b = d.gbar;
+    int ok = 1;
+    const unsigned gen = b[1];
+    __threadfence();
+    if (b[2] != 0u) ok = 0;
+    else
+    {
+      const unsigned arrived = atomicAdd(d.gbar, 1u) + 1u;
+      if (arrived == gridDim.x)
+      {
+        atomicExch(d.gbar, 0u);
+        __threadfence();
+        atomicAdd(d.gbar + 1, 1u);
+      }
+      else
+      {
+        const unsigned long long t0 = global_ns();
+        while (b[1] == gen)
+        {
+          if (b[2] != 0u) { ok = 0; break; }
+          if (global_ns() - t0 > 2000000000ull)
+          {
+            atomicExch(d.gbar + 2, 1u);
+            set_err(d, PG_ERR_TIMEOUT, 20, blockIdx.x, 0);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <int B, int MINB>
+__global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int nsteps, int passes)
+{
+  __shared__ union
+  {
+    unsigned h[256];
+    struct { unsigned wcnt[pgk::SORT_THREADS / 32][256]; unsigned goff[256]; } sc;
+    unsigned part[B];
+  } sm;
+  const int gsz = gridDim.x * B;
+  const int g0 = blockIdx.x * B + threadIdx.x;
+  const int E = d.ellnum, P = d.parnum, T = d.trinum;
+  for (int it = 0; it < nsteps; it ++)
+  {
+    if (E && *(volatile int *)d.rebuild)
+    {
+      for (int s = g0; s < E; s += gsz) pgk::rb_clear_item(d, s);
+      for (int t = g0; t < T; t += gsz) pgk::rb_tref_item(d, t);
+      if (!grid_barrier(d)) return;
+      pgk::Grid g;
+      for (int k = 0; k < 3; k ++) { g.org[k] = 0.0; g.dim[k] = d.dim[k]; }
+      g.cell = d.cell;
+      for (int i = g0; i < E; i += gsz)
+        pgk::cell_keys_item(i, d.center[0], d.center[1], d.center[2], g, d.escene, d.sorg[0], d.sorg[1], d.sorg[2],
+                            3 * d.bits, d.keys[0], d.vals[0], d.cref[0], d.cref[1], d.cref[2]);
+      if (!grid_barrier(d)) return;
+      const int nb = d.nsortblocks;
+      for (int p = 0; p < passes; p ++)
+      {
+        unsigned *ks = (p & 1) ? d.keys[1] : d.keys[0], *kd = (p & 1) ? d.keys[0] : d.keys[1];
+        int *vs = (p & 1) ? d.vals[1] : d.vals[0], *vd = (p & 1) ? d.vals[0] : d.vals[1];
+        for (int tile = blockIdx.x; tile < nb; tile += gridDim.x)
+          pgk::sort_hist_tile(ks, E, d.hist, nb, 8 * p, tile, sm.h);
+        if (!grid_barrier(d)) return;
+        if (blockIdx.x == 0) pgk::sort_scan_block(d.hist, nb, sm.part);
+        if (!grid_barrier(d)) return;
+        for (int tile = blockIdx.x; tile < nb; tile += gridDim.x)
+          pgk::sort_scatter_tile(ks, vs, kd, vd, E, d.hist, nb, 8 * p, tile, sm.sc.wcnt, sm.sc.goff);
+        if (!grid_barrier(d)) return;
+      }
+      for (int s = g0; s < E; s += gsz) pgk::rb_ranges_item(d, s);
+      for (int p = g0; p < P; p += gsz) pgk::rb_rzero_item(d, p);
+      if (!grid_barrier(d)) return;
+      for (int i = g0; i < E; i += gsz) pgk::rb_verlet_item(d, i);
+      if (!grid_barrier(d)) return;
+      for (int i = g0; i < E; i += gsz) pgk::rb_rfill_item(d, i);
+      if (!grid_barrier(d)) return;
+      for (int p = g0; p < P; p += gsz) pgk::rb_rsort_item(d, p);
+      if (blockIdx.x == 0 && threadIdx.x == 0) pgk::rb_done_item(d);
+      if (!grid_barrier(d)) return;
+    }
+    // excitation and contacts: contacts do not read the scene gravity
+    for (int sc = g0; sc < d.nscene; sc += gsz) pgk::excite_item(d, sc, step);
+    for (int i = g0; i < E; i += gsz) mx_contacts_item(d, i, step);
+    if (!grid_barrier(d)) return;
+    // integration and obstacle triangles touch disjoint state
+    bool need = false;
+    for (int i = g0; i < P; i += gsz) need |= mx_integrate_item(d, i, step);
+    for (int t = g0; t < T; t += gsz) need |= pgk::obstacles_item(d, t, step, 1);
+    if (__syncthreads_or(need) && threadIdx.x == 0 && E) atomicExch(d.rebuild, 1);
+    if (!grid_barrier(d)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) pgk::tail_item(d, step, 1);
+    if (!grid_barrier(d)) return;
+  }
+}
+
+typedef void (*FusedKernel)(PgDev, double, int, int);
+
+// the launch shapes the autotuner may pick from (threads, minimum blocks per SM)
+struct FusedShape { int threads, minb; FusedKernel k; };
+const FusedShape fused_shapes[] = {
+  {256, 1, k_fused_mx<256, 1>}, {256, 2, k_fused_mx<256, 2>}, {256, 3, k_fused_mx<256, 3>},
+  {512, 1, k_fused_mx<512, 1>}, {512, 2, k_fused_mx<512, 2>},
+};
+constexpr int n_fused_shapes = sizeof(fused_shapes) / sizeof(fused_shapes[0]);
+
 } // namespace
+
+// candidate launch configurations: every shape at every blocks-per-SM count up
+// to its occupancy limit (cooperative launches need all blocks resident)
+int pg_fused_candidates(PgFusedCfg *out, int cap)
+{
+  int dev = 0, sms = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  for (int k = 0; k < n_fused_shapes; k ++)
+  {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_shapes[k].k, fused_shapes[k].threads, 0)
+        != cudaSuccess) { cudaGetLastError(); continue; }
+    for (int b = 1; b <= per_sm && b <= 4; b ++)
+    {
+      if (b < fused_shapes[k].minb) continue;
+      if (n < cap) out[n] = {k, fused_shapes[k].threads, b * sms};
+      n ++;
+    }
+  }
+  return n < cap ? n : cap;
+}
+
+cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int nsteps, const PgFusedCfg &c)
+{
+  if (c.shape < 0 || c.shape >= n_fused_shapes || c.blocks < 1) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(d.gbar, 0, 4 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  const int passes = pg_sort_passes_bits(pg_rebuild_sort_bits(d));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.blocks);
+  cfg.blockDim = dim3(fused_shapes[c.shape].threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fused_shapes[c.shape].k, d, step, nsteps, passes);
+}
 
 void pg_launch_mx_from64(const PgDev &d, cudaStream_t s, int p0, int p1, int e0, int e1)
 {

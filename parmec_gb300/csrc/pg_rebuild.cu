@@ -24,271 +24,69 @@
 #include "pg_state.h"
 #include "pg_math.cuh"
 #include "pg_launch.h"
+#include "pg_items.cuh"
 #include "../../include/parmec_gb300.h"
 
 namespace {
 
 constexpr int TPB = 128;
-constexpr int MAXKN = 96;                               // upper bound of slots per sphere
 
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
-// record the first error with where it happened (site), the index and a value
-__device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
-{
-  if (atomicCAS(d.err, 0, code) == 0)
-  {
-    d.err[1] = site;
-    d.err[2] = index;
-    d.err[3] = value;
-  }
-}
+using namespace pgk;
 
-__device__ __forceinline__ unsigned spread3(unsigned x)
-{
-  x &= 0x3ff;
-  x = (x | (x << 16)) & 0x030000FF;
-  x = (x | (x << 8)) & 0x0300F00F;
-  x = (x | (x << 4)) & 0x030C30C3;
-  x = (x | (x << 2)) & 0x09249249;
-  return x;
-}
-
-__device__ __forceinline__ void cell_of(const PgDev &d, int scene, const double *c, int *u)
-{
-  for (int k = 0; k < 3; k ++)
-  {
-    double f = floor((c[k] - d.sorg[k][scene]) / d.cell);
-    if (!(f >= 0.0)) f = 0.0;                 // also catches NaN
-    if (f > (double)(d.dim[k] - 1)) f = (double)(d.dim[k] - 1);
-    u[k] = (int)f;
-  }
-}
-
-__device__ __forceinline__ unsigned morton(int x, int y, int z)
-{
-  return spread3((unsigned)x) | (spread3((unsigned)y) << 1) | (spread3((unsigned)z) << 2);
-}
-
-// ---- 0. clear the cell ranges of the previous sort
 __global__ void k_rb_clear(PgDev d)
 {
   if (!*d.rebuild) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.ellnum) return;
-  unsigned key = d.keys[0][s];
-  if (key == 0xffffffffu) return;          // entries of no scene own no cell
-  d.cstart[key] = 0;
-  d.cend[key] = 0;
+  if (s < d.ellnum) rb_clear_item(d, s);
 }
 
-// ---- triangle reference vertices and widened float AABBs
 __global__ void k_rb_tref(PgDev d)
 {
   if (!*d.rebuild) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= d.trinum) return;
-  for (int k = 0; k < 9; k ++) d.tref[k][t] = d.tri[k][t];
-  for (int c = 0; c < 3; c ++)
-  {
-    double lo = fmin(fmin(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
-    double hi = fmax(fmax(d.tri[c][t], d.tri[3+c][t]), d.tri[6+c][t]);
-    d.tbox[(size_t)c * d.trinum + t] = __double2float_rd(lo);
-    d.tbox[(size_t)(3+c) * d.trinum + t] = __double2float_ru(hi);
-  }
+  if (t < d.trinum) rb_tref_item(d, t);
 }
 
-// ---- 3. cell ranges
 __global__ void k_rb_ranges(PgDev d)
 {
   if (!*d.rebuild) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = d.ellnum;
-  if (s >= n) return;
-  unsigned key = d.keys[0][s];
-  if (key == 0xffffffffu) return;
-  if (s == 0 || d.keys[0][s-1] != key) d.cstart[key] = s;
-  if (s == n-1 || d.keys[0][s+1] != key) d.cend[key] = s + 1;
+  if (s < d.ellnum) rb_ranges_item(d, s);
 }
 
-__device__ __forceinline__ unsigned order_key(int code)
-{
-  return code >= 0 ? (unsigned)code : 0x80000000u + (unsigned)(-code - 1);
-}
-
-// ---- 4. candidate lists with carried contact state
 __global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
 {
   if (!*d.rebuild) return;
-  const int E = d.ellnum;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
-  int codes[MAXKN];
-  int n = 0, nsph = 0, nover = 0, ntri = 0;
-  bool over = false;
-  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
-  const double ri = d.radii[0][i];
-  const int pi = d.part[i];
-  const int sc = d.escene[i];
-  const bool live = sc >= 0 && d.sactive[sc] != 0;
-  if (live)
-  {
-    const unsigned prefix = (unsigned)sc << (3 * d.bits);
-    int u[3];
-    cell_of(d, sc, c, u);
-    for (int dz = -1; dz <= 1; dz ++)
-      for (int dy = -1; dy <= 1; dy ++)
-        for (int dx = -1; dx <= 1; dx ++)
-        {
-          int x = u[0]+dx, y = u[1]+dy, z = u[2]+dz;
-          if (x < 0 || y < 0 || z < 0 || x >= d.dim[0] || y >= d.dim[1] || z >= d.dim[2]) continue;
-          unsigned key = prefix | morton(x, y, z);
-          int b = d.cstart[key], e = d.cend[key];
-          for (int s = b; s < e; s ++)
-          {
-            int j = d.vals[0][s];
-            if ((unsigned)j >= (unsigned)E || d.part[j] <= pi) continue;
-            double q0 = c[0] - d.center[0][j], q1 = c[1] - d.center[1][j], q2 = c[2] - d.center[2][j];
-            double lim = ri + d.radii[0][j] + d.skin;
-            if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
-            {
-              if (n < d.kn) codes[n ++] = j;
-              else { over = true; nover ++; }
-            }
-          }
-        }
-    // insertion sort of the sphere partners
-    for (int a = 1; a < n; a ++)
-    {
-      int v = codes[a], b = a - 1;
-      while (b >= 0 && codes[b] > v) { codes[b+1] = codes[b]; b --; }
-      codes[b+1] = v;
-    }
-    nsph = n;
-    // triangles of the sphere's scene within r + skin (AABB in float, then the
-    // true closest-point distance)
-    const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
-    const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
-    const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
-    const int T = d.trinum;
-    for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++)
-    {
-      if (d.tbox[t] > chi[0] || d.tbox[(size_t)3 * T + t] < clo[0] ||
-          d.tbox[(size_t)T + t] > chi[1] || d.tbox[(size_t)4 * T + t] < clo[1] ||
-          d.tbox[(size_t)2 * T + t] > chi[2] || d.tbox[(size_t)5 * T + t] < clo[2]) continue;
-      double A[3], B[3], C[3], pnt[3], nrm[3];
-      for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
-      // the candidate test uses the true closest point: the reference's region
-      // formula can only report a larger distance, so this set stays a superset
-      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, false);
-      if (!(depth > -d.skin) && !(depth != depth)) continue;
-      ntri ++;
-      if (n < d.kn) codes[n ++] = -(t + 1);
-      else { over = true; nover ++; }
-    }
-  }
-  if (!live) return;
-  if (over) set_err(d, PG_ERR_CAPACITY, 1, i, n + nover);
-  atomicMax(&d.stats[1], n + nover);
-  atomicMax(&d.stats[3], ntri);
-
-  // merge with the previous list (both in partner order)
-  const int nold = d.ncnt[i];
-  int ocode[MAXKN];
-  unsigned char oflag[MAXKN];
-  double ost[3][MAXKN];
-  // the tangential state lives in the FP64 arrays (FP64 form) or the FP32
-  // arrays (mixed form); it moves with its contact either way
-  const bool mixed = d.form == PG_FORM_MIXED;
-  for (int k = 0; k < nold; k ++)
-  {
-    size_t idx = (size_t)k * E + i;
-    ocode[k] = d.ncode[idx];
-    oflag[k] = d.nflag[idx];
-    for (int c = 0; c < 3; c ++) ost[c][k] = mixed ? (double)d.nstate_f[c][idx] : d.nstate[c][idx];
-  }
-  int o = 0;
-  for (int k = 0; k < n; k ++)
-  {
-    unsigned key = order_key(codes[k]);
-    while (o < nold && order_key(ocode[o]) < key) o ++;
-    size_t idx = (size_t)k * E + i;
-    d.ncode[idx] = codes[k];
-    const bool kept = o < nold && ocode[o] == codes[k];
-    d.nflag[idx] = kept ? oflag[o] : 0;
-    for (int c = 0; c < 3; c ++)
-    {
-      double st = kept ? ost[c][o] : 0.0;
-      if (mixed) d.nstate_f[c][idx] = (float)st;
-      else d.nstate[c][idx] = st;
-    }
-  }
-  d.ncnt[i] = n;
-  (void)nsph;
+  if (i < d.ellnum) rb_verlet_item(d, i);
 }
 
-// ---- 5. slave lists
 __global__ void k_rb_rzero(PgDev d)
 {
   if (!*d.rebuild) return;
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < d.parnum) d.rcnt[p] = 0;
+  if (p < d.parnum) rb_rzero_item(d, p);
 }
 
 __global__ void k_rb_rfill(PgDev d)
 {
   if (!*d.rebuild) return;
-  const int E = d.ellnum;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
-  const int n = d.ncnt[i];
-  for (int k = 0; k < n; k ++)
-  {
-    int code = d.ncode[(size_t)k * E + i];
-    int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
-    if (pj < 0 || pj >= d.parnum) continue;
-    int r = atomicAdd(&d.rcnt[pj], 1);
-    if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
-    else set_err(d, PG_ERR_CAPACITY, 3, pj, r + 1);
-  }
+  if (i < d.ellnum) rb_rfill_item(d, i);
 }
 
 __global__ void k_rb_rsort(PgDev d)
 {
   if (!*d.rebuild) return;
-  const int P = d.parnum, E = d.ellnum;
   int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  int n = d.rcnt[p];
-  atomicMax(&d.stats[2], n);
-  if (n > d.kr) { n = d.kr; d.rcnt[p] = n; }
-  unsigned long long key[MAXKN];
-  int ref[MAXKN];
-  for (int r = 0; r < n; r ++)
-  {
-    int v = d.rref[(size_t)r * P + p];
-    int i = v % E, k = v / E;
-    key[r] = ((unsigned long long)(unsigned)d.part[i] << 32) | (unsigned)k;
-    ref[r] = v;
-  }
-  for (int a = 1; a < n; a ++)
-  {
-    unsigned long long kv = key[a];
-    int rv = ref[a], b = a - 1;
-    while (b >= 0 && key[b] > kv) { key[b+1] = key[b]; ref[b+1] = ref[b]; b --; }
-    key[b+1] = kv;
-    ref[b+1] = rv;
-  }
-  for (int r = 0; r < n; r ++) d.rref[(size_t)r * P + p] = ref[r];
+  if (p < d.parnum) rb_rsort_item(d, p);
 }
 
 __global__ void k_rb_done(PgDev d)
 {
-  if (threadIdx.x == 0 && blockIdx.x == 0 && *d.rebuild)
-  {
-    *d.rebuild = 0;
-    d.stats[0] += 1;
-  }
+  if (threadIdx.x == 0 && blockIdx.x == 0) rb_done_item(d);
 }
 
 // ---- gate of the drop-in condet(): a rebuild is due when a sphere centre or

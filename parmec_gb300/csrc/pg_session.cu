@@ -39,6 +39,18 @@ struct pg_session
   cudaGraphExec_t graph_exec = nullptr;
   double graph_step = 0.0;
   int use_graph = 1;
+  // persistent fused step (mixed form): launch shape, autotuner state and
+  // the captured graph of one chunk of fstep_chunk steps
+  int fused = 0, tune = 0, tuned = 0, warmed = 0;
+  PgFusedCfg fcfg = {-1, 0, 0};
+  std::vector<PgFusedCfg> cands;
+  std::vector<double> cand_ms;
+  int cand_next = 0, cand_round = 0;
+  cudaGraph_t fgraph = nullptr;
+  cudaGraphExec_t fgraph_exec = nullptr;
+  double fgraph_step = 0.0;
+  int fgraph_chunk = 0, fgraph_ok = 1;
+  long long fused_launches = 0;
 };
 
 // spring force flush events per particle (CSR 'first' over particles), in
@@ -206,6 +218,7 @@ int allocate(pg_session *s, const pg_scene *sc)
   TRY(dalloc(s, &d.sgrav, 3 * NS));
   TRY(dalloc(s, &d.sstart, NS));
   TRY(dalloc(s, &d.gstep, 1));
+  TRY(dalloc(s, &d.gbar, 4));
   return PG_OK;
 }
 
@@ -648,6 +661,125 @@ void drop_graph(pg_session *s)
   if (s->graph) cudaGraphDestroy(s->graph);
   s->graph_exec = nullptr;
   s->graph = nullptr;
+  if (s->fgraph_exec) cudaGraphExecDestroy(s->fgraph_exec);
+  if (s->fgraph) cudaGraphDestroy(s->fgraph);
+  s->fgraph_exec = nullptr;
+  s->fgraph = nullptr;
+}
+
+// the fused kernel for 'n' steps, as a captured graph of 'chunk' steps per
+// replay when capture works, else as direct cooperative launches
+int run_fused(pg_session *s, double step, int n, int chunk)
+{
+  const PgDev &d = s->d;
+  if (n <= 0) return PG_OK;
+  if (s->use_graph && s->fgraph_ok && n >= chunk)
+  {
+    if (!s->fgraph_exec || s->fgraph_step != step || s->fgraph_chunk != chunk)
+    {
+      if (s->fgraph_exec) cudaGraphExecDestroy(s->fgraph_exec);
+      if (s->fgraph) cudaGraphDestroy(s->fgraph);
+      s->fgraph_exec = nullptr;
+      s->fgraph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess)
+      {
+        cudaError_t el = pg_launch_fused_mx(d, s->stream, step, chunk, s->fcfg);
+        e = cudaStreamEndCapture(s->stream, &s->fgraph);
+        if (el != cudaSuccess) e = el;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&s->fgraph_exec, s->fgraph, 0);
+      if (e != cudaSuccess)
+      {
+        // capture of a cooperative launch not available: launch directly
+        cudaGetLastError();
+        if (s->fgraph) cudaGraphDestroy(s->fgraph);
+        s->fgraph = nullptr;
+        s->fgraph_exec = nullptr;
+        s->fgraph_ok = 0;
+      }
+      else
+      {
+        s->fgraph_step = step;
+        s->fgraph_chunk = chunk;
+      }
+    }
+    if (s->fgraph_exec)
+    {
+      const int reps = n / chunk;
+      for (int k = 0; k < reps; k ++) CK(cudaGraphLaunch(s->fgraph_exec, s->stream));
+      s->fused_launches += reps;
+      n -= reps * chunk;
+    }
+  }
+  if (n > 0)
+  {
+    CK(pg_launch_fused_mx(d, s->stream, step, n, s->fcfg));
+    s->fused_launches += 1;
+  }
+  return PG_OK;
+}
+
+// the fused path of pg_session_run: the first steps of a tuning session time
+// every candidate launch shape (the results do not depend on the shape), the
+// rest run with the fastest
+int run_fused_steps(pg_session *s, double step, int n)
+{
+  int done = 0;
+  if (s->tune && !s->tuned)
+  {
+    if (s->cands.empty())
+    {
+      PgFusedCfg buf[32];
+      const int m = pg_fused_candidates(buf, 32);
+      if (m <= 0) return PG_ERR_CUDA;
+      s->cands.assign(buf, buf + m);
+      s->cand_ms.assign(m, 1e30);
+      s->cand_next = 0;
+      s->cand_round = 0;
+    }
+    if (!s->warmed && done < n)
+    {
+      // an untimed step: the first rebuild and cold caches
+      CK(pg_launch_fused_mx(s->d, s->stream, step, 1, s->cands[0]));
+      s->fused_launches += 1;
+      done += 1;
+      s->warmed = 1;
+    }
+    const int trial = 3;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    while (!s->tuned && done + trial <= n)
+    {
+      const PgFusedCfg &c = s->cands[s->cand_next];
+      CK(cudaEventRecord(e0, s->stream));
+      CK(pg_launch_fused_mx(s->d, s->stream, step, trial, c));
+      CK(cudaEventRecord(e1, s->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      s->fused_launches += 1;
+      s->cand_ms[s->cand_next] = std::min(s->cand_ms[s->cand_next], (double)ms);
+      done += trial;
+      if (++ s->cand_next == (int)s->cands.size())
+      {
+        s->cand_next = 0;
+        if (++ s->cand_round == 2)
+        {
+          int best = 0;
+          for (int k = 1; k < (int)s->cands.size(); k ++) if (s->cand_ms[k] < s->cand_ms[best]) best = k;
+          s->fcfg = s->cands[best];
+          s->tuned = 1;
+          drop_graph(s);
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  if (s->fcfg.shape < 0) return PG_ERR_ARGUMENT;
+  return run_fused(s, step, n - done, 16);
 }
 
 void enqueue_step(pg_session *s, double step)
@@ -845,6 +977,15 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   TRY(put(d.t_obs_ang, tab->obs_ang, s->obs_stride));
   TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
   CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
+  if (s->fused && d.form == PG_FORM_MIXED && !s->profile)
+  {
+    const long long before = s->fused_launches;
+    TRY(run_fused_steps(s, step, n));
+    s->launches += s->fused_launches - before;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return PG_OK;
+  }
   const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d);
   if (!s->profile && s->use_graph)
   {
@@ -1119,6 +1260,46 @@ int pg_session_use_graph(pg_session *s, int on)
 {
   if (!s) return PG_ERR_ARGUMENT;
   s->use_graph = on ? 1 : 0;
+  return PG_OK;
+}
+
+int pg_session_use_fused(pg_session *s, int on)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  if (on && s->d.form != PG_FORM_MIXED) return PG_ERR_UNSUPPORTED;
+  CK(cudaStreamSynchronize(s->stream));
+  drop_graph(s);
+  s->fused = on ? 1 : 0;
+  if (on && s->fcfg.shape < 0)
+  {
+    // default before tuning: 256 threads, as many blocks as fit, fewest spills
+    PgFusedCfg buf[32];
+    const int m = pg_fused_candidates(buf, 32);
+    if (m <= 0) return PG_ERR_CUDA;
+    s->fcfg = buf[0];
+    for (int k = 0; k < m; k ++) if (buf[k].threads == 256 && buf[k].blocks > s->fcfg.blocks) s->fcfg = buf[k];
+  }
+  return PG_OK;
+}
+
+int pg_session_autotune(pg_session *s, int on)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  s->tune = on ? 1 : 0;
+  s->tuned = 0;
+  s->warmed = 0;
+  s->cands.clear();
+  s->cand_ms.clear();
+  return PG_OK;
+}
+
+int pg_session_fused_config(pg_session *s, int *out4)
+{
+  if (!s || !out4) return PG_ERR_ARGUMENT;
+  out4[0] = s->fcfg.threads;
+  out4[1] = s->fcfg.blocks;
+  out4[2] = s->tuned;
+  out4[3] = s->fgraph_ok && s->fgraph_exec ? 1 : 0;
   return PG_OK;
 }
 

@@ -84,6 +84,7 @@ struct PgDev
   // ---- rebuild machinery
   int *rebuild;             // 1 when the candidate lists must be rebuilt
   int *err;                 // [4]: first device error (PG_ERR_*), site, index, value; 0 when fine
+  unsigned *gbar;           // [4]: grid barrier of the fused step kernel: arrivals, generation, abort
   int *stats;               // [8]: rebuilds, max candidates, max slave entries, max triangles per sphere
   double skin, cell, half_skin_sq;
   double org[3];

@@ -15,6 +15,7 @@
 #include "pg_state.h"
 #include "pg_math.cuh"
 #include "pg_launch.h"
+#include "pg_items.cuh"
 #include "../../include/parmec_gb300.h"
 
 using namespace pg;
@@ -56,22 +57,7 @@ __device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double, co
 __global__ void k_excite(PgDev d, double step)
 {
   const int sc = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sc >= d.nscene) return;
-  const double *tab = d.t_gravity + 3*(size_t)(*d.stepno);
-  if (!d.sexc_on[sc])
-  {
-    d.sgrav[3*sc] = tab[0]; d.sgrav[3*sc+1] = tab[1]; d.sgrav[3*sc+2] = tab[2];
-    return;
-  }
-  const double *e = d.sexc + (size_t)PG_EXC_LEN * sc;
-  const double t = (double)(*d.gstep - d.sstart[sc]) * step;
-  int nk = (int)e[6];
-  if (nk > 8) nk = 8;
-  double sum = 0.0;
-  for (int k = 0; k < nk; k ++) sum += e[8+3*k] * sin(2.0 * 3.14159265358979323846 * e[9+3*k] * t + e[10+3*k]);
-  d.sgrav[3*sc] = e[0] + e[3] * sum;
-  d.sgrav[3*sc+1] = e[1] + e[4] * sum;
-  d.sgrav[3*sc+2] = e[2] + e[5] * sum;
+  if (sc < d.nscene) pgk::excite_item(d, sc, step);
 }
 
 // ---------------------------------------------------------------- invert (parmec.ispc:62-99)
@@ -174,46 +160,7 @@ __global__ void k_obstacles(PgDev d, double step, int use_row)
 {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
-  if (t < d.trinum)
-  {
-    int o = d.triown[t];
-    if (o >= 0 && d.tscene[t] >= 0 && d.sactive[d.tscene[t]])
-    {
-      const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
-      const double *ang, *lin;
-      if (use_row)
-      {
-        int row = *d.stepno;
-        ang = d.t_obs_ang + (size_t)row * d.tab_obs_stride + 3*o;
-        lin = d.t_obs_lin + (size_t)row * d.tab_obs_stride + 3*o;
-      }
-      else
-      {
-        ang = d.obsang + 3*o;
-        lin = d.obslin + 3*o;
-      }
-      const double *x = d.obspnt + 3*o;
-      double y[3], DL[9], z[3];
-      y[0] = x[0] + step*lin[0];
-      y[1] = x[1] + step*lin[1];
-      y[2] = x[2] + step*lin[2];
-      expmap(step*ang[0], step*ang[1], step*ang[2], DL, typo);
-      for (int v = 0; v < 3; v ++)
-      {
-        z[0] = d.tri[3*v+0][t] - x[0];
-        z[1] = d.tri[3*v+1][t] - x[1];
-        z[2] = d.tri[3*v+2][t] - x[2];
-        double n0 = DL[0]*z[0]+DL[3]*z[1]+DL[6]*z[2] + y[0];
-        double n1 = DL[1]*z[0]+DL[4]*z[1]+DL[7]*z[2] + y[1];
-        double n2 = DL[2]*z[0]+DL[5]*z[1]+DL[8]*z[2] + y[2];
-        d.tri[3*v+0][t] = n0;
-        d.tri[3*v+1][t] = n1;
-        d.tri[3*v+2][t] = n2;
-        double r0 = n0 - d.tref[3*v+0][t], r1 = n1 - d.tref[3*v+1][t], r2 = n2 - d.tref[3*v+2][t];
-        need |= (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
-      }
-    }
-  }
+  if (t < d.trinum) need = pgk::obstacles_item(d, t, step, use_row);
   if (d.ellnum) flag_rebuild(d, need);
 }
 
@@ -222,26 +169,7 @@ __global__ void k_obstacles(PgDev d, double step, int use_row)
 __global__ void k_tail(PgDev d, double step, int use_row)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int row = use_row ? *d.stepno : 0;
-  for (int o = 0; o < d.obsnum; o ++)
-  {
-    if (d.oscene[o] < 0 || !d.sactive[d.oscene[o]]) continue;
-    if (use_row)
-      for (int k = 0; k < 3; k ++)
-      {
-        d.obsang[3*o+k] = d.t_obs_ang[(size_t)row * d.tab_obs_stride + 3*o + k];
-        d.obslin[3*o+k] = d.t_obs_lin[(size_t)row * d.tab_obs_stride + 3*o + k];
-      }
-    double *x = d.obspnt + 3*o;
-    const double *v = d.obslin + 3*o;
-    double y0 = x[0] + step*v[0], y1 = x[1] + step*v[1], y2 = x[2] + step*v[2];
-    x[0] = y0; x[1] = y1; x[2] = y2;
-  }
-  if (use_row)
-  {
-    *d.stepno = row + 1;
-    *d.gstep += 1;
-  }
+  pgk::tail_item(d, step, use_row);
 }
 
 // ---------------------------------------------------------------- pairing (forces.ispc:98-122)

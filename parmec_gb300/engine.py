@@ -15,8 +15,12 @@ class GpuEngine:
     """Runs DEM steps of one Model in a pg_session on the current CUDA device."""
 
     def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False, graph=True,
-                 capacity=None):
+                 capacity=None, fused=False, autotune=False):
+        """fused: the mixed form's persistent step kernel (pg_session_use_fused);
+        autotune: pick its launch shape by timing the first steps."""
         self.lib = abi.load_library()
+        self.fused = fused
+        self.autotune = autotune
         self.graph = graph
         self.capacity = capacity
         self.form = form
@@ -45,6 +49,10 @@ class GpuEngine:
         if self.capacity is not None:
             abi.check(self.lib.pg_session_set_capacity(self.sess, int(self.capacity[0]), int(self.capacity[1])),
                       "pg_session_set_capacity")
+        if self.fused:
+            abi.check(self.lib.pg_session_use_fused(self.sess, 1), "pg_session_use_fused")
+            if self.autotune:
+                abi.check(self.lib.pg_session_autotune(self.sess, 1), "pg_session_autotune")
 
     def stale(self):
         return self.model is None or _counts(self.model) != self.counts
@@ -71,6 +79,12 @@ class GpuEngine:
     def download(self):
         abi.check(self.lib.pg_session_download(self.sess, ctypes.byref(self.scene)), "pg_session_download")
         self.model.pull_obstacles()
+
+    def fused_config(self):
+        """(threads per block, blocks, tuned, graph) of the fused step kernel."""
+        out = (ctypes.c_int * 4)()
+        abi.check(self.lib.pg_session_fused_config(self.sess, out), "pg_session_fused_config")
+        return tuple(out)
 
     def kernel_launches(self):
         n = ctypes.c_longlong()

@@ -100,7 +100,10 @@ class Server:
     """One pooled session; serves requests with continuous batching."""
 
     def __init__(self, template, dt, form=abi.PG_FORM_MIXED, budget_bytes=150e9, max_scenes=256,
-                 max_spheres=None, max_triangles=None, max_scene_extent=4.0, kn=32, kr=32, chunk=250):
+                 max_spheres=None, max_triangles=None, max_scene_extent=4.0, kn=32, kr=32, chunk=250,
+                 fused=True):
+        """fused: the mixed form steps the pool with the persistent fused step
+        kernel, its launch shape picked by the autotuner on the first steps."""
         self.form = form
         self.dt = dt
         self.chunk = chunk
@@ -111,7 +114,8 @@ class Server:
         self.tcap = int(max_triangles if max_triangles is not None else 12 * max_scenes)
         self.max_scenes = max_scenes
         self.P = self._empty_pool(template, cap, self.tcap, max_scenes)
-        self.eng = GpuEngine(form=form, capacity=(kn, kr))
+        use_fused = fused and form == abi.PG_FORM_MIXED
+        self.eng = GpuEngine(form=form, capacity=(kn, kr), fused=use_fused, autotune=use_fused)
         self.eng.attach(self.P)
         self.P.engine = self.eng
         rmax = float(template.E.radii[0, :template.ellnum].max())
