@@ -417,9 +417,15 @@ __device__ __forceinline__ void rb_done_item(const PgDev &d)
 __device__ __forceinline__ void excite_item(const PgDev &d, int sc, double step)
 {
   const double *tab = d.t_gravity + 3*(size_t)(*d.stepno);
+  if (sc == 0 && d.damp_f)
+  {
+    const double *damp = d.t_damping + 6*(size_t)(*d.stepno);
+    for (int k = 0; k < 6; k ++) d.damp_f[k] = (float)damp[k];
+  }
   if (!d.sexc_on[sc])
   {
     d.sgrav[3*sc] = tab[0]; d.sgrav[3*sc+1] = tab[1]; d.sgrav[3*sc+2] = tab[2];
+    if (d.sgrav_f) { d.sgrav_f[3*sc] = (float)tab[0]; d.sgrav_f[3*sc+1] = (float)tab[1]; d.sgrav_f[3*sc+2] = (float)tab[2]; }
     return;
   }
   const double *e = d.sexc + (size_t)PG_EXC_LEN * sc;
@@ -433,6 +439,8 @@ __device__ __forceinline__ void excite_item(const PgDev &d, int sc, double step)
   d.sgrav[3*sc] = __dadd_rn(e[0], __dmul_rn(e[3], sum));
   d.sgrav[3*sc+1] = __dadd_rn(e[1], __dmul_rn(e[4], sum));
   d.sgrav[3*sc+2] = __dadd_rn(e[2], __dmul_rn(e[5], sum));
+  if (d.sgrav_f)
+    for (int k = 0; k < 3; k ++) d.sgrav_f[3*sc+k] = (float)d.sgrav[3*sc+k];
 }
 
 // obstacle triangle t moved by its obstacle's velocities (obstacles.ispc:28-78):

@@ -40,12 +40,6 @@ __device__ __forceinline__ void flag_rebuild(const PgDev &d, bool need)
   if (m && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicExch(d.rebuild, 1);
 }
 
-// gravity of a particle's scene for this step (written by k_excite)
-__device__ __forceinline__ void scene_gravity(const PgDev &d, int sc, double, const double *, double g[3])
-{
-  g[0] = d.sgrav[3*sc]; g[1] = d.sgrav[3*sc+1]; g[2] = d.sgrav[3*sc+2];
-}
-
 // FP32 expmap: the FP64 form's expression tree in single precision
 __device__ __forceinline__ void expmap_f(float O1, float O2, float O3, float *L, bool typo)
 {
@@ -109,6 +103,18 @@ __device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
 }
 
 // ------------------------------------------------------------ conversions
+// j and 1/j of particle i when its inertia is j*I and its inverse (1/j)*I,
+// else 0 (the full FP32 matrices are used then)
+__device__ __forceinline__ void set_iso(const PgDev &d, int i)
+{
+  const double j = d.inertia[0][i], ij = d.inverse[0][i];
+  bool iso = j == d.inertia[4][i] && j == d.inertia[8][i] && ij == d.inverse[4][i] && ij == d.inverse[8][i];
+  const int off[6] = {1, 2, 3, 5, 6, 7};
+  for (int k = 0; k < 6; k ++) iso = iso && d.inertia[off[k]][i] == 0.0 && d.inverse[off[k]][i] == 0.0;
+  d.jiso[i] = iso ? (float)j : 0.0f;
+  d.iiso[i] = iso ? (float)ij : 0.0f;
+}
+
 __global__ void k_mx_from64(PgDev d, int p0, int p1, int e0, int e1)
 {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -132,6 +138,7 @@ __global__ void k_mx_from64(PgDev d, int p0, int p1, int e0, int e1)
     }
     d.mass_f[i] = (float)d.mass[i];
     d.invm_f[i] = (float)d.invm[i];
+    set_iso(d, i);
   }
   int e = e0 + t;
   if (e < e1)
@@ -148,6 +155,27 @@ __global__ void k_mx_inertia(PgDev d)
   for (int k = 0; k < 9; k ++) { d.J_f[k][i] = (float)d.inertia[k][i]; d.I_f[k][i] = (float)d.inverse[k][i]; }
   d.mass_f[i] = (float)d.mass[i];
   d.invm_f[i] = (float)d.invm[i];
+  set_iso(d, i);
+}
+
+// sphere centres (FP64, for the rebuild's keys and distance tests) and their
+// FP32 reference copies, from the particle position pairs; only when a
+// rebuild is due -- between rebuilds the mixed step never reads them
+__device__ __forceinline__ void mx_centres_item(const PgDev &d, int e)
+{
+  const int p = d.part[e];
+  for (int c = 0; c < 3; c ++)
+  {
+    d.center[c][e] = df_to({d.xh[c][p], d.xl[c][p]});
+    d.cref_f[c][e] = d.xh[c][p];
+  }
+}
+
+__global__ void k_mx_centres(PgDev d)
+{
+  if (!*d.rebuild) return;
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < d.ellnum) mx_centres_item(d, e);
 }
 
 __global__ void k_mx_to64(PgDev d, int p0, int p1)
@@ -286,13 +314,13 @@ __device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double s
       if (existing) { state[0] = d.nstate_f[0][idx]; state[1] = d.nstate_f[1][idx]; state[2] = d.nstate_f[2][idx]; }
       else { state[0] = state[1] = state[2] = 0.0f; }
       float ma = pj >= 0 ? 1.0f / (invmi + d.invm_f[pj]) : massi;
-      float kn = (float)d.iparam[0][ij];
-      float en = (float)d.iparam[1][ij] * 2.0f * sqrtf(kn*ma);
+      float kn = d.iparam_f[0][ij];
+      float en = d.iparam_f[1][ij] * 2.0f * sqrtf(kn*ma);
       float vn = vij[0]*normal[0] + vij[1]*normal[1] + vij[2]*normal[2];
       float fn = kn*depth + en*vn;
-      float kskn = (float)d.iparam[6][ij];
+      float kskn = d.iparam_f[6][ij];
       float kt = kn * kskn, et = en * kskn;
-      float mus = (float)d.iparam[2][ij], mud = (float)d.iparam[3][ij];
+      float mus = d.iparam_f[2][ij], mud = d.iparam_f[3][ij];
       float f[3], vt[3], ft[3];
       for (int c = 0; c < 3; c ++)
       {
@@ -339,9 +367,9 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
   if (d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
-    double grav[3];
-    scene_gravity(d, d.pscene[i], step_d, d.t_gravity + 3*(size_t)row, grav);
-    const double *damping = d.t_damping + 6*(size_t)row;
+    const int sc = d.pscene[i];
+    const float grav[3] = {d.sgrav_f[3*sc], d.sgrav_f[3*sc+1], d.sgrav_f[3*sc+2]};
+    const float *damping = d.damp_f;
     const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
     const float step = (float)step_d;
     const int e = d.pell[i];
@@ -363,7 +391,7 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
       }
     }
     const float ma = d.mass_f[i];
-    for (int c = 0; c < 3; c ++) F[c] = F[c] + ma * (float)grav[c];
+    for (int c = 0; c < 3; c ++) F[c] = F[c] + ma * grav[c];
 
     const int pb = d.prsnum ? d.prs_first[i] : 0, pe = d.prsnum ? d.prs_first[i+1] : 0;
     for (int pp = pb; pp < pe; pp ++)
@@ -391,22 +419,31 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
       O[c] = d.Om[c][i];
       o[c] = d.om[c][i];
     }
+    const float js = d.jiso[i], is = d.iiso[i];
     for (int k = 0; k < 9; k ++)
     {
       L[k] = {d.Lh[k][i], d.Ll[k][i]};
       Lf[k] = L[k].hi;
-      J[k] = d.J_f[k][i];
-      I[k] = d.I_f[k][i];
     }
+    if (js != 0.0f)
+    {
+      // isotropic body (a sphere): J = j*I; the products below give the same
+      // values as with the full matrices, without reading them
+      for (int k = 0; k < 9; k ++) { J[k] = 0.0f; I[k] = 0.0f; }
+      J[0] = J[4] = J[8] = js;
+      I[0] = I[4] = I[8] = is;
+    }
+    else
+      for (int k = 0; k < 9; k ++) { J[k] = d.J_f[k][i]; I[k] = d.I_f[k][i]; }
     if (!(d.flags[i] & PG_FLAG_SKIP))
     {
       const float half = 0.5f * step, hstep = step;
-      if (damping[0] != 0.0 || damping[1] != 0.0 || damping[2] != 0.0)
-        for (int c = 0; c < 3; c ++) F[c] -= ma * (float)damping[c] * v[c].hi;
-      if (damping[3] != 0.0 || damping[4] != 0.0 || damping[5] != 0.0)
+      if (damping[0] != 0.0f || damping[1] != 0.0f || damping[2] != 0.0f)
+        for (int c = 0; c < 3; c ++) F[c] -= ma * damping[c] * v[c].hi;
+      if (damping[3] != 0.0f || damping[4] != 0.0f || damping[5] != 0.0f)
       {
         float w[3], t[3], Tb[3];
-        for (int c = 0; c < 3; c ++) w[c] = (float)damping[3+c] * o[c];
+        for (int c = 0; c < 3; c ++) w[c] = damping[3+c] * o[c];
         tvmul_f(Lf, w, t);
         nvmul_f(J, t, Tb);
         nvmul_f(Lf, Tb, t);
@@ -467,15 +504,15 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
     for (int c = 0; c < 3; c ++) { d.F_f[c][i] = F[c]; d.T_f[c][i] = T[c]; }
     if (e >= 0)
     {
+      // displacement since the last rebuild, in FP32 (the FP64 centres are
+      // written only when a rebuild is due)
       float dd = 0.0f;
       for (int c = 0; c < 3; c ++)
       {
-        double cc = df_to(x[c]);
-        d.center[c][e] = cc;
-        float r = (float)(cc - d.cref[c][e]);
+        float r = (x[c].hi - d.cref_f[c][e]) + x[c].lo;
         dd += r*r;
       }
-      need = dd > (float)d.half_skin_sq;
+      need = dd > d.half_skin_sq_f;
     }
   }
   return need;
@@ -568,7 +605,7 @@ __global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int 
   {
     if (E && *(volatile int *)d.rebuild)
     {
-      for (int s = g0; s < E; s += gsz) pgk::rb_clear_item(d, s);
+      for (int s = g0; s < E; s += gsz) { pgk::rb_clear_item(d, s); mx_centres_item(d, s); }
       for (int t = g0; t < T; t += gsz) pgk::rb_tref_item(d, t);
       if (!grid_barrier(d)) return;
       pgk::Grid g;
@@ -688,6 +725,11 @@ void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0, int p1)
 {
   if (p1 < 0) p1 = d.parnum;
   if (p1 > p0) k_mx_to64<<<nblk(p1 - p0), TPB, 0, s>>>(d, p0, p1);
+}
+
+void pg_launch_mx_centres(const PgDev &d, cudaStream_t s)
+{
+  if (d.ellnum) k_mx_centres<<<nblk(d.ellnum), TPB, 0, s>>>(d);
 }
 
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)

@@ -123,6 +123,7 @@ void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmi
 {
   if (!(d.skin > 0.0)) d.skin = 0.3 * rmin;
   d.half_skin_sq = (0.45 * d.skin) * (0.45 * d.skin);
+  d.half_skin_sq_f = (float)d.half_skin_sq;
   double cell = 2.0 * rmax + d.skin;
   double e = 0.0;
   for (int k = 0; k < 3; k ++) e = fmax(e, ext[k]);

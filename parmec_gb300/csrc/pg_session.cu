@@ -383,6 +383,16 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     TRY(h2d(s, d.pairs, sc->pairs, 2*(size_t)sc->pairnum));
     TRY(h2d(s, d.ikind, sc->ikind, (size_t)sc->pairnum));
     for (int k = 0; k < 7; k ++) TRY(h2d(s, d.iparam[k], sc->iparam[k], (size_t)sc->pairnum));
+    if (d.form == PG_FORM_MIXED && sc->pairnum > 0)
+    {
+      std::vector<float> f((size_t)sc->pairnum);
+      for (int k = 0; k < 7; k ++)
+      {
+        for (int q = 0; q < sc->pairnum; q ++) f[q] = (float)sc->iparam[k][q];
+        TRY(h2d(s, d.iparam_f[k], f.data(), f.size()));
+        CK(cudaStreamSynchronize(s->stream));       // f is reused
+      }
+    }
     for (int k = 0; k < 6; k ++) TRY(h2d(s, d.nodes[k], sc->nodes[k], N));
     TRY(h2d(s, d.nodpart, sc->nodpart, N));
     for (int k = 0; k < 3; k ++) TRY(h2d(s, d.facnod[k], sc->facnod[k], F));
@@ -588,6 +598,11 @@ int mixed_buffers(pg_session *s)
   }
   TRY(dalloc(s, &d.mass_f, P)); TRY(dalloc(s, &d.invm_f, P));
   TRY(dalloc(s, &d.rh, E)); TRY(dalloc(s, &d.rl, E));
+  TRY(dalloc(s, &d.jiso, P)); TRY(dalloc(s, &d.iiso, P));
+  for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.cref_f[k], E));
+  for (int k = 0; k < 7; k ++) TRY(dalloc(s, &d.iparam_f[k], (size_t)std::max(d.pairnum, 1)));
+  TRY(dalloc(s, &d.sgrav_f, 3 * (size_t)std::max(d.nscene, 1)));
+  TRY(dalloc(s, &d.damp_f, 6));
   return PG_OK;
 }
 
@@ -785,6 +800,7 @@ int run_fused_steps(pg_session *s, double step, int n)
 void enqueue_step(pg_session *s, double step)
 {
   const PgDev &d = s->d;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_centres(d, s->stream);
   pg_launch_rebuild(d, s->stream);
   pg_launch_excite(d, s->stream, step);
   if (d.form == PG_FORM_MIXED)
@@ -986,7 +1002,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
     CK(cudaStreamSynchronize(s->stream));
     return PG_OK;
   }
-  const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d);
+  const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d) + (d.form == PG_FORM_MIXED ? 1 : 0);
   if (!s->profile && s->use_graph)
   {
     TRY(capture_step(s, step));
@@ -1006,6 +1022,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
     {
       cudaEvent_t *ev = &s->ring[(size_t)k * (G + 1)];
       CK(cudaEventRecord(ev[0], s->stream));
+      if (d.form == PG_FORM_MIXED) pg_launch_mx_centres(d, s->stream);
       pg_launch_rebuild(d, s->stream);
       pg_launch_excite(d, s->stream, step);
       CK(cudaEventRecord(ev[1], s->stream));

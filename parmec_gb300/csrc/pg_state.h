@@ -124,4 +124,10 @@ struct PgDev
   float *F_f[3], *T_f[3];
   float *nstate_f[3], *nfrc_f[3], *narm_f[3];   // per candidate entry; arm = point - slave position
   float *fm_f[3], *tm_f[3];
+  float *iparam_f[7];       // [pairnum] surface pair parameters in FP32
+  float *sgrav_f;           // [nscene][3] this step's scene gravity in FP32 (written with sgrav)
+  float *damp_f;            // [6] this step's damping row in FP32
+  float *jiso, *iiso;       // [parnum] j and 1/j when the inertia is j*I (isotropic), else 0
+  float *cref_f[3];         // [ellnum] sphere centres at the last rebuild (hi parts)
+  float half_skin_sq_f;
 };
