@@ -218,6 +218,41 @@ def batched_form(args, scenes):
     return out
 
 
+def spring_lattice_form(args, n_side):
+    """Config 2: the spring-lattice shaking table, n_side^2 MESH cubes (12
+    triangles each), 2 n (n-1) neighbour springs and n^2 base springs with
+    8-point curves and lookup dashpots, prescribed base acceleration; plain
+    FP64 (no contacts: the reference detects none between meshes)."""
+    import torch
+    from parmec_gb300 import driver
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import spring_lattice
+    t0 = time.perf_counter()
+    m, dt = spring_lattice(n_side)
+    build_s = time.perf_counter() - t0
+    eng = GpuEngine()
+    m.dem(args.warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+    steps = min(args.steps, 200)
+    times, end_time = driver.step_times(m.curtime, steps * dt - 0.5 * dt, dt)
+    tabs = driver.StepTables(m, times, dt, [1e9, 1e9], [None, None], [-1, -1])
+    ctab = tabs.ctab(0, len(times))
+    stream = torch.cuda.ExternalStream(eng.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    eng.run(ctab, dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    out = {"workload": f"{n_side}x{n_side} MESH hexahedra (10 mm), {m.sprnum} springs, {m.trinum} triangles, "
+                       "base 0.5 g sin(2 pi 5 t) along x, FP64", "steps": steps, "dt": dt,
+           "value": m.parnum * steps / (ms * 1e-3), "unit": "particle-steps/s",
+           "spring_steps_per_s": m.sprnum * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+           "particles": m.parnum, "springs": m.sprnum, "build_s": build_s}
+    eng.close()
+    return out
+
+
 def serving_form(args, count):
     """Config 4: a Poisson stream (200 req/s) of excitation-sweep requests
     (sphere counts log-uniform [1024, 262144], 200-5000 steps, sinusoid or
@@ -300,6 +335,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--serving", type=int, default=48, help="requests in the serving stream (0: skip)")
+    ap.add_argument("--lattice", type=int, default=256, help="side of the spring lattice (0: skip)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -459,6 +495,8 @@ def main():
         from parmec_gb300.scenes import batch_scenes
         line["batched"] = batched_form(args, batch_scenes(512))
     line["mixed"] = mixed_form(args, ref64)
+    if args.lattice > 0:
+        line["spring_lattice"] = spring_lattice_form(args, args.lattice)
     if args.serving > 0:
         line["serving"] = serving_form(args, args.serving)
     line["mixed"]["speedup_vs_plain"] = line["mixed"]["value"] / (value / world)

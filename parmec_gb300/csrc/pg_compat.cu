@@ -203,7 +203,13 @@ bool slot_arrays(size_t keep_slots)
   for (int k = 0; ok && k < 3; k ++)
     ok = grow_keep(d.nstate[k], n, keep_slots) && grow_keep(d.nfrc[k], n, keep_slots) &&
          grow_keep(d.npnt[k], n, keep_slots) && grow_keep(d.nnrm[k], n, keep_slots);
-  return ok && grow(d.rref, (size_t)d.kr * P);
+  // slave-list entries (at most kn per sphere) and their sort and scan scratch
+  for (int k = 0; ok && k < 2; k ++) ok = grow(d.skey[k], n) && grow(d.sval[k], n);
+  const int nb = pg_sort_blocks((int)n);
+  const int sb = std::max(pg_scan_blocks(256 * nb), std::max(pg_scan_blocks((int)E + 1), pg_scan_blocks((int)P + 1)));
+  ok = ok && grow(d.shist, 256 * (size_t)nb) && grow(d.sbs, (size_t)sb);
+  d.rref = d.sval[pg_sort_passes_exact(d.sbits) & 1];
+  return ok;
 }
 
 // (re)start the contact state for P particles, E spheres and T triangles
@@ -211,7 +217,9 @@ bool restart_lists(int P, int E, int T)
 {
   PgDev &d = G.d;
   d.parnum = P; d.ellnum = E; d.trinum = T;
-  bool ok = zeros(d.ncnt, E) && zeros(d.rcnt, P) && slot_arrays(0);
+  d.sbits = pg_rebuild_entry_bits(P);
+  bool ok = zeros(d.ncnt, E) && zeros(d.rcnt, P) && grow(d.soff, (size_t)P + 1) && grow(d.eorder, E) &&
+            grow(d.eoff, (size_t)E + 1) && grow(d.smeta, 4) && grow(d.gbar, 4) && slot_arrays(0);
   for (int k = 0; ok && k < 3; k ++) ok = grow(d.cref[k], E) && grow(d.fm[k], P) && grow(d.tm[k], P);
   for (int k = 0; ok && k < 9; k ++) ok = grow(d.tref[k], T);
   ok = ok && grow(d.tbox, 6 * (size_t)std::max(T, 1));
@@ -568,8 +576,12 @@ void condet(int, partitioning *tree, master_conpnt master[], int parnum, int ell
   d.parnum = parnum; d.ellnum = ellnum; d.trinum = T;
   bool ok = true;
   for (int k = 0; ok && k < 3; k ++) ok = up(d.center[k], center[k], ellnum);
+  std::vector<int> ord(ellnum);
+  for (int e = 0; e < ellnum; e ++) ord[e] = e;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return part[a] < part[b]; });
   ok = ok && up(d.radii[0], radii[0], ellnum) && up(d.part, part, ellnum) && up(d.ellcol, ellcol, ellnum) &&
-       up(d.pell, pell.data(), parnum);
+       up(d.pell, pell.data(), parnum) && up(d.eorder, ord.data(), ellnum) &&
+       cuda_ok(cudaStreamSynchronize(G.st), "condet");           // ord is a local
   for (int a = 0; ok && a < 3; a ++)
     for (int c = 0; ok && c < 3; c ++) ok = up(d.tri[3*a+c], T ? tri[a][c] : nullptr, T);
   ok = ok && up(d.tricol, T ? tricol : nullptr, T) && up(d.triobs, T ? triobs : nullptr, T);
@@ -614,18 +626,17 @@ void condet(int, partitioning *tree, master_conpnt master[], int parnum, int ell
       // a list overflowed: more slots (contacts beyond the old capacity restart their state)
       const int z[4] = {0, 0, 0, 0};
       if (!up(d.err, z, 4)) return;
-      const int kn = std::min(96, std::max(d.kn, stats[1] + 8)), kr = std::min(96, std::max(d.kr, stats[2] + 8));
-      if (kn == d.kn && kr == d.kr)
+      const int kn = std::min(96, std::max(d.kn, stats[1] + 8));
+      if (kn == d.kn)
       {
         char msg[200];
         std::snprintf(msg, sizeof msg, "more than 96 contact candidates (site %d, index %d, count %d; "
-                      "largest list %d, largest slave list %d)", err[1], err[2], err[3], stats[1], stats[2]);
+                      "largest list %d)", err[1], err[2], err[3], stats[1]);
         fail(PG_ERR_CAPACITY, msg);
         return;
       }
       const size_t keep = (size_t)d.kn * ellnum;
       d.kn = kn;
-      d.kr = kr;
       if (!slot_arrays(keep)) return;
     }
   }

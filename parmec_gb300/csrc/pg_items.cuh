@@ -98,6 +98,84 @@ __device__ __forceinline__ void cell_keys_item(int i, const double *x, const dou
   if (rx) { rx[i] = c[0]; ry[i] = c[1]; rz[i] = c[2]; }
 }
 
+// ---- exclusive scans over tiles of SCAN_TILE elements (block-level
+// helpers: every thread of the block calls them; blockDim divides SCAN_TILE)
+constexpr int SCAN_TILE = 1024;
+
+template <typename T>
+__device__ __forceinline__ T scan_tile_sum(const T *a, int n, int tile, T *sh)
+{
+  const int B = blockDim.x, t = threadIdx.x, per = SCAN_TILE / B;
+  const int b = tile * SCAN_TILE + t * per;
+  T s = 0;
+  for (int k = 0; k < per; k ++) if (b + k < n) s += a[b + k];
+  sh[t] = s;
+  __syncthreads();
+  for (int off = B / 2; off > 0; off >>= 1)
+  {
+    if (t < off) sh[t] += sh[t + off];
+    __syncthreads();
+  }
+  const T total = sh[0];
+  __syncthreads();
+  return total;
+}
+
+template <typename T>
+__device__ __forceinline__ void scan_tile_apply(T *a, int n, int tile, T base, T *sh)
+{
+  const int B = blockDim.x, t = threadIdx.x, per = SCAN_TILE / B;
+  const int b = tile * SCAN_TILE + t * per;
+  T v[8];
+  T s = 0;
+  for (int k = 0; k < per; k ++) { v[k] = (b + k < n) ? a[b + k] : (T)0; s += v[k]; }
+  sh[t] = s;
+  __syncthreads();
+  for (int off = 1; off < B; off <<= 1)
+  {
+    T x = t >= off ? sh[t - off] : (T)0;
+    __syncthreads();
+    sh[t] += x;
+    __syncthreads();
+  }
+  T run = base + (t ? sh[t - 1] : (T)0);
+  for (int k = 0; k < per; k ++)
+  {
+    if (b + k < n) a[b + k] = run;
+    run += v[k];
+  }
+  __syncthreads();
+}
+
+// exclusive scan of a[0..total) by one block: contiguous chunks per thread
+template <typename T>
+__device__ __forceinline__ void block_scan_seq(T *a, int total, T *part)
+{
+  const int B = blockDim.x, t = threadIdx.x;
+  const int per = (total + B - 1) / B;
+  const int b = t * per;
+  const int e = min(b + per, total);
+  T sum = 0;
+  for (int k = b; k < e; k ++) sum += a[k];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < B; off <<= 1)
+  {
+    T v = t >= off ? part[t - off] : (T)0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  T run = t ? part[t - 1] : (T)0;
+  for (int k = b; k < e; k ++)
+  {
+    T v = a[k];
+    a[k] = run;
+    run += v;
+  }
+  __syncthreads();
+}
+
 // per-tile digit histogram, stored digit-major: hist[digit*nb + tile].  The
 // first 256 threads of the block do the work; every thread must call.
 __device__ __forceinline__ void sort_hist_tile(const unsigned *keys, int n, unsigned *hist, int nb, int shift,
@@ -120,34 +198,10 @@ __device__ __forceinline__ void sort_hist_tile(const unsigned *keys, int n, unsi
   __syncthreads();
 }
 
-// exclusive scan of the digit-major histogram by one block (any size >= 32);
-// part[] holds blockDim.x entries
+// exclusive scan of the digit-major histogram by one block
 __device__ __forceinline__ void sort_scan_block(unsigned *hist, int nb, unsigned *part)
 {
-  const int T = blockDim.x, t = threadIdx.x;
-  const int total = 256 * nb;
-  const int per = (total + T - 1) / T;
-  const int b = t * per;
-  const int e = min(b + per, total);
-  unsigned sum = 0;
-  for (int k = b; k < e; k ++) sum += hist[k];
-  part[t] = sum;
-  __syncthreads();
-  for (int off = 1; off < T; off <<= 1)
-  {
-    unsigned v = t >= off ? part[t - off] : 0u;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  unsigned run = t ? part[t - 1] : 0u;
-  for (int k = b; k < e; k ++)
-  {
-    unsigned v = hist[k];
-    hist[k] = run;
-    run += v;
-  }
-  __syncthreads();
+  block_scan_seq(hist, 256 * nb, part);
 }
 
 // stable scatter of one tile: each of the first 8 warps ranks its contiguous
@@ -354,48 +408,50 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
   d.ncnt[i] = n;
 }
 
-// 5. slave lists: clear, fill, sort by (master particle, master slot)
+// 5. slave lists (CSR): count entries per sphere in particle order, emit
+// (partner, entry) pairs in (master particle, slot) order, then a stable sort
+// by partner gives every particle's entries in that order
 __device__ __forceinline__ void rb_rzero_item(const PgDev &d, int p) { d.rcnt[p] = 0; }
 
-__device__ __forceinline__ void rb_rfill_item(const PgDev &d, int i)
+__device__ __forceinline__ void rb_count_item(const PgDev &d, int q)
 {
-  const int E = d.ellnum;
+  d.eoff[q] = d.ncnt[d.eorder[q]];
+}
+
+__device__ __forceinline__ void rb_emit_item(const PgDev &d, int q)
+{
+  const int E = d.ellnum, P = d.parnum;
+  const int i = d.eorder[q];
   const int n = d.ncnt[i];
+  const int base = d.eoff[q];
   for (int k = 0; k < n; k ++)
   {
-    int code = d.ncode[(size_t)k * E + i];
-    int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
-    if (pj < 0 || pj >= d.parnum) continue;
-    int r = atomicAdd(&d.rcnt[pj], 1);
-    if (r < d.kr) d.rref[(size_t)r * d.parnum + pj] = k * E + i;
-    else set_err(d, PG_ERR_CAPACITY, 3, pj, r + 1);
+    const int code = d.ncode[(size_t)k * E + i];
+    const int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
+    const bool ok = pj >= 0 && pj < P;
+    d.skey[0][base + k] = ok ? (unsigned)pj : 0xffffffffu;
+    d.sval[0][base + k] = k * E + i;
+    if (ok) atomicAdd(&d.rcnt[pj], 1);
   }
 }
 
-__device__ __forceinline__ void rb_rsort_item(const PgDev &d, int p)
+__device__ __forceinline__ void rb_soff_item(const PgDev &d, int p)
 {
-  const int P = d.parnum, E = d.ellnum;
-  int n = d.rcnt[p];
+  const int n = d.rcnt[p];
+  d.soff[p] = n;
   atomicMax(&d.stats[2], n);
-  if (n > d.kr) { n = d.kr; d.rcnt[p] = n; }
-  unsigned long long key[MAXKN];
-  int ref[MAXKN];
-  for (int r = 0; r < n; r ++)
-  {
-    int v = d.rref[(size_t)r * P + p];
-    int i = v % E, k = v / E;
-    key[r] = ((unsigned long long)(unsigned)d.part[i] << 32) | (unsigned)k;
-    ref[r] = v;
-  }
-  for (int a = 1; a < n; a ++)
-  {
-    unsigned long long kv = key[a];
-    int rv = ref[a], b = a - 1;
-    while (b >= 0 && key[b] > kv) { key[b+1] = key[b]; ref[b+1] = ref[b]; b --; }
-    key[b+1] = kv;
-    ref[b+1] = rv;
-  }
-  for (int r = 0; r < n; r ++) d.rref[(size_t)r * P + p] = ref[r];
+}
+
+// sizes of the entry sort (one thread): entries, tiles, histogram length and
+// its scan tiles
+__device__ __forceinline__ void rb_meta_item(const PgDev &d)
+{
+  const int n = d.eoff[d.ellnum];
+  const int nb = n > 0 ? (n + SORT_TILE - 1) / SORT_TILE : 1;
+  d.smeta[0] = n;
+  d.smeta[1] = nb;
+  d.smeta[2] = 256 * nb;
+  d.smeta[3] = (256 * nb + SCAN_TILE - 1) / SCAN_TILE;
 }
 
 // end of a rebuild (one thread)
@@ -407,6 +463,161 @@ __device__ __forceinline__ void rb_done_item(const PgDev &d)
     d.stats[0] += 1;
   }
 }
+
+// ================================================================ cooperative grids
+__device__ __forceinline__ unsigned long long global_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// barrier of all blocks of a cooperative grid.  d.gbar = {arrivals,
+// generation, abort}.  A block that waits more than 2 s records
+// PG_ERR_TIMEOUT and raises abort; every block then leaves its kernel
+// (a false return).
+static __device__ __noinline__ bool grid_barrier(const PgDev &d)
+{
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    volatile unsigned *b = d.gbar;
+    int ok = 1;
+    const unsigned gen = b[1];
+    __threadfence();
+    if (b[2] != 0u) ok = 0;
+    else
+    {
+      const unsigned arrived = atomicAdd(d.gbar, 1u) + 1u;
+      if (arrived == gridDim.x)
+      {
+        atomicExch(d.gbar, 0u);
+        __threadfence();
+        atomicAdd(d.gbar + 1, 1u);
+      }
+      else
+      {
+        const unsigned long long t0 = global_ns();
+        while (b[1] == gen)
+        {
+          if (b[2] != 0u) { ok = 0; break; }
+          if (global_ns() - t0 > 2000000000ull)
+          {
+            atomicExch(d.gbar + 2, 1u);
+            set_err(d, PG_ERR_TIMEOUT, 20, blockIdx.x, 0);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// exclusive scan of a[0..n) by the whole grid (tile sums | their scan by
+// block 0 | tiles), ending with a barrier; false when a barrier gave up
+template <typename T>
+__device__ bool grid_scan(const PgDev &d, T *a, int n, T *bs, T *sh)
+{
+  const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x)
+  {
+    const T s = scan_tile_sum(a, n, t, sh);
+    if (threadIdx.x == 0) bs[t] = s;
+  }
+  if (!grid_barrier(d)) return false;
+  if (blockIdx.x == 0) block_scan_seq(bs, tiles, sh);
+  if (!grid_barrier(d)) return false;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) scan_tile_apply(a, n, t, bs[t], sh);
+  return grid_barrier(d);
+}
+
+template <int B>
+union RebuildSmem
+{
+  unsigned h[256];
+  struct { unsigned wcnt[SORT_THREADS / 32][256]; unsigned goff[256]; } sc;
+  unsigned part[B];
+};
+
+struct NoHook
+{
+  __device__ void operator()(const PgDev &, int) const {}
+};
+
+// the whole candidate-list rebuild by a cooperative grid of B-thread blocks
+// (B >= 256): clear | keys | key sort (passes) | ranges | lists | slave lists
+// (counts | scan | emit | offsets | scan | entry sort (epasses, the result in
+// sval[epasses & 1]) ).  'hook' runs for every sphere in the first phase.
+// Returns false when a barrier gave up.
+template <int B, class Hook>
+__device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem<B> &sm, Hook hook)
+{
+  const int gsz = gridDim.x * B;
+  const int g0 = blockIdx.x * B + threadIdx.x;
+  const int E = d.ellnum, P = d.parnum, T = d.trinum;
+  for (int s = g0; s < E; s += gsz) { rb_clear_item(d, s); hook(d, s); }
+  for (int t = g0; t < T; t += gsz) rb_tref_item(d, t);
+  if (!grid_barrier(d)) return false;
+  Grid g;
+  for (int k = 0; k < 3; k ++) { g.org[k] = 0.0; g.dim[k] = d.dim[k]; }
+  g.cell = d.cell;
+  for (int i = g0; i < E; i += gsz)
+    cell_keys_item(i, d.center[0], d.center[1], d.center[2], g, d.escene, d.sorg[0], d.sorg[1], d.sorg[2],
+                   3 * d.bits, d.keys[0], d.vals[0], d.cref[0], d.cref[1], d.cref[2]);
+  if (!grid_barrier(d)) return false;
+  const int nb = d.nsortblocks;
+  for (int p = 0; p < passes; p ++)
+  {
+    unsigned *ks = (p & 1) ? d.keys[1] : d.keys[0], *kd = (p & 1) ? d.keys[0] : d.keys[1];
+    int *vs = (p & 1) ? d.vals[1] : d.vals[0], *vd = (p & 1) ? d.vals[0] : d.vals[1];
+    for (int tile = blockIdx.x; tile < nb; tile += gridDim.x) sort_hist_tile(ks, E, d.hist, nb, 8 * p, tile, sm.h);
+    if (!grid_barrier(d)) return false;
+    if (!grid_scan(d, d.hist, 256 * nb, (unsigned *)d.sbs, sm.part)) return false;
+    for (int tile = blockIdx.x; tile < nb; tile += gridDim.x)
+      sort_scatter_tile(ks, vs, kd, vd, E, d.hist, nb, 8 * p, tile, sm.sc.wcnt, sm.sc.goff);
+    if (!grid_barrier(d)) return false;
+  }
+  for (int s = g0; s < E; s += gsz) rb_ranges_item(d, s);
+  if (!grid_barrier(d)) return false;
+  for (int i = g0; i < E; i += gsz) rb_verlet_item(d, i);
+  if (!grid_barrier(d)) return false;
+  for (int p = g0; p < P; p += gsz) rb_rzero_item(d, p);
+  for (int q = g0; q < E; q += gsz) rb_count_item(d, q);
+  if (g0 == 0) d.eoff[E] = 0;
+  if (!grid_barrier(d)) return false;
+  if (!grid_scan(d, d.eoff, E + 1, (int *)d.sbs, (int *)sm.part)) return false;
+  for (int q = g0; q < E; q += gsz) rb_emit_item(d, q);
+  if (!grid_barrier(d)) return false;
+  for (int p = g0; p < P; p += gsz) rb_soff_item(d, p);
+  if (g0 == 0) { d.soff[P] = 0; rb_meta_item(d); }
+  if (!grid_barrier(d)) return false;
+  if (!grid_scan(d, d.soff, P + 1, (int *)d.sbs, (int *)sm.part)) return false;
+  {
+    const int n = d.smeta[0], nbe = d.smeta[1];
+    for (int p = 0; p < epasses; p ++)
+    {
+      unsigned *ks = (p & 1) ? d.skey[1] : d.skey[0], *kd = (p & 1) ? d.skey[0] : d.skey[1];
+      int *vs = (p & 1) ? d.sval[1] : d.sval[0], *vd = (p & 1) ? d.sval[0] : d.sval[1];
+      for (int tile = blockIdx.x; tile < nbe; tile += gridDim.x)
+        sort_hist_tile(ks, n, d.shist, nbe, 8 * p, tile, sm.h);
+      if (!grid_barrier(d)) return false;
+      if (!grid_scan(d, d.shist, 256 * nbe, (unsigned *)d.sbs, sm.part)) return false;
+      for (int tile = blockIdx.x; tile < nbe; tile += gridDim.x)
+        sort_scatter_tile(ks, vs, kd, vd, n, d.shist, nbe, 8 * p, tile, sm.sc.wcnt, sm.sc.goff);
+      if (!grid_barrier(d)) return false;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) rb_done_item(d);
+  return grid_barrier(d);
+}
+
 
 // ================================================================ per-step scene state
 // gravity of scene sc for this step: the step table's row, or the scene's

@@ -46,6 +46,8 @@ void pg_launch_cell_keys(const double *x, const double *y, const double *z, int 
                          const int *scene = nullptr, double *const sorg[3] = nullptr, int shift = 0);
 void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned *hist, int n, int passes,
                           const int *gate, cudaStream_t s);
+int  pg_scan_blocks(int n);                                   // scan block sums for n elements
+int  pg_sort_passes_exact(int key_bits);                      // 8-bit passes, not rounded to even
 
 // pg_rebuild.cu
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
@@ -54,3 +56,4 @@ int  pg_rebuild_kernel_count(const PgDev &d);
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin);
 void pg_rebuild_key_bits(PgDev &d);
 int  pg_rebuild_sort_bits(const PgDev &d);
+int  pg_rebuild_entry_bits(int parnum);                         // key bits of the slave-entry sort

@@ -377,10 +377,10 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
     if (e >= 0) for (int c = 0; c < 3; c ++) { F[c] = d.fm_f[c][i]; T[c] = d.tm_f[c][i]; }
     if (d.ellnum)
     {
-      const int nr = d.rcnt[i];
-      for (int r = 0; r < nr; r ++)
+      const int rb = d.soff[i], re = d.soff[i+1];
+      for (int r = rb; r < re; r ++)
       {
-        const int ref = d.rref[(size_t)r * d.parnum + i];
+        const int ref = d.rref[r];
         if (!d.nflag[ref]) continue;
         float f[3] = {-d.nfrc_f[0][ref], -d.nfrc_f[1][ref], -d.nfrc_f[2][ref]};
         float a[3] = {d.narm_f[0][ref], d.narm_f[1][ref], d.narm_f[2][ref]};
@@ -535,127 +535,40 @@ __global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
 // a grid-stride loop; the item bodies are the ones the per-phase kernels run,
 // so the results do not depend on the launch shape.
 
-__device__ __forceinline__ unsigned long long global_ns()
+// the mixed form's extra work in the first rebuild phase: FP64 centres and
+// FP32 reference centres from the position pairs
+struct MxCentres
 {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// barrier of all blocks of a cooperative grid.  d.gbar = {arrivals,
-// generation, abort}.  A block that waits more than 2 s records
-// PG_ERR_TIMEOUT and raises abort; every block then leaves the kernel.
-__device__ bool grid_barrier(const PgDev &d)
-{
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0)
-  {
-    volatile unsigned *b = d.gbar;
-    int ok = 1;
-    const unsigned gen = b[1];
-    __threadfence();
-    if (b[2] != 0u) ok = 0;
-    else
-    {
-      const unsigned arrived = atomicAdd(d.gbar, 1u) + 1u;
-      if (arrived == gridDim.x)
-      {
-        atomicExch(d.gbar, 0u);
-        __threadfence();
-        atomicAdd(d.gbar + 1, 1u);
-      }
-      else
-      {
-        const unsigned long long t0 = global_ns();
-        while (b[1] == gen)
-        {
-          if (b[2] != 0u) { ok = 0; break; }
-          if (global_ns() - t0 > 2000000000ull)
-          {
-            atomicExch(d.gbar + 2, 1u);
-            set_err(d, PG_ERR_TIMEOUT, 20, blockIdx.x, 0);
-            ok = 0;
-            break;
-          }
-          __nanosleep(32);
-        }
-      }
-    }
-    __threadfence();
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
-}
+  __device__ void operator()(const PgDev &d, int e) const { mx_centres_item(d, e); }
+};
 
 template <int B, int MINB>
-__global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int nsteps, int passes)
+__global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int nsteps, int passes, int epasses)
 {
-  __shared__ union
-  {
-    unsigned h[256];
-    struct { unsigned wcnt[pgk::SORT_THREADS / 32][256]; unsigned goff[256]; } sc;
-    unsigned part[B];
-  } sm;
+  __shared__ pgk::RebuildSmem<B> sm;
   const int gsz = gridDim.x * B;
   const int g0 = blockIdx.x * B + threadIdx.x;
   const int E = d.ellnum, P = d.parnum, T = d.trinum;
   for (int it = 0; it < nsteps; it ++)
   {
     if (E && *(volatile int *)d.rebuild)
-    {
-      for (int s = g0; s < E; s += gsz) { pgk::rb_clear_item(d, s); mx_centres_item(d, s); }
-      for (int t = g0; t < T; t += gsz) pgk::rb_tref_item(d, t);
-      if (!grid_barrier(d)) return;
-      pgk::Grid g;
-      for (int k = 0; k < 3; k ++) { g.org[k] = 0.0; g.dim[k] = d.dim[k]; }
-      g.cell = d.cell;
-      for (int i = g0; i < E; i += gsz)
-        pgk::cell_keys_item(i, d.center[0], d.center[1], d.center[2], g, d.escene, d.sorg[0], d.sorg[1], d.sorg[2],
-                            3 * d.bits, d.keys[0], d.vals[0], d.cref[0], d.cref[1], d.cref[2]);
-      if (!grid_barrier(d)) return;
-      const int nb = d.nsortblocks;
-      for (int p = 0; p < passes; p ++)
-      {
-        unsigned *ks = (p & 1) ? d.keys[1] : d.keys[0], *kd = (p & 1) ? d.keys[0] : d.keys[1];
-        int *vs = (p & 1) ? d.vals[1] : d.vals[0], *vd = (p & 1) ? d.vals[0] : d.vals[1];
-        for (int tile = blockIdx.x; tile < nb; tile += gridDim.x)
-          pgk::sort_hist_tile(ks, E, d.hist, nb, 8 * p, tile, sm.h);
-        if (!grid_barrier(d)) return;
-        if (blockIdx.x == 0) pgk::sort_scan_block(d.hist, nb, sm.part);
-        if (!grid_barrier(d)) return;
-        for (int tile = blockIdx.x; tile < nb; tile += gridDim.x)
-          pgk::sort_scatter_tile(ks, vs, kd, vd, E, d.hist, nb, 8 * p, tile, sm.sc.wcnt, sm.sc.goff);
-        if (!grid_barrier(d)) return;
-      }
-      for (int s = g0; s < E; s += gsz) pgk::rb_ranges_item(d, s);
-      for (int p = g0; p < P; p += gsz) pgk::rb_rzero_item(d, p);
-      if (!grid_barrier(d)) return;
-      for (int i = g0; i < E; i += gsz) pgk::rb_verlet_item(d, i);
-      if (!grid_barrier(d)) return;
-      for (int i = g0; i < E; i += gsz) pgk::rb_rfill_item(d, i);
-      if (!grid_barrier(d)) return;
-      for (int p = g0; p < P; p += gsz) pgk::rb_rsort_item(d, p);
-      if (blockIdx.x == 0 && threadIdx.x == 0) pgk::rb_done_item(d);
-      if (!grid_barrier(d)) return;
-    }
+      if (!pgk::rebuild_all<B>(d, passes, epasses, sm, MxCentres())) return;
     // excitation and contacts: contacts do not read the scene gravity
     for (int sc = g0; sc < d.nscene; sc += gsz) pgk::excite_item(d, sc, step);
     for (int i = g0; i < E; i += gsz) mx_contacts_item(d, i, step);
-    if (!grid_barrier(d)) return;
+    if (!pgk::grid_barrier(d)) return;
     // integration and obstacle triangles touch disjoint state
     bool need = false;
     for (int i = g0; i < P; i += gsz) need |= mx_integrate_item(d, i, step);
     for (int t = g0; t < T; t += gsz) need |= pgk::obstacles_item(d, t, step, 1);
     if (__syncthreads_or(need) && threadIdx.x == 0 && E) atomicExch(d.rebuild, 1);
-    if (!grid_barrier(d)) return;
+    if (!pgk::grid_barrier(d)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) pgk::tail_item(d, step, 1);
-    if (!grid_barrier(d)) return;
+    if (!pgk::grid_barrier(d)) return;
   }
 }
 
-typedef void (*FusedKernel)(PgDev, double, int, int);
+typedef void (*FusedKernel)(PgDev, double, int, int, int);
 
 // the launch shapes the autotuner may pick from (threads, minimum blocks per SM)
 struct FusedShape { int threads, minb; FusedKernel k; };
@@ -705,7 +618,8 @@ cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int 
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, fused_shapes[c.shape].k, d, step, nsteps, passes);
+  const int epasses = pg_sort_passes_exact(d.sbits);
+  return cudaLaunchKernelEx(&cfg, fused_shapes[c.shape].k, d, step, nsteps, passes, epasses);
 }
 
 void pg_launch_mx_from64(const PgDev &d, cudaStream_t s, int p0, int p1, int e0, int e1)

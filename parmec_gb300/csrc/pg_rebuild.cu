@@ -35,58 +35,32 @@ inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
 using namespace pgk;
 
-__global__ void k_rb_clear(PgDev d)
+// the whole rebuild as one cooperative launch; returns at once (one empty
+// launch per step) unless a rebuild is due
+template <int B>
+__global__ void __launch_bounds__(B) k_rebuild_coop(PgDev d, int passes, int epasses)
 {
-  if (!*d.rebuild) return;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < d.ellnum) rb_clear_item(d, s);
+  __shared__ RebuildSmem<B> sm;
+  if (!d.ellnum || !*(volatile int *)d.rebuild) return;
+  rebuild_all<B>(d, passes, epasses, sm, NoHook());
 }
 
-__global__ void k_rb_tref(PgDev d)
-{
-  if (!*d.rebuild) return;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < d.trinum) rb_tref_item(d, t);
-}
+constexpr int RB_THREADS = 256;
 
-__global__ void k_rb_ranges(PgDev d)
+// blocks of the cooperative rebuild grid: all that fit at once
+int rebuild_grid()
 {
-  if (!*d.rebuild) return;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < d.ellnum) rb_ranges_item(d, s);
-}
-
-__global__ void __launch_bounds__(TPB) k_rb_verlet(PgDev d)
-{
-  if (!*d.rebuild) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ellnum) rb_verlet_item(d, i);
-}
-
-__global__ void k_rb_rzero(PgDev d)
-{
-  if (!*d.rebuild) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < d.parnum) rb_rzero_item(d, p);
-}
-
-__global__ void k_rb_rfill(PgDev d)
-{
-  if (!*d.rebuild) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ellnum) rb_rfill_item(d, i);
-}
-
-__global__ void k_rb_rsort(PgDev d)
-{
-  if (!*d.rebuild) return;
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < d.parnum) rb_rsort_item(d, p);
-}
-
-__global__ void k_rb_done(PgDev d)
-{
-  if (threadIdx.x == 0 && blockIdx.x == 0) rb_done_item(d);
+  static int grid = 0;
+  if (grid) return grid;
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild_coop<RB_THREADS>, RB_THREADS, 0) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return 1;
+  }
+  grid = sms * (per > 0 ? per : 1);
+  return grid;
 }
 
 // ---- gate of the drop-in condet(): a rebuild is due when a sphere centre or
@@ -158,24 +132,28 @@ int pg_rebuild_sort_bits(const PgDev &d) { return d.keybits + (d.escene ? 1 : 0)
 
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 {
-  const int E = d.ellnum;
-  if (!E) return;
-  k_rb_clear<<<nblk(E), TPB, 0, s>>>(d);
-  pg_launch_cell_keys(d.center[0], d.center[1], d.center[2], E, nullptr, d.cell, d.dim, d.keys[0], d.vals[0],
-                      d.cref[0], d.cref[1], d.cref[2], d.rebuild, s, d.escene, d.sorg, 3 * d.bits);
-  if (d.trinum) k_rb_tref<<<nblk(d.trinum), TPB, 0, s>>>(d);
-  pg_launch_radix_sort(d.keys[0], d.vals[0], d.keys[1], d.vals[1], d.hist, E, pg_sort_passes_bits(pg_rebuild_sort_bits(d)),
-                       d.rebuild, s);
-  k_rb_ranges<<<nblk(E), TPB, 0, s>>>(d);
-  k_rb_verlet<<<nblk(E), TPB, 0, s>>>(d);
-  k_rb_rzero<<<nblk(d.parnum), TPB, 0, s>>>(d);
-  k_rb_rfill<<<nblk(E), TPB, 0, s>>>(d);
-  k_rb_rsort<<<nblk(d.parnum), TPB, 0, s>>>(d);
-  k_rb_done<<<1, 32, 0, s>>>(d);
+  if (!d.ellnum) return;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(rebuild_grid());
+  cfg.blockDim = dim3(RB_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_rebuild_coop<RB_THREADS>, d, pg_sort_passes_bits(pg_rebuild_sort_bits(d)),
+                     pg_sort_passes_exact(d.sbits));
+}
+
+int pg_rebuild_entry_bits(int parnum)
+{
+  int b = 1;
+  while (b < 31 && (1 << b) < parnum) b ++;
+  return b + 1;                               // one more: the no-partner key sorts last
 }
 
 int pg_rebuild_kernel_count(const PgDev &d)
 {
-  if (!d.ellnum) return 0;
-  return 2 + (d.trinum ? 1 : 0) + 3 * pg_sort_passes_bits(pg_rebuild_sort_bits(d)) + 6;
+  return d.ellnum ? 1 : 0;
 }

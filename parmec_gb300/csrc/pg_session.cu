@@ -351,6 +351,15 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     for (size_t p = p0; p < p1; p ++) s->h_pell[p] = pell[p - p0];
     TRY(h2dr(s, d.pell, s->h_pell.data(), p0, p1));
   }
+  // spheres in particle order (stable): the order of the slave-list entries
+  if (d.ellnum)
+  {
+    std::vector<int> ord(d.ellnum);
+    for (int e = 0; e < d.ellnum; e ++) ord[e] = e;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return sc->part[a] < sc->part[b]; });
+    TRY(h2d(s, d.eorder, ord.data(), ord.size()));
+    CK(cudaStreamSynchronize(s->stream));         // ord is a local
+  }
   // triangle -> moving obstacle for the triangles of the range
   {
     std::vector<int> own(d.trinum, -1);
@@ -537,15 +546,25 @@ int slot_buffers(pg_session *s)
       TRY(dalloc(s, &d.narm_f[k], slots));
     }
   }
-  TRY(dalloc(s, &d.rref, (size_t)d.kr * std::max<size_t>(P, 1)));
+  // slave-list entries: at most kn per sphere
+  const size_t ent = slots;
+  for (int k = 0; k < 2; k ++) { TRY(dalloc(s, &d.skey[k], ent)); TRY(dalloc(s, &d.sval[k], ent)); }
+  const int nb = pg_sort_blocks((int)ent);
+  TRY(dalloc(s, &d.shist, 256 * (size_t)nb));
+  const int sb = std::max(pg_scan_blocks(256 * nb), std::max(pg_scan_blocks((int)E + 1), pg_scan_blocks((int)P + 1)));
+  TRY(dalloc(s, &d.sbs, (size_t)sb));
+  d.rref = d.sval[pg_sort_passes_exact(d.sbits) & 1];        // where the entry sort leaves its result
+  (void)P;
   return PG_OK;
 }
 
 void release_slot_buffers(pg_session *s)
 {
   PgDev &d = s->d;
-  release(s, d.ncode); release(s, d.nflag); release(s, d.ndep); release(s, d.rref);
+  release(s, d.ncode); release(s, d.nflag); release(s, d.ndep);
   d.ncode = nullptr; d.nflag = nullptr; d.ndep = nullptr; d.rref = nullptr;
+  for (int k = 0; k < 2; k ++) { release(s, d.skey[k]); release(s, d.sval[k]); d.skey[k] = nullptr; d.sval[k] = nullptr; }
+  release(s, d.shist); release(s, d.sbs); d.shist = nullptr; d.sbs = nullptr;
   for (int k = 0; k < 3; k ++)
   {
     release(s, d.nstate[k]); release(s, d.nfrc[k]); release(s, d.npnt[k]); release(s, d.nnrm[k]);
@@ -567,6 +586,11 @@ int contact_buffers(pg_session *s)
     TRY(dalloc(s, &d.cref[k], E));
   }
   TRY(dalloc(s, &d.rcnt, P));
+  TRY(dalloc(s, &d.soff, P + 1));
+  TRY(dalloc(s, &d.eorder, E));
+  TRY(dalloc(s, &d.eoff, E + 1));
+  TRY(dalloc(s, &d.smeta, 4));
+  d.sbits = pg_rebuild_entry_bits((int)P);
   for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.tref[k], T));
   TRY(dalloc(s, &d.tbox, 6 * std::max<size_t>(T, 1)));
   for (int k = 0; k < 2; k ++)

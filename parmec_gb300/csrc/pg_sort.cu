@@ -54,6 +54,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const unsigned *k
 
 } // namespace
 
+int pg_scan_blocks(int n) { return n > 0 ? (n + SCAN_TILE - 1) / SCAN_TILE : 1; }
+
+int pg_sort_passes_exact(int key_bits)
+{
+  int p = (key_bits + 7) / 8;
+  return p < 1 ? 1 : p;
+}
+
 int pg_sort_blocks(int n) { return n > 0 ? (n + SORT_TILE - 1) / SORT_TILE : 1; }
 
 int pg_sort_passes(int bits_per_axis) { return pg_sort_passes_bits(3 * bits_per_axis); }

@@ -77,9 +77,21 @@ struct PgDev
   double *nnrm[3], *ndep;   // optional: normal and depth (parity exports only)
   int record_geometry;
   double *fm[3], *tm[3];    // [parnum] master-side partial force and torque sums
-  int kr;                   // slave slots per particle
-  int *rcnt;                // [parnum]
-  int *rref;                // [kr][parnum]: entry index slot*ellnum + sphere
+  int kr;                   // (unused: slave lists have no per-particle limit)
+  // slave lists, CSR over particles: the entries that name particle p as
+  // partner are rref[soff[p] .. soff[p+1]), each the candidate-entry index
+  // slot*ellnum + sphere, ordered by (master particle, slot)
+  int *rcnt;                // [parnum] entries per particle
+  int *soff;                // [parnum+1]
+  int *rref;                // = sval[0] after the entry sort
+  int *eorder;              // [ellnum] spheres in particle order (stable)
+  int *eoff;                // [ellnum+1] first entry of each sphere of eorder; eoff[ellnum] = total
+  unsigned *skey[2];        // [kn*ellnum] entry sort: partner particle (0xffffffff: none)
+  int *sval[2];             // [kn*ellnum] entry sort: entry index
+  unsigned *shist;          // entry-sort tile histograms
+  int *smeta;               // [4]: entries, tiles, histogram length, scan tiles of it
+  unsigned *sbs;            // scan block sums
+  int sbits;                // bits of the entry-sort keys
 
   // ---- rebuild machinery
   int *rebuild;             // 1 when the candidate lists must be rebuilt

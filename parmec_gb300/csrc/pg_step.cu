@@ -786,10 +786,10 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
     // slave contacts, in master order (forces.ispc:539-569)
     if (E)
     {
-      const int nr = d.rcnt[i];
-      for (int r = 0; r < nr; r ++)
+      const int rb = d.soff[i], re = d.soff[i+1];
+      for (int r = rb; r < re; r ++)
       {
-        const int ref = d.rref[(size_t)r * d.parnum + i];
+        const int ref = d.rref[r];
         if (!d.nflag[ref]) continue;
         double f[3] = {-d.nfrc[0][ref], -d.nfrc[1][ref], -d.nfrc[2][ref]};
         double a[3] = {d.npnt[0][ref]-po[0], d.npnt[1][ref]-po[1], d.npnt[2][ref]-po[2]};

@@ -172,3 +172,72 @@ def batch_scenes(count=512, seed=3, nmin=2048, nmax=65536):
     for k in range(count):
         out.append(shaken_box(int(ns[k]), seed * 100003 + k, float(fs[k]), float(amps[k])))
     return out
+
+
+def critical_spring_step(kmax, m_eff, emax):
+    """Critical step of a spring with largest curve slope kmax, effective mass
+    m_eff and largest dashpot slope emax: (2/w)(sqrt(1+ksi^2) - ksi) with
+    w = sqrt(kmax/m_eff), ksi = emax/(2 m_eff w) (the formula of
+    critical_perspring, parmec.ispc:485-544)."""
+    w = math.sqrt(kmax / m_eff)
+    ksi = emax / (2.0 * m_eff * w)
+    return (2.0 / w) * (math.sqrt(1.0 + ksi * ksi) - ksi)
+
+
+def spring_lattice(n_side=256, seed=2, edge=0.01, gap=0.002, density=2500.0):
+    """Config 2, the spring-lattice shaking table: n_side x n_side rigid
+    hexahedral MESH particles (12 triangles each) joined to their right and
+    upper neighbours by SPRINGs with 8-point random monotone force-stroke
+    curves (segment slopes in [1e4, 1e6] N/m) and lookup dashpots; each cube
+    hangs on one more spring from a base plate MESH particle whose motion is a
+    PRESCRIBEd acceleration 0.5 g sin(2 pi 5 t) along x.  Gravity -9.81 z.
+    Returns (model, dt) with dt = 0.1 of the critical spring step."""
+    from .model import Model
+    from . import mesh
+    rng = np.random.default_rng(seed)
+    m = Model()
+    mat = m.material(density, 1e9, 0.25)
+    h = edge + gap
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij"), axis=-1).reshape(-1, 2)
+    origins = np.zeros((len(ij), 3))
+    origins[:, 0] = ij[:, 0] * h
+    origins[:, 1] = ij[:, 1] * h
+    parts = mesh.hex_grid(m, origins, edge, mat, 1)
+    # the base plate: one flat hexahedron under the grid
+    L = n_side * h
+    z0 = -gap - edge
+    bx = [(-gap, -gap, z0), (L, -gap, z0), (L, L, z0), (-gap, L, z0),
+          (-gap, -gap, -gap), (L, -gap, -gap), (L, L, -gap), (-gap, L, -gap)]
+    base = m.mesh([v for p in bx for v in p], [8, 0, 1, 2, 3, 4, 5, 6, 7, mat], mat, 1)
+    idx = {(int(a), int(b)): int(p) for (a, b), p in zip(ij, parts)}
+    half = 0.5 * edge
+    kmax = emax = 0.0
+
+    def curve():
+        nonlocal kmax
+        s = np.linspace(-0.75 * gap, 0.75 * gap, 8)
+        k = rng.uniform(1e4, 1e6, 7)
+        kmax = max(kmax, float(k.max()))
+        f = np.concatenate([[0.0], np.cumsum(k * np.diff(s))])
+        f -= np.interp(0.0, s, f)
+        return [float(v) for pair in zip(s, f) for v in pair]
+
+    m_cube = density * edge ** 3
+    c = 2.0 * 0.1 * math.sqrt(5e5 * 0.5 * m_cube)
+    dash = [-1.0, -c, 1.0, c]
+    emax = c
+    for (a, b), p in idx.items():
+        cx, cy = a * h + half, b * h + half
+        for da, db in ((1, 0), (0, 1)):
+            q = idx.get((a + da, b + db))
+            if q is None:
+                continue
+            pa = (cx + half * da, cy + half * db, half)
+            pb = (cx + (h - half) * da, cy + (h - half) * db, half)
+            m.spring(p, pa, q, pb, curve(), dashpot=dash)
+        m.spring(base, (cx, cy, -gap), p, (cx, cy, 0.0), curve(), dashpot=dash)
+    m.prescribe_motion(base, linear=lambda t: (0.5 * 9.81 * math.sin(2.0 * math.pi * 5.0 * t), 0.0, 0.0),
+                       kind="av")
+    m.set_gravity(0.0, 0.0, -9.81)
+    dt = 0.1 * critical_spring_step(kmax, 0.5 * m_cube, emax)
+    return m, dt

@@ -86,14 +86,16 @@ class _Ranges:
 
 
 def bytes_per_sphere(form, kn=32, kr=32):
-    """Device bytes one pooled sphere particle needs (state, candidate and slave lists)."""
-    state = 8 * (6 + 3 + 9 + 6 + 9 + 9 + 2 + 3 + 3) + 8 * (6 + 3) + 4 * 12 + 8 * 6 + 8 * 3
+    """Device bytes one pooled sphere particle needs: state, candidate lists
+    (kn slots) and the slave-list entry buffers (two key and two value words
+    per slot); kr is accepted for older callers and unused."""
+    state = 8 * (6 + 3 + 9 + 6 + 9 + 9 + 2 + 3 + 3) + 8 * (6 + 3) + 4 * 12 + 8 * 6 + 8 * 3 + 4 * 4
     if form == abi.PG_FORM_MIXED:
-        state += 4 * (6 + 6 + 18 + 6 + 2 + 2 + 18 + 6 + 6 + 6)
+        state += 4 * (6 + 6 + 18 + 6 + 2 + 2 + 18 + 6 + 6 + 6 + 2 + 3)
         slots = kn * (4 + 1 + 12 + 12 + 12)
     else:
         slots = kn * (4 + 1 + 24 + 24 + 24 + 24 + 8)
-    return state + slots + kr * 4 + 16
+    return state + slots + kn * 16 + 16
 
 
 class Server:

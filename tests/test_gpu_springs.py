@@ -151,3 +151,55 @@ def test_prescribed_velocity_and_acceleration_bitwise(gpu_lib, oracle_lib):
         m.dem(100 * dt, dt, interval=1e9, engine=eng)
         out.append(m)
     assert_bitwise(out[0], out[1])
+
+
+def test_mesh_spring_lattice_bitwise(gpu_lib, oracle_lib):
+    """The spring-lattice shaking table (MESH cubes, 8-point spring curves,
+    lookup dashpots, prescribed base): particles, mesh nodes, triangles and
+    spring state equal the oracle's bit for bit."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import spring_lattice
+    (mg, dt), (mo, _) = spring_lattice(6), spring_lattice(6)
+    mg.dem(250 * dt - 0.5 * dt, dt, interval=1e9, engine=GpuEngine())
+    mo.dem(250 * dt - 0.5 * dt, dt, interval=1e9, engine=OracleEngine())
+    assert_bitwise(mg, mo)
+    spring_state_equal(mg, mo)
+    assert np.array_equal(bits(mg.N.nodes[:, :mg.nodnum]), bits(mo.N.nodes[:, :mo.nodnum]))
+    assert np.array_equal(bits(mg.Tr.tri[:, :mg.trinum]), bits(mo.Tr.tri[:, :mo.trinum]))
+    assert np.max(np.abs(mg.P.linear[0, :mg.parnum])) > 0.0      # the table moved the lattice
+
+
+def test_spheres_on_a_mesh_particle_bitwise(gpu_lib, oracle_lib):
+    """Spheres fall on a MESH plate that rests on springs: sphere-triangle
+    contacts whose partner is a particle (the reaction goes to the plate
+    through the slave lists)."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.model import Model
+
+    def make():
+        rng = np.random.default_rng(5)
+        m = Model()
+        mat = m.material(2000.0, 1e9, 0.25)
+        a = 0.1
+        nodes = [0.0, 0.0, 0.0, a, 0.0, 0.0, a, a, 0.0, 0.0, a, 0.0,
+                 0.0, 0.0, 0.01, a, 0.0, 0.01, a, a, 0.01, 0.0, a, 0.01]
+        plate = m.mesh(nodes, [8, 0, 1, 2, 3, 4, 5, 6, 7, 0], mat, 2)
+        for k in range(4):
+            for x, y in ((0.02, 0.02), (0.08, 0.02), (0.02, 0.08), (0.08, 0.08)):
+                m.spring(plate, (x, y, 0.0), -1, (x, y, -0.01), [-1.0, -2e4, 1.0, 2e4], dashpot=0.3)
+        for s in range(36):
+            c = (0.012 + 0.015 * (s % 6), 0.012 + 0.015 * (s // 6), 0.0158 + 0.0005 * rng.random())
+            m.sphere(c, 0.006, mat, 1)
+        m.granular(0, 0, 1e4, 0.3, 0.4)
+        m.set_gravity(0.0, 0.0, -9.81)
+        return m
+    step = 2e-5
+    mg, mo = make(), make()
+    mg.dem(400 * step - 0.5 * step, step, interval=1e9, engine=GpuEngine())
+    eo = OracleEngine()
+    mo.dem(400 * step - 0.5 * step, step, interval=1e9, engine=eo)
+    assert_bitwise(mg, mo)
+    assert len(eo.contacts()["mpart"]) >= 10                   # spheres rest on the plate
+    assert np.array_equal(bits(mg.Tr.tri[:, :mg.trinum]), bits(mo.Tr.tri[:, :mo.trinum]))
