@@ -244,11 +244,20 @@ def spring_lattice_form(args, n_side):
     ev1.record(stream)
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1)
+    # per kernel group, from a short profiled run of the same session
+    eng.profile(True)
+    nprof = 10
+    times2, _ = driver.step_times(end_time, nprof * dt - 0.5 * dt, dt)
+    tabs2 = driver.StepTables(m, times2, dt, [1e9, 1e9], [None, None], [-1, -1])
+    eng.run(tabs2.ctab(0, len(times2)), dt)
+    groups = eng.profile_read()
+    eng.profile(False)
     out = {"workload": f"{n_side}x{n_side} MESH hexahedra (10 mm), {m.sprnum} springs, {m.trinum} triangles, "
                        "base 0.5 g sin(2 pi 5 t) along x, FP64", "steps": steps, "dt": dt,
            "value": m.parnum * steps / (ms * 1e-3), "unit": "particle-steps/s",
            "spring_steps_per_s": m.sprnum * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-           "particles": m.parnum, "springs": m.sprnum, "build_s": build_s}
+           "particles": m.parnum, "springs": m.sprnum, "build_s": build_s,
+           "kernel_ms": {k: round(v[0] / nprof, 4) for k, v in groups.items()}}
     eng.close()
     return out
 

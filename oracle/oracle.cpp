@@ -1017,6 +1017,107 @@ double eqm(const pg_scene *s, int part1, const double *point1, int part2, const 
   return mass;
 }
 
+/* ---------------- springs_task's force flushes (forces.ispc:1207-1412) -----
+ * Springs are sorted by (part0, part1).  One task adds a run of springs with
+ * equal part0 to that particle (+=) and a run with equal part1 to that one
+ * (-=), each run summed in spring order, the first run of its kind starting
+ * from zero and later ones from their first element.  A run longer than
+ * SPRING_RUN_LONG springs is summed in chunks (chunk sums in order, then the
+ * chunk sums in order), as tasks whose boundaries fall on the chunks would
+ * flush it; the GPU uses the same definition. */
+static const int SPRING_RUN_LONG = 64;
+static const int SPRING_RUN_MAXCHUNKS = 512;
+
+static int spring_run_chunk(int len)
+{
+  int c = 256;
+  while ((len + c - 1) / c > SPRING_RUN_MAXCHUNKS) c *= 2;
+  return c;
+}
+
+struct SprRun { int part, type, b, e, first; long long pos; };
+
+static void add6(double *acc, const double *x, bool assign)
+{
+  for (int c = 0; c < 6; c ++) acc[c] = assign ? x[c] : acc[c] + x[c];
+}
+
+// sum of one run: acc[0..2] force, acc[3..5] torque
+static void spring_run_sum(const pg_scene *s, double *const out[9], const SprRun &r, double *acc)
+{
+  const int off = r.type == 0 ? 3 : 6;
+  for (int c = 0; c < 6; c ++) acc[c] = 0.0;
+  bool started = false;
+  auto element = [&](int i, double *x) {
+    x[0] = out[0][i]; x[1] = out[1][i]; x[2] = out[2][i];
+    x[3] = out[off][i]; x[4] = out[off+1][i]; x[5] = out[off+2][i];
+  };
+  auto skipped = [&](int i) { return r.type == 1 && s->sprpart[1][i] < 0; };
+  if (r.e - r.b <= SPRING_RUN_LONG)
+  {
+    for (int i = r.b; i < r.e; i ++)
+    {
+      if (skipped(i)) continue;
+      double x[6];
+      element(i, x);
+      add6(acc, x, !started && !r.first);
+      started = true;
+    }
+    return;
+  }
+  const int len = r.e - r.b, ch = spring_run_chunk(len);
+  for (int b = r.b; b < r.e; b += ch)
+  {
+    double part[6] = {0, 0, 0, 0, 0, 0};
+    bool any = false;
+    for (int i = b; i < std::min(b + ch, r.e); i ++)
+    {
+      if (skipped(i)) continue;
+      double x[6];
+      element(i, x);
+      add6(part, x, !any);
+      any = true;
+    }
+    if (!any) continue;
+    add6(acc, part, !started && !r.first);
+    started = true;
+  }
+}
+
+static void spring_flush(pg_scene *s, double *const out[9])
+{
+  const int S = s->sprnum;
+  std::vector<SprRun> runs;
+  int j0 = -1, k0 = -1, jb = 0, kb = 0;
+  bool firstj = true, firstk = true;
+  for (int i = 0; i < S; i ++)
+  {
+    const int j = s->sprpart[0][i], k = s->sprpart[1][i];
+    if (j0 != j && j0 >= 0) { runs.push_back({j0, 0, jb, i, firstj ? 1 : 0, 2LL*i}); firstj = false; jb = i; }
+    if (j0 < 0) jb = i;
+    if (k >= 0)
+    {
+      if (k0 != k && k0 >= 0) { runs.push_back({k0, 1, kb, i, firstk ? 1 : 0, 2LL*i + 1}); firstk = false; kb = i; }
+      if (k0 < 0) kb = i;
+      k0 = k;
+    }
+    j0 = j;
+  }
+  if (j0 >= 0) runs.push_back({j0, 0, jb, S, firstj ? 1 : 0, 2LL*S});
+  if (k0 >= 0) runs.push_back({k0, 1, kb, S, firstk ? 1 : 0, 2LL*S + 1});
+  for (const SprRun &r : runs)                 /* in stream order */
+  {
+    double acc[6];
+    spring_run_sum(s, out, r, acc);
+    const double sg = r.type == 0 ? 1.0 : -1.0;
+    for (int c = 0; c < 3; c ++)
+    {
+      if (sg > 0) { s->force[c][r.part] += acc[c]; s->torque[c][r.part] += acc[3+c]; }
+      else { s->force[c][r.part] -= acc[c]; s->torque[c][r.part] -= acc[3+c]; }
+    }
+  }
+}
+
 /* ---------------- forces.ispc:641-1412 springs_task (single task) --------- */
 void springs_all(pg_scene *s, double step, double time)
 {
@@ -1024,7 +1125,9 @@ void springs_all(pg_scene *s, double step, double time)
   double oj[3] = {0}, vj[3] = {0}, xj[3] = {0}, Xj[3] = {0}, Lj[9] = {0};
   double ok[3] = {0}, vk[3] = {0}, xk[3] = {0}, Xk[3] = {0}, Lk[9] = {0};
   int j0 = -1, k0 = -1;
-  double fj[3] = {0.0, 0.0, 0.0}, tj[3] = {0.0, 0.0, 0.0}, fk[3] = {0.0, 0.0, 0.0}, tk[3] = {0.0, 0.0, 0.0};
+  std::vector<double> outv(9 * (size_t)std::max(S, 1), 0.0);
+  double *out[9];
+  for (int m = 0; m < 9; m ++) out[m] = outv.data() + (size_t)m * std::max(S, 1);
 
   for (int i = 0; i < S; i ++)
   {
@@ -1328,51 +1431,18 @@ void springs_all(pg_scene *s, double step, double time)
     trq[1] = a[2]*frc[0] - a[0]*frc[2];
     trq[2] = a[0]*frc[1] - a[1]*frc[0];
 
-    if (j0 != j && j0 >= 0)
-    {
-      s->force[0][j0] += fj[0]; s->force[1][j0] += fj[1]; s->force[2][j0] += fj[2];
-      s->torque[0][j0] += tj[0]; s->torque[1][j0] += tj[1]; s->torque[2][j0] += tj[2];
-      fj[0] = frc[0]; fj[1] = frc[1]; fj[2] = frc[2];
-      tj[0] = trq[0]; tj[1] = trq[1]; tj[2] = trq[2];
-    }
-    else
-    {
-      fj[0] += frc[0]; fj[1] += frc[1]; fj[2] += frc[2];
-      tj[0] += trq[0]; tj[1] += trq[1]; tj[2] += trq[2];
-    }
-
+    out[0][i] = frc[0]; out[1][i] = frc[1]; out[2][i] = frc[2];
+    out[3][i] = trq[0]; out[4][i] = trq[1]; out[5][i] = trq[2];
     if (k >= 0)
     {
-      trq[0] = b[1]*frc[2] - b[2]*frc[1];
-      trq[1] = b[2]*frc[0] - b[0]*frc[2];
-      trq[2] = b[0]*frc[1] - b[1]*frc[0];
-      if (k0 != k && k0 >= 0)
-      {
-        s->force[0][k0] -= fk[0]; s->force[1][k0] -= fk[1]; s->force[2][k0] -= fk[2];
-        s->torque[0][k0] -= tk[0]; s->torque[1][k0] -= tk[1]; s->torque[2][k0] -= tk[2];
-        fk[0] = frc[0]; fk[1] = frc[1]; fk[2] = frc[2];
-        tk[0] = trq[0]; tk[1] = trq[1]; tk[2] = trq[2];
-      }
-      else
-      {
-        fk[0] += frc[0]; fk[1] += frc[1]; fk[2] += frc[2];
-        tk[0] += trq[0]; tk[1] += trq[1]; tk[2] += trq[2];
-      }
+      out[6][i] = b[1]*frc[2] - b[2]*frc[1];
+      out[7][i] = b[2]*frc[0] - b[0]*frc[2];
+      out[8][i] = b[0]*frc[1] - b[1]*frc[0];
       k0 = k;
     }
     j0 = j;
   }
-
-  if (j0 >= 0)
-  {
-    s->force[0][j0] += fj[0]; s->force[1][j0] += fj[1]; s->force[2][j0] += fj[2];
-    s->torque[0][j0] += tj[0]; s->torque[1][j0] += tj[1]; s->torque[2][j0] += tj[2];
-  }
-  if (k0 >= 0)
-  {
-    s->force[0][k0] -= fk[0]; s->force[1][k0] -= fk[1]; s->force[2][k0] -= fk[2];
-    s->torque[0][k0] -= tk[0]; s->torque[1][k0] -= tk[1]; s->torque[2][k0] -= tk[2];
-  }
+  spring_flush(s, out);
 }
 
 /* ---------------- input.cpp:4247-4341 prescribe_acceleration -------------- */

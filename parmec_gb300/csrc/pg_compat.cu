@@ -715,9 +715,11 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     for (int k = 0; ok && k < 2; k ++) ok = up(d.lcurve[k], nlc > 0 ? lcurve[k] : nullptr, nl);
     for (int k = 0; ok && k < 9; k ++) ok = grow(d.spr_out[k], S);
     std::vector<int> first;
-    std::vector<int4> ev;
-    pg_spring_events(parnum, (int)S, sprpart[0], sprpart[1], first, ev);
-    ok = ok && up(d.sev_first, first.data(), P + 1) && up(d.sev, ev.data(), ev.size());
+    std::vector<int4> ev, big;
+    pg_spring_events(parnum, (int)S, sprpart[0], sprpart[1], first, ev, big);
+    ok = ok && up(d.sev_first, first.data(), P + 1) && up(d.sev, ev.data(), ev.size()) &&
+         up(d.sbig, big.data(), big.size()) && grow(d.sbig_sum, 6 * std::max<size_t>(1, big.size()));
+    d.nbig = (int)big.size();
   }
   if (!ok) return;
   PgDev v = view();
@@ -729,6 +731,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   if (!contacts) { v.ellnum = 0; v.pell = nullptr; }
   pg_launch_contacts(v, G.st, step);
   pg_launch_springs(v, G.st, step);
+  if (S) pg_launch_spring_runs(v, G.st);
   pg_launch_force_sums(v, G.st);
   G.launches += (v.ellnum ? 1 : 0) + (S ? 1 : 0) + 1;
   for (int k = 0; ok && k < 3; k ++) ok = down(force[k], d.force[k], P) && down(torque[k], d.torque[k], P);

@@ -11,6 +11,7 @@ void pg_launch_shapes(const PgDev &d, cudaStream_t s, bool skip_analytical);
 void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step);   // velocities from obsang/obslin
 void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step);
+void pg_launch_spring_runs(const PgDev &d, cudaStream_t s);     // sums of the long flush runs
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_force_sums(const PgDev &d, cudaStream_t s);                          // forces() tail
 void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1); // dynamics()
@@ -34,7 +35,10 @@ int  pg_fused_candidates(PgFusedCfg *out, int cap);
 cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int nsteps, const PgFusedCfg &c);
 
 // pg_session.cu
-void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &ev);
+// spring flush runs longer than this are summed by k_spring_runs
+#define PG_SPRING_RUN_LONG 64
+void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &ev,
+                      std::vector<int4> &big);
 
 // pg_sort.cu
 int  pg_sort_blocks(int n);

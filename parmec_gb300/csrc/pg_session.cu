@@ -57,7 +57,8 @@ struct pg_session
 // the order one springs_task applies them (forces.ispc:1207-1412): springs
 // sorted by (part0, part1) flush a run of equal part0 with += and a run of
 // equal part1 with -=; 'w' marks the first run of its kind, which assigns
-void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &evv)
+void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<int> &first, std::vector<int4> &evv,
+                      std::vector<int4> &big)
 {
   struct Ev { int part; long long pos; int4 v; };
   std::vector<Ev> ev;
@@ -92,7 +93,19 @@ void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<in
     return a.part != b.part ? a.part < b.part : a.pos < b.pos; });
   first.assign(P + 1, 0);
   evv.assign(std::max<size_t>(1, ev.size()), make_int4(0, 0, 0, 0));
-  for (size_t q = 0; q < ev.size(); q ++) { first[ev[q].part + 1] ++; evv[q] = ev[q].v; }
+  big.clear();
+  for (size_t q = 0; q < ev.size(); q ++)
+  {
+    first[ev[q].part + 1] ++;
+    evv[q] = ev[q].v;
+    // a long run is summed by its own block beforehand (k_spring_runs); its
+    // index + 1 sits above the run type in .x
+    if (ev[q].v.z - ev[q].v.y > PG_SPRING_RUN_LONG)
+    {
+      big.push_back(ev[q].v);
+      evv[q].x |= (int)big.size() << 1;
+    }
+  }
   for (int p = 0; p < P; p ++) first[p+1] += first[p];
 }
 
@@ -251,12 +264,17 @@ int upload_static(pg_session *s, const pg_scene *sc)
   // spring flush events: the single-task springs_task order (forces.ispc:1207-1412)
   {
     std::vector<int> first;
-    std::vector<int4> evv;
-    pg_spring_events(P, sc->sprnum, sc->sprpart[0], sc->sprpart[1], first, evv);
+    std::vector<int4> evv, big;
+    pg_spring_events(P, sc->sprnum, sc->sprpart[0], sc->sprpart[1], first, evv, big);
     TRY(dalloc(s, &d.sev_first, P + 1));
     TRY(dalloc(s, &d.sev, evv.size()));
     TRY(h2d(s, d.sev_first, first.data(), P + 1));
     TRY(h2d(s, d.sev, evv.data(), evv.size()));
+    d.nbig = (int)big.size();
+    TRY(dalloc(s, &d.sbig, std::max<size_t>(1, big.size())));
+    TRY(dalloc(s, &d.sbig_sum, 6 * std::max<size_t>(1, big.size())));
+    TRY(h2d(s, d.sbig, big.data(), big.size()));
+    CK(cudaStreamSynchronize(s->stream));
   }
   return PG_OK;
 }
@@ -837,6 +855,7 @@ void enqueue_step(pg_session *s, double step)
   }
   pg_launch_contacts(d, s->stream, step);
   pg_launch_springs(d, s->stream, step);
+  pg_launch_spring_runs(d, s->stream);
   pg_launch_integrate(d, s->stream, step);
   pg_launch_mesh(d, s->stream);
   pg_launch_obstacles_row(d, s->stream, step);
@@ -1053,7 +1072,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       if (d.form == PG_FORM_MIXED) pg_launch_contacts_mx(d, s->stream, step);
       else pg_launch_contacts(d, s->stream, step);
       CK(cudaEventRecord(ev[2], s->stream));
-      if (d.form != PG_FORM_MIXED) pg_launch_springs(d, s->stream, step);
+      if (d.form != PG_FORM_MIXED) { pg_launch_springs(d, s->stream, step); pg_launch_spring_runs(d, s->stream); }
       CK(cudaEventRecord(ev[3], s->stream));
       if (d.form == PG_FORM_MIXED) pg_launch_integrate_mx(d, s->stream, step);
       else pg_launch_integrate(d, s->stream, step);

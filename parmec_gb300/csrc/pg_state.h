@@ -54,7 +54,10 @@ struct PgDev
   double *lcurve[2]; int *lcidx;
   double *spr_out[9];       // per spring: frc[3], trq_j[3], trq_k[3]
   int *sev_first;           // [parnum+1] CSR of spring force events per particle
-  int4 *sev;                // (type, begin, end, first): type 0 = j-run (+=), 1 = k-run (-=)
+  int4 *sev;                // (type | (long run + 1) << 1, begin, end, first): type 0 = j-run (+=), 1 = k-run (-=)
+  int4 *sbig;               // [nbig] the long runs
+  double *sbig_sum;         // [nbig][6] their force and torque sums
+  int nbig;
 
   // ---- prescribed motion
   int *prs_first;           // [parnum+1] CSR of prescriptions per particle

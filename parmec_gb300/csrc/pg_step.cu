@@ -745,6 +745,63 @@ __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
 // contacts_acc_task (slave side) + gravity + spring flushes (single-task order
 // of springs_task) + prescribe_acceleration + dynamics_task +
 // prescribe_velocity + ellipsoids_task, one thread per particle.
+// ---------------------------------------------------------------- long spring flush runs
+// A run longer than PG_SPRING_RUN_LONG springs is summed in chunks: each
+// chunk in spring order (first element assigned), then the chunk sums in
+// order (the first-run rule applied to them), as springs_task tasks whose
+// boundaries fall on the chunks would flush it.  One block per run: thread c
+// sums chunk c, thread 0 sums the chunk sums.  A dependent FP64 add costs
+// tens of ns on this part, so one thread cannot sum 10^5 springs per step.
+constexpr int RUN_THREADS = 256;
+constexpr int RUN_MAXCHUNKS = 512;
+
+__device__ __forceinline__ int run_chunk(int len)
+{
+  int c = 256;
+  while ((len + c - 1) / c > RUN_MAXCHUNKS) c *= 2;
+  return c;
+}
+
+__global__ void __launch_bounds__(RUN_THREADS) k_spring_runs(PgDev d)
+{
+  __shared__ double part[6][RUN_MAXCHUNKS];
+  __shared__ unsigned char has[RUN_MAXCHUNKS];
+  const int4 v = d.sbig[blockIdx.x];
+  const int type = v.x & 1, off = type == 0 ? 3 : 6;
+  const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
+  for (int c = threadIdx.x; c < nc; c += RUN_THREADS)
+  {
+    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    bool any = false;
+    const int b = v.y + c * ch, e = min(b + ch, v.z);
+    for (int s = b; s < e; s ++)
+    {
+      if (type == 1 && d.sprpart[1][s] < 0) continue;
+      const double x[6] = {d.spr_out[0][s], d.spr_out[1][s], d.spr_out[2][s],
+                           d.spr_out[off][s], d.spr_out[off+1][s], d.spr_out[off+2][s]};
+      if (!any) for (int k = 0; k < 6; k ++) a[k] = x[k];
+      else for (int k = 0; k < 6; k ++) a[k] = a[k] + x[k];
+      any = true;
+    }
+    for (int k = 0; k < 6; k ++) part[k][c] = a[k];
+    has[c] = any ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    bool started = false;
+    for (int c = 0; c < nc; c ++)
+    {
+      if (!has[c]) continue;
+      if (!started && !v.w) for (int k = 0; k < 6; k ++) acc[k] = part[k][c];
+      else for (int k = 0; k < 6; k ++) acc[k] = acc[k] + part[k][c];
+      started = true;
+    }
+    for (int k = 0; k < 6; k ++) d.sbig_sum[6*blockIdx.x + k] = acc[k];
+  }
+}
+
 // MODE: INT_FUSED runs the whole particle update of one step; the drop-in
 // entry points split it as the reference does: INT_FORCES ends with the
 // force and torque sums (the tail of forces(), forces.ispc:453-596) and
@@ -809,12 +866,19 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       for (int ev = d.sev_first[i]; ev < d.sev_first[i+1]; ev ++)
       {
         const int4 v = d.sev[ev];
-        const int off = v.x == 0 ? 3 : 6;
+        const int type = v.x & 1, run = (v.x >> 1) - 1;
+        const int off = type == 0 ? 3 : 6;
         double af[3] = {0.0, 0.0, 0.0}, at[3] = {0.0, 0.0, 0.0};
         bool started = false;
+        if (run >= 0)
+        {
+          // a long run, summed in the same order by k_spring_runs
+          for (int c = 0; c < 3; c ++) { af[c] = d.sbig_sum[6*run + c]; at[c] = d.sbig_sum[6*run + 3 + c]; }
+        }
+        else
         for (int s = v.y; s < v.z; s ++)
         {
-          if (v.x == 1 && d.sprpart[1][s] < 0) continue;
+          if (type == 1 && d.sprpart[1][s] < 0) continue;
           double fr[3] = {d.spr_out[0][s], d.spr_out[1][s], d.spr_out[2][s]};
           double tq[3] = {d.spr_out[off][s], d.spr_out[off+1][s], d.spr_out[off+2][s]};
           if (!started && !v.w)
@@ -829,7 +893,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
           }
           started = true;
         }
-        if (v.x == 0)
+        if (type == 0)
         {
           F[0] += af[0]; F[1] += af[1]; F[2] += af[2];
           T[0] += at[0]; T[1] += at[1]; T[2] += at[2];
@@ -1031,6 +1095,11 @@ void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
   if (d.sprnum) k_springs<<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
 }
 
+void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
+{
+  if (d.sprnum && d.nbig > 0) k_spring_runs<<<d.nbig, RUN_THREADS, 0, s>>>(d);
+}
+
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
 {
   if (d.parnum) k_integrate<INT_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, step, step);
@@ -1071,7 +1140,7 @@ int pg_step_kernel_count(const PgDev &d)
 {
   int n = 2;                                   // excite, tail
   if (d.ellnum) n += 1;                        // contacts
-  if (d.sprnum) n += 1;
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0);
   if (d.parnum) n += 1;                        // integrate
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;

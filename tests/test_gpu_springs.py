@@ -160,7 +160,7 @@ def test_mesh_spring_lattice_bitwise(gpu_lib, oracle_lib):
     from oracle.pyoracle import OracleEngine
     from parmec_gb300.engine import GpuEngine
     from parmec_gb300.scenes import spring_lattice
-    (mg, dt), (mo, _) = spring_lattice(6), spring_lattice(6)
+    (mg, dt), (mo, _) = spring_lattice(17), spring_lattice(17)     # 289 base springs: a long run of two chunks
     mg.dem(250 * dt - 0.5 * dt, dt, interval=1e9, engine=GpuEngine())
     mo.dem(250 * dt - 0.5 * dt, dt, interval=1e9, engine=OracleEngine())
     assert_bitwise(mg, mo)
