@@ -261,6 +261,12 @@ int pg_session_autotune(pg_session *s, int on);
 /* out4 = {threads per block, blocks, 1 if tuned, 1 if running as a graph}. */
 int pg_session_fused_config(pg_session *s, int *out4);
 
+/* Self-test of the bounded grid barrier used by the cooperative kernels: a
+ * small cooperative grid waits at a barrier that cannot complete, gives up
+ * after its 2 s limit and records PG_ERR_TIMEOUT; the session stays usable.
+ * Returns PG_OK when the timeout was recorded (wait_ms: the kernel's time). */
+int pg_session_barrier_selftest(pg_session *s, double *wait_ms);
+
 /* ---- scenes sharing a session -------------------------------------------
  * Every scene has its own grid origin (cells of a common size), its own
  * triangles, an active flag, a local time origin and optionally a base

@@ -162,6 +162,7 @@ def load_library():
         "pg_session_use_fused": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_autotune": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_fused_config": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "pg_session_barrier_selftest": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
         "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_diagnostics": (ctypes.c_int, [P, I]),
         "pg_cell_order": (ctypes.c_int, [P, P, P, ctypes.c_int, D, ctypes.c_double, I, P, P, P]),

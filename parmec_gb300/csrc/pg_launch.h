@@ -55,6 +55,7 @@ int  pg_sort_passes_exact(int key_bits);                      // 8-bit passes, n
 
 // pg_rebuild.cu
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s);
+cudaError_t pg_launch_barrier_probe(const PgDev &d, cudaStream_t s, int blocks);   // see pg_session_barrier_selftest
 void pg_launch_rebuild_gate(const PgDev &d, cudaStream_t s);   // sets *rebuild when a sphere or vertex moved
 int  pg_rebuild_kernel_count(const PgDev &d);
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin);

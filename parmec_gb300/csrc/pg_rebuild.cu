@@ -45,6 +45,14 @@ __global__ void __launch_bounds__(B) k_rebuild_coop(PgDev d, int passes, int epa
   rebuild_all<B>(d, passes, epasses, sm, NoHook());
 }
 
+// self-test of the bounded grid barrier: the host presets the arrival count
+// to the grid size, so no arrival completes the barrier and every block
+// waits until the 2 s limit, records PG_ERR_TIMEOUT and leaves
+__global__ void k_barrier_probe(PgDev d)
+{
+  grid_barrier(d);
+}
+
 constexpr int RB_THREADS = 256;
 
 // blocks of the cooperative rebuild grid: all that fit at once
@@ -129,6 +137,20 @@ void pg_rebuild_key_bits(PgDev &d)
 // use, so that the 0xffffffff key of a free entry sorts strictly after every
 // valid key (a valid key of all ones in the sorted bits would tie with it)
 int pg_rebuild_sort_bits(const PgDev &d) { return d.keybits + (d.escene ? 1 : 0); }
+
+cudaError_t pg_launch_barrier_probe(const PgDev &d, cudaStream_t s, int blocks)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_barrier_probe, d);
+}
 
 void pg_launch_rebuild(const PgDev &d, cudaStream_t s)
 {

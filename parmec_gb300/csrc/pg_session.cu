@@ -1395,6 +1395,38 @@ int pg_session_diagnostics(pg_session *s, int *out16)
   return PG_OK;
 }
 
+int pg_session_barrier_selftest(pg_session *s, double *wait_ms)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  CK(cudaStreamSynchronize(s->stream));
+  const int blocks = 8;
+  const unsigned preset[4] = {(unsigned)blocks, 0u, 0u, 0u};     // arrivals already at the grid size
+  const int zero[4] = {0, 0, 0, 0};
+  TRY(h2d(s, d.gbar, preset, 4));
+  TRY(h2d(s, d.err, zero, 4));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s->stream));
+  CK(pg_launch_barrier_probe(d, s->stream, blocks));
+  CK(cudaEventRecord(e1, s->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (wait_ms) *wait_ms = ms;
+  int err[4];
+  CK(cudaMemcpy(err, d.err, sizeof err, cudaMemcpyDeviceToHost));
+  // leave the barrier and the error record clean for the session's own kernels
+  const unsigned clean[4] = {0u, 0u, 0u, 0u};
+  TRY(h2d(s, d.gbar, clean, 4));
+  TRY(h2d(s, d.err, zero, 4));
+  CK(cudaStreamSynchronize(s->stream));
+  return err[0] == PG_ERR_TIMEOUT ? PG_OK : PG_ERR_ARGUMENT;
+}
+
 int pg_session_kernel_launches(pg_session *s, long long *count)
 {
   if (!s || !count) return PG_ERR_ARGUMENT;
