@@ -343,6 +343,7 @@ def main():
     ap.add_argument("--spheres", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=512, help="scenes of the batched leg")
     ap.add_argument("--serving", type=int, default=48, help="requests in the serving stream (0: skip)")
     ap.add_argument("--lattice", type=int, default=256, help="side of the spring lattice (0: skip)")
     args = ap.parse_args()
@@ -502,7 +503,7 @@ def main():
     }
     if not args.no_batched:
         from parmec_gb300.scenes import batch_scenes
-        line["batched"] = batched_form(args, batch_scenes(512))
+        line["batched"] = batched_form(args, batch_scenes(args.batch_scenes))
     line["mixed"] = mixed_form(args, ref64)
     if args.lattice > 0:
         line["spring_lattice"] = spring_lattice_form(args, args.lattice)

@@ -6,6 +6,7 @@
 
 // pg_step.cu
 void pg_launch_invert(const PgDev &d, cudaStream_t s);
+void pg_launch_iso_flags(const PgDev &d, cudaStream_t s, int p0, int p1);   // isotropic-inertia flags
 void pg_launch_euler(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_shapes(const PgDev &d, cudaStream_t s, bool skip_analytical);
 void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step);   // velocities from obsang/obslin

@@ -140,8 +140,9 @@ PG_DEV double clampd(double a, double b, double c) { return a < b ? b : a > c ? 
 // unit normal from the point to the centre; returns r - distance.
 // 'edge_typo' reproduces the reference's -e/c in the s >= 0, t < 0 region
 // beyond edge bc (condet.ispc:373); otherwise the ab-edge parameter -d/a.
-PG_DEV double triangle_sphere(const double *A, const double *Bv, const double *Cv, const double *p, double r,
-                              double *point, double *normal, bool edge_typo)
+// closest point of triangle (A, Bv, Cv) to p (condet.ispc:312-388 regions)
+PG_DEV void triangle_closest(const double *A, const double *Bv, const double *Cv, const double *p,
+                             double *point, bool edge_typo)
 {
   double edge0[3] = {Bv[0]-A[0], Bv[1]-A[1], Bv[2]-A[2]};
   double edge1[3] = {Cv[0]-A[0], Cv[1]-A[1], Cv[2]-A[2]};
@@ -210,6 +211,12 @@ PG_DEV double triangle_sphere(const double *A, const double *Bv, const double *C
   point[0] = A[0] + s*edge0[0] + t*edge1[0];
   point[1] = A[1] + s*edge0[1] + t*edge1[1];
   point[2] = A[2] + s*edge0[2] + t*edge1[2];
+}
+
+PG_DEV double triangle_sphere(const double *A, const double *Bv, const double *Cv, const double *p, double r,
+                              double *point, double *normal, bool edge_typo)
+{
+  triangle_closest(A, Bv, Cv, p, point, edge_typo);
   double q[3] = {p[0]-point[0], p[1]-point[1], p[2]-point[2]};
   double len = sqrt(dot3(q, q));
   double ilen = 1.0/len;

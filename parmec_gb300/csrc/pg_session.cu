@@ -167,6 +167,7 @@ int allocate(pg_session *s, const pg_scene *sc)
   TRY(dalloc(s, &d.flags, P));
   TRY(dalloc(s, &d.parmat, P));
   TRY(dalloc(s, &d.pell, P));
+  TRY(dalloc(s, &d.piso, P));
   for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.center[k], E));
   for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.radii[k], E));
   TRY(dalloc(s, &d.ellcol, E));
@@ -475,6 +476,7 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     TRY(h2d(s, d.sactive, act.data(), d.nscene));
   }
   if (d.form == PG_FORM_MIXED) pg_launch_mx_from64(d, s->stream, (int)p0, (int)p1, (int)e0, (int)e1);
+  else pg_launch_iso_flags(d, s->stream, (int)p0, (int)p1);
   int one = 1;
   TRY(h2d(s, d.rebuild, &one, 1));
   return PG_OK;

@@ -20,6 +20,7 @@ struct PgDev
   double *angular[6], *linear[3], *rotation[9], *position[6];
   double *inertia[9], *inverse[9], *mass, *invm, *force[3], *torque[3];
   int *flags, *parmat;
+  unsigned char *piso;      // 1: inertia j*I and inverse (1/j)*I with +0 off the diagonal (FP64 form)
   int *pell;                // particle -> its sphere, or -1
 
   // ---- spheres (parmec.cpp:86-93)

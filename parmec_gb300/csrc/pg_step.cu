@@ -60,6 +60,58 @@ __global__ void k_excite(PgDev d, double step)
   if (sc < d.nscene) pgk::excite_item(d, sc, step);
 }
 
+// ---------------------------------------------------------------- isotropic bodies
+// A sphere's inertia is j*I and its inverse (1/j)*I, off-diagonals +0.  The
+// 3x3 products with them then reduce to j*x per row, except for the sign of
+// an exact zero: IEEE gives x + (+-0) = x for x != 0, and a sum of zeros is
+// -0 only when every term is -0.  iso_nvmul replays that with integer bit
+// tests, so its results equal nvmul's bit for bit (non-finite inputs take
+// the full product).
+__device__ __forceinline__ void set_piso(const PgDev &d, int i)
+{
+  if (!d.piso) return;
+  const long long j = __double_as_longlong(d.inertia[0][i]), ij = __double_as_longlong(d.inverse[0][i]);
+  bool iso = __double_as_longlong(d.inertia[4][i]) == j && __double_as_longlong(d.inertia[8][i]) == j &&
+             __double_as_longlong(d.inverse[4][i]) == ij && __double_as_longlong(d.inverse[8][i]) == ij;
+  const int off[6] = {1, 2, 3, 5, 6, 7};
+  for (int k = 0; k < 6; k ++)
+    iso = iso && __double_as_longlong(d.inertia[off[k]][i]) == 0 && __double_as_longlong(d.inverse[off[k]][i]) == 0;
+  d.piso[i] = iso ? 1 : 0;
+}
+
+__device__ __forceinline__ bool finite_bits(double x) { return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff; }
+
+// p + 0*a + 0*b as the full product sums them, for finite a and b
+__device__ __forceinline__ double zero_terms(double p, double a, double b)
+{
+  const long long bp = __double_as_longlong(p);
+  if ((bp << 1) != 0) return p;
+  const bool neg = bp < 0 && __double_as_longlong(a) < 0 && __double_as_longlong(b) < 0;
+  return __longlong_as_double(neg ? (long long)0x8000000000000000ull : 0ll);
+}
+
+// C = (j*I) B, bit for bit as nvmul with the full matrix
+__device__ __forceinline__ void iso_nvmul(double j, const double *B, double *C)
+{
+  if (finite_bits(B[0]) && finite_bits(B[1]) && finite_bits(B[2]))
+  {
+    C[0] = zero_terms(j*B[0], B[1], B[2]);
+    C[1] = zero_terms(j*B[1], B[0], B[2]);
+    C[2] = zero_terms(j*B[2], B[0], B[1]);
+  }
+  else
+  {
+    const double M[9] = {j, 0.0, 0.0, 0.0, j, 0.0, 0.0, 0.0, j};
+    nvmul(M, B, C);
+  }
+}
+
+__global__ void k_iso_flags(PgDev d, int p0, int p1)
+{
+  int i = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p1) set_piso(d, i);
+}
+
 // ---------------------------------------------------------------- invert (parmec.ispc:62-99)
 __global__ void k_invert(PgDev d)
 {
@@ -71,6 +123,7 @@ __global__ void k_invert(PgDev d)
   invert3(a, x);
   for (int j = 0; j < 9; j ++) d.inverse[j][i] = x[j];
   d.invm[i] = 1.0 / d.mass[i];
+  set_piso(d, i);
 }
 
 // ---------------------------------------------------------------- euler (parmec.ispc:224-272)
@@ -145,8 +198,11 @@ __global__ void k_faces(PgDev d)
       {
         double val = d.nodes[c][n];
         d.tri[3*v+c][t] = val;
-        double r = val - d.tref[3*v+c][t];
-        dd += r*r;
+        if (d.ellnum)                       // the displacement matters only to sphere candidate lists
+        {
+          double r = val - d.tref[3*v+c][t];
+          dd += r*r;
+        }
       }
       need |= dd > d.half_skin_sq;
     }
@@ -228,38 +284,55 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       const size_t idx = (size_t)k * E + i;
       const int code = d.ncode[idx];
       const bool existing = d.nflag[idx] != 0;
-      double point[3], normal[3], depth;
+      // Geometry in two stages: the squared distance first; a candidate
+      // clearly apart (d2 > (r_i + r_j)^2 (1 + 1e-12), which the rounding of
+      // sqrt and of the products cannot bring back to depth >= 0) skips the
+      // square root and the division.  Every contact that can be active takes
+      // the same operations as the reference's.
+      double point[3], normal[3], depth, q[3], len;
       int pj, colj;
+      bool apart;
+      const double *cjp = nullptr;
+      double cj[3];
       if (code >= 0)
       {
         const int j = code;
         pj = d.part[j];
         colj = d.ellcol[j];
-        double q[3], cj[3];
         cj[0] = d.center[0][j]; cj[1] = d.center[1][j]; cj[2] = d.center[2][j];
+        cjp = cj;
         q[0] = c[0]-cj[0];
         q[1] = c[1]-cj[1];
         q[2] = c[2]-cj[2];
-        double len = sqrt(dot3(q, q));
-        double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
-        point[0] = 0.5*(c[0]+cj[0]);
-        point[1] = 0.5*(c[1]+cj[1]);
-        point[2] = 0.5*(c[2]+cj[2]);
-        normal[0] = ilen*q[0];
-        normal[1] = ilen*q[1];
-        normal[2] = ilen*q[2];
-        depth = ri+d.radii[0][j] - len;
+        const double d2 = dot3(q, q);
+        const double sr = ri+d.radii[0][j];
+        apart = d2 > (sr*sr) * (1.0 + 1e-12);
+        if (!apart)
+        {
+          len = sqrt(d2);
+          depth = sr - len;
+        }
       }
       else
       {
         const int t = -code-1;
         double A[3], B[3], C[3];
         for (int kk = 0; kk < 3; kk ++) { A[kk] = d.tri[kk][t]; B[kk] = d.tri[3+kk][t]; C[kk] = d.tri[6+kk][t]; }
-        depth = triangle_sphere(A, B, C, c, ri, point, normal, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+        triangle_closest(A, B, C, c, point, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+        q[0] = c[0]-point[0];
+        q[1] = c[1]-point[1];
+        q[2] = c[2]-point[2];
+        const double d2 = dot3(q, q);
+        apart = d2 > (ri*ri) * (1.0 + 1e-12);
+        if (!apart)
+        {
+          len = sqrt(d2);
+          depth = ri - len;
+        }
         pj = d.triobs[t];
         colj = d.tricol[t];
       }
-      const bool active = existing ? !(depth < 0.0) : (depth > 0.0);
+      const bool active = !apart && (existing ? !(depth < 0.0) : (depth > 0.0));
       if (!active)
       {
         if (existing)
@@ -268,6 +341,23 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
           d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
         }
         continue;
+      }
+      if (cjp)
+      {
+        double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
+        point[0] = 0.5*(c[0]+cj[0]);
+        point[1] = 0.5*(c[1]+cj[1]);
+        point[2] = 0.5*(c[2]+cj[2]);
+        normal[0] = ilen*q[0];
+        normal[1] = ilen*q[1];
+        normal[2] = ilen*q[2];
+      }
+      else
+      {
+        double ilen = 1.0/len;
+        normal[0] = ilen*q[0];
+        normal[1] = ilen*q[1];
+        normal[2] = ilen*q[2];
       }
 
       // contact point velocities (forces.ispc:226-279)
@@ -951,7 +1041,11 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       const double half = 0.5*step;
       const double hstep = 0.5*(step+step1);
       for (int k = 0; k < 3; k ++) { O[k] = d.angular[k][i]; v[k] = d.linear[k][i]; }
-      for (int k = 0; k < 9; k ++) { L1[k] = d.rotation[k][i]; J[k] = d.inertia[k][i]; I[k] = d.inverse[k][i]; }
+      const bool iso = d.piso && d.piso[i];
+      const double js = iso ? d.inertia[0][i] : 0.0, is = iso ? d.inverse[0][i] : 0.0;
+      for (int k = 0; k < 9; k ++) L1[k] = d.rotation[k][i];
+      if (!iso)
+        for (int k = 0; k < 9; k ++) { J[k] = d.inertia[k][i]; I[k] = d.inverse[k][i]; }
       im = d.invm[i];
       if (damping[0] != 0.0 || damping[1] != 0.0 || damping[2] != 0.0)
       {
@@ -965,7 +1059,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
         o[1] = damping[4]*d.angular[4][i];
         o[2] = damping[5]*d.angular[5][i];
         tvmul(L1, o, t);
-        nvmul(J, t, Tb);
+        if (iso) iso_nvmul(js, t, Tb); else nvmul(J, t, Tb);
         nvmul(L1, Tb, t);
         T[0] -= t[0]; T[1] -= t[1]; T[2] -= t[2];
       }
@@ -973,18 +1067,24 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       t[0] = T[0]; t[1] = T[1]; t[2] = T[2];
       tvmul(L1, t, Tb);
       expmap(-half*O[0], -half*O[1], -half*O[2], DL, typo);
-      nvmul(J, O, A);
+      if (iso) iso_nvmul(js, O, A); else nvmul(J, O, A);
       nvmul(DL, A, B);
       B[0] = B[0] + half*Tb[0];
       B[1] = B[1] + half*Tb[1];
       B[2] = B[2] + half*Tb[2];
-      nvmul(I, B, A);
-      nvmul(J, A, B);
+      if (iso) { iso_nvmul(is, B, A); iso_nvmul(js, A, B); }
+      else { nvmul(I, B, A); nvmul(J, A, B); }
       Tb[0] -= A[1]*B[2] - A[2]*B[1];
       Tb[1] -= A[2]*B[0] - A[0]*B[2];
       Tb[2] -= A[0]*B[1] - A[1]*B[0];
       Tb[0] *= step; Tb[1] *= step; Tb[2] *= step;
-      nvaddmul(O, I, Tb, O);
+      if (iso)
+      {
+        double IT[3];
+        iso_nvmul(is, Tb, IT);
+        O[0] = O[0] + IT[0]; O[1] = O[1] + IT[1]; O[2] = O[2] + IT[2];
+      }
+      else nvaddmul(O, I, Tb, O);
       im *= step;
       v[0] = v[0] + im*f[0];
       v[1] = v[1] + im*f[1];
@@ -1063,6 +1163,11 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
 void pg_launch_invert(const PgDev &d, cudaStream_t s)
 {
   if (d.parnum) k_invert<<<nblk(d.parnum), TPB, 0, s>>>(d);
+}
+
+void pg_launch_iso_flags(const PgDev &d, cudaStream_t s, int p0, int p1)
+{
+  if (p1 > p0 && d.piso) k_iso_flags<<<nblk(p1 - p0), TPB, 0, s>>>(d, p0, p1);
 }
 
 void pg_launch_euler(const PgDev &d, cudaStream_t s, double step)
