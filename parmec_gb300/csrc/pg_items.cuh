@@ -270,6 +270,43 @@ __device__ __forceinline__ void sort_scatter_tile(const unsigned *ksrc, const in
   __syncthreads();
 }
 
+// surface pair of two colours: binary search of the sorted pairs
+// (forces.ispc:98-122; stops where the reference could loop forever)
+__device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
+{
+  int p0 = i, p1 = j, start = 1, end = d.pairnum;
+  if (i > j) { p0 = j; p1 = i; }
+  while (start < end)
+  {
+    int mid = ((end-start)>>1) + start;
+    int a = d.pairs[2*mid], b = d.pairs[2*mid+1];
+    if (p0 > a) { if (start == mid) break; start = mid; }
+    else if (p0 == a)
+    {
+      if (p1 > b) { if (start == mid) break; start = mid; }
+      else if (p1 == b) return mid;
+      else end = mid;
+    }
+    else end = mid;
+  }
+  return 0;
+}
+
+// normal damping coefficient of a master sphere i with partner code 'code'
+// (forces.ispc:125-135): damper * 2 * sqrt(kn * m), m the reduced mass, or
+// the sphere's mass against an obstacle triangle
+__device__ __forceinline__ double pair_en(const PgDev &d, int i, int code)
+{
+  const int pi = d.part[i];
+  int pj, colj;
+  if (code >= 0) { pj = d.part[code]; colj = d.ellcol[code]; }
+  else { pj = d.triobs[-code-1]; colj = d.tricol[-code-1]; }
+  const int ij = pairing(d, d.ellcol[i], colj);
+  const double ma = pj >= 0 ? 1.0 / (d.invm[pi] + d.invm[pj]) : d.mass[pi];
+  const double kn = d.iparam[0][ij];
+  return d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+}
+
 // ================================================================ candidate-list rebuild
 // 0. clear the cell ranges of the previous sort
 __device__ __forceinline__ void rb_clear_item(const PgDev &d, int s)
@@ -396,6 +433,7 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
     while (o < nold && order_key(ocode[o]) < key) o ++;
     size_t idx = (size_t)k * E + i;
     d.ncode[idx] = codes[k];
+    if (d.nen) d.nen[idx] = pair_en(d, i, codes[k]);
     const bool kept = o < nold && ocode[o] == codes[k];
     d.nflag[idx] = kept ? oflag[o] : 0;
     for (int c = 0; c < 3; c ++)

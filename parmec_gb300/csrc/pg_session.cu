@@ -556,6 +556,7 @@ int slot_buffers(pg_session *s)
       TRY(dalloc(s, &d.nnrm[k], slots));
     }
     TRY(dalloc(s, &d.ndep, slots));
+    TRY(dalloc(s, &d.nen, slots));
   }
   else
   {
@@ -581,8 +582,8 @@ int slot_buffers(pg_session *s)
 void release_slot_buffers(pg_session *s)
 {
   PgDev &d = s->d;
-  release(s, d.ncode); release(s, d.nflag); release(s, d.ndep);
-  d.ncode = nullptr; d.nflag = nullptr; d.ndep = nullptr; d.rref = nullptr;
+  release(s, d.ncode); release(s, d.nflag); release(s, d.ndep); release(s, d.nen);
+  d.ncode = nullptr; d.nflag = nullptr; d.ndep = nullptr; d.nen = nullptr; d.rref = nullptr;
   for (int k = 0; k < 2; k ++) { release(s, d.skey[k]); release(s, d.sval[k]); d.skey[k] = nullptr; d.sval[k] = nullptr; }
   release(s, d.shist); release(s, d.sbs); d.shist = nullptr; d.sbs = nullptr;
   for (int k = 0; k < 3; k ++)

@@ -78,6 +78,7 @@ struct PgDev
   double *nstate[3];        // [kn][ellnum]: tangential spring state
   double *nfrc[3];          // [kn][ellnum]: contact force on the master
   double *npnt[3];          // [kn][ellnum]: contact point
+  double *nen;              // [kn][ellnum]: normal damping of the pair, damper*2*sqrt(kn*m) (FP64 session)
   double *nnrm[3], *ndep;   // optional: normal and depth (parity exports only)
   int record_geometry;
   double *fm[3], *tm[3];    // [parnum] master-side partial force and torque sums

@@ -228,26 +228,7 @@ __global__ void k_tail(PgDev d, double step, int use_row)
   pgk::tail_item(d, step, use_row);
 }
 
-// ---------------------------------------------------------------- pairing (forces.ispc:98-122)
-__device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
-{
-  int p0 = i, p1 = j, start = 1, end = d.pairnum;
-  if (i > j) { p0 = j; p1 = i; }
-  while (start < end)
-  {
-    int mid = ((end-start)>>1) + start;
-    int a = d.pairs[2*mid], b = d.pairs[2*mid+1];
-    if (p0 > a) { if (start == mid) break; start = mid; }
-    else if (p0 == a)
-    {
-      if (p1 > b) { if (start == mid) break; start = mid; }
-      else if (p1 == b) return mid;
-      else end = mid;
-    }
-    else end = mid;
-  }
-  return 0;
-}
+using pgk::pairing;
 
 // ---------------------------------------------------------------- contacts
 // One thread per sphere (master side).  For every candidate in its list the
@@ -406,9 +387,16 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       double state[3];
       if (existing) { state[0] = d.nstate[0][idx]; state[1] = d.nstate[1][idx]; state[2] = d.nstate[2][idx]; }
       else { state[0] = 0.0; state[1] = 0.0; state[2] = 0.0; }
-      double ma = pj >= 0 ? 1.0 / (invmi + d.invm[pj]) : massi;
+      // the pair's damping is fixed between uploads: taken from the list
+      // entry (computed at the rebuild with the same expression) or here
       double kn = d.iparam[0][ij];
-      double en = d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+      double en;
+      if (d.nen) en = d.nen[idx];
+      else
+      {
+        double ma = pj >= 0 ? 1.0 / (invmi + d.invm[pj]) : massi;
+        en = d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+      }
       double vn = dot3(vij, normal);
       double fn = kn*depth + en*vn;
       double f[3];
