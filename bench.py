@@ -489,8 +489,9 @@ def main():
                    "contacts_per_particle": round(c_pair, 3)},
         "e2e": {"value": m.parnum * args.steps * world / e2e_s, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": up // args.steps, "d2h_bytes_per_step": down // args.steps,
-                "path": "Model.dem() through the pg_session C ABI: full host->device upload, K steps, "
-                        "device->host download (pageable host arrays)"},
+                "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
+                        "full host->device upload, K steps, device->host download; host SoA arrays "
+                        "page-locked by the engine (cudaHostRegister)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None,

@@ -24,6 +24,8 @@
 #ifndef PARMEC_GB300_H
 #define PARMEC_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -260,6 +262,12 @@ int pg_session_autotune(pg_session *s, int on);
 
 /* out4 = {threads per block, blocks, 1 if tuned, 1 if running as a graph}. */
 int pg_session_fused_config(pg_session *s, int *out4);
+
+/* Page-lock (pin) a host buffer that sessions copy to and from, so that the
+ * copies of upload/download run at full link speed (NVLink-C2C on GB300), and
+ * release it.  Registering an already registered buffer is PG_OK. */
+int pg_host_register(void *ptr, size_t bytes);
+int pg_host_unregister(void *ptr);
 
 /* Self-test of the bounded grid barrier used by the cooperative kernels: a
  * small cooperative grid waits at a barrier that cannot complete, gives up

@@ -163,6 +163,8 @@ def load_library():
         "pg_session_autotune": (ctypes.c_int, [P, ctypes.c_int]),
         "pg_session_fused_config": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
         "pg_session_barrier_selftest": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
+        "pg_host_register": (ctypes.c_int, [P, ctypes.c_size_t]),
+        "pg_host_unregister": (ctypes.c_int, [P]),
         "pg_session_profile_read": (ctypes.c_int, [P, D, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_diagnostics": (ctypes.c_int, [P, I]),
         "pg_cell_order": (ctypes.c_int, [P, P, P, ctypes.c_int, D, ctypes.c_double, I, P, P, P]),

@@ -1398,6 +1398,23 @@ int pg_session_diagnostics(pg_session *s, int *out16)
   return PG_OK;
 }
 
+int pg_host_register(void *ptr, size_t bytes)
+{
+  if (!ptr || bytes == 0) return PG_ERR_ARGUMENT;
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e == cudaErrorHostMemoryAlreadyRegistered) { cudaGetLastError(); return PG_OK; }
+  if (e != cudaSuccess) { cudaGetLastError(); return PG_ERR_CUDA; }
+  return PG_OK;
+}
+
+int pg_host_unregister(void *ptr)
+{
+  if (!ptr) return PG_ERR_ARGUMENT;
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) { cudaGetLastError(); return PG_ERR_CUDA; }
+  return PG_OK;
+}
+
 int pg_session_barrier_selftest(pg_session *s, double *wait_ms)
 {
   if (!s) return PG_ERR_ARGUMENT;

@@ -19,6 +19,7 @@ class GpuEngine:
         """fused: the mixed form's persistent step kernel (pg_session_use_fused);
         autotune: pick its launch shape by timing the first steps."""
         self.lib = abi.load_library()
+        self._pinned = {}
         self.fused = fused
         self.autotune = autotune
         self.graph = graph
@@ -31,9 +32,31 @@ class GpuEngine:
         self.scene = None
         self.counts = None
 
+    # host arrays of at least this many bytes are page-locked while attached
+    PIN_BYTES = 1 << 20
+
+    def _pin(self, m):
+        """Page-lock the model's large SoA arrays, so that upload/download copy
+        at link speed instead of staging through pageable memory."""
+        import numpy as np
+        want = {}
+        for soa in (m.P, m.E, m.Tr, m.N, m.F, m.S):
+            for name in soa.spec:
+                a = getattr(soa, name)
+                if isinstance(a, np.ndarray) and a.nbytes >= self.PIN_BYTES:
+                    want[a.ctypes.data] = (a, a.nbytes)
+        for ptr in list(self._pinned):
+            if ptr not in want:
+                self.lib.pg_host_unregister(ctypes.c_void_p(ptr))
+                del self._pinned[ptr]
+        for ptr, (a, nb) in want.items():
+            if ptr not in self._pinned and self.lib.pg_host_register(ctypes.c_void_p(ptr), nb) == 0:
+                self._pinned[ptr] = a                 # keep the array alive while pinned
+
     def attach(self, m):
         self.close()
         self.model = m
+        self._pin(m)
         self.scene = m.scene()
         self.counts = _counts(m)
         h = ctypes.c_void_p()
@@ -58,6 +81,7 @@ class GpuEngine:
         return self.model is None or _counts(self.model) != self.counts
 
     def upload(self):
+        self._pin(self.model)
         self.scene = self.model.scene()
         abi.check(self.lib.pg_session_upload(self.sess, ctypes.byref(self.scene)), "pg_session_upload")
 
@@ -164,6 +188,9 @@ class GpuEngine:
         if self.sess is not None:
             self.lib.pg_session_destroy(self.sess)
             self.sess = None
+        for ptr in list(getattr(self, "_pinned", {})):
+            self.lib.pg_host_unregister(ctypes.c_void_p(ptr))
+        self._pinned = {}
 
     def __del__(self):
         try:
