@@ -223,7 +223,8 @@ def sample_history(m, t):
                     value += S.sprfrc[1, l]
                 elif ent == "FF":
                     value += S.sprfrc[2, l]
-        h["out"].append(float(value))
+        # a list source reports the mean over its entries (output.cpp:5514-5516)
+        h["out"].append(float(value) / float(len(h["list"])))
 
 
 def default_engine(m):

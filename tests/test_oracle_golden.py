@@ -218,3 +218,21 @@ def test_contact_set_exact(oracle_lib):
     far = {(i, j) for i in range(len(r)) for j in range(i + 1, len(r)) if d[i, j] > r[i] + r[j] + 1e-6}
     assert close <= pairs
     assert not (pairs & far)
+
+
+def test_history_of_a_list_is_the_mean(oracle_lib):
+    """HISTORY over a particle list reports the mean over the list
+    (output.cpp:5514-5516); a single index reports the value itself."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.model import Model
+    m = Model()
+    mat = m.material(1000.0, 1e9, 0.25)
+    a = m.sphere((0.0, 0.0, 1.0), 0.1, mat, 1)
+    b = m.sphere((5.0, 0.0, 3.0), 0.1, mat, 1)
+    m.set_gravity(0.0, 0.0, 0.0)
+    both = m.history("PZ", [a, b])
+    one = m.history("PZ", b)
+    m.dem(0.01, 0.001, interval=0.005, engine=OracleEngine())
+    assert len(both) == len(one) > 0
+    assert both[-1] == (1.0 + 3.0) / 2.0
+    assert one[-1] == 3.0
