@@ -468,7 +468,7 @@ def main():
     bytes_dom = per_launch.get(dom)
     # DRAM bytes per launch: ncu capture of the 262,144-sphere case
     # (profiles/k_integrate_k_contacts_drum_fp64.md) scaled by the units processed
-    traffic_per_unit = {"integrate": 611.0, "contacts": 188.0}
+    traffic_per_unit = {"integrate": 456.0, "contacts": 200.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     if bytes_dom is not None:
         avg_s = ms_dom * 1e-3 / args.steps
