@@ -120,6 +120,7 @@ class OracleEngine:
         if self.ctx is not None:
             self.lib.or_destroy(self.ctx)
             self.ctx = None
+        self.model = None
 
     def __del__(self):
         try:

@@ -1,0 +1,272 @@
+"""CRITICAL per particle (input.cpp:3034-3154, parmec.ispc:275-383, 547-900).
+
+The per-particle critical step estimate of the reference, over the current
+contacts (exported from the device session) and springs:
+
+* critical_perparticle_contacts (parmec.ispc:547-650): per particle, the
+  contacts it takes part in add the absolute contact-normal components to
+  kact, their normal stiffness and damping to kmax/emax, and the rotational
+  stiffness terms of the contact arm to krot;
+* critical_perparticle_springs (parmec.ispc:653-857): springs add their
+  direction (or an in-plane pair for PLANAR springs), largest curve slope,
+  damping and arm terms;
+* time_step_task (parmec.ispc:275-383): translational frequency
+  sqrt(n k / m), rotational frequency from the generalised eigenproblem
+  K x = lambda J x through a Cholesky factor of J, and the damped step
+  (2/w)(sqrt(1+ksi^2) - ksi) of each, the smaller taken.
+
+A setup-time query, not a step: evaluated on the host over data downloaded
+from the session.  Positions taken:
+* the slave side of a contact uses the contact's own normal stiffness and
+  damping; the reference reads them from slave records it never sets
+  (the slave copy, forces.ispc:383-405, copies point and force only);
+* springs are classified by their own dashpot and flags; the reference
+  indexes dashidx and sprflg with the particle index there
+  (parmec.ispc:726, 759);
+* extremum_eigenvalue returns the largest eigenvalue of a diagonal matrix
+  even when the smallest is asked for (macros.h:1545-1553), as in the
+  reference (spheres are unaffected: their J is a multiple of I).
+"""
+import math
+
+import numpy as np
+
+REAL_MAX = 1.7976931348623157E+308
+ALG_PI = 3.14159265358979323846
+
+
+def _extremum_eigenvalue(A, minimum):
+    """extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3."""
+    p1 = A[3] * A[3] + A[6] * A[6] + A[7] * A[7]
+    if p1 == 0.0:
+        return max(max(A[0], A[4]), A[8])
+    q = (A[0] + A[4] + A[8]) / 3.0
+    p2 = (A[0] - q) * (A[0] - q) + (A[4] - q) * (A[4] - q) + (A[8] - q) * (A[8] - q) + 2 * p1
+    p = math.sqrt(p2 / 6.0)
+    invp = 1.0 / p
+    B = [invp * (A[0] - q), invp * A[1], invp * A[2], invp * A[3], invp * (A[4] - q), invp * A[5],
+         invp * A[6], invp * A[7], invp * (A[8] - q)]
+    det = (B[0] * (B[4] * B[8] - B[5] * B[7]) + B[3] * (B[2] * B[7] - B[1] * B[8])
+           + (B[1] * B[5] - B[2] * B[4]) * B[6])
+    r = 0.5 * det
+    if r <= -1.0:
+        phi = ALG_PI / 3.0
+    elif r >= 1.0:
+        phi = 0.0
+    else:
+        phi = math.acos(r) / 3.0
+    if minimum:
+        return q + 2.0 * p * math.cos(phi + (2 * ALG_PI / 3))
+    return q + 2.0 * p * math.cos(phi)
+
+
+def pairing(m, i, j):
+    """pairing (forces.ispc:98-122) over the model's sorted colour pairs."""
+    p0, p1 = (i, j) if i <= j else (j, i)
+    start, end = 1, len(m.pairs)
+    while start < end:
+        mid = ((end - start) >> 1) + start
+        a, b = m.pairs[mid]
+        if p0 > a or (p0 == a and p1 > b):
+            if start == mid:
+                break
+            start = mid
+        elif p0 == a and p1 == b:
+            return mid
+        else:
+            end = mid
+    return 0
+
+
+def _invert(F):
+    det = F[0] * (F[4] * F[8] - F[5] * F[7]) + F[3] * (F[2] * F[7] - F[1] * F[8]) + (F[1] * F[5] - F[2] * F[4]) * F[6]
+    if det == 0.0:
+        return [0.0] * 9
+    det = 1.0 / det
+    return [(F[4] * F[8] - F[5] * F[7]) * det, (F[2] * F[7] - F[1] * F[8]) * det, (F[1] * F[5] - F[2] * F[4]) * det,
+            (F[5] * F[6] - F[3] * F[8]) * det, (F[0] * F[8] - F[2] * F[6]) * det, (F[2] * F[3] - F[0] * F[5]) * det,
+            (F[3] * F[7] - F[4] * F[6]) * det, (F[1] * F[6] - F[0] * F[7]) * det, (F[0] * F[4] - F[1] * F[3]) * det]
+
+
+def _nnmul(A, B):
+    C = [0.0] * 9
+    for c in range(3):
+        for r in range(3):
+            C[3 * c + r] = A[r] * B[3 * c] + A[3 + r] * B[3 * c + 1] + A[6 + r] * B[3 * c + 2]
+    return C
+
+
+def _ntmul(A, B):
+    """NTMUL: A * B^T (column-major)."""
+    Bt = [B[0], B[3], B[6], B[1], B[4], B[7], B[2], B[5], B[8]]
+    return _nnmul(A, Bt)
+
+
+def _add_arm(krot, p, L, a, transpose):
+    """krot terms of an arm a (body frame: L a for contacts, L^T a for springs)."""
+    if transpose:
+        A = np.stack([
+            L[0] * a[0] + L[1] * a[1] + L[2] * a[2],
+            L[3] * a[0] + L[4] * a[1] + L[5] * a[2],
+            L[6] * a[0] + L[7] * a[1] + L[8] * a[2]])
+    else:
+        A = np.stack([L[0] * a[0] + L[3] * a[1] + L[6] * a[2],
+                      L[1] * a[0] + L[4] * a[1] + L[7] * a[2],
+                      L[2] * a[0] + L[5] * a[1] + L[8] * a[2]])
+    dot = A[0] * A[0] + A[1] * A[1] + A[2] * A[2]
+    for k, v in enumerate((dot - A[0] * A[0], dot - A[1] * A[1], dot - A[2] * A[2],
+                           -A[0] * A[1], -A[0] * A[2], -A[1] * A[2])):
+        np.add.at(krot[k], p, v)
+
+
+def _contact_terms(m, contacts, kact, kmax, emax, krot):
+    n = len(contacts["mpart"])
+    if n == 0:
+        return
+    P, E = m.P, m.E
+    pell = np.full(m.parnum, -1, dtype=np.int64)
+    pell[E.part[:m.ellnum]] = np.arange(m.ellnum)
+    mp = contacts["mpart"].astype(np.int64)
+    code = contacts["code"].astype(np.int64)
+    pnt = contacts["point"].T
+    frc = contacts["force"].T
+    ci = E.center[0:3, pell[mp]]
+    sph = code >= 0
+    pj = np.where(sph, E.part[np.maximum(code, 0)], m.Tr.triobs[np.maximum(-code - 1, 0)]).astype(np.int64)
+    # normal: from the partner centre (sphere) or the contact point (triangle) to the master centre
+    other = np.where(sph, E.center[0:3, np.maximum(code, 0)], pnt)
+    q = ci - other
+    ln = np.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2])
+    nrm = q / np.where(ln > 0.0, ln, 1.0)
+    # normal stiffness and damping of each contact (forces.ispc:125-147)
+    coli = E.ellcol[pell[mp]]
+    colj = np.where(sph, E.ellcol[np.maximum(code, 0)], m.Tr.tricol[np.maximum(-code - 1, 0)])
+    kc = np.empty(n)
+    ec = np.empty(n)
+    for c in range(n):
+        ij = pairing(m, int(coli[c]), int(colj[c]))
+        kn = m.iparam[ij][0]
+        ma = 1.0 / (P.invm[mp[c]] + P.invm[pj[c]]) if pj[c] >= 0 else P.mass[mp[c]]
+        kc[c] = kn
+        ec[c] = m.iparam[ij][1] * 2.0 * math.sqrt(kn * ma)
+    L = P.rotation[:, mp]
+    for k in range(3):
+        np.add.at(kact[k], mp, np.abs(nrm[k]))
+    np.maximum.at(kmax, mp, kc)
+    np.maximum.at(emax, mp, ec)
+    _add_arm(krot, mp, L, pnt - P.position[0:3, mp], False)
+    # the partner particle (slave side): the force direction of -f
+    s = pj >= 0
+    if np.any(s):
+        ps = pj[s]
+        f = -frc[:, s]
+        fl = np.sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2])
+        f = np.where(fl != 0.0, f / np.where(fl != 0.0, fl, 1.0), 0.0)
+        for k in range(3):
+            np.add.at(kact[k], ps, np.abs(f[k]))
+        np.maximum.at(kmax, ps, kc[s])
+        np.maximum.at(emax, ps, ec[s])
+        _add_arm(krot, ps, P.rotation[:, ps], pnt[:, s] - P.position[0:3, ps], False)
+
+
+def _spring_terms(m, kact, kmax, emax, krot):
+    from .springs import SPRDIR_PLANAR, _eqm
+    S, P = m.S, m.P
+    for j in range(m.sprnum):
+        i, k = int(S.sprpart[0, j]), int(S.sprpart[1, j])
+        sp = m.spring_tab[j]
+        kspr = 0.0
+        for a in range(len(sp) - 1):
+            kspr = max(abs((sp[a + 1][1] - sp[a][1]) / (sp[a + 1][0] - sp[a][0])), kspr)
+        dp = m.dashpot_tab[j]
+        espr = 0.0
+        if len(dp) == 1:                      # critical damping ratio
+            mass = _eqm(m, i, S.sprpnt[3:6, j], k, S.sprpnt[9:12, j], S.sprdir[0:3, j])
+            espr = dp[0][0] * 2.0 * math.sqrt(kspr * mass)
+        else:
+            for a in range(len(dp) - 1):
+                espr = max(abs((dp[a + 1][1] - dp[a][1]) / (dp[a + 1][0] - dp[a][0])), espr)
+        d = S.sprdir[0:3, j]
+        for p, pnt in ((i, S.sprpnt[0:3, j]), (k, S.sprpnt[6:9, j])):
+            if p < 0:
+                continue
+            if d[0] * d[0] + d[1] * d[1] + d[2] * d[2] > 0.0:
+                if S.sprflg[j] & SPRDIR_PLANAR:
+                    t1 = d + np.array([0.123, 0.346, 0.789])
+                    t2 = np.cross(d, t1)
+                    t2 = t2 * (1.0 / math.sqrt(float(np.dot(t2, t2))))
+                    t1 = np.cross(t2, d)
+                    for c in range(3):
+                        kact[c][p] += abs(t1[c]) + abs(t2[c])
+                else:
+                    for c in range(3):
+                        kact[c][p] += abs(d[c])
+            else:
+                for c in range(3):
+                    kact[c][p] += 1.0
+            L = P.rotation[:, p][:, None]
+            a = (pnt - P.position[0:3, p])[:, None]
+            _add_arm(krot, np.array([p]), L, a, True)
+            kmax[p] = max(kmax[p], kspr)
+            emax[p] = max(emax[p], espr)
+
+
+def _time_steps(m, kact, kmax, emax, krot):
+    """time_step_task (parmec.ispc:275-383) for every particle."""
+    P = m.P
+    n = m.parnum
+    h = np.full(n, REAL_MAX)
+    om = np.zeros(n)
+    ra = np.zeros(n)
+    for i in range(n):
+        nxyz = max(max(kact[0][i], kact[1][i]), kact[2][i])
+        if not (nxyz > 0.0):
+            continue
+        k = kmax[i]
+        mxyz = P.mass[i]
+        omegaxyz = math.sqrt(nxyz * k / mxyz)
+        K = [k * krot[0][i], k * krot[3][i], k * krot[4][i], 0.0, k * krot[1][i], k * krot[5][i], 0.0, 0.0,
+             k * krot[2][i]]
+        K[3], K[6], K[7] = K[1], K[2], K[5]
+        J = [float(x) for x in P.inertia[:, i]]
+        mrot = _extremum_eigenvalue(J, 1)
+        L = [0.0] * 9
+        L[0] = math.sqrt(J[0])
+        inv = 1.0 / L[0]
+        L[1] = inv * J[1]
+        L[2] = inv * J[2]
+        L[4] = math.sqrt(J[4] - L[1] * L[1])
+        inv = 1.0 / L[4]
+        L[5] = inv * (J[5] - L[2] * L[1])
+        L[8] = math.sqrt(J[8] - (L[2] * L[2] + L[5] * L[5]))
+        invL = _invert(L)
+        A = _nnmul(invL, _ntmul(K, invL))
+        lam = _extremum_eigenvalue(A, 0)
+        # no rotational stiffness: the reference divides by zero here
+        omegarot = math.sqrt(lam) if lam > 0.0 else 0.0
+        damping = emax[i]
+        ratioxyz = damping / (2.0 * mxyz * omegaxyz)
+        hxyz = (2.0 / omegaxyz) * (math.sqrt(1.0 + ratioxyz * ratioxyz) - ratioxyz)
+        if omegarot > 0.0:
+            ratiorot = damping / (2.0 * mrot * omegarot)
+            hrot = (2.0 / omegarot) * (math.sqrt(1.0 + ratiorot * ratiorot) - ratiorot)
+        else:
+            ratiorot, hrot = 0.0, REAL_MAX
+        h[i] = min(hxyz, hrot)
+        om[i] = max(omegaxyz, omegarot)
+        ra[i] = max(ratioxyz, ratiorot)
+    return h, om, ra
+
+
+def critical_perparticle(m, contacts=None):
+    """Per-particle (step, omega, ratio) arrays; 'contacts' is the session's
+    contact export (None or empty before any DEM step: no contacts yet)."""
+    n = m.parnum
+    kact = [np.zeros(n) for _ in range(3)]
+    krot = [np.zeros(n) for _ in range(6)]
+    kmax = np.zeros(n)
+    emax = np.zeros(n)
+    if contacts is not None:
+        _contact_terms(m, contacts, kact, kmax, emax, krot)
+    _spring_terms(m, kact, kmax, emax, krot)
+    return _time_steps(m, kact, kmax, emax, krot)

@@ -252,6 +252,7 @@ def run_dem(m, duration, step, interval, engine):
         eng.upload()
     if engine is None:
         m.engine = eng
+    m.last_engine = eng
     m._dirty = False
 
     if m.curtime == 0.0:

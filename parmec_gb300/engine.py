@@ -191,6 +191,7 @@ class GpuEngine:
         for ptr in list(getattr(self, "_pinned", {})):
             self.lib.pg_host_unregister(ctypes.c_void_p(ptr))
         self._pinned = {}
+        self.model = None
 
     def __del__(self):
         try:

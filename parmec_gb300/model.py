@@ -125,6 +125,7 @@ class Model:
         # moving-obstacle index fixed
         self.compat = abi.PG_COMPAT_EXPMAP | abi.PG_COMPAT_TRIEDGE
         self.engine = None                  # compute engine holding device state
+        self.last_engine = None             # engine of the latest DEM (owned or passed in)
         self._dirty = True                  # host arrays changed since the engine last saw them
 
     def _touch(self):
@@ -525,17 +526,45 @@ class Model:
 
     # ------------------------------------------------------------- CRITICAL
     def critical(self, perspring=-1, perparticle=-1):
-        """CRITICAL (input.cpp:3034-3154) with perspring (critical_perspring,
-        parmec.ispc:485-544).  The per-particle estimate needs the adaptive
-        step machinery (not built): it raises NotImplementedError."""
+        """CRITICAL (input.cpp:3034-3154): per-spring and per-particle critical
+        step estimates.  perspring=N returns the N smallest spring steps as
+        (step, index, omega, ratio), perparticle=N the N smallest particle steps
+        likewise, both a tuple of the two lists, and no argument the smallest
+        particle step (REAL_MAX while no contact or spring restrains anything,
+        as in the reference).  Per-particle estimates use the contacts of the
+        attached device session (parmec_gb300.critical)."""
+        from .critical import critical_perparticle
         from .springs import critical_perspring
+        if perspring < -1 or perspring > self.sprnum:
+            raise ValueError("Parameter 'perspring' is out of range")
+        if perparticle < -1 or perparticle > self.parnum:
+            raise ValueError("Parameter 'perparticle' is out of range")
+        if self.springs_changed:
+            from .springs import sort_springs
+            self.sort_materials()
+            sort_springs(self)
+            self.springs_changed = False
+        out_s = out_p = None
         if perspring >= 0:
-            if perspring > self.sprnum:
-                raise ValueError("Parameter 'perspring' is out of range")
             h, o, r = critical_perspring(self)
             order = sorted(range(self.sprnum), key=lambda i: (h[i], i))
-            return [(h[i], i, o[i], r[i]) for i in order[:perspring]]
-        raise NotImplementedError("CRITICAL() per particle needs adaptive time stepping, which is not built")
+            out_s = [(h[i], i, o[i], r[i]) for i in order[:perspring]]
+        contacts = None
+        eng = self.last_engine
+        if eng is not None and eng.model is self and not eng.stale() and hasattr(eng, "contacts"):
+            contacts = eng.contacts()
+        if perparticle >= 0 or out_s is None:
+            h, o, r = critical_perparticle(self, contacts)
+            order = sorted(range(self.parnum), key=lambda i: (h[i], i))
+            if perparticle >= 0:
+                out_p = [(float(h[i]), i, float(o[i]), float(r[i])) for i in order[:perparticle]]
+        if out_s is not None and out_p is not None:
+            return (out_s, out_p)
+        if out_s is not None:
+            return out_s
+        if out_p is not None:
+            return out_p
+        return float(h[order[0]]) if order else REAL_MAX
 
     # ------------------------------------------------------------ scene ABI
     def sort_materials(self):
