@@ -207,6 +207,18 @@ int pg_session_invert_inertia(pg_session *s);
  * with a fixed step (adaptive == 0).  Asynchronous on the session stream. */
 int pg_session_run(pg_session *s, const pg_steptab *tab, double step);
 
+/* The same with adaptive stepping (DEM's 'adaptive', 0 < adaptive <= 1;
+ * parmec.cpp:2443-2450, adaptive_timestep parmec.ispc:397-420): step n runs
+ * with step0 = the previous step's step1 (the first with 'step0'); its step1
+ * is 'adaptive' times the smallest critical step of the particles, estimated
+ * on the device from this step's contacts and springs (time_step_task,
+ * parmec.ispc:275-383), or step0 when nothing is restrained.  The obstacle
+ * rows of 'tab' must be sampled at curtime + step0 of each step, so a caller
+ * with time-dependent inputs runs one step per call.  Writes each step's
+ * step1 to steps[n] (may be NULL) and waits for the steps to finish.  FP64
+ * form, one scene without device excitation; else PG_ERR_UNSUPPORTED. */
+int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, double adaptive, double *steps);
+
 /* Wait for the session stream; returns the first device error seen. */
 int pg_session_sync(pg_session *s);
 

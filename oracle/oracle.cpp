@@ -219,14 +219,36 @@ inline void expmap(double O1, double O2, double O3, double *L, bool typo)
   L[8] += 1.0;
 }
 
-/* extremum_eigenvalue macros.h:1539-1588 (used by eqm only without a direction) */
+/* cos(acos(r)/3) (largest) or cos(acos(r)/3 + 2 pi/3) (smallest), taken as
+ * roots of the triple-angle identity 4c^3 - 3c = r by Newton's method from
+ * c = 1 (or -1): the cubic is convex and increasing on [1/2, 1] (concave and
+ * increasing on [-1, -1/2]), so the iterates move monotonically to the root
+ * and the loop stops when they cease to.  Basic operations only: the same
+ * bits on every IEEE machine (the reference's acos and cos come from the ISPC
+ * standard library, which nothing pins). */
+inline double triple_angle_root(double r, bool largest)
+{
+  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+  double c = largest ? 1.0 : -1.0;
+  for (int it = 0; it < 100; it ++)
+  {
+    const double f = (4.0*c*c - 3.0)*c - r;
+    const double cn = c - f/(12.0*c*c - 3.0);
+    if (largest ? !(cn < c) : !(cn > c)) break;
+    c = cn;
+  }
+  return c;
+}
+
+/* extremum_eigenvalue macros.h:1539-1588; the diagonal branch returns the
+ * maximum whichever is asked for (reference behaviour) */
 inline double extremum_eigenvalue(const double *A, int minimum)
 {
   double p1 = A[3]*A[3] + A[6]*A[6] + A[7]*A[7];
   if (p1 == 0.0)
   {
-    double r = std::max(A[0], A[4]);
-    return std::max(r, A[8]); /* diagonal branch returns the maximum (reference behaviour) */
+    double r = A[0] > A[4] ? A[0] : A[4];
+    return r > A[8] ? r : A[8];
   }
   double q = (A[0]+A[4]+A[8])/3.0;
   double p2 = (A[0]-q)*(A[0]-q) + (A[4]-q)*(A[4]-q) + (A[8]-q)*(A[8]-q) + 2*p1;
@@ -235,12 +257,81 @@ inline double extremum_eigenvalue(const double *A, int minimum)
   double B[9] = {invp*(A[0]-q), invp*A[1], invp*A[2], invp*A[3], invp*(A[4]-q), invp*A[5],
                  invp*A[6], invp*A[7], invp*(A[8]-q)};
   double r = 0.5 * DET(B);
-  double phi;
-  if (r <= -1.0) phi = 3.14159265358979323846 / 3.0;
-  else if (r >= 1.0) phi = 0.0;
-  else phi = std::acos(r) / 3.0;
-  if (minimum) return q + 2.0 * p * std::cos(phi + (2*3.14159265358979323846/3));
-  return q + 2.0 * p * std::cos(phi);
+  return q + 2.0 * p * triple_angle_root(r, !minimum);
+}
+
+/* NTMUL macros.h:932 */
+inline void NTMUL(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[3]*B[3]+A[6]*B[6];
+  C[1] = A[1]*B[0]+A[4]*B[3]+A[7]*B[6];
+  C[2] = A[2]*B[0]+A[5]*B[3]+A[8]*B[6];
+  C[3] = A[0]*B[1]+A[3]*B[4]+A[6]*B[7];
+  C[4] = A[1]*B[1]+A[4]*B[4]+A[7]*B[7];
+  C[5] = A[2]*B[1]+A[5]*B[4]+A[8]*B[7];
+  C[6] = A[0]*B[2]+A[3]*B[5]+A[6]*B[8];
+  C[7] = A[1]*B[2]+A[4]*B[5]+A[7]*B[8];
+  C[8] = A[2]*B[2]+A[5]*B[5]+A[8]*B[8];
+}
+
+/* time_step_task (parmec.ispc:275-383) for one particle.  Position taken: a
+ * particle without rotational stiffness (omega_rot = 0, e.g. springs at the
+ * mass centre) takes its translational step; the reference divides by zero
+ * there and the NaN drops the particle from adaptive_timestep's minimum. */
+inline double critical_step(const double kact[3], double kmax, double emax, const double krot[6], double mass,
+                            const double J[9], double *omega, double *ratio)
+{
+  const double nxy = kact[0] > kact[1] ? kact[0] : kact[1];
+  const double nxyz = nxy > kact[2] ? nxy : kact[2];
+  if (!(nxyz > 0.0)) { *omega = 0.0; *ratio = 0.0; return 1.7976931348623157e308; }
+  const double k = kmax;
+  const double omegaxyz = std::sqrt(nxyz*k/mass);
+  double K[9];
+  K[0] = k*krot[0]; K[1] = k*krot[3]; K[2] = k*krot[4];
+  K[3] = K[1]; K[4] = k*krot[1]; K[5] = k*krot[5];
+  K[6] = K[2]; K[7] = K[5]; K[8] = k*krot[2];
+  const double mrot = extremum_eigenvalue(J, 1);
+  double L[9], invL[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, tmp[9], A[9], inv;
+  L[0] = std::sqrt(J[0]);
+  inv = 1.0/L[0];
+  L[1] = inv * J[1];
+  L[2] = inv * J[2];
+  L[3] = 0.0;
+  L[4] = std::sqrt(J[4] - L[1]*L[1]);
+  inv = 1.0/L[4];
+  L[5] = inv * (J[5] - L[2]*L[1]);
+  L[6] = 0.0;
+  L[7] = 0.0;
+  L[8] = std::sqrt(J[8] - (L[2]*L[2] + L[5]*L[5]));
+  INVERT(L, invL);
+  NTMUL(K, invL, tmp);
+  NNMUL(invL, tmp, A);
+  const double lambda = extremum_eigenvalue(A, 0);
+  const double omegarot = lambda > 0.0 ? std::sqrt(lambda) : 0.0;
+  const double damping = emax;
+  const double ratioxyz = damping / (2.0*mass*omegaxyz);
+  const double hxyz = (2.0/omegaxyz)*(std::sqrt(1.0+ratioxyz*ratioxyz) - ratioxyz);
+  double ratiorot = 0.0, hrot = 1.7976931348623157e308;
+  if (omegarot > 0.0)
+  {
+    ratiorot = damping / (2.0*mrot*omegarot);
+    hrot = (2.0/omegarot)*(std::sqrt(1.0+ratiorot*ratiorot) - ratiorot);
+  }
+  *omega = omegaxyz > omegarot ? omegaxyz : omegarot;
+  *ratio = ratioxyz > ratiorot ? ratioxyz : ratiorot;
+  return hxyz < hrot ? hxyz : hrot;
+}
+
+/* krot terms of one body-frame arm A (forces.ispc:514-522, 1262-1268) */
+inline void krot_add(double *krot, const double *A)
+{
+  const double dt = DOT(A, A);
+  krot[0] += dt - A[0]*A[0];
+  krot[1] += dt - A[1]*A[1];
+  krot[2] += dt - A[2]*A[2];
+  krot[3] += -A[0]*A[1];
+  krot[4] += -A[0]*A[2];
+  krot[5] += -A[1]*A[2];
 }
 
 /* ---------------- contact records (condet.h:33-64 restated) --------------- */
@@ -260,6 +351,7 @@ struct SlaveCon
 {
   int mpart, mell;
   double point[3], force[3];
+  double kcur, ecur;   /* the contact's own (the reference's slave copy leaves them unset, forces.ispc:383-405) */
 };
 
 /* canonical order of a master list: sphere partners by ellipsoid index, then triangles */
@@ -275,6 +367,9 @@ struct or_ctx
   std::vector<std::vector<Con>> master;      /* per particle */
   std::vector<std::vector<SlaveCon>> slave;  /* per particle */
   int threads = 1;
+  /* adaptive stepping terms per particle, component-major:
+   * kact[3][P], krot[6][P], kmax[P], emax[P] (forces.ispc:453-596) */
+  std::vector<double> kact, krot, kmax, emax;
 };
 
 namespace {
@@ -915,13 +1010,21 @@ void contacts_one(pg_scene *s, std::vector<Con> &ml, int i, const double *obsang
   ml.resize(keep);
 }
 
-/* ---------------- forces.ispc:453-596 contacts_acc_task (one particle) ---- */
+/* ---------------- forces.ispc:453-596 contacts_acc_task (one particle) ----
+ * With 'ad' (adaptive stepping) also the stiffness terms: |normal| (master) or
+ * |force direction| (slave) into kact, the contact stiffness and damping into
+ * kmax/emax, and the arm terms of L*a into krot, master list first. */
+struct AdTerms { double *kact[3], *krot[6], *kmax, *emax; };
+
 void contacts_acc_one(pg_scene *s, const std::vector<Con> &ml, const std::vector<SlaveCon> &sl,
-                      int i, const double gravity[3])
+                      int i, const double gravity[3], const AdTerms *ad)
 {
   double fs[3] = {0.0, 0.0, 0.0}, ts[3] = {0.0, 0.0, 0.0};
   double po[3] = {s->position[0][i], s->position[1][i], s->position[2][i]};
   double ma = s->mass[i];
+  double kact0[3] = {0.0, 0.0, 0.0}, krot0[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, kmax0 = 0.0, emax0 = 0.0;
+  double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (ad) for (int k = 0; k < 9; k ++) L[k] = s->rotation[k][i];
   for (const Con &m : ml)
   {
     const double *f = m.force;
@@ -930,6 +1033,17 @@ void contacts_acc_one(pg_scene *s, const std::vector<Con> &ml, const std::vector
     ts[0] += a[1]*f[2] - a[2]*f[1];
     ts[1] += a[2]*f[0] - a[0]*f[2];
     ts[2] += a[0]*f[1] - a[1]*f[0];
+    if (ad)
+    {
+      kact0[0] += std::fabs(m.normal[0]);
+      kact0[1] += std::fabs(m.normal[1]);
+      kact0[2] += std::fabs(m.normal[2]);
+      kmax0 = m.kcur > kmax0 ? m.kcur : kmax0;
+      emax0 = m.ecur > emax0 ? m.ecur : emax0;
+      double A[3];
+      NVMUL(L, a, A);
+      krot_add(krot0, A);
+    }
   }
   for (const SlaveCon &m : sl)
   {
@@ -939,6 +1053,25 @@ void contacts_acc_one(pg_scene *s, const std::vector<Con> &ml, const std::vector
     ts[0] += a[1]*f[2] - a[2]*f[1];
     ts[1] += a[2]*f[0] - a[0]*f[2];
     ts[2] += a[0]*f[1] - a[1]*f[0];
+    if (ad)
+    {
+      double u[3] = {f[0], f[1], f[2]};
+      double len = LEN(u);
+      if (len != 0.0)
+      {
+        len = 1.0/len;
+        u[0] *= len; u[1] *= len; u[2] *= len;
+      }
+      else u[0] = u[1] = u[2] = 0.0;
+      kact0[0] += std::fabs(u[0]);
+      kact0[1] += std::fabs(u[1]);
+      kact0[2] += std::fabs(u[2]);
+      kmax0 = m.kcur > kmax0 ? m.kcur : kmax0;
+      emax0 = m.ecur > emax0 ? m.ecur : emax0;
+      double A[3];
+      NVMUL(L, a, A);
+      krot_add(krot0, A);
+    }
   }
   s->force[0][i] = fs[0] + ma * gravity[0];
   s->force[1][i] = fs[1] + ma * gravity[1];
@@ -946,6 +1079,13 @@ void contacts_acc_one(pg_scene *s, const std::vector<Con> &ml, const std::vector
   s->torque[0][i] = ts[0];
   s->torque[1][i] = ts[1];
   s->torque[2][i] = ts[2];
+  if (ad)
+  {
+    for (int k = 0; k < 3; k ++) ad->kact[k][i] = kact0[k];
+    for (int k = 0; k < 6; k ++) ad->krot[k][i] = krot0[k];
+    ad->kmax[i] = kmax0;
+    ad->emax[i] = emax0;
+  }
 }
 
 /* ---------------- forces.ispc:410-450 look_up / look_up_slope ------------- */
@@ -1084,7 +1224,41 @@ static void spring_run_sum(const pg_scene *s, double *const out[9], const SprRun
   }
 }
 
-static void spring_flush(pg_scene *s, double *const out[9])
+/* adaptive stepping terms of one run (forces.ispc:1248-1345): per spring
+ * |z| (3), |stiffness|, |damping|, then the krot terms of the j arm (6) and
+ * of the k arm (6), zero where the spring's total force is zero; the run's
+ * partial sums start from zero (long runs chunked as above), its stiffness
+ * and damping partials are maxima. */
+static void spring_run_adaptive(const pg_scene *s, double *const ad[17], const SprRun &r, double *p, double *km,
+                                double *em)
+{
+  const int off = r.type == 0 ? 5 : 11;
+  for (int c = 0; c < 9; c ++) p[c] = 0.0;
+  *km = 0.0; *em = 0.0;
+  auto skipped = [&](int i) { return r.type == 1 && s->sprpart[1][i] < 0; };
+  auto add = [&](int i, double *q, double *qk, double *qe) {
+    for (int c = 0; c < 3; c ++) q[c] = q[c] + ad[c][i];
+    for (int c = 0; c < 6; c ++) q[3+c] = q[3+c] + ad[off+c][i];
+    *qk = ad[3][i] > *qk ? ad[3][i] : *qk;
+    *qe = ad[4][i] > *qe ? ad[4][i] : *qe;
+  };
+  if (r.e - r.b <= SPRING_RUN_LONG)
+  {
+    for (int i = r.b; i < r.e; i ++) if (!skipped(i)) add(i, p, km, em);
+    return;
+  }
+  const int len = r.e - r.b, ch = spring_run_chunk(len);
+  for (int b = r.b; b < r.e; b += ch)
+  {
+    double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, qk = 0.0, qe = 0.0;
+    for (int i = b; i < std::min(b + ch, r.e); i ++) if (!skipped(i)) add(i, q, &qk, &qe);
+    for (int c = 0; c < 9; c ++) p[c] = p[c] + q[c];
+    *km = qk > *km ? qk : *km;
+    *em = qe > *em ? qe : *em;
+  }
+}
+
+static void spring_flush(pg_scene *s, double *const out[9], double *const ad[17], const AdTerms *at)
 {
   const int S = s->sprnum;
   std::vector<SprRun> runs;
@@ -1115,13 +1289,25 @@ static void spring_flush(pg_scene *s, double *const out[9])
       if (sg > 0) { s->force[c][r.part] += acc[c]; s->torque[c][r.part] += acc[3+c]; }
       else { s->force[c][r.part] -= acc[c]; s->torque[c][r.part] -= acc[3+c]; }
     }
+    if (at)
+    {
+      double p[9], km, em;
+      spring_run_adaptive(s, ad, r, p, &km, &em);
+      for (int c = 0; c < 3; c ++) at->kact[c][r.part] += p[c];
+      for (int c = 0; c < 6; c ++) at->krot[c][r.part] += p[3+c];
+      at->kmax[r.part] = km > at->kmax[r.part] ? km : at->kmax[r.part];
+      at->emax[r.part] = em > at->emax[r.part] ? em : at->emax[r.part];
+    }
   }
 }
 
 /* ---------------- forces.ispc:641-1412 springs_task (single task) --------- */
-void springs_all(pg_scene *s, double step, double time)
+void springs_all(pg_scene *s, double step, double time, const AdTerms *at)
 {
   const int S = s->sprnum;
+  std::vector<double> adv(at ? 17 * (size_t)std::max(S, 1) : 0, 0.0);
+  double *ad[17];
+  for (int m = 0; m < 17; m ++) ad[m] = at ? adv.data() + (size_t)m * std::max(S, 1) : nullptr;
   double oj[3] = {0}, vj[3] = {0}, xj[3] = {0}, Xj[3] = {0}, Lj[9] = {0};
   double ok[3] = {0}, vk[3] = {0}, xk[3] = {0}, Xk[3] = {0}, Lk[9] = {0};
   int j0 = -1, k0 = -1;
@@ -1433,6 +1619,25 @@ void springs_all(pg_scene *s, double step, double time)
 
     out[0][i] = frc[0]; out[1][i] = frc[1]; out[2][i] = frc[2];
     out[3][i] = trq[0]; out[4][i] = trq[1]; out[5][i] = trq[2];
+    if (at && total_force != 0.0)
+    {
+      /* the k arm is taken in the k particle's frame; the reference rotates it
+       * with the j particle's rotation (forces.ispc:1341) */
+      double A[3], dt;
+      ad[0][i] = std::fabs(z[0]); ad[1][i] = std::fabs(z[1]); ad[2][i] = std::fabs(z[2]);
+      ad[3][i] = std::fabs(stiffness); ad[4][i] = std::fabs(damping);
+      TVMUL(Lj, a, A);
+      dt = DOT(A, A);
+      ad[5][i] = dt - A[0]*A[0]; ad[6][i] = dt - A[1]*A[1]; ad[7][i] = dt - A[2]*A[2];
+      ad[8][i] = -A[0]*A[1]; ad[9][i] = -A[0]*A[2]; ad[10][i] = -A[1]*A[2];
+      if (k >= 0)
+      {
+        TVMUL(Lk, b, A);
+        dt = DOT(A, A);
+        ad[11][i] = dt - A[0]*A[0]; ad[12][i] = dt - A[1]*A[1]; ad[13][i] = dt - A[2]*A[2];
+        ad[14][i] = -A[0]*A[1]; ad[15][i] = -A[0]*A[2]; ad[16][i] = -A[1]*A[2];
+      }
+    }
     if (k >= 0)
     {
       out[6][i] = b[1]*frc[2] - b[2]*frc[1];
@@ -1442,7 +1647,7 @@ void springs_all(pg_scene *s, double step, double time)
     }
     j0 = j;
   }
-  spring_flush(s, out);
+  spring_flush(s, out, ad, at);
 }
 
 /* ---------------- input.cpp:4247-4341 prescribe_acceleration -------------- */
@@ -1511,6 +1716,7 @@ void build_slaves(or_ctx *ctx, const pg_scene *s)
         sc.mpart = i; sc.mell = c.master;
         sc.point[0] = c.point[0]; sc.point[1] = c.point[1]; sc.point[2] = c.point[2];
         sc.force[0] = -c.force[0]; sc.force[1] = -c.force[1]; sc.force[2] = -c.force[2];
+        sc.kcur = c.kcur; sc.ecur = c.ecur;
         ctx->slave[c.slave0].push_back(sc);
       }
 }
@@ -1579,41 +1785,125 @@ void or_condet_forces(or_ctx *ctx, pg_scene *s, double step, double curtime,
   for (int i = 0; i < P; i ++) contacts_one(s, ctx->master[i], i, obs_ang, obs_lin, step, obsc);
   build_slaves(ctx, s);
 #pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
-  for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, gravity);
-  if (s->sprnum) springs_all(s, step, curtime);
+  for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, gravity, nullptr);
+  if (s->sprnum) springs_all(s, step, curtime, nullptr);
 }
+
+} /* extern "C" */
+
+namespace {
+
+AdTerms adaptive_terms(or_ctx *ctx, int P)
+{
+  ctx->kact.assign(3 * (size_t)P, 0.0);
+  ctx->krot.assign(6 * (size_t)P, 0.0);
+  ctx->kmax.assign((size_t)P, 0.0);
+  ctx->emax.assign((size_t)P, 0.0);
+  AdTerms at;
+  for (int c = 0; c < 3; c ++) at.kact[c] = ctx->kact.data() + (size_t)c * P;
+  for (int c = 0; c < 6; c ++) at.krot[c] = ctx->krot.data() + (size_t)c * P;
+  at.kmax = ctx->kmax.data();
+  at.emax = ctx->emax.data();
+  return at;
+}
+
+/* one step of the dem() loop body (parmec.cpp:2418-2517) with step0 and
+ * step1: condet, forces (with the adaptive terms when at != NULL), the step
+ * choice, prescribe, dynamics, shapes, obstacles; returns step1 */
+double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double step0, double adaptive,
+                 const AdTerms *at)
+{
+  const int P = s->parnum;
+  const bool typo = (s->compat & PG_COMPAT_EXPMAP) != 0;
+  const double *grav = tab->gravity ? tab->gravity + 3*(size_t)n : zeros6;
+  const double *damp = tab->damping ? tab->damping + 6*(size_t)n : zeros6;
+  const double *plin = tab->prs_lin ? tab->prs_lin + (size_t)3*s->prsnum*n : NULL;
+  const double *pang = tab->prs_ang ? tab->prs_ang + (size_t)3*s->prsnum*n : NULL;
+  double curtime = tab->curtime ? tab->curtime[n] : 0.0;
+  bool obsc = (s->compat & PG_COMPAT_OBSIDX) != 0;
+
+  /* partitioning_store + condet + read_gravity_and_damping + forces */
+  condet(ctx, s);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
+  for (int i = 0; i < P; i ++) contacts_one(s, ctx->master[i], i, s->obsang, s->obslin, step0, obsc);
+  build_slaves(ctx, s);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
+  for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, grav, at);
+  if (s->sprnum) springs_all(s, step0, curtime, at);
+
+  /* adaptive_timestep (parmec.ispc:397-420) */
+  double step1 = step0;
+  if (at)
+  {
+    double hmin = 1.7976931348623157e308;
+    for (int i = 0; i < P; i ++)
+    {
+      double kact[3] = {at->kact[0][i], at->kact[1][i], at->kact[2][i]}, krot[6], J[9], om, ra;
+      for (int c = 0; c < 6; c ++) krot[c] = at->krot[c][i];
+      for (int c = 0; c < 9; c ++) J[c] = s->inertia[c][i];
+      double h = critical_step(kact, at->kmax[i], at->emax[i], krot, s->mass[i], J, &om, &ra);
+      hmin = h < hmin ? h : hmin;
+    }
+    if (hmin < 1.7976931348623157e308) step1 = adaptive*hmin;
+  }
+
+  /* prescribe_acceleration, dynamics, prescribe_velocity */
+  if (s->prsnum && plin && pang) prescribe_acceleration(s, plin, pang);
+#pragma omp parallel for schedule(static) num_threads(ctx->threads)
+  for (int i = 0; i < P; i ++) dynamics_one(s, i, damp, step0, step1, typo);
+  if (s->prsnum && plin && pang) prescribe_velocity(s, plin, pang);
+
+  /* shapes (partial update), obstaclev(curtime+step0), obstacles(0.5*(step0+step1)) */
+  shapes_all(ctx, s, true);
+  for (int k = 0; k < 3*s->obsnum; k ++)
+  {
+    s->obsang[k] = tab->obs_ang ? tab->obs_ang[(size_t)3*s->obsnum*n + k] : 0.0;
+    s->obslin[k] = tab->obs_lin ? tab->obs_lin[(size_t)3*s->obsnum*n + k] : 0.0;
+  }
+  obstacles_all(s, s->obsang, s->obslin, 0.5*(step0+step1), typo);
+  return step1;
+}
+
+} /* namespace */
+
+extern "C" {
 
 /* The loop body of dem() (parmec.cpp:2418-2517) for tab->nsteps steps with a
  * fixed step (adaptive == 0, so step0 == step1 == step). */
 int or_run(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, double step)
 {
-  const int P = s->parnum;
-  const bool typo = (s->compat & PG_COMPAT_EXPMAP) != 0;
+  for (int n = 0; n < tab->nsteps; n ++) loop_step(ctx, s, tab, n, step, 0.0, nullptr);
+  return 0;
+}
+
+/* The same with adaptive stepping (0 < adaptive <= 1): step n runs with
+ * step0 = the previous step's step1 (the first with 'step0') and writes its
+ * step1, adaptive * the smallest critical step of the particles, or step0
+ * when nothing is restrained, to steps[n]. */
+int or_run_adaptive(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, double step0, double adaptive, double *steps)
+{
+  AdTerms at = adaptive_terms(ctx, s->parnum);
   for (int n = 0; n < tab->nsteps; n ++)
   {
-    const double *grav = tab->gravity ? tab->gravity + 3*(size_t)n : zeros6;
-    const double *damp = tab->damping ? tab->damping + 6*(size_t)n : zeros6;
-    const double *plin = tab->prs_lin ? tab->prs_lin + (size_t)3*s->prsnum*n : NULL;
-    const double *pang = tab->prs_ang ? tab->prs_ang + (size_t)3*s->prsnum*n : NULL;
-    double curtime = tab->curtime ? tab->curtime[n] : 0.0;
+    step0 = loop_step(ctx, s, tab, n, step0, adaptive, &at);
+    if (steps) steps[n] = step0;
+  }
+  return 0;
+}
 
-    /* partitioning_store + condet + read_gravity_and_damping + forces */
-    or_condet_forces(ctx, s, step, curtime, grav, s->obsang, s->obslin);
-
-    /* prescribe_acceleration, dynamics, prescribe_velocity */
-    if (s->prsnum && plin && pang) prescribe_acceleration(s, plin, pang);
-#pragma omp parallel for schedule(static) num_threads(ctx->threads)
-    for (int i = 0; i < P; i ++) dynamics_one(s, i, damp, step, step, typo);
-    if (s->prsnum && plin && pang) prescribe_velocity(s, plin, pang);
-
-    /* shapes (partial update), obstaclev(curtime+step0), obstacles(step) */
-    shapes_all(ctx, s, true);
-    for (int k = 0; k < 3*s->obsnum; k ++)
-    {
-      s->obsang[k] = tab->obs_ang ? tab->obs_ang[(size_t)3*s->obsnum*n + k] : 0.0;
-      s->obslin[k] = tab->obs_lin ? tab->obs_lin[(size_t)3*s->obsnum*n + k] : 0.0;
-    }
-    obstacles_all(s, s->obsang, s->obslin, step, typo);
+/* Per-particle critical step, frequency and damping ratio from the terms of
+ * the latest adaptive step (time_step_task, parmec.ispc:275-383). */
+int or_critical_terms(or_ctx *ctx, const pg_scene *s, double *h, double *omega, double *ratio)
+{
+  const int P = s->parnum;
+  if ((int)ctx->kmax.size() != P) return -1;
+  for (int i = 0; i < P; i ++)
+  {
+    double kact[3], krot[6], J[9];
+    for (int c = 0; c < 3; c ++) kact[c] = ctx->kact[(size_t)c*P + i];
+    for (int c = 0; c < 6; c ++) krot[c] = ctx->krot[(size_t)c*P + i];
+    for (int c = 0; c < 9; c ++) J[c] = s->inertia[c][i];
+    h[i] = critical_step(kact, ctx->kmax[i], ctx->emax[i], krot, s->mass[i], J, &omega[i], &ratio[i]);
   }
   return 0;
 }

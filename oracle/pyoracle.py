@@ -45,6 +45,8 @@ def load():
         "or_first_half_step": (None, [P, S, ctypes.c_double, D, D]),
         "or_condet_forces": (None, [P, S, ctypes.c_double, ctypes.c_double, D, D, D]),
         "or_run": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double]),
+        "or_run_adaptive": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double, ctypes.c_double, D]),
+        "or_critical_terms": (ctypes.c_int, [P, S, D, D, D]),
         "or_dynamics": (None, [P, S, D, ctypes.c_double, ctypes.c_double]),
         "or_shapes": (None, [P, S]),
         "or_obstacles": (None, [P, S, ctypes.c_double]),
@@ -98,6 +100,21 @@ class OracleEngine:
 
     def run(self, tab, step):
         self.lib.or_run(self.ctx, ctypes.byref(self.scene), ctypes.byref(tab), step)
+
+    def run_adaptive(self, tab, step0, adaptive):
+        """tab.nsteps adaptive steps from step0; returns each step's step1."""
+        steps = np.zeros(max(1, tab.nsteps))
+        self.lib.or_run_adaptive(self.ctx, ctypes.byref(self.scene), ctypes.byref(tab), step0, adaptive,
+                                 abi.dptr(steps))
+        return steps[:tab.nsteps]
+
+    def critical_terms(self):
+        """Per-particle (step, omega, ratio) from the latest adaptive step's terms."""
+        n = self.model.parnum
+        h, o, r = np.zeros(max(1, n)), np.zeros(max(1, n)), np.zeros(max(1, n))
+        if self.lib.or_critical_terms(self.ctx, ctypes.byref(self.scene), abi.dptr(h), abi.dptr(o), abi.dptr(r)):
+            raise RuntimeError("no adaptive step has run")
+        return h[:n], o[:n], r[:n]
 
     def sync(self):
         pass

@@ -32,14 +32,34 @@ import math
 import numpy as np
 
 REAL_MAX = 1.7976931348623157E+308
-ALG_PI = 3.14159265358979323846
+
+
+def _triple_angle_root(r, largest):
+    """cos(acos(r)/3) (largest) or cos(acos(r)/3 + 2 pi/3) as roots of the
+    triple-angle identity 4c^3 - 3c = r, by Newton's method from c = 1 (or -1),
+    monotone on [1/2, 1] (and [-1, -1/2]); the device and the CPU restatement
+    run the same operations."""
+    r = -1.0 if r < -1.0 else (1.0 if r > 1.0 else r)
+    c = 1.0 if largest else -1.0
+    for _ in range(100):
+        f = (4.0 * c * c - 3.0) * c - r
+        den = 12.0 * c * c - 3.0
+        if den == 0.0:
+            break
+        cn = c - f / den
+        if (largest and not cn < c) or (not largest and not cn > c):
+            break
+        c = cn
+    return c
 
 
 def _extremum_eigenvalue(A, minimum):
-    """extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3."""
+    """extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3;
+    its diagonal branch returns the largest entry whichever is asked for."""
     p1 = A[3] * A[3] + A[6] * A[6] + A[7] * A[7]
     if p1 == 0.0:
-        return max(max(A[0], A[4]), A[8])
+        r = A[0] if A[0] > A[4] else A[4]
+        return r if r > A[8] else A[8]
     q = (A[0] + A[4] + A[8]) / 3.0
     p2 = (A[0] - q) * (A[0] - q) + (A[4] - q) * (A[4] - q) + (A[8] - q) * (A[8] - q) + 2 * p1
     p = math.sqrt(p2 / 6.0)
@@ -47,17 +67,8 @@ def _extremum_eigenvalue(A, minimum):
     B = [invp * (A[0] - q), invp * A[1], invp * A[2], invp * A[3], invp * (A[4] - q), invp * A[5],
          invp * A[6], invp * A[7], invp * (A[8] - q)]
     det = (B[0] * (B[4] * B[8] - B[5] * B[7]) + B[3] * (B[2] * B[7] - B[1] * B[8])
-           + (B[1] * B[5] - B[2] * B[4]) * B[6])
-    r = 0.5 * det
-    if r <= -1.0:
-        phi = ALG_PI / 3.0
-    elif r >= 1.0:
-        phi = 0.0
-    else:
-        phi = math.acos(r) / 3.0
-    if minimum:
-        return q + 2.0 * p * math.cos(phi + (2 * ALG_PI / 3))
-    return q + 2.0 * p * math.cos(phi)
+           + B[6] * (B[1] * B[5] - B[2] * B[4]))
+    return q + 2.0 * p * _triple_angle_root(0.5 * det, not minimum)
 
 
 def pairing(m, i, j):

@@ -62,6 +62,7 @@ struct Compat
   long long launches = 0;
   const char *fn = "";                        // entry point running (for messages)
   std::vector<int> h_part, h_ellcol, h_triobs, h_tricol;   // of the last condet(), for materialize
+  double *hs = nullptr;                       // adaptive stepping: step0, step1, factor (view().hs when used)
 };
 
 Compat G;
@@ -657,8 +658,8 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
             int lcidx[], double gravity[3], int trqsprnum, int *[2],
             double *[3], double *[3], double *[3][2], int *[3], double *[3][2], int *[3],
             int[], double *[3], double *[3], double *[3], double *[3], double *[3],
-            double *force[3], double *torque[3], double *[3], double kmax[],
-            double emax[], double *[6], int adaptive, int unsprnum, int[],
+            double *force[3], double *torque[3], double *kact[3], double kmax[],
+            double emax[], double *krot[6], int adaptive, int unsprnum, int[],
             int[], int[], int[], double *[2], int[], int[], int[], int[], int[], int[],
             int[], int[], int, double time)
 {
@@ -667,7 +668,11 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   if (parnum <= 0 || !ready()) return;
   if (trqsprnum > 0) { fail(PG_ERR_UNSUPPORTED, "forces: TORSION_SPRING is not supported"); return; }
   if (unsprnum > 0) { fail(PG_ERR_UNSUPPORTED, "forces: UNSPRING is not supported"); return; }
-  if (adaptive) { fail(PG_ERR_UNSUPPORTED, "forces: adaptive time stepping is not supported"); return; }
+  if (adaptive && (!kact || !kmax || !emax || !krot))
+  {
+    fail(PG_ERR_ARGUMENT, "forces: adaptive stepping needs kact, kmax, emax and krot");
+    return;
+  }
   PgDev &d = G.d;
   const size_t P = parnum, S = std::max(sprnum, 0);
   const bool contacts = G.lists && G.owner == (const void *)master && G.P == parnum && G.E > 0;
@@ -689,10 +694,21 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
          up(d.obsang, obsang, 3 * (size_t)rows);
   // gravity of this step (read_gravity_and_damping on the host) and the time for springs
   ok = ok && up(d.sgrav, gravity, 3) && up(d.t_curtime, &time, 1) && zeros(d.stepno, 1) && zeros(d.sexc_on, 1);
+  if (S || adaptive)
+    for (int k = 0; ok && k < 9; k ++) ok = up(d.rotation[k], rotation[k], P);
+  if (adaptive)
+  {
+    // stiffness terms (forces.ispc:453-596, 1248-1345) and the step for the kernels
+    for (int k = 0; ok && k < 3; k ++) ok = grow(d.akact[k], P);
+    for (int k = 0; ok && k < 6; k ++) ok = grow(d.akrot[k], P);
+    ok = ok && grow(d.akmax, P) && grow(d.aemax, P);
+    for (int k = 0; ok && k < 17; k ++) ok = grow(d.sad[k], S);
+    const double h3[3] = {step, step, 1.0};
+    ok = ok && up(G.hs, h3, 3);
+  }
   if (S)
   {
-    for (int k = 0; ok && k < 9; k ++) ok = up(d.rotation[k], rotation[k], P) && up(d.inertia[k], inertia[k], P) &&
-                                       up(d.inverse[k], inverse[k], P);
+    for (int k = 0; ok && k < 9; k ++) ok = up(d.inertia[k], inertia[k], P) && up(d.inverse[k], inverse[k], P);
     for (int k = 0; ok && k < 3; k ++) ok = up(d.position[3+k], position[3+k], P);
     ok = ok && up(d.sprtype, sprtype, S) && up(d.unspring, unspring, S);
     for (int k = 0; ok && k < 2; k ++) ok = up(d.sprpart[k], sprpart[k], S);
@@ -719,6 +735,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     pg_spring_events(parnum, (int)S, sprpart[0], sprpart[1], first, ev, big);
     ok = ok && up(d.sev_first, first.data(), P + 1) && up(d.sev, ev.data(), ev.size()) &&
          up(d.sbig, big.data(), big.size()) && grow(d.sbig_sum, 6 * std::max<size_t>(1, big.size()));
+    if (adaptive) ok = ok && grow(d.sbig_ad, 11 * std::max<size_t>(1, big.size()));
     d.nbig = (int)big.size();
   }
   if (!ok) return;
@@ -729,12 +746,20 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   v.obsnum = rows;
   v.prsnum = 0;
   if (!contacts) { v.ellnum = 0; v.pell = nullptr; }
+  if (adaptive) v.hs = G.hs;
   pg_launch_contacts(v, G.st, step);
   pg_launch_springs(v, G.st, step);
   if (S) pg_launch_spring_runs(v, G.st);
-  pg_launch_force_sums(v, G.st);
-  G.launches += (v.ellnum ? 1 : 0) + (S ? 1 : 0) + 1;
+  if (adaptive) pg_launch_force_sums_adapt(v, G.st);
+  else pg_launch_force_sums(v, G.st);
+  G.launches += (v.ellnum ? 1 : 0) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 2 : 1) : 0) + 1;
   for (int k = 0; ok && k < 3; k ++) ok = down(force[k], d.force[k], P) && down(torque[k], d.torque[k], P);
+  if (adaptive)
+  {
+    for (int k = 0; ok && k < 3; k ++) ok = down(kact[k], d.akact[k], P);
+    for (int k = 0; ok && k < 6; k ++) ok = down(krot[k], d.akrot[k], P);
+    ok = ok && down(kmax, d.akmax, P) && down(emax, d.aemax, P);
+  }
   if (S)
   {
     for (int a = 0; ok && a < 2; a ++)
@@ -747,8 +772,8 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   }
   if (!ok) return;
   // zero_force_torque_kmax (forces.ispc) also clears kmax and emax
-  if (kmax) std::memset(kmax, 0, P * sizeof(double));
-  if (emax) std::memset(emax, 0, P * sizeof(double));
+  if (!adaptive && kmax) std::memset(kmax, 0, P * sizeof(double));
+  if (!adaptive && emax) std::memset(emax, 0, P * sizeof(double));
   finish("forces");
 }
 
@@ -799,10 +824,32 @@ void restrain_forces(int, int rstnum, int[], double *[9], double *[9], double *[
   if (rstnum > 0) fail(PG_ERR_UNSUPPORTED, "restrain_forces: RESTRAIN is not supported");
 }
 
-double adaptive_timestep(int, int, double[], double *[9], double *[3], double[], double[], double *[6], double step, double)
+// ---------------------------------------------------------------- adaptive_timestep (parmec.ispc:397-420)
+double adaptive_timestep(int, int parnum, double mass[], double *inertia[9], double *kact[3], double kmax[],
+                         double emax[], double *krot[6], double curstep, double adaptive)
 {
-  fail(PG_ERR_UNSUPPORTED, "adaptive_timestep: adaptive time stepping is not supported");
-  return step;
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "adaptive_timestep";
+  if (parnum <= 0 || !ready()) return curstep;
+  PgDev &d = G.d;
+  const size_t P = parnum;
+  bool ok = up(d.mass, mass, P) && zeros(d.pscene, P);
+  for (int k = 0; ok && k < 9; k ++) ok = up(d.inertia[k], inertia[k], P);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.akact[k], kact[k], P);
+  for (int k = 0; ok && k < 6; k ++) ok = up(d.akrot[k], krot[k], P);
+  ok = ok && up(d.akmax, kmax, P) && up(d.aemax, emax, P);
+  const double h3[3] = {curstep, curstep, adaptive};
+  const unsigned long long big = 0x7fefffffffffffffull;
+  ok = ok && up(G.hs, h3, 3) && up(d.hmin, &big, 1);
+  if (!ok) return curstep;
+  PgDev v = view();
+  v.parnum = parnum;
+  v.hs = G.hs;
+  pg_launch_adapt_step(v, G.st);
+  G.launches += 2;
+  double h1 = curstep;
+  if (!down(&h1, G.hs + 1, 1) || !finish("adaptive_timestep")) return curstep;
+  return h1;
 }
 
 // ---------------------------------------------------------------- additions

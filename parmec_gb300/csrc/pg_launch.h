@@ -16,6 +16,11 @@ void pg_launch_spring_runs(const PgDev &d, cudaStream_t s);     // sums of the l
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_force_sums(const PgDev &d, cudaStream_t s);                          // forces() tail
 void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1); // dynamics()
+// adaptive stepping (d.hs set): force sums with the stiffness terms, the step
+// choice on the device (adaptive_timestep), and the rest of the step
+void pg_launch_force_sums_adapt(const PgDev &d, cudaStream_t s);
+void pg_launch_adapt_step(const PgDev &d, cudaStream_t s);
+void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s);
 void pg_launch_mesh(const PgDev &d, cudaStream_t s);
 void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     // velocities from the step table
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);

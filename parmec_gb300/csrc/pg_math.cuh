@@ -245,4 +245,124 @@ PG_DEV void invert3(const double *F, double *INV)
   }
 }
 
+// NTMUL: C = A*B^T
+PG_DEV void ntmul(const double *A, const double *B, double *C)
+{
+  C[0] = A[0]*B[0]+A[3]*B[3]+A[6]*B[6];
+  C[1] = A[1]*B[0]+A[4]*B[3]+A[7]*B[6];
+  C[2] = A[2]*B[0]+A[5]*B[3]+A[8]*B[6];
+  C[3] = A[0]*B[1]+A[3]*B[4]+A[6]*B[7];
+  C[4] = A[1]*B[1]+A[4]*B[4]+A[7]*B[7];
+  C[5] = A[2]*B[1]+A[5]*B[4]+A[8]*B[7];
+  C[6] = A[0]*B[2]+A[3]*B[5]+A[6]*B[8];
+  C[7] = A[1]*B[2]+A[4]*B[5]+A[7]*B[8];
+  C[8] = A[2]*B[2]+A[5]*B[5]+A[8]*B[8];
+}
+
+// cos(acos(r)/3) (largest) or cos(acos(r)/3 + 2 pi/3) (smallest) as roots of
+// the triple-angle identity 4c^3 - 3c = r.  Newton's method from c = 1 (or
+// -1): the cubic is convex and increasing on [1/2, 1] (concave and increasing
+// on [-1, -1/2]), so the iterates move monotonically to the root and the loop
+// stops when they cease to.  Basic operations only, so every IEEE machine
+// gives the same bits (the CPU restatement runs the same steps).
+PG_DEV double triple_angle_root(double r, bool largest)
+{
+  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+  double c = largest ? 1.0 : -1.0;
+  for (int it = 0; it < 100; it ++)
+  {
+    const double f = (4.0*c*c - 3.0)*c - r;
+    const double cn = c - f/(12.0*c*c - 3.0);
+    if (largest ? !(cn < c) : !(cn > c)) break;
+    c = cn;
+  }
+  return c;
+}
+
+// extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3:
+// the trigonometric formula with the cosines taken by triple_angle_root.  The
+// diagonal branch returns the largest diagonal entry whichever is asked for,
+// as the reference does (macros.h:1545-1553).
+PG_DEV double extremum_eigenvalue(const double *A, bool minimum)
+{
+  double p1 = A[3]*A[3] + A[6]*A[6] + A[7]*A[7];
+  if (p1 == 0.0)
+  {
+    double r = A[0] > A[4] ? A[0] : A[4];
+    return r > A[8] ? r : A[8];
+  }
+  double q = (A[0]+A[4]+A[8])/3.0;
+  double p2 = (A[0]-q)*(A[0]-q) + (A[4]-q)*(A[4]-q) + (A[8]-q)*(A[8]-q) + 2*p1;
+  double p = sqrt(p2 / 6.0);
+  double invp = 1.0 / p;
+  double B[9] = {invp*(A[0]-q), invp*A[1], invp*A[2], invp*A[3], invp*(A[4]-q), invp*A[5],
+                 invp*A[6], invp*A[7], invp*(A[8]-q)};
+  double r = 0.5 * (B[0]*(B[4]*B[8]-B[5]*B[7]) + B[3]*(B[2]*B[7]-B[1]*B[8]) + B[6]*(B[1]*B[5]-B[2]*B[4]));
+  return q + 2.0 * p * triple_angle_root(r, !minimum);
+}
+
+// Critical step of one particle (time_step_task, parmec.ispc:275-383) from its
+// stiffness terms: translational sqrt(n k / m); rotational from K x = w^2 J x
+// through the Cholesky factor of J; each damped as (2/w)(sqrt(1+ksi^2) - ksi).
+// A particle without rotational stiffness (w_rot = 0: springs attached at the
+// mass centre) takes the translational step; the reference divides by zero
+// there and its NaN drops the particle from the minimum.  Returns DBL_MAX when
+// nothing restrains the particle.
+PG_DEV double critical_step(const double kact[3], double kmax, double emax, const double krot[6], double mass,
+                            const double J[9], double *omega, double *ratio)
+{
+  const double nxy = kact[0] > kact[1] ? kact[0] : kact[1];
+  const double nxyz = nxy > kact[2] ? nxy : kact[2];
+  if (!(nxyz > 0.0)) { *omega = 0.0; *ratio = 0.0; return 1.7976931348623157e308; }
+  const double k = kmax;
+  const double omegaxyz = sqrt(nxyz*k/mass);
+  double K[9];
+  K[0] = k*krot[0]; K[1] = k*krot[3]; K[2] = k*krot[4];
+  K[3] = K[1]; K[4] = k*krot[1]; K[5] = k*krot[5];
+  K[6] = K[2]; K[7] = K[5]; K[8] = k*krot[2];
+  const double mrot = extremum_eigenvalue(J, true);
+  double L[9], invL[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, tmp[9], A[9], inv;
+  L[0] = sqrt(J[0]);
+  inv = 1.0/L[0];
+  L[1] = inv * J[1];
+  L[2] = inv * J[2];
+  L[3] = 0.0;
+  L[4] = sqrt(J[4] - L[1]*L[1]);
+  inv = 1.0/L[4];
+  L[5] = inv * (J[5] - L[2]*L[1]);
+  L[6] = 0.0;
+  L[7] = 0.0;
+  L[8] = sqrt(J[8] - (L[2]*L[2] + L[5]*L[5]));
+  invert3(L, invL);
+  ntmul(K, invL, tmp);
+  nnmul(invL, tmp, A);
+  const double lambda = extremum_eigenvalue(A, false);
+  const double omegarot = lambda > 0.0 ? sqrt(lambda) : 0.0;
+  const double damping = emax;
+  const double ratioxyz = damping / (2.0*mass*omegaxyz);
+  const double hxyz = (2.0/omegaxyz)*(sqrt(1.0+ratioxyz*ratioxyz) - ratioxyz);
+  double ratiorot = 0.0, hrot = 1.7976931348623157e308;
+  if (omegarot > 0.0)
+  {
+    ratiorot = damping / (2.0*mrot*omegarot);
+    hrot = (2.0/omegarot)*(sqrt(1.0+ratiorot*ratiorot) - ratiorot);
+  }
+  *omega = omegaxyz > omegarot ? omegaxyz : omegarot;
+  *ratio = ratioxyz > ratiorot ? ratioxyz : ratiorot;
+  return hxyz < hrot ? hxyz : hrot;
+}
+
+// krot terms of one arm A (body frame): K(1,1), K(2,2), K(3,3), K(2,1),
+// K(3,1), K(3,2) (forces.ispc:514-522, 1262-1268)
+PG_DEV void krot_add(double *krot, const double *A)
+{
+  const double dt = dot3(A, A);
+  krot[0] += dt - A[0]*A[0];
+  krot[1] += dt - A[1]*A[1];
+  krot[2] += dt - A[2]*A[2];
+  krot[3] += -A[0]*A[1];
+  krot[4] += -A[0]*A[2];
+  krot[5] += -A[1]*A[2];
+}
+
 } // namespace pg

@@ -38,7 +38,13 @@ struct pg_session
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   double graph_step = 0.0;
+  int graph_adapt = 0;                     // the captured step is the adaptive one
   int use_graph = 1;
+  // adaptive stepping: device step pair, per-step records and the minimum
+  // (PgDev.hs points at hs_buf only while an adaptive run is enqueued)
+  double *hs_buf = nullptr;
+  int adapt_ready = 0, hrec_cap = 0, sbig_ad_cap = 0;
+  int exc_any = 0;                         // some scene has a device excitation
   // persistent fused step (mixed form): launch shape, autotuner state and
   // the captured graph of one chunk of fstep_chunk steps
   int fused = 0, tune = 0, tuned = 0, warmed = 0;
@@ -869,13 +875,121 @@ void enqueue_step(pg_session *s, double step)
 // graph is re-captured when a buffer is reallocated or the step changes)
 int capture_step(pg_session *s, double step)
 {
-  if (s->graph_exec && s->graph_step == step) return PG_OK;
+  if (s->graph_exec && !s->graph_adapt && s->graph_step == step) return PG_OK;
   drop_graph(s);
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   enqueue_step(s, step);
   CK(cudaStreamEndCapture(s->stream, &s->graph));
   CK(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
   s->graph_step = step;
+  s->graph_adapt = 0;
+  return PG_OK;
+}
+
+void enqueue_step_adaptive(pg_session *s);
+
+int capture_step_adaptive(pg_session *s)
+{
+  if (s->graph_exec && s->graph_adapt) return PG_OK;
+  drop_graph(s);
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step_adaptive(s);
+  CK(cudaStreamEndCapture(s->stream, &s->graph));
+  CK(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
+  s->graph_adapt = 1;
+  return PG_OK;
+}
+
+// per-particle and per-spring stiffness terms, the step pair and the
+// per-step records (sized with the step tables)
+int adapt_buffers(pg_session *s)
+{
+  PgDev &d = s->d;
+  const size_t P = std::max(d.parnum, 1), S = std::max(d.sprnum, 1);
+  if (!s->adapt_ready)
+  {
+    for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.akact[k], P));
+    for (int k = 0; k < 6; k ++) TRY(dalloc(s, &d.akrot[k], P));
+    TRY(dalloc(s, &d.akmax, P));
+    TRY(dalloc(s, &d.aemax, P));
+    for (int k = 0; k < 17; k ++) TRY(dalloc(s, &d.sad[k], S));
+    TRY(dalloc(s, &s->hs_buf, 4));
+    TRY(dalloc(s, &d.hmin, 1));
+    const unsigned long long big = 0x7fefffffffffffffull;
+    TRY(h2d(s, d.hmin, &big, 1));
+    s->adapt_ready = 1;
+  }
+  if (s->sbig_ad_cap < std::max(d.nbig, 1))
+  {
+    drop_graph(s);
+    CK(cudaStreamSynchronize(s->stream));
+    release(s, d.sbig_ad);
+    d.sbig_ad = nullptr;
+    TRY(dalloc(s, &d.sbig_ad, 11 * (size_t)std::max(d.nbig, 1)));
+    s->sbig_ad_cap = std::max(d.nbig, 1);
+  }
+  if (s->hrec_cap < s->tab_cap)
+  {
+    drop_graph(s);
+    CK(cudaStreamSynchronize(s->stream));
+    release(s, d.hrec);
+    d.hrec = nullptr;
+    TRY(dalloc(s, &d.hrec, (size_t)s->tab_cap));
+    s->hrec_cap = s->tab_cap;
+  }
+  return PG_OK;
+}
+
+// one adaptive step: forces with the stiffness terms, the step choice on
+// the device, then the rest of the step with (step0, step1) from d.hs
+void enqueue_step_adaptive(pg_session *s)
+{
+  const PgDev &d = s->d;
+  pg_launch_rebuild(d, s->stream);
+  pg_launch_excite(d, s->stream, 0.0);
+  pg_launch_contacts(d, s->stream, 0.0);
+  pg_launch_springs(d, s->stream, 0.0);
+  pg_launch_spring_runs(d, s->stream);
+  pg_launch_force_sums_adapt(d, s->stream);
+  pg_launch_adapt_step(d, s->stream);
+  pg_launch_dynamics_fused(d, s->stream);
+  pg_launch_mesh(d, s->stream);
+  pg_launch_obstacles_row(d, s->stream, 0.0);
+  pg_launch_tail(d, s->stream, 0.0);
+}
+
+int adaptive_kernel_count(const PgDev &d)
+{
+  int n = pg_rebuild_kernel_count(d) + 2 + 1;     // excite, select, tail
+  if (d.ellnum) n += 1;
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0);
+  if (d.parnum) n += 3;                           // force sums, minimum, dynamics
+  if (d.nodnum) n += 1;
+  if (d.facnum) n += 1;
+  if (d.obsnum && d.trinum) n += 1;
+  return n;
+}
+
+// host step tables of one call -> device (rows [0, n))
+int upload_tables(pg_session *s, const pg_steptab *tab, int n)
+{
+  PgDev &d = s->d;
+  std::vector<double> zeros;
+  auto put = [&](double *dst, const double *src, size_t width) -> int {
+    if (src) return h2d(s, dst, src, (size_t)n * width);
+    zeros.assign((size_t)n * width, 0.0);
+    int r = h2d(s, dst, zeros.data(), (size_t)n * width);
+    if (r == PG_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) return PG_ERR_CUDA;
+    return r;
+  };
+  TRY(put(d.t_curtime, tab->curtime, 1));
+  TRY(put(d.t_gravity, tab->gravity, 3));
+  TRY(put(d.t_damping, tab->damping, 6));
+  TRY(put(d.t_prs_lin, tab->prs_lin, s->prs_stride));
+  TRY(put(d.t_prs_ang, tab->prs_ang, s->prs_stride));
+  TRY(put(d.t_obs_ang, tab->obs_ang, s->obs_stride));
+  TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
+  CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
   return PG_OK;
 }
 
@@ -1022,23 +1136,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   const int n = tab->nsteps;
   if (n == 0) return PG_OK;
   TRY(ensure_tables(s, n));
-  // host tables -> device (rows of this call)
-  std::vector<double> zeros;
-  auto put = [&](double *dst, const double *src, size_t width) -> int {
-    if (src) return h2d(s, dst, src, (size_t)n * width);
-    zeros.assign((size_t)n * width, 0.0);
-    int r = h2d(s, dst, zeros.data(), (size_t)n * width);
-    if (r == PG_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) return PG_ERR_CUDA;
-    return r;
-  };
-  TRY(put(d.t_curtime, tab->curtime, 1));
-  TRY(put(d.t_gravity, tab->gravity, 3));
-  TRY(put(d.t_damping, tab->damping, 6));
-  TRY(put(d.t_prs_lin, tab->prs_lin, s->prs_stride));
-  TRY(put(d.t_prs_ang, tab->prs_ang, s->prs_stride));
-  TRY(put(d.t_obs_ang, tab->obs_ang, s->obs_stride));
-  TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
-  CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
+  TRY(upload_tables(s, tab, n));
   if (s->fused && d.form == PG_FORM_MIXED && !s->profile)
   {
     const long long before = s->fused_launches;
@@ -1104,6 +1202,37 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   s->launches += (long long)per_step * n;
   CK(cudaGetLastError());
   // the host tables are pageable: keep them alive until the copies finished
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, double adaptive, double *steps)
+{
+  if (!s || !tab || tab->nsteps < 0 || !(adaptive > 0.0 && adaptive <= 1.0) || !(step0 > 0.0))
+    return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (d.form != PG_FORM_FP64 || d.nscene > 1 || s->exc_any) return PG_ERR_UNSUPPORTED;
+  const int n = tab->nsteps;
+  if (n == 0) return PG_OK;
+  TRY(ensure_tables(s, n));
+  TRY(adapt_buffers(s));
+  TRY(upload_tables(s, tab, n));
+  const double h3[3] = {step0, step0, adaptive};
+  TRY(h2d(s, s->hs_buf, h3, 3));
+  d.hs = s->hs_buf;
+  int rc = PG_OK;
+  if (s->use_graph && !s->profile)
+  {
+    rc = capture_step_adaptive(s);
+    for (int k = 0; k < n && rc == PG_OK; k ++)
+      if (cudaGraphLaunch(s->graph_exec, s->stream) != cudaSuccess) rc = PG_ERR_CUDA;
+  }
+  else for (int k = 0; k < n; k ++) enqueue_step_adaptive(s);
+  d.hs = nullptr;
+  TRY(rc);
+  s->launches += (long long)adaptive_kernel_count(d) * n;
+  CK(cudaGetLastError());
+  if (steps) TRY(d2h(s, steps, d.hrec, (size_t)n));
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
@@ -1175,6 +1304,7 @@ int pg_session_scene(pg_session *s, int scene, int active, const double origin[3
   if (!s || scene < 0 || scene >= s->d.nscene) return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
   int a = active ? 1 : 0, on = exc ? 1 : 0;
+  if (exc) s->exc_any = 1;
   TRY(h2d(s, d.sactive + scene, &a, 1));
   TRY(h2d(s, d.sexc_on + scene, &on, 1));
   if (exc) TRY(h2d(s, d.sexc + (size_t)PG_EXC_LEN * scene, exc, PG_EXC_LEN));

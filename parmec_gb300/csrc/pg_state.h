@@ -60,6 +60,14 @@ struct PgDev
   double *sbig_sum;         // [nbig][6] their force and torque sums
   int nbig;
 
+  // ---- adaptive time step (parmec.ispc:275-420, forces.ispc:453-596, 1248-1345)
+  double *hs;               // [3]: step0, step1, factor (null: fixed step, from the kernel arguments)
+  double *hrec;             // [table rows] step1 of each step of a call
+  unsigned long long *hmin; // smallest critical step of the particles, as the bits of a non-negative double
+  double *akact[3], *akrot[6], *akmax, *aemax;   // [parnum] stiffness terms (k_contacts: master side only)
+  double *sad[17];          // [sprnum] |z| (3), |stiffness|, |damping|, krot of the j arm (6) and of the k arm (6)
+  double *sbig_ad;          // [nbig][11] long-run partials: kact (3), krot (6), kmax, emax
+
   // ---- prescribed motion
   int *prs_first;           // [parnum+1] CSR of prescriptions per particle
   int *prs_list;            // prescription indices in input order

@@ -214,6 +214,7 @@ __global__ void k_faces(PgDev d)
 // velocities: row of the step table (use_row) or the current obsang/obslin state
 __global__ void k_obstacles(PgDev d, double step, int use_row)
 {
+  if (d.hs) step = 0.5*(d.hs[0] + d.hs[1]);
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
   if (t < d.trinum) need = pgk::obstacles_item(d, t, step, use_row);
@@ -225,6 +226,17 @@ __global__ void k_obstacles(PgDev d, double step, int use_row)
 __global__ void k_tail(PgDev d, double step, int use_row)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (d.hs)
+  {
+    // adaptive: the obstacles move by (step0 + step1)/2; step1 is recorded
+    // for the host and becomes the next step's step0
+    const double h1 = d.hs[1];
+    step = 0.5*(d.hs[0] + h1);
+    d.hrec[use_row ? *d.stepno : 0] = h1;
+    pgk::tail_item(d, step, use_row);
+    d.hs[0] = h1;
+    return;
+  }
   pgk::tail_item(d, step, use_row);
 }
 
@@ -236,15 +248,19 @@ using pgk::pairing;
 // a contact persists while depth >= 0 (forces.ispc:191, removal 327-365) and
 // is created when depth > 0 (condet.ispc:183); existing sphere pairs use the
 // unguarded 1/len (condet.ispc:667), new ones the guarded one (137).
-template <bool GEOM>
+// ADAPT: adaptive stepping; the step comes from d.hs and the master-side
+// stiffness terms (forces.ispc:505-522) go to akact/akmax/aemax/akrot.
+template <bool GEOM, bool ADAPT>
 __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
 {
   const int E = d.ellnum;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= E) return;
+  if (ADAPT) step = d.hs[0];
   const int pi = d.part[i];
   const int cnt = d.ncnt[i];
   double fs[3] = {0.0, 0.0, 0.0}, ts[3] = {0.0, 0.0, 0.0};
+  double kact0[3] = {0.0, 0.0, 0.0}, krot0[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, kmax0 = 0.0, emax0 = 0.0;
   if (cnt > 0)
   {
     const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
@@ -447,10 +463,29 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       ts[0] += a[1]*f[2] - a[2]*f[1];
       ts[1] += a[2]*f[0] - a[0]*f[2];
       ts[2] += a[0]*f[1] - a[1]*f[0];
+      if (ADAPT)
+      {
+        kact0[0] += fabs(normal[0]);
+        kact0[1] += fabs(normal[1]);
+        kact0[2] += fabs(normal[2]);
+        kmax0 = kn > kmax0 ? kn : kmax0;
+        emax0 = en > emax0 ? en : emax0;
+        double L[9], A[3];
+        for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][pi];
+        nvmul(L, a, A);
+        krot_add(krot0, A);
+      }
     }
   }
   d.fm[0][pi] = fs[0]; d.fm[1][pi] = fs[1]; d.fm[2][pi] = fs[2];
   d.tm[0][pi] = ts[0]; d.tm[1][pi] = ts[1]; d.tm[2][pi] = ts[2];
+  if (ADAPT)
+  {
+    for (int k = 0; k < 3; k ++) d.akact[k][pi] = kact0[k];
+    for (int k = 0; k < 6; k ++) d.akrot[k][pi] = krot0[k];
+    d.akmax[pi] = kmax0;
+    d.aemax[pi] = emax0;
+  }
 }
 
 // ---------------------------------------------------------------- springs (forces.ispc:641-1412)
@@ -482,28 +517,6 @@ __device__ double look_up_slope(int i, const double *t0, const double *t1, int l
   if (lo+1 == h0) lo --;
   if (at) at[0] = tj[lo] + (tj[lo+1]-tj[lo])*(arg-ti[lo])/(ti[lo+1]-ti[lo]);
   return (t1[lo+1]-t1[lo])/(t0[lo+1]-t0[lo]);
-}
-
-__device__ double extremum_eigenvalue_min(const double *A)
-{
-  double p1 = A[3]*A[3] + A[6]*A[6] + A[7]*A[7];
-  if (p1 == 0.0)
-  {
-    double r = fmax(A[0], A[4]);
-    return fmax(r, A[8]);
-  }
-  double q = (A[0]+A[4]+A[8])/3.0;
-  double p2 = (A[0]-q)*(A[0]-q) + (A[4]-q)*(A[4]-q) + (A[8]-q)*(A[8]-q) + 2*p1;
-  double p = sqrt(p2 / 6.0);
-  double invp = 1.0 / p;
-  double B[9] = {invp*(A[0]-q), invp*A[1], invp*A[2], invp*A[3], invp*(A[4]-q), invp*A[5],
-                 invp*A[6], invp*A[7], invp*(A[8]-q)};
-  double r = 0.5 * (B[0]*(B[4]*B[8]-B[5]*B[7]) + B[3]*(B[2]*B[7]-B[1]*B[8]) + B[6]*(B[1]*B[5]-B[2]*B[4]));
-  double phi;
-  if (r <= -1.0) phi = 3.14159265358979323846 / 3.0;
-  else if (r >= 1.0) phi = 0.0;
-  else phi = acos(r) / 3.0;
-  return q + 2.0 * p * cos(phi + (2*3.14159265358979323846/3));
 }
 
 // equivalent relative point mass (parmec.ispc:423-482)
@@ -540,13 +553,19 @@ __device__ double eqm(const PgDev &d, int part1, const double *point1, int part2
     nvmul(Miv, direction, tmp);
     return 1.0/dot3(tmp, direction);
   }
-  return 1.0/extremum_eigenvalue_min(Miv);
+  return 1.0/pg::extremum_eigenvalue(Miv, true);
 }
 
+// ADAPT: adaptive stepping; the step comes from d.hs and each spring records
+// its stiffness terms (forces.ispc:1248-1345) in sad, zeros when its total
+// force is zero.  The k arm is taken in the k particle's frame (the reference
+// rotates it with the j particle's rotation, forces.ispc:1341).
+template <bool ADAPT>
 __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
 {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.sprnum) return;
+  if (ADAPT) step = d.hs[0];
   const double time = d.t_curtime[*d.stepno];
   const int j = d.sprpart[0][i], k = d.sprpart[1][i];
   double len = 0.0, inv, velocity, spring_force = 0.0, dashpot_force, total_force;
@@ -817,6 +836,31 @@ __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
   d.spr_out[6][i] = b[1]*frc[2] - b[2]*frc[1];
   d.spr_out[7][i] = b[2]*frc[0] - b[0]*frc[2];
   d.spr_out[8][i] = b[0]*frc[1] - b[1]*frc[0];
+  if (ADAPT)
+  {
+    double v[17];
+    for (int m = 0; m < 17; m ++) v[m] = 0.0;
+    if (total_force != 0.0)
+    {
+      double A[3], dt;
+      v[0] = fabs(z[0]); v[1] = fabs(z[1]); v[2] = fabs(z[2]);
+      v[3] = fabs(stiffness); v[4] = fabs(damping);
+      tvmul(Lj, a, A);
+      dt = dot3(A, A);
+      v[5] = dt - A[0]*A[0]; v[6] = dt - A[1]*A[1]; v[7] = dt - A[2]*A[2];
+      v[8] = -A[0]*A[1]; v[9] = -A[0]*A[2]; v[10] = -A[1]*A[2];
+      if (k >= 0)
+      {
+        double Lk[9];
+        for (int m = 0; m < 9; m ++) Lk[m] = d.rotation[m][k];
+        tvmul(Lk, b, A);
+        dt = dot3(A, A);
+        v[11] = dt - A[0]*A[0]; v[12] = dt - A[1]*A[1]; v[13] = dt - A[2]*A[2];
+        v[14] = -A[0]*A[1]; v[15] = -A[0]*A[2]; v[16] = -A[1]*A[2];
+      }
+    }
+    for (int m = 0; m < 17; m ++) d.sad[m][i] = v[m];
+  }
 }
 
 // ---------------------------------------------------------------- integrate
@@ -880,18 +924,68 @@ __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs(PgDev d)
   }
 }
 
+// Adaptive stiffness partials of the long runs, chunked as the force sums:
+// each chunk sums its springs' terms from zero in spring order (maxima for
+// the stiffness and damping), then the chunk partials are summed in order.
+__global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
+{
+  __shared__ double part[11][RUN_MAXCHUNKS];
+  const int4 v = d.sbig[blockIdx.x];
+  const int type = v.x & 1, off = type == 0 ? 5 : 11;
+  const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
+  for (int c = threadIdx.x; c < nc; c += RUN_THREADS)
+  {
+    double q[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, qk = 0.0, qe = 0.0;
+    const int b = v.y + c * ch, e = min(b + ch, v.z);
+    for (int s = b; s < e; s ++)
+    {
+      if (type == 1 && d.sprpart[1][s] < 0) continue;
+      for (int k = 0; k < 3; k ++) q[k] = q[k] + d.sad[k][s];
+      for (int k = 0; k < 6; k ++) q[3+k] = q[3+k] + d.sad[off+k][s];
+      const double xk = d.sad[3][s], xe = d.sad[4][s];
+      qk = xk > qk ? xk : qk;
+      qe = xe > qe ? xe : qe;
+    }
+    for (int k = 0; k < 9; k ++) part[k][c] = q[k];
+    part[9][c] = qk;
+    part[10][c] = qe;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double p[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, km = 0.0, em = 0.0;
+    for (int c = 0; c < nc; c ++)
+    {
+      for (int k = 0; k < 9; k ++) p[k] = p[k] + part[k][c];
+      km = part[9][c] > km ? part[9][c] : km;
+      em = part[10][c] > em ? part[10][c] : em;
+    }
+    for (int k = 0; k < 9; k ++) d.sbig_ad[11*blockIdx.x + k] = p[k];
+    d.sbig_ad[11*blockIdx.x + 9] = km;
+    d.sbig_ad[11*blockIdx.x + 10] = em;
+  }
+}
+
 // MODE: INT_FUSED runs the whole particle update of one step; the drop-in
 // entry points split it as the reference does: INT_FORCES ends with the
 // force and torque sums (the tail of forces(), forces.ispc:453-596) and
 // INT_DYNAMICS starts from the force and torque arrays (dynamics(),
 // dynamics.ispc:30-169, with h = step and h-bar = (step + step1)/2).
-enum { INT_FUSED = 0, INT_FORCES = 1, INT_DYNAMICS = 2 };
+// With adaptive stepping the step is split at the step choice:
+// INT_FORCES_ADAPT ends with the force sums and the complete stiffness terms
+// of every particle (forces.ispc:453-596, 1207-1412); INT_DYN_FUSED starts
+// from the force arrays and runs the rest of INT_FUSED with step0 and step1
+// from d.hs.
+enum { INT_FUSED = 0, INT_FORCES = 1, INT_DYNAMICS = 2, INT_FORCES_ADAPT = 3, INT_DYN_FUSED = 4 };
 
 template <int MODE>
 __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double step1)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
+  constexpr bool ADAPT = MODE == INT_FORCES_ADAPT;
+  constexpr bool FUSED = MODE == INT_FUSED || MODE == INT_DYN_FUSED;
+  if (MODE == INT_FORCES_ADAPT || MODE == INT_DYN_FUSED) { step = d.hs[0]; step1 = d.hs[1]; }
   if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
@@ -902,7 +996,20 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
     double F[3], T[3];
     const int e = d.pell ? d.pell[i] : -1;
     const double ma = d.mass[i];
-    if (MODE == INT_DYNAMICS)
+    double kact[3] = {0.0, 0.0, 0.0}, krot[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, kmax = 0.0, emax = 0.0;
+    double Li[9];
+    if (ADAPT)
+    {
+      for (int k = 0; k < 9; k ++) Li[k] = d.rotation[k][i];
+      if (e >= 0)
+      {
+        for (int k = 0; k < 3; k ++) kact[k] = d.akact[k][i];
+        for (int k = 0; k < 6; k ++) krot[k] = d.akrot[k][i];
+        kmax = d.akmax[i];
+        emax = d.aemax[i];
+      }
+    }
+    if (MODE == INT_DYNAMICS || MODE == INT_DYN_FUSED)
     {
       F[0] = d.force[0][i]; F[1] = d.force[1][i]; F[2] = d.force[2][i];
       T[0] = d.torque[0][i]; T[1] = d.torque[1][i]; T[2] = d.torque[2][i];
@@ -932,6 +1039,34 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
         T[0] += a[1]*f[2] - a[2]*f[1];
         T[1] += a[2]*f[0] - a[0]*f[2];
         T[2] += a[0]*f[1] - a[1]*f[0];
+        if (ADAPT)
+        {
+          // slave side (forces.ispc:539-567): the force direction, and the
+          // contact's own stiffness and damping (the reference reads slave
+          // records whose kcur/ecur nothing sets)
+          double u[3] = {f[0], f[1], f[2]};
+          double len = sqrt(dot3(u, u));
+          if (len != 0.0)
+          {
+            len = 1.0/len;
+            u[0] *= len; u[1] *= len; u[2] *= len;
+          }
+          else u[0] = u[1] = u[2] = 0.0;
+          kact[0] += fabs(u[0]);
+          kact[1] += fabs(u[1]);
+          kact[2] += fabs(u[2]);
+          const int ms = ref % E, code = d.ncode[ref];
+          const int ij = pairing(d, d.ellcol[ms], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
+          const double kc = d.iparam[0][ij];
+          double ec;
+          if (d.nen) ec = d.nen[ref];
+          else ec = d.iparam[1][ij] * 2.0 * sqrt(kc*(1.0 / (d.invm[d.part[ms]] + d.invm[i])));
+          kmax = kc > kmax ? kc : kmax;
+          emax = ec > emax ? ec : emax;
+          double A[3];
+          nvmul(Li, a, A);
+          krot_add(krot, A);
+        }
       }
     }
     F[0] = F[0] + ma * grav[0];
@@ -981,11 +1116,47 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
           F[0] -= af[0]; F[1] -= af[1]; F[2] -= af[2];
           T[0] -= at[0]; T[1] -= at[1]; T[2] -= at[2];
         }
+        if (ADAPT)
+        {
+          // the run's stiffness partials (forces.ispc:1212-1345): sums from
+          // zero in spring order, maxima for stiffness and damping
+          double p[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, km = 0.0, em = 0.0;
+          if (run >= 0)
+          {
+            for (int c = 0; c < 9; c ++) p[c] = d.sbig_ad[11*run + c];
+            km = d.sbig_ad[11*run + 9];
+            em = d.sbig_ad[11*run + 10];
+          }
+          else
+          {
+            const int ao = type == 0 ? 5 : 11;
+            for (int s = v.y; s < v.z; s ++)
+            {
+              if (type == 1 && d.sprpart[1][s] < 0) continue;
+              for (int c = 0; c < 3; c ++) p[c] = p[c] + d.sad[c][s];
+              for (int c = 0; c < 6; c ++) p[3+c] = p[3+c] + d.sad[ao+c][s];
+              const double xk = d.sad[3][s], xe = d.sad[4][s];
+              km = xk > km ? xk : km;
+              em = xe > em ? xe : em;
+            }
+          }
+          for (int c = 0; c < 3; c ++) kact[c] += p[c];
+          for (int c = 0; c < 6; c ++) krot[c] += p[3+c];
+          kmax = km > kmax ? km : kmax;
+          emax = em > emax ? em : emax;
+        }
       }
     }
 
     }
-    if (MODE == INT_FORCES)
+    if (ADAPT)
+    {
+      for (int k = 0; k < 3; k ++) d.akact[k][i] = kact[k];
+      for (int k = 0; k < 6; k ++) d.akrot[k][i] = krot[k];
+      d.akmax[i] = kmax;
+      d.aemax[i] = emax;
+    }
+    if (MODE == INT_FORCES || MODE == INT_FORCES_ADAPT)
     {
       d.force[0][i] = F[0]; d.force[1][i] = F[1]; d.force[2][i] = F[2];
       d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
@@ -994,7 +1165,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
 
     // prescribe_acceleration (input.cpp:4247-4341); the drop-in entry points
     // leave prescribed motion to the host, as parmec.cpp does
-    const bool prs = MODE == INT_FUSED && d.prsnum;
+    const bool prs = FUSED && d.prsnum;
     const int pb = prs ? d.prs_first[i] : 0, pe = prs ? d.prs_first[i+1] : 0;
     for (int pp = pb; pp < pe; pp ++)
     {
@@ -1132,7 +1303,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
     d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
 
     // ellipsoids_task for this particle's sphere (shapes.ispc:29-98)
-    if (MODE == INT_FUSED && e >= 0)
+    if (FUSED && e >= 0)
     {
       double X[3] = {d.position[3][i], d.position[4][i], d.position[5][i]};
       double C[3] = {d.center[3][e], d.center[4][e], d.center[5][e]}, c[3];
@@ -1142,7 +1313,43 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       need = (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
     }
   }
-  if (MODE == INT_FUSED && d.ellnum) flag_rebuild(d, need);
+  if (FUSED && d.ellnum) flag_rebuild(d, need);
+}
+
+// ---------------------------------------------------------------- adaptive step
+// adaptive_timestep (parmec.ispc:397-420): every particle's critical step
+// from its stiffness terms, reduced to the smallest.  Non-negative doubles
+// order as their bit patterns, so the minimum is an integer atomicMin (NaN
+// patterns sort above every finite step and never win, as NaN is dropped by
+// the reference's min).
+__global__ void __launch_bounds__(TPB) k_adapt_min(PgDev d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long bits = 0x7fefffffffffffffull;          // DBL_MAX
+  if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
+  {
+    double kact[3] = {d.akact[0][i], d.akact[1][i], d.akact[2][i]}, krot[6], J[9], om, ra;
+    for (int k = 0; k < 6; k ++) krot[k] = d.akrot[k][i];
+    for (int k = 0; k < 9; k ++) J[k] = d.inertia[k][i];
+    const double h = critical_step(kact, d.akmax[i], d.aemax[i], krot, d.mass[i], J, &om, &ra);
+    bits = (unsigned long long)__double_as_longlong(h);
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    const unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMin(d.hmin, bits);
+}
+
+// step1 = factor * the smallest critical step, or step0 when nothing is
+// restrained; re-arms the minimum for the next step
+__global__ void k_adapt_select(PgDev d)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double hmin = __longlong_as_double((long long)*d.hmin);
+  d.hs[1] = hmin < 1.7976931348623157e308 ? d.hs[2]*hmin : d.hs[0];
+  *d.hmin = 0x7fefffffffffffffull;
 }
 
 } // namespace
@@ -1179,18 +1386,26 @@ void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step)
 void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
 {
   if (!d.ellnum) return;
-  if (d.record_geometry) k_contacts<true><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
-  else k_contacts<false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  if (d.hs)
+  {
+    if (d.record_geometry) k_contacts<true, true><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+    else k_contacts<false, true><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  }
+  else if (d.record_geometry) k_contacts<true, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  else k_contacts<false, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
 }
 
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.sprnum) k_springs<<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
+  if (!d.sprnum) return;
+  if (d.hs) k_springs<true><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
+  else k_springs<false><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
 }
 
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
 {
   if (d.sprnum && d.nbig > 0) k_spring_runs<<<d.nbig, RUN_THREADS, 0, s>>>(d);
+  if (d.sprnum && d.nbig > 0 && d.hs) k_spring_runs_adapt<<<d.nbig, RUN_THREADS, 0, s>>>(d);
 }
 
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
@@ -1206,6 +1421,22 @@ void pg_launch_force_sums(const PgDev &d, cudaStream_t s)
 void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1)
 {
   if (d.parnum) k_integrate<INT_DYNAMICS><<<nblk(d.parnum), TPB, 0, s>>>(d, step0, step1);
+}
+
+void pg_launch_force_sums_adapt(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_integrate<INT_FORCES_ADAPT><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+}
+
+void pg_launch_adapt_step(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_adapt_min<<<nblk(d.parnum), TPB, 0, s>>>(d);
+  k_adapt_select<<<1, 32, 0, s>>>(d);
+}
+
+void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum) k_integrate<INT_DYN_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
 }
 
 void pg_launch_mesh(const PgDev &d, cudaStream_t s)

@@ -232,8 +232,8 @@ def default_engine(m):
     return GpuEngine(m)
 
 
-def run_dem(m, duration, step, interval, engine):
-    """dem() (parmec.cpp:2315-2530) for adaptive == 0."""
+def run_dem(m, duration, step, interval, engine, adaptive=0.0):
+    """dem() (parmec.cpp:2315-2530); 0 < adaptive <= 1 selects adaptive steps."""
     from .springs import sort_springs
     t_start = _time.perf_counter()
     dt, dt_func, dt_tms = _interval(m, interval, step)
@@ -264,6 +264,9 @@ def run_dem(m, duration, step, interval, engine):
         step0 = m.curstep
     eng.invert_inertia()
 
+    if 0.0 < adaptive <= 1.0:
+        return _run_adaptive(m, eng, duration, step0, adaptive, dt, dt_func, dt_tms, t_start)
+
     times, end_time = step_times(m.curtime, duration, step0)
     tabs = StepTables(m, times, step0, list(dt), dt_func, dt_tms)
 
@@ -286,5 +289,32 @@ def run_dem(m, duration, step, interval, engine):
     eng.download()
     m.curtime = end_time
     m.curstep = step0
+    m.stepnum += 1
+    return _time.perf_counter() - t_start
+
+
+def _run_adaptive(m, eng, duration, step0, adaptive, dt, dt_func, dt_tms, t_start):
+    """The dem() loop with adaptive steps (parmec.cpp:2418-2517): each step's
+    callbacks are sampled at its start time, which depends on the previous
+    step's step1, so the host runs one step per device call and advances
+    time += (step0 + step1)/2 with the step1 the device chose."""
+    dtl = list(dt)
+    t = 0.0
+    ct = m.curtime
+    step1 = step0
+    while t < duration:
+        tabs = StepTables(m, [ct], step0, dtl, dt_func, dt_tms)
+        step1 = float(eng.run_adaptive(tabs.ctab(0, 1), step0, adaptive)[0])
+        if ct >= m.curtime_history + tabs.interval[0, 1]:
+            eng.download()
+            sample_history(m, ct)
+            m.curtime_history += tabs.interval[0, 1]
+        inc = 0.5 * (step0 + step1)
+        t += inc
+        ct += inc
+        step0 = step1
+    eng.download()
+    m.curtime = ct
+    m.curstep = step1
     m.stepnum += 1
     return _time.perf_counter() - t_start

@@ -97,6 +97,13 @@ class GpuEngine:
     def run(self, tab, step):
         abi.check(self.lib.pg_session_run(self.sess, ctypes.byref(tab), step), "pg_session_run")
 
+    def run_adaptive(self, tab, step0, adaptive):
+        """tab.nsteps adaptive steps from step0 (pg_session_run_adaptive); returns each step's step1."""
+        steps = np.zeros(max(1, tab.nsteps))
+        abi.check(self.lib.pg_session_run_adaptive(self.sess, ctypes.byref(tab), step0, adaptive, abi.dptr(steps)),
+                  "pg_session_run_adaptive")
+        return steps[:tab.nsteps]
+
     def sync(self):
         abi.check(self.lib.pg_session_sync(self.sess), "pg_session_sync")
 

@@ -690,7 +690,8 @@ class Model:
 
     # ------------------------------------------------------------------ DEM
     def dem(self, duration, step, interval=None, prefix=None, adaptive=0.0, engine=None):
-        """DEM (input.cpp:3958-4091, parmec.cpp:2315-2530) with fixed steps.
+        """DEM (input.cpp:3958-4091, parmec.cpp:2315-2530); adaptive in (0, 1]
+        scales the smallest per-particle critical step into the next step.
 
         Returns the wall time in seconds, as the reference does."""
         from .driver import run_dem
@@ -700,9 +701,7 @@ class Model:
             raise ValueError("'step' must be positive")
         if not (0.0 <= adaptive <= 1.0):
             raise ValueError("'adaptive' must be in [0, 1]")
-        if adaptive > 0.0:
-            raise NotImplementedError("adaptive time stepping is not built (fixed steps only)")
-        return run_dem(self, float(duration), float(step), interval, engine)
+        return run_dem(self, float(duration), float(step), interval, engine, float(adaptive))
 
 
 def _invert(J):

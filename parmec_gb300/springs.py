@@ -224,7 +224,8 @@ def _eqm(m, part1, point1, part2, point2, direction):
     d = np.array(direction, dtype=float)
     if d @ d > 0.0:
         return 1.0 / float(d @ (Miv @ d))
-    return 1.0 / float(np.linalg.eigvalsh(Miv)[0])
+    from .critical import _extremum_eigenvalue
+    return 1.0 / _extremum_eigenvalue([float(x) for x in Miv.T.reshape(-1)], 1)
 
 
 def critical_perspring(m):

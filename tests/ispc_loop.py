@@ -92,8 +92,10 @@ def _prescribe_velocity(m, tab, k):
             P.angular[3:6, j] = o
 
 
-def dem(lib, host, duration, step):
-    """One DEM() call (fixed steps, no output) through the drop-in exports."""
+def dem(lib, host, duration, step, adaptive=0.0):
+    """One DEM() call (no output) through the drop-in exports; adaptive in
+    (0, 1] runs forces with the stiffness terms and adaptive_timestep
+    (parmec.cpp:2435-2450), sampling each step's host inputs at its start."""
     from parmec_gb300.springs import sort_springs
     m = host.m
     # dem() prologue: sort_materials and sort_springs (parmec.cpp:1636-1965)
@@ -104,8 +106,12 @@ def dem(lib, host, duration, step):
     s = m.scene()
     obspnt, obsang, obslin = m._obs_views
     ntasks = 1
-    times, _ = step_times(m.curtime, duration, step)
-    tab = StepTables(m, times, step, [1e9, 1e9], [None, None], [-1, -1])
+    adapt = 0.0 < adaptive <= 1.0
+    if adapt:
+        times = None
+    else:
+        times, _ = step_times(m.curtime, duration, step)
+        tab = StepTables(m, times, step, [1e9, 1e9], [None, None], [-1, -1])
     ellcon = tricon = faccon = 0
     step0 = step
     if m.curtime == 0.0:
@@ -123,10 +129,27 @@ def dem(lib, host, duration, step):
     tree = lib.partitioning_create(ntasks, s.ellnum - ellcon, s.center)
     kmax = np.zeros(max(1, s.parnum))
     emax = np.zeros(max(1, s.parnum))
+    kact = [np.zeros(max(1, s.parnum)) for _ in range(3)]
+    krot = [np.zeros(max(1, s.parnum)) for _ in range(6)]
+    kact_p = (abi.D * 3)(*[abi.dptr(a) for a in kact])
+    krot_p = (abi.D * 6)(*[abi.dptr(a) for a in krot])
     gravity = np.zeros(3)
     damping = np.zeros(6)
     step1 = step0
-    for k, t in enumerate(times):
+
+    def steps():
+        nonlocal tab
+        if not adapt:
+            yield from enumerate(times)
+            return
+        time = 0.0
+        while time < duration:
+            s0 = step0
+            tab = StepTables(m, [m.curtime], s0, [1e9, 1e9], [None, None], [-1, -1])
+            yield 0, m.curtime
+            time += 0.5 * (s0 + step1)                 # the body has set step1 (and step0 = step1)
+
+    for k, t in steps():
         if lib.partitioning_store(ntasks, ctypes.c_void_p(tree), s.ellnum - ellcon, s.ellcol, s.part, s.center,
                                   s.radii, NULL) > 0:
             raise AssertionError("partitioning_store overflowed")
@@ -141,9 +164,14 @@ def dem(lib, host, duration, step):
                    s.dashpot, s.dashidx, s.unload, s.unidx, s.yield_, s.sprdir, s.sprflg, s.sproffset,
                    s.sprfric, s.sprkskn, s.sprsdsp, s.stroke0, s.stroke, s.sprfrc, s.lcurve, s.lcidx,
                    abi.dptr(gravity), 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL,
-                   NULL, NULL, s.force, s.torque, NULL, abi.dptr(kmax), abi.dptr(emax), NULL, 0, 0,
+                   NULL, NULL, s.force, s.torque, kact_p if adapt else NULL, abi.dptr(kmax), abi.dptr(emax),
+                   krot_p if adapt else NULL, 1 if adapt else 0, 0,
                    NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, m.stepnum, D(t))
-        step1 = step0
+        if adapt:
+            step1 = lib.adaptive_timestep(ntasks, s.parnum, s.mass, s.inertia, kact_p, abi.dptr(kmax),
+                                          abi.dptr(emax), krot_p, D(step0), D(adaptive))
+        else:
+            step1 = step0
         lib.restrain_forces(ntasks, 0, NULL, NULL, NULL, s.force, s.torque)
         _prescribe_acceleration(m, tab, k, s)
         lib.dynamics(ntasks, ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), s.parnum, s.angular,

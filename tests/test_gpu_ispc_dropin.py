@@ -122,3 +122,42 @@ def test_dropin_unsupported_cases_report(gpu_lib):
     lib.restrain_velocities(1, 1, None, None, None, None, None, None)
     assert lib.pg_compat_status() == abi.PG_ERR_UNSUPPORTED
     lib.pg_compat_exit_on_error(1)
+
+
+def test_dropin_adaptive_bitwise(gpu_lib, oracle_lib):
+    """Adaptive stepping through forces(adaptive=1) + adaptive_timestep: the
+    stiffness terms come back to the host arrays, the step is chosen on the
+    device, and the state and chosen steps equal the oracle's bit for bit."""
+    from oracle.pyoracle import OracleEngine
+    lib = ispc_loop.library()
+    lib.pg_compat_exit_on_error(0)
+    lib.pg_compat_set_skin(ctypes.c_double(0.0))
+    mc, dt = make_collision_scene(n_side=4)
+    mo, _ = make_collision_scene(n_side=4)
+    host = ispc_loop.Host(lib, mc)
+    eo = OracleEngine()
+    mo.dem(40 * dt, dt, interval=1e9, adaptive=0.6, engine=eo)
+    ispc_loop.dem(lib, host, 40 * dt, dt, adaptive=0.6)
+    assert mc.curstep == mo.curstep and mc.curtime == mo.curtime
+    assert mc.curstep != dt
+    assert_bitwise(mc, mo)
+    host.close()
+
+
+def test_dropin_adaptive_springs_bitwise(gpu_lib, oracle_lib):
+    """Analytical bodies with full inertia tensors on springs of every
+    direction mode and a prescribed base, with adaptive steps (the rotational
+    eigenproblem takes its general branch)."""
+    from oracle.pyoracle import OracleEngine
+    from test_gpu_springs import lattice
+    lib = ispc_loop.library()
+    lib.pg_compat_exit_on_error(0)
+    step = 2e-5
+    mc, mo = lattice(), lattice()
+    host = ispc_loop.Host(lib, mc)
+    eo = OracleEngine()
+    mo.dem(40 * step, step, interval=1e9, adaptive=0.5, engine=eo)
+    ispc_loop.dem(lib, host, 40 * step, step, adaptive=0.5)
+    assert mc.curstep == mo.curstep and mc.curtime == mo.curtime
+    assert_bitwise(mc, mo)
+    host.close()
