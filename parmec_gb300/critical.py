@@ -22,7 +22,7 @@ from the session.  Positions taken:
   (the slave copy, forces.ispc:383-405, copies point and force only);
 * springs are classified by their own dashpot and flags; the reference
   indexes dashidx and sprflg with the particle index there
-  (parmec.ispc:726, 759);
+  (parmec.ispc:728, 759);
 * extremum_eigenvalue returns the largest eigenvalue of a diagonal matrix
   even when the smallest is asked for (macros.h:1545-1553), as in the
   reference (spheres are unaffected: their J is a multiple of I).
