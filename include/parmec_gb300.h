@@ -159,6 +159,15 @@ typedef struct pg_scene {
   int *tscene;          /* [trinum] scene of each triangle (a scene's triangles are contiguous) */
   int *oscene;          /* [obsnum] scene of each obstacle */
   int *sactive;         /* [nscene] 1 when the scene steps */
+
+  /* restraints (RESTRAIN, input.cpp:2458-2644): particle, then three linear
+   * and three angular orthonormal directions (zero rows where fewer are
+   * given) along which velocities (at each DEM call) and forces (each step)
+   * lose their components (restrain.ispc:30-133) */
+  int rstnum;
+  int *rstpart;
+  double *rstlin[9];
+  double *rstang[9];
 } pg_scene;
 
 /*
@@ -206,6 +215,11 @@ int pg_session_invert_inertia(pg_session *s);
 /* Advance tab->nsteps steps of the loop body of dem() (parmec.cpp:2418-2517)
  * with a fixed step (adaptive == 0).  Asynchronous on the session stream. */
 int pg_session_run(pg_session *s, const pg_steptab *tab, double step);
+
+/* restrain_velocities (restrain.ispc:137) of the scene's restraints: the
+ * DEM prologue calls it once after invert_inertia (parmec.cpp:2413).  The
+ * per-step restrain_forces runs inside the step. */
+int pg_session_restrain_velocities(pg_session *s);
 
 /* The same with adaptive stepping (DEM's 'adaptive', 0 < adaptive <= 1;
  * parmec.cpp:2443-2450, adaptive_timestep parmec.ispc:397-420): step n runs

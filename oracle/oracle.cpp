@@ -1650,6 +1650,70 @@ void springs_all(pg_scene *s, double step, double time, const AdTerms *at)
   spring_flush(s, out, ad, at);
 }
 
+/* ---------------- restrain.ispc:30-133 ------------------------------------ */
+/* v loses its components along the three direction rows of restraint q, in order */
+inline void restrain_vec(double *v, double *const dir[9], int q)
+{
+  for (int k = 0; k < 3; k ++)
+  {
+    const double l[3] = {dir[3*k][q], dir[3*k+1][q], dir[3*k+2][q]};
+    const double dot = DOT(v, l);
+    v[0] = v[0] - dot*l[0];
+    v[1] = v[1] - dot*l[1];
+    v[2] = v[2] - dot*l[2];
+  }
+}
+
+/* restrain_forces_task, restraints in input order */
+void restrain_forces(pg_scene *s)
+{
+  for (int q = 0; q < s->rstnum; q ++)
+  {
+    const int j = s->rstpart[q];
+    double f[3] = {s->force[0][j], s->force[1][j], s->force[2][j]};
+    double t[3] = {s->torque[0][j], s->torque[1][j], s->torque[2][j]};
+    restrain_vec(f, s->rstlin, q);
+    restrain_vec(t, s->rstang, q);
+    for (int c = 0; c < 3; c ++) { s->force[c][j] = f[c]; s->torque[c][j] = t[c]; }
+  }
+}
+
+/* restrain_velocities_task: linear, spatial and (with the directions taken to
+ * the body frame, L^T a) referential angular velocity */
+void restrain_velocities(pg_scene *s)
+{
+  for (int q = 0; q < s->rstnum; q ++)
+  {
+    const int j = s->rstpart[q];
+    double v[3] = {s->linear[0][j], s->linear[1][j], s->linear[2][j]};
+    double O[3] = {s->angular[0][j], s->angular[1][j], s->angular[2][j]};
+    double o[3] = {s->angular[3][j], s->angular[4][j], s->angular[5][j]};
+    double L[9];
+    for (int c = 0; c < 9; c ++) L[c] = s->rotation[c][j];
+    restrain_vec(v, s->rstlin, q);
+    restrain_vec(o, s->rstang, q);
+    double A[3][3];
+    for (int k = 0; k < 3; k ++)
+    {
+      const double a[3] = {s->rstang[3*k][q], s->rstang[3*k+1][q], s->rstang[3*k+2][q]};
+      TVMUL(L, a, A[k]);
+    }
+    for (int k = 0; k < 3; k ++)
+    {
+      const double dot = DOT(O, A[k]);
+      O[0] = O[0] - dot*A[k][0];
+      O[1] = O[1] - dot*A[k][1];
+      O[2] = O[2] - dot*A[k][2];
+    }
+    for (int c = 0; c < 3; c ++)
+    {
+      s->linear[c][j] = v[c];
+      s->angular[c][j] = O[c];
+      s->angular[3+c][j] = o[c];
+    }
+  }
+}
+
 /* ---------------- input.cpp:4247-4341 prescribe_acceleration -------------- */
 void prescribe_acceleration(pg_scene *s, const double *lin, const double *ang)
 {
@@ -1847,7 +1911,8 @@ double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double 
     if (hmin < 1.7976931348623157e308) step1 = adaptive*hmin;
   }
 
-  /* prescribe_acceleration, dynamics, prescribe_velocity */
+  /* restrain_forces, prescribe_acceleration, dynamics, prescribe_velocity */
+  if (s->rstnum) restrain_forces(s);
   if (s->prsnum && plin && pang) prescribe_acceleration(s, plin, pang);
 #pragma omp parallel for schedule(static) num_threads(ctx->threads)
   for (int i = 0; i < P; i ++) dynamics_one(s, i, damp, step0, step1, typo);
@@ -1890,6 +1955,13 @@ int or_run_adaptive(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, double step
   }
   return 0;
 }
+
+/* restrain_velocities export (restrain.ispc:137), called once per DEM call
+ * after invert_inertia (parmec.cpp:2413) */
+void or_restrain_velocities(or_ctx *, pg_scene *s) { restrain_velocities(s); }
+
+/* restrain_forces export (restrain.ispc:147) */
+void or_restrain_forces(or_ctx *, pg_scene *s) { restrain_forces(s); }
 
 /* Per-particle critical step, frequency and damping ratio from the terms of
  * the latest adaptive step (time_step_task, parmec.ispc:275-383). */

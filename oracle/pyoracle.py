@@ -47,6 +47,8 @@ def load():
         "or_run": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double]),
         "or_run_adaptive": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double, ctypes.c_double, D]),
         "or_critical_terms": (ctypes.c_int, [P, S, D, D, D]),
+        "or_restrain_velocities": (None, [P, S]),
+        "or_restrain_forces": (None, [P, S]),
         "or_dynamics": (None, [P, S, D, ctypes.c_double, ctypes.c_double]),
         "or_shapes": (None, [P, S]),
         "or_obstacles": (None, [P, S, ctypes.c_double]),
@@ -100,6 +102,9 @@ class OracleEngine:
 
     def run(self, tab, step):
         self.lib.or_run(self.ctx, ctypes.byref(self.scene), ctypes.byref(tab), step)
+
+    def restrain_velocities(self):
+        self.lib.or_restrain_velocities(self.ctx, ctypes.byref(self.scene))
 
     def run_adaptive(self, tab, step0, adaptive):
         """tab.nsteps adaptive steps from step0; returns each step's step1."""

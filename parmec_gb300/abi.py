@@ -68,6 +68,8 @@ class PgScene(ctypes.Structure):
         ("compat", ctypes.c_int),
         ("nscene", ctypes.c_int),
         ("pscene", I), ("tscene", I), ("oscene", I), ("sactive", I),
+        ("rstnum", ctypes.c_int),
+        ("rstpart", I), ("rstlin", D * 9), ("rstang", D * 9),
     ]
 
 
@@ -143,6 +145,7 @@ def load_library():
         "pg_session_invert_inertia": (ctypes.c_int, [P]),
         "pg_session_run": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double]),
         "pg_session_run_adaptive": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double, ctypes.c_double, D]),
+        "pg_session_restrain_velocities": (ctypes.c_int, [P]),
         "pg_session_sync": (ctypes.c_int, [P]),
         "pg_session_download": (ctypes.c_int, [P, ctypes.POINTER(PgScene)]),
         "pg_session_upload": (ctypes.c_int, [P, ctypes.POINTER(PgScene)]),

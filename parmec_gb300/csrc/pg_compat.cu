@@ -814,14 +814,71 @@ void dynamics(int, master_conpnt[], slave_conpnt[], int parnum, double *angular[
 }
 
 // ---------------------------------------------------------------- outside the hot path
-void restrain_velocities(int, int rstnum, int[], double *[9], double *[9], double *[3], double *[6], double *[9])
+// restraints of one call as per-particle lists in input order, on the device
+static bool upload_restraints(int parnum, int rstnum, const int rstpart[], double *rstlin[9], double *rstang[9])
 {
-  if (rstnum > 0) fail(PG_ERR_UNSUPPORTED, "restrain_velocities: RESTRAIN is not supported");
+  PgDev &d = G.d;
+  const size_t P = parnum, R = rstnum;
+  std::vector<int> first(P + 1, 0), list(std::max<size_t>(1, R));
+  for (size_t q = 0; q < R; q ++)
+  {
+    if (rstpart[q] < 0 || rstpart[q] >= parnum) { fail(PG_ERR_ARGUMENT, "restraint particle out of range"); return false; }
+    first[rstpart[q] + 1] ++;
+  }
+  for (size_t p = 0; p < P; p ++) first[p+1] += first[p];
+  std::vector<int> fill(first.begin(), first.end() - 1);
+  for (size_t q = 0; q < R; q ++) list[fill[rstpart[q]] ++] = (int)q;
+  bool ok = up(d.rst_first, first.data(), P + 1) && up(d.rst_list, list.data(), list.size());
+  for (int k = 0; ok && k < 9; k ++) ok = up(d.rstlin[k], rstlin[k], R) && up(d.rstang[k], rstang[k], R);
+  return ok;
 }
 
-void restrain_forces(int, int rstnum, int[], double *[9], double *[9], double *[3], double *[3])
+// ---------------------------------------------------------------- restrain (restrain.ispc:137-154)
+void restrain_velocities(int, int rstnum, int rstpart[], double *rstlin[9], double *rstang[9], double *linear[3],
+                         double *angular[6], double *rotation[9])
 {
-  if (rstnum > 0) fail(PG_ERR_UNSUPPORTED, "restrain_forces: RESTRAIN is not supported");
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "restrain_velocities";
+  if (rstnum <= 0 || !ready()) return;
+  int parnum = 0;
+  for (int q = 0; q < rstnum; q ++) parnum = std::max(parnum, rstpart[q] + 1);
+  PgDev &d = G.d;
+  const size_t P = parnum;
+  bool ok = upload_restraints(parnum, rstnum, rstpart, rstlin, rstang);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.linear[k], linear[k], P);
+  for (int k = 0; ok && k < 6; k ++) ok = up(d.angular[k], angular[k], P);
+  for (int k = 0; ok && k < 9; k ++) ok = up(d.rotation[k], rotation[k], P);
+  if (!ok) return;
+  PgDev v = view();
+  v.parnum = parnum;
+  v.rstnum = rstnum;
+  pg_launch_restrain_velocities(v, G.st);
+  G.launches += 1;
+  for (int k = 0; ok && k < 3; k ++) ok = down(linear[k], d.linear[k], P);
+  for (int k = 0; ok && k < 6; k ++) ok = down(angular[k], d.angular[k], P);
+  if (ok) finish("restrain_velocities");
+}
+
+void restrain_forces(int, int rstnum, int rstpart[], double *rstlin[9], double *rstang[9], double *force[3],
+                     double *torque[3])
+{
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "restrain_forces";
+  if (rstnum <= 0 || !ready()) return;
+  int parnum = 0;
+  for (int q = 0; q < rstnum; q ++) parnum = std::max(parnum, rstpart[q] + 1);
+  PgDev &d = G.d;
+  const size_t P = parnum;
+  bool ok = upload_restraints(parnum, rstnum, rstpart, rstlin, rstang);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.force[k], force[k], P) && up(d.torque[k], torque[k], P);
+  if (!ok) return;
+  PgDev v = view();
+  v.parnum = parnum;
+  v.rstnum = rstnum;
+  pg_launch_restrain_forces(v, G.st);
+  G.launches += 1;
+  for (int k = 0; ok && k < 3; k ++) ok = down(force[k], d.force[k], P) && down(torque[k], d.torque[k], P);
+  if (ok) finish("restrain_forces");
 }
 
 // ---------------------------------------------------------------- adaptive_timestep (parmec.ispc:397-420)

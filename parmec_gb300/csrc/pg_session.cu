@@ -268,6 +268,27 @@ int upload_static(pg_session *s, const pg_scene *sc)
     TRY(h2d(s, d.linkind, sc->linkind, sc->prsnum));
     TRY(h2d(s, d.angkind, sc->angkind, sc->prsnum));
   }
+  // restraints per particle, in input order
+  {
+    const int R = std::max(sc->rstnum, 0);
+    std::vector<int> first(P + 1, 0), list(std::max(1, R));
+    for (int q = 0; q < R; q ++) first[sc->rstpart[q] + 1] ++;
+    for (int p = 0; p < P; p ++) first[p+1] += first[p];
+    std::vector<int> fill(first.begin(), first.end() - 1);
+    for (int q = 0; q < R; q ++) list[fill[sc->rstpart[q]] ++] = q;
+    d.rstnum = R;
+    TRY(dalloc(s, &d.rst_first, P + 1));
+    TRY(dalloc(s, &d.rst_list, list.size()));
+    TRY(h2d(s, d.rst_first, first.data(), P + 1));
+    TRY(h2d(s, d.rst_list, list.data(), list.size()));
+    for (int k = 0; k < 9; k ++)
+    {
+      TRY(dalloc(s, &d.rstlin[k], std::max(1, R)));
+      TRY(dalloc(s, &d.rstang[k], std::max(1, R)));
+      TRY(h2d(s, d.rstlin[k], sc->rstlin[k], R));
+      TRY(h2d(s, d.rstang[k], sc->rstang[k], R));
+    }
+  }
   // spring flush events: the single-task springs_task order (forces.ispc:1207-1412)
   {
     std::vector<int> first;
@@ -1014,7 +1035,7 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if (form == PG_FORM_MIXED)
   {
     // scope of the mixed form: spheres centred on their particle, obstacles, analytical particles
-    if (sc->sprnum || sc->nodnum || sc->facnum) return PG_ERR_UNSUPPORTED;
+    if (sc->sprnum || sc->nodnum || sc->facnum || sc->rstnum > 0) return PG_ERR_UNSUPPORTED;
     for (int e = 0; e < sc->ellnum; e ++)
     {
       int p = sc->part[e];
@@ -1203,6 +1224,16 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   CK(cudaGetLastError());
   // the host tables are pageable: keep them alive until the copies finished
   CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_restrain_velocities(pg_session *s)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  if (s->d.rstnum == 0) return PG_OK;
+  pg_launch_restrain_velocities(s->d, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
   return PG_OK;
 }
 

@@ -68,6 +68,12 @@ struct PgDev
   double *sad[17];          // [sprnum] |z| (3), |stiffness|, |damping|, krot of the j arm (6) and of the k arm (6)
   double *sbig_ad;          // [nbig][11] long-run partials: kact (3), krot (6), kmax, emax
 
+  // ---- restraints (restrain.ispc:30-133), CSR per particle in input order
+  int rstnum;
+  int *rst_first;           // [parnum+1]
+  int *rst_list;            // restraint indices
+  double *rstlin[9], *rstang[9];   // [rstnum] three orthonormal directions each (zero rows unused)
+
   // ---- prescribed motion
   int *prs_first;           // [parnum+1] CSR of prescriptions per particle
   int *prs_list;            // prescription indices in input order

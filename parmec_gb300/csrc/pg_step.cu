@@ -971,6 +971,75 @@ __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
 // force and torque sums (the tail of forces(), forces.ispc:453-596) and
 // INT_DYNAMICS starts from the force and torque arrays (dynamics(),
 // dynamics.ispc:30-169, with h = step and h-bar = (step + step1)/2).
+// RESTRAIN (restrain.ispc:30-133): v loses its components along the three
+// direction rows of restraint q, in order (SUBMUL (v, DOT (v, l), l, v))
+__device__ __forceinline__ void restrain_vec(double *v, double *const dir[9], int q)
+{
+  for (int k = 0; k < 3; k ++)
+  {
+    const double l[3] = {dir[3*k][q], dir[3*k+1][q], dir[3*k+2][q]};
+    const double dt = dot3(v, l);
+    v[0] = v[0] - dt*l[0];
+    v[1] = v[1] - dt*l[1];
+    v[2] = v[2] - dt*l[2];
+  }
+}
+
+// restrain_velocities_task (restrain.ispc:30-90) for one particle's
+// restraints in input order: linear, spatial angular, and referential angular
+// velocity against the directions taken to the body frame (L^T a)
+__global__ void k_restrain_velocities(PgDev d, const int *first, const int *list, int parnum)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= parnum || first[j] == first[j+1]) return;
+  double v[3] = {d.linear[0][j], d.linear[1][j], d.linear[2][j]};
+  double O[3] = {d.angular[0][j], d.angular[1][j], d.angular[2][j]};
+  double o[3] = {d.angular[3][j], d.angular[4][j], d.angular[5][j]};
+  double L[9];
+  for (int c = 0; c < 9; c ++) L[c] = d.rotation[c][j];
+  for (int rr = first[j]; rr < first[j+1]; rr ++)
+  {
+    const int q = list[rr];
+    restrain_vec(v, d.rstlin, q);
+    restrain_vec(o, d.rstang, q);
+    double A[3][3];
+    for (int k = 0; k < 3; k ++)
+    {
+      const double a[3] = {d.rstang[3*k][q], d.rstang[3*k+1][q], d.rstang[3*k+2][q]};
+      tvmul(L, a, A[k]);
+    }
+    for (int k = 0; k < 3; k ++)
+    {
+      const double dt = dot3(O, A[k]);
+      O[0] = O[0] - dt*A[k][0];
+      O[1] = O[1] - dt*A[k][1];
+      O[2] = O[2] - dt*A[k][2];
+    }
+  }
+  for (int c = 0; c < 3; c ++)
+  {
+    d.linear[c][j] = v[c];
+    d.angular[c][j] = O[c];
+    d.angular[3+c][j] = o[c];
+  }
+}
+
+// restrain_forces_task (restrain.ispc:93-133) over the force arrays, for the
+// drop-in export
+__global__ void k_restrain_forces(PgDev d, const int *first, const int *list, int parnum)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= parnum || first[j] == first[j+1]) return;
+  double f[3] = {d.force[0][j], d.force[1][j], d.force[2][j]};
+  double t[3] = {d.torque[0][j], d.torque[1][j], d.torque[2][j]};
+  for (int rr = first[j]; rr < first[j+1]; rr ++)
+  {
+    restrain_vec(f, d.rstlin, list[rr]);
+    restrain_vec(t, d.rstang, list[rr]);
+  }
+  for (int c = 0; c < 3; c ++) { d.force[c][j] = f[c]; d.torque[c][j] = t[c]; }
+}
+
 // With adaptive stepping the step is split at the step choice:
 // INT_FORCES_ADAPT ends with the force sums and the complete stiffness terms
 // of every particle (forces.ispc:453-596, 1207-1412); INT_DYN_FUSED starts
@@ -1162,6 +1231,16 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       d.torque[0][i] = T[0]; d.torque[1][i] = T[1]; d.torque[2][i] = T[2];
       return;
     }
+
+    // restrain_forces (restrain.ispc:93-133), in input order; the drop-in
+    // entry points run it as its own export
+    if (FUSED && d.rstnum)
+      for (int rr = d.rst_first[i]; rr < d.rst_first[i+1]; rr ++)
+      {
+        const int q = d.rst_list[rr];
+        restrain_vec(F, d.rstlin, q);
+        restrain_vec(T, d.rstang, q);
+      }
 
     // prescribe_acceleration (input.cpp:4247-4341); the drop-in entry points
     // leave prescribed motion to the host, as parmec.cpp does
@@ -1437,6 +1516,16 @@ void pg_launch_adapt_step(const PgDev &d, cudaStream_t s)
 void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s)
 {
   if (d.parnum) k_integrate<INT_DYN_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+}
+
+void pg_launch_restrain_velocities(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum && d.rstnum) k_restrain_velocities<<<nblk(d.parnum), TPB, 0, s>>>(d, d.rst_first, d.rst_list, d.parnum);
+}
+
+void pg_launch_restrain_forces(const PgDev &d, cudaStream_t s)
+{
+  if (d.parnum && d.rstnum) k_restrain_forces<<<nblk(d.parnum), TPB, 0, s>>>(d, d.rst_first, d.rst_list, d.parnum);
 }
 
 void pg_launch_mesh(const PgDev &d, cudaStream_t s)

@@ -263,6 +263,8 @@ def run_dem(m, duration, step, interval, engine, adaptive=0.0):
     else:
         step0 = m.curstep
     eng.invert_inertia()
+    if m.restraints:
+        eng.restrain_velocities()                       # parmec.cpp:2413
 
     if 0.0 < adaptive <= 1.0:
         return _run_adaptive(m, eng, duration, step0, adaptive, dt, dt_func, dt_tms, t_start)

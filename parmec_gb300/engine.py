@@ -8,7 +8,7 @@ from . import abi
 
 def _counts(m):
     return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
-            len(m.prescribe), len(m.pairs), len(m.lcurves))
+            len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints))
 
 
 class GpuEngine:
@@ -93,6 +93,9 @@ class GpuEngine:
 
     def invert_inertia(self):
         abi.check(self.lib.pg_session_invert_inertia(self.sess), "pg_session_invert_inertia")
+
+    def restrain_velocities(self):
+        abi.check(self.lib.pg_session_restrain_velocities(self.sess), "pg_session_restrain_velocities")
 
     def run(self, tab, step):
         abi.check(self.lib.pg_session_run(self.sess, ctypes.byref(tab), step), "pg_session_run")

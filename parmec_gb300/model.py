@@ -107,6 +107,7 @@ class Model:
         self.tms = []                       # TSERIES objects
         self.lcurves = []                   # time series copied as lookup curves (sproffset)
         self.prescribe = []                 # dicts: part, lin, ang, linkind, angkind
+        self.restraints = []                # (part, lin[9], ang[9]) orthonormal direction rows
         self.gravity = [0.0, 0.0, 0.0]
         self.gravfunc = [None, None, None]
         self.gravtms = [-1, -1, -1]
@@ -430,6 +431,50 @@ class Model:
                                "linkind": 0 if kind[0] == "v" else 1,
                                "angkind": 0 if kind[1] == "v" else 1})
 
+    # ------------------------------------------------------------- RESTRAIN
+    def restrain(self, parnum, linear=None, angular=None):
+        """RESTRAIN (input.cpp:2458-2644): up to three linear and three angular
+        directions along which the particle's motion is removed; lists of 3, 6
+        or 9 numbers, orthonormalised in order (Gram-Schmidt, NORMALIZE divides
+        by the length as macros.h:427 does)."""
+        if not (0 <= parnum < self.parnum):
+            raise ValueError("'parnum' out of range")
+        for v, n in ((linear, "linear"), (angular, "angular")):
+            if v is not None and not isinstance(v, list):
+                raise TypeError(f"'{n}' must be a list")
+
+        def dirs(v, what):
+            if v is None:
+                return [0.0] * 9
+            if len(v) not in (3, 6, 9):
+                raise ValueError(f"Invalid {what} constrained directions list")
+            d = [[0.0] * 3 for _ in range(3)]
+            for k in range(len(v) // 3):
+                d[k] = [float(v[3 * k]), float(v[3 * k + 1]), float(v[3 * k + 2])]
+
+            def normalize(a):
+                ln = math.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2])
+                return [a[0] / ln, a[1] / ln, a[2] / ln]
+
+            def submul(a, dot, b):
+                return [a[0] - dot * b[0], a[1] - dot * b[1], a[2] - dot * b[2]]
+
+            def dot3(a, b):
+                return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+            d[0] = normalize(d[0])
+            if len(v) >= 6:
+                d[1] = normalize(submul(d[1], dot3(d[0], d[1]), d[0]))
+            if len(v) == 9:
+                d[2] = submul(d[2], dot3(d[0], d[2]), d[0])
+                d[2] = normalize(submul(d[2], dot3(d[1], d[2]), d[1]))
+            return d[0] + d[1] + d[2]
+        lin = dirs(linear, "linear")
+        ang = dirs(angular, "angular")
+        if linear is None and angular is None:
+            return
+        self._touch()
+        self.restraints.append((int(parnum), lin, ang))
+
     # ------------------------------------------------------------- VELOCITY
     def velocity(self, parnum, linear=None, angular=None):
         """VELOCITY (input.cpp:2798-2837)."""
@@ -670,6 +715,15 @@ class Model:
         s.linkind = abi.iptr(linkind)
         s.angkind = abi.iptr(angkind)
         s.compat = self.compat
+        nr = len(self.restraints)
+        rstpart = np.array([r[0] for r in self.restraints] or [0], dtype=np.int32)
+        rstlin = np.ascontiguousarray(np.array([r[1] for r in self.restraints] or [[0.0] * 9], dtype=np.float64).T)
+        rstang = np.ascontiguousarray(np.array([r[2] for r in self.restraints] or [[0.0] * 9], dtype=np.float64).T)
+        keep += [rstpart, rstlin, rstang]
+        s.rstnum = nr
+        s.rstpart = abi.iptr(rstpart)
+        s.rstlin = abi.rows(rstlin, 9)
+        s.rstang = abi.rows(rstang, 9)
         nscene = getattr(self, "nscene", 0)
         if nscene:
             s.nscene = nscene

@@ -68,6 +68,10 @@ def PRESCRIBE(parnum, linear=None, angular=None, kind=None):
     return _model.prescribe_motion(parnum, linear, angular, kind)
 
 
+def RESTRAIN(parnum, linear=None, angular=None):
+    return _model.restrain(parnum, linear, angular)
+
+
 def VELOCITY(parnum, linear=None, angular=None):
     return _model.velocity(parnum, linear, angular)
 
@@ -105,7 +109,7 @@ def DEM(duration, step, interval=None, prefix=None, adaptive=0.0):
 
 
 COMMANDS = ["RESET", "TSERIES", "MATERIAL", "SPHERE", "MESH", "ANALYTICAL", "OBSTACLE", "GRANULAR",
-            "SPRING", "PRESCRIBE", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
+            "SPRING", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
             "ARGV", "DEM"]
 
 

@@ -125,7 +125,7 @@ def dem(lib, host, duration, step, adaptive=0.0):
     else:
         step0 = m.curstep
     lib.invert_inertia(ntasks, s.parnum, s.inertia, s.inverse, s.mass, s.invm)
-    lib.restrain_velocities(ntasks, 0, NULL, NULL, NULL, s.linear, s.angular, s.rotation)
+    lib.restrain_velocities(ntasks, s.rstnum, s.rstpart, s.rstlin, s.rstang, s.linear, s.angular, s.rotation)
     tree = lib.partitioning_create(ntasks, s.ellnum - ellcon, s.center)
     kmax = np.zeros(max(1, s.parnum))
     emax = np.zeros(max(1, s.parnum))
@@ -172,7 +172,7 @@ def dem(lib, host, duration, step, adaptive=0.0):
                                           abi.dptr(emax), krot_p, D(step0), D(adaptive))
         else:
             step1 = step0
-        lib.restrain_forces(ntasks, 0, NULL, NULL, NULL, s.force, s.torque)
+        lib.restrain_forces(ntasks, s.rstnum, s.rstpart, s.rstlin, s.rstang, s.force, s.torque)
         _prescribe_acceleration(m, tab, k, s)
         lib.dynamics(ntasks, ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), s.parnum, s.angular,
                      s.linear, s.rotation, s.position, s.inertia, s.inverse, s.mass, s.invm, abi.dptr(damping),

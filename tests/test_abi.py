@@ -115,7 +115,7 @@ def test_ispc_header_compiles(tmp_path, lang):
 
 
 def test_ispc_host_side_functions_without_gpu():
-    """Allocation, grid handles and the no-op restraint paths need no device."""
+    """Allocation, grid handles and the empty restraint call need no device."""
     from parmec_gb300 import abi
     lib = abi.load_library()
     lib.aligned_real_alloc.restype = ctypes.POINTER(ctypes.c_double)
@@ -137,6 +137,16 @@ def test_ispc_host_side_functions_without_gpu():
     lib.pg_compat_exit_on_error(0)
     lib.restrain_forces(1, 0, None, None, None, None, None)
     assert lib.pg_compat_status() == 0
-    lib.restrain_forces(1, 2, None, None, None, None, None)
-    assert lib.pg_compat_status() == abi.PG_ERR_UNSUPPORTED
+    # a restraint runs on the device: without one the call reports PG_ERR_CUDA
+    import numpy as np
+    part = np.zeros(1, dtype=np.int32)
+    dirs = np.zeros((9, 1))
+    dirs[2, 0] = 1.0
+    vec = np.ones((3, 1))
+    lib.restrain_forces(1, 1, abi.iptr(part), abi.rows(dirs, 9), abi.rows(np.zeros((9, 1)), 9),
+                        abi.rows(vec, 3), abi.rows(vec.copy(), 3))
+    st = lib.pg_compat_status()
+    assert st in (abi.PG_OK, abi.PG_ERR_CUDA)
+    if st == abi.PG_OK:
+        assert list(vec[:, 0]) == [1.0, 1.0, 0.0]
     lib.pg_compat_exit_on_error(1)

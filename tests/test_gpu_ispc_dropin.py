@@ -109,8 +109,7 @@ def test_dropin_springs_and_prescribe(gpu_lib, oracle_lib):
 
 
 def test_dropin_unsupported_cases_report(gpu_lib):
-    """Ellipsoids and restraints report PG_ERR_UNSUPPORTED instead of running."""
-    from parmec_gb300 import abi
+    """Ellipsoids report PG_ERR_UNSUPPORTED instead of running."""
     lib = ispc_loop.library()
     lib.pg_compat_exit_on_error(0)
     m, dt = make_collision_scene(n_side=2)
@@ -119,8 +118,7 @@ def test_dropin_unsupported_cases_report(gpu_lib):
     with pytest.raises(RuntimeError):
         ispc_loop.dem(lib, host, 2.5 * dt, dt)
     host.close()
-    lib.restrain_velocities(1, 1, None, None, None, None, None, None)
-    assert lib.pg_compat_status() == abi.PG_ERR_UNSUPPORTED
+    assert lib.pg_compat_status() == 0               # read (and cleared) by ispc_loop.dem's raise
     lib.pg_compat_exit_on_error(1)
 
 
@@ -161,3 +159,18 @@ def test_dropin_adaptive_springs_bitwise(gpu_lib, oracle_lib):
     assert mc.curstep == mo.curstep and mc.curtime == mo.curtime
     assert_bitwise(mc, mo)
     host.close()
+
+
+def test_dropin_restraints_bitwise(gpu_lib, oracle_lib):
+    """restrain_velocities at the DEM call and restrain_forces every step
+    through the exports, beside the oracle's restraints."""
+    from oracle.pyoracle import OracleEngine
+
+    def make():
+        m, dt = make_collision_scene(n_side=3)
+        m.restrain(0, linear=[0.0, 0.0, 1.0])
+        m.restrain(1, linear=[1.0, 1.0, 0.0, 0.0, 1.0, 1.0], angular=[0.0, 0.0, 1.0])
+        m.restrain(1, angular=[1.0, 0.0, 0.0])
+        m.restrain(5, angular=[1.0, 0.2, 0.0, 0.0, 1.0, 0.3, 0.1, 0.0, 1.0])
+        return m, dt
+    run_both(make, 30)
