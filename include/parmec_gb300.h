@@ -168,7 +168,30 @@ typedef struct pg_scene {
   int *rstpart;
   double *rstlin[9];
   double *rstang[9];
+
+  /* spring failure rules (UNSPRING, input.cpp:2083-2295; unspring_task,
+   * forces.ispc:2058-2127).  Spring lists hold spring ids (creation order),
+   * mapped to sorted positions through sprmap.  unent uses the reference's
+   * history codes (PG_HIS_STROKE .. PG_HIS_FF), unop its operator codes.
+   * nfreq counts failures down and is written back by pg_session_download;
+   * unaction is -1 (zero force) or an lcurve index (unload curve). */
+  int unsprnum;
+  int *tsprings, *tspridx;   /* tested springs, CSR over rules */
+  int *msprings, *mspridx;   /* monitored springs: fail when the rule fires */
+  int *activate, *actidx;    /* springs switched on when the rule fires */
+  double *unlim[2];          /* lower, upper limit */
+  int *unent, *unop, *unabs, *nsteps, *nfreq, *unaction;
+  int *sprmap;               /* [sprnum] spring id -> sorted position */
 } pg_scene;
+
+/* UNSPRING entity and operator codes (constants.h:43-46, 70) */
+#define PG_HIS_STROKE 25
+#define PG_HIS_F      26
+#define PG_HIS_SF     27
+#define PG_HIS_FF     28
+#define PG_OP_SUM     0
+#define PG_OP_MAX     1
+#define PG_OP_MIN     2
 
 /*
  * Per-step host inputs of the time loop.  The reference evaluates these through
@@ -185,6 +208,7 @@ typedef struct pg_steptab {
   const double *prs_ang;   /* [n][prsnum][3] at curtime */
   const double *obs_ang;   /* [n][obsnum][3] at curtime+step */
   const double *obs_lin;   /* [n][obsnum][3] at curtime+step */
+  int stepnum;             /* DEM calls made before this one (stepnum, parmec.cpp:2523; UNSPRING's nsteps) */
 } pg_steptab;
 
 /* ======================================================================== */

@@ -1650,6 +1650,48 @@ void springs_all(pg_scene *s, double step, double time, const AdTerms *at)
   spring_flush(s, out, ad, at);
 }
 
+/* ---------------- forces.ispc:2058-2127 unspring_task (rules in order) ------
+ * A rule is checked when stepnum % nsteps == 0 and it has not fired: the SUM,
+ * MIN or MAX of an entity (optionally absolute) over its tested springs; a
+ * value outside (unlim[0], unlim[1]) counts nfreq down, and at zero the
+ * monitored springs take the rule's action (-1: zero force, >= 0: unload
+ * along an lcurve) and the activated springs switch on (-3). */
+void unspring_all(pg_scene *s, int stepnum)
+{
+  for (int i = 0; i < s->unsprnum; i ++)
+  {
+    if (stepnum % s->nsteps[i]) continue;
+    if (s->nfreq[i] == 0) continue;
+    const int op = s->unop[i];
+    double result = op == PG_OP_MIN ? 1.7976931348623157e308 : (op == PG_OP_MAX ? -1.7976931348623157e308 : 0.0);
+    for (int j = s->tspridx[i]; j < s->tspridx[i+1]; j ++)
+    {
+      const int q = s->sprmap[s->tsprings[j]];
+      double value = 0.0;
+      switch (s->unent[i])
+      {
+        case PG_HIS_STROKE: value = s->stroke[0][q]; break;
+        case PG_HIS_F: value = s->sprfrc[0][q]; break;
+        case PG_HIS_SF: value = s->sprfrc[1][q]; break;
+        case PG_HIS_FF: value = s->sprfrc[2][q]; break;
+      }
+      if (s->unabs[i]) value = std::fabs(value);
+      if (op == PG_OP_MIN) result = value < result ? value : result;
+      else if (op == PG_OP_MAX) result = value > result ? value : result;
+      else result += value;
+    }
+    if (result < s->unlim[0][i] || result > s->unlim[1][i])
+    {
+      s->nfreq[i] --;
+      if (s->nfreq[i] == 0)
+      {
+        for (int j = s->mspridx[i]; j < s->mspridx[i+1]; j ++) s->unspring[s->sprmap[s->msprings[j]]] = s->unaction[i];
+        for (int j = s->actidx[i]; j < s->actidx[i+1]; j ++) s->unspring[s->sprmap[s->activate[j]]] = -3;
+      }
+    }
+  }
+}
+
 /* ---------------- restrain.ispc:30-133 ------------------------------------ */
 /* v loses its components along the three direction rows of restraint q, in order */
 inline void restrain_vec(double *v, double *const dir[9], int q)
@@ -1894,6 +1936,7 @@ double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double 
 #pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
   for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, grav, at);
   if (s->sprnum) springs_all(s, step0, curtime, at);
+  if (s->unsprnum) unspring_all(s, tab->stepnum);
 
   /* adaptive_timestep (parmec.ispc:397-420) */
   double step1 = step0;

@@ -70,6 +70,10 @@ class PgScene(ctypes.Structure):
         ("pscene", I), ("tscene", I), ("oscene", I), ("sactive", I),
         ("rstnum", ctypes.c_int),
         ("rstpart", I), ("rstlin", D * 9), ("rstang", D * 9),
+        ("unsprnum", ctypes.c_int),
+        ("tsprings", I), ("tspridx", I), ("msprings", I), ("mspridx", I), ("activate", I), ("actidx", I),
+        ("unlim", D * 2), ("unent", I), ("unop", I), ("unabs", I), ("nsteps", I), ("nfreq", I),
+        ("unaction", I), ("sprmap", I),
     ]
 
 
@@ -79,6 +83,7 @@ class PgStepTab(ctypes.Structure):
         ("nsteps", ctypes.c_int),
         ("curtime", D), ("gravity", D), ("damping", D),
         ("prs_lin", D), ("prs_ang", D), ("obs_ang", D), ("obs_lin", D),
+        ("stepnum", ctypes.c_int),
     ]
 
 

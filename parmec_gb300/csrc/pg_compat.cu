@@ -649,7 +649,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
             double *rotation[9], double *position[3], double *inertia[9], double *inverse[9], double mass[], double invm[],
             double obspnt[], double obslin[], double obsang[], int[], double *[PG_ISPC_NMAT],
             int pairnum, int pairs[], int ikind[], double *iparam[PG_ISPC_NIPARAM],
-            double step, int sprnum, int sprtype[], int unspring[], int[],
+            double step, int sprnum, int sprtype[], int unspring[], int sprmap[],
             int *sprpart[2], double *sprpnt[2][6], double *spring[2], int spridx[],
             double *dashpot[2], int dashidx[], double *unload[2], int unidx[],
             double *yield[2], double *sprdir[6], int sprflg[], int sproffset[],
@@ -659,15 +659,15 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
             double *[3], double *[3], double *[3][2], int *[3], double *[3][2], int *[3],
             int[], double *[3], double *[3], double *[3], double *[3], double *[3],
             double *force[3], double *torque[3], double *kact[3], double kmax[],
-            double emax[], double *krot[6], int adaptive, int unsprnum, int[],
-            int[], int[], int[], double *[2], int[], int[], int[], int[], int[], int[],
-            int[], int[], int, double time)
+            double emax[], double *krot[6], int adaptive, int unsprnum, int tsprings[],
+            int tspridx[], int msprings[], int mspridx[], double *unlim[2], int unent[], int unop[], int unabs[],
+            int nsteps[], int nfreq[], int unaction[], int activate[], int actidx[], int stepnum, double time)
 {
   std::lock_guard<std::mutex> g(M);
   G.fn = "forces";
   if (parnum <= 0 || !ready()) return;
   if (trqsprnum > 0) { fail(PG_ERR_UNSUPPORTED, "forces: TORSION_SPRING is not supported"); return; }
-  if (unsprnum > 0) { fail(PG_ERR_UNSUPPORTED, "forces: UNSPRING is not supported"); return; }
+  if (unsprnum > 0 && (sprnum <= 0 || !sprmap)) { fail(PG_ERR_ARGUMENT, "forces: UNSPRING needs the springs and sprmap"); return; }
   if (adaptive && (!kact || !kmax || !emax || !krot))
   {
     fail(PG_ERR_ARGUMENT, "forces: adaptive stepping needs kact, kmax, emax and krot");
@@ -738,6 +738,26 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     if (adaptive) ok = ok && grow(d.sbig_ad, 11 * std::max<size_t>(1, big.size()));
     d.nbig = (int)big.size();
   }
+  const int U = S ? std::max(unsprnum, 0) : 0;
+  if (U)
+  {
+    // spring failure rules, spring ids mapped to sorted positions
+    auto mapped = [&](const int *ids, const int *idx, int *&dl, int *&di) -> bool {
+      const int n = idx[U];
+      std::vector<int> pos(std::max(1, n));
+      for (int j = 0; j < n; j ++)
+      {
+        if (ids[j] < 0 || ids[j] >= sprnum) { fail(PG_ERR_ARGUMENT, "UNSPRING spring index out of range"); return false; }
+        pos[j] = sprmap[ids[j]];
+      }
+      return up(dl, pos.data(), pos.size()) && up(di, idx, (size_t)U + 1);
+    };
+    ok = ok && mapped(tsprings, tspridx, d.u_t, d.u_tidx) && mapped(msprings, mspridx, d.u_m, d.u_midx) &&
+         mapped(activate, actidx, d.u_a, d.u_aidx);
+    for (int k = 0; ok && k < 2; k ++) ok = up(d.unlim[k], unlim[k], U);
+    ok = ok && up(d.unent, unent, U) && up(d.unop, unop, U) && up(d.unabs, unabs, U) && up(d.unsteps, nsteps, U) &&
+         up(d.nfreq, nfreq, U) && up(d.unaction, unaction, U) && up(d.ustep, &stepnum, 1);
+  }
   if (!ok) return;
   PgDev v = view();
   v.parnum = parnum;
@@ -747,9 +767,11 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   v.prsnum = 0;
   if (!contacts) { v.ellnum = 0; v.pell = nullptr; }
   if (adaptive) v.hs = G.hs;
+  v.unsprnum = U;
   pg_launch_contacts(v, G.st, step);
   pg_launch_springs(v, G.st, step);
   if (S) pg_launch_spring_runs(v, G.st);
+  if (U) { pg_launch_unspring(v, G.st); G.launches += 1; }
   if (adaptive) pg_launch_force_sums_adapt(v, G.st);
   else pg_launch_force_sums(v, G.st);
   G.launches += (v.ellnum ? 1 : 0) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 2 : 1) : 0) + 1;
@@ -769,6 +791,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
            down(sprsdsp[k], d.sprsdsp[k], S);
     for (int k = 0; ok && k < 2; k ++) ok = down(yield[k], d.yield[k], S);
     ok = ok && down(unspring, d.unspring, S) && down(sprflg, d.sprflg, S);
+    if (U) ok = ok && down(nfreq, d.nfreq, U);
   }
   if (!ok) return;
   // zero_force_torque_kmax (forces.ispc) also clears kmax and emax

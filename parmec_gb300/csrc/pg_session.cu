@@ -289,6 +289,40 @@ int upload_static(pg_session *s, const pg_scene *sc)
       TRY(h2d(s, d.rstang[k], sc->rstang[k], R));
     }
   }
+  // spring failure rules, spring ids mapped to sorted positions
+  {
+    const int U = std::max(sc->unsprnum, 0);
+    d.unsprnum = U;
+    auto mapped = [&](const int *ids, const int *idx, int **dl, int **di) -> int {
+      const int n = U ? idx[U] : 0;
+      std::vector<int> pos(std::max(1, n)), ix(U + 1, 0);
+      for (int j = 0; j < n; j ++)
+      {
+        const int id = ids[j];
+        if (id < 0 || id >= sc->sprnum) return PG_ERR_ARGUMENT;
+        pos[j] = sc->sprmap ? sc->sprmap[id] : id;
+      }
+      for (int i = 0; i <= U; i ++) ix[i] = U ? idx[i] : 0;
+      TRY(dalloc(s, dl, pos.size()));
+      TRY(dalloc(s, di, ix.size()));
+      TRY(h2d(s, *dl, pos.data(), pos.size()));
+      TRY(h2d(s, *di, ix.data(), ix.size()));
+      CK(cudaStreamSynchronize(s->stream));
+      return PG_OK;
+    };
+    TRY(mapped(sc->tsprings, sc->tspridx, &d.u_t, &d.u_tidx));
+    TRY(mapped(sc->msprings, sc->mspridx, &d.u_m, &d.u_midx));
+    TRY(mapped(sc->activate, sc->actidx, &d.u_a, &d.u_aidx));
+    const size_t n = std::max(1, U);
+    for (int k = 0; k < 2; k ++) { TRY(dalloc(s, &d.unlim[k], n)); TRY(h2d(s, d.unlim[k], sc->unlim[k], U)); }
+    TRY(dalloc(s, &d.unent, n)); TRY(h2d(s, d.unent, sc->unent, U));
+    TRY(dalloc(s, &d.unop, n)); TRY(h2d(s, d.unop, sc->unop, U));
+    TRY(dalloc(s, &d.unabs, n)); TRY(h2d(s, d.unabs, sc->unabs, U));
+    TRY(dalloc(s, &d.unsteps, n)); TRY(h2d(s, d.unsteps, sc->nsteps, U));
+    TRY(dalloc(s, &d.nfreq, n)); TRY(h2d(s, d.nfreq, sc->nfreq, U));
+    TRY(dalloc(s, &d.unaction, n)); TRY(h2d(s, d.unaction, sc->unaction, U));
+    TRY(dalloc(s, &d.ustep, 1));
+  }
   // spring flush events: the single-task springs_task order (forces.ispc:1207-1412)
   {
     std::vector<int> first;
@@ -886,6 +920,7 @@ void enqueue_step(pg_session *s, double step)
   pg_launch_contacts(d, s->stream, step);
   pg_launch_springs(d, s->stream, step);
   pg_launch_spring_runs(d, s->stream);
+  pg_launch_unspring(d, s->stream);
   pg_launch_integrate(d, s->stream, step);
   pg_launch_mesh(d, s->stream);
   pg_launch_obstacles_row(d, s->stream, step);
@@ -971,6 +1006,7 @@ void enqueue_step_adaptive(pg_session *s)
   pg_launch_contacts(d, s->stream, 0.0);
   pg_launch_springs(d, s->stream, 0.0);
   pg_launch_spring_runs(d, s->stream);
+  pg_launch_unspring(d, s->stream);
   pg_launch_force_sums_adapt(d, s->stream);
   pg_launch_adapt_step(d, s->stream);
   pg_launch_dynamics_fused(d, s->stream);
@@ -983,7 +1019,7 @@ int adaptive_kernel_count(const PgDev &d)
 {
   int n = pg_rebuild_kernel_count(d) + 2 + 1;     // excite, select, tail
   if (d.ellnum) n += 1;
-  if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0);
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0) + (d.unsprnum ? 1 : 0);
   if (d.parnum) n += 3;                           // force sums, minimum, dynamics
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;
@@ -1011,6 +1047,7 @@ int upload_tables(pg_session *s, const pg_steptab *tab, int n)
   TRY(put(d.t_obs_ang, tab->obs_ang, s->obs_stride));
   TRY(put(d.t_obs_lin, tab->obs_lin, s->obs_stride));
   CK(cudaMemsetAsync(d.stepno, 0, sizeof(int), s->stream));
+  if (d.ustep) TRY(h2d(s, d.ustep, &tab->stepnum, 1));
   return PG_OK;
 }
 
@@ -1117,6 +1154,7 @@ int pg_session_upload(pg_session *s, const pg_scene *sc)
   if (s->d.compat != sc->compat) drop_graph(s);
   s->d.compat = sc->compat;
   TRY(upload_all(s, sc));
+  if (sc->unsprnum == s->d.unsprnum && s->d.unsprnum) TRY(h2d(s, s->d.nfreq, sc->nfreq, s->d.unsprnum));
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
@@ -1194,7 +1232,12 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       if (d.form == PG_FORM_MIXED) pg_launch_contacts_mx(d, s->stream, step);
       else pg_launch_contacts(d, s->stream, step);
       CK(cudaEventRecord(ev[2], s->stream));
-      if (d.form != PG_FORM_MIXED) { pg_launch_springs(d, s->stream, step); pg_launch_spring_runs(d, s->stream); }
+      if (d.form != PG_FORM_MIXED)
+      {
+        pg_launch_springs(d, s->stream, step);
+        pg_launch_spring_runs(d, s->stream);
+        pg_launch_unspring(d, s->stream);
+      }
       CK(cudaEventRecord(ev[3], s->stream));
       if (d.form == PG_FORM_MIXED) pg_launch_integrate_mx(d, s->stream, step);
       else pg_launch_integrate(d, s->stream, step);
@@ -1284,6 +1327,7 @@ int pg_session_download(pg_session *s, pg_scene *sc)
   TRY(download_ranges(s, sc, full_ranges(d)));
   for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->nodes[k], d.nodes[k], N));
   TRY(d2h(s, sc->unspring, d.unspring, S));
+  if (d.unsprnum && sc->nfreq && sc->unsprnum == d.unsprnum) TRY(d2h(s, sc->nfreq, d.nfreq, d.unsprnum));
   for (int a = 0; a < 2; a ++)
     for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->sprpnt[a][k], d.sprpnt[6*a+k], S));
   for (int k = 0; k < 2; k ++) TRY(d2h(s, sc->yield[k], d.yield[k], S));

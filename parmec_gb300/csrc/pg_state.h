@@ -74,6 +74,14 @@ struct PgDev
   int *rst_list;            // restraint indices
   double *rstlin[9], *rstang[9];   // [rstnum] three orthonormal directions each (zero rows unused)
 
+  // ---- spring failure rules (unspring_task, forces.ispc:2058-2127); spring
+  // lists hold sorted positions
+  int unsprnum;
+  int *u_t, *u_tidx, *u_m, *u_midx, *u_a, *u_aidx;
+  double *unlim[2];
+  int *unent, *unop, *unabs, *unsteps, *nfreq, *unaction;
+  int *ustep;               // stepnum of the running DEM call (from the step table)
+
   // ---- prescribed motion
   int *prs_first;           // [parnum+1] CSR of prescriptions per particle
   int *prs_list;            // prescription indices in input order

@@ -1395,6 +1395,52 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
   if (FUSED && d.ellnum) flag_rebuild(d, need);
 }
 
+// ---------------------------------------------------------------- spring failures
+// unspring_task (forces.ispc:2058-2127): the rules in order, by one thread, so
+// that rules sharing springs act in the reference's sequence.  A rule is
+// checked when stepnum % nsteps == 0 and nfreq > 0: the SUM/MIN/MAX of the
+// entity over its tested springs, leaving (lower, upper) counts nfreq down,
+// and at zero the monitored springs take the rule's action and the
+// activated ones switch on.
+__global__ void k_unspring(PgDev d)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int stepnum = *d.ustep;
+  for (int i = 0; i < d.unsprnum; i ++)
+  {
+    if (stepnum % d.unsteps[i]) continue;
+    if (d.nfreq[i] == 0) continue;
+    const int op = d.unop[i];
+    double result = op == PG_OP_MIN ? 1.7976931348623157e308 : (op == PG_OP_MAX ? -1.7976931348623157e308 : 0.0);
+    for (int j = d.u_tidx[i]; j < d.u_tidx[i+1]; j ++)
+    {
+      const int q = d.u_t[j];
+      double value = 0.0;
+      switch (d.unent[i])
+      {
+        case PG_HIS_STROKE: value = d.stroke[0][q]; break;
+        case PG_HIS_F: value = d.sprfrc[0][q]; break;
+        case PG_HIS_SF: value = d.sprfrc[1][q]; break;
+        case PG_HIS_FF: value = d.sprfrc[2][q]; break;
+      }
+      if (d.unabs[i]) value = fabs(value);
+      if (op == PG_OP_MIN) result = value < result ? value : result;
+      else if (op == PG_OP_MAX) result = value > result ? value : result;
+      else result += value;
+    }
+    if (result < d.unlim[0][i] || result > d.unlim[1][i])
+    {
+      const int nf = d.nfreq[i] - 1;
+      d.nfreq[i] = nf;
+      if (nf == 0)
+      {
+        for (int j = d.u_midx[i]; j < d.u_midx[i+1]; j ++) d.unspring[d.u_m[j]] = d.unaction[i];
+        for (int j = d.u_aidx[i]; j < d.u_aidx[i+1]; j ++) d.unspring[d.u_a[j]] = -3;
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------- adaptive step
 // adaptive_timestep (parmec.ispc:397-420): every particle's critical step
 // from its stiffness terms, reduced to the smallest.  Non-negative doubles
@@ -1481,6 +1527,11 @@ void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
   else k_springs<false><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
 }
 
+void pg_launch_unspring(const PgDev &d, cudaStream_t s)
+{
+  if (d.sprnum && d.unsprnum) k_unspring<<<1, 32, 0, s>>>(d);
+}
+
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
 {
   if (d.sprnum && d.nbig > 0) k_spring_runs<<<d.nbig, RUN_THREADS, 0, s>>>(d);
@@ -1553,7 +1604,7 @@ int pg_step_kernel_count(const PgDev &d)
 {
   int n = 2;                                   // excite, tail
   if (d.ellnum) n += 1;                        // contacts
-  if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0);
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0) + (d.unsprnum ? 1 : 0);
   if (d.parnum) n += 1;                        // integrate
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;

@@ -71,6 +71,7 @@ class StepTables:
 
     def __init__(self, m, times, step, dt, dt_func, dt_tms):
         n = len(times)
+        self.stepnum = m.stepnum
         npr = len(m.prescribe)
         self.curtime = np.array(times, dtype=np.float64)
         self.gravity = np.zeros((n, 3))
@@ -131,6 +132,7 @@ class StepTables:
                         self.obs_ang, self.obs_lin)]
         t.curtime, t.gravity, t.damping, t.prs_lin, t.prs_ang, t.obs_ang, t.obs_lin = \
             [abi.dptr(v) for v in self._views]
+        t.stepnum = self.stepnum
         return t
 
 

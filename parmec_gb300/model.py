@@ -108,6 +108,8 @@ class Model:
         self.lcurves = []                   # time series copied as lookup curves (sproffset)
         self.prescribe = []                 # dicts: part, lin, ang, linkind, angkind
         self.restraints = []                # (part, lin[9], ang[9]) orthonormal direction rows
+        self.unsprings = []                 # UNSPRING rules (dicts); failure countdowns in unspring_nfreq
+        self.unspring_nfreq = np.zeros(1, dtype=np.int32)
         self.gravity = [0.0, 0.0, 0.0]
         self.gravfunc = [None, None, None]
         self.gravtms = [-1, -1, -1]
@@ -475,6 +477,78 @@ class Model:
         self._touch()
         self.restraints.append((int(parnum), lin, ang))
 
+    # ------------------------------------------------------------- UNSPRING
+    UNSPRING_ENTITIES = {"STROKE": 25, "F": 26, "SF": 27, "FF": 28}   # HIS_* codes (constants.h:43-46)
+    UNSPRING_OPERATORS = {"SUM": 0, "MAX": 1, "MIN": 2}             # OP_* codes (constants.h:70)
+
+    def unspring(self, tsprings, msprings, limits, entity=None, operator=None, abs=False, nsteps=1, nfreq=1,
+                 unload=-1, activate=None):
+        """UNSPRING (input.cpp:2083-2295): when the SUM/MIN/MAX of an entity over
+        the tested springs leaves 'limits' nfreq times (checked every nsteps),
+        the monitored springs fail (zero force, or unload along a TSERIES
+        curve) and the springs in 'activate' switch on; returns the rule index."""
+        from .springs import _lcurve_from_time_series
+        if not isinstance(tsprings, list) or not isinstance(msprings, list):
+            raise TypeError("'tsprings' and 'msprings' must be lists")
+        if not (isinstance(limits, tuple) and len(limits) == 2):
+            raise TypeError("'limits' must be a tuple of size 2")
+        if activate is not None and not isinstance(activate, list):
+            raise TypeError("'activate' must be a list")
+        if not isinstance(abs, bool):
+            raise TypeError("'abs' must be a boolean")
+        if nsteps <= 0 or nfreq <= 0:
+            raise ValueError("'nsteps' and 'nfreq' must be positive")
+        if unload < -1 or unload >= len(self.tms):
+            raise ValueError("unload TSERIES index is out of range")
+        if unload >= 0:
+            pts = self.tms[unload].points
+            for j in range(1, len(pts)):
+                if (pts[j][1] - pts[j - 1][1]) / (pts[j][0] - pts[j - 1][0]) <= 0.0:
+                    raise ValueError("Unloading curve must be monotonically increasing")
+        S = self.S
+        for j in tsprings:
+            if not (0 <= j < self.sprnum):
+                raise ValueError("tsprings SPRING index is out of range")
+        for j in msprings:
+            if not (0 <= j < self.sprnum):
+                raise ValueError("msprings SPRING index is out of range")
+            u = S.unspring[S.sprmap[j]]
+            if u == -2:
+                raise ValueError(f"in msprings, spring index {j} already in use by an earlier UNSPRING call")
+            if u == -1:
+                raise ValueError(f"in msprings, trying to use an inactive SPRING with index {j}")
+        lim = []
+        for k, v in enumerate(limits):
+            if v is None:
+                lim.append(-REAL_MAX if k == 0 else REAL_MAX)
+            elif isinstance(v, (int, float)) and not isinstance(v, bool):
+                lim.append(float(v))
+            else:
+                raise ValueError("Invalid lower limit" if k == 0 else "Invalid upper limit")
+        if lim[0] >= lim[1]:
+            raise ValueError("Lower limit >= upper limit")
+        ent = self.UNSPRING_ENTITIES.get(entity if entity is not None else "SF")
+        if ent is None:
+            raise ValueError("Invalid entity")
+        op = self.UNSPRING_OPERATORS.get(operator if operator is not None else "SUM")
+        if op is None:
+            raise ValueError("Invalid operator")
+        for j in (activate or []):
+            if not (0 <= j < self.sprnum) or S.unspring[S.sprmap[j]] != -1:
+                raise ValueError(f"in activate list: SPRING {j} is already active")
+        self._touch()
+        for j in msprings:
+            S.unspring[S.sprmap[j]] = -2                # in use by UNSPRING
+        action = unload if unload < 0 else _lcurve_from_time_series(self, unload)
+        self.unsprings.append({"tsprings": [int(j) for j in tsprings], "msprings": [int(j) for j in msprings],
+                               "activate": [int(j) for j in (activate or [])], "limits": lim, "entity": ent,
+                               "op": op, "abs": 1 if abs else 0, "nsteps": int(nsteps), "action": int(action)})
+        nf = np.zeros(len(self.unsprings), dtype=np.int32)
+        nf[:len(self.unsprings) - 1] = self.unspring_nfreq[:len(self.unsprings) - 1]
+        nf[-1] = int(nfreq)
+        self.unspring_nfreq = nf
+        return len(self.unsprings) - 1
+
     # ------------------------------------------------------------- VELOCITY
     def velocity(self, parnum, linear=None, angular=None):
         """VELOCITY (input.cpp:2798-2837)."""
@@ -724,6 +798,34 @@ class Model:
         s.rstpart = abi.iptr(rstpart)
         s.rstlin = abi.rows(rstlin, 9)
         s.rstang = abi.rows(rstang, 9)
+        U = self.unsprings
+
+        def csr(key):
+            idx = np.zeros(len(U) + 1, dtype=np.int32)
+            for i, u in enumerate(U):
+                idx[i + 1] = idx[i] + len(u[key])
+            lst = np.array([j for u in U for j in u[key]] or [0], dtype=np.int32)
+            return lst, idx
+        tspr, tidx = csr("tsprings")
+        mspr, midx = csr("msprings")
+        act, aidx = csr("activate")
+        unlim = np.ascontiguousarray(np.array([u["limits"] for u in U] or [[0.0, 0.0]], dtype=np.float64).T)
+        unent = np.array([u["entity"] for u in U] or [0], dtype=np.int32)
+        unop = np.array([u["op"] for u in U] or [0], dtype=np.int32)
+        unabs = np.array([u["abs"] for u in U] or [0], dtype=np.int32)
+        nsteps = np.array([u["nsteps"] for u in U] or [1], dtype=np.int32)
+        unaction = np.array([u["action"] for u in U] or [0], dtype=np.int32)
+        if len(self.unspring_nfreq) < max(1, len(U)):
+            self.unspring_nfreq = np.zeros(max(1, len(U)), dtype=np.int32)
+        keep += [tspr, tidx, mspr, midx, act, aidx, unlim, unent, unop, unabs, nsteps, unaction]
+        s.unsprnum = len(U)
+        s.tsprings, s.tspridx = abi.iptr(tspr), abi.iptr(tidx)
+        s.msprings, s.mspridx = abi.iptr(mspr), abi.iptr(midx)
+        s.activate, s.actidx = abi.iptr(act), abi.iptr(aidx)
+        s.unlim = abi.rows(unlim, 2)
+        s.unent, s.unop, s.unabs = abi.iptr(unent), abi.iptr(unop), abi.iptr(unabs)
+        s.nsteps, s.nfreq, s.unaction = abi.iptr(nsteps), abi.iptr(self.unspring_nfreq), abi.iptr(unaction)
+        s.sprmap = abi.iptr(S.sprmap)
         nscene = getattr(self, "nscene", 0)
         if nscene:
             s.nscene = nscene

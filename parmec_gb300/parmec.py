@@ -68,6 +68,11 @@ def PRESCRIBE(parnum, linear=None, angular=None, kind=None):
     return _model.prescribe_motion(parnum, linear, angular, kind)
 
 
+def UNSPRING(tsprings, msprings, limits, entity=None, operator=None, abs=False, nsteps=1, nfreq=1, unload=-1,
+             activate=None):
+    return _model.unspring(tsprings, msprings, limits, entity, operator, abs, nsteps, nfreq, unload, activate)
+
+
 def RESTRAIN(parnum, linear=None, angular=None):
     return _model.restrain(parnum, linear, angular)
 
@@ -109,7 +114,7 @@ def DEM(duration, step, interval=None, prefix=None, adaptive=0.0):
 
 
 COMMANDS = ["RESET", "TSERIES", "MATERIAL", "SPHERE", "MESH", "ANALYTICAL", "OBSTACLE", "GRANULAR",
-            "SPRING", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
+            "SPRING", "UNSPRING", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
             "ARGV", "DEM"]
 
 

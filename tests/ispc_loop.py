@@ -160,13 +160,14 @@ def dem(lib, host, duration, step, adaptive=0.0):
         lib.forces(ntasks, ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), s.parnum,
                    s.angular, s.linear, s.rotation, s.position, s.inertia, s.inverse, s.mass, s.invm,
                    s.obspnt, s.obslin, s.obsang, s.parmat, NULL, s.pairnum, s.pairs, s.ikind, s.iparam,
-                   D(step0), s.sprnum, s.sprtype, s.unspring, NULL, s.sprpart, s.sprpnt, s.spring, s.spridx,
+                   D(step0), s.sprnum, s.sprtype, s.unspring, s.sprmap, s.sprpart, s.sprpnt, s.spring, s.spridx,
                    s.dashpot, s.dashidx, s.unload, s.unidx, s.yield_, s.sprdir, s.sprflg, s.sproffset,
                    s.sprfric, s.sprkskn, s.sprsdsp, s.stroke0, s.stroke, s.sprfrc, s.lcurve, s.lcidx,
                    abi.dptr(gravity), 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL,
                    NULL, NULL, s.force, s.torque, kact_p if adapt else NULL, abi.dptr(kmax), abi.dptr(emax),
-                   krot_p if adapt else NULL, 1 if adapt else 0, 0,
-                   NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, m.stepnum, D(t))
+                   krot_p if adapt else NULL, 1 if adapt else 0, s.unsprnum,
+                   s.tsprings, s.tspridx, s.msprings, s.mspridx, s.unlim, s.unent, s.unop, s.unabs, s.nsteps,
+                   s.nfreq, s.unaction, s.activate, s.actidx, m.stepnum, D(t))
         if adapt:
             step1 = lib.adaptive_timestep(ntasks, s.parnum, s.mass, s.inertia, kact_p, abi.dptr(kmax),
                                           abi.dptr(emax), krot_p, D(step0), D(adaptive))
