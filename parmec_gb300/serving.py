@@ -217,6 +217,7 @@ class Server:
             t.prs_ang = np.zeros((n, 1, 3))
             t.obs_ang = np.zeros((n, 1, 3))
             t.obs_lin = np.zeros((n, 1, 3))
+            t.stepnum = 0
             self._zero_tab = (n, t)
         return self._zero_tab[1].ctab(0, n)
 
