@@ -726,6 +726,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
       ok = up(d.sprsdsp[k], sprsdsp[k], S) && up(d.stroke[k], stroke[k], S) && up(d.sprfrc[k], sprfrc[k], S);
     int nlc = 0;
     for (size_t i = 0; sproffset && i < S; i ++) nlc = std::max(nlc, sproffset[i] + 1);
+    for (int i = 0; unaction && i < unsprnum; i ++) nlc = std::max(nlc, unaction[i] + 1);
     const size_t nl = (nlc > 0 && lcidx) ? (size_t)lcidx[nlc] : 0;
     ok = ok && up(d.lcidx, nlc > 0 ? lcidx : nullptr, (size_t)nlc + 1);
     for (int k = 0; ok && k < 2; k ++) ok = up(d.lcurve[k], nlc > 0 ? lcurve[k] : nullptr, nl);

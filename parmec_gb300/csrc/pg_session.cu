@@ -518,9 +518,13 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
       TRY(h2d(s, d.sprfrc[k], sc->sprfrc[k], S));
     }
     TRY(h2d(s, d.stroke0, sc->stroke0, S));
+    // lookup curves used as stroke offsets (sproffset) and as UNSPRING unload
+    // curves (unaction >= 0)
     int nlc = 0;
     if (sc->sproffset)
       for (size_t i = 0; i < S; i ++) nlc = std::max(nlc, sc->sproffset[i] + 1);
+    if (sc->unaction)
+      for (int i = 0; i < sc->unsprnum; i ++) nlc = std::max(nlc, sc->unaction[i] + 1);
     size_t nl = (nlc > 0 && sc->lcidx) ? (size_t)sc->lcidx[nlc] : 0;
     if (!d.lcidx)
     {
