@@ -433,6 +433,27 @@ class Model:
                                "linkind": 0 if kind[0] == "v" else 1,
                                "angkind": 0 if kind[1] == "v" else 1})
 
+    # ------------------------------------------------------------------ EQM
+    def eqm(self, part1, point1, part2=-1, point2=None, direction=None):
+        """EQM (input.cpp:2336-2381): the equivalent point mass of one particle
+        (or of a particle pair) at the given points, along 'direction' or, with
+        none, from the smallest eigenvalue of the inverse mass matrix
+        (eqm, parmec.ispc:423-482)."""
+        from .springs import _eqm
+        if not (0 <= part1 < self.parnum):
+            raise ValueError("'part1' out of range")
+        for v, n in ((point1, "point1"), (point2, "point2"), (direction, "direction")):
+            if v is not None and not _is_tuple(v, 3):
+                raise TypeError(f"'{n}' must be a tuple of size 3")
+        if part2 >= self.parnum:
+            raise ValueError("Particle number 'part2' is out of range")
+        if part2 >= 0 and point2 is None:
+            raise TypeError("'point2' must be a tuple of size 3")
+        p1 = [float(x) for x in point1]
+        p2 = [float(x) for x in point2] if part2 >= 0 else [0.0, 0.0, 0.0]
+        d = [float(x) for x in direction] if direction is not None else [0.0, 0.0, 0.0]
+        return float(_eqm(self, part1, p1, part2 if part2 >= 0 else -1, p2, d))
+
     # ------------------------------------------------------------- RESTRAIN
     def restrain(self, parnum, linear=None, angular=None):
         """RESTRAIN (input.cpp:2458-2644): up to three linear and three angular

@@ -73,6 +73,10 @@ def UNSPRING(tsprings, msprings, limits, entity=None, operator=None, abs=False, 
     return _model.unspring(tsprings, msprings, limits, entity, operator, abs, nsteps, nfreq, unload, activate)
 
 
+def EQM(part1, point1, part2=-1, point2=None, direction=None):
+    return _model.eqm(part1, point1, part2, point2, direction)
+
+
 def RESTRAIN(parnum, linear=None, angular=None):
     return _model.restrain(parnum, linear, angular)
 
@@ -114,7 +118,7 @@ def DEM(duration, step, interval=None, prefix=None, adaptive=0.0):
 
 
 COMMANDS = ["RESET", "TSERIES", "MATERIAL", "SPHERE", "MESH", "ANALYTICAL", "OBSTACLE", "GRANULAR",
-            "SPRING", "UNSPRING", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
+            "SPRING", "UNSPRING", "EQM", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
             "ARGV", "DEM"]
 
 

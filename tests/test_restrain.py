@@ -87,3 +87,21 @@ def test_gpu_restraints_bitwise(gpu_lib, oracle_lib):
         mg.dem(25 * dt, dt, interval=1e9, engine=GpuEngine() if k == 0 else mg.last_engine)
         mo.dem(25 * dt, dt, interval=1e9, engine=OracleEngine() if k == 0 else mo.last_engine)
         assert_bitwise(mg, mo)
+
+
+def test_eqm_command():
+    """EQM (input.cpp:2336-2381): a sphere at its centre along a direction has
+    its own mass; two equal spheres in series half of it; off-centre points
+    lower the mass through the rotational term."""
+    from parmec_gb300 import parmec as P
+    P.RESET()
+    mat = P.MATERIAL(1000.0, 1e9, 0.25)
+    a = P.SPHERE((0.0, 0.0, 0.0), 0.1, mat, 1)
+    b = P.SPHERE((1.0, 0.0, 0.0), 0.1, mat, 1)
+    m = P.model().P.mass[a]
+    assert abs(P.EQM(a, (0.0, 0.0, 0.0), direction=(1.0, 0.0, 0.0)) - m) <= 1e-12 * m
+    assert abs(P.EQM(a, (0.0, 0.0, 0.0), b, (1.0, 0.0, 0.0), (1.0, 0.0, 0.0)) - 0.5 * m) <= 1e-12 * m
+    assert P.EQM(a, (0.0, 0.1, 0.0), direction=(1.0, 0.0, 0.0)) < m
+    with pytest.raises(ValueError):
+        P.EQM(5, (0.0, 0.0, 0.0))
+    P.RESET()
