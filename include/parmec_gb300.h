@@ -240,6 +240,14 @@ int pg_session_invert_inertia(pg_session *s);
  * with a fixed step (adaptive == 0).  Asynchronous on the session stream. */
 int pg_session_run(pg_session *s, const pg_steptab *tab, double step);
 
+/* Copy the state of particles idx[0..n) (velocities, rotation, position,
+ * force, torque) or of springs idx[0..n) (sorted positions: current points,
+ * stroke, forces) into the host arrays of 'scene' at the same indices, through
+ * one device gather and one small copy.  What output_history reads
+ * (output.cpp:5143-5533) without downloading every array. */
+int pg_session_download_particles(pg_session *s, pg_scene *scene, const int *idx, int n);
+int pg_session_download_springs(pg_session *s, pg_scene *scene, const int *idx, int n);
+
 /* restrain_velocities (restrain.ispc:137) of the scene's restraints: the
  * DEM prologue calls it once after invert_inertia (parmec.cpp:2413).  The
  * per-step restrain_forces runs inside the step. */

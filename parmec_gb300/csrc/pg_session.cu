@@ -45,6 +45,9 @@ struct pg_session
   double *hs_buf = nullptr;
   int adapt_ready = 0, hrec_cap = 0, sbig_ad_cap = 0;
   int exc_any = 0;                         // some scene has a device excitation
+  // partial downloads: device scratch for indices, column table and rows
+  int *g_idx = nullptr; const double **g_cols = nullptr; double *g_out = nullptr;
+  size_t g_idx_cap = 0, g_cols_cap = 0, g_out_cap = 0;
   // persistent fused step (mixed form): launch shape, autotuner state and
   // the captured graph of one chunk of fstep_chunk steps
   int fused = 0, tune = 0, tuned = 0, warmed = 0;
@@ -1272,6 +1275,80 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   // the host tables are pageable: keep them alive until the copies finished
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
+}
+
+} // extern "C"
+
+namespace {
+
+template <typename T>
+int grow_scratch(pg_session *s, T *&p, size_t &cap, size_t n)
+{
+  if (n <= cap) return PG_OK;
+  CK(cudaStreamSynchronize(s->stream));
+  release(s, (void *)p);
+  p = nullptr;
+  cap = 0;
+  TRY(dalloc(s, &p, n));
+  cap = n;
+  return PG_OK;
+}
+
+// rows idx[0..n) of ncols device arrays into the matching host arrays
+int gather_download(pg_session *s, const double *const *dcols, double *const *hcols, int ncols, const int *idx, int n,
+                    int limit)
+{
+  if (n <= 0 || ncols <= 0) return PG_OK;
+  for (int j = 0; j < n; j ++) if (idx[j] < 0 || idx[j] >= limit) return PG_ERR_ARGUMENT;
+  TRY(grow_scratch(s, s->g_idx, s->g_idx_cap, (size_t)n));
+  TRY(grow_scratch(s, s->g_cols, s->g_cols_cap, (size_t)ncols));
+  TRY(grow_scratch(s, s->g_out, s->g_out_cap, (size_t)n * ncols));
+  std::vector<double> out((size_t)n * ncols);
+  TRY(h2d(s, s->g_idx, idx, (size_t)n));
+  TRY(h2d(s, s->g_cols, dcols, (size_t)ncols));
+  pg_launch_gather(s->g_cols, ncols, s->g_idx, n, s->g_out, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  TRY(d2h(s, out.data(), s->g_out, out.size()));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int c = 0; c < ncols; c ++)
+    if (hcols[c]) for (int j = 0; j < n; j ++) hcols[c][idx[j]] = out[(size_t)c * n + j];
+  return PG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int pg_session_download_particles(pg_session *s, pg_scene *sc, const int *idx, int n)
+{
+  if (!s || !sc || n < 0 || (n > 0 && !idx)) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream);
+  const double *dc[30];
+  double *hc[30];
+  int c = 0;
+  for (int k = 0; k < 6; k ++) { dc[c] = d.angular[k]; hc[c ++] = sc->angular[k]; }
+  for (int k = 0; k < 3; k ++) { dc[c] = d.linear[k]; hc[c ++] = sc->linear[k]; }
+  for (int k = 0; k < 9; k ++) { dc[c] = d.rotation[k]; hc[c ++] = sc->rotation[k]; }
+  for (int k = 0; k < 6; k ++) { dc[c] = d.position[k]; hc[c ++] = sc->position[k]; }
+  for (int k = 0; k < 3; k ++) { dc[c] = d.force[k]; hc[c ++] = sc->force[k]; }
+  for (int k = 0; k < 3; k ++) { dc[c] = d.torque[k]; hc[c ++] = sc->torque[k]; }
+  return gather_download(s, dc, hc, c, idx, n, d.parnum);
+}
+
+int pg_session_download_springs(pg_session *s, pg_scene *sc, const int *idx, int n)
+{
+  if (!s || !sc || n < 0 || (n > 0 && !idx)) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  const double *dc[12];
+  double *hc[12];
+  int c = 0;
+  for (int a = 0; a < 2; a ++)
+    for (int k = 0; k < 3; k ++) { dc[c] = d.sprpnt[6*a+k]; hc[c ++] = sc->sprpnt[a][k]; }
+  for (int k = 0; k < 3; k ++) { dc[c] = d.stroke[k]; hc[c ++] = sc->stroke[k]; }
+  for (int k = 0; k < 3; k ++) { dc[c] = d.sprfrc[k]; hc[c ++] = sc->sprfrc[k]; }
+  return gather_download(s, dc, hc, c, idx, n, d.sprnum);
 }
 
 int pg_session_restrain_velocities(pg_session *s)

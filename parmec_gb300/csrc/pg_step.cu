@@ -1395,6 +1395,17 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
   if (FUSED && d.ellnum) flag_rebuild(d, need);
 }
 
+// ---------------------------------------------------------------- partial downloads
+// out[c*n + j] = cols[c][idx[j]]: the rows a HISTORY sample reads, gathered
+// into one buffer so that one small copy replaces a download of every array
+__global__ void k_gather(const double *const *cols, int ncols, const int *idx, int n, double *out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncols * n) return;
+  const int c = t / n, j = t - c * n;
+  out[t] = cols[c][idx[j]];
+}
+
 // ---------------------------------------------------------------- spring failures
 // unspring_task (forces.ispc:2058-2127): the rules in order, by one thread, so
 // that rules sharing springs act in the reference's sequence.  A rule is
@@ -1525,6 +1536,11 @@ void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
   if (!d.sprnum) return;
   if (d.hs) k_springs<true><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
   else k_springs<false><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
+}
+
+void pg_launch_gather(const double *const *cols, int ncols, const int *idx, int n, double *out, cudaStream_t s)
+{
+  if (ncols > 0 && n > 0) k_gather<<<nblk(ncols * n), TPB, 0, s>>>(cols, ncols, idx, n, out);
 }
 
 void pg_launch_unspring(const PgDev &d, cudaStream_t s)

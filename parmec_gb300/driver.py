@@ -150,6 +150,32 @@ def step_times(curtime, duration, step):
     return times, ct
 
 
+SPRING_ENTITIES = ("LENGTH", "STROKE", "F", "SF", "FF")
+
+
+def history_rows(m):
+    """(particles, spring positions) that the histories read, sorted and unique."""
+    parts, sprs = set(), set()
+    for h in m.histories:
+        if h["ent"] == "TIME":
+            continue
+        if h["ent"] in SPRING_ENTITIES and h["point"] is None:
+            sprs.update(int(m.S.sprmap[k]) for k in h["list"])
+        else:
+            parts.update(int(k) for k in h["list"])
+    return sorted(parts), sorted(sprs)
+
+
+def download_for_history(m, eng):
+    """What the next history sample reads: a gather of its rows where the
+    engine has one, else a full download."""
+    if hasattr(eng, "download_rows"):
+        p, s = history_rows(m)
+        eng.download_rows(p, s)
+    else:
+        eng.download()
+
+
 def sample_history(m, t):
     """output_history (output.cpp:5143-5533) for list sources."""
     P, S = m.P, m.S
@@ -284,7 +310,7 @@ def run_dem(m, duration, step, interval, engine, adaptive=0.0):
     b = 0
     for k in cuts:
         eng.run(tabs.ctab(b, k + 1), step0)
-        eng.download()
+        download_for_history(m, eng)
         sample_history(m, times[k])
         m.curtime_history += tabs.interval[k, 1]
         b = k + 1
@@ -310,7 +336,7 @@ def _run_adaptive(m, eng, duration, step0, adaptive, dt, dt_func, dt_tms, t_star
         tabs = StepTables(m, [ct], step0, dtl, dt_func, dt_tms)
         step1 = float(eng.run_adaptive(tabs.ctab(0, 1), step0, adaptive)[0])
         if ct >= m.curtime_history + tabs.interval[0, 1]:
-            eng.download()
+            download_for_history(m, eng)
             sample_history(m, ct)
             m.curtime_history += tabs.interval[0, 1]
         inc = 0.5 * (step0 + step1)

@@ -114,6 +114,17 @@ class GpuEngine:
         abi.check(self.lib.pg_session_download(self.sess, ctypes.byref(self.scene)), "pg_session_download")
         self.model.pull_obstacles()
 
+    def download_rows(self, particles, springs):
+        """Only the given particles' and springs' state (pg_session_download_particles/_springs)."""
+        if len(particles):
+            idx = np.ascontiguousarray(particles, dtype=np.int32)
+            abi.check(self.lib.pg_session_download_particles(self.sess, ctypes.byref(self.scene), abi.iptr(idx),
+                                                             len(idx)), "pg_session_download_particles")
+        if len(springs):
+            idx = np.ascontiguousarray(springs, dtype=np.int32)
+            abi.check(self.lib.pg_session_download_springs(self.sess, ctypes.byref(self.scene), abi.iptr(idx),
+                                                           len(idx)), "pg_session_download_springs")
+
     def fused_config(self):
         """(threads per block, blocks, tuned, graph) of the fused step kernel."""
         out = (ctypes.c_int * 4)()

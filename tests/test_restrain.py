@@ -105,3 +105,4 @@ def test_eqm_command():
     with pytest.raises(ValueError):
         P.EQM(5, (0.0, 0.0, 0.0))
     P.RESET()
+
