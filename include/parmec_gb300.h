@@ -182,6 +182,20 @@ typedef struct pg_scene {
   double *unlim[2];          /* lower, upper limit */
   int *unent, *unop, *unabs, *nsteps, *nfreq, *unaction;
   int *sprmap;               /* [sprnum] spring id -> sorted position */
+
+  /* torsion springs (TORSION_SPRING, input.cpp:1791-2080), sorted by
+   * (part0, part1) (sort_trqspr, parmec.cpp:1968); krpy/drpy are per-axis
+   * (roll, pitch, yaw) lookup tables, a one-entry damper table is a critical
+   * damping ratio; trqcone holds the TRQCONE_* flags (constants.h:66-68);
+   * zdir1/xdir1, the angles and the moments are state written by the step */
+  int trqsprnum;
+  int *trqsprpart[2];
+  double *trqzdir0[3], *trqxdir0[3];
+  double *krpy[3][2]; int *krpyidx[3];
+  double *drpy[3][2]; int *drpyidx[3];
+  int *trqcone;
+  double *trqzdir1[3], *trqxdir1[3];
+  double *trqrpy[3], *trqrpytot[3], *trqrpyspr[3];
 } pg_scene;
 
 /* UNSPRING entity and operator codes (constants.h:43-46, 70) */

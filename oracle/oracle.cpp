@@ -1650,6 +1650,227 @@ void springs_all(pg_scene *s, double step, double time, const AdTerms *at)
   spring_flush(s, out, ad, at);
 }
 
+/* ---------------- forces.ispc:1415-2057 trqspr_task (single task) ---------
+ * Per torsion spring: the current frame rot1j = Lj [x0 y0 z0]; roll, pitch
+ * and yaw rates from the relative spatial angular velocity; the angles
+ * integrate those rates; spring torques from the angle lookups (or from the
+ * combined angle of a cone), dampers by lookup or by a critical damping ratio
+ * against the local equivalent inertia; the torque rot1j * (roll, pitch,
+ * yaw) is added to part0 and subtracted from part1 run by run, as the
+ * translational springs are.  Position taken: the pitch-yaw cone's pitch
+ * damper reads the pitch ratio (the reference reads the roll entry,
+ * forces.ispc:1823). */
+void trqspr_all(pg_scene *s, double step, const AdTerms *at)
+{
+  const int S = s->trqsprnum;
+  std::vector<double> out(3 * (size_t)std::max(S, 1), 0.0), kk(3 * (size_t)std::max(S, 1), 0.0);
+  for (int i = 0; i < S; i ++)
+  {
+    const int j = s->trqsprpart[0][i], k = s->trqsprpart[1][i];
+    double oj[3] = {s->angular[3][j], s->angular[4][j], s->angular[5][j]}, Lj[9];
+    for (int c = 0; c < 9; c ++) Lj[c] = s->rotation[c][j];
+    double zdir0[3] = {s->trqzdir0[0][i], s->trqzdir0[1][i], s->trqzdir0[2][i]};
+    double xdir0[3] = {s->trqxdir0[0][i], s->trqxdir0[1][i], s->trqxdir0[2][i]};
+    double ydir0[3] = {zdir0[1]*xdir0[2] - zdir0[2]*xdir0[1], zdir0[2]*xdir0[0] - zdir0[0]*xdir0[2],
+                       zdir0[0]*xdir0[1] - zdir0[1]*xdir0[0]};
+    double rot1j[9];
+    NVMUL(Lj, xdir0, rot1j);
+    NVMUL(Lj, ydir0, rot1j+3);
+    NVMUL(Lj, zdir0, rot1j+6);
+    for (int c = 0; c < 3; c ++) { s->trqzdir1[c][i] = rot1j[6+c]; s->trqxdir1[c][i] = rot1j[c]; }
+    double ok[3] = {0.0, 0.0, 0.0};
+    if (k >= 0) { ok[0] = s->angular[3][k]; ok[1] = s->angular[4][k]; ok[2] = s->angular[5][k]; }
+    double ojk[3] = {oj[0]-ok[0], oj[1]-ok[1], oj[2]-ok[2]};
+    const double rolldot = DOT(rot1j, ojk), pitchdot = DOT(rot1j+3, ojk), yawdot = DOT(rot1j+6, ojk);
+    double roll = s->trqrpy[0][i], pitch = s->trqrpy[1][i], yaw = s->trqrpy[2][i];
+    roll += rolldot*step;
+    pitch += pitchdot*step;
+    yaw += yawdot*step;
+    s->trqrpy[0][i] = roll; s->trqrpy[1][i] = pitch; s->trqrpy[2][i] = yaw;
+    int *const kidx[3] = {s->krpyidx[0], s->krpyidx[1], s->krpyidx[2]};
+    int *const didx[3] = {s->drpyidx[0], s->drpyidx[1], s->drpyidx[2]};
+    auto ratio_of = [&](int o) { return didx[o][i]+1 == didx[o][i+1]; };
+    double Ixx = 0.0, Iyy = 0.0, Izz = 0.0;
+    if (ratio_of(0) || ratio_of(1) || ratio_of(2))
+    {
+      double I[9], tmp[9];
+      for (int c = 0; c < 9; c ++) I[c] = s->inverse[c][j];
+      if (k >= 0) for (int c = 0; c < 9; c ++) I[c] += s->inverse[c][k];
+      NTMUL(I, rot1j, tmp);
+      NNMUL(rot1j, tmp, I);
+      INVERT(I, tmp);
+      Ixx = tmp[0]; Iyy = tmp[4]; Izz = tmp[8];
+    }
+    auto spring = [&](int o, double arg, double *kslope) {
+      if (kidx[o][i+1] > kidx[o][i]) return look_up(s->krpy[o], kidx[o][i], kidx[o][i+1], arg, kslope);
+      *kslope = 0.0;
+      return 0.0;
+    };
+    auto damper = [&](int o, int ro, double rate, double kslope, double inertia) {
+      if (ratio_of(o))
+      {
+        const double ratio = s->drpy[ro][0][didx[ro][i]];
+        const double d = - ratio * 2.0 * std::sqrt(std::fabs(kslope) * inertia);
+        return rate * d;
+      }
+      double d;
+      return look_up(s->drpy[o], didx[o][i], didx[o][i+1], rate, &d);
+    };
+    double kroll = 0.0, kpitch = 0.0, kyaw = 0.0;
+    double trqroll = 0.0, trqpitch = 0.0, trqyaw = 0.0, trqrolltot = 0.0, trqpitchtot = 0.0, trqyawtot = 0.0;
+    switch (s->trqcone[i])
+    {
+      case 0:
+      {
+        trqroll = spring(0, roll, &kroll);
+        trqpitch = spring(1, pitch, &kpitch);
+        trqyaw = spring(2, yaw, &kyaw);
+        const double trqrolldot = damper(0, 0, rolldot, kroll, Ixx);
+        const double trqpitchdot = damper(1, 1, pitchdot, kpitch, Iyy);
+        const double trqyawdot = damper(2, 2, yawdot, kyaw, Izz);
+        trqrolltot = trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot);
+        trqpitchtot = trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot);
+        trqyawtot = trqyaw + (trqyaw == 0.0 ? 0.0 : trqyawdot);
+        break;
+      }
+      case 3: /* roll-pitch cone */
+      {
+        const double angle = std::sqrt(roll*roll + pitch*pitch);
+        const double angledot = angle > 0.0 ? (rolldot*roll+pitchdot*pitch)/angle : 0.0;
+        trqroll = spring(0, angle, &kroll);
+        kpitch = kroll;
+        const double trqrolldot = damper(0, 0, angledot, kroll, std::sqrt(Ixx*Ixx + Iyy*Iyy));
+        trqyaw = spring(2, yaw, &kyaw);
+        const double trqyawdot = damper(2, 2, yawdot, kyaw, Izz);
+        trqyawtot = trqyaw + (trqyaw == 0.0 ? 0.0 : trqyawdot);
+        if (angle > 0.)
+        {
+          const double xcoef = roll/angle, ycoef = pitch/angle;
+          trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqpitchtot = ycoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqpitch = trqroll*ycoef;
+          trqroll *= xcoef;
+        }
+        else { trqrolltot = trqpitchtot = 0.0; trqroll = trqpitch = 0.0; }
+        break;
+      }
+      case 5: /* roll-yaw cone */
+      {
+        const double angle = std::sqrt(roll*roll + yaw*yaw);
+        const double angledot = angle > 0.0 ? (rolldot*roll+yawdot*yaw)/angle : 0.0;
+        trqroll = spring(0, angle, &kroll);
+        kyaw = kroll;
+        const double trqrolldot = damper(0, 0, angledot, kroll, std::sqrt(Ixx*Ixx + Izz*Izz));
+        trqpitch = spring(1, pitch, &kpitch);
+        const double trqpitchdot = damper(1, 1, pitchdot, kpitch, Iyy);
+        trqpitchtot = trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot);
+        if (angle > 0.)
+        {
+          const double xcoef = roll/angle, zcoef = yaw/angle;
+          trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqyawtot = zcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqyaw = trqroll*zcoef;
+          trqroll *= xcoef;
+        }
+        else { trqrolltot = trqyawtot = 0.0; trqroll = trqyaw = 0.0; }
+        break;
+      }
+      case 6: /* pitch-yaw cone */
+      {
+        trqroll = spring(0, roll, &kroll);
+        const double trqrolldot = damper(0, 0, rolldot, kroll, Ixx);
+        const double angle = std::sqrt(pitch*pitch + yaw*yaw);
+        const double angledot = angle > 0.0 ? (pitchdot*pitch+yawdot*yaw)/angle : 0.0;
+        trqpitch = spring(1, angle, &kpitch);
+        kyaw = kpitch;
+        const double trqpitchdot = damper(1, 1, angledot, kpitch, std::sqrt(Iyy*Iyy + Izz*Izz));
+        trqrolltot = trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot);
+        if (angle > 0.)
+        {
+          const double ycoef = pitch/angle, zcoef = yaw/angle;
+          trqpitchtot = ycoef*(trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot));
+          trqyawtot = zcoef*(trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot));
+          trqyaw = zcoef*trqpitch;
+          trqpitch *= ycoef;
+        }
+        else { trqpitchtot = trqyawtot = 0.0; trqpitch = trqyaw = 0.0; }
+        break;
+      }
+      case 7: /* roll-pitch-yaw cone */
+      {
+        const double angle = std::sqrt(roll*roll + pitch*pitch + yaw*yaw);
+        const double angledot = angle > 0.0 ? (rolldot*roll+pitchdot*pitch+yawdot*yaw)/angle : 0.0;
+        trqroll = spring(0, angle, &kroll);
+        kpitch = kyaw = kroll;
+        const double trqrolldot = damper(0, 0, angledot, kroll, std::sqrt(Ixx*Ixx + Iyy*Iyy + Izz*Izz));
+        if (angle > 0.)
+        {
+          const double xcoef = roll/angle, ycoef = pitch/angle, zcoef = yaw/angle;
+          trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqpitchtot = ycoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqyawtot = zcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+          trqpitch = ycoef*trqroll;
+          trqyaw = zcoef*trqroll;
+          trqroll *= xcoef;
+        }
+        else { trqrolltot = trqpitchtot = trqyawtot = 0.0; trqroll = trqpitch = trqyaw = 0.0; }
+        break;
+      }
+    }
+    out[3*i+0] = trqrolltot*rot1j[0] + trqpitchtot*rot1j[3] + trqyawtot*rot1j[6];
+    out[3*i+1] = trqrolltot*rot1j[1] + trqpitchtot*rot1j[4] + trqyawtot*rot1j[7];
+    out[3*i+2] = trqrolltot*rot1j[2] + trqpitchtot*rot1j[5] + trqyawtot*rot1j[8];
+    s->trqrpytot[0][i] = trqrolltot; s->trqrpytot[1][i] = trqpitchtot; s->trqrpytot[2][i] = trqyawtot;
+    s->trqrpyspr[0][i] = trqroll; s->trqrpyspr[1][i] = trqpitch; s->trqrpyspr[2][i] = trqyaw;
+    kk[3*i+0] = std::fabs(kroll)*rot1j[0];
+    kk[3*i+1] = std::fabs(kpitch)*rot1j[4];
+    kk[3*i+2] = std::fabs(kyaw)*rot1j[8];
+  }
+  /* flush: runs of equal part0 added, runs of equal part1 subtracted, in
+   * stream order; the first run of a kind starts from zero, later ones from
+   * their first element; the adaptive krot partials start from zero */
+  int j0 = -1, k0 = -1, jb = 0, kb = 0;
+  bool firstj = true, firstk = true;
+  auto flush = [&](int part, int type, int b, int e, bool first) {
+    double acc[3] = {0.0, 0.0, 0.0}, kp[3] = {0.0, 0.0, 0.0};
+    bool started = false;
+    for (int i = b; i < e; i ++)
+    {
+      if (type == 1 && s->trqsprpart[1][i] < 0) continue;
+      for (int c = 0; c < 3; c ++)
+      {
+        acc[c] = (!started && !first) ? out[3*i+c] : acc[c] + out[3*i+c];
+        kp[c] = kp[c] + kk[3*i+c];
+      }
+      started = true;
+    }
+    for (int c = 0; c < 3; c ++)
+    {
+      if (type == 0) s->torque[c][part] += acc[c];
+      else s->torque[c][part] -= acc[c];
+      if (at) at->krot[c][part] += kp[c];
+    }
+  };
+  struct Run { int part, type, b, e, first; long long pos; };
+  std::vector<Run> runs;
+  for (int i = 0; i < S; i ++)
+  {
+    const int j = s->trqsprpart[0][i], k = s->trqsprpart[1][i];
+    if (j0 != j && j0 >= 0) { runs.push_back({j0, 0, jb, i, firstj ? 1 : 0, 2LL*i}); firstj = false; jb = i; }
+    if (j0 < 0) jb = i;
+    if (k >= 0)
+    {
+      if (k0 != k && k0 >= 0) { runs.push_back({k0, 1, kb, i, firstk ? 1 : 0, 2LL*i + 1}); firstk = false; kb = i; }
+      if (k0 < 0) kb = i;
+      k0 = k;
+    }
+    j0 = j;
+  }
+  if (j0 >= 0) runs.push_back({j0, 0, jb, S, firstj ? 1 : 0, 2LL*S});
+  if (k0 >= 0) runs.push_back({k0, 1, kb, S, firstk ? 1 : 0, 2LL*S + 1});
+  for (const Run &r : runs) flush(r.part, r.type, r.b, r.e, r.first != 0);
+}
+
 /* ---------------- forces.ispc:2058-2127 unspring_task (rules in order) ------
  * A rule is checked when stepnum % nsteps == 0 and it has not fired: the SUM,
  * MIN or MAX of an entity (optionally absolute) over its tested springs; a
@@ -1936,6 +2157,7 @@ double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double 
 #pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
   for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, grav, at);
   if (s->sprnum) springs_all(s, step0, curtime, at);
+  if (s->trqsprnum) trqspr_all(s, step0, at);
   if (s->unsprnum) unspring_all(s, tab->stepnum);
 
   /* adaptive_timestep (parmec.ispc:397-420) */

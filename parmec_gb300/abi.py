@@ -74,6 +74,11 @@ class PgScene(ctypes.Structure):
         ("tsprings", I), ("tspridx", I), ("msprings", I), ("mspridx", I), ("activate", I), ("actidx", I),
         ("unlim", D * 2), ("unent", I), ("unop", I), ("unabs", I), ("nsteps", I), ("nfreq", I),
         ("unaction", I), ("sprmap", I),
+        ("trqsprnum", ctypes.c_int),
+        ("trqsprpart", I * 2), ("trqzdir0", D * 3), ("trqxdir0", D * 3),
+        ("krpy", (D * 2) * 3), ("krpyidx", I * 3), ("drpy", (D * 2) * 3), ("drpyidx", I * 3),
+        ("trqcone", I), ("trqzdir1", D * 3), ("trqxdir1", D * 3),
+        ("trqrpy", D * 3), ("trqrpytot", D * 3), ("trqrpyspr", D * 3),
     ]
 
 

@@ -655,9 +655,10 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
             double *yield[2], double *sprdir[6], int sprflg[], int sproffset[],
             double sprfric[], double sprkskn[], double *sprsdsp[3], double stroke0[],
             double *stroke[3], double *sprfrc[3], double *lcurve[2],
-            int lcidx[], double gravity[3], int trqsprnum, int *[2],
-            double *[3], double *[3], double *[3][2], int *[3], double *[3][2], int *[3],
-            int[], double *[3], double *[3], double *[3], double *[3], double *[3],
+            int lcidx[], double gravity[3], int trqsprnum, int *trqsprpart[2],
+            double *trqzdir0[3], double *trqxdir0[3], double *krpy[3][2], int *krpyidx[3], double *drpy[3][2],
+            int *drpyidx[3], int trqcone[], double *trqzdir1[3], double *trqxdir1[3], double *trqrpy[3],
+            double *trqrpytot[3], double *trqrpyspr[3],
             double *force[3], double *torque[3], double *kact[3], double kmax[],
             double emax[], double *krot[6], int adaptive, int unsprnum, int tsprings[],
             int tspridx[], int msprings[], int mspridx[], double *unlim[2], int unent[], int unop[], int unabs[],
@@ -666,7 +667,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   std::lock_guard<std::mutex> g(M);
   G.fn = "forces";
   if (parnum <= 0 || !ready()) return;
-  if (trqsprnum > 0) { fail(PG_ERR_UNSUPPORTED, "forces: TORSION_SPRING is not supported"); return; }
+
   if (unsprnum > 0 && (sprnum <= 0 || !sprmap)) { fail(PG_ERR_ARGUMENT, "forces: UNSPRING needs the springs and sprmap"); return; }
   if (adaptive && (!kact || !kmax || !emax || !krot))
   {
@@ -739,6 +740,31 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     if (adaptive) ok = ok && grow(d.sbig_ad, 11 * std::max<size_t>(1, big.size()));
     d.nbig = (int)big.size();
   }
+  const int Q = std::max(trqsprnum, 0);
+  if (Q)
+  {
+    // torsion springs: tables, directions, state and their flush events
+    if (!(S || adaptive)) for (int k = 0; ok && k < 9; k ++) ok = up(d.rotation[k], rotation[k], P);
+    for (int k = 0; ok && k < 9; k ++) ok = up(d.inverse[k], inverse[k], P);
+    for (int a = 0; ok && a < 2; a ++) ok = up(d.trqsprpart[a], trqsprpart[a], (size_t)Q);
+    for (int c = 0; ok && c < 3; c ++)
+      ok = up(d.trqzdir0[c], trqzdir0[c], Q) && up(d.trqxdir0[c], trqxdir0[c], Q) &&
+           up(d.trqzdir1[c], trqzdir1[c], Q) && up(d.trqxdir1[c], trqxdir1[c], Q) && up(d.trqrpy[c], trqrpy[c], Q) &&
+           up(d.trqrpytot[c], trqrpytot[c], Q) && up(d.trqrpyspr[c], trqrpyspr[c], Q) && grow(d.tq_out[c], Q) &&
+           (!adaptive || grow(d.tq_k[c], Q));
+    for (int o = 0; ok && o < 3; o ++)
+    {
+      ok = up(d.krpyidx[o], krpyidx[o], (size_t)Q + 1) && up(d.drpyidx[o], drpyidx[o], (size_t)Q + 1);
+      for (int c = 0; ok && c < 2; c ++)
+        ok = up(d.krpy[o][c], krpy[o][c], (size_t)krpyidx[o][Q]) && up(d.drpy[o][c], drpy[o][c], (size_t)drpyidx[o][Q]);
+    }
+    ok = ok && up(d.trqcone, trqcone, (size_t)Q);
+    std::vector<int> first;
+    std::vector<int4> ev, big;
+    pg_spring_events(parnum, Q, trqsprpart[0], trqsprpart[1], first, ev, big);
+    for (auto &e : ev) e.x &= 1;               // torsion runs are summed whole
+    ok = ok && up(d.tev_first, first.data(), P + 1) && up(d.tev, ev.data(), ev.size());
+  }
   const int U = S ? std::max(unsprnum, 0) : 0;
   if (U)
   {
@@ -769,9 +795,12 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   if (!contacts) { v.ellnum = 0; v.pell = nullptr; }
   if (adaptive) v.hs = G.hs;
   v.unsprnum = U;
+  v.trqsprnum = Q;
+  if (!adaptive) for (int c = 0; c < 3; c ++) v.tq_k[c] = nullptr;
   pg_launch_contacts(v, G.st, step);
   pg_launch_springs(v, G.st, step);
   if (S) pg_launch_spring_runs(v, G.st);
+  if (Q) { pg_launch_torsion(v, G.st, step); G.launches += 1; }
   if (U) { pg_launch_unspring(v, G.st); G.launches += 1; }
   if (adaptive) pg_launch_force_sums_adapt(v, G.st);
   else pg_launch_force_sums(v, G.st);
@@ -794,6 +823,9 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     ok = ok && down(unspring, d.unspring, S) && down(sprflg, d.sprflg, S);
     if (U) ok = ok && down(nfreq, d.nfreq, U);
   }
+  for (int c = 0; ok && Q && c < 3; c ++)
+    ok = down(trqzdir1[c], d.trqzdir1[c], Q) && down(trqxdir1[c], d.trqxdir1[c], Q) && down(trqrpy[c], d.trqrpy[c], Q) &&
+         down(trqrpytot[c], d.trqrpytot[c], Q) && down(trqrpyspr[c], d.trqrpyspr[c], Q);
   if (!ok) return;
   // zero_force_torque_kmax (forces.ispc) also clears kmax and emax
   if (!adaptive && kmax) std::memset(kmax, 0, P * sizeof(double));

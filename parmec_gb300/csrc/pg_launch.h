@@ -14,6 +14,7 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s);     // sums of the long flush runs
 void pg_launch_unspring(const PgDev &d, cudaStream_t s);        // UNSPRING rules, after the springs
+void pg_launch_torsion(const PgDev &d, cudaStream_t s, double step);   // torsion springs, before the force sums
 void pg_launch_gather(const double *const *cols, int ncols, const int *idx, int n, double *out, cudaStream_t s);
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_force_sums(const PgDev &d, cudaStream_t s);                          // forces() tail

@@ -292,6 +292,42 @@ int upload_static(pg_session *s, const pg_scene *sc)
       TRY(h2d(s, d.rstang[k], sc->rstang[k], R));
     }
   }
+  // torsion springs: tables, directions and their flush events
+  {
+    const int Q = std::max(sc->trqsprnum, 0);
+    d.trqsprnum = Q;
+    const size_t n = std::max(1, Q);
+    for (int a = 0; a < 2; a ++) { TRY(dalloc(s, &d.trqsprpart[a], n)); TRY(h2d(s, d.trqsprpart[a], sc->trqsprpart[a], Q)); }
+    for (int c = 0; c < 3; c ++)
+    {
+      TRY(dalloc(s, &d.trqzdir0[c], n)); TRY(h2d(s, d.trqzdir0[c], sc->trqzdir0[c], Q));
+      TRY(dalloc(s, &d.trqxdir0[c], n)); TRY(h2d(s, d.trqxdir0[c], sc->trqxdir0[c], Q));
+      TRY(dalloc(s, &d.trqzdir1[c], n)); TRY(dalloc(s, &d.trqxdir1[c], n));
+      TRY(dalloc(s, &d.trqrpy[c], n)); TRY(dalloc(s, &d.trqrpytot[c], n)); TRY(dalloc(s, &d.trqrpyspr[c], n));
+      TRY(dalloc(s, &d.tq_out[c], n));
+    }
+    for (int o = 0; o < 3; o ++)
+    {
+      const size_t nk = Q ? (size_t)sc->krpyidx[o][Q] : 0, nd = Q ? (size_t)sc->drpyidx[o][Q] : 0;
+      TRY(dalloc(s, &d.krpyidx[o], n + 1)); TRY(h2d(s, d.krpyidx[o], sc->krpyidx[o], Q ? Q + 1 : 0));
+      TRY(dalloc(s, &d.drpyidx[o], n + 1)); TRY(h2d(s, d.drpyidx[o], sc->drpyidx[o], Q ? Q + 1 : 0));
+      for (int c = 0; c < 2; c ++)
+      {
+        TRY(dalloc(s, &d.krpy[o][c], std::max<size_t>(1, nk))); TRY(h2d(s, d.krpy[o][c], sc->krpy[o][c], nk));
+        TRY(dalloc(s, &d.drpy[o][c], std::max<size_t>(1, nd))); TRY(h2d(s, d.drpy[o][c], sc->drpy[o][c], nd));
+      }
+    }
+    TRY(dalloc(s, &d.trqcone, n)); TRY(h2d(s, d.trqcone, sc->trqcone, Q));
+    std::vector<int> first;
+    std::vector<int4> evv, big;
+    pg_spring_events(P, Q, Q ? sc->trqsprpart[0] : nullptr, Q ? sc->trqsprpart[1] : nullptr, first, evv, big);
+    for (auto &e : evv) e.x &= 1;               // torsion runs are summed whole
+    TRY(dalloc(s, &d.tev_first, P + 1));
+    TRY(dalloc(s, &d.tev, evv.size()));
+    TRY(h2d(s, d.tev_first, first.data(), P + 1));
+    TRY(h2d(s, d.tev, evv.data(), evv.size()));
+    CK(cudaStreamSynchronize(s->stream));
+  }
   // spring failure rules, spring ids mapped to sorted positions
   {
     const int U = std::max(sc->unsprnum, 0);
@@ -550,7 +586,30 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
   return PG_OK;
 }
 
-int upload_all(pg_session *s, const pg_scene *sc) { return upload_ranges(s, sc, full_ranges(s->d), true, false); }
+// torsion spring state (directions, angles, moments)
+int torsion_state(pg_session *s, const pg_scene *sc, bool up)
+{
+  PgDev &d = s->d;
+  const size_t Q = d.trqsprnum;
+  if (!Q || sc->trqsprnum != d.trqsprnum) return PG_OK;
+  for (int c = 0; c < 3; c ++)
+  {
+    double *dv[5] = {d.trqzdir1[c], d.trqxdir1[c], d.trqrpy[c], d.trqrpytot[c], d.trqrpyspr[c]};
+    double *hv[5] = {sc->trqzdir1[c], sc->trqxdir1[c], sc->trqrpy[c], sc->trqrpytot[c], sc->trqrpyspr[c]};
+    for (int a = 0; a < 5; a ++)
+    {
+      if (up) TRY(h2d(s, dv[a], hv[a], Q));
+      else TRY(d2h(s, hv[a], dv[a], Q));
+    }
+  }
+  return PG_OK;
+}
+
+int upload_all(pg_session *s, const pg_scene *sc)
+{
+  TRY(upload_ranges(s, sc, full_ranges(s->d), true, false));
+  return torsion_state(s, sc, true);
+}
 
 int download_ranges(pg_session *s, pg_scene *sc, Ranges r)
 {
@@ -927,6 +986,7 @@ void enqueue_step(pg_session *s, double step)
   pg_launch_contacts(d, s->stream, step);
   pg_launch_springs(d, s->stream, step);
   pg_launch_spring_runs(d, s->stream);
+  pg_launch_torsion(d, s->stream, step);
   pg_launch_unspring(d, s->stream);
   pg_launch_integrate(d, s->stream, step);
   pg_launch_mesh(d, s->stream);
@@ -976,6 +1036,7 @@ int adapt_buffers(pg_session *s)
     TRY(dalloc(s, &d.akmax, P));
     TRY(dalloc(s, &d.aemax, P));
     for (int k = 0; k < 17; k ++) TRY(dalloc(s, &d.sad[k], S));
+    for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.tq_k[k], (size_t)std::max(d.trqsprnum, 1)));
     TRY(dalloc(s, &s->hs_buf, 4));
     TRY(dalloc(s, &d.hmin, 1));
     const unsigned long long big = 0x7fefffffffffffffull;
@@ -1013,6 +1074,7 @@ void enqueue_step_adaptive(pg_session *s)
   pg_launch_contacts(d, s->stream, 0.0);
   pg_launch_springs(d, s->stream, 0.0);
   pg_launch_spring_runs(d, s->stream);
+  pg_launch_torsion(d, s->stream, 0.0);
   pg_launch_unspring(d, s->stream);
   pg_launch_force_sums_adapt(d, s->stream);
   pg_launch_adapt_step(d, s->stream);
@@ -1027,6 +1089,7 @@ int adaptive_kernel_count(const PgDev &d)
   int n = pg_rebuild_kernel_count(d) + 2 + 1;     // excite, select, tail
   if (d.ellnum) n += 1;
   if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0) + (d.unsprnum ? 1 : 0);
+  if (d.trqsprnum) n += 1;
   if (d.parnum) n += 3;                           // force sums, minimum, dynamics
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;
@@ -1079,7 +1142,7 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if (form == PG_FORM_MIXED)
   {
     // scope of the mixed form: spheres centred on their particle, obstacles, analytical particles
-    if (sc->sprnum || sc->nodnum || sc->facnum || sc->rstnum > 0) return PG_ERR_UNSUPPORTED;
+    if (sc->sprnum || sc->nodnum || sc->facnum || sc->rstnum > 0 || sc->trqsprnum > 0) return PG_ERR_UNSUPPORTED;
     for (int e = 0; e < sc->ellnum; e ++)
     {
       int p = sc->part[e];
@@ -1243,6 +1306,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       {
         pg_launch_springs(d, s->stream, step);
         pg_launch_spring_runs(d, s->stream);
+        pg_launch_torsion(d, s->stream, step);
         pg_launch_unspring(d, s->stream);
       }
       CK(cudaEventRecord(ev[3], s->stream));
@@ -1409,6 +1473,7 @@ int pg_session_download(pg_session *s, pg_scene *sc)
   for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->nodes[k], d.nodes[k], N));
   TRY(d2h(s, sc->unspring, d.unspring, S));
   if (d.unsprnum && sc->nfreq && sc->unsprnum == d.unsprnum) TRY(d2h(s, sc->nfreq, d.nfreq, d.unsprnum));
+  TRY(torsion_state(s, sc, false));
   for (int a = 0; a < 2; a ++)
     for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->sprpnt[a][k], d.sprpnt[6*a+k], S));
   for (int k = 0; k < 2; k ++) TRY(d2h(s, sc->yield[k], d.yield[k], S));

@@ -74,6 +74,19 @@ struct PgDev
   int *rst_list;            // restraint indices
   double *rstlin[9], *rstang[9];   // [rstnum] three orthonormal directions each (zero rows unused)
 
+  // ---- torsion springs (trqspr_task, forces.ispc:1415-2057), sorted by (part0, part1)
+  int trqsprnum;
+  int *trqsprpart[2];
+  double *trqzdir0[3], *trqxdir0[3];
+  double *krpy[3][2]; int *krpyidx[3];
+  double *drpy[3][2]; int *drpyidx[3];
+  int *trqcone;
+  double *trqzdir1[3], *trqxdir1[3], *trqrpy[3], *trqrpytot[3], *trqrpyspr[3];
+  double *tq_out[3];        // per torsion spring: torque in the global frame
+  double *tq_k[3];          // per torsion spring: adaptive krot diagonal terms
+  int *tev_first;           // [parnum+1] CSR of torsion torque flush events per particle
+  int4 *tev;                // (type, begin, end, first) as sev, without long-run chunking
+
   // ---- spring failure rules (unspring_task, forces.ispc:2058-2127); spring
   // lists hold sorted positions
   int unsprnum;

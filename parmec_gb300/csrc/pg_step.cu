@@ -1217,6 +1217,31 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       }
     }
 
+    // torsion spring torque flushes (trqspr_task, forces.ispc:1667-2055),
+    // after every translational spring flush, in the same run rule
+    if (d.trqsprnum)
+    {
+      for (int ev = d.tev_first[i]; ev < d.tev_first[i+1]; ev ++)
+      {
+        const int4 v = d.tev[ev];
+        const int type = v.x & 1;
+        double at[3] = {0.0, 0.0, 0.0}, kp[3] = {0.0, 0.0, 0.0};
+        bool started = false;
+        for (int s = v.y; s < v.z; s ++)
+        {
+          if (type == 1 && d.trqsprpart[1][s] < 0) continue;
+          const double tq[3] = {d.tq_out[0][s], d.tq_out[1][s], d.tq_out[2][s]};
+          if (!started && !v.w) { at[0] = tq[0]; at[1] = tq[1]; at[2] = tq[2]; }
+          else { at[0] += tq[0]; at[1] += tq[1]; at[2] += tq[2]; }
+          if (ADAPT) for (int c = 0; c < 3; c ++) kp[c] = kp[c] + d.tq_k[c][s];
+          started = true;
+        }
+        if (type == 0) { T[0] += at[0]; T[1] += at[1]; T[2] += at[2]; }
+        else { T[0] -= at[0]; T[1] -= at[1]; T[2] -= at[2]; }
+        if (ADAPT) for (int c = 0; c < 3; c ++) krot[c] += kp[c];
+      }
+    }
+
     }
     if (ADAPT)
     {
@@ -1395,6 +1420,189 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
   if (FUSED && d.ellnum) flag_rebuild(d, need);
 }
 
+// ---------------------------------------------------------------- torsion springs
+// trqspr_task (forces.ispc:1415-2057), one thread per torsion spring: the
+// current frame rot1j = Lj [x0 y0 z0], roll/pitch/yaw rates of the relative
+// spatial angular velocity, the integrated angles, spring torques from the
+// angle lookups (or from the combined angle of a cone), dampers by lookup or
+// by a critical damping ratio against the local equivalent inertia
+// inv(rot1j (Jj^-1 + Jk^-1) rot1j^T).  The torque rot1j (roll, pitch, yaw)
+// goes to tq_out and is flushed to the particles by k_integrate.  The
+// pitch-yaw cone's pitch damper reads the pitch ratio (the reference reads
+// the roll entry, forces.ispc:1823).
+__device__ __forceinline__ double tq_spring(const PgDev &d, int o, int i, double arg, double *kslope)
+{
+  if (d.krpyidx[o][i+1] > d.krpyidx[o][i])
+    return look_up(d.krpy[o][0], d.krpy[o][1], d.krpyidx[o][i], d.krpyidx[o][i+1], arg, kslope);
+  *kslope = 0.0;
+  return 0.0;
+}
+
+__device__ __forceinline__ double tq_damper(const PgDev &d, int o, int i, double rate, double kslope, double inertia)
+{
+  if (d.drpyidx[o][i]+1 == d.drpyidx[o][i+1])
+  {
+    const double ratio = d.drpy[o][0][d.drpyidx[o][i]];
+    const double dm = - ratio * 2.0 * sqrt(fabs(kslope) * inertia);
+    return rate * dm;
+  }
+  double dm;
+  return look_up(d.drpy[o][0], d.drpy[o][1], d.drpyidx[o][i], d.drpyidx[o][i+1], rate, &dm);
+}
+
+__global__ void __launch_bounds__(TPB) k_torsion(PgDev d, double step)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.trqsprnum) return;
+  if (d.hs) step = d.hs[0];
+  const int j = d.trqsprpart[0][i], k = d.trqsprpart[1][i];
+  double oj[3] = {d.angular[3][j], d.angular[4][j], d.angular[5][j]}, Lj[9];
+  for (int c = 0; c < 9; c ++) Lj[c] = d.rotation[c][j];
+  const double zdir0[3] = {d.trqzdir0[0][i], d.trqzdir0[1][i], d.trqzdir0[2][i]};
+  const double xdir0[3] = {d.trqxdir0[0][i], d.trqxdir0[1][i], d.trqxdir0[2][i]};
+  const double ydir0[3] = {zdir0[1]*xdir0[2] - zdir0[2]*xdir0[1], zdir0[2]*xdir0[0] - zdir0[0]*xdir0[2],
+                           zdir0[0]*xdir0[1] - zdir0[1]*xdir0[0]};
+  double rot1j[9];
+  nvmul(Lj, xdir0, rot1j);
+  nvmul(Lj, ydir0, rot1j+3);
+  nvmul(Lj, zdir0, rot1j+6);
+  for (int c = 0; c < 3; c ++) { d.trqzdir1[c][i] = rot1j[6+c]; d.trqxdir1[c][i] = rot1j[c]; }
+  double ok[3] = {0.0, 0.0, 0.0};
+  if (k >= 0) { ok[0] = d.angular[3][k]; ok[1] = d.angular[4][k]; ok[2] = d.angular[5][k]; }
+  const double ojk[3] = {oj[0]-ok[0], oj[1]-ok[1], oj[2]-ok[2]};
+  const double rolldot = dot3(rot1j, ojk), pitchdot = dot3(rot1j+3, ojk), yawdot = dot3(rot1j+6, ojk);
+  double roll = d.trqrpy[0][i], pitch = d.trqrpy[1][i], yaw = d.trqrpy[2][i];
+  roll += rolldot*step;
+  pitch += pitchdot*step;
+  yaw += yawdot*step;
+  d.trqrpy[0][i] = roll; d.trqrpy[1][i] = pitch; d.trqrpy[2][i] = yaw;
+  double Ixx = 0.0, Iyy = 0.0, Izz = 0.0;
+  bool ratio = false;
+  for (int o = 0; o < 3; o ++) ratio = ratio || d.drpyidx[o][i]+1 == d.drpyidx[o][i+1];
+  if (ratio)
+  {
+    double I[9], tmp[9];
+    for (int c = 0; c < 9; c ++) I[c] = d.inverse[c][j];
+    if (k >= 0) for (int c = 0; c < 9; c ++) I[c] += d.inverse[c][k];
+    ntmul(I, rot1j, tmp);
+    nnmul(rot1j, tmp, I);
+    invert3(I, tmp);
+    Ixx = tmp[0]; Iyy = tmp[4]; Izz = tmp[8];
+  }
+  double kroll = 0.0, kpitch = 0.0, kyaw = 0.0;
+  double trqroll = 0.0, trqpitch = 0.0, trqyaw = 0.0, trqrolltot = 0.0, trqpitchtot = 0.0, trqyawtot = 0.0;
+  switch (d.trqcone[i])
+  {
+    case 0:
+    {
+      trqroll = tq_spring(d, 0, i, roll, &kroll);
+      trqpitch = tq_spring(d, 1, i, pitch, &kpitch);
+      trqyaw = tq_spring(d, 2, i, yaw, &kyaw);
+      const double trqrolldot = tq_damper(d, 0, i, rolldot, kroll, Ixx);
+      const double trqpitchdot = tq_damper(d, 1, i, pitchdot, kpitch, Iyy);
+      const double trqyawdot = tq_damper(d, 2, i, yawdot, kyaw, Izz);
+      trqrolltot = trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot);
+      trqpitchtot = trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot);
+      trqyawtot = trqyaw + (trqyaw == 0.0 ? 0.0 : trqyawdot);
+      break;
+    }
+    case 3:                                     // roll-pitch cone
+    {
+      const double angle = sqrt(roll*roll + pitch*pitch);
+      const double angledot = angle > 0.0 ? (rolldot*roll+pitchdot*pitch)/angle : 0.0;
+      trqroll = tq_spring(d, 0, i, angle, &kroll);
+      kpitch = kroll;
+      const double trqrolldot = tq_damper(d, 0, i, angledot, kroll, sqrt(Ixx*Ixx + Iyy*Iyy));
+      trqyaw = tq_spring(d, 2, i, yaw, &kyaw);
+      const double trqyawdot = tq_damper(d, 2, i, yawdot, kyaw, Izz);
+      trqyawtot = trqyaw + (trqyaw == 0.0 ? 0.0 : trqyawdot);
+      if (angle > 0.)
+      {
+        const double xcoef = roll/angle, ycoef = pitch/angle;
+        trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqpitchtot = ycoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqpitch = trqroll*ycoef;
+        trqroll *= xcoef;
+      }
+      else { trqrolltot = trqpitchtot = 0.0; trqroll = trqpitch = 0.0; }
+      break;
+    }
+    case 5:                                     // roll-yaw cone
+    {
+      const double angle = sqrt(roll*roll + yaw*yaw);
+      const double angledot = angle > 0.0 ? (rolldot*roll+yawdot*yaw)/angle : 0.0;
+      trqroll = tq_spring(d, 0, i, angle, &kroll);
+      kyaw = kroll;
+      const double trqrolldot = tq_damper(d, 0, i, angledot, kroll, sqrt(Ixx*Ixx + Izz*Izz));
+      trqpitch = tq_spring(d, 1, i, pitch, &kpitch);
+      const double trqpitchdot = tq_damper(d, 1, i, pitchdot, kpitch, Iyy);
+      trqpitchtot = trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot);
+      if (angle > 0.)
+      {
+        const double xcoef = roll/angle, zcoef = yaw/angle;
+        trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqyawtot = zcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqyaw = trqroll*zcoef;
+        trqroll *= xcoef;
+      }
+      else { trqrolltot = trqyawtot = 0.0; trqroll = trqyaw = 0.0; }
+      break;
+    }
+    case 6:                                     // pitch-yaw cone
+    {
+      trqroll = tq_spring(d, 0, i, roll, &kroll);
+      const double trqrolldot = tq_damper(d, 0, i, rolldot, kroll, Ixx);
+      const double angle = sqrt(pitch*pitch + yaw*yaw);
+      const double angledot = angle > 0.0 ? (pitchdot*pitch+yawdot*yaw)/angle : 0.0;
+      trqpitch = tq_spring(d, 1, i, angle, &kpitch);
+      kyaw = kpitch;
+      const double trqpitchdot = tq_damper(d, 1, i, angledot, kpitch, sqrt(Iyy*Iyy + Izz*Izz));
+      trqrolltot = trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot);
+      if (angle > 0.)
+      {
+        const double ycoef = pitch/angle, zcoef = yaw/angle;
+        trqpitchtot = ycoef*(trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot));
+        trqyawtot = zcoef*(trqpitch + (trqpitch == 0.0 ? 0.0 : trqpitchdot));
+        trqyaw = zcoef*trqpitch;
+        trqpitch *= ycoef;
+      }
+      else { trqpitchtot = trqyawtot = 0.0; trqpitch = trqyaw = 0.0; }
+      break;
+    }
+    case 7:                                     // roll-pitch-yaw cone
+    {
+      const double angle = sqrt(roll*roll + pitch*pitch + yaw*yaw);
+      const double angledot = angle > 0.0 ? (rolldot*roll+pitchdot*pitch+yawdot*yaw)/angle : 0.0;
+      trqroll = tq_spring(d, 0, i, angle, &kroll);
+      kpitch = kyaw = kroll;
+      const double trqrolldot = tq_damper(d, 0, i, angledot, kroll, sqrt(Ixx*Ixx + Iyy*Iyy + Izz*Izz));
+      if (angle > 0.)
+      {
+        const double xcoef = roll/angle, ycoef = pitch/angle, zcoef = yaw/angle;
+        trqrolltot = xcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqpitchtot = ycoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqyawtot = zcoef*(trqroll + (trqroll == 0.0 ? 0.0 : trqrolldot));
+        trqpitch = ycoef*trqroll;
+        trqyaw = zcoef*trqroll;
+        trqroll *= xcoef;
+      }
+      else { trqrolltot = trqpitchtot = trqyawtot = 0.0; trqroll = trqpitch = trqyaw = 0.0; }
+      break;
+    }
+  }
+  d.tq_out[0][i] = trqrolltot*rot1j[0] + trqpitchtot*rot1j[3] + trqyawtot*rot1j[6];
+  d.tq_out[1][i] = trqrolltot*rot1j[1] + trqpitchtot*rot1j[4] + trqyawtot*rot1j[7];
+  d.tq_out[2][i] = trqrolltot*rot1j[2] + trqpitchtot*rot1j[5] + trqyawtot*rot1j[8];
+  d.trqrpytot[0][i] = trqrolltot; d.trqrpytot[1][i] = trqpitchtot; d.trqrpytot[2][i] = trqyawtot;
+  d.trqrpyspr[0][i] = trqroll; d.trqrpyspr[1][i] = trqpitch; d.trqrpyspr[2][i] = trqyaw;
+  if (d.tq_k[0])
+  {
+    d.tq_k[0][i] = fabs(kroll)*rot1j[0];
+    d.tq_k[1][i] = fabs(kpitch)*rot1j[4];
+    d.tq_k[2][i] = fabs(kyaw)*rot1j[8];
+  }
+}
+
 // ---------------------------------------------------------------- partial downloads
 // out[c*n + j] = cols[c][idx[j]]: the rows a HISTORY sample reads, gathered
 // into one buffer so that one small copy replaces a download of every array
@@ -1538,6 +1746,11 @@ void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
   else k_springs<false><<<nblk(d.sprnum), TPB, 0, s>>>(d, step);
 }
 
+void pg_launch_torsion(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.trqsprnum) k_torsion<<<nblk(d.trqsprnum), TPB, 0, s>>>(d, step);
+}
+
 void pg_launch_gather(const double *const *cols, int ncols, const int *idx, int n, double *out, cudaStream_t s)
 {
   if (ncols > 0 && n > 0) k_gather<<<nblk(ncols * n), TPB, 0, s>>>(cols, ncols, idx, n, out);
@@ -1621,6 +1834,7 @@ int pg_step_kernel_count(const PgDev &d)
   int n = 2;                                   // excite, tail
   if (d.ellnum) n += 1;                        // contacts
   if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0) + (d.unsprnum ? 1 : 0);
+  if (d.trqsprnum) n += 1;                     // torsion springs
   if (d.parnum) n += 1;                        // integrate
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;

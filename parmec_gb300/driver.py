@@ -269,6 +269,10 @@ def run_dem(m, duration, step, interval, engine, adaptive=0.0):
     if m.springs_changed:
         sort_springs(m)
         m.springs_changed = False
+    if m.torsion_changed:
+        from .torsion import sort_torsion
+        sort_torsion(m)
+        m.torsion_changed = False
 
     eng = engine if engine is not None else m.engine
     if eng is None or eng.model is not m or eng.stale():

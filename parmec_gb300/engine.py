@@ -8,7 +8,7 @@ from . import abi
 
 def _counts(m):
     return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
-            len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings))
+            len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings), m.trqsprnum)
 
 
 class GpuEngine:

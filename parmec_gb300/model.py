@@ -94,8 +94,13 @@ class Model:
                        "sprdir": (6, f8), "sprflg": (0, i4), "sproffset": (0, i4), "sprfric": (0, f8),
                        "sprkskn": (0, f8), "sprsdsp": (3, f8), "stroke0": (0, f8), "stroke": (3, f8),
                        "sprfrc": (3, f8), "sprid": (0, i4), "sprmap": (0, i4)}, 64)
+        self.Q = _SoA({"tsprpart": (2, i4), "zdir0": (3, f8), "xdir0": (3, f8), "zdir1": (3, f8),
+                       "xdir1": (3, f8), "rpy": (3, f8), "rpytot": (3, f8), "rpyspr": (3, f8),
+                       "refpnt": (3, f8), "cone": (0, i4), "tsprid": (0, i4), "tsprmap": (0, i4)}, 16)
         self.parnum = self.ellnum = self.trinum = self.obsnum = 0
-        self.nodnum = self.facnum = self.sprnum = 0
+        self.nodnum = self.facnum = self.sprnum = self.trqsprnum = 0
+        self.krpy_tab, self.drpy_tab = [], []   # per torsion spring: three (angle|rate, torque) tables
+        self.torsion_changed = False
         self.mparam = []                    # [density, young, poisson]
         self.pairs = [(0, 0)]               # pair_reset (parmec.cpp:375-388)
         self.ikind = [0]
@@ -406,6 +411,14 @@ class Model:
         self.springs_changed = True
         return spring_command(self, part1, point1, part2, geom2, spring, dashpot, direction, planar,
                               unload, ylim, inactive, offset, friction, kskn)
+
+    def torsion_spring(self, part1, part2, zdir, xdir, kroll=None, kpitch=None, kyaw=None, droll=None,
+                       dpitch=None, dyaw=None, cone=None, refpnt=None):
+        """TORSION_SPRING (input.cpp:1791-2080): roll/pitch/yaw torsion spring
+        between two particles (or a particle and the ground); returns its id."""
+        from .torsion import torsion_command
+        return torsion_command(self, part1, part2, zdir, xdir, kroll, kpitch, kyaw, droll, dpitch, dyaw,
+                               cone, refpnt)
 
     # ------------------------------------------------------------ PRESCRIBE
     def prescribe_motion(self, parnum, linear=None, angular=None, kind=None):
@@ -847,6 +860,26 @@ class Model:
         s.unent, s.unop, s.unabs = abi.iptr(unent), abi.iptr(unop), abi.iptr(unabs)
         s.nsteps, s.nfreq, s.unaction = abi.iptr(nsteps), abi.iptr(self.unspring_nfreq), abi.iptr(unaction)
         s.sprmap = abi.iptr(S.sprmap)
+        from .torsion import torsion_tables
+        Q = self.Q
+        tt = torsion_tables(self)
+        keep.append(tt)
+        s.trqsprnum = self.trqsprnum
+        s.trqsprpart = abi.rows(Q.tsprpart, 2, abi.I)
+        s.trqzdir0 = abi.rows(Q.zdir0, 3)
+        s.trqxdir0 = abi.rows(Q.xdir0, 3)
+        for o in range(3):
+            for c in range(2):
+                s.krpy[o][c] = tt[f"krpy{o}"][c].ctypes.data_as(abi.D)
+                s.drpy[o][c] = tt[f"drpy{o}"][c].ctypes.data_as(abi.D)
+            s.krpyidx[o] = abi.iptr(tt[f"krpyidx{o}"])
+            s.drpyidx[o] = abi.iptr(tt[f"drpyidx{o}"])
+        s.trqcone = abi.iptr(Q.cone)
+        s.trqzdir1 = abi.rows(Q.zdir1, 3)
+        s.trqxdir1 = abi.rows(Q.xdir1, 3)
+        s.trqrpy = abi.rows(Q.rpy, 3)
+        s.trqrpytot = abi.rows(Q.rpytot, 3)
+        s.trqrpyspr = abi.rows(Q.rpyspr, 3)
         nscene = getattr(self, "nscene", 0)
         if nscene:
             s.nscene = nscene

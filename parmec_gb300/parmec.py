@@ -68,6 +68,11 @@ def PRESCRIBE(parnum, linear=None, angular=None, kind=None):
     return _model.prescribe_motion(parnum, linear, angular, kind)
 
 
+def TORSION_SPRING(part1, part2, zdir, xdir, kroll=None, kpitch=None, kyaw=None, droll=None, dpitch=None,
+                   dyaw=None, cone=None, refpnt=None):
+    return _model.torsion_spring(part1, part2, zdir, xdir, kroll, kpitch, kyaw, droll, dpitch, dyaw, cone, refpnt)
+
+
 def UNSPRING(tsprings, msprings, limits, entity=None, operator=None, abs=False, nsteps=1, nfreq=1, unload=-1,
              activate=None):
     return _model.unspring(tsprings, msprings, limits, entity, operator, abs, nsteps, nfreq, unload, activate)
@@ -118,7 +123,7 @@ def DEM(duration, step, interval=None, prefix=None, adaptive=0.0):
 
 
 COMMANDS = ["RESET", "TSERIES", "MATERIAL", "SPHERE", "MESH", "ANALYTICAL", "OBSTACLE", "GRANULAR",
-            "SPRING", "UNSPRING", "EQM", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
+            "SPRING", "TORSION_SPRING", "UNSPRING", "EQM", "PRESCRIBE", "RESTRAIN", "VELOCITY", "GRAVITY", "DAMPING", "HISTORY", "CRITICAL", "OUTPUT",
             "ARGV", "DEM"]
 
 

@@ -103,6 +103,10 @@ def dem(lib, host, duration, step, adaptive=0.0):
     if m.springs_changed:
         sort_springs(m)
         m.springs_changed = False
+    if m.torsion_changed:
+        from parmec_gb300.torsion import sort_torsion
+        sort_torsion(m)
+        m.torsion_changed = False
     s = m.scene()
     obspnt, obsang, obslin = m._obs_views
     ntasks = 1
@@ -163,8 +167,9 @@ def dem(lib, host, duration, step, adaptive=0.0):
                    D(step0), s.sprnum, s.sprtype, s.unspring, s.sprmap, s.sprpart, s.sprpnt, s.spring, s.spridx,
                    s.dashpot, s.dashidx, s.unload, s.unidx, s.yield_, s.sprdir, s.sprflg, s.sproffset,
                    s.sprfric, s.sprkskn, s.sprsdsp, s.stroke0, s.stroke, s.sprfrc, s.lcurve, s.lcidx,
-                   abi.dptr(gravity), 0, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL,
-                   NULL, NULL, s.force, s.torque, kact_p if adapt else NULL, abi.dptr(kmax), abi.dptr(emax),
+                   abi.dptr(gravity), s.trqsprnum, s.trqsprpart, s.trqzdir0, s.trqxdir0, s.krpy, s.krpyidx,
+                   s.drpy, s.drpyidx, s.trqcone, s.trqzdir1, s.trqxdir1, s.trqrpy, s.trqrpytot, s.trqrpyspr,
+                   s.force, s.torque, kact_p if adapt else NULL, abi.dptr(kmax), abi.dptr(emax),
                    krot_p if adapt else NULL, 1 if adapt else 0, s.unsprnum,
                    s.tsprings, s.tspridx, s.msprings, s.mspridx, s.unlim, s.unent, s.unop, s.unabs, s.nsteps,
                    s.nfreq, s.unaction, s.activate, s.actidx, m.stepnum, D(t))
