@@ -196,6 +196,16 @@ typedef struct pg_scene {
   int *trqcone;
   double *trqzdir1[3], *trqxdir1[3];
   double *trqrpy[3], *trqrpytot[3], *trqrpyspr[3];
+
+  /* externally prescribed body forces (parmec.h:281-289, applied by
+   * prescribe_body_forces, parmec.cpp:2202-2224): one record per particle;
+   * each step the particle's force and torque after forces() are exported to
+   * pbfin (inner: force xyz, torque xyz; written back by
+   * pg_session_download) and pbfout (outer) is added to them */
+  int pbfnum;
+  int *pbfpart;
+  double *pbfout[6];
+  double *pbfin[6];
 } pg_scene;
 
 /* UNSPRING entity and operator codes (constants.h:43-46, 70) */

@@ -2160,6 +2160,19 @@ double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double 
   if (s->trqsprnum) trqspr_all(s, step0, at);
   if (s->unsprnum) unspring_all(s, tab->stepnum);
 
+  /* prescribe_body_forces (parmec.cpp:2202-2224): export, then add */
+  for (int q = 0; q < s->pbfnum; q ++)
+  {
+    const int p = s->pbfpart[q];
+    for (int c = 0; c < 3; c ++)
+    {
+      s->pbfin[c][q] = s->force[c][p];
+      s->pbfin[3+c][q] = s->torque[c][p];
+      s->force[c][p] += s->pbfout[c][q];
+      s->torque[c][p] += s->pbfout[3+c][q];
+    }
+  }
+
   /* adaptive_timestep (parmec.ispc:397-420) */
   double step1 = step0;
   if (at)

@@ -126,6 +126,7 @@ class OracleEngine:
 
     def download(self):
         self.model.pull_obstacles()
+        self.model.pull_body_forces()
 
     def contacts(self):
         n = self.lib.or_contact_count(self.ctx)

@@ -79,6 +79,7 @@ class PgScene(ctypes.Structure):
         ("krpy", (D * 2) * 3), ("krpyidx", I * 3), ("drpy", (D * 2) * 3), ("drpyidx", I * 3),
         ("trqcone", I), ("trqzdir1", D * 3), ("trqxdir1", D * 3),
         ("trqrpy", D * 3), ("trqrpytot", D * 3), ("trqrpyspr", D * 3),
+        ("pbfnum", ctypes.c_int), ("pbfpart", I), ("pbfout", D * 6), ("pbfin", D * 6),
     ]
 
 

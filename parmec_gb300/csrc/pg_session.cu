@@ -328,6 +328,13 @@ int upload_static(pg_session *s, const pg_scene *sc)
     TRY(h2d(s, d.tev, evv.data(), evv.size()));
     CK(cudaStreamSynchronize(s->stream));
   }
+  // prescribed body forces: record storage (values and the particle map come with each upload)
+  {
+    d.pbfnum = std::max(sc->pbfnum, 0);
+    const size_t n = std::max(1, d.pbfnum);
+    TRY(dalloc(s, &d.pbf_slot, (size_t)std::max(P, 1)));
+    for (int c = 0; c < 6; c ++) { TRY(dalloc(s, &d.pbfout[c], n)); TRY(dalloc(s, &d.pbfin[c], n)); }
+  }
   // spring failure rules, spring ids mapped to sorted positions
   {
     const int U = std::max(sc->unsprnum, 0);
@@ -605,9 +612,28 @@ int torsion_state(pg_session *s, const pg_scene *sc, bool up)
   return PG_OK;
 }
 
+// prescribed body forces: the outer values and the particle -> record map
+int body_forces_up(pg_session *s, const pg_scene *sc)
+{
+  PgDev &d = s->d;
+  if (!d.pbfnum || sc->pbfnum != d.pbfnum) return PG_OK;
+  std::vector<int> slot(d.parnum, -1);
+  for (int q = 0; q < d.pbfnum; q ++)
+  {
+    const int p = sc->pbfpart[q];
+    if (p < 0 || p >= d.parnum) return PG_ERR_ARGUMENT;
+    slot[p] = q;
+  }
+  TRY(h2d(s, d.pbf_slot, slot.data(), slot.size()));
+  for (int c = 0; c < 6; c ++) TRY(h2d(s, d.pbfout[c], sc->pbfout[c], (size_t)d.pbfnum));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
 int upload_all(pg_session *s, const pg_scene *sc)
 {
   TRY(upload_ranges(s, sc, full_ranges(s->d), true, false));
+  TRY(body_forces_up(s, sc));
   return torsion_state(s, sc, true);
 }
 
@@ -1142,7 +1168,8 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if (form == PG_FORM_MIXED)
   {
     // scope of the mixed form: spheres centred on their particle, obstacles, analytical particles
-    if (sc->sprnum || sc->nodnum || sc->facnum || sc->rstnum > 0 || sc->trqsprnum > 0) return PG_ERR_UNSUPPORTED;
+    if (sc->sprnum || sc->nodnum || sc->facnum || sc->rstnum > 0 || sc->trqsprnum > 0 || sc->pbfnum > 0)
+      return PG_ERR_UNSUPPORTED;
     for (int e = 0; e < sc->ellnum; e ++)
     {
       int p = sc->part[e];
@@ -1474,6 +1501,8 @@ int pg_session_download(pg_session *s, pg_scene *sc)
   TRY(d2h(s, sc->unspring, d.unspring, S));
   if (d.unsprnum && sc->nfreq && sc->unsprnum == d.unsprnum) TRY(d2h(s, sc->nfreq, d.nfreq, d.unsprnum));
   TRY(torsion_state(s, sc, false));
+  if (d.pbfnum && sc->pbfnum == d.pbfnum)
+    for (int c = 0; c < 6; c ++) TRY(d2h(s, sc->pbfin[c], d.pbfin[c], (size_t)d.pbfnum));
   for (int a = 0; a < 2; a ++)
     for (int k = 0; k < 3; k ++) TRY(d2h(s, sc->sprpnt[a][k], d.sprpnt[6*a+k], S));
   for (int k = 0; k < 2; k ++) TRY(d2h(s, sc->yield[k], d.yield[k], S));

@@ -87,6 +87,11 @@ struct PgDev
   int *tev_first;           // [parnum+1] CSR of torsion torque flush events per particle
   int4 *tev;                // (type, begin, end, first) as sev, without long-run chunking
 
+  // ---- prescribed body forces (prescribe_body_forces, parmec.cpp:2202-2224)
+  int pbfnum;
+  int *pbf_slot;            // [parnum] record of the particle, or -1
+  double *pbfout[6], *pbfin[6];   // [pbfnum] outer (added) and inner (exported) force and torque
+
   // ---- spring failure rules (unspring_task, forces.ispc:2058-2127); spring
   // lists hold sorted positions
   int unsprnum;

@@ -1242,6 +1242,21 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       }
     }
 
+    // prescribe_body_forces (parmec.cpp:2202-2224): the particle's force and
+    // torque are exported, then the prescribed ones added
+    if ((MODE == INT_FUSED || MODE == INT_FORCES_ADAPT) && d.pbfnum)
+    {
+      const int q = d.pbf_slot[i];
+      if (q >= 0)
+        for (int c = 0; c < 3; c ++)
+        {
+          d.pbfin[c][q] = F[c];
+          d.pbfin[3+c][q] = T[c];
+          F[c] += d.pbfout[c][q];
+          T[c] += d.pbfout[3+c][q];
+        }
+    }
+
     }
     if (ADAPT)
     {

@@ -8,7 +8,8 @@ from . import abi
 
 def _counts(m):
     return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
-            len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings), m.trqsprnum)
+            len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings), m.trqsprnum,
+            len(m.body_forces))
 
 
 class GpuEngine:
@@ -113,6 +114,7 @@ class GpuEngine:
     def download(self):
         abi.check(self.lib.pg_session_download(self.sess, ctypes.byref(self.scene)), "pg_session_download")
         self.model.pull_obstacles()
+        self.model.pull_body_forces()
 
     def download_rows(self, particles, springs):
         """Only the given particles' and springs' state (pg_session_download_particles/_springs)."""

@@ -113,6 +113,8 @@ class Model:
         self.lcurves = []                   # time series copied as lookup curves (sproffset)
         self.prescribe = []                 # dicts: part, lin, ang, linkind, angkind
         self.restraints = []                # (part, lin[9], ang[9]) orthonormal direction rows
+        self.body_forces = {}               # particle -> outer force xyz, torque xyz (coupling import)
+        self.body_forces_inner = {}         # particle -> inner force xyz, torque xyz (coupling export)
         self.unsprings = []                 # UNSPRING rules (dicts); failure countdowns in unspring_nfreq
         self.unspring_nfreq = np.zeros(1, dtype=np.int32)
         self.gravity = [0.0, 0.0, 0.0]
@@ -445,6 +447,28 @@ class Model:
         self.prescribe.append({"part": parnum, "lin": linear, "ang": angular,
                                "linkind": 0 if kind[0] == "v" else 1,
                                "angkind": 0 if kind[1] == "v" else 1})
+
+    # ---------------------------------------------------- coupling interface
+    def set_body_force(self, particle, force=(0.0, 0.0, 0.0), torque=(0.0, 0.0, 0.0)):
+        """A prescribed body force (struct prescribed_body_force, parmec.h:281-289):
+        each step of the next DEM calls adds 'force' and 'torque' to the
+        particle's after the contact and spring forces, and records the
+        particle's own force and torque before that addition (body_force_inner).
+        None removes the record."""
+        if not (0 <= particle < self.parnum):
+            raise ValueError("'particle' out of range")
+        self._touch()
+        if force is None:
+            self.body_forces.pop(int(particle), None)
+            self.body_forces_inner.pop(int(particle), None)
+            return
+        self.body_forces[int(particle)] = [float(x) for x in force] + [float(x) for x in torque]
+
+    def body_force_inner(self, particle):
+        """(force, torque) of the particle exported at the latest step
+        (prescribe_body_forces, parmec.cpp:2202-2224)."""
+        v = self.body_forces_inner.get(int(particle))
+        return None if v is None else (tuple(v[:3]), tuple(v[3:]))
 
     # ------------------------------------------------------------------ EQM
     def eqm(self, part1, point1, part2=-1, point2=None, direction=None):
@@ -860,6 +884,17 @@ class Model:
         s.unent, s.unop, s.unabs = abi.iptr(unent), abi.iptr(unop), abi.iptr(unabs)
         s.nsteps, s.nfreq, s.unaction = abi.iptr(nsteps), abi.iptr(self.unspring_nfreq), abi.iptr(unaction)
         s.sprmap = abi.iptr(S.sprmap)
+        parts = sorted(self.body_forces)
+        pbfpart = np.array(parts or [0], dtype=np.int32)
+        pbfout = np.ascontiguousarray(np.array([self.body_forces[p] for p in parts] or [[0.0] * 6]).T)
+        if getattr(self, "_pbfin", None) is None or self._pbfin.shape[1] != max(1, len(parts)):
+            self._pbfin = np.zeros((6, max(1, len(parts))))
+        keep += [pbfpart, pbfout]
+        s.pbfnum = len(parts)
+        s.pbfpart = abi.iptr(pbfpart)
+        s.pbfout = abi.rows(pbfout, 6)
+        s.pbfin = abi.rows(self._pbfin, 6)
+        self._pbf_parts = parts
         from .torsion import torsion_tables
         Q = self.Q
         tt = torsion_tables(self)
@@ -889,6 +924,12 @@ class Model:
             s.sactive = abi.iptr(self.sactive)
         s._keep = keep
         return s
+
+    def pull_body_forces(self):
+        """Copy the exported inner forces of the last scene() into body_forces_inner."""
+        parts = getattr(self, "_pbf_parts", [])
+        for k, p in enumerate(parts):
+            self.body_forces_inner[p] = [float(x) for x in self._pbfin[:, k]]
 
     def pull_obstacles(self):
         """Copy obstacle point/velocity state from the flat views of the last scene()."""
