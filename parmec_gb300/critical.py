@@ -152,14 +152,13 @@ def _contact_terms(m, contacts, kact, kmax, emax, krot):
     # normal stiffness and damping of each contact (forces.ispc:125-147)
     coli = E.ellcol[pell[mp]]
     colj = np.where(sph, E.ellcol[np.maximum(code, 0)], m.Tr.tricol[np.maximum(-code - 1, 0)])
-    kc = np.empty(n)
-    ec = np.empty(n)
-    for c in range(n):
-        ij = pairing(m, int(coli[c]), int(colj[c]))
-        kn = m.iparam[ij][0]
-        ma = 1.0 / (P.invm[mp[c]] + P.invm[pj[c]]) if pj[c] >= 0 else P.mass[mp[c]]
-        kc[c] = kn
-        ec[c] = m.iparam[ij][1] * 2.0 * math.sqrt(kn * ma)
+    uniq, inv = np.unique(np.stack([coli, colj]), axis=1, return_inverse=True)
+    pair = np.array([pairing(m, int(a), int(b)) for a, b in uniq.T], dtype=np.int64)[inv.reshape(-1)]
+    ipar = np.array(m.iparam, dtype=np.float64)
+    kc = ipar[pair, 0]
+    with np.errstate(divide="ignore"):
+        ma = np.where(pj >= 0, 1.0 / (P.invm[mp] + P.invm[np.maximum(pj, 0)]), P.mass[mp])
+    ec = ipar[pair, 1] * 2.0 * np.sqrt(kc * ma)
     L = P.rotation[:, mp]
     for k in range(3):
         np.add.at(kact[k], mp, np.abs(nrm[k]))
@@ -222,51 +221,108 @@ def _spring_terms(m, kact, kmax, emax, krot):
             emax[p] = max(emax[p], espr)
 
 
+def _triple_angle_root_v(r, largest):
+    """_triple_angle_root over arrays, element by element the same operations."""
+    r = np.clip(r, -1.0, 1.0)
+    c = np.full(r.shape, 1.0 if largest else -1.0)
+    live = np.ones(r.shape, dtype=bool)
+    for _ in range(100):
+        if not live.any():
+            break
+        f = (4.0 * c * c - 3.0) * c - r
+        den = 12.0 * c * c - 3.0
+        with np.errstate(divide="ignore", invalid="ignore"):
+            cn = c - f / den
+        step = (cn < c) if largest else (cn > c)
+        live &= step & (den != 0.0)
+        c = np.where(live, cn, c)
+    return c
+
+
+def _extremum_eigenvalue_v(A, minimum):
+    """_extremum_eigenvalue over arrays A[9][n]."""
+    p1 = A[3] * A[3] + A[6] * A[6] + A[7] * A[7]
+    diag = np.maximum(np.maximum(A[0], A[4]), A[8])
+    q = (A[0] + A[4] + A[8]) / 3.0
+    p2 = (A[0] - q) * (A[0] - q) + (A[4] - q) * (A[4] - q) + (A[8] - q) * (A[8] - q) + 2 * p1
+    with np.errstate(divide="ignore", invalid="ignore"):
+        p = np.sqrt(p2 / 6.0)
+        invp = 1.0 / p
+        B = [invp * (A[0] - q), invp * A[1], invp * A[2], invp * A[3], invp * (A[4] - q), invp * A[5],
+             invp * A[6], invp * A[7], invp * (A[8] - q)]
+        det = (B[0] * (B[4] * B[8] - B[5] * B[7]) + B[3] * (B[2] * B[7] - B[1] * B[8])
+               + B[6] * (B[1] * B[5] - B[2] * B[4]))
+        gen = q + 2.0 * p * _triple_angle_root_v(np.where(p1 == 0.0, 0.0, 0.5 * det), not minimum)
+    return np.where(p1 == 0.0, diag, gen)
+
+
 def _time_steps(m, kact, kmax, emax, krot):
-    """time_step_task (parmec.ispc:275-383) for every particle."""
+    """time_step_task (parmec.ispc:275-383) for every particle, over arrays."""
     P = m.P
     n = m.parnum
+    nxyz = np.maximum(np.maximum(kact[0], kact[1]), kact[2])
+    live = nxyz > 0.0
     h = np.full(n, REAL_MAX)
     om = np.zeros(n)
     ra = np.zeros(n)
-    for i in range(n):
-        nxyz = max(max(kact[0][i], kact[1][i]), kact[2][i])
-        if not (nxyz > 0.0):
-            continue
-        k = kmax[i]
-        mxyz = P.mass[i]
-        omegaxyz = math.sqrt(nxyz * k / mxyz)
-        K = [k * krot[0][i], k * krot[3][i], k * krot[4][i], 0.0, k * krot[1][i], k * krot[5][i], 0.0, 0.0,
-             k * krot[2][i]]
-        K[3], K[6], K[7] = K[1], K[2], K[5]
-        J = [float(x) for x in P.inertia[:, i]]
-        mrot = _extremum_eigenvalue(J, 1)
-        L = [0.0] * 9
-        L[0] = math.sqrt(J[0])
-        inv = 1.0 / L[0]
-        L[1] = inv * J[1]
-        L[2] = inv * J[2]
-        L[4] = math.sqrt(J[4] - L[1] * L[1])
-        inv = 1.0 / L[4]
-        L[5] = inv * (J[5] - L[2] * L[1])
-        L[8] = math.sqrt(J[8] - (L[2] * L[2] + L[5] * L[5]))
-        invL = _invert(L)
-        A = _nnmul(invL, _ntmul(K, invL))
-        lam = _extremum_eigenvalue(A, 0)
-        # no rotational stiffness: the reference divides by zero here
-        omegarot = math.sqrt(lam) if lam > 0.0 else 0.0
-        damping = emax[i]
-        ratioxyz = damping / (2.0 * mxyz * omegaxyz)
-        hxyz = (2.0 / omegaxyz) * (math.sqrt(1.0 + ratioxyz * ratioxyz) - ratioxyz)
-        if omegarot > 0.0:
-            ratiorot = damping / (2.0 * mrot * omegarot)
-            hrot = (2.0 / omegarot) * (math.sqrt(1.0 + ratiorot * ratiorot) - ratiorot)
-        else:
-            ratiorot, hrot = 0.0, REAL_MAX
-        h[i] = min(hxyz, hrot)
-        om[i] = max(omegaxyz, omegarot)
-        ra[i] = max(ratioxyz, ratiorot)
+    if not live.any():
+        return h, om, ra
+    ix = np.nonzero(live)[0]
+    k = kmax[ix]
+    mxyz = P.mass[ix]
+    omegaxyz = np.sqrt(nxyz[ix] * k / mxyz)
+    K = [k * krot[0][ix], k * krot[3][ix], k * krot[4][ix], None, k * krot[1][ix], k * krot[5][ix], None, None,
+         k * krot[2][ix]]
+    K[3], K[6], K[7] = K[1], K[2], K[5]
+    J = [P.inertia[c, ix] for c in range(9)]
+    mrot = _extremum_eigenvalue_v(J, 1)
+    z = np.zeros(len(ix))
+    L = [z] * 9
+    L[0] = np.sqrt(J[0])
+    inv = 1.0 / L[0]
+    L[1] = inv * J[1]
+    L[2] = inv * J[2]
+    L[4] = np.sqrt(J[4] - L[1] * L[1])
+    inv = 1.0 / L[4]
+    L[5] = inv * (J[5] - L[2] * L[1])
+    L[8] = np.sqrt(J[8] - (L[2] * L[2] + L[5] * L[5]))
+    invL = _invert_v(L)
+    A = _nnmul_v(invL, _ntmul_v(K, invL))
+    lam = _extremum_eigenvalue_v(A, 0)
+    omegarot = np.where(lam > 0.0, np.sqrt(np.maximum(lam, 0.0)), 0.0)
+    damping = emax[ix]
+    ratioxyz = damping / (2.0 * mxyz * omegaxyz)
+    hxyz = (2.0 / omegaxyz) * (np.sqrt(1.0 + ratioxyz * ratioxyz) - ratioxyz)
+    rot = omegarot > 0.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ratiorot = np.where(rot, damping / (2.0 * mrot * omegarot), 0.0)
+        hrot = np.where(rot, (2.0 / omegarot) * (np.sqrt(1.0 + ratiorot * ratiorot) - ratiorot), REAL_MAX)
+    h[ix] = np.minimum(hxyz, hrot)
+    om[ix] = np.maximum(omegaxyz, omegarot)
+    ra[ix] = np.maximum(ratioxyz, ratiorot)
     return h, om, ra
+
+
+def _invert_v(F):
+    det = F[0] * (F[4] * F[8] - F[5] * F[7]) + F[3] * (F[2] * F[7] - F[1] * F[8]) + (F[1] * F[5] - F[2] * F[4]) * F[6]
+    ok = det != 0.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        det = np.where(ok, 1.0 / np.where(ok, det, 1.0), 0.0)
+    return [(F[4] * F[8] - F[5] * F[7]) * det, (F[2] * F[7] - F[1] * F[8]) * det, (F[1] * F[5] - F[2] * F[4]) * det,
+            (F[5] * F[6] - F[3] * F[8]) * det, (F[0] * F[8] - F[2] * F[6]) * det, (F[2] * F[3] - F[0] * F[5]) * det,
+            (F[3] * F[7] - F[4] * F[6]) * det, (F[1] * F[6] - F[0] * F[7]) * det, (F[0] * F[4] - F[1] * F[3]) * det]
+
+
+def _nnmul_v(A, B):
+    C = [None] * 9
+    for c in range(3):
+        for r in range(3):
+            C[3 * c + r] = A[r] * B[3 * c] + A[3 + r] * B[3 * c + 1] + A[6 + r] * B[3 * c + 2]
+    return C
+
+
+def _ntmul_v(A, B):
+    return _nnmul_v(A, [B[0], B[3], B[6], B[1], B[4], B[7], B[2], B[5], B[8]])
 
 
 def critical_perparticle(m, contacts=None):
