@@ -176,6 +176,18 @@ def download_for_history(m, eng):
         eng.download()
 
 
+def output_files_now(m, eng, t, downloaded=False):
+    """output_files (output.cpp:5127-5140) at time t; downloads the state first
+    when a file format this build writes (DUMP, VTK) is selected.  Returns
+    whether the host arrays were brought up to date."""
+    from .output import OUT_FORMAT_DUMP, OUT_FORMAT_VTK, output_files
+    writes = bool(m.out.format & (OUT_FORMAT_DUMP | OUT_FORMAT_VTK))
+    if writes and not downloaded:
+        eng.download()
+    output_files(m, t)
+    return writes
+
+
 def sample_history(m, t):
     """output_history (output.cpp:5143-5533) for list sources."""
     P, S = m.P, m.S
@@ -289,6 +301,7 @@ def run_dem(m, duration, step, interval, engine, adaptive=0.0):
 
     if m.curtime == 0.0:
         step0 = step
+        output_files_now(m, eng, m.curtime, downloaded=True)
         sample_history(m, m.curtime)
         a, l = obstaclev(m, 0.5 * step0)
         eng.first_half_step(step0, a, l)
@@ -304,19 +317,32 @@ def run_dem(m, duration, step, interval, engine, adaptive=0.0):
     times, end_time = step_times(m.curtime, duration, step0)
     tabs = StepTables(m, times, step0, list(dt), dt_func, dt_tms)
 
-    # history cadence: sample after step k when t_k >= curtime_history + interval[1]
+    # output and history cadence (parmec.cpp:2482-2511): after step k, files
+    # when t_k >= curtime_output + interval[0], a history sample when
+    # t_k >= curtime_history + interval[1]
     cuts = []
-    ch = m.curtime_history
+    co, ch = m.curtime_output, m.curtime_history
     for k, t in enumerate(times):
-        if t >= ch + tabs.interval[k, 1]:
-            cuts.append(k)
+        o = t >= co + tabs.interval[k, 0]
+        if o:
+            co += tabs.interval[k, 0]
+        h = t >= ch + tabs.interval[k, 1]
+        if h:
             ch += tabs.interval[k, 1]
+        if o or h:
+            cuts.append((k, o, h))
     b = 0
-    for k in cuts:
+    for k, o, h in cuts:
         eng.run(tabs.ctab(b, k + 1), step0)
-        download_for_history(m, eng)
-        sample_history(m, times[k])
-        m.curtime_history += tabs.interval[k, 1]
+        got = False
+        if o:
+            got = output_files_now(m, eng, times[k])
+            m.curtime_output += tabs.interval[k, 0]
+        if h:
+            if not got:
+                download_for_history(m, eng)
+            sample_history(m, times[k])
+            m.curtime_history += tabs.interval[k, 1]
         b = k + 1
     if b < len(times):
         eng.run(tabs.ctab(b, len(times)), step0)
@@ -339,8 +365,13 @@ def _run_adaptive(m, eng, duration, step0, adaptive, dt, dt_func, dt_tms, t_star
     while t < duration:
         tabs = StepTables(m, [ct], step0, dtl, dt_func, dt_tms)
         step1 = float(eng.run_adaptive(tabs.ctab(0, 1), step0, adaptive)[0])
+        got = False
+        if ct >= m.curtime_output + tabs.interval[0, 0]:
+            got = output_files_now(m, eng, ct)
+            m.curtime_output += tabs.interval[0, 0]
         if ct >= m.curtime_history + tabs.interval[0, 1]:
-            download_for_history(m, eng)
+            if not got:
+                download_for_history(m, eng)
             sample_history(m, ct)
             m.curtime_history += tabs.interval[0, 1]
         inc = 0.5 * (step0 + step1)

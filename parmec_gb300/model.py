@@ -14,6 +14,7 @@ VELOCITY, DAMPING, ANALYTICAL, RESET and CRITICAL(perspring=...), which decks
 built from them need.
 """
 import math
+import os
 import time as _time
 
 import numpy as np
@@ -125,6 +126,8 @@ class Model:
         self.angdamptms = [-1, -1, -1]
         self.damping = [0.0] * 6
         self.histories = []
+        from .output import OutputState
+        self.out = OutputState()            # OUTPUT settings and frame counter
         self.curtime = 0.0
         self.curstep = 0.0
         self.curtime_history = 0.0
@@ -952,6 +955,11 @@ class Model:
             raise ValueError("'step' must be positive")
         if not (0.0 <= adaptive <= 1.0):
             raise ValueError("'adaptive' must be in [0, 1]")
+        if prefix is not None:
+            # the output path keeps its directory and takes the prefix as its name (parmec.cpp:2328-2343)
+            from .output import default_path
+            base = self.out.path if self.out.path is not None else default_path()
+            self.out.path = os.path.join(os.path.dirname(base), str(prefix))
         return run_dem(self, float(duration), float(step), interval, engine, float(adaptive))
 
 

@@ -109,8 +109,9 @@ def CRITICAL(perspring=-1, perparticle=-1):
 
 
 def OUTPUT(entities=None, subset=None, mode=None, format=None):
-    """OUTPUT (input.cpp:3560): accepted; file output (VTK/XDMF/MED) is not written by this build."""
-    return 0
+    """OUTPUT (input.cpp:3560-3955): entities, particle subset, modes and file formats."""
+    from .output import output_command
+    return output_command(_model, entities, subset, mode, format)
 
 
 def ARGV():
@@ -131,6 +132,8 @@ def run_deck(path, argv=None):
     """parmec::input (input.cpp:4133-4196): execute a deck with the commands as globals."""
     if argv is not None:
         sys.argv = [path] + list(argv)
+    if path.endswith(".py"):
+        _model.out.path = path[:-3]                   # output_path (input.cpp:4141-4155)
     g = {name: globals()[name] for name in COMMANDS}
     g["__name__"] = "__main__"
     g["__file__"] = path
