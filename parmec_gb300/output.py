@@ -12,10 +12,10 @@ The XDMF (the reference's default) and MED formats need the HDF5 and MED
 libraries, which this build does not have: a DEM with only those formats
 selected writes no files and says so once.  Positions taken:
 * the unselected-spring test reads flags & OUTREST (the reference writes
-  flags && OUTREST, output.cpp:4556, 4621, selecting every spring);
+  flags && OUTREST, output.cpp:4553, 4625, selecting every spring);
 * OUTPUT's RB/CD/SL/ST/JT modes without a subset set the unselected
   particles' modes (the reference writes outmode[1] or outmode[i] there,
-  input.cpp:3653-3671).
+  input.cpp:3654-3669, 3701-3721).
 """
 import os
 import sys
