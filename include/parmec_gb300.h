@@ -390,6 +390,13 @@ int pg_session_upload_range(pg_session *s, const pg_scene *scene, const int rang
 /* Copy the same ranges of the dynamic state back to the host scene. */
 int pg_session_download_range(pg_session *s, pg_scene *scene, const int range[8]);
 
+/* Free the same ranges in a pool: their particles, spheres, triangles and
+ * obstacles get scene id -1, which every kernel skips, and the spheres'
+ * candidate lists restart empty.  Only device scene ids change: the state
+ * arrays keep their values until the next upload of the ranges.  No
+ * counterpart in the reference, which runs one scene per process. */
+int pg_session_release_range(pg_session *s, const int range[8]);
+
 /* Steps the session has run so far. */
 int pg_session_global_step(pg_session *s, long long *step);
 

@@ -28,6 +28,7 @@ struct pg_session
   size_t ncells = 0;
   int prs_stride = 3, obs_stride = 3;
   std::vector<int> h_pell;
+  std::vector<int> h_part;                 // sphere -> particle map the device's eorder was built from
   // per kernel group timing with CUDA events on the session stream
   int profile = 0;
   cudaEvent_t ev[8] = {};
@@ -477,14 +478,23 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     for (size_t p = p0; p < p1; p ++) s->h_pell[p] = pell[p - p0];
     TRY(h2dr(s, d.pell, s->h_pell.data(), p0, p1));
   }
-  // spheres in particle order (stable): the order of the slave-list entries
+  // spheres in particle order (stable): the order of the slave-list entries.
+  // It depends on the sphere -> particle map alone, so a range upload that
+  // leaves the map as it was (a pooled scene loaded into its own ranges)
+  // keeps the order already on the device.
   if (d.ellnum)
   {
-    std::vector<int> ord(d.ellnum);
-    for (int e = 0; e < d.ellnum; e ++) ord[e] = e;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return sc->part[a] < sc->part[b]; });
-    TRY(h2d(s, d.eorder, ord.data(), ord.size()));
-    CK(cudaStreamSynchronize(s->stream));         // ord is a local
+    bool same = !global && s->h_part.size() == (size_t)d.ellnum;
+    for (size_t e = e0; same && e < e1; e ++) same = s->h_part[e] == sc->part[e];
+    if (!same)
+    {
+      s->h_part.assign(sc->part, sc->part + d.ellnum);
+      std::vector<int> ord(d.ellnum);
+      for (int e = 0; e < d.ellnum; e ++) ord[e] = e;
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return s->h_part[a] < s->h_part[b]; });
+      TRY(h2d(s, d.eorder, ord.data(), ord.size()));
+      CK(cudaStreamSynchronize(s->stream));         // ord is a local
+    }
   }
   // triangle -> moving obstacle for the triangles of the range
   {
@@ -494,19 +504,20 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
         if (t >= 0 && t < d.trinum) own[t] = o;
     TRY(h2dr(s, d.triown, own.data(), t0, t1));
   }
-  // scenes
+  // scenes (host vectors hold the ranges only)
   {
-    std::vector<int> ps(d.parnum, 0), es(d.ellnum, 0), ts(d.trinum, 0), os(d.obsnum, 0);
+    std::vector<int> ps(p1 - p0, 0), es(e1 - e0, 0), ts(t1 - t0, 0), os(o1 - o0, 0);
     const bool many = sc->nscene > 0;
-    for (size_t p = p0; p < p1; p ++) ps[p] = many ? sc->pscene[p] : 0;
-    for (size_t e = e0; e < e1; e ++) es[e] = many ? sc->pscene[sc->part[e]] : 0;   // -1: no scene
-    for (size_t t = t0; t < t1; t ++) ts[t] = many ? sc->tscene[t] : 0;
-    for (size_t o = o0; o < o1; o ++) os[o] = many ? sc->oscene[o] : 0;
-    TRY(h2dr(s, d.pscene, ps.data(), p0, p1));
-    TRY(h2dr(s, d.escene, es.data(), e0, e1));
-    TRY(h2dr(s, d.tscene, ts.data(), t0, t1));
-    TRY(h2dr(s, d.oscene, os.data(), o0, o1));
+    for (size_t p = p0; p < p1; p ++) ps[p - p0] = many ? sc->pscene[p] : 0;
+    for (size_t e = e0; e < e1; e ++) es[e - e0] = many ? sc->pscene[sc->part[e]] : 0;   // -1: no scene
+    for (size_t t = t0; t < t1; t ++) ts[t - t0] = many ? sc->tscene[t] : 0;
+    for (size_t o = o0; o < o1; o ++) os[o - o0] = many ? sc->oscene[o] : 0;
+    TRY(h2d(s, d.pscene + p0, ps.data(), ps.size()));
+    TRY(h2d(s, d.escene + e0, es.data(), es.size()));
+    TRY(h2d(s, d.tscene + t0, ts.data(), ts.size()));
+    TRY(h2d(s, d.oscene + o0, os.data(), os.size()));
     TRY(scene_triangle_ranges(s, sc));
+    CK(cudaStreamSynchronize(s->stream));           // the vectors are locals
   }
   // a newly loaded scene's spheres start with empty candidate lists; a
   // re-upload of the same scene keeps its contacts and their state
@@ -762,6 +773,7 @@ int contact_buffers(pg_session *s)
   TRY(dalloc(s, &d.rcnt, P));
   TRY(dalloc(s, &d.soff, P + 1));
   TRY(dalloc(s, &d.eorder, E));
+  s->h_part.clear();                              // eorder is rebuilt at the next upload
   TRY(dalloc(s, &d.eoff, E + 1));
   TRY(dalloc(s, &d.smeta, 4));
   d.sbits = pg_rebuild_entry_bits((int)P);
@@ -1589,6 +1601,24 @@ int pg_session_upload_range(pg_session *s, const pg_scene *sc, const int range[8
   Ranges r;
   TRY(ranges_of(s->d, range, &r));
   TRY(upload_ranges(s, sc, r, false, true));
+  CK(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_session_release_range(pg_session *s, const int range[8])
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  Ranges r;
+  TRY(ranges_of(d, range, &r));
+  // scene id -1 (all bits set) marks a free entry, which every kernel skips
+  if (r.p1 > r.p0) CK(cudaMemsetAsync(d.pscene + r.p0, 0xff, (r.p1 - r.p0) * sizeof(int), s->stream));
+  if (r.e1 > r.e0) CK(cudaMemsetAsync(d.escene + r.e0, 0xff, (r.e1 - r.e0) * sizeof(int), s->stream));
+  if (r.t1 > r.t0) CK(cudaMemsetAsync(d.tscene + r.t0, 0xff, (r.t1 - r.t0) * sizeof(int), s->stream));
+  if (r.o1 > r.o0) CK(cudaMemsetAsync(d.oscene + r.o0, 0xff, (r.o1 - r.o0) * sizeof(int), s->stream));
+  if (r.e1 > r.e0) CK(cudaMemsetAsync(d.ncnt + r.e0, 0, (r.e1 - r.e0) * sizeof(int), s->stream));
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
   CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }

@@ -161,6 +161,11 @@ class GpuEngine:
                   "pg_session_download_range")
         self.model.pull_obstacles()
 
+    def release_range(self, r):
+        """Free pool ranges on the device: scene id -1 for their entries."""
+        rr = np.ascontiguousarray(r, dtype=np.int32)
+        abi.check(self.lib.pg_session_release_range(self.sess, abi.iptr(rr)), "pg_session_release_range")
+
     def scene_refresh(self):
         """Re-point the ctypes scene at the model's arrays (after host edits)."""
         self.scene = self.model.scene()

@@ -16,6 +16,44 @@ import numpy as np
 from .model import Model
 
 
+_LN2_HI = 6.93147180369123816490e-01     # ln 2 split so that k * _LN2_HI is exact for |k| < 2^20
+_LN2_LO = 1.90821492927058770002e-10
+
+
+def exp_ieee(x):
+    """exp of a float64 array from +, -, *, / and ldexp only, so that scene
+    inputs are the same bits on every IEEE-754 host (vectorised libm exp
+    differs in the last bit between x86 and Arm builds of numpy).  Cody-Waite
+    reduction x = k ln 2 + r, |r| <= ln(2)/2, then the Taylor series of e^r to
+    the 20th power in Horner form (truncation below 1e-28)."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x / 0.6931471805599453)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.ones_like(r)
+    for n in range(20, 0, -1):
+        p = 1.0 + p * r / n
+    return np.ldexp(p, k.astype(np.int64))
+
+
+def log_ieee(x):
+    """Natural log of a positive float (scalar) from basic operations only:
+    x = m 2^e with m in [1/sqrt 2, sqrt 2), ln x = e ln 2 + 2 atanh((m-1)/(m+1))."""
+    m, e = math.frexp(float(x))
+    if m < 0.7071067811865476:
+        m, e = 2.0 * m, e - 1
+    t = (m - 1.0) / (m + 1.0)
+    t2, term, acc = t * t, t, 0.0
+    for n in range(1, 60, 2):
+        acc += term / n
+        term *= t2
+    return (e * _LN2_HI + 2.0 * acc) + e * _LN2_LO
+
+
+def log_uniform(rng, lo, hi, size):
+    """Log-uniform draws in [lo, hi] with exp_ieee/log_ieee (host-independent bits)."""
+    return exp_ieee(rng.uniform(log_ieee(lo), log_ieee(hi), size=size))
+
+
 def critical_step(kn, m_min, xi):
     """Single-contact critical step h = (2/w)(sqrt(1+xi^2) - xi), w = sqrt(kn/m)
     (the LS-DYNA form used by parmec.ispc:300-379)."""
@@ -99,7 +137,7 @@ def drum(n=1048576, seed=1, radius=0.5, length=0.3, rmin=0.5e-3, rmax=2e-3, dens
     fraction of the bed and the initial contact count are reported in `info`.
     """
     rng = np.random.default_rng(seed)
-    r = np.exp(rng.uniform(math.log(rmin), math.log(rmax), size=n))
+    r = log_uniform(rng, rmin, rmax, n)
     r = np.sort(r)[::-1]
     centers = np.zeros((n, 3))
     half = 0.5 * length - rmax
@@ -165,7 +203,7 @@ def batch_scenes(count=512, seed=3, nmin=2048, nmax=65536):
     """Config 3: `count` shaken boxes with sphere counts log-uniform in
     [nmin, nmax], base excitation f ~ U[1,20] Hz, amplitude ~ U[0.1,1] g."""
     rng = np.random.default_rng(seed)
-    ns = np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=count))
+    ns = log_uniform(rng, nmin, nmax, count)
     fs = rng.uniform(1.0, 20.0, size=count)
     amps = rng.uniform(0.1, 1.0, size=count)
     out = []

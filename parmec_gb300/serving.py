@@ -199,7 +199,7 @@ class Server:
         self.eng.set_scene(slot, False)
         P.pscene[e0:e1] = -1
         P.tscene[t0:t1] = -1
-        self.eng.upload_range(r)
+        self.eng.release_range(r)
         self.spheres.give(e0, e1 - e0)
         self.tris.give(t0, t1 - t0)
         self.slots.append(slot)
