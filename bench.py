@@ -473,6 +473,18 @@ def main():
     # (profiles/k_integrate_k_contacts_drum_fp64.md) scaled by the units processed
     traffic_per_unit = {"integrate": 456.0, "contacts": 200.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
+    # FP64 pipe: thread-level FP64 instructions (DADD + DMUL + DFMA) per unit,
+    # counted by ncu on the same capture; peak = 2 per clock per SM
+    fp64_per_unit = {"integrate": 312.0, "contacts": 161.0}
+    fp64 = None
+    if dom in fp64_per_unit:
+        sm_mhz = clk.get("sm_mhz") or 2070.0
+        peak_g = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * sm_mhz * 1e6 / 1e9
+        ach_g = fp64_per_unit[dom] * P / (ms_dom * 1e-3 / args.steps) / 1e9
+        fp64 = {"kernel": dom, "ops_per_unit": fp64_per_unit[dom], "achieved": ach_g, "peak": peak_g,
+                "unit": "G FP64 inst/s", "frac": ach_g / peak_g,
+                "source": "ops per unit from ncu (profiles/k_integrate_k_contacts_drum_fp64.md); "
+                          "peak 2 FP64 lanes/clk/SM at the sampled SM clock"}
     if bytes_dom is not None:
         avg_s = ms_dom * 1e-3 / args.steps
         achieved = bytes_dom / avg_s / 1e9
@@ -501,7 +513,8 @@ def main():
                      "traffic": traffic, "traffic_source": "ncu 262,144-sphere capture scaled per unit",
                      "peak_source": peak_kind,
                      "step_algorithmic_gbs": step_gbs, "step_frac": step_gbs / hbm,
-                     "note": "FP64-ALU bound on GB300 (2 DFMA/clk/SM); see profiles/"},
+                     "note": "FP64-ALU bound on GB300 (2 DFMA/clk/SM): see fp64_pipe and profiles/"},
+        "fp64_pipe": fp64,
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in groups.items()},
         "clocks": clk,
     }
