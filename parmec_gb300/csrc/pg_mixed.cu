@@ -28,6 +28,12 @@ namespace {
 
 constexpr int TPB = 128;
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+// resident blocks per SM asked of the register allocator for the per-phase
+// contact and integration kernels (latency-bound gathers: more resident
+// warps keep more loads in flight)
+#ifndef PG_MX_MIN_BLOCKS
+#define PG_MX_MIN_BLOCKS 8
+#endif
 
 __device__ __forceinline__ void set_err(const PgDev &d, int code, int site, int index, int value)
 {
@@ -353,7 +359,7 @@ __device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double s
   for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
 }
 
-__global__ void __launch_bounds__(TPB) k_contacts_mx(PgDev d, double step_d)
+__global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_contacts_mx(PgDev d, double step_d)
 {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ellnum) mx_contacts_item(d, i, step_d);
@@ -518,7 +524,7 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
   return need;
 }
 
-__global__ void __launch_bounds__(TPB) k_integrate_mx(PgDev d, double step_d)
+__global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_integrate_mx(PgDev d, double step_d)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;

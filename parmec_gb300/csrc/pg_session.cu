@@ -479,12 +479,13 @@ int upload_ranges(pg_session *s, const pg_scene *sc, Ranges r, bool global, bool
     TRY(h2dr(s, d.pell, s->h_pell.data(), p0, p1));
   }
   // spheres in particle order (stable): the order of the slave-list entries.
-  // It depends on the sphere -> particle map alone, so a range upload that
-  // leaves the map as it was (a pooled scene loaded into its own ranges)
-  // keeps the order already on the device.
+  // It depends on the sphere -> particle map alone, so an upload that leaves
+  // the map of its range as it was (the next DEM call of the same model, a
+  // pooled scene loaded into its own ranges) keeps the order already on the
+  // device.
   if (d.ellnum)
   {
-    bool same = !global && s->h_part.size() == (size_t)d.ellnum;
+    bool same = s->h_part.size() == (size_t)d.ellnum;
     for (size_t e = e0; same && e < e1; e ++) same = s->h_part[e] == sc->part[e];
     if (!same)
     {
