@@ -804,7 +804,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   if (U) { pg_launch_unspring(v, G.st); G.launches += 1; }
   if (adaptive) pg_launch_force_sums_adapt(v, G.st);
   else pg_launch_force_sums(v, G.st);
-  G.launches += (v.ellnum ? 1 : 0) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 2 : 1) : 0) + 1;
+  G.launches += pg_contacts_kernel_count(v) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 2 : 1) : 0) + 1;
   for (int k = 0; ok && k < 3; k ++) ok = down(force[k], d.force[k], P) && down(torque[k], d.torque[k], P);
   if (adaptive)
   {

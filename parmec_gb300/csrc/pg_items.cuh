@@ -60,6 +60,46 @@ __device__ __forceinline__ unsigned order_key(int code)
   return code >= 0 ? (unsigned)code : 0x80000000u + (unsigned)(-code - 1);
 }
 
+// ================================================================ triangle work queue
+// The contact kernels evaluate a sphere's sphere partners in one pass and
+// queue the spheres whose lists go on with triangles (order_key puts them
+// last); a second pass evaluates those triangles, one thread per queued
+// sphere, so that the long triangle code runs on full warps.
+
+// every thread of the warp calls this; `more`: sphere i has triangles
+__device__ __forceinline__ void tri_queue_push(const PgDev &d, bool more, int i)
+{
+  const unsigned m = __ballot_sync(0xffffffffu, more);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+  int base = 0;
+  if (lane == lead) base = atomicAdd(&d.tcnt[0], __popc(m));
+  base = __shfl_sync(0xffffffffu, base, lead);
+  if (more) d.twork[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// queue length, read at the start of the triangle pass
+__device__ __forceinline__ int tri_queue_len(const PgDev &d) { return *(volatile int *)&d.tcnt[0]; }
+
+// every thread of the block calls this after its triangles; the last block
+// of the grid empties the queue for the next step
+__device__ __forceinline__ void tri_queue_done(const PgDev &d)
+{
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    __threadfence();
+    if (atomicAdd(&d.tcnt[1], 1) == (int)gridDim.x - 1)
+    {
+      d.tcnt[0] = 0;
+      d.tcnt[1] = 0;
+      __threadfence();
+    }
+  }
+}
+
+constexpr int TRI_PASS_BLOCKS = 4 * 152;   // grid of the triangle pass (grid-stride over the queue)
+
 // ================================================================ cell keys and radix sort
 struct Grid { double org[3]; double cell; int dim[3]; };
 

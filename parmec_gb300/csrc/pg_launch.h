@@ -11,6 +11,7 @@ void pg_launch_euler(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_shapes(const PgDev &d, cudaStream_t s, bool skip_analytical);
 void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step);   // velocities from obsang/obslin
 void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step);
+int pg_contacts_kernel_count(const PgDev &d);   // launches of one contact evaluation (either form)
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step);
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s);     // sums of the long flush runs
 void pg_launch_unspring(const PgDev &d, cudaStream_t s);        // UNSPRING rules, after the springs

@@ -12,6 +12,22 @@ namespace pg {
 
 PG_DEV double dot3(const double *a, const double *b) { return a[0]*b[0] + a[1]*b[1] + a[2]*b[2]; }
 
+// Comparisons on the integer pipe.  GB300 issues FP64 instructions, DSETP
+// included, at 2 lanes per clock per SM; these give the truth values of the
+// FP64 comparisons they stand for, from the bit patterns.
+PG_DEV unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+PG_DEV bool nan_bits(unsigned long long b) { return (b & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
+PG_DEV bool finite_d(double x) { return ((dbits(x) >> 52) & 0x7ff) != 0x7ff; }
+// x != 0.0 (true for NaN, as the FP64 comparison)
+PG_DEV bool nonzero_d(double x) { return (dbits(x) << 1) != 0; }
+// a > b where each of a and b is +0, positive or NaN (never negative or -0,
+// as a sum of squares or a square): IEEE order is the bit patterns' order
+PG_DEV bool gt_nonneg(double a, double b)
+{
+  const unsigned long long ua = dbits(a), ub = dbits(b);
+  return !nan_bits(ua) && !nan_bits(ub) && ua > ub;
+}
+
 // NVMUL: C = A*B, A column-major 3x3
 PG_DEV void nvmul(const double *A, const double *B, double *C)
 {
@@ -71,7 +87,7 @@ PG_DEV void expmap(double O1, double O2, double O3, double *L, bool typo)
   v1 = O2 * O2;
   v2 = O3 * O3;
   angsq = v0 + v1 + v2;
-  if (angsq < 3.0461741978671E-02)
+  if (gt_nonneg(3.0461741978671E-02, angsq))
   {
     sx = 1.0 +
       (-1.666666666666667E-1 +

@@ -88,6 +88,23 @@ __device__ __forceinline__ void tvmul_f(const float *A, const float *B, float *C
   C[2] = A[6]*B[0]+A[7]*B[1]+A[8]*B[2];
 }
 
+// C = M B for the inertia tensor (or its inverse) of particle i: an isotropic
+// body (a sphere, scalar s != 0) multiplies by s; any other body reads its
+// FP32 tensor at each product, so no 3x3 tensor stays live in registers
+__device__ __forceinline__ void inertia_mul(float s, float *const M[9], int i, const float *B, float *C)
+{
+  if (s != 0.0f)
+  {
+    C[0] = s*B[0]; C[1] = s*B[1]; C[2] = s*B[2];
+  }
+  else
+  {
+    C[0] = M[0][i]*B[0]+M[3][i]*B[1]+M[6][i]*B[2];
+    C[1] = M[1][i]*B[0]+M[4][i]*B[1]+M[7][i]*B[2];
+    C[2] = M[2][i]*B[0]+M[5][i]*B[1]+M[8][i]*B[2];
+  }
+}
+
 __device__ __forceinline__ int pairing(const PgDev &d, int i, int j)
 {
   int p0 = i, p1 = j, start = 1, end = d.pairnum;
@@ -203,12 +220,24 @@ __global__ void k_mx_to64(PgDev d, int p0, int p1)
 }
 
 // ------------------------------------------------------------ contacts
-__device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double step_d)
+// A sphere's candidate list holds its sphere partners first, then its
+// triangles (order_key).  PASS selects the entries one call evaluates:
+//   MX_SPHERES   the sphere partners; returns whether triangles follow;
+//   MX_TRIANGLES the triangles, continuing the sums the sphere pass stored.
+// The force and torque sums take the FP32 additions of a single pass over
+// the list, in the same order.
+constexpr int MX_SPHERES = 1, MX_TRIANGLES = 2;
+
+template <int PASS>
+__device__ __forceinline__ bool mx_contacts_item(const PgDev &d, int i, double step_d)
 {
   const int E = d.ellnum;
   const int pi = d.part[i];
   const int cnt = d.ncnt[i];
+  bool more = false;
   float fs[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
+  if (PASS == MX_TRIANGLES)
+    for (int c = 0; c < 3; c ++) { fs[c] = d.fm_f[c][pi]; ts[c] = d.tm_f[c][pi]; }
   if (cnt > 0)
   {
     const float step = (float)step_d;
@@ -225,10 +254,16 @@ __device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double s
     const df ri = {d.rh[i], d.rl[i]};
     const int coli = d.ellcol[i];
     const float invmi = d.invm_f[pi], massi = d.mass_f[pi];
-    for (int k = 0; k < cnt; k ++)
+    // the triangle pass starts at the first triangle, so that the j-th
+    // triangles of the threads of a warp are evaluated together
+    int k0 = 0;
+    if (PASS == MX_TRIANGLES)
+      while (k0 < cnt && d.ncode[(size_t)k0 * E + i] >= 0) k0 ++;
+    for (int k = k0; k < cnt; k ++)
     {
       const size_t idx = (size_t)k * E + i;
       const int code = d.ncode[idx];
+      if (PASS == MX_SPHERES && code < 0) { more = true; break; }
       const bool existing = d.nflag[idx] != 0;
       float normal[3], armi[3], armj[3] = {0.0f, 0.0f, 0.0f}, depth;
       bool pos, neg;
@@ -357,12 +392,28 @@ __device__ __forceinline__ void mx_contacts_item(const PgDev &d, int i, double s
     }
   }
   for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
+  return more;
 }
 
+// the sphere partners of every sphere; spheres whose lists go on with
+// triangles are queued for k_tri_mx (queue order does not matter: each
+// sphere's triangles are evaluated by one thread, in list order)
 __global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_contacts_mx(PgDev d, double step_d)
 {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ellnum) mx_contacts_item(d, i, step_d);
+  bool more = false;
+  if (i < d.ellnum) more = mx_contacts_item<MX_SPHERES>(d, i, step_d);
+  pgk::tri_queue_push(d, more, i);
+}
+
+// the triangle candidates of the queued spheres, one thread per sphere; the
+// last block to finish resets the queue for the next step
+__global__ void __launch_bounds__(TPB) k_tri_mx(PgDev d, double step_d)
+{
+  const int n = pgk::tri_queue_len(d);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    mx_contacts_item<MX_TRIANGLES>(d, d.twork[q], step_d);
+  pgk::tri_queue_done(d);
 }
 
 // ------------------------------------------------------------ integrate
@@ -417,7 +468,7 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
     }
 
     df x[3], v[3], L[9];
-    float O[3], o[3], Lf[9], J[9], I[9];
+    float O[3], o[3], Lf[9];
     for (int c = 0; c < 3; c ++)
     {
       x[c] = {d.xh[c][i], d.xl[c][i]};
@@ -425,22 +476,13 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
       O[c] = d.Om[c][i];
       o[c] = d.om[c][i];
     }
+    // isotropic bodies (spheres) have js = j, is = 1/j; others js = is = 0
     const float js = d.jiso[i], is = d.iiso[i];
     for (int k = 0; k < 9; k ++)
     {
       L[k] = {d.Lh[k][i], d.Ll[k][i]};
       Lf[k] = L[k].hi;
     }
-    if (js != 0.0f)
-    {
-      // isotropic body (a sphere): J = j*I; the products below give the same
-      // values as with the full matrices, without reading them
-      for (int k = 0; k < 9; k ++) { J[k] = 0.0f; I[k] = 0.0f; }
-      J[0] = J[4] = J[8] = js;
-      I[0] = I[4] = I[8] = is;
-    }
-    else
-      for (int k = 0; k < 9; k ++) { J[k] = d.J_f[k][i]; I[k] = d.I_f[k][i]; }
     if (!(d.flags[i] & PG_FLAG_SKIP))
     {
       const float half = 0.5f * step, hstep = step;
@@ -451,24 +493,24 @@ __device__ __forceinline__ bool mx_integrate_item(const PgDev &d, int i, double 
         float w[3], t[3], Tb[3];
         for (int c = 0; c < 3; c ++) w[c] = damping[3+c] * o[c];
         tvmul_f(Lf, w, t);
-        nvmul_f(J, t, Tb);
+        inertia_mul(js, d.J_f, i, t, Tb);
         nvmul_f(Lf, Tb, t);
         for (int c = 0; c < 3; c ++) T[c] -= t[c];
       }
       float Tb[3], DL[9], A[3], B[3];
       tvmul_f(Lf, T, Tb);
       expmap_f(-half*O[0], -half*O[1], -half*O[2], DL, typo);
-      nvmul_f(J, O, A);
+      inertia_mul(js, d.J_f, i, O, A);
       nvmul_f(DL, A, B);
       for (int c = 0; c < 3; c ++) B[c] = B[c] + half*Tb[c];
-      nvmul_f(I, B, A);
-      nvmul_f(J, A, B);
+      inertia_mul(is, d.I_f, i, B, A);
+      inertia_mul(js, d.J_f, i, A, B);
       Tb[0] -= A[1]*B[2] - A[2]*B[1];
       Tb[1] -= A[2]*B[0] - A[0]*B[2];
       Tb[2] -= A[0]*B[1] - A[1]*B[0];
       for (int c = 0; c < 3; c ++) Tb[c] *= step;
       float IT[3];
-      nvmul_f(I, Tb, IT);
+      inertia_mul(is, d.I_f, i, Tb, IT);
       for (int c = 0; c < 3; c ++) O[c] = O[c] + IT[c];
       const float im = d.invm_f[i] * step;
       for (int c = 0; c < 3; c ++) v[c] = df_add_f(v[c], im * F[c]);
@@ -561,9 +603,23 @@ __global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int 
       if (!pgk::rebuild_all<B>(d, passes, epasses, sm, MxCentres())) return;
     // excitation and contacts: contacts do not read the scene gravity
     for (int sc = g0; sc < d.nscene; sc += gsz) pgk::excite_item(d, sc, step);
-    for (int i = g0; i < E; i += gsz) mx_contacts_item(d, i, step);
+    // sphere partners, queueing spheres with triangles (the loop's trip count
+    // is the same for every lane of a warp: the queue push is a warp vote)
+    for (int i = g0; i - (int)(threadIdx.x & 31) < E; i += gsz)
+    {
+      bool more = false;
+      if (i < E) more = mx_contacts_item<MX_SPHERES>(d, i, step);
+      pgk::tri_queue_push(d, more, i);
+    }
     if (!pgk::grid_barrier(d)) return;
-    // integration and obstacle triangles touch disjoint state
+    {
+      const int n = pgk::tri_queue_len(d);
+      for (int q = g0; q < n; q += gsz) mx_contacts_item<MX_TRIANGLES>(d, d.twork[q], step);
+    }
+    if (!pgk::grid_barrier(d)) return;
+    // integration and obstacle triangles touch disjoint state; nothing reads
+    // the triangle queue again before the next step's contacts
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.tcnt[0] = 0;
     bool need = false;
     for (int i = g0; i < P; i += gsz) need |= mx_integrate_item(d, i, step);
     for (int t = g0; t < T; t += gsz) need |= pgk::obstacles_item(d, t, step, 1);
@@ -654,7 +710,10 @@ void pg_launch_mx_centres(const PgDev &d, cudaStream_t s)
 
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.ellnum) k_contacts_mx<<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  if (!d.ellnum) return;
+  k_contacts_mx<<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
+  const int nb = nblk(d.ellnum);
+  k_tri_mx<<<nb < pgk::TRI_PASS_BLOCKS ? nb : pgk::TRI_PASS_BLOCKS, TPB, 0, s>>>(d, step);
 }
 
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step)

@@ -809,6 +809,8 @@ int mixed_buffers(pg_session *s)
   }
   TRY(dalloc(s, &d.mass_f, P)); TRY(dalloc(s, &d.invm_f, P));
   TRY(dalloc(s, &d.rh, E)); TRY(dalloc(s, &d.rl, E));
+  TRY(dalloc(s, &d.twork, std::max<size_t>(E, 1)));   // triangle queue of the contact passes
+  TRY(dalloc(s, &d.tcnt, 2));
   TRY(dalloc(s, &d.jiso, P)); TRY(dalloc(s, &d.iiso, P));
   for (int k = 0; k < 3; k ++) TRY(dalloc(s, &d.cref_f[k], E));
   for (int k = 0; k < 7; k ++) TRY(dalloc(s, &d.iparam_f[k], (size_t)std::max(d.pairnum, 1)));
@@ -1360,7 +1362,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
       CK(cudaEventRecord(ev[6], s->stream));
     }
     CK(cudaStreamSynchronize(s->stream));
-    const int counts[6] = {pg_rebuild_kernel_count(d), d.ellnum ? 1 : 0, d.sprnum ? 1 : 0, d.parnum ? 1 : 0,
+    const int counts[6] = {pg_rebuild_kernel_count(d), pg_contacts_kernel_count(d), d.sprnum ? 1 : 0, d.parnum ? 1 : 0,
                            (d.nodnum ? 1 : 0) + (d.facnum ? 1 : 0), 1 + ((d.obsnum && d.trinum) ? 1 : 0)};
     for (int k = 0; k < n; k ++)
     {

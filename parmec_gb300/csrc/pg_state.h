@@ -181,6 +181,8 @@ struct PgDev
   float *F_f[3], *T_f[3];
   float *nstate_f[3], *nfrc_f[3], *narm_f[3];   // per candidate entry; arm = point - slave position
   float *fm_f[3], *tm_f[3];
+  int *twork;               // [ellnum] spheres with triangle candidates this step
+  int *tcnt;                // [2] length of twork, blocks of the triangle pass done
   float *iparam_f[7];       // [pairnum] surface pair parameters in FP32
   float *sgrav_f;           // [nscene][3] this step's scene gravity in FP32 (written with sgrav)
   float *damp_f;            // [6] this step's damping row in FP32

@@ -158,6 +158,22 @@ __device__ __forceinline__ void body_point(const double *x, const double *L, con
   nvaddmul(x, L, C, c);
 }
 
+// c = x + L (C - X) is x itself, bit for bit, when C and X have the same
+// bits and are finite (C - X is +0), every entry of L is finite (each product
+// is a zero, so their sum is a zero) and each x[k] is finite and nonzero
+// (x + 0 = x).  That is every SPHERE particle, whose sphere centre is its
+// reference point; the test runs on the integer pipe and saves the 21 FP64
+// instructions of body_point.
+__device__ __forceinline__ bool centre_is_position(const double *x, const double *L, const double *X,
+                                                   const double *C)
+{
+  bool ok = true;
+  for (int k = 0; k < 3; k ++)
+    ok = ok && dbits(C[k]) == dbits(X[k]) && finite_d(X[k]) && finite_d(x[k]) && nonzero_d(x[k]);
+  for (int k = 0; k < 9; k ++) ok = ok && finite_d(L[k]);
+  return ok;
+}
+
 __global__ void k_spheres(PgDev d)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -166,7 +182,8 @@ __global__ void k_spheres(PgDev d)
   double L[9], X[3], x[3], C[3], c[3];
   for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][j];
   for (int k = 0; k < 3; k ++) { X[k] = d.position[3+k][j]; x[k] = d.position[k][j]; C[k] = d.center[3+k][e]; }
-  body_point(x, L, X, C, c);
+  if (centre_is_position(x, L, X, C)) { c[0] = x[0]; c[1] = x[1]; c[2] = x[2]; }
+  else body_point(x, L, X, C, c);
   for (int k = 0; k < 3; k ++) d.center[k][e] = c[k];
 }
 
@@ -1325,13 +1342,13 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
       if (!iso)
         for (int k = 0; k < 9; k ++) { J[k] = d.inertia[k][i]; I[k] = d.inverse[k][i]; }
       im = d.invm[i];
-      if (damping[0] != 0.0 || damping[1] != 0.0 || damping[2] != 0.0)
+      if (nonzero_d(damping[0]) || nonzero_d(damping[1]) || nonzero_d(damping[2]))
       {
         F[0] -= ma * damping[0] * v[0];
         F[1] -= ma * damping[1] * v[1];
         F[2] -= ma * damping[2] * v[2];
       }
-      if (damping[3] != 0.0 || damping[4] != 0.0 || damping[5] != 0.0)
+      if (nonzero_d(damping[3]) || nonzero_d(damping[4]) || nonzero_d(damping[5]))
       {
         o[0] = damping[3]*d.angular[3][i];
         o[1] = damping[4]*d.angular[4][i];
@@ -1426,10 +1443,11 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
     {
       double X[3] = {d.position[3][i], d.position[4][i], d.position[5][i]};
       double C[3] = {d.center[3][e], d.center[4][e], d.center[5][e]}, c[3];
-      body_point(x, L2, X, C, c);
+      if (centre_is_position(x, L2, X, C)) { c[0] = x[0]; c[1] = x[1]; c[2] = x[2]; }
+      else body_point(x, L2, X, C, c);
       d.center[0][e] = c[0]; d.center[1][e] = c[1]; d.center[2][e] = c[2];
       double r0 = c[0] - d.cref[0][e], r1 = c[1] - d.cref[1][e], r2 = c[2] - d.cref[2][e];
-      need = (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
+      need = gt_nonneg(r0*r0 + r1*r1 + r2*r2, d.half_skin_sq);
     }
   }
   if (FUSED && d.ellnum) flag_rebuild(d, need);
@@ -1754,6 +1772,14 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   else k_contacts<false, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
 }
 
+// the FP64 form evaluates each list in one pass; the mixed form in a sphere
+// and a triangle pass (pg_mixed.cu)
+int pg_contacts_kernel_count(const PgDev &d)
+{
+  if (!d.ellnum) return 0;
+  return d.form == PG_FORM_MIXED ? 2 : 1;
+}
+
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
 {
   if (!d.sprnum) return;
@@ -1847,7 +1873,7 @@ void pg_launch_tail(const PgDev &d, cudaStream_t s, double step)
 int pg_step_kernel_count(const PgDev &d)
 {
   int n = 2;                                   // excite, tail
-  if (d.ellnum) n += 1;                        // contacts
+  n += pg_contacts_kernel_count(d);            // contacts: sphere and triangle passes
   if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0) + (d.unsprnum ? 1 : 0);
   if (d.trqsprnum) n += 1;                     // torsion springs
   if (d.parnum) n += 1;                        // integrate
