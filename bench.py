@@ -471,11 +471,11 @@ def main():
     bytes_dom = per_launch.get(dom)
     # DRAM bytes per launch: ncu capture of the 262,144-sphere case
     # (profiles/k_integrate_k_contacts_drum_fp64.md) scaled by the units processed
-    traffic_per_unit = {"integrate": 456.0, "contacts": 200.0}
+    traffic_per_unit = {"integrate": 458.0, "contacts": 200.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     # FP64 pipe: thread-level FP64 instructions (DADD + DMUL + DFMA) per unit,
     # counted by ncu on the same capture; peak = 2 per clock per SM
-    fp64_per_unit = {"integrate": 312.0, "contacts": 161.0}
+    fp64_per_unit = {"integrate": 294.0, "contacts": 161.0}
     fp64 = None
     if dom in fp64_per_unit:
         sm_mhz = clk.get("sm_mhz") or 2070.0
