@@ -370,33 +370,59 @@ __device__ __forceinline__ void rb_tref_item(const PgDev &d, int t)
   }
 }
 
-// 3. cell ranges
+// 3. cell ranges, and the float centre, radius and particle of the sphere at
+// each sorted position (the candidate search reads a cell's spheres from
+// these contiguous copies)
 __device__ __forceinline__ void rb_ranges_item(const PgDev &d, int s)
 {
   const int n = d.ellnum;
   unsigned key = d.keys[0][s];
+  {
+    const int j = d.vals[0][s];
+    d.cfs[s] = make_float4((float)d.center[0][j], (float)d.center[1][j], (float)d.center[2][j],
+                           (float)d.radii[0][j]);
+    d.pfs[s] = d.part[j];
+  }
   if (key == 0xffffffffu) return;
   if (s == 0 || d.keys[0][s-1] != key) d.cstart[key] = s;
   if (s == n-1 || d.keys[0][s+1] != key) d.cend[key] = s + 1;
 }
 
 // 4. candidate list of sphere i with carried contact state
-__device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
+// Every lane of the warp calls it (valid: i is a sphere index): the triangle
+// scan is shared by the warp.
+__device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i, bool valid)
 {
   const int E = d.ellnum;
   int codes[MAXKN];
   int n = 0, nover = 0, ntri = 0;
   bool over = false;
-  double c[3] = {d.center[0][i], d.center[1][i], d.center[2][i]};
-  const double ri = d.radii[0][i];
-  const int pi = d.part[i];
-  const int sc = d.escene[i];
+  double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
+  int pi = 0, sc = -1;
+  if (valid)
+  {
+    for (int k = 0; k < 3; k ++) c[k] = d.center[k][i];
+    ri = d.radii[0][i];
+    pi = d.part[i];
+    sc = d.escene[i];
+  }
   const bool live = sc >= 0 && d.sactive[sc] != 0;
-  if (!live) return;
+  if (live)
   {
     const unsigned prefix = (unsigned)sc << (3 * d.bits);
     int u[3];
     cell_of(d, sc, c, u);
+    // FP32 prefilter: a neighbour is skipped only when its float distance
+    // exceeds the float limit by tol, more than the rounding of the float
+    // copies and of the float arithmetic can account for, so the FP64 test
+    // below still decides every candidate (the lists are those of the FP64
+    // test alone).  Float coordinates carry at most 2^-24 |c| of error;
+    // tol = 2^-20 (max|c_i| + 2 cell) bounds the distance error 16 times over
+    // for partners within a cell.
+    const float cif[3] = {(float)c[0], (float)c[1], (float)c[2]};
+    const float rsf = (float)ri + (float)d.skin;
+    const float tol = 9.5367431640625e-7f *
+                      (fmaxf(fmaxf(fabsf(cif[0]), fabsf(cif[1])), fabsf(cif[2])) + 2.0f * (float)d.cell);
     for (int dz = -1; dz <= 1; dz ++)
       for (int dy = -1; dy <= 1; dy ++)
         for (int dx = -1; dx <= 1; dx ++)
@@ -407,8 +433,13 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
           int b = d.cstart[key], e = d.cend[key];
           for (int s = b; s < e; s ++)
           {
+            const float4 q = d.cfs[s];
+            const float f0 = cif[0] - q.x, f1 = cif[1] - q.y, f2 = cif[2] - q.z;
+            const float lf = rsf + q.w + tol;
+            if (f0*f0 + f1*f1 + f2*f2 >= lf*lf) continue;
+            if (d.pfs[s] <= pi) continue;
             int j = d.vals[0][s];
-            if ((unsigned)j >= (unsigned)E || d.part[j] <= pi) continue;
+            if ((unsigned)j >= (unsigned)E) continue;
             double q0 = c[0] - d.center[0][j], q1 = c[1] - d.center[1][j], q2 = c[2] - d.center[2][j];
             double lim = ri + d.radii[0][j] + d.skin;
             if (q0*q0 + q1*q1 + q2*q2 < lim*lim)
@@ -425,28 +456,68 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i)
       while (b >= 0 && codes[b] > v) { codes[b+1] = codes[b]; b --; }
       codes[b+1] = v;
     }
-    // triangles of the sphere's scene within r + skin (AABB in float, then the
-    // true closest-point distance)
+  }
+  // triangles of the sphere's scene within r + skin (AABB in float, then the
+  // true closest-point distance), in triangle order
+  const float inf = __int_as_float(0x7f800000);
+  float clo[3] = {inf, inf, inf}, chi[3] = {-inf, -inf, -inf};
+  if (live)
+  {
     const float rr = (float)(ri + d.skin) * 1.0001f + 1e-30f;
-    const float clo[3] = {__double2float_rd(c[0]) - rr, __double2float_rd(c[1]) - rr, __double2float_rd(c[2]) - rr};
-    const float chi[3] = {__double2float_ru(c[0]) + rr, __double2float_ru(c[1]) + rr, __double2float_ru(c[2]) + rr};
-    const int T = d.trinum;
-    for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++)
+    for (int k = 0; k < 3; k ++) { clo[k] = __double2float_rd(c[k]) - rr; chi[k] = __double2float_ru(c[k]) + rr; }
+  }
+  const int T = d.trinum;
+  auto box_apart = [&](int t, const float *lo, const float *hi) {
+    return d.tbox[t] > hi[0] || d.tbox[(size_t)3 * T + t] < lo[0] ||
+           d.tbox[(size_t)T + t] > hi[1] || d.tbox[(size_t)4 * T + t] < lo[1] ||
+           d.tbox[(size_t)2 * T + t] > hi[2] || d.tbox[(size_t)5 * T + t] < lo[2];
+  };
+  auto try_triangle = [&](int t) {
+    if (box_apart(t, clo, chi)) return;
+    double A[3], B[3], C[3], pnt[3], nrm[3];
+    for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
+    // the candidate test uses the true closest point: the reference's region
+    // formula can only report a larger distance, so this set stays a superset
+    double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, false);
+    if (!(depth > -d.skin) && !(depth != depth)) return;
+    ntri ++;
+    if (n < d.kn) codes[n ++] = -(t + 1);
+    else { over = true; nover ++; }
+  };
+  // when every live lane of the warp is in one scene, the warp tests 32
+  // triangles at a time against the box of all its spheres and each lane
+  // then tests its own box against the triangles that box reached
+  const unsigned full = 0xffffffffu, lm = __ballot_sync(full, live);
+  if (!lm) return;
+  const int lane = threadIdx.x & 31, sc0 = __shfl_sync(full, sc, __ffs(lm) - 1);
+  if (__all_sync(full, !live || sc == sc0))
+  {
+    float wlo[3], whi[3];
+    for (int k = 0; k < 3; k ++)
     {
-      if (d.tbox[t] > chi[0] || d.tbox[(size_t)3 * T + t] < clo[0] ||
-          d.tbox[(size_t)T + t] > chi[1] || d.tbox[(size_t)4 * T + t] < clo[1] ||
-          d.tbox[(size_t)2 * T + t] > chi[2] || d.tbox[(size_t)5 * T + t] < clo[2]) continue;
-      double A[3], B[3], C[3], pnt[3], nrm[3];
-      for (int q = 0; q < 3; q ++) { A[q] = d.tri[q][t]; B[q] = d.tri[3+q][t]; C[q] = d.tri[6+q][t]; }
-      // the candidate test uses the true closest point: the reference's region
-      // formula can only report a larger distance, so this set stays a superset
-      double depth = pg::triangle_sphere(A, B, C, c, ri, pnt, nrm, false);
-      if (!(depth > -d.skin) && !(depth != depth)) continue;
-      ntri ++;
-      if (n < d.kn) codes[n ++] = -(t + 1);
-      else { over = true; nover ++; }
+      wlo[k] = clo[k]; whi[k] = chi[k];
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        wlo[k] = fminf(wlo[k], __shfl_xor_sync(full, wlo[k], o));
+        whi[k] = fmaxf(whi[k], __shfl_xor_sync(full, whi[k], o));
+      }
+    }
+    const int tb = d.stbeg[sc0], te = d.stend[sc0];
+    for (int t0 = tb; t0 < te; t0 += 32)
+    {
+      const int t = t0 + lane;
+      unsigned hm = __ballot_sync(full, t < te && !box_apart(t, wlo, whi));
+      while (hm)
+      {
+        const int tt = t0 + __ffs(hm) - 1;
+        hm &= hm - 1;
+        if (live) try_triangle(tt);
+      }
     }
   }
+  else if (live)
+    for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++) try_triangle(t);
+  if (!live) return;
   if (over) set_err(d, PG_ERR_CAPACITY, 1, i, n + nover);
   atomicMax(&d.stats[1], n + nover);
   atomicMax(&d.stats[3], ntri);
@@ -647,8 +718,10 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   for (int k = 0; k < 3; k ++) { g.org[k] = 0.0; g.dim[k] = d.dim[k]; }
   g.cell = d.cell;
   for (int i = g0; i < E; i += gsz)
+  {
     cell_keys_item(i, d.center[0], d.center[1], d.center[2], g, d.escene, d.sorg[0], d.sorg[1], d.sorg[2],
                    3 * d.bits, d.keys[0], d.vals[0], d.cref[0], d.cref[1], d.cref[2]);
+  }
   if (!grid_barrier(d)) return false;
   const int nb = d.nsortblocks;
   for (int p = 0; p < passes; p ++)
@@ -664,7 +737,7 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   }
   for (int s = g0; s < E; s += gsz) rb_ranges_item(d, s);
   if (!grid_barrier(d)) return false;
-  for (int i = g0; i < E; i += gsz) rb_verlet_item(d, i);
+  for (int i = g0; i - (int)(threadIdx.x & 31) < E; i += gsz) rb_verlet_item(d, i, i < E);
   if (!grid_barrier(d)) return false;
   for (int p = g0; p < P; p += gsz) rb_rzero_item(d, p);
   for (int q = g0; q < E; q += gsz) rb_count_item(d, q);

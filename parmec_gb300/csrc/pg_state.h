@@ -147,6 +147,8 @@ struct PgDev
   double org[3];
   int dim[3], bits, keybits;   // cells per axis, Morton bits per axis, bits of (scene, cell) keys
   double *cref[3];          // sphere centres at the last rebuild
+  float4 *cfs;              // [ellnum] float centre and radius of the sphere at each sorted position (rebuild)
+  int *pfs;                 // [ellnum] particle of the sphere at each sorted position (rebuild)
   double *tref[9];          // triangle vertices at the last rebuild
   unsigned *keys[2];        // radix-sort ping-pong buffers
   int *vals[2];
