@@ -517,10 +517,18 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i, bool valid
   }
   else if (live)
     for (int t = d.stbeg[sc]; t < d.stend[sc]; t ++) try_triangle(t);
+  // one atomic per warp for the largest list and triangle counts
+  {
+    const int cmax = __reduce_max_sync(full, live ? n + nover : 0);
+    const int tmax = __reduce_max_sync(full, live ? ntri : 0);
+    if (lane == 0)
+    {
+      if (cmax > 0) atomicMax(&d.stats[1], cmax);
+      if (tmax > 0) atomicMax(&d.stats[3], tmax);
+    }
+  }
   if (!live) return;
   if (over) set_err(d, PG_ERR_CAPACITY, 1, i, n + nover);
-  atomicMax(&d.stats[1], n + nover);
-  atomicMax(&d.stats[3], ntri);
 
   // merge with the previous list (both in partner order)
   const int nold = d.ncnt[i];
@@ -588,7 +596,10 @@ __device__ __forceinline__ void rb_soff_item(const PgDev &d, int p)
 {
   const int n = d.rcnt[p];
   d.soff[p] = n;
-  atomicMax(&d.stats[2], n);
+  // one atomic per warp for the largest slave count
+  const unsigned am = __activemask();
+  const int wmax = __reduce_max_sync(am, n);
+  if ((threadIdx.x & 31) == __ffs(am) - 1 && wmax > 0) atomicMax(&d.stats[2], wmax);
 }
 
 // sizes of the entry sort (one thread): entries, tiles, histogram length and
