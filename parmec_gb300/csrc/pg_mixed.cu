@@ -574,63 +574,50 @@ __global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_integrate_mx(PgDev d,
   if (d.ellnum) flag_rebuild(d, need);
 }
 
-// ------------------------------------------------------------ persistent fused step
-// One cooperatively launched grid runs whole steps of the mixed form:
-//   [rebuild, when flagged: clear | keys | radix sort passes | ranges |
-//    candidate lists | slave lists]
-//   excitation + contacts | integration + obstacles | tail
+// ------------------------------------------------------------ fused step
+// One cooperatively launched grid runs a whole step of the mixed form:
+//   excitation + sphere contacts | triangle contacts | integration +
+//   obstacles | tail
 // with a grid barrier at each '|'.  Every block walks the items of a phase in
 // a grid-stride loop; the item bodies are the ones the per-phase kernels run,
-// so the results do not depend on the launch shape.
-
-// the mixed form's extra work in the first rebuild phase: FP64 centres and
-// FP32 reference centres from the position pairs
-struct MxCentres
-{
-  __device__ void operator()(const PgDev &d, int e) const { mx_centres_item(d, e); }
-};
-
+// so the results do not depend on the launch shape.  The candidate-list
+// rebuild, when flagged, is the cooperative rebuild kernel launched before
+// each step (pg_launch_fused_mx): inside this kernel's register budget
+// (chosen for the step phases) the rebuild ran at a fraction of its speed.
 template <int B, int MINB>
-__global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step, int nsteps, int passes, int epasses)
+__global__ void __launch_bounds__(B, MINB) k_fused_mx(PgDev d, double step)
 {
-  __shared__ pgk::RebuildSmem<B> sm;
   const int gsz = gridDim.x * B;
   const int g0 = blockIdx.x * B + threadIdx.x;
   const int E = d.ellnum, P = d.parnum, T = d.trinum;
-  for (int it = 0; it < nsteps; it ++)
+  // excitation and contacts: contacts do not read the scene gravity
+  for (int sc = g0; sc < d.nscene; sc += gsz) pgk::excite_item(d, sc, step);
+  // sphere partners, queueing spheres with triangles (the loop's trip count
+  // is the same for every lane of a warp: the queue push is a warp vote)
+  for (int i = g0; i - (int)(threadIdx.x & 31) < E; i += gsz)
   {
-    if (E && *(volatile int *)d.rebuild)
-      if (!pgk::rebuild_all<B>(d, passes, epasses, sm, MxCentres())) return;
-    // excitation and contacts: contacts do not read the scene gravity
-    for (int sc = g0; sc < d.nscene; sc += gsz) pgk::excite_item(d, sc, step);
-    // sphere partners, queueing spheres with triangles (the loop's trip count
-    // is the same for every lane of a warp: the queue push is a warp vote)
-    for (int i = g0; i - (int)(threadIdx.x & 31) < E; i += gsz)
-    {
-      bool more = false;
-      if (i < E) more = mx_contacts_item<MX_SPHERES>(d, i, step);
-      pgk::tri_queue_push(d, more, i);
-    }
-    if (!pgk::grid_barrier(d)) return;
-    {
-      const int n = pgk::tri_queue_len(d);
-      for (int q = g0; q < n; q += gsz) mx_contacts_item<MX_TRIANGLES>(d, d.twork[q], step);
-    }
-    if (!pgk::grid_barrier(d)) return;
-    // integration and obstacle triangles touch disjoint state; nothing reads
-    // the triangle queue again before the next step's contacts
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.tcnt[0] = 0;
-    bool need = false;
-    for (int i = g0; i < P; i += gsz) need |= mx_integrate_item(d, i, step);
-    for (int t = g0; t < T; t += gsz) need |= pgk::obstacles_item(d, t, step, 1);
-    if (__syncthreads_or(need) && threadIdx.x == 0 && E) atomicExch(d.rebuild, 1);
-    if (!pgk::grid_barrier(d)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) pgk::tail_item(d, step, 1);
-    if (!pgk::grid_barrier(d)) return;
+    bool more = false;
+    if (i < E) more = mx_contacts_item<MX_SPHERES>(d, i, step);
+    pgk::tri_queue_push(d, more, i);
   }
+  if (!pgk::grid_barrier(d)) return;
+  {
+    const int n = pgk::tri_queue_len(d);
+    for (int q = g0; q < n; q += gsz) mx_contacts_item<MX_TRIANGLES>(d, d.twork[q], step);
+  }
+  if (!pgk::grid_barrier(d)) return;
+  // integration and obstacle triangles touch disjoint state; nothing reads
+  // the triangle queue again before the next step's contacts
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.tcnt[0] = 0;
+  bool need = false;
+  for (int i = g0; i < P; i += gsz) need |= mx_integrate_item(d, i, step);
+  for (int t = g0; t < T; t += gsz) need |= pgk::obstacles_item(d, t, step, 1);
+  if (__syncthreads_or(need) && threadIdx.x == 0 && E) atomicExch(d.rebuild, 1);
+  if (!pgk::grid_barrier(d)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) pgk::tail_item(d, step, 1);
 }
 
-typedef void (*FusedKernel)(PgDev, double, int, int, int);
+typedef void (*FusedKernel)(PgDev, double);
 
 // the launch shapes the autotuner may pick from (threads, minimum blocks per SM)
 struct FusedShape { int threads, minb; FusedKernel k; };
@@ -667,9 +654,6 @@ int pg_fused_candidates(PgFusedCfg *out, int cap)
 cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int nsteps, const PgFusedCfg &c)
 {
   if (c.shape < 0 || c.shape >= n_fused_shapes || c.blocks < 1) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(d.gbar, 0, 4 * sizeof(unsigned), s);
-  if (e != cudaSuccess) return e;
-  const int passes = pg_sort_passes_bits(pg_rebuild_sort_bits(d));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(c.blocks);
   cfg.blockDim = dim3(fused_shapes[c.shape].threads);
@@ -680,8 +664,17 @@ cudaError_t pg_launch_fused_mx(const PgDev &d, cudaStream_t s, double step, int 
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  const int epasses = pg_sort_passes_exact(d.sbits);
-  return cudaLaunchKernelEx(&cfg, fused_shapes[c.shape].k, d, step, nsteps, passes, epasses);
+  for (int k = 0; k < nsteps; k ++)
+  {
+    // the rebuild, when flagged (both return at once otherwise)
+    pg_launch_mx_centres(d, s);
+    pg_launch_rebuild(d, s);
+    cudaError_t e = cudaMemsetAsync(d.gbar, 0, 4 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    e = cudaLaunchKernelEx(&cfg, fused_shapes[c.shape].k, d, step);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
 }
 
 void pg_launch_mx_from64(const PgDev &d, cudaStream_t s, int p0, int p1, int e0, int e1)

@@ -899,6 +899,10 @@ void drop_graph(pg_session *s)
 
 // the fused kernel for 'n' steps, as a captured graph of 'chunk' steps per
 // replay when capture works, else as direct cooperative launches
+// kernels one fused step launches: the gated centre conversion and rebuild
+// (with spheres), then the fused step kernel
+static int fused_kernels_per_step(const PgDev &d) { return d.ellnum ? 3 : 1; }
+
 int run_fused(pg_session *s, double step, int n, int chunk)
 {
   const PgDev &d = s->d;
@@ -938,14 +942,14 @@ int run_fused(pg_session *s, double step, int n, int chunk)
     {
       const int reps = n / chunk;
       for (int k = 0; k < reps; k ++) CK(cudaGraphLaunch(s->fgraph_exec, s->stream));
-      s->fused_launches += reps;
+      s->fused_launches += (long long)reps * chunk * fused_kernels_per_step(d);
       n -= reps * chunk;
     }
   }
   if (n > 0)
   {
     CK(pg_launch_fused_mx(d, s->stream, step, n, s->fcfg));
-    s->fused_launches += 1;
+    s->fused_launches += (long long)n * fused_kernels_per_step(d);
   }
   return PG_OK;
 }
@@ -972,7 +976,7 @@ int run_fused_steps(pg_session *s, double step, int n)
     {
       // an untimed step: the first rebuild and cold caches
       CK(pg_launch_fused_mx(s->d, s->stream, step, 1, s->cands[0]));
-      s->fused_launches += 1;
+      s->fused_launches += fused_kernels_per_step(s->d);
       done += 1;
       s->warmed = 1;
     }
@@ -986,6 +990,7 @@ int run_fused_steps(pg_session *s, double step, int n)
       CK(cudaEventRecord(e0, s->stream));
       CK(pg_launch_fused_mx(s->d, s->stream, step, trial, c));
       CK(cudaEventRecord(e1, s->stream));
+      s->fused_launches += (long long)trial * fused_kernels_per_step(s->d) - 1;
       CK(cudaEventSynchronize(e1));
       float ms = 0.0f;
       CK(cudaEventElapsedTime(&ms, e0, e1));
