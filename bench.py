@@ -185,7 +185,7 @@ def batched_form(args, scenes):
         models = [sc[0] for sc in scenes]
         P, _ = batch.pool(models)
         dt = scenes[0][1]
-        # the persistent fused step kernel picks its launch shape during the
+        # the fused step kernel picks its launch shape during the
         # warm-up steps (real steps; the result does not depend on the shape)
         eng = GpuEngine(form=form, capacity=(32, 32), fused=fused, autotune=fused)
         eng.attach(P)
@@ -210,7 +210,7 @@ def batched_form(args, scenes):
                     "ms_per_step": ms / steps, "spheres": P.parnum}
         if fused:
             threads, blocks, tuned, graph = eng.fused_config()
-            out[key]["kernel"] = {"persistent_fused": True, "threads": threads, "blocks": blocks,
+            out[key]["kernel"] = {"fused_step": True, "threads": threads, "blocks": blocks,
                                   "autotuned": bool(tuned), "cuda_graph": bool(graph)}
         eng.close()
         del P
@@ -218,7 +218,7 @@ def batched_form(args, scenes):
     best = max(("mixed", "mixed_per_phase_kernels"), key=lambda k: out[k]["value"])
     out["mixed_best"] = {"value": out[best]["value"], "unit": "particle-steps/s",
                          "ms_per_step": out[best]["ms_per_step"],
-                         "path": "persistent fused kernel" if best == "mixed" else
+                         "path": "fused step kernel" if best == "mixed" else
                                  "per-phase kernels, one CUDA graph per step"}
     out["mixed_over_fp64"] = out["mixed_best"]["value"] / out["fp64"]["value"]
     return out

@@ -329,11 +329,12 @@ int pg_session_record_geometry(pg_session *s, int on);
  * individual stream launches (off).  Results are identical. */
 int pg_session_use_graph(pg_session *s, int on);
 
-/* Mixed form only: run steps in one persistent, cooperatively launched step
- * kernel (rebuild, radix sort, contacts, integration, obstacles and scene
- * excitation between grid barriers), captured as a CUDA graph of 16 steps per
- * replay.  Results are bit-identical to the per-phase kernels for any launch
- * shape.  A grid barrier that waits more than 2 s gives PG_ERR_TIMEOUT in
+/* Mixed form only: run each step as one cooperatively launched step kernel
+ * (scene excitation, sphere and triangle contacts, integration and obstacles
+ * between grid barriers), preceded by the cooperative rebuild kernel, which
+ * returns at once unless a rebuild is due; 16 steps are captured as one CUDA
+ * graph per replay.  Results are bit-identical to the per-phase kernels for
+ * any launch shape.  A grid barrier that waits more than 2 s gives PG_ERR_TIMEOUT in
  * the diagnostics instead of hanging.  PG_ERR_UNSUPPORTED in the FP64 form. */
 int pg_session_use_fused(pg_session *s, int on);
 

@@ -17,7 +17,7 @@ class GpuEngine:
 
     def __init__(self, model=None, form=abi.PG_FORM_FP64, skin=None, record_geometry=False, graph=True,
                  capacity=None, fused=False, autotune=False):
-        """fused: the mixed form's persistent step kernel (pg_session_use_fused);
+        """fused: the mixed form's fused step kernel (pg_session_use_fused);
         autotune: pick its launch shape by timing the first steps."""
         self.lib = abi.load_library()
         self._pinned = {}

@@ -103,9 +103,11 @@ class Server:
 
     def __init__(self, template, dt, form=abi.PG_FORM_MIXED, budget_bytes=150e9, max_scenes=256,
                  max_spheres=None, max_triangles=None, max_scene_extent=4.0, kn=32, kr=32, chunk=250,
-                 fused=True):
-        """fused: the mixed form steps the pool with the persistent fused step
-        kernel, its launch shape picked by the autotuner on the first steps."""
+                 fused=False):
+        """fused: the mixed form steps the pool with the fused step kernel, its
+        launch shape picked by the autotuner on the first steps; by default
+        the per-phase kernels (one CUDA graph per step), which measured
+        faster on the batch workload."""
         self.form = form
         self.dt = dt
         self.chunk = chunk

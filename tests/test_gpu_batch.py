@@ -87,7 +87,7 @@ def same_state(a, b):
 
 @pytest.mark.parametrize("autotune", [False, True])
 def test_fused_step_kernel_equals_per_phase_kernels(gpu_lib, autotune):
-    """The persistent fused step (mixed form) gives the per-phase kernels'
+    """The fused step kernel (mixed form) gives the per-phase kernels'
     state bit for bit, whatever launch shapes the autotuner tries on the way."""
     mk = makers()
     ref = run_pool(mk, 150, 1)

@@ -11,7 +11,7 @@
   positions within 1e-6 m, the same contact pairs but for pairs whose gap is
   within twice the largest position difference of zero (at most one in 1e5).
 * The 512-scene batch (9.04M spheres, sizes log-uniform in [2048, 65536],
-  each scene with its own base excitation): the persistent fused step kernel
+  each scene with its own base excitation): the fused step kernel
   gives the per-phase kernels' state bit for bit after 20 steps.
 """
 import copy
