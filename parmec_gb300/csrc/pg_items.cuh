@@ -39,20 +39,20 @@ __device__ __forceinline__ unsigned spread3(unsigned x)
   return x;
 }
 
+// inverse of spread3: every third bit, packed
+__device__ __forceinline__ unsigned compact3(unsigned x)
+{
+  x &= 0x09249249;
+  x = (x | (x >> 2)) & 0x030C30C3;
+  x = (x | (x >> 4)) & 0x0300F00F;
+  x = (x | (x >> 8)) & 0x030000FF;
+  x = (x | (x >> 16)) & 0x3ff;
+  return x;
+}
+
 __device__ __forceinline__ unsigned morton(int x, int y, int z)
 {
   return spread3((unsigned)x) | (spread3((unsigned)y) << 1) | (spread3((unsigned)z) << 2);
-}
-
-__device__ __forceinline__ void cell_of(const PgDev &d, int scene, const double *c, int *u)
-{
-  for (int k = 0; k < 3; k ++)
-  {
-    double f = floor((c[k] - d.sorg[k][scene]) / d.cell);
-    if (!(f >= 0.0)) f = 0.0;                 // also catches NaN
-    if (f > (double)(d.dim[k] - 1)) f = (double)(d.dim[k] - 1);
-    u[k] = (int)f;
-  }
 }
 
 __device__ __forceinline__ unsigned order_key(int code)
@@ -410,8 +410,10 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i, bool valid
   if (live)
   {
     const unsigned prefix = (unsigned)sc << (3 * d.bits);
-    int u[3];
-    cell_of(d, sc, c, u);
+    // the sphere's cell, from the key the key phase computed, instead of
+    // three FP64 divisions again
+    const unsigned cm = d.ekey[i] & ((1u << (3 * d.bits)) - 1u);
+    const int u[3] = {(int)compact3(cm), (int)compact3(cm >> 1), (int)compact3(cm >> 2)};
     // FP32 prefilter: a neighbour is skipped only when its float distance
     // exceeds the float limit by tol, more than the rounding of the float
     // copies and of the float arithmetic can account for, so the FP64 test
@@ -732,6 +734,7 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   {
     cell_keys_item(i, d.center[0], d.center[1], d.center[2], g, d.escene, d.sorg[0], d.sorg[1], d.sorg[2],
                    3 * d.bits, d.keys[0], d.vals[0], d.cref[0], d.cref[1], d.cref[2]);
+    d.ekey[i] = d.keys[0][i];        // the sort reorders keys[]; the search reads its own cell here
   }
   if (!grid_barrier(d)) return false;
   const int nb = d.nsortblocks;

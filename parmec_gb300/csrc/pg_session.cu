@@ -773,6 +773,7 @@ int contact_buffers(pg_session *s)
   }
   TRY(dalloc(s, &d.cfs, E));
   TRY(dalloc(s, &d.pfs, E));
+  TRY(dalloc(s, &d.ekey, E));
   TRY(dalloc(s, &d.rcnt, P));
   TRY(dalloc(s, &d.soff, P + 1));
   TRY(dalloc(s, &d.eorder, E));

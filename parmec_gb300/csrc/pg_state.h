@@ -149,6 +149,7 @@ struct PgDev
   double *cref[3];          // sphere centres at the last rebuild
   float4 *cfs;              // [ellnum] float centre and radius of the sphere at each sorted position (rebuild)
   int *pfs;                 // [ellnum] particle of the sphere at each sorted position (rebuild)
+  unsigned *ekey;           // [ellnum] cell key of each sphere at the last rebuild, in sphere order
   double *tref[9];          // triangle vertices at the last rebuild
   unsigned *keys[2];        // radix-sort ping-pong buffers
   int *vals[2];
