@@ -103,7 +103,10 @@ void pg_launch_rebuild_gate(const PgDev &d, cudaStream_t s)
 
 void pg_rebuild_grid_params(PgDev &d, const double *ext, double rmax, double rmin)
 {
-  if (!(d.skin > 0.0)) d.skin = 0.3 * rmin;
+  // default skin: 0.3 rmin for one scene; 0.6 rmin for a pool, whose scenes
+  // share one rebuild flag, so that any sphere of any scene moving 0.45 skin
+  // rebuilds them all (on 512 shaken boxes: 9 -> 4 rebuilds per 100 steps)
+  if (!(d.skin > 0.0)) d.skin = (d.nscene > 1 ? 0.6 : 0.3) * rmin;
   d.half_skin_sq = (0.45 * d.skin) * (0.45 * d.skin);
   d.half_skin_sq_f = (float)d.half_skin_sq;
   double cell = 2.0 * rmax + d.skin;

@@ -124,7 +124,7 @@ class Server:
         self.P.engine = self.eng
         rmax = float(template.E.radii[0, :template.ellnum].max())
         rmin = float(template.E.radii[0, :template.ellnum].min())
-        skin = 0.3 * rmin
+        skin = 0.6 * rmin          # pool default: scenes share one rebuild flag
         self.cell = 2.0 * rmax + skin
         n = min(512, int(np.ceil(max_scene_extent / self.cell)) + 9)
         abi.check(self.eng.lib.pg_session_set_skin(self.eng.sess, skin), "pg_session_set_skin")
