@@ -1162,15 +1162,20 @@ double eqm(const pg_scene *s, int part1, const double *point1, int part2, const 
  * equal part0 to that particle (+=) and a run with equal part1 to that one
  * (-=), each run summed in spring order, the first run of its kind starting
  * from zero and later ones from their first element.  A run longer than
- * SPRING_RUN_LONG springs is summed in chunks (chunk sums in order, then the
- * chunk sums in order), as tasks whose boundaries fall on the chunks would
- * flush it; the GPU uses the same definition. */
+ * SPRING_RUN_LONG springs is summed in three levels: chunks of springs in
+ * spring order, groups of SPRING_RUN_GROUP chunk sums in order, then the
+ * group sums in order, as tasks whose boundaries fall on the chunks would
+ * flush their partials (the reference adds task partials under a lock, in an
+ * order that depends on the tasks, forces.ispc:1272-1327); the GPU uses the
+ * same definition.  Chunks hold 64 springs, doubled until there are at most
+ * SPRING_RUN_MAXCHUNKS. */
 static const int SPRING_RUN_LONG = 64;
-static const int SPRING_RUN_MAXCHUNKS = 512;
+static const int SPRING_RUN_MAXCHUNKS = 1024;
+static const int SPRING_RUN_GROUP = 32;
 
 static int spring_run_chunk(int len)
 {
-  int c = 256;
+  int c = 64;
   while ((len + c - 1) / c > SPRING_RUN_MAXCHUNKS) c *= 2;
   return c;
 }
@@ -1205,21 +1210,30 @@ static void spring_run_sum(const pg_scene *s, double *const out[9], const SprRun
     }
     return;
   }
-  const int len = r.e - r.b, ch = spring_run_chunk(len);
-  for (int b = r.b; b < r.e; b += ch)
+  const int len = r.e - r.b, ch = spring_run_chunk(len), nc = (len + ch - 1) / ch;
+  for (int g0 = 0; g0 < nc; g0 += SPRING_RUN_GROUP)
   {
-    double part[6] = {0, 0, 0, 0, 0, 0};
-    bool any = false;
-    for (int i = b; i < std::min(b + ch, r.e); i ++)
+    double gp[6] = {0, 0, 0, 0, 0, 0};
+    bool gany = false;
+    for (int c = g0; c < std::min(g0 + SPRING_RUN_GROUP, nc); c ++)
     {
-      if (skipped(i)) continue;
-      double x[6];
-      element(i, x);
-      add6(part, x, !any);
-      any = true;
+      const int b = r.b + c * ch;
+      double part[6] = {0, 0, 0, 0, 0, 0};
+      bool any = false;
+      for (int i = b; i < std::min(b + ch, r.e); i ++)
+      {
+        if (skipped(i)) continue;
+        double x[6];
+        element(i, x);
+        add6(part, x, !any);
+        any = true;
+      }
+      if (!any) continue;
+      add6(gp, part, !gany);
+      gany = true;
     }
-    if (!any) continue;
-    add6(acc, part, !started && !r.first);
+    if (!gany) continue;
+    add6(acc, gp, !started && !r.first);
     started = true;
   }
 }
@@ -1247,14 +1261,22 @@ static void spring_run_adaptive(const pg_scene *s, double *const ad[17], const S
     for (int i = r.b; i < r.e; i ++) if (!skipped(i)) add(i, p, km, em);
     return;
   }
-  const int len = r.e - r.b, ch = spring_run_chunk(len);
-  for (int b = r.b; b < r.e; b += ch)
+  const int len = r.e - r.b, ch = spring_run_chunk(len), nc = (len + ch - 1) / ch;
+  for (int g0 = 0; g0 < nc; g0 += SPRING_RUN_GROUP)
   {
-    double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, qk = 0.0, qe = 0.0;
-    for (int i = b; i < std::min(b + ch, r.e); i ++) if (!skipped(i)) add(i, q, &qk, &qe);
-    for (int c = 0; c < 9; c ++) p[c] = p[c] + q[c];
-    *km = qk > *km ? qk : *km;
-    *em = qe > *em ? qe : *em;
+    double gq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, gk = 0.0, ge = 0.0;
+    for (int c = g0; c < std::min(g0 + SPRING_RUN_GROUP, nc); c ++)
+    {
+      const int b = r.b + c * ch;
+      double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, qk = 0.0, qe = 0.0;
+      for (int i = b; i < std::min(b + ch, r.e); i ++) if (!skipped(i)) add(i, q, &qk, &qe);
+      for (int k = 0; k < 9; k ++) gq[k] = gq[k] + q[k];
+      gk = qk > gk ? qk : gk;
+      ge = qe > ge ? qe : ge;
+    }
+    for (int k = 0; k < 9; k ++) p[k] = p[k] + gq[k];
+    *km = gk > *km ? gk : *km;
+    *em = ge > *em ? ge : *em;
   }
 }
 

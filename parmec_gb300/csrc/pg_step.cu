@@ -885,33 +885,38 @@ __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
 // of springs_task) + prescribe_acceleration + dynamics_task +
 // prescribe_velocity + ellipsoids_task, one thread per particle.
 // ---------------------------------------------------------------- long spring flush runs
-// A run longer than PG_SPRING_RUN_LONG springs is summed in chunks: each
-// chunk in spring order (first element assigned), then the chunk sums in
-// order (the first-run rule applied to them), as springs_task tasks whose
-// boundaries fall on the chunks would flush it.  One block per run: thread c
-// sums chunk c, thread 0 sums the chunk sums.  A dependent FP64 add costs
-// tens of ns on this part, so one thread cannot sum 10^5 springs per step.
-constexpr int RUN_THREADS = 256;
-constexpr int RUN_MAXCHUNKS = 512;
+// A run longer than PG_SPRING_RUN_LONG springs is summed in three levels:
+// chunks of springs in spring order (first element assigned), groups of 32
+// chunk sums in order, then the group sums in order (the first-run rule
+// applied to them).  Chunks hold 64 springs, doubled until there are at most
+// 1,024.  One block per run: thread c sums chunk c, warp w sums group w (the
+// chunk sums of its lanes, in lane order, through shuffles), thread 0 sums
+// the group sums.  A dependent FP64 add costs tens of ns on this part, so
+// the sequential depth is kept near 64 + 32 + 32 adds for any run length.
+constexpr int RUN_THREADS = 1024;
+constexpr int RUN_MAXCHUNKS = RUN_THREADS;
+constexpr int RUN_GROUPS = RUN_THREADS / 32;
 
 __device__ __forceinline__ int run_chunk(int len)
 {
-  int c = 256;
+  int c = 64;
   while ((len + c - 1) / c > RUN_MAXCHUNKS) c *= 2;
   return c;
 }
 
 __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs(PgDev d)
 {
-  __shared__ double part[6][RUN_MAXCHUNKS];
-  __shared__ unsigned char has[RUN_MAXCHUNKS];
+  __shared__ double gpart[6][RUN_GROUPS];
+  __shared__ int ghas[RUN_GROUPS];
+  const unsigned full = 0xffffffffu;
   const int4 v = d.sbig[blockIdx.x];
   const int type = v.x & 1, off = type == 0 ? 3 : 6;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
-  for (int c = threadIdx.x; c < nc; c += RUN_THREADS)
+  const int c = threadIdx.x, lane = c & 31, w = c >> 5;
+  double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int any = 0;
+  if (c < nc)
   {
-    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    bool any = false;
     const int b = v.y + c * ch, e = min(b + ch, v.z);
     for (int s = b; s < e; s ++)
     {
@@ -920,39 +925,57 @@ __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs(PgDev d)
                            d.spr_out[off][s], d.spr_out[off+1][s], d.spr_out[off+2][s]};
       if (!any) for (int k = 0; k < 6; k ++) a[k] = x[k];
       else for (int k = 0; k < 6; k ++) a[k] = a[k] + x[k];
-      any = true;
+      any = 1;
     }
-    for (int k = 0; k < 6; k ++) part[k][c] = a[k];
-    has[c] = any ? 1 : 0;
+  }
+  double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int gany = 0;
+  for (int l = 0; l < 32; l ++)
+  {
+    const int la = __shfl_sync(full, any, l);
+    double x[6];
+    for (int k = 0; k < 6; k ++) x[k] = __shfl_sync(full, a[k], l);
+    if (!la) continue;
+    if (!gany) for (int k = 0; k < 6; k ++) g[k] = x[k];
+    else for (int k = 0; k < 6; k ++) g[k] = g[k] + x[k];
+    gany = 1;
+  }
+  if (lane == 0)
+  {
+    for (int k = 0; k < 6; k ++) gpart[k][w] = g[k];
+    ghas[w] = gany;
   }
   __syncthreads();
   if (threadIdx.x == 0)
   {
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     bool started = false;
-    for (int c = 0; c < nc; c ++)
+    for (int q = 0; q < RUN_GROUPS; q ++)
     {
-      if (!has[c]) continue;
-      if (!started && !v.w) for (int k = 0; k < 6; k ++) acc[k] = part[k][c];
-      else for (int k = 0; k < 6; k ++) acc[k] = acc[k] + part[k][c];
+      if (!ghas[q]) continue;
+      if (!started && !v.w) for (int k = 0; k < 6; k ++) acc[k] = gpart[k][q];
+      else for (int k = 0; k < 6; k ++) acc[k] = acc[k] + gpart[k][q];
       started = true;
     }
     for (int k = 0; k < 6; k ++) d.sbig_sum[6*blockIdx.x + k] = acc[k];
   }
 }
 
-// Adaptive stiffness partials of the long runs, chunked as the force sums:
-// each chunk sums its springs' terms from zero in spring order (maxima for
-// the stiffness and damping), then the chunk partials are summed in order.
+// Adaptive stiffness partials of the long runs, in the levels of the force
+// sums: each chunk sums its springs' terms from zero in spring order (maxima
+// for the stiffness and damping), each group its chunk partials from zero,
+// then the group partials from zero.
 __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
 {
-  __shared__ double part[11][RUN_MAXCHUNKS];
+  __shared__ double gpart[11][RUN_GROUPS];
+  const unsigned full = 0xffffffffu;
   const int4 v = d.sbig[blockIdx.x];
   const int type = v.x & 1, off = type == 0 ? 5 : 11;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
-  for (int c = threadIdx.x; c < nc; c += RUN_THREADS)
+  const int c = threadIdx.x, lane = c & 31, w = c >> 5;
+  double q[11] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (c < nc)
   {
-    double q[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, qk = 0.0, qe = 0.0;
     const int b = v.y + c * ch, e = min(b + ch, v.z);
     for (int s = b; s < e; s ++)
     {
@@ -960,22 +983,32 @@ __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
       for (int k = 0; k < 3; k ++) q[k] = q[k] + d.sad[k][s];
       for (int k = 0; k < 6; k ++) q[3+k] = q[3+k] + d.sad[off+k][s];
       const double xk = d.sad[3][s], xe = d.sad[4][s];
-      qk = xk > qk ? xk : qk;
-      qe = xe > qe ? xe : qe;
+      q[9] = xk > q[9] ? xk : q[9];
+      q[10] = xe > q[10] ? xe : q[10];
     }
-    for (int k = 0; k < 9; k ++) part[k][c] = q[k];
-    part[9][c] = qk;
-    part[10][c] = qe;
   }
+  // a group adds the partials of its chunks that lie in the run
+  double g[11] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int l = 0; l < 32; l ++)
+  {
+    double x[11];
+    for (int k = 0; k < 11; k ++) x[k] = __shfl_sync(full, q[k], l);
+    if (w * 32 + l >= nc) break;
+    for (int k = 0; k < 9; k ++) g[k] = g[k] + x[k];
+    g[9] = x[9] > g[9] ? x[9] : g[9];
+    g[10] = x[10] > g[10] ? x[10] : g[10];
+  }
+  if (lane == 0) for (int k = 0; k < 11; k ++) gpart[k][w] = g[k];
   __syncthreads();
   if (threadIdx.x == 0)
   {
     double p[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, km = 0.0, em = 0.0;
-    for (int c = 0; c < nc; c ++)
+    const int ng = (nc + 31) / 32;
+    for (int r = 0; r < ng; r ++)
     {
-      for (int k = 0; k < 9; k ++) p[k] = p[k] + part[k][c];
-      km = part[9][c] > km ? part[9][c] : km;
-      em = part[10][c] > em ? part[10][c] : em;
+      for (int k = 0; k < 9; k ++) p[k] = p[k] + gpart[k][r];
+      km = gpart[9][r] > km ? gpart[9][r] : km;
+      em = gpart[10][r] > em ? gpart[10][r] : em;
     }
     for (int k = 0; k < 9; k ++) d.sbig_ad[11*blockIdx.x + k] = p[k];
     d.sbig_ad[11*blockIdx.x + 9] = km;
