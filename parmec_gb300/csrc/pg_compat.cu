@@ -737,7 +737,8 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
     std::vector<int4> ev, big;
     pg_spring_events(parnum, (int)S, sprpart[0], sprpart[1], first, ev, big);
     ok = ok && up(d.sev_first, first.data(), P + 1) && up(d.sev, ev.data(), ev.size()) &&
-         up(d.sbig, big.data(), big.size()) && grow(d.sbig_sum, 6 * std::max<size_t>(1, big.size()));
+         up(d.sbig, big.data(), big.size()) && grow(d.sbig_sum, 6 * std::max<size_t>(1, big.size())) &&
+         grow(d.sbig_grp, 32 * 12 * std::max<size_t>(1, big.size()));
     if (adaptive) ok = ok && grow(d.sbig_ad, 11 * std::max<size_t>(1, big.size()));
     d.nbig = (int)big.size();
   }
@@ -805,7 +806,7 @@ void forces(int, master_conpnt master[], slave_conpnt[], int parnum, double *ang
   if (U) { pg_launch_unspring(v, G.st); G.launches += 1; }
   if (adaptive) pg_launch_force_sums_adapt(v, G.st);
   else pg_launch_force_sums(v, G.st);
-  G.launches += pg_contacts_kernel_count(v) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 2 : 1) : 0) + 1;
+  G.launches += pg_contacts_kernel_count(v) + (S ? 1 : 0) + (S && d.nbig ? (adaptive ? 4 : 2) : 0) + 1;
   for (int k = 0; ok && k < 3; k ++) ok = down(force[k], d.force[k], P) && down(torque[k], d.torque[k], P);
   if (adaptive)
   {

@@ -382,6 +382,7 @@ int upload_static(pg_session *s, const pg_scene *sc)
     d.nbig = (int)big.size();
     TRY(dalloc(s, &d.sbig, std::max<size_t>(1, big.size())));
     TRY(dalloc(s, &d.sbig_sum, 6 * std::max<size_t>(1, big.size())));
+    TRY(dalloc(s, &d.sbig_grp, 32 * 12 * std::max<size_t>(1, big.size())));
     TRY(h2d(s, d.sbig, big.data(), big.size()));
     CK(cudaStreamSynchronize(s->stream));
   }
@@ -1137,7 +1138,7 @@ int adaptive_kernel_count(const PgDev &d)
 {
   int n = pg_rebuild_kernel_count(d) + 2 + 1;     // excite, select, tail
   if (d.ellnum) n += 1;
-  if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0) + (d.unsprnum ? 1 : 0);
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 4 : 0) + (d.unsprnum ? 1 : 0);
   if (d.trqsprnum) n += 1;
   if (d.parnum) n += 3;                           // force sums, minimum, dynamics
   if (d.nodnum) n += 1;

@@ -58,6 +58,7 @@ struct PgDev
   int4 *sev;                // (type | (long run + 1) << 1, begin, end, first): type 0 = j-run (+=), 1 = k-run (-=)
   int4 *sbig;               // [nbig] the long runs
   double *sbig_sum;         // [nbig][6] their force and torque sums
+  double *sbig_grp;         // [nbig][32][12] group partials of the long-run sums
   int nbig;
 
   // ---- adaptive time step (parmec.ispc:275-420, forces.ispc:453-596, 1248-1345)

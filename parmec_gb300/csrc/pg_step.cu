@@ -889,13 +889,16 @@ __global__ void __launch_bounds__(TPB) k_springs(PgDev d, double step)
 // chunks of springs in spring order (first element assigned), groups of 32
 // chunk sums in order, then the group sums in order (the first-run rule
 // applied to them).  Chunks hold 64 springs, doubled until there are at most
-// 1,024.  One block per run: thread c sums chunk c, warp w sums group w (the
-// chunk sums of its lanes, in lane order, through shuffles), thread 0 sums
-// the group sums.  A dependent FP64 add costs tens of ns on this part, so
-// the sequential depth is kept near 64 + 32 + 32 adds for any run length.
-constexpr int RUN_THREADS = 1024;
-constexpr int RUN_MAXCHUNKS = RUN_THREADS;
-constexpr int RUN_GROUPS = RUN_THREADS / 32;
+// 1,024.  k_spring_run_groups runs one warp per group (grid: groups x runs):
+// lane l sums chunk 32 g + l, loading four springs at a time, and the warp
+// sums its chunk sums in lane order through shuffles; k_spring_run_totals
+// sums each run's group partials in order.  A dependent FP64 add costs tens
+// of ns on this part, so the sequential depth stays near 64 + 32 + 32 adds
+// for any run length, and the groups of a run spread over the SMs.
+constexpr int RUN_GROUP = 32;
+constexpr int RUN_MAXCHUNKS = 1024;
+constexpr int RUN_GROUPS = RUN_MAXCHUNKS / RUN_GROUP;
+constexpr int RUN_SLOT = 12;                   // doubles per group partial: 11 values, has-flag
 
 __device__ __forceinline__ int run_chunk(int len)
 {
@@ -904,75 +907,94 @@ __device__ __forceinline__ int run_chunk(int len)
   return c;
 }
 
-__global__ void __launch_bounds__(RUN_THREADS) k_spring_runs(PgDev d)
+__global__ void __launch_bounds__(RUN_GROUP) k_spring_run_groups(PgDev d)
 {
-  __shared__ double gpart[6][RUN_GROUPS];
-  __shared__ int ghas[RUN_GROUPS];
   const unsigned full = 0xffffffffu;
-  const int4 v = d.sbig[blockIdx.x];
+  const int run = blockIdx.y, g = blockIdx.x, lane = threadIdx.x;
+  const int4 v = d.sbig[run];
   const int type = v.x & 1, off = type == 0 ? 3 : 6;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
-  const int c = threadIdx.x, lane = c & 31, w = c >> 5;
+  if (g * RUN_GROUP >= nc) return;
+  const int c = g * RUN_GROUP + lane;
   double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   int any = 0;
   if (c < nc)
   {
     const int b = v.y + c * ch, e = min(b + ch, v.z);
-    for (int s = b; s < e; s ++)
+    for (int s0 = b; s0 < e; s0 += 4)
     {
-      if (type == 1 && d.sprpart[1][s] < 0) continue;
-      const double x[6] = {d.spr_out[0][s], d.spr_out[1][s], d.spr_out[2][s],
-                           d.spr_out[off][s], d.spr_out[off+1][s], d.spr_out[off+2][s]};
-      if (!any) for (int k = 0; k < 6; k ++) a[k] = x[k];
-      else for (int k = 0; k < 6; k ++) a[k] = a[k] + x[k];
-      any = 1;
+      double x[4][6];
+      bool ok[4];
+      #pragma unroll
+      for (int u = 0; u < 4; u ++)
+      {
+        const int sp = s0 + u < e ? s0 + u : b;
+        ok[u] = s0 + u < e && !(type == 1 && d.sprpart[1][sp] < 0);
+        x[u][0] = d.spr_out[0][sp]; x[u][1] = d.spr_out[1][sp]; x[u][2] = d.spr_out[2][sp];
+        x[u][3] = d.spr_out[off][sp]; x[u][4] = d.spr_out[off+1][sp]; x[u][5] = d.spr_out[off+2][sp];
+      }
+      #pragma unroll
+      for (int u = 0; u < 4; u ++)
+        if (ok[u])
+        {
+          if (!any) for (int k = 0; k < 6; k ++) a[k] = x[u][k];
+          else for (int k = 0; k < 6; k ++) a[k] = a[k] + x[u][k];
+          any = 1;
+        }
     }
   }
-  double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double gs[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   int gany = 0;
-  for (int l = 0; l < 32; l ++)
+  for (int l = 0; l < RUN_GROUP; l ++)
   {
     const int la = __shfl_sync(full, any, l);
     double x[6];
     for (int k = 0; k < 6; k ++) x[k] = __shfl_sync(full, a[k], l);
     if (!la) continue;
-    if (!gany) for (int k = 0; k < 6; k ++) g[k] = x[k];
-    else for (int k = 0; k < 6; k ++) g[k] = g[k] + x[k];
+    if (!gany) for (int k = 0; k < 6; k ++) gs[k] = x[k];
+    else for (int k = 0; k < 6; k ++) gs[k] = gs[k] + x[k];
     gany = 1;
   }
   if (lane == 0)
   {
-    for (int k = 0; k < 6; k ++) gpart[k][w] = g[k];
-    ghas[w] = gany;
+    double *o = d.sbig_grp + ((size_t)run * RUN_GROUPS + g) * RUN_SLOT;
+    for (int k = 0; k < 6; k ++) o[k] = gs[k];
+    o[11] = gany ? 1.0 : 0.0;
   }
-  __syncthreads();
-  if (threadIdx.x == 0)
+}
+
+__global__ void k_spring_run_totals(PgDev d)
+{
+  const int run = blockIdx.x * blockDim.x + threadIdx.x;
+  if (run >= d.nbig) return;
+  const int4 v = d.sbig[run];
+  const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch, ng = (nc + RUN_GROUP - 1) / RUN_GROUP;
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  bool started = false;
+  for (int q = 0; q < ng; q ++)
   {
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    bool started = false;
-    for (int q = 0; q < RUN_GROUPS; q ++)
-    {
-      if (!ghas[q]) continue;
-      if (!started && !v.w) for (int k = 0; k < 6; k ++) acc[k] = gpart[k][q];
-      else for (int k = 0; k < 6; k ++) acc[k] = acc[k] + gpart[k][q];
-      started = true;
-    }
-    for (int k = 0; k < 6; k ++) d.sbig_sum[6*blockIdx.x + k] = acc[k];
+    const double *o = d.sbig_grp + ((size_t)run * RUN_GROUPS + q) * RUN_SLOT;
+    if (o[11] == 0.0) continue;
+    if (!started && !v.w) for (int k = 0; k < 6; k ++) acc[k] = o[k];
+    else for (int k = 0; k < 6; k ++) acc[k] = acc[k] + o[k];
+    started = true;
   }
+  for (int k = 0; k < 6; k ++) d.sbig_sum[6*run + k] = acc[k];
 }
 
 // Adaptive stiffness partials of the long runs, in the levels of the force
 // sums: each chunk sums its springs' terms from zero in spring order (maxima
-// for the stiffness and damping), each group its chunk partials from zero,
-// then the group partials from zero.
-__global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
+// for the stiffness and damping), each group the partials of its chunks from
+// zero, then the group partials from zero.
+__global__ void __launch_bounds__(RUN_GROUP) k_spring_run_groups_adapt(PgDev d)
 {
-  __shared__ double gpart[11][RUN_GROUPS];
   const unsigned full = 0xffffffffu;
-  const int4 v = d.sbig[blockIdx.x];
+  const int run = blockIdx.y, g = blockIdx.x, lane = threadIdx.x;
+  const int4 v = d.sbig[run];
   const int type = v.x & 1, off = type == 0 ? 5 : 11;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
-  const int c = threadIdx.x, lane = c & 31, w = c >> 5;
+  if (g * RUN_GROUP >= nc) return;
+  const int c = g * RUN_GROUP + lane;
   double q[11] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (c < nc)
   {
@@ -987,33 +1009,40 @@ __global__ void __launch_bounds__(RUN_THREADS) k_spring_runs_adapt(PgDev d)
       q[10] = xe > q[10] ? xe : q[10];
     }
   }
-  // a group adds the partials of its chunks that lie in the run
-  double g[11] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int l = 0; l < 32; l ++)
+  double gq[11] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int l = 0; l < RUN_GROUP; l ++)
   {
     double x[11];
     for (int k = 0; k < 11; k ++) x[k] = __shfl_sync(full, q[k], l);
-    if (w * 32 + l >= nc) break;
-    for (int k = 0; k < 9; k ++) g[k] = g[k] + x[k];
-    g[9] = x[9] > g[9] ? x[9] : g[9];
-    g[10] = x[10] > g[10] ? x[10] : g[10];
+    if (g * RUN_GROUP + l >= nc) break;
+    for (int k = 0; k < 9; k ++) gq[k] = gq[k] + x[k];
+    gq[9] = x[9] > gq[9] ? x[9] : gq[9];
+    gq[10] = x[10] > gq[10] ? x[10] : gq[10];
   }
-  if (lane == 0) for (int k = 0; k < 11; k ++) gpart[k][w] = g[k];
-  __syncthreads();
-  if (threadIdx.x == 0)
+  if (lane == 0)
   {
-    double p[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, km = 0.0, em = 0.0;
-    const int ng = (nc + 31) / 32;
-    for (int r = 0; r < ng; r ++)
-    {
-      for (int k = 0; k < 9; k ++) p[k] = p[k] + gpart[k][r];
-      km = gpart[9][r] > km ? gpart[9][r] : km;
-      em = gpart[10][r] > em ? gpart[10][r] : em;
-    }
-    for (int k = 0; k < 9; k ++) d.sbig_ad[11*blockIdx.x + k] = p[k];
-    d.sbig_ad[11*blockIdx.x + 9] = km;
-    d.sbig_ad[11*blockIdx.x + 10] = em;
+    double *o = d.sbig_grp + ((size_t)run * RUN_GROUPS + g) * RUN_SLOT;
+    for (int k = 0; k < 11; k ++) o[k] = gq[k];
   }
+}
+
+__global__ void k_spring_run_totals_adapt(PgDev d)
+{
+  const int run = blockIdx.x * blockDim.x + threadIdx.x;
+  if (run >= d.nbig) return;
+  const int4 v = d.sbig[run];
+  const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch, ng = (nc + RUN_GROUP - 1) / RUN_GROUP;
+  double p[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, km = 0.0, em = 0.0;
+  for (int r = 0; r < ng; r ++)
+  {
+    const double *o = d.sbig_grp + ((size_t)run * RUN_GROUPS + r) * RUN_SLOT;
+    for (int k = 0; k < 9; k ++) p[k] = p[k] + o[k];
+    km = o[9] > km ? o[9] : km;
+    em = o[10] > em ? o[10] : em;
+  }
+  for (int k = 0; k < 9; k ++) d.sbig_ad[11*run + k] = p[k];
+  d.sbig_ad[11*run + 9] = km;
+  d.sbig_ad[11*run + 10] = em;
 }
 
 // MODE: INT_FUSED runs the whole particle update of one step; the drop-in
@@ -1837,8 +1866,16 @@ void pg_launch_unspring(const PgDev &d, cudaStream_t s)
 
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
 {
-  if (d.sprnum && d.nbig > 0) k_spring_runs<<<d.nbig, RUN_THREADS, 0, s>>>(d);
-  if (d.sprnum && d.nbig > 0 && d.hs) k_spring_runs_adapt<<<d.nbig, RUN_THREADS, 0, s>>>(d);
+  if (!(d.sprnum && d.nbig > 0)) return;
+  const dim3 grid(RUN_GROUPS, d.nbig);
+  const int tb = (d.nbig + 127) / 128;
+  k_spring_run_groups<<<grid, RUN_GROUP, 0, s>>>(d);
+  k_spring_run_totals<<<tb, 128, 0, s>>>(d);
+  if (d.hs)
+  {
+    k_spring_run_groups_adapt<<<grid, RUN_GROUP, 0, s>>>(d);
+    k_spring_run_totals_adapt<<<tb, 128, 0, s>>>(d);
+  }
 }
 
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
@@ -1907,7 +1944,7 @@ int pg_step_kernel_count(const PgDev &d)
 {
   int n = 2;                                   // excite, tail
   n += pg_contacts_kernel_count(d);            // contacts: sphere and triangle passes
-  if (d.sprnum) n += 1 + (d.nbig > 0 ? 1 : 0) + (d.unsprnum ? 1 : 0);
+  if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0) + (d.unsprnum ? 1 : 0);
   if (d.trqsprnum) n += 1;                     // torsion springs
   if (d.parnum) n += 1;                        // integrate
   if (d.nodnum) n += 1;
