@@ -289,6 +289,16 @@ int pg_session_restrain_velocities(pg_session *s);
  * form, one scene without device excitation; else PG_ERR_UNSUPPORTED. */
 int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, double adaptive, double *steps);
 
+/* CRITICAL (input.cpp:3034-3154) on the device.  which = 0: per particle
+ * (critical_perparticle, parmec.ispc:547-888) from the contacts of the last
+ * step and the springs: h, omega, ratio get parnum entries; which = 1: per
+ * spring (critical_perspring, parmec.ispc:485-544): sprnum entries, in the
+ * session's sorted spring order.  Contact normals are the recorded ones when
+ * the session records geometry (pg_session_record_geometry), else the
+ * direction from the partner to the sphere centre at the current positions.
+ * FP64 form; PG_ERR_UNSUPPORTED for the mixed form. */
+int pg_session_critical(pg_session *s, int which, double *h, double *omega, double *ratio);
+
 /* Wait for the session stream; returns the first device error seen. */
 int pg_session_sync(pg_session *s);
 
@@ -440,9 +450,11 @@ int pg_cell_order(const double *x, const double *y, const double *z, int n,
  * a static device array of the library, sized for at most 65,536 spheres
  * (about 0.55 MB, held by every GPU that loads the library until exit);
  * larger n returns PG_ERR_CAPACITY.  Calls share that array: calls that
- * overlap on the GPU race.  The first call on a device sets up the array's
- * address and should come before any stream capture.  Same arguments and
- * results as pg_cell_order. */
+ * overlap on the GPU race.  A call on a stream that is not capturing looks
+ * up the array's address on the current device; a call during stream
+ * capture uses the address found by the last such call, so the first call
+ * on a device (and the first after a device reset) should come before any
+ * stream capture.  Same arguments and results as pg_cell_order. */
 int pg_cell_order_static(const double *x, const double *y, const double *z, int n,
                          const double origin[3], double cell, const int dim[3],
                          unsigned *keys_out, int *order_out, void *stream);

@@ -144,15 +144,41 @@ void shapes (int ntasks, int ellnum, int part[], double *center[6], double *radi
 void obstacles (int obsnum, int trirng[], double point[], double angular[], double linear[],
                 double *tri[3][3], double step);
 
-/* ---- exports outside the DEM hot path.  They exist so that parmec.cpp
- * links; with nothing to do (rstnum == 0) they return, else they report an
- * unsupported case (restraints, adaptive stepping, CRITICAL, EQM). */
+/* ---- restraints and adaptive stepping, called by dem() beside the hot
+ * path (restrain.ispc:137, 147; parmec.ispc:397-420).  All three run on the
+ * device with host arrays copied in and out. */
 void restrain_velocities (int ntasks, int rstnum, int rstpart[], double *rstlin[9], double *rstang[9],
                           double *linear[3], double *angular[6], double *rotation[9]);
 void restrain_forces (int ntasks, int rstnum, int rstpart[], double *rstlin[9], double *rstang[9],
                       double *force[3], double *torque[3]);
 double adaptive_timestep (int ntasks, int parnum, double mass[], double *inertia[9], double *kact[3],
                           double kmax[], double emax[], double *krot[6], double step, double adaptive);
+
+/* ---- the setup-time queries input.cpp calls (EQM input.cpp:2378, CRITICAL
+ * input.cpp:3064, 3097, 3133), on the device. */
+/* eqm (parmec.ispc:423): equivalent point mass of part1 at point1 and part2
+ * (or -1: ground) at point2 along direction (zero length: the smallest
+ * eigenvalue direction); reads position[3..5] (reference positions) */
+double eqm (int part1, double *point1, int part2, double *point2, double *direction,
+            double *inverse[9], double invm[], double *position[3]);
+/* critical_perspring (parmec.ispc:485): per-spring critical step hcri,
+ * circular frequency ocri and damping ratio rcri; particles are read up to
+ * the largest index the springs name */
+void critical_perspring (int sprnum, int *sprpart[2], double *sprpnt[2][6], double *sprdir[6],
+                         double *spring[2], int spridx[], double *dashpot[2], int dashidx[],
+                         double *inverse[9], double invm[], double *position[3],
+                         double hcri[], double ocri[], double rcri[]);
+/* critical_perparticle (parmec.ispc:860): per-particle critical step, frequency
+ * and ratio from the contacts that condet()/forces() hold for this master
+ * array and from the springs; kact, kmax, emax and krot receive the terms.
+ * Returns the smallest step (the reference leaves its return value unset). */
+double critical_perparticle (int ntasks, struct master_conpnt master[], struct slave_conpnt slave[],
+                             int parnum, double mass[], double *inertia[9], double invm[],
+                             double *inverse[9], double *rotation[9], double *position[6],
+                             int sprnum, int sprflg[], int *sprpart[2], double *sprpnt[2][6],
+                             double *sprdir[6], double *spring[2], int spridx[], double *dashpot[2],
+                             int dashidx[], double *kact[3], double kmax[], double emax[],
+                             double *krot[6], double hcri[], double ocri[], double rcri[]);
 
 /* ---- GB300 additions (not in the reference) */
 int pg_compat_status (void);               /* first error since the last call (PG_ERR_*), then cleared */

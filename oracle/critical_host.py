@@ -1,7 +1,9 @@
-"""CRITICAL per particle (input.cpp:3034-3154, parmec.ispc:275-383, 547-900).
+"""CRITICAL restated on the host (TEST INFRASTRUCTURE ONLY; input.cpp:3034-3154,
+parmec.ispc:275-383, 485-900).
 
-The per-particle critical step estimate of the reference, over the current
-contacts (exported from the device session) and springs:
+The oracle engine's CRITICAL and the checker of the device's
+(pg_session_critical).  The per-particle critical step estimate of the
+reference, over the current contacts and springs:
 
 * critical_perparticle_contacts (parmec.ispc:547-650): per particle, the
   contacts it takes part in add the absolute contact-normal components to
@@ -15,8 +17,7 @@ contacts (exported from the device session) and springs:
   K x = lambda J x through a Cholesky factor of J, and the damped step
   (2/w)(sqrt(1+ksi^2) - ksi) of each, the smaller taken.
 
-A setup-time query, not a step: evaluated on the host over data downloaded
-from the session.  Positions taken:
+Positions taken (the device takes the same):
 * the slave side of a contact uses the contact's own normal stiffness and
   damping; the reference reads them from slave records it never sets
   (the slave copy, forces.ispc:383-405, copies point and force only);
@@ -31,44 +32,9 @@ import math
 
 import numpy as np
 
+from parmec_gb300.springs import _eqm, _extremum_eigenvalue, _triple_angle_root  # noqa: F401
+
 REAL_MAX = 1.7976931348623157E+308
-
-
-def _triple_angle_root(r, largest):
-    """cos(acos(r)/3) (largest) or cos(acos(r)/3 + 2 pi/3) as roots of the
-    triple-angle identity 4c^3 - 3c = r, by Newton's method from c = 1 (or -1),
-    monotone on [1/2, 1] (and [-1, -1/2]); the device and the CPU restatement
-    run the same operations."""
-    r = -1.0 if r < -1.0 else (1.0 if r > 1.0 else r)
-    c = 1.0 if largest else -1.0
-    for _ in range(100):
-        f = (4.0 * c * c - 3.0) * c - r
-        den = 12.0 * c * c - 3.0
-        if den == 0.0:
-            break
-        cn = c - f / den
-        if (largest and not cn < c) or (not largest and not cn > c):
-            break
-        c = cn
-    return c
-
-
-def _extremum_eigenvalue(A, minimum):
-    """extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3;
-    its diagonal branch returns the largest entry whichever is asked for."""
-    p1 = A[3] * A[3] + A[6] * A[6] + A[7] * A[7]
-    if p1 == 0.0:
-        r = A[0] if A[0] > A[4] else A[4]
-        return r if r > A[8] else A[8]
-    q = (A[0] + A[4] + A[8]) / 3.0
-    p2 = (A[0] - q) * (A[0] - q) + (A[4] - q) * (A[4] - q) + (A[8] - q) * (A[8] - q) + 2 * p1
-    p = math.sqrt(p2 / 6.0)
-    invp = 1.0 / p
-    B = [invp * (A[0] - q), invp * A[1], invp * A[2], invp * A[3], invp * (A[4] - q), invp * A[5],
-         invp * A[6], invp * A[7], invp * (A[8] - q)]
-    det = (B[0] * (B[4] * B[8] - B[5] * B[7]) + B[3] * (B[2] * B[7] - B[1] * B[8])
-           + B[6] * (B[1] * B[5] - B[2] * B[4]))
-    return q + 2.0 * p * _triple_angle_root(0.5 * det, not minimum)
 
 
 def pairing(m, i, j):
@@ -144,11 +110,14 @@ def _contact_terms(m, contacts, kact, kmax, emax, krot):
     ci = E.center[0:3, pell[mp]]
     sph = code >= 0
     pj = np.where(sph, E.part[np.maximum(code, 0)], m.Tr.triobs[np.maximum(-code - 1, 0)]).astype(np.int64)
-    # normal: from the partner centre (sphere) or the contact point (triangle) to the master centre
-    other = np.where(sph, E.center[0:3, np.maximum(code, 0)], pnt)
-    q = ci - other
-    ln = np.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2])
-    nrm = q / np.where(ln > 0.0, ln, 1.0)
+    # normal: the recorded one, else from the partner centre (sphere) or the
+    # contact point (triangle) to the master centre
+    nrm = contacts["normal"].T if "normal" in contacts else None
+    if nrm is None or not np.all(np.isfinite(nrm)):
+        other = np.where(sph, E.center[0:3, np.maximum(code, 0)], pnt)
+        q = ci - other
+        ln = np.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2])
+        nrm = q / np.where(ln > 0.0, ln, 1.0)
     # normal stiffness and damping of each contact (forces.ispc:125-147)
     coli = E.ellcol[pell[mp]]
     colj = np.where(sph, E.ellcol[np.maximum(code, 0)], m.Tr.tricol[np.maximum(-code - 1, 0)])
@@ -180,7 +149,7 @@ def _contact_terms(m, contacts, kact, kmax, emax, krot):
 
 
 def _spring_terms(m, kact, kmax, emax, krot):
-    from .springs import SPRDIR_PLANAR, _eqm
+    from parmec_gb300.springs import SPRDIR_PLANAR, _eqm
     S, P = m.S, m.P
     for j in range(m.sprnum):
         i, k = int(S.sprpart[0, j]), int(S.sprpart[1, j])
@@ -337,3 +306,33 @@ def critical_perparticle(m, contacts=None):
         _contact_terms(m, contacts, kact, kmax, emax, krot)
     _spring_terms(m, kact, kmax, emax, krot)
     return _time_steps(m, kact, kmax, emax, krot)
+
+
+def critical_perspring(m):
+    """critical_perspring (parmec.ispc:485-544): per-spring critical step, omega, damping ratio."""
+    S = m.S
+    h, o, r = [], [], []
+    for j in range(m.sprnum):
+        i, k = int(S.sprpart[0, j]), int(S.sprpart[1, j])
+        sp = m.spring_tab[j]
+        kspr = 0.0
+        for a in range(len(sp) - 1):
+            kk = (sp[a + 1][1] - sp[a][1]) / (sp[a + 1][0] - sp[a][0])
+            kspr = max(abs(kk), kspr)
+        mspr = _eqm(m, i, S.sprpnt[3:6, j], k, S.sprpnt[9:12, j], S.sprdir[0:3, j])
+        omega = math.sqrt(kspr / mspr)
+        ksi = 0.0
+        dp = m.dashpot_tab[j]
+        if len(dp) == 1:
+            ksi = dp[0][0]
+        else:
+            espr = 0.0
+            for a in range(len(dp) - 1):
+                e = (dp[a + 1][1] - dp[a][1]) / (dp[a + 1][0] - dp[a][0])
+                espr = max(abs(e), espr)
+            if omega > 0.0:
+                ksi = espr / (2 * mspr * omega)
+        h.append((2.0 / omega) * (math.sqrt(1.0 + ksi * ksi) - ksi) if omega > 0.0 else 1.0)
+        o.append(omega)
+        r.append(ksi)
+    return h, o, r

@@ -121,6 +121,14 @@ class OracleEngine:
             raise RuntimeError("no adaptive step has run")
         return h[:n], o[:n], r[:n]
 
+    def critical(self, which):
+        """CRITICAL restated on the host (oracle/critical_host.py) over this
+        engine's contacts: which = 0 per particle, 1 per spring."""
+        from oracle import critical_host
+        if which == 1:
+            return tuple(np.array(a) for a in critical_host.critical_perspring(self.model))
+        return critical_host.critical_perparticle(self.model, self.contacts())
+
     def sync(self):
         pass
 

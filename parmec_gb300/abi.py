@@ -157,6 +157,7 @@ def load_library():
         "pg_session_run": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double]),
         "pg_session_run_adaptive": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double, ctypes.c_double, D]),
         "pg_session_restrain_velocities": (ctypes.c_int, [P]),
+        "pg_session_critical": (ctypes.c_int, [P, ctypes.c_int, D, D, D]),
         "pg_session_download_particles": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_download_springs": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_sync": (ctypes.c_int, [P]),

@@ -63,6 +63,10 @@ struct Compat
   const char *fn = "";                        // entry point running (for messages)
   std::vector<int> h_part, h_ellcol, h_triobs, h_tricol;   // of the last condet(), for materialize
   double *hs = nullptr;                       // adaptive stepping: step0, step1, factor (view().hs when used)
+  double *crit_ke = nullptr;                  // CRITICAL: per-spring largest slope and damping
+  double *crit_h = nullptr, *crit_o = nullptr, *crit_r = nullptr;   // CRITICAL outputs
+  PgDev eqd{};                                // eqm: the two particles' rows
+  double *eq_pts = nullptr, *eq_out = nullptr;
 };
 
 Compat G;
@@ -965,6 +969,142 @@ double adaptive_timestep(int, int parnum, double mass[], double *inertia[9], dou
   double h1 = curstep;
   if (!down(&h1, G.hs + 1, 1) || !finish("adaptive_timestep")) return curstep;
   return h1;
+}
+
+// ---------------------------------------------------------------- eqm (parmec.ispc:423-482)
+// The equivalent point mass of the EQM command (input.cpp:2336-2381): the
+// two particles' rows go to the device and the same eqm as the springs'
+// critical damping evaluates it.
+double eqm(int part1, double *point1, int part2, double *point2, double *direction, double *inverse[9],
+           double invm[], double *position[3])
+{
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "eqm";
+  if (part1 < 0 || !point1 || !inverse || !invm || !position || !ready()) return 0.0;
+  PgDev &e = G.eqd;
+  const int n = part2 >= 0 ? 2 : 1;
+  const int rows[2] = {part1, part2};
+  double inv[9][2], im[2], pos[3][2], pts[9];
+  for (int r = 0; r < n; r ++)
+  {
+    for (int k = 0; k < 9; k ++) inv[k][r] = inverse[k][rows[r]];
+    im[r] = invm[rows[r]];
+    for (int k = 0; k < 3; k ++) pos[k][r] = position[3+k][rows[r]];
+  }
+  for (int k = 0; k < 3; k ++)
+  {
+    pts[k] = point1[k];
+    pts[3+k] = part2 >= 0 && point2 ? point2[k] : 0.0;
+    pts[6+k] = direction ? direction[k] : 0.0;
+  }
+  bool ok = up(e.invm, im, n) && up(G.eq_pts, pts, 9) && grow(G.eq_out, 1);
+  for (int k = 0; ok && k < 9; k ++) ok = up(e.inverse[k], inv[k], n);
+  for (int k = 0; ok && k < 3; k ++) ok = up(e.position[3+k], pos[k], n);
+  if (!ok) return 0.0;
+  pg_launch_eqm_one(e, G.st, part2, G.eq_pts, G.eq_out);
+  G.launches += 1;
+  double out = 0.0;
+  if (!down(&out, G.eq_out, 1) || !finish("eqm")) return 0.0;
+  return out;
+}
+
+// upload the spring arrays CRITICAL reads; P particles' rows of inverse,
+// invm and the reference positions (for eqm)
+static bool upload_critical_springs(int P, int sprnum, int *sprpart[2], double *sprpnt[2][6], double *sprdir[6],
+                                    double *spring[2], int spridx[], double *dashpot[2], int dashidx[],
+                                    double *inverse[9], double invm[], double *position[], int sprflg[])
+{
+  PgDev &d = G.d;
+  const size_t S = sprnum;
+  bool ok = up(d.invm, invm, P);
+  for (int k = 0; ok && k < 9; k ++) ok = up(d.inverse[k], inverse[k], P);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.position[3+k], position[3+k], P);
+  for (int k = 0; ok && k < 2; k ++) ok = up(d.sprpart[k], sprpart[k], S);
+  for (int a = 0; ok && a < 2; a ++)
+    for (int k = 0; ok && k < 6; k ++) ok = up(d.sprpnt[6*a+k], sprpnt[a][k], S);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.sprdir[k], sprdir[k], S);
+  const size_t ns = spridx ? spridx[S] : 0, nd = dashidx ? dashidx[S] : 0;
+  for (int k = 0; ok && k < 2; k ++) ok = up(d.spring[k], spring[k], ns) && up(d.dashpot[k], dashpot[k], nd);
+  ok = ok && up(d.spridx, spridx, S + 1) && up(d.dashidx, dashidx, S + 1);
+  if (sprflg) ok = ok && up(d.sprflg, sprflg, S);
+  return ok;
+}
+
+// ---------------------------------------------------------------- critical_perspring (parmec.ispc:485-544)
+void critical_perspring(int sprnum, int *sprpart[2], double *sprpnt[2][6], double *sprdir[6], double *spring[2],
+                        int spridx[], double *dashpot[2], int dashidx[], double *inverse[9], double invm[],
+                        double *position[3], double hcri[], double ocri[], double rcri[])
+{
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "critical_perspring";
+  if (sprnum <= 0 || !ready()) return;
+  // the call names no particle count: the rows up to the largest spring end
+  int P = 1;
+  for (int j = 0; j < sprnum; j ++) P = std::max(P, std::max(sprpart[0][j], sprpart[1][j]) + 1);
+  const size_t S = sprnum;
+  bool ok = upload_critical_springs(P, sprnum, sprpart, sprpnt, sprdir, spring, spridx, dashpot, dashidx, inverse,
+                                    invm, position, nullptr) &&
+            grow(G.crit_h, S) && grow(G.crit_o, S) && grow(G.crit_r, S);
+  if (!ok) return;
+  PgDev v = view();
+  v.sprnum = sprnum;
+  pg_launch_critical_perspring(v, G.st, G.crit_h, G.crit_o, G.crit_r);
+  G.launches += 1;
+  ok = down(hcri, G.crit_h, S) && down(ocri, G.crit_o, S) && down(rcri, G.crit_r, S);
+  if (ok) finish("critical_perspring");
+}
+
+// ---------------------------------------------------------------- critical_perparticle (parmec.ispc:860-888)
+// The contact terms come from the device contact lists that condet() and
+// forces() keep for this master array.  Returns the smallest particle step
+// (the reference declares a return value it never sets).
+double critical_perparticle(int, master_conpnt master[], slave_conpnt[], int parnum, double mass[],
+                            double *inertia[9], double invm[], double *inverse[9], double *rotation[9],
+                            double *position[6], int sprnum, int sprflg[], int *sprpart[2], double *sprpnt[2][6],
+                            double *sprdir[6], double *spring[2], int spridx[], double *dashpot[2], int dashidx[],
+                            double *kact[3], double kmax[], double emax[], double *krot[6], double hcri[],
+                            double ocri[], double rcri[])
+{
+  std::lock_guard<std::mutex> g(M);
+  G.fn = "critical_perparticle";
+  const double big = 1.7976931348623157e308;
+  if (parnum <= 0 || !ready()) return big;
+  PgDev &d = G.d;
+  const size_t P = parnum, S = std::max(sprnum, 0);
+  const bool contacts = G.lists && G.owner == (const void *)master && G.P == parnum && G.E > 0;
+  bool ok = up(d.mass, mass, P) && up(d.invm, invm, P);
+  for (int k = 0; ok && k < 9; k ++) ok = up(d.inertia[k], inertia[k], P) && up(d.rotation[k], rotation[k], P);
+  for (int k = 0; ok && k < 3; k ++) ok = up(d.position[k], position[k], P);
+  if (S)
+  {
+    ok = ok && upload_critical_springs(parnum, sprnum, sprpart, sprpnt, sprdir, spring, spridx, dashpot, dashidx,
+                                       inverse, invm, position, sprflg);
+    std::vector<int> first;
+    std::vector<int4> ev, bigv;
+    pg_spring_events(parnum, (int)S, sprpart[0], sprpart[1], first, ev, bigv);
+    ok = ok && up(d.sev_first, first.data(), P + 1) && up(d.sev, ev.data(), ev.size());
+  }
+  for (int k = 0; ok && k < 3; k ++) ok = grow(d.akact[k], P);
+  for (int k = 0; ok && k < 6; k ++) ok = grow(d.akrot[k], P);
+  ok = ok && grow(d.akmax, P) && grow(d.aemax, P) && grow(G.crit_ke, 2 * std::max<size_t>(S, 1)) &&
+       grow(G.crit_h, P) && grow(G.crit_o, P) && grow(G.crit_r, P);
+  if (!ok) return big;
+  PgDev v = view();
+  v.parnum = parnum;
+  v.sprnum = (int)S;
+  if (!contacts) { v.ellnum = 0; v.pell = nullptr; }
+  pg_launch_critical_perparticle(v, G.st, G.crit_ke, contacts ? 1 : 0, G.crit_h, G.crit_o, G.crit_r);
+  G.launches += S ? 2 : 1;
+  for (int k = 0; ok && k < 3; k ++) ok = down(kact ? kact[k] : nullptr, d.akact[k], P);
+  for (int k = 0; ok && k < 6; k ++) ok = down(krot ? krot[k] : nullptr, d.akrot[k], P);
+  ok = ok && down(kmax, d.akmax, P) && down(emax, d.aemax, P);
+  std::vector<double> hv(hcri ? 0 : P);
+  double *hout = hcri ? hcri : hv.data();
+  ok = ok && down(hout, G.crit_h, P) && down(ocri, G.crit_o, P) && down(rcri, G.crit_r, P);
+  if (!ok || !finish("critical_perparticle")) return big;
+  double hmin = big;
+  for (size_t i = 0; i < P; i ++) hmin = hout[i] < hmin ? hout[i] : hmin;
+  return hmin;
 }
 
 // ---------------------------------------------------------------- additions

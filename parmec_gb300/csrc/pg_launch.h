@@ -25,6 +25,10 @@ void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double ste
 void pg_launch_force_sums_adapt(const PgDev &d, cudaStream_t s);
 void pg_launch_adapt_step(const PgDev &d, cudaStream_t s);
 void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s);
+void pg_launch_critical_perspring(const PgDev &d, cudaStream_t s, double *h, double *om, double *ra);
+void pg_launch_critical_perparticle(const PgDev &d, cudaStream_t s, double *ke, int use_contacts, double *h,
+                                    double *om, double *ra);
+void pg_launch_eqm_one(const PgDev &d, cudaStream_t s, int part2, const double *pts, double *out);
 void pg_launch_restrain_velocities(const PgDev &d, cudaStream_t s);   // once per DEM call
 void pg_launch_restrain_forces(const PgDev &d, cudaStream_t s);       // drop-in export (fused steps do it in k_integrate)
 void pg_launch_mesh(const PgDev &d, cudaStream_t s);

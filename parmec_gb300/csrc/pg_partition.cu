@@ -79,13 +79,19 @@ extern "C" int pg_cell_order(const double *x, const double *y, const double *z, 
 // exits.  Every call on a device shares the one array, so calls that overlap
 // on the GPU (from different streams or threads) race and must not be made.
 // Nothing in the array needs to start at zero: each sort pass writes every
-// histogram entry and every key before it reads them.  The first call on a
-// device looks up the array's device address (cudaGetSymbolAddress); make
-// that first call before any stream capture on the device.
+// histogram entry and every key before it reads them.  Each call on a
+// stream that is not capturing looks up the array's device address
+// (cudaGetSymbolAddress) with the caller's device current; a call on a
+// capturing stream uses the address the last such call found on that device.
+// So make one call before any stream capture on a device, and again after a
+// device reset (a reset may load the library's module at another address).
 // ---------------------------------------------------------------------------
 
 #define PG_CELL_ORDER_STATIC_MAX 65536
-#define PG_CELL_ORDER_STATIC_BLOCKS ((PG_CELL_ORDER_STATIC_MAX + 2047) / 2048)
+// sort tiles of the largest call: pg_launch_radix_sort writes 256 histogram
+// entries per tile (tile = the sort's SORT_TILE keys, 2048 when this was
+// written); the call checks pg_sort_blocks(n) against this bound
+#define PG_CELL_ORDER_STATIC_BLOCKS 32
 
 namespace {
 
@@ -100,13 +106,16 @@ constexpr int MAX_DEVICES = 64;
 std::atomic<unsigned char *> g_scratch_addr[MAX_DEVICES];
 
 // The host-side name g_cell_order_scratch is not a device address; ask the
-// runtime for the device address once per device, with that device current.
-int scratch_address(unsigned char **out)
+// runtime for the device address with the device current, unless the stream
+// is capturing (then the address found by the last call on this device).
+int scratch_address(cudaStream_t s, unsigned char **out)
 {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return PG_ERR_CUDA;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return PG_ERR_CUDA;
   unsigned char *p = g_scratch_addr[dev].load();
-  if (!p)
+  if (cap == cudaStreamCaptureStatusNone || !p)
   {
     void *q = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&q, g_cell_order_scratch);
@@ -136,11 +145,17 @@ extern "C" int pg_cell_order_static(const double *x, const double *y, const doub
                          "spheres; use pg_cell_order\n", n, PG_CELL_ORDER_STATIC_MAX);
     return PG_ERR_CAPACITY;
   }
+  if (pg_sort_blocks(n) > PG_CELL_ORDER_STATIC_BLOCKS)
+  {
+    std::fprintf(stderr, "parmec_gb300: pg_cell_order_static: %d sort tiles exceed the static histogram room "
+                         "of %d\n", pg_sort_blocks(n), PG_CELL_ORDER_STATIC_BLOCKS);
+    return PG_ERR_CAPACITY;
+  }
   if (n == 0) return PG_OK;
-  unsigned char *base = nullptr;
-  int r = scratch_address(&base);
-  if (r != PG_OK) return r;
   cudaStream_t s = (cudaStream_t)stream;
+  unsigned char *base = nullptr;
+  int r = scratch_address(s, &base);
+  if (r != PG_OK) return r;
   unsigned *k1 = (unsigned *)(base + STATIC_KEYS_OFF);
   int *v1 = (int *)(base + STATIC_VALS_OFF);
   unsigned *hist = (unsigned *)(base + STATIC_HIST_OFF);

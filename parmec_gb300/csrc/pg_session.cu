@@ -45,6 +45,8 @@ struct pg_session
   // (PgDev.hs points at hs_buf only while an adaptive run is enqueued)
   double *hs_buf = nullptr;
   int adapt_ready = 0, hrec_cap = 0, sbig_ad_cap = 0;
+  // CRITICAL: per-spring slope and damping, and the per-item outputs
+  double *crit_ke = nullptr, *crit_h = nullptr, *crit_o = nullptr, *crit_r = nullptr;
   int exc_any = 0;                         // some scene has a device excitation
   // partial downloads: device scratch for indices, column table and rows
   int *g_idx = nullptr; const double **g_cols = nullptr; double *g_out = nullptr;
@@ -1473,6 +1475,41 @@ int pg_session_restrain_velocities(pg_session *s)
   pg_launch_restrain_velocities(s->d, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_session_critical(pg_session *s, int which, double *h, double *omega, double *ratio)
+{
+  if (!s || (which != 0 && which != 1)) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (d.form != PG_FORM_FP64) return PG_ERR_UNSUPPORTED;
+  const size_t P = std::max(d.parnum, 1), S = std::max(d.sprnum, 1);
+  if (!s->crit_h)
+  {
+    TRY(adapt_buffers(s));
+    TRY(dalloc(s, &s->crit_ke, 2 * S));
+    TRY(dalloc(s, &s->crit_h, std::max(P, S)));
+    TRY(dalloc(s, &s->crit_o, std::max(P, S)));
+    TRY(dalloc(s, &s->crit_r, std::max(P, S)));
+  }
+  size_t n;
+  if (which == 0)
+  {
+    pg_launch_critical_perparticle(d, s->stream, s->crit_ke, 1, s->crit_h, s->crit_o, s->crit_r);
+    s->launches += d.sprnum ? 2 : 1;
+    n = d.parnum;
+  }
+  else
+  {
+    pg_launch_critical_perspring(d, s->stream, s->crit_h, s->crit_o, s->crit_r);
+    s->launches += d.sprnum ? 1 : 0;
+    n = d.sprnum;
+  }
+  CK(cudaGetLastError());
+  TRY(d2h(s, h, s->crit_h, n));
+  TRY(d2h(s, omega, s->crit_o, n));
+  TRY(d2h(s, ratio, s->crit_r, n));
+  CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
 

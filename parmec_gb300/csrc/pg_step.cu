@@ -1781,6 +1781,230 @@ __global__ void __launch_bounds__(TPB) k_adapt_min(PgDev d)
   if ((threadIdx.x & 31) == 0) atomicMin(d.hmin, bits);
 }
 
+// ---------------------------------------------------------------- CRITICAL (parmec.ispc:485-888)
+// Largest absolute slope of a piecewise-linear table (the spring curve or the
+// damping curve of spring j).
+__device__ double table_max_slope(const double *t0, const double *t1, int lo, int hi)
+{
+  double m = 0.0;
+  for (int q = lo; q < hi-1; q ++)
+  {
+    const double k = (t1[q+1]-t1[q]) / (t0[q+1]-t0[q]);
+    const double a = fabs(k);
+    m = a > m ? a : m;
+  }
+  return m;
+}
+
+// critical_perspring (parmec.ispc:485-544): one thread per spring; the
+// equivalent mass of the two reference points along the spring direction,
+// the curve's largest slope, the damping ratio given or from the damping
+// curve, and the damped step (2/w)(sqrt(1+ksi^2) - ksi).
+__global__ void __launch_bounds__(TPB) k_crit_perspring(PgDev d, double *h, double *om, double *ra)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.sprnum) return;
+  const int i = d.sprpart[0][j], k = d.sprpart[1][j];
+  const double pi[3] = {d.sprpnt[3][j], d.sprpnt[4][j], d.sprpnt[5][j]};
+  const double pk[3] = {d.sprpnt[9][j], d.sprpnt[10][j], d.sprpnt[11][j]};
+  const double dir[3] = {d.sprdir[0][j], d.sprdir[1][j], d.sprdir[2][j]};
+  const double kspr = table_max_slope(d.spring[0], d.spring[1], d.spridx[j], d.spridx[j+1]);
+  const double mspr = eqm(d, i, pi, k, pk, dir);
+  const double omega = sqrt(kspr/mspr);
+  double ksi = 0.0;
+  if (d.dashidx[j]+1 == d.dashidx[j+1]) ksi = d.dashpot[0][d.dashidx[j]];
+  else
+  {
+    const double espr = table_max_slope(d.dashpot[0], d.dashpot[1], d.dashidx[j], d.dashidx[j+1]);
+    if (omega > 0.0) ksi = espr / (2*mspr*omega);
+  }
+  h[j] = omega > 0.0 ? (2.0/omega)*(sqrt(1.0+ksi*ksi) - ksi) : 1.0;
+  om[j] = omega;
+  ra[j] = ksi;
+}
+
+// critical_perparticle_springs, per-spring part (parmec.ispc:711-745): the
+// curve's largest slope and the damping, a critical ratio through the
+// equivalent mass or the damping curve's largest slope.  The spring's own
+// damping table decides which (the reference indexes dashidx with the
+// particle there, parmec.ispc:728).
+__global__ void __launch_bounds__(TPB) k_crit_spring_terms(PgDev d, double *ke)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.sprnum) return;
+  const double kspr = table_max_slope(d.spring[0], d.spring[1], d.spridx[j], d.spridx[j+1]);
+  double espr = 0.0;
+  if (d.dashidx[j]+1 == d.dashidx[j+1])
+  {
+    const double Pi[3] = {d.sprpnt[3][j], d.sprpnt[4][j], d.sprpnt[5][j]};
+    const double Pk[3] = {d.sprpnt[9][j], d.sprpnt[10][j], d.sprpnt[11][j]};
+    const double dir[3] = {d.sprdir[0][j], d.sprdir[1][j], d.sprdir[2][j]};
+    const double mass = eqm(d, d.sprpart[0][j], Pi, d.sprpart[1][j], Pk, dir);
+    espr = d.dashpot[0][d.dashidx[j]] * 2.0 * sqrt(kspr * mass);
+  }
+  else espr = table_max_slope(d.dashpot[0], d.dashpot[1], d.dashidx[j], d.dashidx[j+1]);
+  ke[2*j] = kspr;
+  ke[2*j+1] = espr;
+}
+
+// critical_perparticle (parmec.ispc:547-888): one thread per particle.
+// Terms in the reference's order: the contacts the particle masters (its
+// sphere's list, in list order), the contacts it is the partner of (slave
+// list order), then its springs in spring order (the flush events of a
+// particle are disjoint spring ranges in ascending order).  Contact normals
+// are the recorded ones when the session records geometry, else the
+// direction from the partner (sphere centre or contact point) to the
+// sphere centre.  The slave side takes the contact's own stiffness and
+// damping (the reference reads slave records whose kcur/ecur nothing sets);
+// springs are classified by their own flags (the reference reads sprflg
+// with the particle index, parmec.ispc:759).  Then time_step_task.
+__global__ void __launch_bounds__(TPB) k_crit_perparticle(PgDev d, const double *ke, int use_contacts,
+                                                          double *h, double *om, double *ra)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.parnum) return;
+  const int E = d.ellnum;
+  double kact[3] = {0.0, 0.0, 0.0}, krot[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, kmax = 0.0, emax = 0.0;
+  double L[9], po[3] = {d.position[0][i], d.position[1][i], d.position[2][i]};
+  for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][i];
+  if (use_contacts && E)
+  {
+    const int e = d.pell ? d.pell[i] : -1;
+    if (e >= 0)
+    {
+      const double c[3] = {d.center[0][e], d.center[1][e], d.center[2][e]};
+      for (int k = 0; k < d.ncnt[e]; k ++)
+      {
+        const size_t idx = (size_t)k * E + e;
+        if (!d.nflag[idx]) continue;
+        const int code = d.ncode[idx];
+        const double pnt[3] = {d.npnt[0][idx], d.npnt[1][idx], d.npnt[2][idx]};
+        double n[3];
+        if (d.record_geometry)
+        {
+          n[0] = d.nnrm[0][idx]; n[1] = d.nnrm[1][idx]; n[2] = d.nnrm[2][idx];
+        }
+        else
+        {
+          double q[3];
+          if (code >= 0) { q[0] = c[0]-d.center[0][code]; q[1] = c[1]-d.center[1][code]; q[2] = c[2]-d.center[2][code]; }
+          else { q[0] = c[0]-pnt[0]; q[1] = c[1]-pnt[1]; q[2] = c[2]-pnt[2]; }
+          double ln = sqrt(dot3(q, q));
+          if (!(ln > 0.0)) ln = 1.0;
+          n[0] = q[0]/ln; n[1] = q[1]/ln; n[2] = q[2]/ln;
+        }
+        const int pj = code >= 0 ? d.part[code] : d.triobs[-code-1];
+        const int ij = pairing(d, d.ellcol[e], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
+        const double kc = d.iparam[0][ij];
+        const double ma = pj >= 0 ? 1.0 / (d.invm[i] + d.invm[pj]) : d.mass[i];
+        const double ec = d.iparam[1][ij] * 2.0 * sqrt(kc*ma);
+        kact[0] += fabs(n[0]);
+        kact[1] += fabs(n[1]);
+        kact[2] += fabs(n[2]);
+        kmax = kc > kmax ? kc : kmax;
+        emax = ec > emax ? ec : emax;
+        const double a[3] = {pnt[0]-po[0], pnt[1]-po[1], pnt[2]-po[2]};
+        double A[3];
+        nvmul(L, a, A);
+        krot_add(krot, A);
+      }
+    }
+    for (int r = d.soff[i]; r < d.soff[i+1]; r ++)
+    {
+      const int ref = d.rref[r];
+      if (!d.nflag[ref]) continue;
+      double u[3] = {-d.nfrc[0][ref], -d.nfrc[1][ref], -d.nfrc[2][ref]};
+      double len = sqrt(dot3(u, u));
+      if (len != 0.0)
+      {
+        len = 1.0/len;
+        u[0] *= len; u[1] *= len; u[2] *= len;
+      }
+      else u[0] = u[1] = u[2] = 0.0;
+      kact[0] += fabs(u[0]);
+      kact[1] += fabs(u[1]);
+      kact[2] += fabs(u[2]);
+      const int ms = ref % E, code = d.ncode[ref];
+      const int ij = pairing(d, d.ellcol[ms], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
+      const double kc = d.iparam[0][ij];
+      const double ec = d.iparam[1][ij] * 2.0 * sqrt(kc*(1.0 / (d.invm[d.part[ms]] + d.invm[i])));
+      kmax = kc > kmax ? kc : kmax;
+      emax = ec > emax ? ec : emax;
+      const double a[3] = {d.npnt[0][ref]-po[0], d.npnt[1][ref]-po[1], d.npnt[2][ref]-po[2]};
+      double A[3];
+      nvmul(L, a, A);
+      krot_add(krot, A);
+    }
+  }
+  if (d.sprnum)
+    for (int ev = d.sev_first[i]; ev < d.sev_first[i+1]; ev ++)
+    {
+      const int4 v = d.sev[ev];
+      const int side = v.x & 1;
+      for (int s = v.y; s < v.z; s ++)
+      {
+        if (side == 1 && d.sprpart[1][s] < 0) continue;
+        const double dir[3] = {d.sprdir[0][s], d.sprdir[1][s], d.sprdir[2][s]};
+        if (dot3(dir, dir) > 0.0)
+        {
+          if (d.sprflg[s] & PG_SPRDIR_PLANAR)
+          {
+            double t1[3] = {dir[0] + 0.123, dir[1] + 0.346, dir[2] + 0.789}, t2[3];
+            t2[0] = dir[1]*t1[2] - dir[2]*t1[1];
+            t2[1] = dir[2]*t1[0] - dir[0]*t1[2];
+            t2[2] = dir[0]*t1[1] - dir[1]*t1[0];
+            const double i2 = 1.0/sqrt(dot3(t2, t2));
+            t2[0] *= i2; t2[1] *= i2; t2[2] *= i2;
+            t1[0] = t2[1]*dir[2] - t2[2]*dir[1];
+            t1[1] = t2[2]*dir[0] - t2[0]*dir[2];
+            t1[2] = t2[0]*dir[1] - t2[1]*dir[0];
+            kact[0] += fabs(t1[0]) + fabs(t2[0]);
+            kact[1] += fabs(t1[1]) + fabs(t2[1]);
+            kact[2] += fabs(t1[2]) + fabs(t2[2]);
+          }
+          else
+          {
+            kact[0] += fabs(dir[0]);
+            kact[1] += fabs(dir[1]);
+            kact[2] += fabs(dir[2]);
+          }
+        }
+        else
+        {
+          kact[0] += 1.0;
+          kact[1] += 1.0;
+          kact[2] += 1.0;
+        }
+        const int o = 6*side;
+        const double a[3] = {d.sprpnt[o][s]-po[0], d.sprpnt[o+1][s]-po[1], d.sprpnt[o+2][s]-po[2]};
+        double A[3];
+        tvmul(L, a, A);
+        krot_add(krot, A);
+        const double kspr = ke[2*s], espr = ke[2*s+1];
+        kmax = kmax > kspr ? kmax : kspr;
+        emax = emax > espr ? emax : espr;
+      }
+    }
+  for (int k = 0; k < 3; k ++) d.akact[k][i] = kact[k];
+  for (int k = 0; k < 6; k ++) d.akrot[k][i] = krot[k];
+  d.akmax[i] = kmax;
+  d.aemax[i] = emax;
+  double J[9], w, r;
+  for (int k = 0; k < 9; k ++) J[k] = d.inertia[k][i];
+  h[i] = critical_step(kact, kmax, emax, krot, d.mass[i], J, &w, &r);
+  om[i] = w;
+  ra[i] = r;
+}
+
+// One equivalent mass (the EQM command's eqm export) on particles 0 and
+// (part2 >= 0) 1 of the view.
+__global__ void k_eqm_one(PgDev d, int part2, const double *pts, double *out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double *dir = pts + 6;
+  out[0] = eqm(d, 0, pts, part2 >= 0 ? 1 : -1, pts + 3, dot3(dir, dir) > 0.0 ? dir : nullptr);
+}
+
 // step1 = factor * the smallest critical step, or step0 when nothing is
 // restrained; re-arms the minimum for the next step
 __global__ void k_adapt_select(PgDev d)
@@ -1902,6 +2126,23 @@ void pg_launch_adapt_step(const PgDev &d, cudaStream_t s)
 {
   if (d.parnum) k_adapt_min<<<nblk(d.parnum), TPB, 0, s>>>(d);
   k_adapt_select<<<1, 32, 0, s>>>(d);
+}
+
+void pg_launch_critical_perspring(const PgDev &d, cudaStream_t s, double *h, double *om, double *ra)
+{
+  if (d.sprnum) k_crit_perspring<<<nblk(d.sprnum), TPB, 0, s>>>(d, h, om, ra);
+}
+
+void pg_launch_critical_perparticle(const PgDev &d, cudaStream_t s, double *ke, int use_contacts, double *h,
+                                    double *om, double *ra)
+{
+  if (d.sprnum) k_crit_spring_terms<<<nblk(d.sprnum), TPB, 0, s>>>(d, ke);
+  if (d.parnum) k_crit_perparticle<<<nblk(d.parnum), TPB, 0, s>>>(d, ke, use_contacts, h, om, ra);
+}
+
+void pg_launch_eqm_one(const PgDev &d, cudaStream_t s, int part2, const double *pts, double *out)
+{
+  k_eqm_one<<<1, 32, 0, s>>>(d, part2, pts, out);
 }
 
 void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s)

@@ -108,6 +108,16 @@ class GpuEngine:
                   "pg_session_run_adaptive")
         return steps[:tab.nsteps]
 
+    def critical(self, which):
+        """CRITICAL on the device (pg_session_critical): which = 0 per particle
+        (parnum entries), 1 per spring (sprnum entries, sorted spring order);
+        returns (step, omega, ratio) arrays."""
+        n = self.model.parnum if which == 0 else self.model.sprnum
+        out = [np.zeros(max(1, n)) for _ in range(3)]
+        abi.check(self.lib.pg_session_critical(self.sess, int(which), *(abi.dptr(a) for a in out)),
+                  "pg_session_critical")
+        return tuple(a[:n] for a in out)
+
     def sync(self):
         abi.check(self.lib.pg_session_sync(self.sess), "pg_session_sync")
 

@@ -705,16 +705,16 @@ class Model:
         return out
 
     # ------------------------------------------------------------- CRITICAL
-    def critical(self, perspring=-1, perparticle=-1):
+    def critical(self, perspring=-1, perparticle=-1, engine=None):
         """CRITICAL (input.cpp:3034-3154): per-spring and per-particle critical
         step estimates.  perspring=N returns the N smallest spring steps as
         (step, index, omega, ratio), perparticle=N the N smallest particle steps
         likewise, both a tuple of the two lists, and no argument the smallest
         particle step (REAL_MAX while no contact or spring restrains anything,
-        as in the reference).  Per-particle estimates use the contacts of the
-        attached device session (parmec_gb300.critical)."""
-        from .critical import critical_perparticle
-        from .springs import critical_perspring
+        as in the reference).  The estimates run on the device
+        (pg_session_critical) of 'engine', else of the session the last DEM
+        call stepped this model with (its contacts), else of a session opened
+        for the query (springs only: no contact exists before DEM)."""
         if perspring < -1 or perspring > self.sprnum:
             raise ValueError("Parameter 'perspring' is out of range")
         if perparticle < -1 or perparticle > self.parnum:
@@ -724,20 +724,30 @@ class Model:
             self.sort_materials()
             sort_springs(self)
             self.springs_changed = False
-        out_s = out_p = None
-        if perspring >= 0:
-            h, o, r = critical_perspring(self)
-            order = sorted(range(self.sprnum), key=lambda i: (h[i], i))
-            out_s = [(h[i], i, o[i], r[i]) for i in order[:perspring]]
-        contacts = None
-        eng = self.last_engine
-        if eng is not None and eng.model is self and not eng.stale() and hasattr(eng, "contacts"):
-            contacts = eng.contacts()
-        if perparticle >= 0 or out_s is None:
-            h, o, r = critical_perparticle(self, contacts)
-            order = sorted(range(self.parnum), key=lambda i: (h[i], i))
-            if perparticle >= 0:
-                out_p = [(float(h[i]), i, float(o[i]), float(r[i])) for i in order[:perparticle]]
+        eng, temp = engine, None
+        if eng is None:
+            last = self.last_engine
+            if last is not None and last.model is self and not last.stale() and hasattr(last, "critical"):
+                eng = last
+        if eng is None:
+            from .engine import GpuEngine
+            self.sort_materials()
+            eng = temp = GpuEngine()
+            eng.attach(self)
+        try:
+            out_s = out_p = None
+            if perspring >= 0:
+                h, o, r = eng.critical(1)
+                order = sorted(range(self.sprnum), key=lambda i: (h[i], i))
+                out_s = [(float(h[i]), i, float(o[i]), float(r[i])) for i in order[:perspring]]
+            if perparticle >= 0 or out_s is None:
+                h, o, r = eng.critical(0)
+                order = sorted(range(self.parnum), key=lambda i: (h[i], i))
+                if perparticle >= 0:
+                    out_p = [(float(h[i]), i, float(o[i]), float(r[i])) for i in order[:perparticle]]
+        finally:
+            if temp is not None:
+                temp.close()
         if out_s is not None and out_p is not None:
             return (out_s, out_p)
         if out_s is not None:

@@ -1,9 +1,9 @@
 """SPRING command, spring ordering and spring tables (host side).
 
 Restates input.cpp:1440-1788 (SPRING), parmec.cpp:1683-1965 (sort_springs),
-parmec.cpp:1239-1269 (lcurve_from_time_series) and parmec.ispc:485-544
-(critical_perspring) for the host.  The per-step spring force itself runs on
-the device.
+parmec.cpp:1239-1269 (lcurve_from_time_series) and parmec.ispc:423-482 (eqm,
+for the EQM command) for the host.  The per-step spring force and CRITICAL
+run on the device.
 """
 import math
 
@@ -224,35 +224,41 @@ def _eqm(m, part1, point1, part2, point2, direction):
     d = np.array(direction, dtype=float)
     if d @ d > 0.0:
         return 1.0 / float(d @ (Miv @ d))
-    from .critical import _extremum_eigenvalue
     return 1.0 / _extremum_eigenvalue([float(x) for x in Miv.T.reshape(-1)], 1)
 
 
-def critical_perspring(m):
-    """critical_perspring (parmec.ispc:485-544): per-spring critical step, omega, damping ratio."""
-    S = m.S
-    h, o, r = [], [], []
-    for j in range(m.sprnum):
-        i, k = int(S.sprpart[0, j]), int(S.sprpart[1, j])
-        sp = m.spring_tab[j]
-        kspr = 0.0
-        for a in range(len(sp) - 1):
-            kk = (sp[a + 1][1] - sp[a][1]) / (sp[a + 1][0] - sp[a][0])
-            kspr = max(abs(kk), kspr)
-        mspr = _eqm(m, i, S.sprpnt[3:6, j], k, S.sprpnt[9:12, j], S.sprdir[0:3, j])
-        omega = math.sqrt(kspr / mspr)
-        ksi = 0.0
-        dp = m.dashpot_tab[j]
-        if len(dp) == 1:
-            ksi = dp[0][0]
-        else:
-            espr = 0.0
-            for a in range(len(dp) - 1):
-                e = (dp[a + 1][1] - dp[a][1]) / (dp[a + 1][0] - dp[a][0])
-                espr = max(abs(e), espr)
-            if omega > 0.0:
-                ksi = espr / (2 * mspr * omega)
-        h.append((2.0 / omega) * (math.sqrt(1.0 + ksi * ksi) - ksi) if omega > 0.0 else 1.0)
-        o.append(omega)
-        r.append(ksi)
-    return h, o, r
+def _triple_angle_root(r, largest):
+    """cos(acos(r)/3) (largest) or cos(acos(r)/3 + 2 pi/3) as roots of the
+    triple-angle identity 4c^3 - 3c = r, by Newton's method from c = 1 (or -1),
+    monotone on [1/2, 1] (and [-1, -1/2]); the device and the CPU restatement
+    run the same operations."""
+    r = -1.0 if r < -1.0 else (1.0 if r > 1.0 else r)
+    c = 1.0 if largest else -1.0
+    for _ in range(100):
+        f = (4.0 * c * c - 3.0) * c - r
+        den = 12.0 * c * c - 3.0
+        if den == 0.0:
+            break
+        cn = c - f / den
+        if (largest and not cn < c) or (not largest and not cn > c):
+            break
+        c = cn
+    return c
+
+
+def _extremum_eigenvalue(A, minimum):
+    """extremum_eigenvalue (macros.h:1539-1588) of a symmetric column-major 3x3;
+    its diagonal branch returns the largest entry whichever is asked for."""
+    p1 = A[3] * A[3] + A[6] * A[6] + A[7] * A[7]
+    if p1 == 0.0:
+        r = A[0] if A[0] > A[4] else A[4]
+        return r if r > A[8] else A[8]
+    q = (A[0] + A[4] + A[8]) / 3.0
+    p2 = (A[0] - q) * (A[0] - q) + (A[4] - q) * (A[4] - q) + (A[8] - q) * (A[8] - q) + 2 * p1
+    p = math.sqrt(p2 / 6.0)
+    invp = 1.0 / p
+    B = [invp * (A[0] - q), invp * A[1], invp * A[2], invp * A[3], invp * (A[4] - q), invp * A[5],
+         invp * A[6], invp * A[7], invp * (A[8] - q)]
+    det = (B[0] * (B[4] * B[8] - B[5] * B[7]) + B[3] * (B[2] * B[7] - B[1] * B[8])
+           + B[6] * (B[1] * B[5] - B[2] * B[4]))
+    return q + 2.0 * p * _triple_angle_root(0.5 * det, not minimum)

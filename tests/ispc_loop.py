@@ -18,13 +18,17 @@ from parmec_gb300.driver import StepTables, obstaclev, step_times
 NULL = None
 
 
-def library():
-    lib = abi.load_library()
+def library(path=None):
+    """The drop-in exports of libparmec_gb300.so, or (path given) of another
+    library with the reference's ISPC entry points, such as the reference's
+    own hot path built by oracle/ispc_ref.py."""
+    lib = ctypes.CDLL(path) if path else abi.load_library()
     lib.adaptive_timestep.restype = ctypes.c_double
     lib.partitioning_create.restype = ctypes.c_void_p
     lib.master_alloc.restype = ctypes.c_void_p
     lib.slave_alloc.restype = ctypes.c_void_p
-    lib.pg_compat_kernel_launches.restype = ctypes.c_longlong
+    if hasattr(lib, "pg_compat_kernel_launches"):
+        lib.pg_compat_kernel_launches.restype = ctypes.c_longlong
     for name in ("master_alloc", "slave_alloc"):
         getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.master_free.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -40,13 +44,24 @@ class Host:
     """The reference's global buffers for one Model (parmec.cpp:61-285) and
     its contact-list arrays, as the loop passes them."""
 
-    def __init__(self, lib, m, buffer_size=None):
+    def __init__(self, lib, m, buffer_size=None, orient=False, ntasks=1):
         self.lib = lib
         self.m = m
         n = buffer_size or max(m.parnum, 1)
         self.size = n
+        self.ntasks = ntasks
         self.master = lib.master_alloc(None, 0, n)
         self.slave = lib.slave_alloc(None, 0, n)
+        # parmec.cpp passes its orient buffers (18 rows); the drop-in ignores
+        # them for spheres, the reference's partitioning_store reads them
+        # only for ellipsoids
+        self.orient_rows = None
+        self.orient = NULL
+        if orient:
+            self.orient_rows = np.zeros((18, max(m.ellnum, m.parnum, 1)))
+            self.orient = abi.rows(self.orient_rows, 18)
+            # shapes() tests radii[1][j] with the particle index j
+            m.E.ensure(max(m.parnum, m.ellnum))
 
     def close(self):
         self.lib.master_free(self.master, self.size)
@@ -109,7 +124,8 @@ def dem(lib, host, duration, step, adaptive=0.0):
         m.torsion_changed = False
     s = m.scene()
     obspnt, obsang, obslin = m._obs_views
-    ntasks = 1
+    ntasks = host.ntasks
+    orient = host.orient
     adapt = 0.0 < adaptive <= 1.0
     if adapt:
         times = None
@@ -120,7 +136,7 @@ def dem(lib, host, duration, step, adaptive=0.0):
     step0 = step
     if m.curtime == 0.0:
         lib.euler(ntasks, s.parnum, s.angular, s.linear, s.rotation, s.position, D(0.5 * step0))
-        lib.shapes(ntasks, s.ellnum, s.part, s.center, s.radii, NULL, s.nodnum, s.nodes, s.nodpart, NULL,
+        lib.shapes(ntasks, s.ellnum, s.part, s.center, s.radii, orient, s.nodnum, s.nodes, s.nodpart, NULL,
                    s.facnum, s.facnod, s.factri, s.tri, s.rotation, s.position)
         a, l = obstaclev(m, 0.5 * step0)
         obsang[:a.size] = a[:obsang.size]
@@ -155,10 +171,15 @@ def dem(lib, host, duration, step, adaptive=0.0):
 
     for k, t in steps():
         if lib.partitioning_store(ntasks, ctypes.c_void_p(tree), s.ellnum - ellcon, s.ellcol, s.part, s.center,
-                                  s.radii, NULL) > 0:
-            raise AssertionError("partitioning_store overflowed")
+                                  s.radii, orient) > 0:
+            # a leaf overflowed: parmec.cpp:2421-2428 rebuilds the tree
+            lib.partitioning_destroy(ctypes.c_void_p(tree))
+            tree = lib.partitioning_create(ntasks, s.ellnum - ellcon, s.center)
+            if lib.partitioning_store(ntasks, ctypes.c_void_p(tree), s.ellnum - ellcon, s.ellcol, s.part,
+                                      s.center, s.radii, orient) != 0:
+                raise AssertionError("Repartitioning failed")
         lib.condet(ntasks, ctypes.c_void_p(tree), ctypes.c_void_p(host.master), s.parnum, s.ellnum - ellcon,
-                   s.ellcol, s.part, s.center, s.radii, NULL, s.trinum - tricon, s.tricol, s.triobs, s.tri)
+                   s.ellcol, s.part, s.center, s.radii, orient, s.trinum - tricon, s.tricol, s.triobs, s.tri)
         gravity[:] = tab.gravity[k]
         damping[:] = tab.damping[k]
         lib.forces(ntasks, ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), s.parnum,
@@ -169,8 +190,8 @@ def dem(lib, host, duration, step, adaptive=0.0):
                    s.sprfric, s.sprkskn, s.sprsdsp, s.stroke0, s.stroke, s.sprfrc, s.lcurve, s.lcidx,
                    abi.dptr(gravity), s.trqsprnum, s.trqsprpart, s.trqzdir0, s.trqxdir0, s.krpy, s.krpyidx,
                    s.drpy, s.drpyidx, s.trqcone, s.trqzdir1, s.trqxdir1, s.trqrpy, s.trqrpytot, s.trqrpyspr,
-                   s.force, s.torque, kact_p if adapt else NULL, abi.dptr(kmax), abi.dptr(emax),
-                   krot_p if adapt else NULL, 1 if adapt else 0, s.unsprnum,
+                   s.force, s.torque, kact_p, abi.dptr(kmax), abi.dptr(emax),
+                   krot_p, 1 if adapt else 0, s.unsprnum,
                    s.tsprings, s.tspridx, s.msprings, s.mspridx, s.unlim, s.unent, s.unop, s.unabs, s.nsteps,
                    s.nfreq, s.unaction, s.activate, s.actidx, m.stepnum, D(t))
         if adapt:
@@ -184,7 +205,7 @@ def dem(lib, host, duration, step, adaptive=0.0):
                      s.linear, s.rotation, s.position, s.inertia, s.inverse, s.mass, s.invm, abi.dptr(damping),
                      s.force, s.torque, s.flags, D(step0), D(step1))
         _prescribe_velocity(m, tab, k)
-        lib.shapes(ntasks, s.ellnum - ellcon, s.part, s.center, s.radii, NULL, s.nodnum, s.nodes, s.nodpart,
+        lib.shapes(ntasks, s.ellnum - ellcon, s.part, s.center, s.radii, orient, s.nodnum, s.nodes, s.nodpart,
                    s.flags, s.facnum - faccon, s.facnod, s.factri, s.tri, s.rotation, s.position)
         a, l = obstaclev(m, t + step0)
         obsang[:a.size] = a[:obsang.size]
@@ -196,6 +217,68 @@ def dem(lib, host, duration, step, adaptive=0.0):
     m.curstep = step1
     m.stepnum += 1
     m.pull_obstacles()
-    st = lib.pg_compat_status()
-    if st != 0:
-        raise RuntimeError(f"drop-in entry points reported status {st}")
+    if hasattr(lib, "pg_compat_status"):
+        st = lib.pg_compat_status()
+        if st != 0:
+            raise RuntimeError(f"drop-in entry points reported status {st}")
+
+
+class Master(ctypes.Structure):
+    """master_conpnt (condet.h:33-49) at REAL=8."""
+
+
+Master._fields_ = [("master", ctypes.c_int * 8), ("slave", (ctypes.c_int * 8) * 2),
+                   ("color", (ctypes.c_int * 8) * 2), ("point", (ctypes.c_double * 8) * 3),
+                   ("normal", (ctypes.c_double * 8) * 3), ("depth", ctypes.c_double * 8),
+                   ("force", (ctypes.c_double * 8) * 3), ("kcur", ctypes.c_double * 8),
+                   ("ecur", ctypes.c_double * 8), ("state", (ctypes.c_double * 8) * 8),
+                   ("size", ctypes.c_int), ("next", ctypes.POINTER(Master)), ("lock", ctypes.c_int)]
+
+
+def master_lists(host):
+    """Every contact in the master lists, in list order: a dict of arrays with
+    the master particle, the slave code (sphere index, or -(triangle+1)), the
+    slave particle, point, normal, depth, force and tangential state."""
+    P = host.m.parnum
+    arr = (Master * P).from_address(host.master)
+    out = {k: [] for k in ("mpart", "code", "spart", "point", "normal", "depth", "force", "state")}
+    for p in range(P):
+        b = arr[p]
+        while True:
+            for k in range(b.size):
+                out["mpart"].append(p)
+                out["code"].append(b.slave[1][k])
+                out["spart"].append(b.slave[0][k])
+                out["point"].append([b.point[c][k] for c in range(3)])
+                out["normal"].append([b.normal[c][k] for c in range(3)])
+                out["depth"].append(b.depth[k])
+                out["force"].append([b.force[c][k] for c in range(3)])
+                out["state"].append([b.state[c][k] for c in range(3)])
+            if not b.next:
+                break
+            b = b.next.contents
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def critical(lib, host):
+    """CRITICAL's two exports (critical_perspring, critical_perparticle) on
+    the host arrays, as input.cpp:3064-3140 calls them: per-spring and
+    per-particle (step, omega, ratio) arrays."""
+    m = host.m
+    s = m.scene()
+    P, S = m.parnum, m.sprnum
+    out_s = [np.zeros(max(1, S)) for _ in range(3)]
+    out_p = [np.zeros(max(1, P)) for _ in range(3)]
+    kact = [np.zeros(max(1, P)) for _ in range(3)]
+    krot = [np.zeros(max(1, P)) for _ in range(6)]
+    kmax, emax = np.zeros(max(1, P)), np.zeros(max(1, P))
+    if S:
+        lib.critical_perspring(S, s.sprpart, s.sprpnt, s.sprdir, s.spring, s.spridx, s.dashpot, s.dashidx,
+                               s.inverse, s.invm, s.position, *(abi.dptr(a) for a in out_s))
+    lib.critical_perparticle.restype = ctypes.c_double
+    lib.critical_perparticle(host.ntasks, ctypes.c_void_p(host.master), ctypes.c_void_p(host.slave), P, s.mass,
+                             s.inertia, s.invm, s.inverse, s.rotation, s.position, S, s.sprflg, s.sprpart,
+                             s.sprpnt, s.sprdir, s.spring, s.spridx, s.dashpot, s.dashidx,
+                             (abi.D * 3)(*[abi.dptr(a) for a in kact]), abi.dptr(kmax), abi.dptr(emax),
+                             (abi.D * 6)(*[abi.dptr(a) for a in krot]), *(abi.dptr(a) for a in out_p))
+    return tuple(a[:S] for a in out_s), tuple(a[:P] for a in out_p)

@@ -76,7 +76,7 @@ def test_contact_terms_match_critical(oracle_lib):
     estimate over the same contacts (no springs), up to the positions moved by
     the last step's dynamics."""
     from oracle.pyoracle import OracleEngine
-    from parmec_gb300.critical import critical_perparticle
+    from oracle.critical_host import critical_perparticle
     m, dt = make_collision_scene(n_side=4, speed=0.2)
     eng = OracleEngine()
     m.dem(20 * dt - 0.5 * dt, dt, interval=1e9, adaptive=1.0, engine=eng)

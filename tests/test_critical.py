@@ -1,5 +1,6 @@
 """CRITICAL (input.cpp:3034-3154): per-spring and per-particle critical step
-estimates against closed forms (CPU: springs need no device session)."""
+estimates against closed forms, through the oracle's restatement on the CPU
+and the device (pg_session_critical) on the GPU."""
 import math
 
 import pytest
@@ -20,33 +21,60 @@ def damped_step(omega, ksi):
     return (2.0 / omega) * (math.sqrt(1.0 + ksi * ksi) - ksi)
 
 
-def test_particle_on_a_spring():
+def engines():
+    from oracle.pyoracle import OracleEngine
+    return [pytest.param(lambda: OracleEngine(), id="oracle"),
+            pytest.param(lambda: __import__("parmec_gb300.engine", fromlist=["GpuEngine"]).GpuEngine(),
+                         id="gpu", marks=pytest.mark.gpu)]
+
+
+def attached(make_engine, m, request):
+    """An engine of the parametrised kind attached to m (springs sorted first,
+    as DEM and CRITICAL sort them)."""
+    from parmec_gb300.springs import sort_springs
+    if "gpu" in request.node.callspec.id:
+        request.getfixturevalue("gpu_lib")
+    m.sort_materials()
+    if m.springs_changed:
+        sort_springs(m)
+        m.springs_changed = False
+    eng = make_engine()
+    eng.attach(m)
+    return eng
+
+
+@pytest.mark.parametrize("make_engine", engines())
+def test_particle_on_a_spring(make_engine, request):
     """kact = 1 per axis (no direction yet), k = the curve slope, no arm:
     h = 2/sqrt(k/m) without damping."""
     m, p = spring_particle()
+    eng = attached(make_engine, m, request)
     w = math.sqrt(1e4 / m.P.mass[p])
-    h = m.critical()
+    h = m.critical(engine=eng)
     assert abs(h - 2.0 / w) <= 1e-12 * h
-    (hp, i, om, ra), = m.critical(perparticle=1)
+    (hp, i, om, ra), = m.critical(perparticle=1, engine=eng)
     assert i == p and abs(om - w) <= 1e-12 * w and ra == 0.0
 
 
-def test_particle_on_a_damped_spring():
+@pytest.mark.parametrize("make_engine", engines())
+def test_particle_on_a_damped_spring(make_engine, request):
     m, p = spring_particle(ratio=0.3)
+    eng = attached(make_engine, m, request)
     w = math.sqrt(1e4 / m.P.mass[p])
-    h = m.critical()
+    h = m.critical(engine=eng)
     assert abs(h - damped_step(w, 0.3)) <= 1e-12 * h
-    s, q = m.critical(perspring=1, perparticle=1)
+    s, q = m.critical(perspring=1, perparticle=1, engine=eng)
     assert len(s) == 1 and len(q) == 1
     assert abs(s[0][0] - damped_step(w, 0.3)) <= 1e-12 * h      # the spring's own estimate agrees
 
 
-def test_nothing_restrains_nothing():
+@pytest.mark.parametrize("make_engine", engines())
+def test_nothing_restrains_nothing(make_engine, request):
     """No contact and no spring: REAL_MAX, as the reference returns before any contact."""
     m = Model()
     mat = m.material(1000.0, 1e9, 0.25)
     m.sphere((0.0, 0.0, 0.0), 0.05, mat, 1)
-    assert m.critical() == REAL_MAX
+    assert m.critical(engine=attached(make_engine, m, request)) == REAL_MAX
 
 
 def test_argument_ranges():
@@ -76,13 +104,6 @@ def sphere_pair():
     b = m.sphere((0.0999, 0.0, 0.0), 0.05, mat, 1)
     m.granular(0, 0, 1e6, 0.2, 0.5)
     return m, a, b
-
-
-def engines():
-    from oracle.pyoracle import OracleEngine
-    return [pytest.param(lambda: OracleEngine(), id="oracle"),
-            pytest.param(lambda: __import__("parmec_gb300.engine", fromlist=["GpuEngine"]).GpuEngine(),
-                         id="gpu", marks=pytest.mark.gpu)]
 
 
 @pytest.mark.parametrize("make_engine", engines())
@@ -140,3 +161,36 @@ def test_sphere_pair(make_engine, oracle_lib, request):
         assert abs(h - min(hx, hr)) <= 1e-9 * h
         assert abs(om - max(w, wr)) <= 1e-9 * om
         assert abs(e / (2.0 * mass * w) - 0.2 / math.sqrt(2.0)) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_critical_matches_restatement(gpu_lib, oracle_lib):
+    """The device CRITICAL (pg_session_critical) against the host
+    restatement over the same contacts and springs: colliding spheres in a
+    box (master and slave contact terms), and bodies with full inertia
+    tensors on springs of every direction mode with a prescribed base."""
+    import numpy as np
+    from helpers import make_collision_scene
+    from oracle.critical_host import critical_perparticle, critical_perspring
+    from parmec_gb300.engine import GpuEngine
+    from test_gpu_springs import lattice
+    cases = ((lambda: make_collision_scene(n_side=5), 40), (lambda: (lattice(), 2e-5), 60))
+    for make, steps in cases:
+        m, dt = make()
+        eng = GpuEngine(record_geometry=True)
+        m.dem(steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        h, o, r = eng.critical(0)
+        hh, oh, rh = critical_perparticle(m, eng.contacts())
+        touched = hh < 1e300
+        assert touched.sum() > 10
+        assert np.array_equal(touched, h < 1e300)
+        for a, b in ((h, hh), (o, oh), (r, rh)):
+            assert np.allclose(a[touched], b[touched], rtol=1e-12, atol=0.0)
+        if m.sprnum:
+            hs, os_, rs = eng.critical(1)
+            for a, b in zip((hs, os_, rs), critical_perspring(m)):
+                assert np.allclose(a, np.array(b), rtol=1e-12, atol=0.0)
+        # Model.critical takes the session the DEM call stepped with
+        (hp, i, om, ra), = m.critical(perparticle=1)
+        assert hp == float(np.min(h)) and i == int(np.argmin(h))
+        eng.close()

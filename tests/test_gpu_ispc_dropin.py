@@ -174,3 +174,66 @@ def test_dropin_restraints_bitwise(gpu_lib, oracle_lib):
         m.restrain(5, angular=[1.0, 0.2, 0.0, 0.0, 1.0, 0.3, 0.1, 0.0, 1.0])
         return m, dt
     run_both(make, 30)
+
+
+def test_dropin_critical(gpu_lib, oracle_lib):
+    """critical_perparticle and critical_perspring through the drop-in
+    exports (input.cpp:3064-3140) after a DEM call: the device contact
+    lists of the master array and the host spring arrays, against the host
+    restatement over the oracle's equal state; and eqm (the EQM command)
+    against the model's."""
+    from oracle.critical_host import critical_perparticle, critical_perspring
+    from test_gpu_springs import lattice
+    lib, host, mc, mo, eo = run_both(lambda: make_collision_scene(n_side=5), 40)
+    _, (h, o, r) = ispc_loop.critical(lib, host)
+    hh, oh, rh = critical_perparticle(mo, eo.contacts())
+    touched = hh < 1e300
+    assert touched.sum() > 10 and np.array_equal(touched, h < 1e300)
+    for a, b in ((h, hh), (o, oh), (r, rh)):
+        assert np.allclose(a[touched], b[touched], rtol=1e-12, atol=0.0)
+    host.close()
+    step = 2e-5
+    lib, host, mc, mo, eo = run_both(lambda: (lattice(), step), 50)
+    (hs, os_, rs), (h, o, r) = ispc_loop.critical(lib, host)
+    for a, b in zip((hs, os_, rs), critical_perspring(mo)):
+        assert np.allclose(a, np.array(b), rtol=1e-12, atol=0.0)
+    hh, oh, rh = critical_perparticle(mo, eo.contacts())
+    for a, b in ((h, hh), (o, oh), (r, rh)):
+        assert np.allclose(a, b, rtol=1e-12, atol=0.0)
+    s = mc.scene()
+    p1 = (ctypes.c_double * 3)(0.001, 0.002, 0.0)
+    p2 = (ctypes.c_double * 3)(0.0, 0.0, -0.01)
+    for part2, d in ((-1, (0.0, 0.0, 0.0)), (1, (0.0, 0.0, 1.0)), (3, (0.6, 0.8, 0.0))):
+        dd = (ctypes.c_double * 3)(*d)
+        lib.eqm.restype = ctypes.c_double
+        got = lib.eqm(0, p1, part2, p2, dd, s.inverse, s.invm, s.position)
+        want = mc.eqm(0, tuple(p1), part2, tuple(p2) if part2 >= 0 else None, d)
+        assert abs(got - want) <= 1e-12 * abs(want)
+    host.close()
+
+
+def test_dropin_critical_against_reference(gpu_lib, oracle_lib):
+    """The drop-in CRITICAL against the reference's own critical_perparticle
+    (oracle/ispc_ref.py, when its translation is on this host): spheres
+    resting on a plane, each master of its contacts."""
+    from oracle import ispc_ref
+    from test_reference_pin import spheres_on_a_plane
+    if ispc_ref.build() is None:
+        pytest.skip("the reference's translation is not on this host")
+    ref = ispc_loop.library(ispc_ref.LIB)
+    lib = ispc_loop.library()
+    lib.pg_compat_exit_on_error(0)
+    lib.pg_compat_set_skin(ctypes.c_double(0.0))
+    mc, dt = spheres_on_a_plane()
+    mr, _ = spheres_on_a_plane()
+    hc = ispc_loop.Host(lib, mc)
+    hr = ispc_loop.Host(ref, mr, orient=True)
+    ispc_loop.dem(lib, hc, 30 * dt - 0.5 * dt, dt)
+    ispc_loop.dem(ref, hr, 30 * dt - 0.5 * dt, dt)
+    _, (h, o, r) = ispc_loop.critical(lib, hc)
+    _, (h2, o2, r2) = ispc_loop.critical(ref, hr)
+    touched = h2 < 1e300
+    assert touched.sum() >= 20 and np.array_equal(touched, h < 1e300)
+    for a, b in ((h, h2), (o, o2), (r, r2)):
+        assert np.allclose(a[touched], b[touched], rtol=1e-7, atol=0.0)
+    hc.close()
