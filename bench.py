@@ -110,20 +110,49 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(n_spheres, threads, steps=3):
-    """The oracle (restatement of the reference's ISPC path) on a bounded sample:
-    the same drum scene, one untimed step, then `steps` timed steps."""
-    from oracle.pyoracle import OracleEngine
+def reference_cpu(n_spheres, threads, steps, warmup=1):
+    """The reference's own hot path on the host cores: its ISPC sources
+    translated to C++ (oracle/ispc_ref.py; tasks spread over `threads`
+    OpenMP threads, as its task system spreads them), driven by parmec.cpp's
+    dem() call sequence on the same drum.  Falls back to the oracle (the
+    restatement) where the translation is not on this host.  Returns
+    (particle-steps/s, kind, sample description)."""
     from parmec_gb300.scenes import drum
     m, dt, _ = drum(n_spheres)
-    eng = OracleEngine(threads=threads)
-    m.dem(0.5 * dt, dt, interval=1e9, engine=eng)
-    t0 = time.perf_counter()
-    m.dem(steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
-    el = time.perf_counter() - t0
-    return {"value": m.parnum * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} DEM steps of the full {m.parnum}-sphere drum after one untimed step, "
-                      f"{el:.1f} s"}
+    try:
+        from oracle import dem_loop, ispc_ref
+        lib_path = ispc_ref.build()
+    except Exception:
+        lib_path = None
+    if lib_path:
+        lib = dem_loop.library(lib_path)
+        host = dem_loop.Host(lib, m, orient=True, ntasks=threads)
+        dem_loop.dem(lib, host, warmup * dt - 0.5 * dt, dt)
+        t0 = time.perf_counter()
+        dem_loop.dem(lib, host, steps * dt - 0.5 * dt, dt)
+        el = time.perf_counter() - t0
+        host.close()
+        kind = "reference"
+        what = ("the reference's condet/forces/dynamics/shapes/obstacles/partition ISPC sources translated to C++ "
+                f"at gang size one (oracle/ispc_ref.py), g++ -O2, {threads} tasks on OpenMP threads, "
+                "driven by parmec.cpp's dem() call sequence")
+    else:
+        from oracle.pyoracle import OracleEngine
+        eng = OracleEngine(threads=threads)
+        m.dem(warmup * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        t0 = time.perf_counter()
+        m.dem(steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        el = time.perf_counter() - t0
+        kind = "port"
+        what = f"the oracle restatement on {threads} threads (the reference's sources are not on this host)"
+    sample = f"{steps} DEM steps of the full {m.parnum}-sphere drum after {warmup} untimed, {el:.1f} s; {what}"
+    return m.parnum * steps / el, kind, sample
+
+
+def cpu_baseline(n_spheres, threads, steps=3):
+    """The reference's CPU hot path on a bounded sample of the same drum."""
+    v, kind, sample = reference_cpu(n_spheres, threads, steps)
+    return {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind, "sample": sample}
 
 
 def mixed_form(args, ref64):
@@ -179,8 +208,10 @@ def batched_form(args, scenes):
     steps = min(args.steps, 100)
     out = {"workload": f"{len(scenes)} shaken boxes, sphere counts log-uniform [2048,65536], "
                        "base excitation f~U[1,20] Hz, a~U[0.1,1] g", "steps": steps}
+    from parmec_gb300.serving import range_energy
     legs = ((abi.PG_FORM_MIXED, "mixed", True), (abi.PG_FORM_MIXED, "mixed_per_phase_kernels", False),
             (abi.PG_FORM_FP64, "fp64", False))
+    snap = {}
     for form, key, fused in legs:
         models = [sc[0] for sc in scenes]
         P, _ = batch.pool(models)
@@ -208,6 +239,12 @@ def batched_form(args, scenes):
         ms = ev0.elapsed_time(ev1)
         out[key] = {"value": P.parnum * steps / (ms * 1e-3), "unit": "particle-steps/s",
                     "ms_per_step": ms / steps, "spheres": P.parnum}
+        if key in ("mixed_per_phase_kernels", "fp64"):
+            # the same W + K steps from the same state in both forms: kept for the error report
+            eng.download()
+            n = P.parnum
+            snap[key] = {"x": P.P.position[0:3, :n].copy(), "f": P.P.force[:, :n].copy(),
+                         "E": [range_energy(P, r[0], r[1], sc[2][0:3]) for r, sc in zip(P.scene_ranges, scenes)]}
         if fused:
             threads, blocks, tuned, graph = eng.fused_config()
             out[key]["kernel"] = {"fused_step": True, "threads": threads, "blocks": blocks,
@@ -221,6 +258,17 @@ def batched_form(args, scenes):
                          "path": "fused step kernel" if best == "mixed" else
                                  "per-phase kernels, one CUDA graph per step"}
     out["mixed_over_fp64"] = out["mixed_best"]["value"] / out["fp64"]["value"]
+    a, b = snap["mixed_per_phase_kernels"], snap["fp64"]
+    erel = np.abs(np.array(a["E"]) - np.array(b["E"])) / np.abs(np.array(b["E"]))
+    fmax = float(np.max(np.abs(b["f"])))
+    out["errors_vs_fp64"] = {
+        "steps": args.warmup + steps, "scenes": len(scenes),
+        "energy_rel_max": float(erel.max()), "energy_rel_p50": float(np.percentile(erel, 50)),
+        "energy_rel_p99": float(np.percentile(erel, 99)), "scenes_energy_rel_under_1e-6": int(np.sum(erel <= 1e-6)),
+        "position_max_abs_m": float(np.max(np.abs(a["x"] - b["x"]))),
+        "force_max_abs_rel_to_max": float(np.max(np.abs(a["f"] - b["f"]))) / fmax,
+        "energy_definition": "per scene: kinetic + rotational + potential of the scene's base gravity g0, "
+                             "mixed form (per-phase kernels; the fused kernel gives the same bits) against FP64"}
     return out
 
 
@@ -272,25 +320,41 @@ def serving_form(args, count):
     """Config 4: a Poisson stream (200 req/s) of excitation-sweep requests
     (sphere counts log-uniform [1024, 262144], 200-5000 steps, sinusoid or
     band-limited noise), served by the continuous-batching pool (mixed and
-    FP64 forms, 150 GB HBM budget) and, for comparison, by the plain FP64
-    drop-in path one request at a time (a DEM() call per request)."""
+    FP64 forms, pool sized by the 150 GB HBM budget alone) and by the plain
+    FP64 drop-in path one request at a time (a DEM() call per request, the
+    same excitation through a GRAVITY callable)."""
     import torch
     from parmec_gb300 import abi
     from parmec_gb300.engine import GpuEngine
-    from parmec_gb300.serving import Server, request_stream
+    from parmec_gb300.serving import Server, excitation_gravity, request_stream
+    t_gen = time.perf_counter()
     reqs = request_stream(count)
+    t_gen = time.perf_counter() - t_gen
     out = {"workload": f"{count} requests, Poisson 200 req/s, spheres log-uniform [1024,262144], "
-                       "steps U[200,5000], sinusoid or band-limited noise base excitation", "hbm_budget_gb": 150}
-    big = max(q.model.parnum for q in reqs)
+                       "steps U[200,5000], sinusoid or band-limited noise base excitation", "hbm_budget_gb": 150,
+           "requests_built_s": t_gen}
+    energies = {}
     for form, key in ((abi.PG_FORM_MIXED, "mixed_pool"), (abi.PG_FORM_FP64, "fp64_pool")):
         srv = Server(reqs[0].model, reqs[0].dt, form=form, budget_bytes=150e9, max_scenes=256,
-                     max_spheres=max(big, sum(q.model.parnum for q in reqs)), max_scene_extent=4.0)
+                     max_scene_extent=4.0)
         torch.cuda.synchronize()
         res, st = srv.serve(reqs, realtime=True)
         srv.close()
+        energies[key] = {r.rid: r.energy for r in res if r.error is None}
         out[key] = {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "throughput": st["throughput"],
-                    "unit": "particle-steps/s", "wall_s": st["wall_s"], "requests": st["requests"]}
-    # the plain FP64 drop-in: each request alone through DEM(), in arrival order
+                    "unit": "particle-steps/s", "wall_s": st["wall_s"], "requests": st["requests"],
+                    "rejected": st["rejected"], "admission_wait_s": st["admission_wait_s"], "pool": st["pool"]}
+        del srv
+    rel = np.array([abs(energies["mixed_pool"][k] - e) / abs(e) for k, e in energies["fp64_pool"].items()
+                    if k in energies["mixed_pool"] and e != 0.0])
+    out["mixed_vs_fp64_energy_rel"] = {"requests": int(len(rel)), "max": float(rel.max()) if len(rel) else None,
+                                       "p50": float(np.percentile(rel, 50)) if len(rel) else None,
+                                       "p99": float(np.percentile(rel, 99)) if len(rel) else None,
+                                       "under_1e-6": int(np.sum(rel <= 1e-6)),
+                                       "definition": "kinetic + rotational + potential of the base gravity g0 "
+                                                     "at the request's end, mixed pool against FP64 pool"}
+    # the plain FP64 drop-in: each request alone through DEM(), in arrival
+    # order, with its excitation as the GRAVITY callable
     t0 = time.perf_counter()
     lat, ps = [], 0
     for q in reqs:
@@ -298,7 +362,8 @@ def serving_form(args, count):
         if now < q.arrival:
             time.sleep(q.arrival - now)
         m = q.model
-        m.set_gravity(0.0, 0.0, -9.81)
+        g = excitation_gravity(q.excitation)
+        m.set_gravity(lambda t, g=g: g(t)[0], lambda t, g=g: g(t)[1], lambda t, g=g: g(t)[2])
         eng = GpuEngine()
         m.dem(q.steps * q.dt - 0.5 * q.dt, q.dt, interval=1e9, engine=eng)
         eng.close()
@@ -307,37 +372,39 @@ def serving_form(args, count):
     wall = time.perf_counter() - t0
     out["fp64_dropin"] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                           "throughput": ps / wall, "unit": "particle-steps/s", "wall_s": wall,
-                          "note": "sinusoid excitation replaced by constant gravity; one DEM() per request"}
+                          "requests": len(lat),
+                          "note": "one DEM() per request with the request's excitation as a GRAVITY callable"}
+    out["mixed_pool_over_fp64_pool"] = out["mixed_pool"]["throughput"] / out["fp64_pool"]["throughput"]
     out["mixed_pool_over_fp64_dropin"] = out["mixed_pool"]["throughput"] / out["fp64_dropin"]["throughput"]
     return out
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the CPU restatement on all host cores, rank 0 only."""
+    """--impl reference: the reference's CPU hot path on all host cores, rank 0
+    only, on the same drum, config, metric and unit as the GPU arm; each step
+    is a bounded sample of the workload."""
     if rank != 0:
         return 0
-    from oracle.pyoracle import OracleEngine
-    from parmec_gb300.scenes import drum
     threads = os.cpu_count() or 1
-    m, dt, info = drum(args.spheres)
-    eng = OracleEngine(threads=threads)
-    m.dem(0.5 * dt, dt, interval=1e9, engine=eng)
-    if args.warmup > 1:
-        m.dem((args.warmup - 1) * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
-    t0 = time.perf_counter()
-    m.dem(args.steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
-    el = time.perf_counter() - t0
-    v = m.parnum * args.steps / el
+    from parmec_gb300.scenes import drum
+    _, _, info = drum(args.spheres)
+    v, kind, sample = reference_cpu(args.spheres, threads, args.steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": "particle-steps/s", "value": v, "unit": "particle-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "spheres": m.parnum},
-            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} DEM steps of the full drum (the reference's ISPC build "
-                                       "cannot be compiled here: no ispc, no HDF5)"},
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * args.spheres / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": arm_config(args, info, world),
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind,
+                             "sample": sample},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def arm_config(args, info, world):
+    """The workload both arms run (identical dicts)."""
+    return {"workload": WORKLOAD, "form": "plain FP64", "spheres": args.spheres, "triangles": 4096,
+            "parallelism": f"replicas x{world}", "l2": "state ~0.6 GB per replica, larger than L2; no flush",
+            "bed_solid_fraction": round(info["solid_fraction"], 3)}
 
 
 def main():
@@ -350,7 +417,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=512, help="scenes of the batched leg")
-    ap.add_argument("--serving", type=int, default=48, help="requests in the serving stream (0: skip)")
+    ap.add_argument("--serving", type=int, default=500, help="requests in the serving stream (0: skip)")
     ap.add_argument("--lattice", type=int, default=256, help="side of the spring lattice (0: skip)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -464,50 +531,45 @@ def main():
     total_ps = m.parnum * args.steps * world
     value = total_ps / (el_ms * 1e-3)
     hbm, peak_kind = peaks()
-    # roofline of the dominant kernel group (algorithmic bytes: each datum the
-    # kernel must read or write, counted once; formulas in the design doc)
+    # roofline of the dominant kernel group: the step's compulsory bytes per
+    # particle, B = 420 + 56 c (c = contact pairs per particle, measured on
+    # the pair list) times the particles of one launch, over the group's
+    # average CUDA-event time per step
     groups = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(groups, key=lambda k: groups[k][0])
     P = m.parnum
-    per_launch = {
-        "integrate": P * (696.0 + 53.0 * c_pair),
-        "contacts": P * (172.0 + 96.0 * c_pair),
-    }
     ms_dom, n_dom = groups[dom]
-    bytes_dom = per_launch.get(dom)
-    # DRAM bytes per launch: ncu capture of the 262,144-sphere case
-    # (profiles/k_integrate_k_contacts_drum_fp64.md) scaled by the units processed
+    avg_s = ms_dom * 1e-3 / args.steps
+    step_bytes = P * (420.0 + 56.0 * c_pair)
+    achieved = step_bytes / avg_s / 1e9
+    # the kernel's own data (each datum it reads or writes, counted once):
+    # 696 + 53 c_s bytes per particle for the integration (c_s: slave
+    # contacts), 172 + 96 c per sphere for the contacts
+    kernel_model = {"integrate": P * (696.0 + 53.0 * c_pair), "contacts": P * (172.0 + 96.0 * c_pair)}
+    # DRAM bytes per unit and FP64 instructions per unit of each kernel, from
+    # one ncu capture of the 262,144-sphere drum (dram__bytes_read.sum +
+    # dram__bytes_write.sum, and DADD + DMUL + DFMA thread instructions, per
+    # launch divided by the spheres), scaled to the full drum
     traffic_per_unit = {"integrate": 458.0, "contacts": 200.0}
-    traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
-    # FP64 pipe: thread-level FP64 instructions (DADD + DMUL + DFMA) per unit,
-    # counted by ncu on the same capture; peak = 2 per clock per SM
     fp64_per_unit = {"integrate": 294.0, "contacts": 161.0}
+    traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     fp64 = None
     if dom in fp64_per_unit:
         sm_mhz = clk.get("sm_mhz") or 2070.0
         peak_g = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * sm_mhz * 1e6 / 1e9
-        ach_g = fp64_per_unit[dom] * P / (ms_dom * 1e-3 / args.steps) / 1e9
+        ach_g = fp64_per_unit[dom] * P / avg_s / 1e9
         fp64 = {"kernel": dom, "ops_per_unit": fp64_per_unit[dom], "achieved": ach_g, "peak": peak_g,
                 "unit": "G FP64 inst/s", "frac": ach_g / peak_g,
-                "source": "ops per unit from ncu (profiles/k_integrate_k_contacts_drum_fp64.md); "
-                          "peak 2 FP64 lanes/clk/SM at the sampled SM clock"}
-    if bytes_dom is not None:
-        avg_s = ms_dom * 1e-3 / args.steps
-        achieved = bytes_dom / avg_s / 1e9
-    else:
-        achieved = None
-    step_bytes = P * (420.0 + 56.0 * c_pair)
+                "source": "FP64 instructions per unit from one ncu capture; peak 2 FP64 lanes/clk/SM at the "
+                          "sampled SM clock"}
     step_gbs = step_bytes / (el_ms * 1e-3 / args.steps) / 1e9
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "plain FP64 (bit-exact with the oracle)",
-                   "spheres": m.parnum, "triangles": m.trinum, "parallelism": f"replicas x{world}",
-                   "l2": "state ~0.6 GB per replica, larger than L2; no flush",
-                   "bed_solid_fraction": round(info["solid_fraction"], 3),
-                   "contacts_per_particle": round(c_pair, 3)},
+        "config": arm_config(args, info, world),
+        "contacts_per_particle": round(c_pair, 3),
         "e2e": {"value": m.parnum * args.steps * world / e2e_s, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": up // args.steps, "d2h_bytes_per_step": down // args.steps,
                 "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
@@ -515,11 +577,14 @@ def main():
                         "page-locked by the engine (cudaHostRegister)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None,
-                     "traffic": traffic, "traffic_source": "ncu 262,144-sphere capture scaled per unit",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "algorithmic_bytes": "420 + 56 c per particle-step (the whole step's compulsory traffic), "
+                                          "c = contact pairs per particle",
+                     "traffic_source": "ncu DRAM bytes per unit of the 262,144-sphere drum, scaled to the launch",
                      "peak_source": peak_kind,
+                     "kernel_model_gbs": kernel_model[dom] / avg_s / 1e9 if dom in kernel_model else None,
                      "step_algorithmic_gbs": step_gbs, "step_frac": step_gbs / hbm,
-                     "note": "FP64-ALU bound on GB300 (2 DFMA/clk/SM): see fp64_pipe and profiles/"},
+                     "note": "the FP64 form is bound by the FP64 pipe (2 DFMA/clk/SM on GB300): see fp64_pipe"},
         "fp64_pipe": fp64,
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in groups.items()},
         "clocks": clk,

@@ -1,12 +1,14 @@
-"""parmec.cpp's dem() loop over the drop-in ISPC entry points.
+"""parmec.cpp's dem() loop over a library of the reference's ISPC entry points
+(TEST INFRASTRUCTURE ONLY).
 
 This restates, in Python on a Model's host arrays, what an unmodified
-parmec.cpp does when it links against libparmec_gb300.so in place of the
-ISPC objects (include/parmec_ispc.h): the call sequence of dem()
-(parmec.cpp:2386-2517) with the host code between the calls
+parmec.cpp does when it links against such a library: the call sequence of
+dem() (parmec.cpp:2386-2517) with the host code between the calls
 (read_gravity_and_damping, prescribe_acceleration, prescribe_velocity and
-obstaclev, input.cpp:4199-4503).  Test infrastructure: the GPU parity tests
-run it beside the oracle.
+obstaclev, input.cpp:4199-4503).  It drives two libraries with the same
+exports: libparmec_gb300.so's drop-in (include/parmec_ispc.h; the GPU parity
+tests) and the reference's own hot path translated from its ISPC sources
+(oracle/ispc_ref.py; the CPU pins and bench.py's reference arm).
 """
 import ctypes
 

@@ -47,6 +47,11 @@ class Result:
     position: np.ndarray = field(repr=False)
     linear: np.ndarray = field(repr=False)
     error: str = None
+    energy: float = None      # kinetic + rotational + potential of the base gravity g0, at the end
+
+    @property
+    def wait(self):
+        return self.admitted - self.arrival
 
     @property
     def latency(self):
@@ -111,10 +116,13 @@ class Server:
         self.form = form
         self.dt = dt
         self.chunk = chunk
-        cap = int(budget_bytes // bytes_per_sphere(form, kn, kr))
+        self.bps = bytes_per_sphere(form, kn, kr)
+        self.budget = float(budget_bytes)
+        cap = int(budget_bytes // self.bps)
         if max_spheres is not None:
             cap = min(cap, int(max_spheres))
         self.cap = cap
+        self.last_energy = None
         self.tcap = int(max_triangles if max_triangles is not None else 12 * max_scenes)
         self.max_scenes = max_scenes
         self.P = self._empty_pool(template, cap, self.tcap, max_scenes)
@@ -198,6 +206,7 @@ class Server:
         P = self.P
         pos = P.P.position[0:3, e0:e1].copy()
         lin = P.P.linear[:, e0:e1].copy()
+        self.last_energy = range_energy(P, e0, e1, req.excitation[0:3])
         self.eng.set_scene(slot, False)
         P.pscene[e0:e1] = -1
         P.tscene[t0:t1] = -1
@@ -252,6 +261,7 @@ class Server:
         now = lambda: time.perf_counter() - t0
         steps_done = 0
         psteps = 0
+        peak_spheres = peak_scenes = 0
         while pending or self.active:
             # admit in arrival order while there is room
             while pending and (not realtime or pending[0].arrival <= now()) and self.slots:
@@ -277,19 +287,65 @@ class Server:
                 self.active[slot] = (req, r, rem, adm)
                 if rem == 0:
                     pos, lin = self._unload(slot)
-                    results.append(Result(req.rid, req.arrival, adm, now(), req.steps, r[1] - r[0], pos, lin))
+                    results.append(Result(req.rid, req.arrival, adm, now(), req.steps, r[1] - r[0], pos, lin,
+                                          energy=self.last_energy))
+            in_use = self.cap - sum(e - b for b, e in self.spheres.free)
+            peak_spheres = max(peak_spheres, in_use)
+            peak_scenes = max(peak_scenes, len(self.active))
         wall = now()
-        lat = np.array([x.latency for x in results if x.error is None])
+        ok = [x for x in results if x.error is None]
+        lat = np.array([x.latency for x in ok])
+        wait = np.array([x.wait for x in ok])
+        edges = [0.0, 0.01, 0.1, 1.0, 10.0, float("inf")]
+        hist = np.histogram(wait, bins=edges)[0].tolist() if len(wait) else [0] * (len(edges) - 1)
         stats = {"requests": len(lat), "rejected": sum(1 for x in results if x.error), "wall_s": wall,
                  "particle_steps": psteps,
                  "throughput": psteps / wall if wall > 0 else 0.0,
                  "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
                  "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                 "admission_wait_s": {"p50": float(np.percentile(wait, 50)) if len(wait) else None,
+                                      "p99": float(np.percentile(wait, 99)) if len(wait) else None,
+                                      "histogram_edges_s": edges[:-1] + ["inf"], "histogram": hist},
+                 "pool": {"sphere_capacity": self.cap, "peak_spheres": peak_spheres,
+                          "scene_slots": self.max_scenes, "peak_scenes": peak_scenes,
+                          "budget_bytes": self.budget, "bytes_per_sphere": self.bps},
                  "steps_launched": steps_done}
         return results, stats
 
     def close(self):
         self.eng.close()
+
+
+def range_energy(P, e0, e1, g0):
+    """Kinetic, rotational and gravity-potential energy (base gravity g0) of
+    pool particles [e0, e1)."""
+    mass = P.P.mass[e0:e1]
+    v = P.P.linear[:, e0:e1]
+    O = P.P.angular[0:3, e0:e1]
+    J = P.P.inertia[:, e0:e1]
+    JO = np.stack([J[0] * O[0] + J[3] * O[1] + J[6] * O[2],
+                   J[1] * O[0] + J[4] * O[1] + J[7] * O[2],
+                   J[2] * O[0] + J[5] * O[1] + J[8] * O[2]])
+    g = np.asarray(g0, dtype=np.float64).reshape(3, 1)
+    return (0.5 * float(np.sum(mass * np.sum(v * v, axis=0))) + 0.5 * float(np.sum(O * JO))
+            - float(np.sum(mass * np.sum(g * P.P.position[0:3, e0:e1], axis=0))))
+
+
+def excitation_gravity(exc):
+    """The base excitation record as a host GRAVITY callable g(t) =
+    g0 + dir * sum_k amp_k sin(2 pi freq_k t + phase_k): the same excitation
+    for a request run through DEM() one at a time."""
+    import math
+    g0 = [float(x) for x in exc[0:3]]
+    d = [float(x) for x in exc[3:6]]
+    comps = [(float(exc[8 + 3 * k]), float(exc[9 + 3 * k]), float(exc[10 + 3 * k])) for k in range(int(exc[6]))]
+
+    def g(t):
+        a = 0.0
+        for amp, f, ph in comps:
+            a += amp * math.sin(2.0 * math.pi * f * t + ph)
+        return (g0[0] + d[0] * a, g0[1] + d[1] * a, g0[2] + d[2] * a)
+    return g
 
 
 def request_stream(count, rate=200.0, seed=4, nmin=1024, nmax=262144, smin=200, smax=5000):

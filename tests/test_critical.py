@@ -184,12 +184,15 @@ def test_gpu_critical_matches_restatement(gpu_lib, oracle_lib):
         touched = hh < 1e300
         assert touched.sum() > 10
         assert np.array_equal(touched, h < 1e300)
+        # the rotational frequency is an eigenvalue of a nearly double-rooted
+        # 3x3 (a contact arm gives a rank-two stiffness): last-bit differences
+        # of two evaluations grow by its conditioning, so 1e-7 relative
         for a, b in ((h, hh), (o, oh), (r, rh)):
-            assert np.allclose(a[touched], b[touched], rtol=1e-12, atol=0.0)
+            assert np.allclose(a[touched], b[touched], rtol=1e-7, atol=0.0)
         if m.sprnum:
             hs, os_, rs = eng.critical(1)
             for a, b in zip((hs, os_, rs), critical_perspring(m)):
-                assert np.allclose(a, np.array(b), rtol=1e-12, atol=0.0)
+                assert np.allclose(a, np.array(b), rtol=1e-7, atol=0.0)
         # Model.critical takes the session the DEM call stepped with
         (hp, i, om, ra), = m.critical(perparticle=1)
         assert hp == float(np.min(h)) and i == int(np.argmin(h))

@@ -33,7 +33,7 @@ import subprocess
 import numpy as np
 import pytest
 
-import ispc_loop
+from oracle import dem_loop as ispc_loop
 from helpers import make_collision_scene
 
 STATE = ("position", "linear", "angular", "rotation", "force", "torque")

@@ -148,7 +148,7 @@ def test_gpu_torsion_adaptive_bitwise(gpu_lib, oracle_lib):
 @pytest.mark.gpu
 def test_dropin_torsion_bitwise(gpu_lib, oracle_lib):
     """forces() with torsion springs through the drop-in exports."""
-    import ispc_loop
+    from oracle import dem_loop as ispc_loop
     from oracle.pyoracle import OracleEngine
     lib = ispc_loop.library()
     lib.pg_compat_exit_on_error(0)

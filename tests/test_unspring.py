@@ -122,7 +122,7 @@ def test_dropin_unspring_bitwise(gpu_lib, oracle_lib):
     """forces() with UNSPRING rules through the drop-in exports."""
     import ctypes
 
-    import ispc_loop
+    from oracle import dem_loop as ispc_loop
     from oracle.pyoracle import OracleEngine
     lib = ispc_loop.library()
     lib.pg_compat_exit_on_error(0)
