@@ -289,6 +289,21 @@ int pg_session_restrain_velocities(pg_session *s);
  * form, one scene without device excitation; else PG_ERR_UNSUPPORTED. */
 int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, double adaptive, double *steps);
 
+/* Mesh-mesh contact, an extension with no counterpart in the reference
+ * (whose contact detection holds spheres only, partition.ispc:600-646, and
+ * returns at once for meshes, condet.ispc:786): every triangle of a MESH
+ * particle is swept by a sphere of 'radius', and triangles of different
+ * particles closer than 2 * radius touch, with the GRANULAR law of their
+ * colours (pg_tritri.cuh states the geometry).  'cell' is the grid cell
+ * (at least the largest box of a triangle not flagged in 'big', radius
+ * included); big[t] = 1 marks triangles searched against all others.
+ * radius = 0 turns it off.  FP64 form, one scene, fixed steps (adaptive
+ * stepping returns PG_ERR_UNSUPPORTED while it is on); steps with it run
+ * without CUDA graphs. */
+int pg_session_mesh_contact(pg_session *s, double radius, double cell, const unsigned char *big);
+/* Triangle pairs whose boxes overlapped in the last step, and those in contact. */
+int pg_session_mesh_contact_stats(pg_session *s, int *pairs, int *active);
+
 /* CRITICAL (input.cpp:3034-3154) on the device.  which = 0: per particle
  * (critical_perparticle, parmec.ispc:547-888) from the contacts of the last
  * step and the springs: h, omega, ratio get parnum entries; which = 1: per

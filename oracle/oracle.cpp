@@ -46,11 +46,18 @@
  *
  * Parity pins: tests/golden holds the two self-checking decks of the
  * reference (tests/damping.py, tests/spring_curve_tests.py) restated in
- * Python 3, plus analytic known-answer cases.  The contact-detection and
- * granular-force parts have no golden vector in the reference; for those the
- * oracle is pinned only by the analytic cases.
+ * Python 3, plus analytic known-answer cases; tests/test_reference_pin.py
+ * compares the whole step with the reference's own ISPC sources, translated
+ * to C++ by oracle/ispc_ref.py and run with parmec.cpp's call sequence.
+ *
+ * Mesh-mesh contact (or_mesh_contact) is an extension with no counterpart in
+ * the reference: its pair search is a brute-force restatement of the
+ * device's definitions (pg_meshcontact.cu), and its narrow phase and contact
+ * law are the shared functions of parmec_gb300/csrc/pg_tritri.cuh, checked
+ * on their own against analytic distances by tests/test_meshcontact.py.
  */
 #include "../include/parmec_gb300.h"
+#include "../parmec_gb300/csrc/pg_tritri.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -370,6 +377,13 @@ struct or_ctx
   /* adaptive stepping terms per particle, component-major:
    * kact[3][P], krot[6][P], kmax[P], emax[P] (forces.ispc:453-596) */
   std::vector<double> kact, krot, kmax, emax;
+  /* mesh-mesh contact: swept radius (0: off), big-triangle flags, and the
+   * previous step's pairs (offsets per finder, partners, active, state) */
+  double tt_r = 0.0;
+  std::vector<unsigned char> tt_big;
+  std::vector<int> tt_poff, tt_ppu;
+  std::vector<unsigned char> tt_pact;
+  std::vector<double> tt_pst;
 };
 
 namespace {
@@ -2142,6 +2156,141 @@ void or_condet_forces(or_ctx *ctx, pg_scene *s, double step, double curtime,
 
 namespace {
 
+/* ---------------- mesh-mesh contact (extension; pg_meshcontact.cu) -------
+ * Pairs in finder order: every mesh triangle t in index order finds, among
+ * all triangles u in index order, the partners of another particle whose
+ * boxes (widened by r) overlap, by the device's rule (two small or two big
+ * triangles: the lower index finds; small and big: the small one finds).
+ * Each pair's contact and granular force, with its tangential state from
+ * the previous step's pair (finder, partner); then per particle the entries
+ * (+f for the finder's particle, -f for the partner's) in pair order, summed
+ * by 32 strided lanes from zero and the lane sums added in lane order, and
+ * added to the force and torque after gravity. */
+int tt_pair_finder(const or_ctx *ctx, const pg_scene *s, int t, int u, const std::vector<double> &box)
+{
+  if (u == t || s->triobs[u] < 0 || s->triobs[u] == s->triobs[t]) return 0;
+  const bool big = ctx->tt_big[t] != 0, ubig = ctx->tt_big[u] != 0;
+  if (big && !ubig) return 0;
+  if (big == ubig && u < t) return 0;
+  const int T = s->trinum;
+  for (int c = 0; c < 3; c ++)
+    if (!(box[(size_t)c*T + t] < box[(size_t)(3+c)*T + u] && box[(size_t)c*T + u] < box[(size_t)(3+c)*T + t]))
+      return 0;
+  return 1;
+}
+
+void tt_all(or_ctx *ctx, pg_scene *s, double step)
+{
+  const int T = s->trinum, P = s->parnum;
+  const double r = ctx->tt_r;
+  std::vector<double> box(6 * (size_t)T, 0.0);
+  for (int t = 0; t < T; t ++)
+  {
+    if (s->triobs[t] < 0) continue;
+    for (int c = 0; c < 3; c ++)
+    {
+      const double a = s->tri[0][c][t], b = s->tri[1][c][t], e = s->tri[2][c][t];
+      double l = a < b ? a : b, h = a > b ? a : b;
+      l = l < e ? l : e;
+      h = h > e ? h : e;
+      box[(size_t)c*T + t] = l - r;
+      box[(size_t)(3+c)*T + t] = h + r;
+    }
+  }
+  std::vector<int> off(T + 1, 0), pf, pu;
+  for (int t = 0; t < T; t ++)
+  {
+    off[t] = (int)pu.size();
+    if (s->triobs[t] < 0) continue;
+    for (int u = 0; u < T; u ++)
+      if (tt_pair_finder(ctx, s, t, u, box)) { pf.push_back(t); pu.push_back(u); }
+  }
+  off[T] = (int)pu.size();
+  const size_t np = pu.size();
+  std::vector<unsigned char> act(np, 0);
+  std::vector<double> st(3 * np, 0.0), fr(3 * np, 0.0), pt(3 * np, 0.0);
+  for (size_t k = 0; k < np; k ++)
+  {
+    const int f = pf[k], u = pu[k];
+    double va[3][3], vb[3][3];
+    for (int a = 0; a < 3; a ++)
+      for (int c = 0; c < 3; c ++) { va[a][c] = s->tri[a][c][f]; vb[a][c] = s->tri[a][c][u]; }
+    const double *A[3] = {va[0], va[1], va[2]}, *B[3] = {vb[0], vb[1], vb[2]};
+    double point[3], normal[3], sk[3] = {0.0, 0.0, 0.0}, fk[3] = {0.0, 0.0, 0.0};
+    const double depth = pgtt::contact(A, B, r, r, point, normal);
+    const bool active = depth > 0.0;
+    if (active)
+    {
+      if (!ctx->tt_poff.empty())
+      {
+        const int b0 = ctx->tt_poff[f], b1 = ctx->tt_poff[f+1];
+        const int *q = std::lower_bound(ctx->tt_ppu.data() + b0, ctx->tt_ppu.data() + b1, u);
+        const int j = (int)(q - ctx->tt_ppu.data());
+        if (j < b1 && ctx->tt_ppu[j] == u && ctx->tt_pact[j])
+          for (int c = 0; c < 3; c ++) sk[c] = ctx->tt_pst[3*(size_t)j + c];
+      }
+      const int pa = s->triobs[f], pb = s->triobs[u];
+      double vij[3];
+      const double za[3] = {point[0]-s->position[0][pa], point[1]-s->position[1][pa], point[2]-s->position[2][pa]};
+      const double zb[3] = {point[0]-s->position[0][pb], point[1]-s->position[1][pb], point[2]-s->position[2][pb]};
+      for (int c = 0; c < 3; c ++)
+      {
+        const int c1 = (c+1)%3, c2 = (c+2)%3;
+        const double vi = s->angular[3+c1][pa]*za[c2] - s->angular[3+c2][pa]*za[c1] + s->linear[c][pa];
+        const double vj = s->angular[3+c1][pb]*zb[c2] - s->angular[3+c2][pb]*zb[c1] + s->linear[c][pb];
+        vij[c] = vj - vi;
+      }
+      const int ij = pairing(s->pairnum, s->pairs, s->tricol[f], s->tricol[u]);
+      const double ma = 1.0 / (s->invm[pa] + s->invm[pb]);
+      pgtt::granular(s->iparam[SPRING][ij], s->iparam[DAMPER][ij], s->iparam[KSKN][ij], s->iparam[FRISTAT][ij],
+                     s->iparam[FRIDYN][ij], ma, normal, vij, depth, step, sk, fk);
+    }
+    act[k] = active ? 1 : 0;
+    for (int c = 0; c < 3; c ++) { st[3*k + c] = sk[c]; fr[3*k + c] = fk[c]; pt[3*k + c] = point[c]; }
+  }
+  std::vector<std::vector<int>> ent(P);
+  for (size_t k = 0; k < np; k ++)
+    if (act[k])
+    {
+      ent[s->triobs[pf[k]]].push_back(2 * (int)k);
+      ent[s->triobs[pu[k]]].push_back(2 * (int)k + 1);
+    }
+  for (int p = 0; p < P; p ++)
+  {
+    if (ent[p].empty()) continue;
+    double part[32][6];
+    const double x[3] = {s->position[0][p], s->position[1][p], s->position[2][p]};
+    for (int L = 0; L < 32; L ++)
+    {
+      double a6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (size_t q = L; q < ent[p].size(); q += 32)
+      {
+        const int v = ent[p][q], k = v >> 1;
+        double f[3] = {fr[3*(size_t)k], fr[3*(size_t)k + 1], fr[3*(size_t)k + 2]};
+        if (v & 1) { f[0] = -f[0]; f[1] = -f[1]; f[2] = -f[2]; }
+        const double a[3] = {pt[3*(size_t)k]-x[0], pt[3*(size_t)k + 1]-x[1], pt[3*(size_t)k + 2]-x[2]};
+        a6[0] += f[0]; a6[1] += f[1]; a6[2] += f[2];
+        a6[3] += a[1]*f[2] - a[2]*f[1];
+        a6[4] += a[2]*f[0] - a[0]*f[2];
+        a6[5] += a[0]*f[1] - a[1]*f[0];
+      }
+      for (int c = 0; c < 6; c ++) part[L][c] = a6[c];
+    }
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int L = 0; L < 32; L ++)
+      for (int c = 0; c < 6; c ++) acc[c] += part[L][c];
+    for (int c = 0; c < 3; c ++)
+    {
+      s->force[c][p] = s->force[c][p] + acc[c];
+      s->torque[c][p] = s->torque[c][p] + acc[3+c];
+    }
+  }
+  ctx->tt_poff = off;
+  ctx->tt_ppu = pu;
+  ctx->tt_pact = act;
+  ctx->tt_pst = st;
+}
+
 AdTerms adaptive_terms(or_ctx *ctx, int P)
 {
   ctx->kact.assign(3 * (size_t)P, 0.0);
@@ -2178,6 +2327,7 @@ double loop_step(or_ctx *ctx, pg_scene *s, const pg_steptab *tab, int n, double 
   build_slaves(ctx, s);
 #pragma omp parallel for schedule(dynamic, 64) num_threads(ctx->threads)
   for (int i = 0; i < P; i ++) contacts_acc_one(s, ctx->master[i], ctx->slave[i], i, grav, at);
+  if (ctx->tt_r > 0.0) tt_all(ctx, s, step0);
   if (s->sprnum) springs_all(s, step0, curtime, at);
   if (s->trqsprnum) trqspr_all(s, step0, at);
   if (s->unsprnum) unspring_all(s, tab->stepnum);
@@ -2262,6 +2412,36 @@ void or_restrain_velocities(or_ctx *, pg_scene *s) { restrain_velocities(s); }
 
 /* restrain_forces export (restrain.ispc:147) */
 void or_restrain_forces(or_ctx *, pg_scene *s) { restrain_forces(s); }
+
+/* Mesh-mesh contact on (radius > 0, with the big-triangle flags of the
+ * device's search) or off; the previous step's pairs are dropped. */
+void or_mesh_contact(or_ctx *ctx, const pg_scene *s, double radius, const unsigned char *big)
+{
+  ctx->tt_r = radius > 0.0 ? radius : 0.0;
+  ctx->tt_big.assign(big ? big : (const unsigned char *)nullptr, big ? big + s->trinum : nullptr);
+  if (!big) ctx->tt_big.assign((size_t)s->trinum, 0);
+  ctx->tt_poff.clear();
+  ctx->tt_ppu.clear();
+  ctx->tt_pact.clear();
+  ctx->tt_pst.clear();
+}
+
+/* The swept-triangle contact of triangles a and b (9 coordinates each,
+ * vertex after vertex): depth, point and normal (pg_tritri.cuh). */
+double or_tt_contact(const double *a9, const double *b9, double ra, double rb, double *point, double *normal)
+{
+  const double *A[3] = {a9, a9 + 3, a9 + 6}, *B[3] = {b9, b9 + 3, b9 + 6};
+  return pgtt::contact(A, B, ra, rb, point, normal);
+}
+
+/* Pairs and active pairs of the last mesh-contact stage. */
+void or_mesh_contact_stats(const or_ctx *ctx, int *pairs, int *active)
+{
+  *pairs = (int)ctx->tt_ppu.size();
+  int a = 0;
+  for (unsigned char v : ctx->tt_pact) a += v ? 1 : 0;
+  *active = a;
+}
 
 /* Per-particle critical step, frequency and damping ratio from the terms of
  * the latest adaptive step (time_step_task, parmec.ispc:275-383). */

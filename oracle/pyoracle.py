@@ -47,6 +47,9 @@ def load():
         "or_run": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double]),
         "or_run_adaptive": (ctypes.c_int, [P, S, ctypes.POINTER(abi.PgStepTab), ctypes.c_double, ctypes.c_double, D]),
         "or_critical_terms": (ctypes.c_int, [P, S, D, D, D]),
+        "or_mesh_contact": (None, [P, S, ctypes.c_double, ctypes.c_void_p]),
+        "or_mesh_contact_stats": (None, [P, abi.I, abi.I]),
+        "or_tt_contact": (ctypes.c_double, [D, D, ctypes.c_double, ctypes.c_double, D, D]),
         "or_restrain_velocities": (None, [P, S]),
         "or_restrain_forces": (None, [P, S]),
         "or_dynamics": (None, [P, S, D, ctypes.c_double, ctypes.c_double]),
@@ -84,6 +87,11 @@ class OracleEngine:
         self.counts = _counts(m)
         self.ctx = self.lib.or_create(ctypes.byref(self.scene))
         self.lib.or_set_threads(self.ctx, self.threads)
+        if getattr(m, "tt_radius", 0.0) > 0.0:
+            from parmec_gb300.mesh import mesh_contact_grid
+            _, big = mesh_contact_grid(m)
+            self._tt_big = big
+            self.lib.or_mesh_contact(self.ctx, ctypes.byref(self.scene), m.tt_radius, big.ctypes.data)
 
     def stale(self):
         from parmec_gb300.engine import _counts
@@ -120,6 +128,12 @@ class OracleEngine:
         if self.lib.or_critical_terms(self.ctx, ctypes.byref(self.scene), abi.dptr(h), abi.dptr(o), abi.dptr(r)):
             raise RuntimeError("no adaptive step has run")
         return h[:n], o[:n], r[:n]
+
+    def mesh_contact_stats(self):
+        """(pairs, active pairs) of the last step's mesh-mesh contact stage."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self.lib.or_mesh_contact_stats(self.ctx, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
 
     def critical(self, which):
         """CRITICAL restated on the host (oracle/critical_host.py) over this

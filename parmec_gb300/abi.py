@@ -158,6 +158,8 @@ def load_library():
         "pg_session_run_adaptive": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double, ctypes.c_double, D]),
         "pg_session_restrain_velocities": (ctypes.c_int, [P]),
         "pg_session_critical": (ctypes.c_int, [P, ctypes.c_int, D, D, D]),
+        "pg_session_mesh_contact": (ctypes.c_int, [P, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+        "pg_session_mesh_contact_stats": (ctypes.c_int, [P, I, I]),
         "pg_session_download_particles": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_download_springs": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_sync": (ctypes.c_int, [P]),

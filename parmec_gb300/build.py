@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 SOURCES = ["pg_step.cu", "pg_rebuild.cu", "pg_sort.cu", "pg_partition.cu", "pg_mixed.cu", "pg_session.cu",
-           "pg_compat.cu"]
+           "pg_compat.cu", "pg_meshcontact.cu"]
 # the FP64 form must not contract multiply-adds (bit parity with the oracle);
 # the mixed form is FP32 arithmetic with explicit error-free transformations
 FMAD = {"pg_mixed.cu": "true"}

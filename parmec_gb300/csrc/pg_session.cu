@@ -13,6 +13,7 @@
 #include <cmath>
 #include "pg_state.h"
 #include "pg_launch.h"
+#include "pg_meshcontact.h"
 #include "../../include/parmec_gb300.h"
 
 struct pg_session
@@ -45,6 +46,8 @@ struct pg_session
   // (PgDev.hs points at hs_buf only while an adaptive run is enqueued)
   double *hs_buf = nullptr;
   int adapt_ready = 0, hrec_cap = 0, sbig_ad_cap = 0;
+  // mesh-mesh contact (pg_meshcontact.cu); steps then run without graphs
+  PgTT tt;
   // CRITICAL: per-spring slope and damping, and the per-item outputs
   double *crit_ke = nullptr, *crit_h = nullptr, *crit_o = nullptr, *crit_r = nullptr;
   int exc_any = 0;                         // some scene has a device excitation
@@ -1021,6 +1024,8 @@ int run_fused_steps(pg_session *s, double step, int n)
   return run_fused(s, step, n - done, 16);
 }
 
+int tt_stage(pg_session *s, double step);
+
 void enqueue_step(pg_session *s, double step)
 {
   const PgDev &d = s->d;
@@ -1040,10 +1045,65 @@ void enqueue_step(pg_session *s, double step)
   pg_launch_spring_runs(d, s->stream);
   pg_launch_torsion(d, s->stream, step);
   pg_launch_unspring(d, s->stream);
+  if (d.tt_on) tt_stage(s, step);
   pg_launch_integrate(d, s->stream, step);
   pg_launch_mesh(d, s->stream);
   pg_launch_obstacles_row(d, s->stream, step);
   pg_launch_tail(d, s->stream, step);
+}
+
+// the mesh-contact stage of one step: pairs, forces and per-particle sums;
+// it reads the pair count back (one host wait per step), so steps with mesh
+// contact are not captured in graphs
+int tt_stage(pg_session *s, double step)
+{
+  PgDev &d = s->d;
+  PgTT &g = s->tt;
+  pg_tt_find(d, g, s->stream);
+  int np = 0;
+  TRY(d2h(s, &np, g.np_dev, 1));
+  CK(cudaStreamSynchronize(s->stream));
+  if (np > g.cap)
+  {
+    // room for the pairs of this step (and the next): both pair lists grow
+    // together, the previous step's list keeping its entries
+    const int cap = np + np / 2 + 1024;
+    int *ppu = nullptr; unsigned char *pact = nullptr; double *pst[3] = {};
+    int *pf = nullptr, *pu = nullptr; unsigned char *act = nullptr; double *st[3] = {}, *f[3] = {}, *p[3] = {};
+    TRY(dalloc(s, &pf, cap)); TRY(dalloc(s, &pu, cap)); TRY(dalloc(s, &act, cap)); TRY(dalloc(s, &ppu, cap));
+    TRY(dalloc(s, &pact, cap));
+    for (int c = 0; c < 3; c ++)
+    {
+      TRY(dalloc(s, &st[c], cap)); TRY(dalloc(s, &f[c], cap)); TRY(dalloc(s, &p[c], cap)); TRY(dalloc(s, &pst[c], cap));
+    }
+    if (g.cap > 0)
+    {
+      CK(cudaMemcpyAsync(ppu, g.ppu, (size_t)g.cap * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+      CK(cudaMemcpyAsync(pact, g.pact, (size_t)g.cap, cudaMemcpyDeviceToDevice, s->stream));
+      for (int c = 0; c < 3; c ++)
+        CK(cudaMemcpyAsync(pst[c], g.pst[c], (size_t)g.cap * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    for (void *q : {(void *)g.pf, (void *)g.pu, (void *)g.act, (void *)g.ppu, (void *)g.pact}) release(s, q);
+    for (int c = 0; c < 3; c ++) for (void *q : {(void *)g.st[c], (void *)g.f[c], (void *)g.p[c], (void *)g.pst[c]}) release(s, q);
+    release(s, g.ekeys[0]); release(s, g.ekeys[1]); release(s, g.evals[0]); release(s, g.evals[1]); release(s, g.ehist);
+    TRY(dalloc(s, &g.ekeys[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.ekeys[1], 2 * (size_t)cap));
+    TRY(dalloc(s, &g.evals[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.evals[1], 2 * (size_t)cap));
+    TRY(dalloc(s, &g.ehist, 256 * (size_t)pg_sort_blocks(2 * cap)));
+    g.pf = pf; g.pu = pu; g.act = act; g.ppu = ppu; g.pact = pact;
+    for (int c = 0; c < 3; c ++) { g.st[c] = st[c]; g.f[c] = f[c]; g.p[c] = p[c]; g.pst[c] = pst[c]; }
+    g.cap = cap;
+  }
+  pg_tt_forces(d, g, s->stream, np, step);
+  s->launches += pg_tt_kernel_count(g, np);
+  // this step's pairs become the previous step's
+  g.np_last = np;
+  std::swap(g.off, g.poff);
+  std::swap(g.pu, g.ppu);
+  std::swap(g.act, g.pact);
+  for (int c = 0; c < 3; c ++) std::swap(g.st[c], g.pst[c]);
+  CK(cudaGetLastError());
+  return PG_OK;
 }
 
 // capture one step into a CUDA graph (kernel arguments are baked in: the
@@ -1329,7 +1389,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
     return PG_OK;
   }
   const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d) + (d.form == PG_FORM_MIXED ? 1 : 0);
-  if (!s->profile && s->use_graph)
+  if (!s->profile && s->use_graph && !d.tt_on)
   {
     TRY(capture_step(s, step));
     for (int k = 0; k < n; k ++) CK(cudaGraphLaunch(s->graph_exec, s->stream));
@@ -1361,6 +1421,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
         pg_launch_spring_runs(d, s->stream);
         pg_launch_torsion(d, s->stream, step);
         pg_launch_unspring(d, s->stream);
+        if (d.tt_on) TRY(tt_stage(s, step));
       }
       CK(cudaEventRecord(ev[3], s->stream));
       if (d.form == PG_FORM_MIXED) pg_launch_integrate_mx(d, s->stream, step);
@@ -1478,6 +1539,107 @@ int pg_session_restrain_velocities(pg_session *s)
   return PG_OK;
 }
 
+int pg_session_mesh_contact(pg_session *s, double radius, double cell, const unsigned char *big)
+{
+  if (!s || !(radius >= 0.0)) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (radius == 0.0) { d.tt_on = 0; return PG_OK; }
+  if (!(cell > 0.0) || !big) return PG_ERR_ARGUMENT;
+  if (d.form != PG_FORM_FP64 || d.nscene > 1) return PG_ERR_UNSUPPORTED;
+  PgTT &g = s->tt;
+  const int T = d.trinum, P = d.parnum;
+  if (T <= 0 || P <= 0) return PG_OK;
+  drop_graph(s);
+  CK(cudaStreamSynchronize(s->stream));
+  // the grid spans the mesh triangles' present boxes with two cells of
+  // margin each way (triangles that leave it take the nearest cell: only
+  // the search slows, no pair is lost)
+  std::vector<double> tri(9 * (size_t)T);
+  std::vector<int> tob(T);
+  for (int k = 0; k < 9; k ++) TRY(d2h(s, tri.data() + (size_t)k * T, d.tri[k], T));
+  TRY(d2h(s, tob.data(), d.triobs, T));
+  CK(cudaStreamSynchronize(s->stream));
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int t = 0; t < T; t ++)
+  {
+    if (tob[t] < 0 || big[t]) continue;
+    for (int a = 0; a < 3; a ++)
+      for (int c = 0; c < 3; c ++)
+      {
+        const double x = tri[(size_t)(3*a + c) * T + t];
+        lo[c] = std::min(lo[c], x);
+        hi[c] = std::max(hi[c], x);
+      }
+  }
+  double h = cell;
+  for (int c = 0; c < 3; c ++) if (!(hi[c] >= lo[c])) { lo[c] = 0.0; hi[c] = 0.0; }
+  long long cells = 0;
+  int dim[3];
+  for (;;)
+  {
+    cells = 1;
+    for (int c = 0; c < 3; c ++)
+    {
+      dim[c] = (int)std::ceil((hi[c] - lo[c]) / h) + 5;
+      cells *= dim[c];
+    }
+    if (cells <= (1LL << 26)) break;
+    h *= 1.25;                                 // a coarser grid: more triangles per cell, the same pairs
+  }
+  g.r = radius;
+  g.h = h;
+  for (int c = 0; c < 3; c ++) { g.org[c] = lo[c] - 2.0 * h; g.dim[c] = dim[c]; }
+  g.ncells = (int)cells;
+  const int kb = pg_tt_key_bits(g.ncells);
+  g.none = (1u << kb) - 1u;
+  g.passes = pg_sort_passes_bits(kb);
+  int pb = 1;
+  while ((1u << pb) <= (unsigned)P) pb ++;
+  g.enone = (1u << pb) - 1u;
+  g.epasses = pg_sort_passes_bits(pb);
+  if (!g.big)
+  {
+    TRY(dalloc(s, &g.big, T));
+    for (int c = 0; c < 6; c ++) TRY(dalloc(s, &g.box[c], T));
+    for (int k = 0; k < 2; k ++) { TRY(dalloc(s, &g.keys[k], T)); TRY(dalloc(s, &g.vals[k], T)); }
+    TRY(dalloc(s, &g.hist, 256 * (size_t)pg_sort_blocks(T)));
+    TRY(dalloc(s, &g.cand, (size_t)g.kmax * T));
+    TRY(dalloc(s, &g.cnt, T));
+    TRY(dalloc(s, &g.off, (size_t)T + 1));
+    TRY(dalloc(s, &g.poff, (size_t)T + 1));
+    TRY(dalloc(s, &g.np_dev, 1));
+    TRY(dalloc(s, &g.pfirst, P));
+    TRY(dalloc(s, &g.plast, P));
+    for (int c = 0; c < 3; c ++) { TRY(dalloc(s, &d.ttF[c], P)); TRY(dalloc(s, &d.ttT[c], P)); }
+  }
+  release(s, g.cstart);
+  release(s, g.cend);
+  TRY(dalloc(s, &g.cstart, (size_t)g.ncells + 1));
+  TRY(dalloc(s, &g.cend, (size_t)g.ncells + 1));
+  TRY(h2d(s, g.big, big, T));
+  // no pairs carried into the first step
+  CK(cudaMemsetAsync(g.poff, 0, ((size_t)T + 1) * sizeof(int), s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  d.tt_on = 1;
+  return PG_OK;
+}
+
+int pg_session_mesh_contact_stats(pg_session *s, int *pairs, int *active)
+{
+  if (!s || !pairs || !active) return PG_ERR_ARGUMENT;
+  PgTT &g = s->tt;
+  *pairs = s->d.tt_on ? g.np_last : 0;
+  *active = 0;
+  if (*pairs > 0)
+  {
+    std::vector<unsigned char> a(*pairs);
+    TRY(d2h(s, a.data(), g.pact, a.size()));
+    CK(cudaStreamSynchronize(s->stream));
+    for (unsigned char v : a) *active += v ? 1 : 0;
+  }
+  return PG_OK;
+}
+
 int pg_session_critical(pg_session *s, int which, double *h, double *omega, double *ratio)
 {
   if (!s || (which != 0 && which != 1)) return PG_ERR_ARGUMENT;
@@ -1518,7 +1680,7 @@ int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, 
   if (!s || !tab || tab->nsteps < 0 || !(adaptive > 0.0 && adaptive <= 1.0) || !(step0 > 0.0))
     return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
-  if (d.form != PG_FORM_FP64 || d.nscene > 1 || s->exc_any) return PG_ERR_UNSUPPORTED;
+  if (d.form != PG_FORM_FP64 || d.nscene > 1 || s->exc_any || d.tt_on) return PG_ERR_UNSUPPORTED;
   const int n = tab->nsteps;
   if (n == 0) return PG_OK;
   TRY(ensure_tables(s, n));

@@ -161,6 +161,12 @@ struct PgDev
   int *ncode_new;
   float *tbox;              // [6][trinum] triangle AABBs at rebuild (float, widened)
 
+  // ---- mesh-mesh contact (extension, pg_meshcontact.cu): per-particle
+  // force and torque sums of this step's triangle contacts, added after
+  // gravity by the force sums when tt_on
+  int tt_on;
+  double *ttF[3], *ttT[3];
+
   // ---- independent scenes in one session (batching / serving pool)
   int nscene;
   int *pscene;              // [parnum] scene of each particle

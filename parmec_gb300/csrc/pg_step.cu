@@ -1220,6 +1220,12 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
     F[0] = F[0] + ma * grav[0];
     F[1] = F[1] + ma * grav[1];
     F[2] = F[2] + ma * grav[2];
+    if (d.tt_on)
+    {
+      // mesh-mesh contacts (pg_meshcontact.cu), summed per particle beforehand
+      F[0] = F[0] + d.ttF[0][i]; F[1] = F[1] + d.ttF[1][i]; F[2] = F[2] + d.ttF[2][i];
+      T[0] = T[0] + d.ttT[0][i]; T[1] = T[1] + d.ttT[1][i]; T[2] = T[2] + d.ttT[2][i];
+    }
 
     // spring force flushes, in the order a single springs_task applies them
     if (d.sprnum)

@@ -1,0 +1,282 @@
+// pg_tritri.cuh -- mesh-mesh contact between triangles (an extension: the
+// reference detects no contact between meshes, partition.ispc:600-646 and
+// condet.ispc:786).
+//
+// Each mesh triangle is swept by a sphere of radius r (a triangle of
+// thickness 2r).  Two triangles of different particles touch when their
+// distance d is below rA + rB: the contact point is the midpoint of their
+// closest points, the normal points from B's closest point to A's, and the
+// depth is rA + rB - d.  When the triangles intersect (d = 0) the normal is
+// B's face normal turned towards A's centroid and the depth rA + rB.
+//
+// The distance of two triangles that do not intersect is the smallest of
+// the six vertex-triangle and the nine edge-edge distances; an intersection
+// shows as an edge of one crossing the other.  Ties keep the first candidate
+// in that order, so the result is a function of the inputs alone.  The
+// functions are compiled for the device and for the CPU oracle (FP64 with no
+// contraction on both), which therefore evaluate the same operations.
+#pragma once
+#include <math.h>
+
+#ifdef __CUDACC__
+#define PG_TT __host__ __device__ __forceinline__
+#else
+#define PG_TT inline
+#endif
+
+namespace pgtt {
+
+PG_TT double dot(const double *a, const double *b) { return a[0]*b[0] + a[1]*b[1] + a[2]*b[2]; }
+PG_TT void sub(const double *a, const double *b, double *c) { c[0] = a[0]-b[0]; c[1] = a[1]-b[1]; c[2] = a[2]-b[2]; }
+PG_TT void cross(const double *a, const double *b, double *c)
+{
+  c[0] = a[1]*b[2] - a[2]*b[1];
+  c[1] = a[2]*b[0] - a[0]*b[2];
+  c[2] = a[0]*b[1] - a[1]*b[0];
+}
+PG_TT double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+// Closest point q of triangle (a, b, c) to p: the Voronoi-region method
+// (Ericson, Real-Time Collision Detection, 5.1.5).
+PG_TT void point_triangle(const double *p, const double *a, const double *b, const double *c, double *q)
+{
+  double ab[3], ac[3], ap[3];
+  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap);
+  const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0.0 && d2 <= 0.0) { q[0] = a[0]; q[1] = a[1]; q[2] = a[2]; return; }
+  double bp[3];
+  sub(p, b, bp);
+  const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0.0 && d4 <= d3) { q[0] = b[0]; q[1] = b[1]; q[2] = b[2]; return; }
+  const double vc = d1*d4 - d3*d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0)
+  {
+    const double v = d1 / (d1 - d3);
+    q[0] = a[0] + v*ab[0]; q[1] = a[1] + v*ab[1]; q[2] = a[2] + v*ab[2];
+    return;
+  }
+  double cp[3];
+  sub(p, c, cp);
+  const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0.0 && d5 <= d6) { q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; return; }
+  const double vb = d5*d2 - d1*d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0)
+  {
+    const double w = d2 / (d2 - d6);
+    q[0] = a[0] + w*ac[0]; q[1] = a[1] + w*ac[1]; q[2] = a[2] + w*ac[2];
+    return;
+  }
+  const double va = d3*d6 - d5*d4;
+  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
+  {
+    const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    q[0] = b[0] + w*(c[0]-b[0]); q[1] = b[1] + w*(c[1]-b[1]); q[2] = b[2] + w*(c[2]-b[2]);
+    return;
+  }
+  const double den = 1.0 / (va + vb + vc);
+  const double v = vb * den, w = vc * den;
+  q[0] = a[0] + ab[0]*v + ac[0]*w;
+  q[1] = a[1] + ab[1]*v + ac[1]*w;
+  q[2] = a[2] + ab[2]*v + ac[2]*w;
+}
+
+// Closest points c1 on p1q1 and c2 on p2q2 (Ericson 5.1.9); returns |c1-c2|^2.
+// Parallel segments take s = 0.
+PG_TT double segment_segment(const double *p1, const double *q1, const double *p2, const double *q2,
+                             double *c1, double *c2)
+{
+  double d1[3], d2[3], r[3];
+  sub(q1, p1, d1); sub(q2, p2, d2); sub(p1, p2, r);
+  const double a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+  double s, t;
+  if (a <= 0.0 && e <= 0.0) { s = 0.0; t = 0.0; }
+  else if (a <= 0.0) { s = 0.0; t = clamp01(f / e); }
+  else
+  {
+    const double c = dot(d1, r);
+    if (e <= 0.0) { t = 0.0; s = clamp01(-c / a); }
+    else
+    {
+      const double b = dot(d1, d2);
+      const double den = a*e - b*b;
+      s = den != 0.0 ? clamp01((b*f - c*e) / den) : 0.0;
+      t = (b*s + f) / e;
+      if (t < 0.0) { t = 0.0; s = clamp01(-c / a); }
+      else if (t > 1.0) { t = 1.0; s = clamp01((b - c) / a); }
+    }
+  }
+  c1[0] = p1[0] + d1[0]*s; c1[1] = p1[1] + d1[1]*s; c1[2] = p1[2] + d1[2]*s;
+  c2[0] = p2[0] + d2[0]*t; c2[1] = p2[1] + d2[1]*t; c2[2] = p2[2] + d2[2]*t;
+  double w[3];
+  sub(c1, c2, w);
+  return dot(w, w);
+}
+
+// Does segment pq cross triangle (a, b, c) through its interior or boundary?
+// The end points lie strictly on opposite sides of the plane and the
+// crossing point lies inside the triangle (same-side tests).  x: the point.
+PG_TT bool segment_crosses(const double *p, const double *q, const double *a, const double *b, const double *c,
+                           double *x)
+{
+  double ab[3], ac[3], n[3], ap[3], aq[3];
+  sub(b, a, ab); sub(c, a, ac);
+  cross(ab, ac, n);
+  sub(p, a, ap); sub(q, a, aq);
+  const double dp = dot(n, ap), dq = dot(n, aq);
+  if (!((dp > 0.0 && dq < 0.0) || (dp < 0.0 && dq > 0.0))) return false;
+  const double t = dp / (dp - dq);
+  x[0] = p[0] + (q[0]-p[0])*t; x[1] = p[1] + (q[1]-p[1])*t; x[2] = p[2] + (q[2]-p[2])*t;
+  const double *v[3] = {a, b, c};
+  for (int k = 0; k < 3; k ++)
+  {
+    double e[3], h[3], m[3];
+    sub(v[(k+1)%3], v[k], e);
+    sub(x, v[k], h);
+    cross(e, h, m);
+    if (dot(n, m) < 0.0) return false;
+  }
+  return true;
+}
+
+// Distance squared of triangles A (a[0..2]) and B (b[0..2]) with their
+// closest points pa on A and pb on B; returns 0 when they intersect (pa =
+// pb = the first crossing found).
+PG_TT double triangle_triangle(const double *const a[3], const double *const b[3], double *pa, double *pb)
+{
+  for (int i = 0; i < 3; i ++)
+  {
+    double x[3];
+    if (segment_crosses(a[i], a[(i+1)%3], b[0], b[1], b[2], x) ||
+        segment_crosses(b[i], b[(i+1)%3], a[0], a[1], a[2], x))
+    {
+      pa[0] = pb[0] = x[0]; pa[1] = pb[1] = x[1]; pa[2] = pb[2] = x[2];
+      return 0.0;
+    }
+  }
+  double best = 1.7976931348623157e308;
+  for (int i = 0; i < 3; i ++)
+  {
+    double q[3], w[3];
+    point_triangle(a[i], b[0], b[1], b[2], q);
+    sub(a[i], q, w);
+    const double d2 = dot(w, w);
+    if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = a[i][k]; pb[k] = q[k]; } }
+  }
+  for (int i = 0; i < 3; i ++)
+  {
+    double q[3], w[3];
+    point_triangle(b[i], a[0], a[1], a[2], q);
+    sub(q, b[i], w);
+    const double d2 = dot(w, w);
+    if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = q[k]; pb[k] = b[i][k]; } }
+  }
+  for (int i = 0; i < 3; i ++)
+    for (int j = 0; j < 3; j ++)
+    {
+      double c1[3], c2[3];
+      const double d2 = segment_segment(a[i], a[(i+1)%3], b[j], b[(j+1)%3], c1, c2);
+      if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = c1[k]; pb[k] = c2[k]; } }
+    }
+  return best;
+}
+
+// Are Q's vertices all farther than s from P's plane, on one side?  (The
+// plane normal is left unnormalised: distances are compared with s |n|.)
+PG_TT bool beyond_plane(const double *const P[3], const double *const Q[3], double s)
+{
+  double e1[3], e2[3], n[3];
+  sub(P[1], P[0], e1); sub(P[2], P[0], e2);
+  cross(e1, e2, n);
+  const double lim = s * sqrt(dot(n, n));
+  int above = 0, below = 0;
+  for (int k = 0; k < 3; k ++)
+  {
+    double w[3];
+    sub(Q[k], P[0], w);
+    const double h = dot(n, w);
+    above += h > lim ? 1 : 0;
+    below += h < -lim ? 1 : 0;
+  }
+  return above == 3 || below == 3;
+}
+
+// Contact of swept triangles A and B (radii ra, rb): returns the depth
+// (> 0: touching) with the point and the unit normal from B towards A.
+// Triangles with one wholly beyond the other's plane by ra + rb are apart:
+// depth -1, point and normal zero.
+PG_TT double contact(const double *const a[3], const double *const b[3], double ra, double rb,
+                     double *point, double *normal)
+{
+  if (beyond_plane(a, b, ra + rb) || beyond_plane(b, a, ra + rb))
+  {
+    point[0] = point[1] = point[2] = 0.0;
+    normal[0] = normal[1] = normal[2] = 0.0;
+    return -1.0;
+  }
+  double pa[3], pb[3];
+  const double d2 = triangle_triangle(a, b, pa, pb);
+  point[0] = 0.5*(pa[0]+pb[0]); point[1] = 0.5*(pa[1]+pb[1]); point[2] = 0.5*(pa[2]+pb[2]);
+  if (d2 > 0.0)
+  {
+    const double d = sqrt(d2);
+    const double id = 1.0 / d;
+    normal[0] = (pa[0]-pb[0])*id; normal[1] = (pa[1]-pb[1])*id; normal[2] = (pa[2]-pb[2])*id;
+    return (ra + rb) - d;
+  }
+  double e1[3], e2[3], n[3];
+  sub(b[1], b[0], e1); sub(b[2], b[0], e2);
+  cross(e1, e2, n);
+  const double ln = sqrt(dot(n, n));
+  const double il = ln > 0.0 ? 1.0 / ln : 0.0;
+  double ca[3], cb[3], w[3];
+  for (int k = 0; k < 3; k ++)
+  {
+    ca[k] = (a[0][k] + a[1][k] + a[2][k]) / 3.0;
+    cb[k] = (b[0][k] + b[1][k] + b[2][k]) / 3.0;
+  }
+  sub(ca, cb, w);
+  const double sg = dot(n, w) < 0.0 ? -il : il;
+  normal[0] = n[0]*sg; normal[1] = n[1]*sg; normal[2] = n[2]*sg;
+  return ra + rb;
+}
+
+// The granular contact law (forces.ispc:125-192) for normal n (from the
+// partner towards the master), relative velocity vij = v_partner - v_master,
+// depth, pair parameters and reduced mass: the force f on the master, and
+// the tangential spring state advanced by step * the tangential velocity.
+PG_TT void granular(double kn, double damper, double kskn, double mus, double mud, double ma,
+                    const double *n, const double *vij, double depth, double step, double *state, double *f)
+{
+  const double en = damper * 2.0 * sqrt(kn*ma);
+  const double vn = dot(vij, n);
+  const double fn = kn*depth + en*vn;
+  f[0] = fn*n[0];
+  f[1] = fn*n[1];
+  f[2] = fn*n[2];
+  const double kt = kn * kskn;
+  const double et = en * kskn;
+  double vt[3], ft[3];
+  vt[0] = vij[0] - vn*n[0];
+  vt[1] = vij[1] - vn*n[1];
+  vt[2] = vij[2] - vn*n[2];
+  state[0] += step*vt[0];
+  state[1] += step*vt[1];
+  state[2] += step*vt[2];
+  ft[0] = kt*state[0] + et*vt[0];
+  ft[1] = kt*state[1] + et*vt[1];
+  ft[2] = kt*state[2] + et*vt[2];
+  const double len = sqrt(dot(ft, ft));
+  double lim = mus*fn;
+  if (len > lim)
+  {
+    lim = mud*fn/len;
+    ft[0] *= lim;
+    ft[1] *= lim;
+    ft[2] *= lim;
+  }
+  f[0] += ft[0];
+  f[1] += ft[1];
+  f[2] += ft[2];
+}
+
+} // namespace pgtt

@@ -9,7 +9,7 @@ from . import abi
 def _counts(m):
     return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
             len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings), m.trqsprnum,
-            len(m.body_forces))
+            len(m.body_forces), getattr(m, "tt_radius", 0.0))
 
 
 class GpuEngine:
@@ -73,6 +73,11 @@ class GpuEngine:
         if self.capacity is not None:
             abi.check(self.lib.pg_session_set_capacity(self.sess, int(self.capacity[0]), int(self.capacity[1])),
                       "pg_session_set_capacity")
+        if getattr(m, "tt_radius", 0.0) > 0.0:
+            from .mesh import mesh_contact_grid
+            cell, big = mesh_contact_grid(m)
+            abi.check(self.lib.pg_session_mesh_contact(self.sess, m.tt_radius, cell, big.ctypes.data),
+                      "pg_session_mesh_contact")
         if self.fused:
             abi.check(self.lib.pg_session_use_fused(self.sess, 1), "pg_session_use_fused")
             if self.autotune:
@@ -107,6 +112,13 @@ class GpuEngine:
         abi.check(self.lib.pg_session_run_adaptive(self.sess, ctypes.byref(tab), step0, adaptive, abi.dptr(steps)),
                   "pg_session_run_adaptive")
         return steps[:tab.nsteps]
+
+    def mesh_contact_stats(self):
+        """(pairs, active pairs) of the last step's mesh-mesh contact stage."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        abi.check(self.lib.pg_session_mesh_contact_stats(self.sess, ctypes.byref(a), ctypes.byref(b)),
+                  "pg_session_mesh_contact_stats")
+        return a.value, b.value
 
     def critical(self, which):
         """CRITICAL on the device (pg_session_critical): which = 0 per particle

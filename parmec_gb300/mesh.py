@@ -363,3 +363,27 @@ def hex_grid(m, origins, a, material, color):
     P.flags[parts] = OUTREST
     m._touch()
     return parts
+
+
+def mesh_contact_grid(m):
+    """Grid cell and big-triangle flags of the mesh-mesh contact search
+    (pg_session_mesh_contact): a triangle's box, widened by the swept radius
+    r on each side, spans at most its longest edge + 2r along any axis
+    whatever its rotation; triangles up to 4 times the median of that bound
+    set the cell (the largest of them), longer ones are "big" and searched
+    against every triangle.  Returns (cell, big) with big a uint8 array over
+    all triangles (0 for obstacle triangles)."""
+    T = m.trinum
+    big = np.zeros(max(T, 1), dtype=np.uint8)
+    r = float(m.tt_radius)
+    own = m.Tr.triobs[:T] >= 0
+    if not np.any(own):
+        return 2.0 * r if r > 0.0 else 1.0, big
+    v = m.Tr.tri[:, :T].reshape(3, 3, T)
+    e = [np.sqrt(np.sum((v[a] - v[(a + 1) % 3]) ** 2, axis=0)) for a in range(3)]
+    ext = np.maximum(np.maximum(e[0], e[1]), e[2]) + 2.0 * r
+    med = float(np.median(ext[own]))
+    small = own & (ext <= 4.0 * med)
+    cell = float(np.max(ext[small]))
+    big[:T] = (own & ~small).astype(np.uint8)
+    return cell, big

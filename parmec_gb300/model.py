@@ -86,6 +86,7 @@ class Model:
                        "inertia": (9, f8), "inverse": (9, f8), "mass": (0, f8), "invm": (0, f8),
                        "force": (3, f8), "torque": (3, f8), "flags": (0, i4), "parmat": (0, i4)}, 256)
         self.E = _SoA({"center": (6, f8), "radii": (3, f8), "ellcol": (0, i4), "part": (0, i4)}, 256)
+        self.tt_radius = 0.0                  # mesh-mesh contact (mesh_contact); 0: off
         self.Tr = _SoA({"tri": (9, f8), "tricol": (0, i4), "triobs": (0, i4)}, 256)
         self.O = _SoA({"trirng": (2, i4), "obspnt": (3, f8), "obsang": (3, f8), "obslin": (3, f8)}, 16)
         self.N = _SoA({"nodes": (6, f8), "nodpart": (0, i4)}, 256)
@@ -705,6 +706,18 @@ class Model:
         return out
 
     # ------------------------------------------------------------- CRITICAL
+    def mesh_contact(self, radius):
+        """Mesh-mesh contact, an extension with no counterpart in the
+        reference (its contact detection holds spheres only, so MESH
+        particles meet spheres but never each other): every triangle of a
+        MESH particle is swept by a sphere of 'radius', and triangles of
+        different particles closer than 2 * radius touch, under the GRANULAR
+        law of their colours.  0 (the default) turns it off."""
+        r = float(radius)
+        if not (r >= 0.0) or r != r:
+            raise ValueError("'radius' must be non-negative")
+        self.tt_radius = r
+
     def critical(self, perspring=-1, perparticle=-1, engine=None):
         """CRITICAL (input.cpp:3034-3154): per-spring and per-particle critical
         step estimates.  perspring=N returns the N smallest spring steps as

@@ -222,14 +222,19 @@ def critical_spring_step(kmax, m_eff, emax):
     return (2.0 / w) * (math.sqrt(1.0 + ksi * ksi) - ksi)
 
 
-def spring_lattice(n_side=256, seed=2, edge=0.01, gap=0.002, density=2500.0):
+def spring_lattice(n_side=256, seed=2, edge=0.01, gap=0.002, density=2500.0, contact_radius=0.0):
     """Config 2, the spring-lattice shaking table: n_side x n_side rigid
     hexahedral MESH particles (12 triangles each) joined to their right and
     upper neighbours by SPRINGs with 8-point random monotone force-stroke
     curves (segment slopes in [1e4, 1e6] N/m) and lookup dashpots; each cube
     hangs on one more spring from a base plate MESH particle whose motion is a
     PRESCRIBEd acceleration 0.5 g sin(2 pi 5 t) along x.  Gravity -9.81 z.
-    Returns (model, dt) with dt = 0.1 of the critical spring step."""
+    contact_radius > 0 turns mesh-mesh contact on (Model.mesh_contact) with
+    GRANULAR spring 1e4 N/m per triangle pair, damping 0.2, friction 0.3
+    between the cubes and the plate: with the radius at half the gap, faces
+    touch as soon as a gap closes (a cube face meets its neighbour through
+    tens of triangle pairs, so the pair stiffness is kept low enough for the
+    springs' step).  Returns (model, dt) with dt = 0.1 of the critical spring step."""
     from .model import Model
     from . import mesh
     rng = np.random.default_rng(seed)
@@ -277,5 +282,8 @@ def spring_lattice(n_side=256, seed=2, edge=0.01, gap=0.002, density=2500.0):
     m.prescribe_motion(base, linear=lambda t: (0.5 * 9.81 * math.sin(2.0 * math.pi * 5.0 * t), 0.0, 0.0),
                        kind="av")
     m.set_gravity(0.0, 0.0, -9.81)
+    if contact_radius > 0.0:
+        m.granular(0, 0, 1e4, 0.2, 0.3)
+        m.mesh_contact(contact_radius)
     dt = 0.1 * critical_spring_step(kmax, 0.5 * m_cube, emax)
     return m, dt
