@@ -301,6 +301,14 @@ int pg_session_run_adaptive(pg_session *s, const pg_steptab *tab, double step0, 
  * stepping returns PG_ERR_UNSUPPORTED while it is on); steps with it run
  * without CUDA graphs. */
 int pg_session_mesh_contact(pg_session *s, double radius, double cell, const unsigned char *big);
+/* A pool's live extents: the steps cover particles [0, particles), spheres
+ * [0, spheres) and triangles [0, triangles) of the session's arrays, whose
+ * entries beyond are free (scene id -1).  A serving pool sized for its
+ * whole memory budget then costs per step what its admitted scenes hold.
+ * The values must not exceed the session's counts; the counts themselves
+ * restore the whole arrays.  The next step rebuilds the candidate lists. */
+int pg_session_set_live(pg_session *s, int particles, int spheres, int triangles);
+
 /* Triangle pairs whose boxes overlapped in the last step, and those in contact. */
 int pg_session_mesh_contact_stats(pg_session *s, int *pairs, int *active);
 

@@ -160,6 +160,7 @@ def load_library():
         "pg_session_critical": (ctypes.c_int, [P, ctypes.c_int, D, D, D]),
         "pg_session_mesh_contact": (ctypes.c_int, [P, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
         "pg_session_mesh_contact_stats": (ctypes.c_int, [P, I, I]),
+        "pg_session_set_live": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "pg_session_download_particles": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_download_springs": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I, ctypes.c_int]),
         "pg_session_sync": (ctypes.c_int, [P]),

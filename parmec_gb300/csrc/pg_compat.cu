@@ -222,6 +222,7 @@ bool restart_lists(int P, int E, int T)
 {
   PgDev &d = G.d;
   d.parnum = P; d.ellnum = E; d.trinum = T;
+  d.estride = E;
   d.sbits = pg_rebuild_entry_bits(P);
   bool ok = zeros(d.ncnt, E) && zeros(d.rcnt, P) && grow(d.soff, (size_t)P + 1) && grow(d.eorder, E) &&
             grow(d.eoff, (size_t)E + 1) && grow(d.smeta, 4) && grow(d.gbar, 4) && slot_arrays(0);
@@ -580,6 +581,7 @@ void condet(int, partitioning *tree, master_conpnt master[], int parnum, int ell
   if (restart && !restart_lists(parnum, ellnum, T)) return;
   G.owner = master;
   d.parnum = parnum; d.ellnum = ellnum; d.trinum = T;
+  d.estride = ellnum;
   bool ok = true;
   for (int k = 0; ok && k < 3; k ++) ok = up(d.center[k], center[k], ellnum);
   std::vector<int> ord(ellnum);

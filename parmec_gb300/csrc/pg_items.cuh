@@ -542,7 +542,7 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i, bool valid
   const bool mixed = d.form == PG_FORM_MIXED;
   for (int k = 0; k < nold; k ++)
   {
-    size_t idx = (size_t)k * E + i;
+    size_t idx = (size_t)k * d.estride + i;
     ocode[k] = d.ncode[idx];
     oflag[k] = d.nflag[idx];
     for (int c = 0; c < 3; c ++) ost[c][k] = mixed ? (double)d.nstate_f[c][idx] : d.nstate[c][idx];
@@ -552,7 +552,7 @@ __device__ __forceinline__ void rb_verlet_item(const PgDev &d, int i, bool valid
   {
     unsigned key = order_key(codes[k]);
     while (o < nold && order_key(ocode[o]) < key) o ++;
-    size_t idx = (size_t)k * E + i;
+    size_t idx = (size_t)k * d.estride + i;
     d.ncode[idx] = codes[k];
     if (d.nen) d.nen[idx] = pair_en(d, i, codes[k]);
     const bool kept = o < nold && ocode[o] == codes[k];
@@ -585,11 +585,11 @@ __device__ __forceinline__ void rb_emit_item(const PgDev &d, int q)
   const int base = d.eoff[q];
   for (int k = 0; k < n; k ++)
   {
-    const int code = d.ncode[(size_t)k * E + i];
+    const int code = d.ncode[(size_t)k * d.estride + i];
     const int pj = code >= 0 ? d.part[code] : d.triobs[-code - 1];
     const bool ok = pj >= 0 && pj < P;
     d.skey[0][base + k] = ok ? (unsigned)pj : 0xffffffffu;
-    d.sval[0][base + k] = k * E + i;
+    d.sval[0][base + k] = k * d.estride + i;
     if (ok) atomicAdd(&d.rcnt[pj], 1);
   }
 }

@@ -258,10 +258,10 @@ __device__ __forceinline__ bool mx_contacts_item(const PgDev &d, int i, double s
     // triangles of the threads of a warp are evaluated together
     int k0 = 0;
     if (PASS == MX_TRIANGLES)
-      while (k0 < cnt && d.ncode[(size_t)k0 * E + i] >= 0) k0 ++;
+      while (k0 < cnt && d.ncode[(size_t)k0 * d.estride + i] >= 0) k0 ++;
     for (int k = k0; k < cnt; k ++)
     {
-      const size_t idx = (size_t)k * E + i;
+      const size_t idx = (size_t)k * d.estride + i;
       const int code = d.ncode[idx];
       if (PASS == MX_SPHERES && code < 0) { more = true; break; }
       const bool existing = d.nflag[idx] != 0;

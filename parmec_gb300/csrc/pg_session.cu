@@ -48,6 +48,9 @@ struct pg_session
   int adapt_ready = 0, hrec_cap = 0, sbig_ad_cap = 0;
   // mesh-mesh contact (pg_meshcontact.cu); steps then run without graphs
   PgTT tt;
+  // a pool's live extents (pg_session_set_live): the steps cover particles,
+  // spheres and triangles below them; 0: the whole arrays
+  int plive = 0, elive = 0, tlive = 0;
   // CRITICAL: per-spring slope and damping, and the per-item outputs
   double *crit_ke = nullptr, *crit_h = nullptr, *crit_o = nullptr, *crit_r = nullptr;
   int exc_any = 0;                         // some scene has a device excitation
@@ -908,11 +911,13 @@ void drop_graph(pg_session *s)
 // replay when capture works, else as direct cooperative launches
 // kernels one fused step launches: the gated centre conversion and rebuild
 // (with spheres), then the fused step kernel
+PgDev live_view(const pg_session *s);
+
 static int fused_kernels_per_step(const PgDev &d) { return d.ellnum ? 3 : 1; }
 
 int run_fused(pg_session *s, double step, int n, int chunk)
 {
-  const PgDev &d = s->d;
+  const PgDev d = live_view(s);
   if (n <= 0) return PG_OK;
   if (s->use_graph && s->fgraph_ok && n >= chunk)
   {
@@ -982,7 +987,7 @@ int run_fused_steps(pg_session *s, double step, int n)
     if (!s->warmed && done < n)
     {
       // an untimed step: the first rebuild and cold caches
-      CK(pg_launch_fused_mx(s->d, s->stream, step, 1, s->cands[0]));
+      CK(pg_launch_fused_mx(live_view(s), s->stream, step, 1, s->cands[0]));
       s->fused_launches += fused_kernels_per_step(s->d);
       done += 1;
       s->warmed = 1;
@@ -995,7 +1000,7 @@ int run_fused_steps(pg_session *s, double step, int n)
     {
       const PgFusedCfg &c = s->cands[s->cand_next];
       CK(cudaEventRecord(e0, s->stream));
-      CK(pg_launch_fused_mx(s->d, s->stream, step, trial, c));
+      CK(pg_launch_fused_mx(live_view(s), s->stream, step, trial, c));
       CK(cudaEventRecord(e1, s->stream));
       s->fused_launches += (long long)trial * fused_kernels_per_step(s->d) - 1;
       CK(cudaEventSynchronize(e1));
@@ -1026,9 +1031,24 @@ int run_fused_steps(pg_session *s, double step, int n)
 
 int tt_stage(pg_session *s, double step);
 
+// the view the step kernels get: the whole arrays, or a pool's live extents
+// (the slot arrays keep their stride, d.estride)
+PgDev live_view(const pg_session *s)
+{
+  PgDev v = s->d;
+  if (s->plive > 0 || s->elive > 0 || s->tlive > 0)
+  {
+    v.parnum = s->plive;
+    v.ellnum = s->elive;
+    v.trinum = s->tlive;
+    v.nsortblocks = pg_sort_blocks(s->elive);
+  }
+  return v;
+}
+
 void enqueue_step(pg_session *s, double step)
 {
-  const PgDev &d = s->d;
+  const PgDev d = live_view(s);
   if (d.form == PG_FORM_MIXED) pg_launch_mx_centres(d, s->stream);
   pg_launch_rebuild(d, s->stream);
   pg_launch_excite(d, s->stream, step);
@@ -1271,6 +1291,7 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   int r = PG_OK;
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return PG_ERR_CUDA; }
   d.parnum = sc->parnum; d.ellnum = sc->ellnum; d.trinum = sc->trinum; d.obsnum = sc->obsnum;
+  d.estride = d.ellnum;
   d.nodnum = sc->nodnum; d.facnum = sc->facnum; d.sprnum = sc->sprnum; d.pairnum = sc->pairnum;
   d.prsnum = sc->prsnum; d.compat = sc->compat; d.form = form;
   d.nscene = sc->nscene > 0 ? sc->nscene : 1;
@@ -1401,6 +1422,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   else
   {
     // groups: 0 rebuild, 1 contacts, 2 springs, 3 integrate, 4 mesh, 5 obstacles + tail
+    const PgDev d = live_view(s);
     const int G = 6;
     s->ring.resize((size_t)n * (G + 1));
     for (auto &e : s->ring) if (!e) CK(cudaEventCreate(&e));
@@ -1621,6 +1643,36 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
   CK(cudaMemsetAsync(g.poff, 0, ((size_t)T + 1) * sizeof(int), s->stream));
   CK(cudaStreamSynchronize(s->stream));
   d.tt_on = 1;
+  return PG_OK;
+}
+
+int pg_session_set_live(pg_session *s, int particles, int spheres, int triangles)
+{
+  if (!s) return PG_ERR_ARGUMENT;
+  PgDev &d = s->d;
+  if (particles < 0 || spheres < 0 || triangles < 0 || particles > d.parnum || spheres > d.ellnum ||
+      triangles > d.trinum)
+    return PG_ERR_ARGUMENT;
+  const bool whole = particles == d.parnum && spheres == d.ellnum && triangles == d.trinum;
+  const int e_now = s->elive > 0 ? s->elive : d.ellnum;
+  drop_graph(s);
+  if (s->fgraph_exec) { cudaGraphExecDestroy(s->fgraph_exec); s->fgraph_exec = nullptr; }
+  if (s->fgraph) { cudaGraphDestroy(s->fgraph); s->fgraph = nullptr; }
+  CK(cudaStreamSynchronize(s->stream));
+  // a rebuild clears the cells of the spheres it sorted last time: cells
+  // of spheres beyond a smaller extent would keep stale ranges, so the whole
+  // cell table starts empty
+  if (spheres < e_now && s->ncells)
+  {
+    CK(cudaMemsetAsync(d.cstart, 0, s->ncells * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(d.cend, 0, s->ncells * sizeof(int), s->stream));
+  }
+  s->plive = whole ? 0 : particles;
+  s->elive = whole ? 0 : spheres;
+  s->tlive = whole ? 0 : triangles;
+  int one = 1;
+  TRY(h2d(s, d.rebuild, &one, 1));
+  CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
 

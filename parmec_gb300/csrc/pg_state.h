@@ -113,6 +113,8 @@ struct PgDev
 
   // ---- contact candidates (Verlet lists), master side, slot-major
   int kn;                   // slots per sphere
+  int estride;              // sphere stride of the slot-major arrays ([slot][estride]); the sphere
+                            // capacity, which a pool's live view keeps while its ellnum shrinks
   int *ncnt;                // [ellnum]
   int *ncode;               // [kn][ellnum]: sphere j >= 0, or -(triangle+1)
   unsigned char *nflag;     // [kn][ellnum]: contact active

@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
 
     for (int k = 0; k < cnt; k ++)
     {
-      const size_t idx = (size_t)k * E + i;
+      const size_t idx = (size_t)k * d.estride + i;
       const int code = d.ncode[idx];
       const bool existing = d.nflag[idx] != 0;
       // Geometry in two stages: the squared distance first; a candidate
@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double 
           kact[0] += fabs(u[0]);
           kact[1] += fabs(u[1]);
           kact[2] += fabs(u[2]);
-          const int ms = ref % E, code = d.ncode[ref];
+          const int ms = ref % d.estride, code = d.ncode[ref];
           const int ij = pairing(d, d.ellcol[ms], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
           const double kc = d.iparam[0][ij];
           double ec;
@@ -1881,7 +1881,7 @@ __global__ void __launch_bounds__(TPB) k_crit_perparticle(PgDev d, const double 
       const double c[3] = {d.center[0][e], d.center[1][e], d.center[2][e]};
       for (int k = 0; k < d.ncnt[e]; k ++)
       {
-        const size_t idx = (size_t)k * E + e;
+        const size_t idx = (size_t)k * d.estride + e;
         if (!d.nflag[idx]) continue;
         const int code = d.ncode[idx];
         const double pnt[3] = {d.npnt[0][idx], d.npnt[1][idx], d.npnt[2][idx]};
@@ -1930,7 +1930,7 @@ __global__ void __launch_bounds__(TPB) k_crit_perparticle(PgDev d, const double 
       kact[0] += fabs(u[0]);
       kact[1] += fabs(u[1]);
       kact[2] += fabs(u[2]);
-      const int ms = ref % E, code = d.ncode[ref];
+      const int ms = ref % d.estride, code = d.ncode[ref];
       const int ij = pairing(d, d.ellcol[ms], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
       const double kc = d.iparam[0][ij];
       const double ec = d.iparam[1][ij] * 2.0 * sqrt(kc*(1.0 / (d.invm[d.part[ms]] + d.invm[i])));

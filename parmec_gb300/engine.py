@@ -9,7 +9,7 @@ from . import abi
 def _counts(m):
     return (m.parnum, m.ellnum, m.trinum, m.obsnum, m.nodnum, m.facnum, m.sprnum,
             len(m.prescribe), len(m.pairs), len(m.lcurves), len(m.restraints), len(m.unsprings), m.trqsprnum,
-            len(m.body_forces), getattr(m, "tt_radius", 0.0))
+            len(m.body_forces), getattr(m, "tt_radius", 0.0), m.ellcon, m.tricon, m.faccon)
 
 
 class GpuEngine:
@@ -112,6 +112,11 @@ class GpuEngine:
         abi.check(self.lib.pg_session_run_adaptive(self.sess, ctypes.byref(tab), step0, adaptive, abi.dptr(steps)),
                   "pg_session_run_adaptive")
         return steps[:tab.nsteps]
+
+    def set_live(self, particles, spheres, triangles):
+        """A pool's live extents (pg_session_set_live)."""
+        abi.check(self.lib.pg_session_set_live(self.sess, int(particles), int(spheres), int(triangles)),
+                  "pg_session_set_live")
 
     def mesh_contact_stats(self):
         """(pairs, active pairs) of the last step's mesh-mesh contact stage."""

@@ -101,6 +101,10 @@ class Model:
                        "refpnt": (3, f8), "cone": (0, i4), "tsprid": (0, i4), "tsprmap": (0, i4)}, 16)
         self.parnum = self.ellnum = self.trinum = self.obsnum = 0
         self.nodnum = self.facnum = self.sprnum = self.trqsprnum = 0
+        # spheres, mesh faces and triangles of analytical particles sit in
+        # front of the arrays, out of contact detection and the shape
+        # updates (ellcon, faccon, tricon, parmec.cpp:87-93, 1401-1592)
+        self.ellcon = self.faccon = self.tricon = 0
         self.krpy_tab, self.drpy_tab = [], []   # per torsion spring: three (angle|rate, torque) tables
         self.torsion_changed = False
         self.mparam = []                    # [density, young, poisson]
@@ -313,6 +317,7 @@ class Model:
         else:
             if particle >= self.parnum:
                 raise ValueError("Particle index is out of range")
+            self.declare_analytical(particle)
             i = particle
             if position is not None:
                 P.position[0:3, i] = vpos
@@ -326,6 +331,63 @@ class Model:
                 set_inertia(i)
         P.flags[i] = ANALYTICAL_FLAG | OUTREST
         return i
+
+    def declare_analytical(self, k):
+        """declare_analytical (parmec.cpp:1585-1592): particle k's spheres, or
+        if it has none its mesh faces and their triangles, leave contact
+        detection and the shape updates.  They move in front of the ranges
+        the engines see (ellcon, faccon, tricon grow), the others keeping
+        their order; obstacle triangle ranges and face-triangle indices follow
+        the moved triangles.  The reference's shuffles swap every earlier
+        entry with one fixed position and include one entry of the preceding
+        particle in the range (parmec.cpp:1419-1423, 1515-1519), and its
+        triangle swap leaves factri and the obstacles' triangle ranges
+        pointing at the old positions (parmec.cpp:1541-1577); here the
+        entries are moved as a stable partition instead."""
+        k = int(k)
+        if not (0 <= k < self.parnum):
+            raise ValueError("Particle index is out of range")
+        self._touch()
+        c, n = self.ellcon, self.ellnum
+        part = self.E.part[c:n]
+        sel = np.nonzero(part == k)[0]
+        if len(sel):
+            order = np.concatenate([sel, np.nonzero(part != k)[0]]) + c
+            for name in self.E.spec:
+                a = getattr(self.E, name)
+                a[..., c:n] = a[..., order]
+            self.ellcon += len(sel)
+            return
+        f0, nf = self.faccon, self.facnum
+        if nf <= f0:
+            return
+        owner = self.N.nodpart[self.F.facnod[0, f0:nf]]
+        fsel = np.nonzero(owner == k)[0]
+        if not len(fsel):
+            return
+        forder = np.concatenate([fsel, np.nonzero(owner != k)[0]]) + f0
+        for name in self.F.spec:
+            a = getattr(self.F, name)
+            a[..., f0:nf] = a[..., forder]
+        t0, nt = self.tricon, self.trinum
+        moved = self.F.factri[f0:f0 + len(fsel)].astype(np.int64)
+        mask = np.zeros(nt, dtype=bool)
+        mask[moved] = True
+        rest = np.nonzero(~mask[t0:nt])[0] + t0
+        torder = np.concatenate([moved, rest])
+        where = np.arange(nt, dtype=np.int64)              # old index -> new index
+        where[torder] = np.arange(t0, nt)
+        for name in self.Tr.spec:
+            a = getattr(self.Tr, name)
+            a[..., t0:nt] = a[..., torder]
+        self.F.factri[:nf] = where[self.F.factri[:nf]]
+        for o in range(self.obsnum):
+            b, e = int(self.O.trirng[0, o]), int(self.O.trirng[1, o])
+            if e > b:
+                self.O.trirng[0, o] = where[b]
+                self.O.trirng[1, o] = where[e - 1] + 1
+        self.tricon += len(moved)
+        self.faccon += len(fsel)
 
     # ---------------------------------------------------------------- MESH
     def mesh(self, nodes, elements, material, colors):
@@ -796,19 +858,22 @@ class Model:
         s.torque = abi.rows(P.torque, 3)
         s.flags = abi.iptr(P.flags)
         s.parmat = abi.iptr(P.parmat)
-        s.ellnum = self.ellnum
-        s.center = abi.rows(E.center, 6)
-        s.radii = abi.rows(E.radii, 3)
-        s.ellcol = abi.iptr(E.ellcol)
-        s.part = abi.iptr(E.part)
-        s.trinum = self.trinum
+        # the engines see the spheres, triangles and faces from the contact
+        # offsets on (parmec.cpp:2353-2357 passes icenter = center + ellcon)
+        ec, tc, fc = self.ellcon, self.tricon, self.faccon
+        s.ellnum = self.ellnum - ec
+        s.center = abi.rows(E.center[:, ec:], 6)
+        s.radii = abi.rows(E.radii[:, ec:], 3)
+        s.ellcol = abi.iptr(E.ellcol[ec:])
+        s.part = abi.iptr(E.part[ec:])
+        s.trinum = self.trinum - tc
         for v in range(3):
             for d in range(3):
-                s.tri[v][d] = Tr.tri[3 * v + d].ctypes.data_as(abi.D)
-        s.tricol = abi.iptr(Tr.tricol)
-        s.triobs = abi.iptr(Tr.triobs)
+                s.tri[v][d] = Tr.tri[3 * v + d, tc:].ctypes.data_as(abi.D)
+        s.tricol = abi.iptr(Tr.tricol[tc:])
+        s.triobs = abi.iptr(Tr.triobs[tc:])
         s.obsnum = self.obsnum
-        trirng = np.ascontiguousarray(O.trirng.T.reshape(-1)[:2 * max(1, O.cap)])
+        trirng = np.ascontiguousarray(O.trirng.T.reshape(-1)[:2 * max(1, O.cap)] - tc)
         obspnt = np.ascontiguousarray(O.obspnt.T.reshape(-1))
         obsang = np.ascontiguousarray(O.obsang.T.reshape(-1))
         obslin = np.ascontiguousarray(O.obslin.T.reshape(-1))
@@ -829,9 +894,11 @@ class Model:
         s.nodnum = self.nodnum
         s.nodes = abi.rows(N.nodes, 6)
         s.nodpart = abi.iptr(N.nodpart)
-        s.facnum = self.facnum
-        s.facnod = abi.rows(F.facnod, 3, abi.I)
-        s.factri = abi.iptr(F.factri)
+        s.facnum = self.facnum - fc
+        s.facnod = abi.rows(F.facnod[:, fc:], 3, abi.I)
+        factri = np.ascontiguousarray(F.factri[fc:] - tc) if tc else F.factri[fc:]
+        keep.append(factri)
+        s.factri = abi.iptr(factri)
         s.sprnum = self.sprnum
         tabs = spring_tables(self)
         keep.append(tabs)

@@ -142,6 +142,8 @@ class Server:
         self.slots = list(range(max_scenes))
         self.active = {}         # scene slot -> (request, ranges, remaining, admitted)
         self._zero_tab = None
+        self._live = None
+        self._update_live()
 
     @staticmethod
     def _empty_pool(template, cap, tcap, nscene):
@@ -216,6 +218,20 @@ class Server:
         self.slots.append(slot)
         return pos, lin
 
+    LIVE_QUANTUM = 4096
+
+    def _update_live(self):
+        """Steps cover the pool up to the end of its last allocated range
+        (rounded up), not its whole capacity (pg_session_set_live)."""
+        def top(r, cap):
+            end = r.free[-1][0] if r.free and r.free[-1][1] == cap else cap
+            q = self.LIVE_QUANTUM
+            return min(cap, ((end + q - 1) // q) * q)
+        e, t = top(self.spheres, self.cap), top(self.tris, self.tcap)
+        if (e, t) != self._live:
+            self.eng.set_live(e, e, t)
+            self._live = (e, t)
+
     # ---------------------------------------------------------------- loop
     def _tab(self, n):
         from .driver import StepTables
@@ -273,6 +289,7 @@ class Server:
                     break
                 pending.pop(0)
                 self.active[slot] = (req, r, req.steps, now())
+            self._update_live()
             if not self.active:
                 if pending and realtime:
                     time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
@@ -289,6 +306,7 @@ class Server:
                     pos, lin = self._unload(slot)
                     results.append(Result(req.rid, req.arrival, adm, now(), req.steps, r[1] - r[0], pos, lin,
                                           energy=self.last_energy))
+            self._update_live()
             in_use = self.cap - sum(e - b for b, e in self.spheres.free)
             peak_spheres = max(peak_spheres, in_use)
             peak_scenes = max(peak_scenes, len(self.active))
