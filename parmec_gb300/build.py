@@ -49,6 +49,29 @@ def build(verbose=False, extra=()):
     lib = os.path.join(OUT, "libparmec_gb300.so")
     cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
     subprocess.run(cmd, check=True)
+    if build_coupling() is None:
+        sys.stderr.write("note: libparmec_gb300_coupling.so not built (Python headers or library missing)\n")
+    return lib
+
+
+def build_coupling():
+    """libparmec_gb300_coupling.so: the C library interface (pg_coupling.cpp,
+    include/parmec_coupling.h), linked against this interpreter's libpython.
+    Returns the path, or None when the Python headers or library are absent."""
+    import sysconfig
+    inc = sysconfig.get_paths().get("include")
+    libdir = sysconfig.get_config_var("LIBDIR")
+    ver = sysconfig.get_config_var("LDVERSION") or sysconfig.get_config_var("VERSION")
+    if not inc or not os.path.exists(os.path.join(inc, "Python.h")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    lib = os.path.join(OUT, "libparmec_gb300_coupling.so")
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", inc, os.path.join(CSRC, "pg_coupling.cpp"),
+           "-o", lib, "-L", libdir, "-Wl,-rpath," + libdir, "-lpython" + ver, "-ldl"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout[-3000:])
+        return None
     return lib
 
 

@@ -204,7 +204,8 @@ bool slot_arrays(size_t keep_slots)
   PgDev &d = G.d;
   const size_t E = std::max(d.ellnum, 1), P = std::max(d.parnum, 1);
   const size_t n = (size_t)d.kn * E;
-  bool ok = grow_keep(d.ncode, n, keep_slots) && grow_keep(d.nflag, n, keep_slots) && grow_keep(d.ndep, n, keep_slots);
+  bool ok = grow_keep(d.ncode, n, keep_slots) && grow_keep(d.nflag, n, keep_slots) && grow_keep(d.ndep, n, keep_slots) &&
+            grow(d.cwork, n) && grow(d.cwork_n, 1);
   for (int k = 0; ok && k < 3; k ++)
     ok = grow_keep(d.nstate[k], n, keep_slots) && grow_keep(d.nfrc[k], n, keep_slots) &&
          grow_keep(d.npnt[k], n, keep_slots) && grow_keep(d.nnrm[k], n, keep_slots);

@@ -731,6 +731,8 @@ int slot_buffers(pg_session *s)
     }
     TRY(dalloc(s, &d.ndep, slots));
     TRY(dalloc(s, &d.nen, slots));
+    TRY(dalloc(s, &d.cwork, slots));
+    TRY(dalloc(s, &d.cwork_n, 1));
   }
   else
   {
@@ -757,7 +759,9 @@ void release_slot_buffers(pg_session *s)
 {
   PgDev &d = s->d;
   release(s, d.ncode); release(s, d.nflag); release(s, d.ndep); release(s, d.nen);
+  release(s, d.cwork); release(s, d.cwork_n);
   d.ncode = nullptr; d.nflag = nullptr; d.ndep = nullptr; d.nen = nullptr; d.rref = nullptr;
+  d.cwork = nullptr; d.cwork_n = nullptr;
   for (int k = 0; k < 2; k ++) { release(s, d.skey[k]); release(s, d.sval[k]); d.skey[k] = nullptr; d.sval[k] = nullptr; }
   release(s, d.shist); release(s, d.sbs); d.shist = nullptr; d.sbs = nullptr;
   for (int k = 0; k < 3; k ++)

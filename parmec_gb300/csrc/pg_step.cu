@@ -505,6 +505,339 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
   }
 }
 
+// ---------------------------------------------------------------- contacts in three passes
+// The same evaluation as k_contacts, split so that the FP64 work runs on
+// full warps: one thread per sphere walks a list whose active contacts sit
+// at different slots, so its warp's FP64 instructions ran with a fraction of
+// the lanes.
+//   k_contacts_probe  one thread per sphere: the squared-distance test of
+//                     every sphere candidate; a candidate clearly apart is
+//                     settled there (an existing contact ends), every other
+//                     slot goes to the work queue (one atomic per warp);
+//   k_contacts_eval   one thread per queued slot (a grid-stride loop over
+//                     the queue): geometry, the creation/persistence rule,
+//                     contact velocities and the granular law, written to
+//                     the slot;
+//   k_contacts_sum    one thread per sphere: the master-side force, torque
+//                     and (adaptive) stiffness sums over its slots in slot
+//                     order, as k_contacts sums them.
+// Every slot takes the same operations as in k_contacts and the sums the
+// same order, so the results are the same bits; the queue's order plays no
+// part.
+__device__ __forceinline__ void queue_push(int *work, int *count, bool push, int idx)
+{
+  const unsigned m = __ballot_sync(__activemask(), push);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(__activemask(), base, leader);
+  if (push) work[base + __popc(m & ((1u << lane) - 1u))] = idx;
+}
+
+__global__ void __launch_bounds__(TPB) k_contacts_probe(PgDev d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = i < d.ellnum ? d.ncnt[i] : 0;
+  double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
+  if (cnt > 0)
+  {
+    c[0] = d.center[0][i]; c[1] = d.center[1][i]; c[2] = d.center[2][i];
+    ri = d.radii[0][i];
+  }
+  // every lane of the warp takes part in each round's vote
+  int kmax = cnt;
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    const int other = __shfl_xor_sync(0xffffffffu, kmax, o);
+    kmax = other > kmax ? other : kmax;
+  }
+  for (int k = 0; k < kmax; k ++)
+  {
+    bool push = false;
+    size_t idx = 0;
+    if (k < cnt)
+    {
+      idx = (size_t)k * d.estride + i;
+      const int code = d.ncode[idx];
+      push = true;
+      if (code >= 0)
+      {
+        double q[3];
+        q[0] = c[0]-d.center[0][code];
+        q[1] = c[1]-d.center[1][code];
+        q[2] = c[2]-d.center[2][code];
+        const double d2 = dot3(q, q);
+        const double sr = ri+d.radii[0][code];
+        if (d2 > (sr*sr) * (1.0 + 1e-12))
+        {
+          push = false;
+          if (d.nflag[idx])
+          {
+            d.nflag[idx] = 0;
+            d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+          }
+        }
+      }
+    }
+    queue_push(d.cwork, d.cwork_n, push, (int)idx);
+  }
+}
+
+template <bool GEOM, bool ADAPT>
+__global__ void __launch_bounds__(TPB) k_contacts_eval(PgDev d, double step)
+{
+  if (ADAPT) step = d.hs[0];
+  const int n = *d.cwork_n;
+  const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+  {
+    const int idx0 = d.cwork[w];
+    const size_t idx = (size_t)idx0;
+    const int i = idx0 % d.estride;
+    const int pi = d.part[i];
+    double x[3], v[3], oi[3], c[3];
+    for (int k = 0; k < 3; k ++)
+    {
+      x[k] = d.position[k][pi];
+      v[k] = d.linear[k][pi];
+      oi[k] = d.angular[3+k][pi];
+      c[k] = d.center[k][i];
+    }
+    const double ri = d.radii[0][i];
+    const int coli = d.ellcol[i];
+    const double invmi = d.invm[pi], massi = d.mass[pi];
+    const int code = d.ncode[idx];
+    const bool existing = d.nflag[idx] != 0;
+    double point[3], normal[3], depth = 0.0, q[3], len = 0.0;
+    int pj, colj;
+    bool apart;
+    bool sphere = code >= 0;
+    double cj[3];
+    if (sphere)
+    {
+      const int j = code;
+      pj = d.part[j];
+      colj = d.ellcol[j];
+      cj[0] = d.center[0][j]; cj[1] = d.center[1][j]; cj[2] = d.center[2][j];
+      q[0] = c[0]-cj[0];
+      q[1] = c[1]-cj[1];
+      q[2] = c[2]-cj[2];
+      const double d2 = dot3(q, q);
+      const double sr = ri+d.radii[0][j];
+      apart = d2 > (sr*sr) * (1.0 + 1e-12);
+      if (!apart)
+      {
+        len = sqrt(d2);
+        depth = sr - len;
+      }
+    }
+    else
+    {
+      const int t = -code-1;
+      double A[3], B[3], C[3];
+      for (int kk = 0; kk < 3; kk ++) { A[kk] = d.tri[kk][t]; B[kk] = d.tri[3+kk][t]; C[kk] = d.tri[6+kk][t]; }
+      triangle_closest(A, B, C, c, point, (d.compat & PG_COMPAT_TRIEDGE) != 0);
+      q[0] = c[0]-point[0];
+      q[1] = c[1]-point[1];
+      q[2] = c[2]-point[2];
+      const double d2 = dot3(q, q);
+      apart = d2 > (ri*ri) * (1.0 + 1e-12);
+      if (!apart)
+      {
+        len = sqrt(d2);
+        depth = ri - len;
+      }
+      pj = d.triobs[t];
+      colj = d.tricol[t];
+    }
+    const bool active = !apart && (existing ? !(depth < 0.0) : (depth > 0.0));
+    if (!active)
+    {
+      if (existing)
+      {
+        d.nflag[idx] = 0;
+        d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+      }
+      continue;
+    }
+    if (sphere)
+    {
+      double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
+      point[0] = 0.5*(c[0]+cj[0]);
+      point[1] = 0.5*(c[1]+cj[1]);
+      point[2] = 0.5*(c[2]+cj[2]);
+      normal[0] = ilen*q[0];
+      normal[1] = ilen*q[1];
+      normal[2] = ilen*q[2];
+    }
+    else
+    {
+      double ilen = 1.0/len;
+      normal[0] = ilen*q[0];
+      normal[1] = ilen*q[1];
+      normal[2] = ilen*q[2];
+    }
+
+    // contact point velocities (forces.ispc:226-279)
+    double z[3], vi[3], vj[3], oj[3], vij[3];
+    z[0] = point[0]-x[0]; z[1] = point[1]-x[1]; z[2] = point[2]-x[2];
+    vi[0] = oi[1]*z[2]-oi[2]*z[1] + v[0];
+    vi[1] = oi[2]*z[0]-oi[0]*z[2] + v[1];
+    vi[2] = oi[0]*z[1]-oi[1]*z[0] + v[2];
+    if (pj >= 0)
+    {
+      z[0] = point[0]-d.position[0][pj];
+      z[1] = point[1]-d.position[1][pj];
+      z[2] = point[2]-d.position[2][pj];
+      oj[0] = d.angular[3][pj]; oj[1] = d.angular[4][pj]; oj[2] = d.angular[5][pj];
+      vj[0] = oj[1]*z[2]-oj[2]*z[1] + d.linear[0][pj];
+      vj[1] = oj[2]*z[0]-oj[0]*z[2] + d.linear[1][pj];
+      vj[2] = oj[0]*z[1]-oj[1]*z[0] + d.linear[2][pj];
+    }
+    else
+    {
+      int l = -pj-2;
+      if (obsc && l >= 0) l = l+1;
+      if (l >= 0 && l < d.obsnum)
+      {
+        z[0] = point[0]-d.obspnt[3*l];
+        z[1] = point[1]-d.obspnt[3*l+1];
+        z[2] = point[2]-d.obspnt[3*l+2];
+        oj[0] = d.obsang[3*l]; oj[1] = d.obsang[3*l+1]; oj[2] = d.obsang[3*l+2];
+        vj[0] = oj[1]*z[2]-oj[2]*z[1] + d.obslin[3*l];
+        vj[1] = oj[2]*z[0]-oj[0]*z[2] + d.obslin[3*l+1];
+        vj[2] = oj[0]*z[1]-oj[1]*z[0] + d.obslin[3*l+2];
+      }
+      else
+      {
+        vj[0] = vj[1] = vj[2] = 0.0;
+      }
+    }
+    vij[0] = vj[0] - vi[0];
+    vij[1] = vj[1] - vi[1];
+    vij[2] = vj[2] - vi[2];
+
+    const int ij = pairing(d, coli, colj);
+    if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED, 4, i, ij);
+
+    // granular force (forces.ispc:125-192)
+    double state[3];
+    if (existing) { state[0] = d.nstate[0][idx]; state[1] = d.nstate[1][idx]; state[2] = d.nstate[2][idx]; }
+    else { state[0] = 0.0; state[1] = 0.0; state[2] = 0.0; }
+    double kn = d.iparam[0][ij];
+    double en;
+    if (d.nen) en = d.nen[idx];
+    else
+    {
+      double ma = pj >= 0 ? 1.0 / (invmi + d.invm[pj]) : massi;
+      en = d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+    }
+    double vn = dot3(vij, normal);
+    double fn = kn*depth + en*vn;
+    double f[3];
+    f[0] = fn*normal[0];
+    f[1] = fn*normal[1];
+    f[2] = fn*normal[2];
+    double kskn = d.iparam[6][ij];
+    double kt = kn * kskn;
+    double et = en * kskn;
+    double mus = d.iparam[2][ij];
+    double mud = d.iparam[3][ij];
+    double vt[3], ft[3];
+    vt[0] = vij[0] - vn*normal[0];
+    vt[1] = vij[1] - vn*normal[1];
+    vt[2] = vij[2] - vn*normal[2];
+    state[0] += step*vt[0];
+    state[1] += step*vt[1];
+    state[2] += step*vt[2];
+    ft[0] = kt*state[0] + et*vt[0];
+    ft[1] = kt*state[1] + et*vt[1];
+    ft[2] = kt*state[2] + et*vt[2];
+    double flen = sqrt(dot3(ft, ft));
+    double lim = mus*fn;
+    if (flen > lim)
+    {
+      lim = mud*fn/flen;
+      ft[0] *= lim;
+      ft[1] *= lim;
+      ft[2] *= lim;
+    }
+    f[0] += ft[0];
+    f[1] += ft[1];
+    f[2] += ft[2];
+
+    d.nflag[idx] = 1;
+    d.nstate[0][idx] = state[0]; d.nstate[1][idx] = state[1]; d.nstate[2][idx] = state[2];
+    d.nfrc[0][idx] = f[0]; d.nfrc[1][idx] = f[1]; d.nfrc[2][idx] = f[2];
+    d.npnt[0][idx] = point[0]; d.npnt[1][idx] = point[1]; d.npnt[2][idx] = point[2];
+    if (GEOM || ADAPT)
+    {
+      d.nnrm[0][idx] = normal[0]; d.nnrm[1][idx] = normal[1]; d.nnrm[2][idx] = normal[2];
+    }
+    if (GEOM) d.ndep[idx] = depth;
+  }
+}
+
+template <bool ADAPT>
+__global__ void __launch_bounds__(TPB) k_contacts_sum(PgDev d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ellnum) return;
+  const int pi = d.part[i];
+  const int cnt = d.ncnt[i];
+  double fs[3] = {0.0, 0.0, 0.0}, ts[3] = {0.0, 0.0, 0.0};
+  double kact0[3] = {0.0, 0.0, 0.0}, krot0[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, kmax0 = 0.0, emax0 = 0.0;
+  if (cnt > 0)
+  {
+    const double x[3] = {d.position[0][pi], d.position[1][pi], d.position[2][pi]};
+    double L[9];
+    if (ADAPT) for (int k = 0; k < 9; k ++) L[k] = d.rotation[k][pi];
+    for (int k = 0; k < cnt; k ++)
+    {
+      const size_t idx = (size_t)k * d.estride + i;
+      if (!d.nflag[idx]) continue;
+      const double f[3] = {d.nfrc[0][idx], d.nfrc[1][idx], d.nfrc[2][idx]};
+      const double a[3] = {d.npnt[0][idx]-x[0], d.npnt[1][idx]-x[1], d.npnt[2][idx]-x[2]};
+      fs[0] += f[0]; fs[1] += f[1]; fs[2] += f[2];
+      ts[0] += a[1]*f[2] - a[2]*f[1];
+      ts[1] += a[2]*f[0] - a[0]*f[2];
+      ts[2] += a[0]*f[1] - a[1]*f[0];
+      if (ADAPT)
+      {
+        const int code = d.ncode[idx];
+        const int pj = code >= 0 ? d.part[code] : d.triobs[-code-1];
+        const int ij = pairing(d, d.ellcol[i], code >= 0 ? d.ellcol[code] : d.tricol[-code-1]);
+        const double kn = d.iparam[0][ij];
+        double en;
+        if (d.nen) en = d.nen[idx];
+        else
+        {
+          double ma = pj >= 0 ? 1.0 / (d.invm[pi] + d.invm[pj]) : d.mass[pi];
+          en = d.iparam[1][ij] * 2.0 * sqrt(kn*ma);
+        }
+        kact0[0] += fabs(d.nnrm[0][idx]);
+        kact0[1] += fabs(d.nnrm[1][idx]);
+        kact0[2] += fabs(d.nnrm[2][idx]);
+        kmax0 = kn > kmax0 ? kn : kmax0;
+        emax0 = en > emax0 ? en : emax0;
+        double A[3];
+        nvmul(L, a, A);
+        krot_add(krot0, A);
+      }
+    }
+  }
+  d.fm[0][pi] = fs[0]; d.fm[1][pi] = fs[1]; d.fm[2][pi] = fs[2];
+  d.tm[0][pi] = ts[0]; d.tm[1][pi] = ts[1]; d.tm[2][pi] = ts[2];
+  if (ADAPT)
+  {
+    for (int k = 0; k < 3; k ++) d.akact[k][pi] = kact0[k];
+    for (int k = 0; k < 6; k ++) d.akrot[k][pi] = krot0[k];
+    d.akmax[pi] = kmax0;
+    d.aemax[pi] = emax0;
+  }
+}
+
 // ---------------------------------------------------------------- springs (forces.ispc:641-1412)
 __device__ double look_up(const double *t0, const double *t1, int lo, int hi, double arg, double *slope)
 {
@@ -2052,9 +2385,44 @@ void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step)
   if (d.obsnum) k_tail<<<1, 32, 0, s>>>(d, step, 0);
 }
 
+// the grid of the queue pass: resident blocks over every SM
+static int eval_blocks()
+{
+  static int nb = 0;
+  if (!nb)
+  {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_contacts_eval<false, false>, TPB, 0);
+    nb = (sms > 0 ? sms : 152) * (per > 0 ? per : 8);
+  }
+  return nb;
+}
+
 void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
 {
   if (!d.ellnum) return;
+  if (d.cwork && d.cwork_n)
+  {
+    // three passes (probe, queued evaluation, sums): the same bits as k_contacts
+    cudaMemsetAsync(d.cwork_n, 0, sizeof(int), s);
+    k_contacts_probe<<<nblk(d.ellnum), TPB, 0, s>>>(d);
+    const int nb = eval_blocks();
+    if (d.hs)
+    {
+      if (d.record_geometry) k_contacts_eval<true, true><<<nb, TPB, 0, s>>>(d, step);
+      else k_contacts_eval<false, true><<<nb, TPB, 0, s>>>(d, step);
+      k_contacts_sum<true><<<nblk(d.ellnum), TPB, 0, s>>>(d);
+    }
+    else
+    {
+      if (d.record_geometry) k_contacts_eval<true, false><<<nb, TPB, 0, s>>>(d, step);
+      else k_contacts_eval<false, false><<<nb, TPB, 0, s>>>(d, step);
+      k_contacts_sum<false><<<nblk(d.ellnum), TPB, 0, s>>>(d);
+    }
+    return;
+  }
   if (d.hs)
   {
     if (d.record_geometry) k_contacts<true, true><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
@@ -2064,12 +2432,13 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   else k_contacts<false, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
 }
 
-// the FP64 form evaluates each list in one pass; the mixed form in a sphere
-// and a triangle pass (pg_mixed.cu)
+// the FP64 form evaluates the lists in three passes (one when no work queue
+// is allocated); the mixed form in a sphere and a triangle pass (pg_mixed.cu)
 int pg_contacts_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
-  return d.form == PG_FORM_MIXED ? 2 : 1;
+  if (d.form == PG_FORM_MIXED) return 2;
+  return (d.cwork && d.cwork_n) ? 3 : 1;
 }
 
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)

@@ -99,7 +99,7 @@ def bytes_per_sphere(form, kn=32, kr=32):
         state += 4 * (6 + 6 + 18 + 6 + 2 + 2 + 18 + 6 + 6 + 6 + 2 + 3)
         slots = kn * (4 + 1 + 12 + 12 + 12)
     else:
-        slots = kn * (4 + 1 + 24 + 24 + 24 + 24 + 8)
+        slots = kn * (4 + 1 + 24 + 24 + 24 + 24 + 8 + 8 + 4)
     return state + slots + kn * 16 + 16
 
 
