@@ -276,10 +276,11 @@ def spring_lattice_form(args, n_side):
     """Config 2: the spring-lattice shaking table, n_side^2 MESH cubes (12
     triangles each), 2 n (n-1) neighbour springs and n^2 base springs with
     8-point curves and lookup dashpots, prescribed base acceleration; plain
-    FP64.  Run twice: with mesh-mesh contact (triangles swept by 1 mm, half
-    the gap: the cubes touch the plate and their neighbours; the reference
-    has no contact between meshes), and with springs alone as the reference
-    computes it."""
+    FP64.  Run twice: with springs alone, as the reference computes it (the
+    leg's headline), and with mesh-mesh contact on (triangles swept by 1 mm,
+    half the gap: every cube touches the plate and its neighbours, so the
+    contact work is that of a packed lattice; the reference has no contact
+    between meshes)."""
     import torch
     from parmec_gb300 import driver
     from parmec_gb300.engine import GpuEngine
@@ -327,7 +328,8 @@ def spring_lattice_form(args, n_side):
         eng.close()
     out["workload"] = (f"{n_side}x{n_side} MESH hexahedra (10 mm), {out['springs']} springs, {out['triangles']} "
                        "triangles, base 0.5 g sin(2 pi 5 t) along x, FP64")
-    head = out["with_mesh_contact"]
+    # the headline is the reference's computation (springs, no contact between meshes)
+    head = out["springs_only"]
     out.update({"value": head["value"], "unit": "particle-steps/s", "ms_per_step": head["ms_per_step"],
                 "steps": head["steps"]})
     return out

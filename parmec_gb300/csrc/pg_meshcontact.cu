@@ -100,30 +100,31 @@ __global__ void __launch_bounds__(TPB) k_tt_ranges(PgTT g, int n)
 }
 
 // 3. partners found by triangle t, sorted by index, in cand[slot][t]
+// (sorted in a thread-local array, written once)
 __global__ void __launch_bounds__(TPB) k_tt_find(PgDev d, PgTT g)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= d.trinum) return;
   int cnt = 0;
+  int loc[PG_TT_KMAX];
   if (mesh_tri(d, t))
   {
     const int owner = d.triobs[t];
     const bool big = g.big[t] != 0;
+    double lo[3], hi[3];
+    for (int c = 0; c < 3; c ++) { lo[c] = g.box[c][t]; hi[c] = g.box[3+c][t]; }
     auto take = [&](int u) {
       if (u == t || !mesh_tri(d, u) || d.triobs[u] == owner) return;
       const bool ubig = g.big[u] != 0;
       if (big && !ubig) return;                       // found from the small side
       if (big == ubig && u < t) return;               // found by the lower index
-      if (!boxes_overlap(g, t, u)) return;
+      for (int c = 0; c < 3; c ++)
+        if (!(lo[c] < g.box[3+c][u] && g.box[c][u] < hi[c])) return;
       if (cnt >= g.kmax) { pgk::set_err(d, PG_ERR_CAPACITY, 40, t, cnt); return; }
       // insertion in index order
       int k = cnt ++;
-      while (k > 0 && g.cand[(size_t)(k-1) * d.trinum + t] > u)
-      {
-        g.cand[(size_t)k * d.trinum + t] = g.cand[(size_t)(k-1) * d.trinum + t];
-        k --;
-      }
-      g.cand[(size_t)k * d.trinum + t] = u;
+      while (k > 0 && loc[k-1] > u) { loc[k] = loc[k-1]; k --; }
+      loc[k] = u;
     };
     if (!big)
     {
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(TPB) k_tt_find(PgDev d, PgTT g)
     }
     for (int k = g.cstart[g.ncells]; k < g.cend[g.ncells]; k ++) take(g.vals[0][k]);
   }
+  for (int k = 0; k < cnt; k ++) g.cand[(size_t)k * d.trinum + t] = loc[k];
   g.cnt[t] = cnt;
 }
 

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include "pg_state.h"
 
+#define PG_TT_KMAX 64             // partners one triangle may find (the search's thread-local list)
+
 struct PgTT
 {
   double r = 0.0;                 // swept radius of every mesh triangle
@@ -12,7 +14,7 @@ struct PgTT
   int dim[3] = {1, 1, 1}, ncells = 1;
   unsigned none = 0, enone = 0;   // sentinel keys (above every cell / particle)
   int passes = 2, epasses = 2;    // radix-sort passes of the two sorts
-  int kmax = 64;                  // partners one triangle may find
+  int kmax = PG_TT_KMAX;          // partners one triangle may find
   unsigned char *big = nullptr;   // [trinum] 1: larger than a cell
   double *box[6] = {};            // [trinum] box widened by r: min xyz, max xyz
   unsigned *keys[2] = {}; int *vals[2] = {}; unsigned *hist = nullptr;
