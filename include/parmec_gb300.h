@@ -261,8 +261,16 @@ int pg_session_first_half_step(pg_session *s, double step,
 int pg_session_invert_inertia(pg_session *s);
 
 /* Advance tab->nsteps steps of the loop body of dem() (parmec.cpp:2418-2517)
- * with a fixed step (adaptive == 0).  Asynchronous on the session stream. */
+ * with a fixed step (adaptive == 0); returns once the steps finished. */
 int pg_session_run(pg_session *s, const pg_steptab *tab, double step);
+
+/* pg_session_run without the final wait: the steps are enqueued on the
+ * session stream and the call returns (no counterpart in the reference, whose
+ * dem() is synchronous).  'tab' is consumed before the call returns.  The
+ * host may prepare its next uploads meanwhile; pg_session_sync waits for the
+ * steps.  Sessions with mesh contact on, or stepped by the fused kernel,
+ * still read a count back inside the call. */
+int pg_session_run_async(pg_session *s, const pg_steptab *tab, double step);
 
 /* Copy the state of particles idx[0..n) (velocities, rotation, position,
  * force, torque) or of springs idx[0..n) (sorted positions: current points,

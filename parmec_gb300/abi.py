@@ -155,6 +155,7 @@ def load_library():
         "pg_session_first_half_step": (ctypes.c_int, [P, ctypes.c_double, D, D]),
         "pg_session_invert_inertia": (ctypes.c_int, [P]),
         "pg_session_run": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double]),
+        "pg_session_run_async": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double]),
         "pg_session_run_adaptive": (ctypes.c_int, [P, ctypes.POINTER(PgStepTab), ctypes.c_double, ctypes.c_double, D]),
         "pg_session_restrain_velocities": (ctypes.c_int, [P]),
         "pg_session_critical": (ctypes.c_int, [P, ctypes.c_int, D, D, D]),

@@ -1396,7 +1396,17 @@ int pg_session_first_half_step(pg_session *s, double step, const double *obs_ang
   return PG_OK;
 }
 
-int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
+static int run_steps(pg_session *s, const pg_steptab *tab, double step, bool wait);
+
+int pg_session_run(pg_session *s, const pg_steptab *tab, double step) { return run_steps(s, tab, step, true); }
+
+int pg_session_run_async(pg_session *s, const pg_steptab *tab, double step) { return run_steps(s, tab, step, false); }
+
+// enqueue tab->nsteps steps; with 'wait' return once they finished.  The
+// step tables are copied to the device before the first launch (the copies
+// from pageable memory are staged by the driver before the call returns), so
+// the host tables may change as soon as this returns.
+static int run_steps(pg_session *s, const pg_steptab *tab, double step, bool wait)
 {
   if (!s || !tab || tab->nsteps < 0) return PG_ERR_ARGUMENT;
   PgDev &d = s->d;
@@ -1410,7 +1420,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
     TRY(run_fused_steps(s, step, n));
     s->launches += s->fused_launches - before;
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s->stream));
+    if (wait) CK(cudaStreamSynchronize(s->stream));
     return PG_OK;
   }
   const int per_step = pg_rebuild_kernel_count(d) + pg_step_kernel_count(d) + (d.form == PG_FORM_MIXED ? 1 : 0);
@@ -1476,8 +1486,7 @@ int pg_session_run(pg_session *s, const pg_steptab *tab, double step)
   }
   s->launches += (long long)per_step * n;
   CK(cudaGetLastError());
-  // the host tables are pageable: keep them alive until the copies finished
-  CK(cudaStreamSynchronize(s->stream));
+  if (wait) CK(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
 

@@ -1243,7 +1243,7 @@ __device__ __forceinline__ int run_chunk(int len)
 __global__ void __launch_bounds__(RUN_GROUP) k_spring_run_groups(PgDev d)
 {
   const unsigned full = 0xffffffffu;
-  const int run = blockIdx.y, g = blockIdx.x, lane = threadIdx.x;
+  const int run = blockIdx.x, g = blockIdx.y, lane = threadIdx.x;
   const int4 v = d.sbig[run];
   const int type = v.x & 1, off = type == 0 ? 3 : 6;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
@@ -1322,7 +1322,7 @@ __global__ void k_spring_run_totals(PgDev d)
 __global__ void __launch_bounds__(RUN_GROUP) k_spring_run_groups_adapt(PgDev d)
 {
   const unsigned full = 0xffffffffu;
-  const int run = blockIdx.y, g = blockIdx.x, lane = threadIdx.x;
+  const int run = blockIdx.x, g = blockIdx.y, lane = threadIdx.x;
   const int4 v = d.sbig[run];
   const int type = v.x & 1, off = type == 0 ? 5 : 11;
   const int len = v.z - v.y, ch = run_chunk(len), nc = (len + ch - 1) / ch;
@@ -2466,7 +2466,7 @@ void pg_launch_unspring(const PgDev &d, cudaStream_t s)
 void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
 {
   if (!(d.sprnum && d.nbig > 0)) return;
-  const dim3 grid(RUN_GROUPS, d.nbig);
+  const dim3 grid(d.nbig, RUN_GROUPS);      // runs on x: no 65,535 limit on their count
   const int tb = (d.nbig + 127) / 128;
   k_spring_run_groups<<<grid, RUN_GROUP, 0, s>>>(d);
   k_spring_run_totals<<<tb, 128, 0, s>>>(d);

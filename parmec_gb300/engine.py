@@ -106,6 +106,10 @@ class GpuEngine:
     def run(self, tab, step):
         abi.check(self.lib.pg_session_run(self.sess, ctypes.byref(tab), step), "pg_session_run")
 
+    def run_async(self, tab, step):
+        """Enqueue the steps and return (pg_session_run_async); sync() waits for them."""
+        abi.check(self.lib.pg_session_run_async(self.sess, ctypes.byref(tab), step), "pg_session_run_async")
+
     def run_adaptive(self, tab, step0, adaptive):
         """tab.nsteps adaptive steps from step0 (pg_session_run_adaptive); returns each step's step1."""
         steps = np.zeros(max(1, tab.nsteps))

@@ -8,7 +8,10 @@ excitation.  Requests are admitted, in arrival order, as soon as a scene slot
 and room in the pool (sized from an HBM budget) are free; all admitted scenes
 advance together, one launch per kernel per step, so their work overlaps on
 the device.  When a request's steps are done its state is read back, its
-ranges are freed and a waiting request can take them.
+ranges are freed and a waiting request can take them.  While a chunk of
+steps runs (pg_session_run_async), the host copies requests that have
+arrived into free ranges of the pool's host arrays; they are uploaded and
+switched on after the chunk.
 
 A scene's arithmetic does not depend on the other scenes in the pool, so a
 request's result is bitwise the same alone and in the mix
@@ -173,7 +176,10 @@ class Server:
         return P
 
     # ---------------------------------------------------------------- load
-    def _load(self, req, slot):
+    def _stage(self, req):
+        """Take pool ranges for a request and copy its scene into the pool's
+        host arrays: no device work, so this runs while a chunk of steps is
+        in flight.  Returns the ranges, or None when the pool has no room."""
         m = req.model
         n, nt = m.parnum, m.trinum
         if m.ellnum != n or m.obsnum or m.sprnum or m.prescribe:
@@ -193,12 +199,23 @@ class Server:
         P.E.part[e0:e0 + n] = np.arange(e0, e0 + n, dtype=np.int32)
         for name in P.Tr.spec:
             getattr(P.Tr, name)[..., t0:t0 + nt] = getattr(m.Tr, name)[..., :nt]
-        P.pscene[e0:e0 + n] = slot
-        P.tscene[t0:t0 + nt] = slot
-        r = (e0, e0 + n, e0, e0 + n, t0, t0 + nt, 0, 0)
+        return (e0, e0 + n, e0, e0 + n, t0, t0 + nt, 0, 0)
+
+    def _commit(self, req, slot, r):
+        """Upload a staged request's ranges and switch its scene on (no step
+        is in flight)."""
+        m = req.model
+        e0, e1, _, _, t0, t1, _, _ = r
+        self.P.pscene[e0:e1] = slot
+        self.P.tscene[t0:t1] = slot
         self.eng.upload_range(r)
-        lo = m.E.center[0:3, :n].min(axis=1)
+        lo = m.E.center[0:3, :m.parnum].min(axis=1)
         self.eng.set_scene(slot, True, origin=lo - 4.0 * self.cell, excitation=req.excitation, start=-1)
+
+    def _load(self, req, slot):
+        r = self._stage(req)
+        if r is not None:
+            self._commit(req, slot, r)
         return r
 
     def _unload(self, slot):
@@ -278,7 +295,14 @@ class Server:
         steps_done = 0
         psteps = 0
         peak_spheres = peak_scenes = 0
-        while pending or self.active:
+        staged = []                # (request, ranges): in the pool's host arrays, not yet on the device
+        while pending or self.active or staged:
+            # no step is in flight here: commit what was staged during the last chunk
+            for req, r in staged:
+                slot = self.slots.pop(0)
+                self._commit(req, slot, r)
+                self.active[slot] = (req, r, req.steps, now())
+            staged = []
             # admit in arrival order while there is room
             while pending and (not realtime or pending[0].arrival <= now()) and self.slots:
                 req = pending[0]
@@ -295,7 +319,15 @@ class Server:
                     time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
                 continue
             c = min(self.chunk, min(v[2] for v in self.active.values()))
-            self.eng.run(self._tab(c), self.dt)
+            self.eng.run_async(self._tab(c), self.dt)
+            # while the chunk runs, copy arrived requests into free ranges of
+            # the host arrays; they go to the device after the wait
+            while pending and (not realtime or pending[0].arrival <= now()) and len(staged) < len(self.slots):
+                r = self._stage(pending[0])
+                if r is None:
+                    break
+                staged.append((pending.pop(0), r))
+            self.eng.sync()
             steps_done += c
             for slot in list(self.active):
                 req, r, rem, adm = self.active[slot]
@@ -306,10 +338,9 @@ class Server:
                     pos, lin = self._unload(slot)
                     results.append(Result(req.rid, req.arrival, adm, now(), req.steps, r[1] - r[0], pos, lin,
                                           energy=self.last_energy))
-            self._update_live()
             in_use = self.cap - sum(e - b for b, e in self.spheres.free)
             peak_spheres = max(peak_spheres, in_use)
-            peak_scenes = max(peak_scenes, len(self.active))
+            peak_scenes = max(peak_scenes, len(self.active) + len(staged))
         wall = now()
         ok = [x for x in results if x.error is None]
         lat = np.array([x.latency for x in ok])
