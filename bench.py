@@ -149,8 +149,9 @@ def reference_cpu(n_spheres, threads, steps, warmup=1):
     return m.parnum * steps / el, kind, sample
 
 
-def cpu_baseline(n_spheres, threads, steps=3):
-    """The reference's CPU hot path on a bounded sample of the same drum."""
+def cpu_baseline(n_spheres, threads, steps=60):
+    """The reference's CPU hot path on a bounded sample of the same drum
+    (60 steps: about 10 s on 16 cores)."""
     v, kind, sample = reference_cpu(n_spheres, threads, steps)
     return {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind, "sample": sample}
 
