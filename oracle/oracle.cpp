@@ -2164,8 +2164,9 @@ namespace {
  * Each pair's contact and granular force, with its tangential state from
  * the previous step's pair (finder, partner); then per particle the entries
  * (+f for the finder's particle, -f for the partner's) in pair order, summed
- * by 32 strided lanes from zero and the lane sums added in lane order, and
- * added to the force and torque after gravity. */
+ * in chunks of 1,024 entries (PG_TT_CHUNK): in a chunk by 32 strided lanes
+ * from zero and the lane sums added in lane order, then the chunk sums in
+ * chunk order from zero; added to the force and torque after gravity. */
 int tt_pair_finder(const or_ctx *ctx, const pg_scene *s, int t, int u, const std::vector<double> &box)
 {
   if (u == t || s->triobs[u] < 0 || s->triobs[u] == s->triobs[t]) return 0;
@@ -2258,12 +2259,17 @@ void tt_all(or_ctx *ctx, pg_scene *s, double step)
   for (int p = 0; p < P; p ++)
   {
     if (ent[p].empty()) continue;
-    double part[32][6];
     const double x[3] = {s->position[0][p], s->position[1][p], s->position[2][p]};
+    const size_t ne = ent[p].size(), chunk = 1024;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (size_t b = 0; b < ne; b += chunk)
+    {
+    const size_t e = std::min(ne, b + chunk);
+    double part[32][6];
     for (int L = 0; L < 32; L ++)
     {
       double a6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-      for (size_t q = L; q < ent[p].size(); q += 32)
+      for (size_t q = b + L; q < e; q += 32)
       {
         const int v = ent[p][q], k = v >> 1;
         double f[3] = {fr[3*(size_t)k], fr[3*(size_t)k + 1], fr[3*(size_t)k + 2]};
@@ -2276,9 +2282,11 @@ void tt_all(or_ctx *ctx, pg_scene *s, double step)
       }
       for (int c = 0; c < 6; c ++) part[L][c] = a6[c];
     }
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double csum[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int L = 0; L < 32; L ++)
-      for (int c = 0; c < 6; c ++) acc[c] += part[L][c];
+      for (int c = 0; c < 6; c ++) csum[c] += part[L][c];
+    for (int c = 0; c < 6; c ++) acc[c] += csum[c];
+    }
     for (int c = 0; c < 3; c ++)
     {
       s->force[c][p] = s->force[c][p] + acc[c];

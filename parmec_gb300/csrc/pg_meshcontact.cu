@@ -20,9 +20,13 @@
 //      the previous step's pair list by (finder, partner);
 //   6. the force of each active pair goes to its two particles (+f to the
 //      finder's, -f to the partner's): the entries are sorted by particle
-//      (stably, so in pair order) and one warp per particle sums them, lane
-//      L taking entries L, L+32, ... from zero and the 32 lane sums added in
-//      lane order.  k_integrate adds these sums after gravity.
+//      (stably, so in pair order) and summed per particle in chunks of
+//      PG_TT_CHUNK entries: one warp per chunk, lane L taking entries L,
+//      L+32, ... of the chunk from zero and the 32 lane sums added in lane
+//      order; then the chunk sums in chunk order from zero, one thread per
+//      particle.  A particle with many contacts (a base plate under a whole
+//      lattice) spreads over many warps.  k_integrate adds these sums after
+//      gravity.
 // The CPU oracle restates the same definitions with a brute-force search.
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -267,38 +271,74 @@ __global__ void __launch_bounds__(TPB) k_tt_segments(PgTT g, int n)
   if (k == n-1 || g.ekeys[0][k+1] != key) g.plast[key] = k + 1;
 }
 
-// 6c. one warp per particle: lane sums over entries lane, lane+32, ...,
-// then the lane sums in lane order
-__global__ void __launch_bounds__(TPB) k_tt_sums(PgDev d, PgTT g)
+// 6c. chunks per particle
+__global__ void __launch_bounds__(TPB) k_tt_chunks(PgDev d, PgTT g)
 {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= d.parnum) return;
-  const int b = g.pfirst[w], e = g.plast[w];
-  double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  const double x[3] = {d.position[0][w], d.position[1][w], d.position[2][w]};
-  for (int q = b + lane; q < e; q += 32)
+  g.nch[w] = (g.plast[w] - g.pfirst[w] + PG_TT_CHUNK - 1) / PG_TT_CHUNK;
+}
+
+// 6d. one warp per chunk: lane sums over entries lane, lane+32, ... of the
+// chunk, then the lane sums in lane order
+__global__ void __launch_bounds__(TPB) k_tt_chunk_sums(PgDev d, PgTT g)
+{
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const bool on = c < *g.nchunks;
+  int w = 0;
+  if (on)
   {
-    const int v = g.evals[0][q];
-    const int k = v >> 1;
-    double f[3] = {g.f[0][k], g.f[1][k], g.f[2][k]};
-    if (v & 1) { f[0] = -f[0]; f[1] = -f[1]; f[2] = -f[2]; }
-    const double a[3] = {g.p[0][k]-x[0], g.p[1][k]-x[1], g.p[2][k]-x[2]};
-    s[0] += f[0]; s[1] += f[1]; s[2] += f[2];
-    s[3] += a[1]*f[2] - a[2]*f[1];
-    s[4] += a[2]*f[0] - a[0]*f[2];
-    s[5] += a[0]*f[1] - a[1]*f[0];
+    // the particle whose chunks hold c: the last w with choff[w] <= c
+    int lo = 0, hi = d.parnum - 1;
+    while (lo < hi)
+    {
+      const int mid = (lo + hi + 1) >> 1;
+      if (g.choff[mid] <= c) lo = mid;
+      else hi = mid - 1;
+    }
+    w = lo;
+  }
+  double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (on)
+  {
+    const int b = g.pfirst[w] + (c - g.choff[w]) * PG_TT_CHUNK;
+    const int e = min(b + PG_TT_CHUNK, g.plast[w]);
+    const double x[3] = {d.position[0][w], d.position[1][w], d.position[2][w]};
+    for (int q = b + lane; q < e; q += 32)
+    {
+      const int v = g.evals[0][q];
+      const int k = v >> 1;
+      double f[3] = {g.f[0][k], g.f[1][k], g.f[2][k]};
+      if (v & 1) { f[0] = -f[0]; f[1] = -f[1]; f[2] = -f[2]; }
+      const double a[3] = {g.p[0][k]-x[0], g.p[1][k]-x[1], g.p[2][k]-x[2]};
+      s[0] += f[0]; s[1] += f[1]; s[2] += f[2];
+      s[3] += a[1]*f[2] - a[2]*f[1];
+      s[4] += a[2]*f[0] - a[0]*f[2];
+      s[5] += a[0]*f[1] - a[1]*f[0];
+    }
   }
   __shared__ double part[TPB / 32][32][6];
   const int wl = threadIdx.x >> 5;
-  for (int c = 0; c < 6; c ++) part[wl][lane][c] = s[c];
+  for (int k = 0; k < 6; k ++) part[wl][lane][k] = s[k];
   __syncwarp();
-  if (lane == 0)
+  if (on && lane == 0)
   {
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int L = 0; L < 32; L ++)
-      for (int c = 0; c < 6; c ++) acc[c] += part[wl][L][c];
-    for (int c = 0; c < 3; c ++) { d.ttF[c][w] = acc[c]; d.ttT[c][w] = acc[3+c]; }
+      for (int k = 0; k < 6; k ++) acc[k] += part[wl][L][k];
+    for (int k = 0; k < 6; k ++) g.csum[k][c] = acc[k];
   }
+}
+
+// 6e. one thread per particle: its chunk sums in chunk order
+__global__ void __launch_bounds__(TPB) k_tt_sums(PgDev d, PgTT g)
+{
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= d.parnum) return;
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int c = g.choff[w]; c < g.choff[w+1]; c ++)
+    for (int k = 0; k < 6; k ++) acc[k] += g.csum[k][c];
+  for (int k = 0; k < 3; k ++) { d.ttF[k][w] = acc[k]; d.ttT[k][w] = acc[3+k]; }
 }
 
 } // namespace
@@ -336,11 +376,21 @@ void pg_tt_forces(const PgDev &d, PgTT &g, cudaStream_t s, int np, double step)
   cudaMemsetAsync(g.pfirst, 0, (size_t)d.parnum * sizeof(int), s);
   cudaMemsetAsync(g.plast, 0, (size_t)d.parnum * sizeof(int), s);
   if (np > 0) k_tt_segments<<<nblk(2*(long long)np), TPB, 0, s>>>(g, 2*np);
-  k_tt_sums<<<nblk(32LL * d.parnum), TPB, 0, s>>>(d, g);
+  k_tt_chunks<<<nblk(d.parnum), TPB, 0, s>>>(d, g);
+  k_tt_scan<<<1, 1024, 0, s>>>(g.nch, g.choff, d.parnum, g.nchunks);
+  k_tt_chunk_sums<<<nblk(32LL * pg_tt_max_chunks(d.parnum, np)), TPB, 0, s>>>(d, g);
+  k_tt_sums<<<nblk(d.parnum), TPB, 0, s>>>(d, g);
+}
+
+long long pg_tt_max_chunks(int parnum, int np)
+{
+  // each particle's entries fill its chunks but the last: at most parnum
+  // partial chunks beside 2 np / PG_TT_CHUNK full ones
+  return (long long)parnum + (2LL * np) / PG_TT_CHUNK + 1;
 }
 
 // kernels of one step's mesh-contact stage (the radix sorts launch three per pass)
 int pg_tt_kernel_count(const PgTT &g, int np)
 {
-  return 5 + 3 * g.passes + (np > 0 ? 4 + 3 * g.epasses : 0) + 1;
+  return 5 + 3 * g.passes + (np > 0 ? 4 + 3 * g.epasses : 0) + 4;
 }

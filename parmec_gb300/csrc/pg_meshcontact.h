@@ -33,9 +33,17 @@ struct PgTT
   double *pst[3] = {};
   unsigned *ekeys[2] = {}; int *evals[2] = {}; unsigned *ehist = nullptr;
   int *pfirst = nullptr, *plast = nullptr;  // [parnum] each particle's entries
+  // sums in chunks of PG_TT_CHUNK entries: chunks per particle, their
+  // offsets (an exclusive scan), the chunk sums (force, torque)
+  int *nch = nullptr, *choff = nullptr, *nchunks = nullptr;
+  double *csum[6] = {};
+  long long ccap = 0;             // chunk-sum capacity
 };
+
+#define PG_TT_CHUNK 1024          // entries one warp sums into one chunk sum
 
 int pg_tt_key_bits(int ncells);
 void pg_tt_find(const PgDev &d, PgTT &g, cudaStream_t s);                 // steps 1-4a; total in g.np_dev
 void pg_tt_forces(const PgDev &d, PgTT &g, cudaStream_t s, int np, double step);   // steps 4b-6
 int pg_tt_kernel_count(const PgTT &g, int np);
+long long pg_tt_max_chunks(int parnum, int np);   // chunk sums a step can need

@@ -1118,6 +1118,19 @@ int tt_stage(pg_session *s, double step)
     for (int c = 0; c < 3; c ++) { g.st[c] = st[c]; g.f[c] = f[c]; g.p[c] = p[c]; g.pst[c] = pst[c]; }
     g.cap = cap;
   }
+  const long long chunks = pg_tt_max_chunks(d.parnum, np);
+  if (chunks > g.ccap)
+  {
+    const long long cap = chunks + chunks / 2;
+    CK(cudaStreamSynchronize(s->stream));
+    for (int c = 0; c < 6; c ++)
+    {
+      release(s, g.csum[c]);
+      g.csum[c] = nullptr;
+      TRY(dalloc(s, &g.csum[c], (size_t)cap));
+    }
+    g.ccap = cap;
+  }
   pg_tt_forces(d, g, s->stream, np, step);
   s->launches += pg_tt_kernel_count(g, np);
   // this step's pairs become the previous step's
@@ -1645,6 +1658,9 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
     TRY(dalloc(s, &g.np_dev, 1));
     TRY(dalloc(s, &g.pfirst, P));
     TRY(dalloc(s, &g.plast, P));
+    TRY(dalloc(s, &g.nch, P));
+    TRY(dalloc(s, &g.choff, (size_t)P + 1));
+    TRY(dalloc(s, &g.nchunks, 1));
     for (int c = 0; c < 3; c ++) { TRY(dalloc(s, &d.ttF[c], P)); TRY(dalloc(s, &d.ttT[c], P)); }
   }
   release(s, g.cstart);

@@ -173,3 +173,23 @@ def test_gpu_spring_lattice_with_contact_bitwise(gpu_lib, oracle_lib):
     assert_bitwise(mg, mo)
     assert eg.mesh_contact_stats() == eo.mesh_contact_stats()
     assert eo.mesh_contact_stats()[1] > 0
+
+
+@pytest.mark.gpu
+def test_gpu_lattice_plate_sums_in_chunks_bitwise(gpu_lib, oracle_lib):
+    """A 24x24 lattice with contact on: tens of thousands of active pairs,
+    the base plate's share of them summed in several chunks of 1,024 entries
+    (one warp per chunk, the chunk sums in order), bit for bit against the
+    oracle's chunked sums."""
+    from oracle.pyoracle import OracleEngine
+    from parmec_gb300.engine import GpuEngine
+    from parmec_gb300.scenes import spring_lattice
+    (mg, dt), (mo, _) = spring_lattice(24, contact_radius=1e-3), spring_lattice(24, contact_radius=1e-3)
+    eg, eo = GpuEngine(), OracleEngine()
+    for k in range(2):
+        d = 20 * dt - (0.5 * dt if k == 0 else 0.0)
+        mg.dem(d, dt, interval=1e9, engine=eg)
+        mo.dem(d, dt, interval=1e9, engine=eo)
+        assert_bitwise(mg, mo)
+        assert eg.mesh_contact_stats() == eo.mesh_contact_stats()
+    assert eo.mesh_contact_stats()[1] > 8 * 1024
