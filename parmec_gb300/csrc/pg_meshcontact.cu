@@ -15,9 +15,12 @@
 //   4. the pairs, in the order of the finding triangles and their sorted
 //      partners (an exclusive scan of the counts gives each triangle's
 //      offset);
-//   5. one thread per pair: the swept-triangle contact (pg_tritri.cuh) and
-//      the granular law with the pair's tangential state, carried over from
-//      the previous step's pair list by (finder, partner);
+//   5. one thread per pair: the plane test that settles most pairs as
+//      apart; the others are queued (one atomic per warp) and evaluated by a
+//      grid-stride loop, so that the narrow phase runs on full warps: the
+//      swept-triangle contact (pg_tritri.cuh) and the granular law with the
+//      pair's tangential state, carried over from the previous step's pair
+//      list by (finder, partner);
 //   6. the force of each active pair goes to its two particles (+f to the
 //      finder's, -f to the partner's): the entries are sorted by particle
 //      (stably, so in pair order) and summed per particle in chunks of
@@ -195,18 +198,49 @@ __global__ void __launch_bounds__(TPB) k_tt_emit(PgDev d, PgTT g)
   }
 }
 
-// 5. contact and granular force of each pair
-__global__ void __launch_bounds__(TPB) k_tt_pairs(PgDev d, PgTT g, int np, double step)
+// 5a. pairs apart by the plane test get their (zero) results; the others
+// are queued
+__global__ void __launch_bounds__(TPB) k_tt_cull(PgDev d, PgTT g, int np)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= np) return;
+  bool near = false;
+  if (k < np)
+  {
+    double va[3][3], vb[3][3];
+    tri_vertices(d, g.pf[k], va);
+    tri_vertices(d, g.pu[k], vb);
+    const double *A[3] = {va[0], va[1], va[2]}, *B[3] = {vb[0], vb[1], vb[2]};
+    near = !pgtt::apart(A, B, g.r, g.r);
+    if (!near)
+    {
+      g.act[k] = 0;
+      for (int c = 0; c < 3; c ++) { g.st[c][k] = 0.0; g.f[c][k] = 0.0; g.p[c][k] = 0.0; }
+    }
+  }
+  // warp-aggregated push of the near pairs
+  const unsigned m = __ballot_sync(0xffffffffu, near);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(g.qn, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (near) g.queue[base + __popc(m & ((1u << lane) - 1u))] = k;
+}
+
+// 5b. contact and granular force of each queued pair
+__global__ void __launch_bounds__(TPB) k_tt_pairs(PgDev d, PgTT g, double step)
+{
+  const int nq = *g.qn;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x)
+  {
+  const int k = g.queue[w];
   const int f = g.pf[k], u = g.pu[k];
   double va[3][3], vb[3][3];
   tri_vertices(d, f, va);
   tri_vertices(d, u, vb);
   const double *A[3] = {va[0], va[1], va[2]}, *B[3] = {vb[0], vb[1], vb[2]};
   double point[3], normal[3];
-  const double depth = pgtt::contact(A, B, g.r, g.r, point, normal);
+  const double depth = pgtt::contact_near(A, B, g.r, g.r, point, normal);
   double st[3] = {0.0, 0.0, 0.0}, fr[3] = {0.0, 0.0, 0.0};
   const bool active = depth > 0.0;
   if (active)
@@ -246,6 +280,22 @@ __global__ void __launch_bounds__(TPB) k_tt_pairs(PgDev d, PgTT g, int np, doubl
     g.f[c][k] = fr[c];
     g.p[c][k] = point[c];
   }
+  }
+}
+
+// resident blocks of k_tt_pairs over every SM
+int pairs_blocks()
+{
+  static int nb = 0;
+  if (!nb)
+  {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tt_pairs, TPB, 0);
+    nb = (sms > 0 ? sms : 152) * (per > 0 ? per : 4);
+  }
+  return nb;
 }
 
 // 6a. two entries per pair, keyed by particle (inactive: the sentinel)
@@ -369,7 +419,9 @@ void pg_tt_forces(const PgDev &d, PgTT &g, cudaStream_t s, int np, double step)
   if (np > 0)
   {
     k_tt_emit<<<nblk(T), TPB, 0, s>>>(d, g);
-    k_tt_pairs<<<nblk(np), TPB, 0, s>>>(d, g, np, step);
+    cudaMemsetAsync(g.qn, 0, sizeof(int), s);
+    k_tt_cull<<<nblk(np), TPB, 0, s>>>(d, g, np);
+    k_tt_pairs<<<pairs_blocks(), TPB, 0, s>>>(d, g, step);
     k_tt_entries<<<nblk(np), TPB, 0, s>>>(d, g, np);
     pg_launch_radix_sort(g.ekeys[0], g.evals[0], g.ekeys[1], g.evals[1], g.ehist, 2*np, g.epasses, nullptr, s);
   }
@@ -392,5 +444,5 @@ long long pg_tt_max_chunks(int parnum, int np)
 // kernels of one step's mesh-contact stage (the radix sorts launch three per pass)
 int pg_tt_kernel_count(const PgTT &g, int np)
 {
-  return 5 + 3 * g.passes + (np > 0 ? 4 + 3 * g.epasses : 0) + 4;
+  return 5 + 3 * g.passes + (np > 0 ? 5 + 3 * g.epasses : 0) + 4;
 }

@@ -25,6 +25,7 @@ struct PgTT
   int cap = 0;                    // pair capacity
   int np_last = 0;                // pairs of the last step
   int *pf = nullptr, *pu = nullptr;         // [cap] finder and partner of each pair
+  int *queue = nullptr, *qn = nullptr;      // [cap] pairs that are not plainly apart, their count
   unsigned char *act = nullptr;
   double *st[3] = {}, *f[3] = {}, *p[3] = {};   // tangential state, force on the finder's particle, point
   // the previous step's pairs (state carried by (finder, partner))

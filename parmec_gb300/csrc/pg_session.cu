@@ -1094,7 +1094,9 @@ int tt_stage(pg_session *s, double step)
     const int cap = np + np / 2 + 1024;
     int *ppu = nullptr; unsigned char *pact = nullptr; double *pst[3] = {};
     int *pf = nullptr, *pu = nullptr; unsigned char *act = nullptr; double *st[3] = {}, *f[3] = {}, *p[3] = {};
+    int *queue = nullptr;
     TRY(dalloc(s, &pf, cap)); TRY(dalloc(s, &pu, cap)); TRY(dalloc(s, &act, cap)); TRY(dalloc(s, &ppu, cap));
+    TRY(dalloc(s, &queue, cap));
     TRY(dalloc(s, &pact, cap));
     for (int c = 0; c < 3; c ++)
     {
@@ -1108,13 +1110,14 @@ int tt_stage(pg_session *s, double step)
         CK(cudaMemcpyAsync(pst[c], g.pst[c], (size_t)g.cap * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
     }
     CK(cudaStreamSynchronize(s->stream));
-    for (void *q : {(void *)g.pf, (void *)g.pu, (void *)g.act, (void *)g.ppu, (void *)g.pact}) release(s, q);
+    for (void *q : {(void *)g.pf, (void *)g.pu, (void *)g.act, (void *)g.ppu, (void *)g.pact, (void *)g.queue})
+      release(s, q);
     for (int c = 0; c < 3; c ++) for (void *q : {(void *)g.st[c], (void *)g.f[c], (void *)g.p[c], (void *)g.pst[c]}) release(s, q);
     release(s, g.ekeys[0]); release(s, g.ekeys[1]); release(s, g.evals[0]); release(s, g.evals[1]); release(s, g.ehist);
     TRY(dalloc(s, &g.ekeys[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.ekeys[1], 2 * (size_t)cap));
     TRY(dalloc(s, &g.evals[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.evals[1], 2 * (size_t)cap));
     TRY(dalloc(s, &g.ehist, 256 * (size_t)pg_sort_blocks(2 * cap)));
-    g.pf = pf; g.pu = pu; g.act = act; g.ppu = ppu; g.pact = pact;
+    g.pf = pf; g.pu = pu; g.act = act; g.ppu = ppu; g.pact = pact; g.queue = queue;
     for (int c = 0; c < 3; c ++) { g.st[c] = st[c]; g.f[c] = f[c]; g.p[c] = p[c]; g.pst[c] = pst[c]; }
     g.cap = cap;
   }
@@ -1661,6 +1664,7 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
     TRY(dalloc(s, &g.nch, P));
     TRY(dalloc(s, &g.choff, (size_t)P + 1));
     TRY(dalloc(s, &g.nchunks, 1));
+    TRY(dalloc(s, &g.qn, 1));
     for (int c = 0; c < 3; c ++) { TRY(dalloc(s, &d.ttF[c], P)); TRY(dalloc(s, &d.ttT[c], P)); }
   }
   release(s, g.cstart);

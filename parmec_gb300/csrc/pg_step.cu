@@ -24,6 +24,25 @@ namespace {
 
 constexpr int TPB = 128;
 
+// minimum resident blocks per SM asked of the FP64 particle update and of
+// the contact evaluation (register budget against warps in flight)
+#ifndef PG_INTEGRATE_MINB
+#define PG_INTEGRATE_MINB 0
+#endif
+#ifndef PG_EVAL_MINB
+#define PG_EVAL_MINB 0
+#endif
+#if PG_INTEGRATE_MINB
+#define PG_LB_INTEGRATE __launch_bounds__(TPB, PG_INTEGRATE_MINB)
+#else
+#define PG_LB_INTEGRATE __launch_bounds__(TPB)
+#endif
+#if PG_EVAL_MINB
+#define PG_LB_EVAL __launch_bounds__(TPB, PG_EVAL_MINB)
+#else
+#define PG_LB_EVAL __launch_bounds__(TPB)
+#endif
+
 inline int nblk(int n) { return (n + TPB - 1) / TPB; }
 
 // record the first error with where it happened (site), the index and a value
@@ -585,7 +604,7 @@ __global__ void __launch_bounds__(TPB) k_contacts_probe(PgDev d)
 }
 
 template <bool GEOM, bool ADAPT>
-__global__ void __launch_bounds__(TPB) k_contacts_eval(PgDev d, double step)
+__global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
 {
   if (ADAPT) step = d.hs[0];
   const int n = *d.cwork_n;
@@ -1460,7 +1479,7 @@ __global__ void k_restrain_forces(PgDev d, const int *first, const int *list, in
 enum { INT_FUSED = 0, INT_FORCES = 1, INT_DYNAMICS = 2, INT_FORCES_ADAPT = 3, INT_DYN_FUSED = 4 };
 
 template <int MODE>
-__global__ void __launch_bounds__(TPB) k_integrate(PgDev d, double step, double step1)
+__global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double step1)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;

@@ -200,19 +200,16 @@ PG_TT bool beyond_plane(const double *const P[3], const double *const Q[3], doub
   return above == 3 || below == 3;
 }
 
-// Contact of swept triangles A and B (radii ra, rb): returns the depth
-// (> 0: touching) with the point and the unit normal from B towards A.
-// Triangles with one wholly beyond the other's plane by ra + rb are apart:
-// depth -1, point and normal zero.
-PG_TT double contact(const double *const a[3], const double *const b[3], double ra, double rb,
-                     double *point, double *normal)
+// Triangles with one wholly beyond the other's plane by ra + rb are apart.
+PG_TT bool apart(const double *const a[3], const double *const b[3], double ra, double rb)
 {
-  if (beyond_plane(a, b, ra + rb) || beyond_plane(b, a, ra + rb))
-  {
-    point[0] = point[1] = point[2] = 0.0;
-    normal[0] = normal[1] = normal[2] = 0.0;
-    return -1.0;
-  }
+  return beyond_plane(a, b, ra + rb) || beyond_plane(b, a, ra + rb);
+}
+
+// contact() for triangles that are not apart
+PG_TT double contact_near(const double *const a[3], const double *const b[3], double ra, double rb,
+                          double *point, double *normal)
+{
   double pa[3], pb[3];
   const double d2 = triangle_triangle(a, b, pa, pb);
   point[0] = 0.5*(pa[0]+pb[0]); point[1] = 0.5*(pa[1]+pb[1]); point[2] = 0.5*(pa[2]+pb[2]);
@@ -238,6 +235,21 @@ PG_TT double contact(const double *const a[3], const double *const b[3], double 
   const double sg = dot(n, w) < 0.0 ? -il : il;
   normal[0] = n[0]*sg; normal[1] = n[1]*sg; normal[2] = n[2]*sg;
   return ra + rb;
+}
+
+// Contact of swept triangles A and B (radii ra, rb): returns the depth
+// (> 0: touching) with the point and the unit normal from B towards A.
+// Triangles apart: depth -1, point and normal zero.
+PG_TT double contact(const double *const a[3], const double *const b[3], double ra, double rb,
+                     double *point, double *normal)
+{
+  if (apart(a, b, ra, rb))
+  {
+    point[0] = point[1] = point[2] = 0.0;
+    normal[0] = normal[1] = normal[2] = 0.0;
+    return -1.0;
+  }
+  return contact_near(a, b, ra, rb, point, normal);
 }
 
 // The granular contact law (forces.ispc:125-192) for normal n (from the
