@@ -565,12 +565,13 @@ def main():
     # 696 + 53 c_s bytes per particle for the integration (c_s: slave
     # contacts), 172 + 96 c per sphere for the contacts
     kernel_model = {"integrate": P * (696.0 + 53.0 * c_pair), "contacts": P * (172.0 + 96.0 * c_pair)}
-    # DRAM bytes per unit and FP64 instructions per unit of each kernel, from
-    # one ncu capture of the 262,144-sphere drum (dram__bytes_read.sum +
+    # DRAM bytes per unit and FP64 instructions per unit of each kernel group,
+    # from ncu captures of the 262,144-sphere drum (dram__bytes_read.sum +
     # dram__bytes_write.sum, and DADD + DMUL + DFMA thread instructions, per
-    # launch divided by the spheres), scaled to the full drum
-    traffic_per_unit = {"integrate": 458.0, "contacts": 200.0}
-    fp64_per_unit = {"integrate": 294.0, "contacts": 161.0}
+    # launch divided by the spheres), scaled to the full drum; the contact
+    # group is its three passes (probe, evaluation, sums) together
+    traffic_per_unit = {"integrate": 458.0, "contacts": 338.0}
+    fp64_per_unit = {"integrate": 294.0, "contacts": 174.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     fp64 = None
     if dom in fp64_per_unit:

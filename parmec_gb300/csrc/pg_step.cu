@@ -27,10 +27,10 @@ constexpr int TPB = 128;
 // minimum resident blocks per SM asked of the FP64 particle update and of
 // the contact evaluation (register budget against warps in flight)
 #ifndef PG_INTEGRATE_MINB
-#define PG_INTEGRATE_MINB 0
+#define PG_INTEGRATE_MINB 1
 #endif
 #ifndef PG_EVAL_MINB
-#define PG_EVAL_MINB 0
+#define PG_EVAL_MINB 8
 #endif
 #if PG_INTEGRATE_MINB
 #define PG_LB_INTEGRATE __launch_bounds__(TPB, PG_INTEGRATE_MINB)
