@@ -528,14 +528,20 @@ def main():
     m._dirty = True
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    try:
-        m.dem(args.steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
-    except RuntimeError:
-        print(json.dumps({"e2e_failure_diagnostics": eng.diagnostics()}), file=sys.stderr)
-        raise
-    e2e_s = time.perf_counter() - t0
+    # three timed DEM calls (each a full upload, K steps and a full download):
+    # the median is the line's e2e value
+    e2e_runs = []
+    for _ in range(3):
+        m._dirty = True
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            m.dem(args.steps * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        except RuntimeError:
+            print(json.dumps({"e2e_failure_diagnostics": eng.diagnostics()}), file=sys.stderr)
+            raise
+        e2e_runs.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_runs))
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -594,7 +600,8 @@ def main():
                 "h2d_bytes_per_step": up // args.steps, "d2h_bytes_per_step": down // args.steps,
                 "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
                         "full host->device upload, K steps, device->host download; host SoA arrays "
-                        "page-locked by the engine (cudaHostRegister)"},
+                        "page-locked by the engine (cudaHostRegister)",
+                "runs_s": [round(x, 4) for x in e2e_runs], "statistic": "median of the three DEM calls"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,

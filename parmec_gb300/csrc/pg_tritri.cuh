@@ -37,51 +37,56 @@ PG_TT void cross(const double *a, const double *b, double *c)
 PG_TT double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
 
 // Closest point q of triangle (a, b, c) to p: the Voronoi-region method
-// (Ericson, Real-Time Collision Detection, 5.1.5).
+// (Ericson, Real-Time Collision Detection, 5.1.5).  The region is found
+// first and its one division taken at a single place, so that threads of a
+// warp in different regions share the division's instructions; each region
+// divides the same operands as the textbook branches do.
 PG_TT void point_triangle(const double *p, const double *a, const double *b, const double *c, double *q)
 {
-  double ab[3], ac[3], ap[3];
-  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap);
+  double ab[3], ac[3], ap[3], bp[3], cp[3];
+  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap); sub(p, b, bp); sub(p, c, cp);
   const double d1 = dot(ab, ap), d2 = dot(ac, ap);
-  if (d1 <= 0.0 && d2 <= 0.0) { q[0] = a[0]; q[1] = a[1]; q[2] = a[2]; return; }
-  double bp[3];
-  sub(p, b, bp);
   const double d3 = dot(ab, bp), d4 = dot(ac, bp);
-  if (d3 >= 0.0 && d4 <= d3) { q[0] = b[0]; q[1] = b[1]; q[2] = b[2]; return; }
-  const double vc = d1*d4 - d3*d2;
-  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0)
-  {
-    const double v = d1 / (d1 - d3);
-    q[0] = a[0] + v*ab[0]; q[1] = a[1] + v*ab[1]; q[2] = a[2] + v*ab[2];
-    return;
-  }
-  double cp[3];
-  sub(p, c, cp);
   const double d5 = dot(ab, cp), d6 = dot(ac, cp);
-  if (d6 >= 0.0 && d5 <= d6) { q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; return; }
+  const double vc = d1*d4 - d3*d2;
   const double vb = d5*d2 - d1*d6;
-  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0)
-  {
-    const double w = d2 / (d2 - d6);
-    q[0] = a[0] + w*ac[0]; q[1] = a[1] + w*ac[1]; q[2] = a[2] + w*ac[2];
-    return;
-  }
   const double va = d3*d6 - d5*d4;
-  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
+  const double e43 = d4 - d3, e56 = d5 - d6;
+  // 0: vertex a, 1: vertex b, 2: edge ab, 3: vertex c, 4: edge ac, 5: edge bc, 6: face
+  const int region = (d1 <= 0.0 && d2 <= 0.0) ? 0 :
+                     (d3 >= 0.0 && d4 <= d3) ? 1 :
+                     (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) ? 2 :
+                     (d6 >= 0.0 && d5 <= d6) ? 3 :
+                     (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) ? 4 :
+                     (va <= 0.0 && e43 >= 0.0 && e56 >= 0.0) ? 5 : 6;
+  double num = 0.0, den = 1.0;
+  if (region == 2) { num = d1; den = d1 - d3; }
+  else if (region == 4) { num = d2; den = d2 - d6; }
+  else if (region == 5) { num = e43; den = e43 + e56; }
+  else if (region == 6) { num = 1.0; den = va + vb + vc; }
+  const double x = num / den;
+  switch (region)
   {
-    const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-    q[0] = b[0] + w*(c[0]-b[0]); q[1] = b[1] + w*(c[1]-b[1]); q[2] = b[2] + w*(c[2]-b[2]);
-    return;
+  case 0: q[0] = a[0]; q[1] = a[1]; q[2] = a[2]; break;
+  case 1: q[0] = b[0]; q[1] = b[1]; q[2] = b[2]; break;
+  case 3: q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; break;
+  case 2: q[0] = a[0] + x*ab[0]; q[1] = a[1] + x*ab[1]; q[2] = a[2] + x*ab[2]; break;
+  case 4: q[0] = a[0] + x*ac[0]; q[1] = a[1] + x*ac[1]; q[2] = a[2] + x*ac[2]; break;
+  case 5: q[0] = b[0] + x*(c[0]-b[0]); q[1] = b[1] + x*(c[1]-b[1]); q[2] = b[2] + x*(c[2]-b[2]); break;
+  default:
+  {
+    const double v = vb * x, w = vc * x;
+    q[0] = a[0] + ab[0]*v + ac[0]*w;
+    q[1] = a[1] + ab[1]*v + ac[1]*w;
+    q[2] = a[2] + ab[2]*v + ac[2]*w;
   }
-  const double den = 1.0 / (va + vb + vc);
-  const double v = vb * den, w = vc * den;
-  q[0] = a[0] + ab[0]*v + ac[0]*w;
-  q[1] = a[1] + ab[1]*v + ac[1]*w;
-  q[2] = a[2] + ab[2]*v + ac[2]*w;
+  }
 }
 
 // Closest points c1 on p1q1 and c2 on p2q2 (Ericson 5.1.9); returns |c1-c2|^2.
-// Parallel segments take s = 0.
+// Parallel segments take s = 0.  The divisions of the general case are taken
+// at single places (the clamped end's recomputation of s divides whichever
+// numerator applies), so that threads of a warp share them.
 PG_TT double segment_segment(const double *p1, const double *q1, const double *p2, const double *q2,
                              double *c1, double *c2)
 {
@@ -99,10 +104,13 @@ PG_TT double segment_segment(const double *p1, const double *q1, const double *p
     {
       const double b = dot(d1, d2);
       const double den = a*e - b*b;
-      s = den != 0.0 ? clamp01((b*f - c*e) / den) : 0.0;
+      const double s0 = (b*f - c*e) / (den != 0.0 ? den : 1.0);
+      s = den != 0.0 ? clamp01(s0) : 0.0;
       t = (b*s + f) / e;
-      if (t < 0.0) { t = 0.0; s = clamp01(-c / a); }
-      else if (t > 1.0) { t = 1.0; s = clamp01((b - c) / a); }
+      const bool low = t < 0.0, high = t > 1.0;
+      const double s1 = (low ? -c : b - c) / a;
+      if (low) { t = 0.0; s = clamp01(s1); }
+      else if (high) { t = 1.0; s = clamp01(s1); }
     }
   }
   c1[0] = p1[0] + d1[0]*s; c1[1] = p1[1] + d1[1]*s; c1[2] = p1[2] + d1[2]*s;
