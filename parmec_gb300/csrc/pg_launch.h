@@ -58,6 +58,12 @@ void pg_spring_events(int P, int S, const int *sj, const int *sk, std::vector<in
 
 // pg_sort.cu
 int  pg_sort_blocks(int n);
+// histogram scratch a radix sort of n keys needs (pg_launch_radix_sort):
+// 256 counts per tile, and past PG_SORT_SCAN_ONE_BLOCK tiles the sums of the
+// scan's tiles after them
+#define PG_SORT_SCAN_ONE_BLOCK 32
+size_t pg_sort_hist_len(int n);
+int  pg_sort_kernel_count(int n, int passes);   // kernels one radix sort launches
 int  pg_sort_passes(int bits_per_axis);
 int  pg_sort_passes_bits(int key_bits);
 void pg_launch_cell_keys(const double *x, const double *y, const double *z, int n, const double org[3],

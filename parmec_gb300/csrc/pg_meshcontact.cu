@@ -441,8 +441,8 @@ long long pg_tt_max_chunks(int parnum, int np)
   return (long long)parnum + (2LL * np) / PG_TT_CHUNK + 1;
 }
 
-// kernels of one step's mesh-contact stage (the radix sorts launch three per pass)
-int pg_tt_kernel_count(const PgTT &g, int np)
+// kernels of one step's mesh-contact stage
+int pg_tt_kernel_count(const PgTT &g, int trinum, int np)
 {
-  return 5 + 3 * g.passes + (np > 0 ? 5 + 3 * g.epasses : 0) + 4;
+  return 5 + pg_sort_kernel_count(trinum, g.passes) + (np > 0 ? 5 + pg_sort_kernel_count(2 * np, g.epasses) : 0) + 4;
 }

@@ -46,5 +46,5 @@ struct PgTT
 int pg_tt_key_bits(int ncells);
 void pg_tt_find(const PgDev &d, PgTT &g, cudaStream_t s);                 // steps 1-4a; total in g.np_dev
 void pg_tt_forces(const PgDev &d, PgTT &g, cudaStream_t s, int np, double step);   // steps 4b-6
-int pg_tt_kernel_count(const PgTT &g, int np);
+int pg_tt_kernel_count(const PgTT &g, int trinum, int np);
 long long pg_tt_max_chunks(int parnum, int np);   // chunk sums a step can need

@@ -46,7 +46,7 @@ extern "C" int pg_cell_order(const double *x, const double *y, const double *z, 
   int *v1 = nullptr;
   if (cudaMallocAsync((void **)&k1, sizeof(unsigned) * (size_t)n, s) != cudaSuccess ||
       cudaMallocAsync((void **)&v1, sizeof(int) * (size_t)n, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&hist, sizeof(unsigned) * 256 * (size_t)nb, s) != cudaSuccess)
+      cudaMallocAsync((void **)&hist, sizeof(unsigned) * pg_sort_hist_len(n), s) != cudaSuccess)
   {
     if (k1) cudaFreeAsync(k1, s);
     if (v1) cudaFreeAsync(v1, s);

@@ -1116,7 +1116,7 @@ int tt_stage(pg_session *s, double step)
     release(s, g.ekeys[0]); release(s, g.ekeys[1]); release(s, g.evals[0]); release(s, g.evals[1]); release(s, g.ehist);
     TRY(dalloc(s, &g.ekeys[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.ekeys[1], 2 * (size_t)cap));
     TRY(dalloc(s, &g.evals[0], 2 * (size_t)cap)); TRY(dalloc(s, &g.evals[1], 2 * (size_t)cap));
-    TRY(dalloc(s, &g.ehist, 256 * (size_t)pg_sort_blocks(2 * cap)));
+    TRY(dalloc(s, &g.ehist, pg_sort_hist_len(2 * cap)));
     g.pf = pf; g.pu = pu; g.act = act; g.ppu = ppu; g.pact = pact; g.queue = queue;
     for (int c = 0; c < 3; c ++) { g.st[c] = st[c]; g.f[c] = f[c]; g.p[c] = p[c]; g.pst[c] = pst[c]; }
     g.cap = cap;
@@ -1135,7 +1135,7 @@ int tt_stage(pg_session *s, double step)
     g.ccap = cap;
   }
   pg_tt_forces(d, g, s->stream, np, step);
-  s->launches += pg_tt_kernel_count(g, np);
+  s->launches += pg_tt_kernel_count(g, d.trinum, np);
   // this step's pairs become the previous step's
   g.np_last = np;
   std::swap(g.off, g.poff);
@@ -1653,7 +1653,7 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
     TRY(dalloc(s, &g.big, T));
     for (int c = 0; c < 6; c ++) TRY(dalloc(s, &g.box[c], T));
     for (int k = 0; k < 2; k ++) { TRY(dalloc(s, &g.keys[k], T)); TRY(dalloc(s, &g.vals[k], T)); }
-    TRY(dalloc(s, &g.hist, 256 * (size_t)pg_sort_blocks(T)));
+    TRY(dalloc(s, &g.hist, pg_sort_hist_len(T)));
     TRY(dalloc(s, &g.cand, (size_t)g.kmax * T));
     TRY(dalloc(s, &g.cnt, T));
     TRY(dalloc(s, &g.off, (size_t)T + 1));

@@ -41,6 +41,34 @@ __global__ void __launch_bounds__(1024) k_sort_scan(unsigned *hist, int nblocks,
   sort_scan_block(hist, nblocks, part);
 }
 
+// The histogram of a large sort (more than PG_SORT_SCAN_ONE_BLOCK tiles) is
+// scanned by the whole grid: tile sums | their scan by one block | each tile
+// rescanned from its base.  The tile sums sit after the histogram
+// (pg_sort_hist_len).
+constexpr int SCAN_BLOCK = 256;
+
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_tiles(const unsigned *a, int n, unsigned *bs, const int *gate)
+{
+  if (closed(gate)) return;
+  __shared__ unsigned sh[SCAN_BLOCK];
+  const unsigned sum = scan_tile_sum(a, n, blockIdx.x, sh);
+  if (threadIdx.x == 0) bs[blockIdx.x] = sum;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(unsigned *bs, int tiles, const int *gate)
+{
+  if (closed(gate)) return;
+  __shared__ unsigned part[1024];
+  block_scan_seq(bs, tiles, part);
+}
+
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_apply(unsigned *a, int n, const unsigned *bs, const int *gate)
+{
+  if (closed(gate)) return;
+  __shared__ unsigned sh[SCAN_BLOCK];
+  scan_tile_apply(a, n, blockIdx.x, bs[blockIdx.x], sh);
+}
+
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const unsigned *ksrc, const int *vsrc,
                                                                unsigned *kdst, int *vdst, int n,
                                                                const unsigned *hist, int nblocks, int shift,
@@ -63,6 +91,18 @@ int pg_sort_passes_exact(int key_bits)
 }
 
 int pg_sort_blocks(int n) { return n > 0 ? (n + SORT_TILE - 1) / SORT_TILE : 1; }
+
+size_t pg_sort_hist_len(int n)
+{
+  const int nb = pg_sort_blocks(n);
+  const size_t h = 256 * (size_t)nb;
+  return nb <= PG_SORT_SCAN_ONE_BLOCK ? h : h + (size_t)pg_scan_blocks((int)h);
+}
+
+int pg_sort_kernel_count(int n, int passes)
+{
+  return passes * (pg_sort_blocks(n) <= PG_SORT_SCAN_ONE_BLOCK ? 3 : 5);
+}
 
 int pg_sort_passes(int bits_per_axis) { return pg_sort_passes_bits(3 * bits_per_axis); }
 
@@ -98,7 +138,14 @@ void pg_launch_radix_sort(unsigned *k0, int *v0, unsigned *k1, int *v1, unsigned
     unsigned *ks = (p & 1) ? k1 : k0, *kd = (p & 1) ? k0 : k1;
     int *vs = (p & 1) ? v1 : v0, *vd = (p & 1) ? v0 : v1;
     k_sort_hist<<<nb, SORT_THREADS, 0, s>>>(ks, n, hist, nb, 8 * p, gate);
-    k_sort_scan<<<1, 1024, 0, s>>>(hist, nb, gate);
+    if (nb <= PG_SORT_SCAN_ONE_BLOCK) k_sort_scan<<<1, 1024, 0, s>>>(hist, nb, gate);
+    else
+    {
+      const int h = 256 * nb, tiles = pg_scan_blocks(h);
+      k_scan_tiles<<<tiles, SCAN_BLOCK, 0, s>>>(hist, h, hist + h, gate);
+      k_scan_sums<<<1, 1024, 0, s>>>(hist + h, tiles, gate);
+      k_scan_apply<<<tiles, SCAN_BLOCK, 0, s>>>(hist, h, hist + h, gate);
+    }
     k_sort_scatter<<<nb, SORT_THREADS, 0, s>>>(ks, vs, kd, vd, n, hist, nb, 8 * p, gate);
   }
 }

@@ -39,6 +39,8 @@ def call(lib, fn, c, org, cell, dim):
 
 CASES = [
     (1, 0), (2, 1), (2047, 2), (2048, 3), (2049, 4), (100000, 5), (300001, 6),
+    # the last size whose histogram one block scans, the first that the grid scans, and a large one
+    (65536, 7), (65537, 8), (2500000, 9),
 ]
 
 
