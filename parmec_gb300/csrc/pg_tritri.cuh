@@ -41,10 +41,13 @@ PG_TT double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
 // first and its one division taken at a single place, so that threads of a
 // warp in different regions share the division's instructions; each region
 // divides the same operands as the textbook branches do.
-PG_TT void point_triangle(const double *p, const double *a, const double *b, const double *c, double *q)
+// (ab = b - a and ac = c - a come with the triangle, computed once for the
+// three calls of a triangle pair that use them.)
+PG_TT void point_triangle(const double *p, const double *a, const double *b, const double *c,
+                          const double *ab, const double *ac, double *q)
 {
-  double ab[3], ac[3], ap[3], bp[3], cp[3];
-  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap); sub(p, b, bp); sub(p, c, cp);
+  double ap[3], bp[3], cp[3];
+  sub(p, a, ap); sub(p, b, bp); sub(p, c, cp);
   const double d1 = dot(ab, ap), d2 = dot(ac, ap);
   const double d3 = dot(ab, bp), d4 = dot(ac, bp);
   const double d5 = dot(ab, cp), d6 = dot(ac, cp);
@@ -120,28 +123,42 @@ PG_TT double segment_segment(const double *p1, const double *q1, const double *p
   return dot(w, w);
 }
 
-// Does segment pq cross triangle (a, b, c) through its interior or boundary?
-// The end points lie strictly on opposite sides of the plane and the
-// crossing point lies inside the triangle (same-side tests).  x: the point.
-PG_TT bool segment_crosses(const double *p, const double *q, const double *a, const double *b, const double *c,
-                           double *x)
+// A triangle with the differences every test of a pair takes from it: its
+// edges from each vertex to the next, ac = c - a, and the plane normal
+// n = (b - a) x (c - a).
+struct Tri
 {
-  double ab[3], ac[3], n[3], ap[3], aq[3];
-  sub(b, a, ab); sub(c, a, ac);
-  cross(ab, ac, n);
+  const double *v[3];
+  double e[3][3];                 // e[k] = v[k+1] - v[k]
+  double ac[3], n[3];
+};
+
+PG_TT void tri_prep(const double *const t[3], Tri &T)
+{
+  for (int k = 0; k < 3; k ++) T.v[k] = t[k];
+  for (int k = 0; k < 3; k ++) sub(t[(k+1)%3], t[k], T.e[k]);
+  sub(t[2], t[0], T.ac);
+  cross(T.e[0], T.ac, T.n);
+}
+
+// Does segment pq cross triangle T through its interior or boundary?  The
+// end points lie strictly on opposite sides of the plane and the crossing
+// point lies inside the triangle (same-side tests).  x: the point.
+PG_TT bool segment_crosses(const double *p, const double *q, const Tri &T, double *x)
+{
+  const double *a = T.v[0];
+  double ap[3], aq[3];
   sub(p, a, ap); sub(q, a, aq);
-  const double dp = dot(n, ap), dq = dot(n, aq);
+  const double dp = dot(T.n, ap), dq = dot(T.n, aq);
   if (!((dp > 0.0 && dq < 0.0) || (dp < 0.0 && dq > 0.0))) return false;
   const double t = dp / (dp - dq);
   x[0] = p[0] + (q[0]-p[0])*t; x[1] = p[1] + (q[1]-p[1])*t; x[2] = p[2] + (q[2]-p[2])*t;
-  const double *v[3] = {a, b, c};
   for (int k = 0; k < 3; k ++)
   {
-    double e[3], h[3], m[3];
-    sub(v[(k+1)%3], v[k], e);
-    sub(x, v[k], h);
-    cross(e, h, m);
-    if (dot(n, m) < 0.0) return false;
+    double h[3], m[3];
+    sub(x, T.v[k], h);
+    cross(T.e[k], h, m);
+    if (dot(T.n, m) < 0.0) return false;
   }
   return true;
 }
@@ -151,11 +168,13 @@ PG_TT bool segment_crosses(const double *p, const double *q, const double *a, co
 // pb = the first crossing found).
 PG_TT double triangle_triangle(const double *const a[3], const double *const b[3], double *pa, double *pb)
 {
+  Tri A, B;
+  tri_prep(a, A);
+  tri_prep(b, B);
   for (int i = 0; i < 3; i ++)
   {
     double x[3];
-    if (segment_crosses(a[i], a[(i+1)%3], b[0], b[1], b[2], x) ||
-        segment_crosses(b[i], b[(i+1)%3], a[0], a[1], a[2], x))
+    if (segment_crosses(a[i], a[(i+1)%3], B, x) || segment_crosses(b[i], b[(i+1)%3], A, x))
     {
       pa[0] = pb[0] = x[0]; pa[1] = pb[1] = x[1]; pa[2] = pb[2] = x[2];
       return 0.0;
@@ -165,7 +184,7 @@ PG_TT double triangle_triangle(const double *const a[3], const double *const b[3
   for (int i = 0; i < 3; i ++)
   {
     double q[3], w[3];
-    point_triangle(a[i], b[0], b[1], b[2], q);
+    point_triangle(a[i], b[0], b[1], b[2], B.e[0], B.ac, q);
     sub(a[i], q, w);
     const double d2 = dot(w, w);
     if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = a[i][k]; pb[k] = q[k]; } }
@@ -173,7 +192,7 @@ PG_TT double triangle_triangle(const double *const a[3], const double *const b[3
   for (int i = 0; i < 3; i ++)
   {
     double q[3], w[3];
-    point_triangle(b[i], a[0], a[1], a[2], q);
+    point_triangle(b[i], a[0], a[1], a[2], A.e[0], A.ac, q);
     sub(q, b[i], w);
     const double d2 = dot(w, w);
     if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = q[k]; pb[k] = b[i][k]; } }
