@@ -90,12 +90,14 @@ PG_TT void point_triangle(const double *p, const double *a, const double *b, con
 // Parallel segments take s = 0.  The divisions of the general case are taken
 // at single places (the clamped end's recomputation of s divides whichever
 // numerator applies), so that threads of a warp share them.
-PG_TT double segment_segment(const double *p1, const double *q1, const double *p2, const double *q2,
-                             double *c1, double *c2)
+// (d1 = q1 - p1 and d2 = q2 - p2 come with the triangles' edges, a = d1.d1
+// and e = d2.d2 with them.)
+PG_TT double segment_segment(const double *p1, const double *d1, double a, const double *p2, const double *d2,
+                             double e, double *c1, double *c2)
 {
-  double d1[3], d2[3], r[3];
-  sub(q1, p1, d1); sub(q2, p2, d2); sub(p1, p2, r);
-  const double a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+  double r[3];
+  sub(p1, p2, r);
+  const double f = dot(d2, r);
   double s, t;
   if (a <= 0.0 && e <= 0.0) { s = 0.0; t = 0.0; }
   else if (a <= 0.0) { s = 0.0; t = clamp01(f / e); }
@@ -130,6 +132,7 @@ struct Tri
 {
   const double *v[3];
   double e[3][3];                 // e[k] = v[k+1] - v[k]
+  double l2[3];                   // e[k].e[k]
   double ac[3], n[3];
 };
 
@@ -137,6 +140,7 @@ PG_TT void tri_prep(const double *const t[3], Tri &T)
 {
   for (int k = 0; k < 3; k ++) T.v[k] = t[k];
   for (int k = 0; k < 3; k ++) sub(t[(k+1)%3], t[k], T.e[k]);
+  for (int k = 0; k < 3; k ++) T.l2[k] = dot(T.e[k], T.e[k]);
   sub(t[2], t[0], T.ac);
   cross(T.e[0], T.ac, T.n);
 }
@@ -201,7 +205,7 @@ PG_TT double triangle_triangle(const double *const a[3], const double *const b[3
     for (int j = 0; j < 3; j ++)
     {
       double c1[3], c2[3];
-      const double d2 = segment_segment(a[i], a[(i+1)%3], b[j], b[(j+1)%3], c1, c2);
+      const double d2 = segment_segment(a[i], A.e[i], A.l2[i], b[j], B.e[j], B.l2[j], c1, c2);
       if (d2 < best) { best = d2; for (int k = 0; k < 3; k ++) { pa[k] = c1[k]; pb[k] = c2[k]; } }
     }
   return best;
