@@ -528,10 +528,10 @@ def main():
     m._dirty = True
     if dist:
         dist.barrier()
-    # three timed DEM calls (each a full upload, K steps and a full download):
+    # five timed DEM calls (each a full upload, K steps and a full download):
     # the median is the line's e2e value
     e2e_runs = []
-    for _ in range(3):
+    for _ in range(5):
         m._dirty = True
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -601,7 +601,7 @@ def main():
                 "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
                         "full host->device upload, K steps, device->host download; host SoA arrays "
                         "page-locked by the engine (cudaHostRegister)",
-                "runs_s": [round(x, 4) for x in e2e_runs], "statistic": "median of the three DEM calls"},
+                "runs_s": [round(x, 4) for x in e2e_runs], "statistic": "median of five DEM calls"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
