@@ -113,9 +113,11 @@ PG_TT double segment_segment(const double *p1, const double *d1, double a, const
       s = den != 0.0 ? clamp01(s0) : 0.0;
       t = (b*s + f) / e;
       const bool low = t < 0.0, high = t > 1.0;
-      const double s1 = (low ? -c : b - c) / a;
-      if (low) { t = 0.0; s = clamp01(s1); }
-      else if (high) { t = 1.0; s = clamp01(s1); }
+      if (low || high)
+      {
+        s = clamp01((low ? -c : b - c) / a);
+        t = low ? 0.0 : 1.0;
+      }
     }
   }
   c1[0] = p1[0] + d1[0]*s; c1[1] = p1[1] + d1[1]*s; c1[2] = p1[2] + d1[2]*s;
