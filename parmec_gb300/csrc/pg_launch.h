@@ -43,7 +43,6 @@ void pg_launch_mx_inertia(const PgDev &d, cudaStream_t s);
 void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0 = 0, int p1 = -1);
 void pg_launch_mx_centres(const PgDev &d, cudaStream_t s);   // before a due rebuild
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step);
-int  pg_contacts_mx_kernel_count(const PgDev &d);
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step);
 // the persistent fused step of the mixed form: shape index into the kernel
 // table, threads per block and blocks of the cooperative grid

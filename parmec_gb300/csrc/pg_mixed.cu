@@ -228,161 +228,10 @@ __global__ void k_mx_to64(PgDev d, int p0, int p1)
 // the list, in the same order.
 constexpr int MX_SPHERES = 1, MX_TRIANGLES = 2;
 
-// What one candidate evaluation needs of its sphere i.
-struct MxSphere
-{
-  int pi, coli;
-  df x[3], ri;
-  float v[3], oi[3], invmi, massi;
-};
-
-__device__ __forceinline__ void mx_sphere_load(const PgDev &d, int i, MxSphere &m)
-{
-  m.pi = d.part[i];
-  m.coli = d.ellcol[i];
-  for (int k = 0; k < 3; k ++)
-  {
-    m.x[k] = {d.xh[k][m.pi], d.xl[k][m.pi]};
-    m.v[k] = d.vh[k][m.pi];
-    m.oi[k] = d.om[k][m.pi];
-  }
-  m.ri = {d.rh[i], d.rl[i]};
-  m.invmi = d.invm_f[m.pi];
-  m.massi = d.mass_f[m.pi];
-}
-
-// The contact law of one candidate entry idx of sphere i, once its geometry
-// is known: the creation/persistence rule, contact point velocities, the
-// granular law; writes the entry's flag, state, force and partner arm.
-// Returns whether the contact is active (f: the force on i).
-__device__ __forceinline__ bool mx_contact_law(const PgDev &d, int i, size_t idx, const MxSphere &m, float step,
-                                               bool existing, bool pos, bool neg, float depth, const float *normal,
-                                               const float *armi, const float *armj, int pj, int colj,
-                                               const double *pnt, bool obsc, float *f)
-{
-  const bool active = existing ? !neg : pos;
-  if (!active)
-  {
-    if (existing)
-    {
-      d.nflag[idx] = 0;
-      d.nstate_f[0][idx] = 0.0f; d.nstate_f[1][idx] = 0.0f; d.nstate_f[2][idx] = 0.0f;
-    }
-    return false;
-  }
-  float vi[3], vj[3], vij[3];
-  vi[0] = m.oi[1]*armi[2]-m.oi[2]*armi[1] + m.v[0];
-  vi[1] = m.oi[2]*armi[0]-m.oi[0]*armi[2] + m.v[1];
-  vi[2] = m.oi[0]*armi[1]-m.oi[1]*armi[0] + m.v[2];
-  if (pj >= 0)
-  {
-    float oj[3] = {d.om[0][pj], d.om[1][pj], d.om[2][pj]};
-    vj[0] = oj[1]*armj[2]-oj[2]*armj[1] + d.vh[0][pj];
-    vj[1] = oj[2]*armj[0]-oj[0]*armj[2] + d.vh[1][pj];
-    vj[2] = oj[0]*armj[1]-oj[1]*armj[0] + d.vh[2][pj];
-  }
-  else
-  {
-    int l = -pj-2;
-    if (obsc && l >= 0) l = l+1;
-    if (l >= 0 && l < d.obsnum)
-    {
-      float z[3], oj[3];
-      for (int c = 0; c < 3; c ++)
-      {
-        z[c] = (float)(pnt[c] - d.obspnt[3*l+c]);
-        oj[c] = (float)d.obsang[3*l+c];
-      }
-      vj[0] = oj[1]*z[2]-oj[2]*z[1] + (float)d.obslin[3*l];
-      vj[1] = oj[2]*z[0]-oj[0]*z[2] + (float)d.obslin[3*l+1];
-      vj[2] = oj[0]*z[1]-oj[1]*z[0] + (float)d.obslin[3*l+2];
-    }
-    else { vj[0] = vj[1] = vj[2] = 0.0f; }
-  }
-  for (int c = 0; c < 3; c ++) vij[c] = vj[c] - vi[c];
-  const int ij = pairing(d, m.coli, colj);
-  if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED, 4, i, ij);
-  float state[3];
-  if (existing) { state[0] = d.nstate_f[0][idx]; state[1] = d.nstate_f[1][idx]; state[2] = d.nstate_f[2][idx]; }
-  else { state[0] = state[1] = state[2] = 0.0f; }
-  float ma = pj >= 0 ? 1.0f / (m.invmi + d.invm_f[pj]) : m.massi;
-  float kn = d.iparam_f[0][ij];
-  float en = d.iparam_f[1][ij] * 2.0f * sqrtf(kn*ma);
-  float vn = vij[0]*normal[0] + vij[1]*normal[1] + vij[2]*normal[2];
-  float fn = kn*depth + en*vn;
-  float kskn = d.iparam_f[6][ij];
-  float kt = kn * kskn, et = en * kskn;
-  float mus = d.iparam_f[2][ij], mud = d.iparam_f[3][ij];
-  float vt[3], ft[3];
-  for (int c = 0; c < 3; c ++)
-  {
-    f[c] = fn*normal[c];
-    vt[c] = vij[c] - vn*normal[c];
-    state[c] += step*vt[c];
-    ft[c] = kt*state[c] + et*vt[c];
-  }
-  float flen = sqrtf(ft[0]*ft[0] + ft[1]*ft[1] + ft[2]*ft[2]);
-  float lim = mus*fn;
-  if (flen > lim)
-  {
-    lim = mud*fn/flen;
-    ft[0] *= lim; ft[1] *= lim; ft[2] *= lim;
-  }
-  for (int c = 0; c < 3; c ++) f[c] += ft[c];
-  d.nflag[idx] = 1;
-  for (int c = 0; c < 3; c ++)
-  {
-    d.nstate_f[c][idx] = state[c];
-    d.nfrc_f[c][idx] = f[c];
-    d.narm_f[c][idx] = armj[c];
-  }
-  return true;
-}
-
-// One sphere-partner entry (code >= 0) of sphere i: the compensated-pair
-// gap, FP32 normal and arms, then the contact law.  Its arm on i is minus
-// the partner's arm the entry keeps.
-__device__ __forceinline__ bool mx_sphere_entry(const PgDev &d, int i, size_t idx, int j, const MxSphere &m,
-                                                float step, bool obsc, float *f)
-{
-  const bool existing = d.nflag[idx] != 0;
-  const int pj = d.part[j];
-  const int colj = d.ellcol[j];
-  df q[3];
-  for (int c = 0; c < 3; c ++) q[c] = df_sub(m.x[c], {d.xh[c][pj], d.xl[c][pj]});
-  df d2 = df_add(df_add(df_mul(q[0], q[0]), df_mul(q[1], q[1])), df_mul(q[2], q[2]));
-  df len = df_sqrt(d2);
-  df dep = df_sub(df_add(m.ri, {d.rh[j], d.rl[j]}), len);
-  const float depth = df_f(dep);
-  const bool pos = df_pos(dep);
-  const bool neg = df_neg_(dep);
-  float qf[3] = {df_f(q[0]), df_f(q[1]), df_f(q[2])};
-  float lenf = df_f(len);
-  float ilen = existing ? 1.0f / lenf : (lenf > 0.0f ? 1.0f / lenf : 1.0f);
-  float normal[3], armi[3], armj[3];
-  for (int c = 0; c < 3; c ++)
-  {
-    normal[c] = ilen * qf[c];
-    armi[c] = -0.5f * qf[c];
-    armj[c] = 0.5f * qf[c];
-  }
-  const double pnt[3] = {0.0, 0.0, 0.0};
-  return mx_contact_law(d, i, idx, m, step, existing, pos, neg, depth, normal, armi, armj, pj, colj, pnt, obsc, f);
-}
-
-// fs += f and ts += armi x f, with the products and sums rounded one by one
-// (no contraction), the same in every kernel that sums entries
-__device__ __forceinline__ void mx_accumulate(float *fs, float *ts, const float *armi, const float *f)
-{
-  for (int c = 0; c < 3; c ++) fs[c] = __fadd_rn(fs[c], f[c]);
-  ts[0] = __fadd_rn(ts[0], __fsub_rn(__fmul_rn(armi[1], f[2]), __fmul_rn(armi[2], f[1])));
-  ts[1] = __fadd_rn(ts[1], __fsub_rn(__fmul_rn(armi[2], f[0]), __fmul_rn(armi[0], f[2])));
-  ts[2] = __fadd_rn(ts[2], __fsub_rn(__fmul_rn(armi[0], f[1]), __fmul_rn(armi[1], f[0])));
-}
-
 template <int PASS>
 __device__ __forceinline__ bool mx_contacts_item(const PgDev &d, int i, double step_d)
 {
+  const int E = d.ellnum;
   const int pi = d.part[i];
   const int cnt = d.ncnt[i];
   bool more = false;
@@ -394,8 +243,17 @@ __device__ __forceinline__ bool mx_contacts_item(const PgDev &d, int i, double s
     const float step = (float)step_d;
     const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
     const bool etypo = (d.compat & PG_COMPAT_TRIEDGE) != 0;
-    MxSphere m;
-    mx_sphere_load(d, i, m);
+    df x[3];
+    float v[3], oi[3];
+    for (int k = 0; k < 3; k ++)
+    {
+      x[k] = {d.xh[k][pi], d.xl[k][pi]};
+      v[k] = d.vh[k][pi];
+      oi[k] = d.om[k][pi];
+    }
+    const df ri = {d.rh[i], d.rl[i]};
+    const int coli = d.ellcol[i];
+    const float invmi = d.invm_f[pi], massi = d.mass_f[pi];
     // the triangle pass starts at the first triangle, so that the j-th
     // triangles of the threads of a warp are evaluated together
     int k0 = 0;
@@ -406,31 +264,131 @@ __device__ __forceinline__ bool mx_contacts_item(const PgDev &d, int i, double s
       const size_t idx = (size_t)k * d.estride + i;
       const int code = d.ncode[idx];
       if (PASS == MX_SPHERES && code < 0) { more = true; break; }
-      float f[3];
+      const bool existing = d.nflag[idx] != 0;
+      float normal[3], armi[3], armj[3] = {0.0f, 0.0f, 0.0f}, depth;
+      bool pos, neg;
+      int pj, colj;
+      double pnt[3] = {0.0, 0.0, 0.0};
       if (code >= 0)
       {
-        if (mx_sphere_entry(d, i, idx, code, m, step, obsc, f))
+        const int j = code;
+        pj = d.part[j];
+        colj = d.ellcol[j];
+        df q[3];
+        for (int c = 0; c < 3; c ++) q[c] = df_sub(x[c], {d.xh[c][pj], d.xl[c][pj]});
+        df d2 = df_add(df_add(df_mul(q[0], q[0]), df_mul(q[1], q[1])), df_mul(q[2], q[2]));
+        df len = df_sqrt(d2);
+        df dep = df_sub(df_add(ri, {d.rh[j], d.rl[j]}), len);
+        depth = df_f(dep);
+        pos = df_pos(dep);
+        neg = df_neg_(dep);
+        float qf[3] = {df_f(q[0]), df_f(q[1]), df_f(q[2])};
+        float lenf = df_f(len);
+        float ilen = existing ? 1.0f / lenf : (lenf > 0.0f ? 1.0f / lenf : 1.0f);
+        for (int c = 0; c < 3; c ++)
         {
-          const float armi[3] = {-d.narm_f[0][idx], -d.narm_f[1][idx], -d.narm_f[2][idx]};
-          mx_accumulate(fs, ts, armi, f);
+          normal[c] = ilen * qf[c];
+          armi[c] = -0.5f * qf[c];
+          armj[c] = 0.5f * qf[c];
+        }
+      }
+      else
+      {
+        const int t = -code-1;
+        double A[3], B[3], C[3], cd[3], nd[3];
+        for (int c = 0; c < 3; c ++)
+        {
+          A[c] = d.tri[c][t]; B[c] = d.tri[3+c][t]; C[c] = d.tri[6+c][t];
+          cd[c] = df_to(x[c]);
+        }
+        double dd = triangle_sphere(A, B, C, cd, df_to(ri), pnt, nd, etypo);
+        depth = (float)dd;
+        pos = dd > 0.0;
+        neg = dd < 0.0;
+        for (int c = 0; c < 3; c ++) { normal[c] = (float)nd[c]; armi[c] = (float)(pnt[c] - cd[c]); }
+        pj = d.triobs[t];
+        colj = d.tricol[t];
+      }
+      const bool active = existing ? !neg : pos;
+      if (!active)
+      {
+        if (existing)
+        {
+          d.nflag[idx] = 0;
+          d.nstate_f[0][idx] = 0.0f; d.nstate_f[1][idx] = 0.0f; d.nstate_f[2][idx] = 0.0f;
         }
         continue;
       }
-      const bool existing = d.nflag[idx] != 0;
-      const int t = -code-1;
-      double A[3], B[3], C[3], cd[3], nd[3], pnt[3];
+      float vi[3], vj[3], vij[3];
+      vi[0] = oi[1]*armi[2]-oi[2]*armi[1] + v[0];
+      vi[1] = oi[2]*armi[0]-oi[0]*armi[2] + v[1];
+      vi[2] = oi[0]*armi[1]-oi[1]*armi[0] + v[2];
+      if (pj >= 0)
+      {
+        float oj[3] = {d.om[0][pj], d.om[1][pj], d.om[2][pj]};
+        vj[0] = oj[1]*armj[2]-oj[2]*armj[1] + d.vh[0][pj];
+        vj[1] = oj[2]*armj[0]-oj[0]*armj[2] + d.vh[1][pj];
+        vj[2] = oj[0]*armj[1]-oj[1]*armj[0] + d.vh[2][pj];
+      }
+      else
+      {
+        int l = -pj-2;
+        if (obsc && l >= 0) l = l+1;
+        if (l >= 0 && l < d.obsnum)
+        {
+          float z[3], oj[3];
+          for (int c = 0; c < 3; c ++)
+          {
+            z[c] = (float)(pnt[c] - d.obspnt[3*l+c]);
+            oj[c] = (float)d.obsang[3*l+c];
+          }
+          vj[0] = oj[1]*z[2]-oj[2]*z[1] + (float)d.obslin[3*l];
+          vj[1] = oj[2]*z[0]-oj[0]*z[2] + (float)d.obslin[3*l+1];
+          vj[2] = oj[0]*z[1]-oj[1]*z[0] + (float)d.obslin[3*l+2];
+        }
+        else { vj[0] = vj[1] = vj[2] = 0.0f; }
+      }
+      for (int c = 0; c < 3; c ++) vij[c] = vj[c] - vi[c];
+      const int ij = pairing(d, coli, colj);
+      if (d.ikind[ij] != 0) set_err(d, PG_ERR_UNSUPPORTED, 4, i, ij);
+      float state[3];
+      if (existing) { state[0] = d.nstate_f[0][idx]; state[1] = d.nstate_f[1][idx]; state[2] = d.nstate_f[2][idx]; }
+      else { state[0] = state[1] = state[2] = 0.0f; }
+      float ma = pj >= 0 ? 1.0f / (invmi + d.invm_f[pj]) : massi;
+      float kn = d.iparam_f[0][ij];
+      float en = d.iparam_f[1][ij] * 2.0f * sqrtf(kn*ma);
+      float vn = vij[0]*normal[0] + vij[1]*normal[1] + vij[2]*normal[2];
+      float fn = kn*depth + en*vn;
+      float kskn = d.iparam_f[6][ij];
+      float kt = kn * kskn, et = en * kskn;
+      float mus = d.iparam_f[2][ij], mud = d.iparam_f[3][ij];
+      float f[3], vt[3], ft[3];
       for (int c = 0; c < 3; c ++)
       {
-        A[c] = d.tri[c][t]; B[c] = d.tri[3+c][t]; C[c] = d.tri[6+c][t];
-        cd[c] = df_to(m.x[c]);
+        f[c] = fn*normal[c];
+        vt[c] = vij[c] - vn*normal[c];
+        state[c] += step*vt[c];
+        ft[c] = kt*state[c] + et*vt[c];
       }
-      double dd = triangle_sphere(A, B, C, cd, df_to(m.ri), pnt, nd, etypo);
-      float normal[3], armi[3];
-      const float armj[3] = {0.0f, 0.0f, 0.0f};
-      for (int c = 0; c < 3; c ++) { normal[c] = (float)nd[c]; armi[c] = (float)(pnt[c] - cd[c]); }
-      if (mx_contact_law(d, i, idx, m, step, existing, dd > 0.0, dd < 0.0, (float)dd, normal, armi, armj,
-                         d.triobs[t], d.tricol[t], pnt, obsc, f))
-        mx_accumulate(fs, ts, armi, f);
+      float flen = sqrtf(ft[0]*ft[0] + ft[1]*ft[1] + ft[2]*ft[2]);
+      float lim = mus*fn;
+      if (flen > lim)
+      {
+        lim = mud*fn/flen;
+        ft[0] *= lim; ft[1] *= lim; ft[2] *= lim;
+      }
+      for (int c = 0; c < 3; c ++) f[c] += ft[c];
+      d.nflag[idx] = 1;
+      for (int c = 0; c < 3; c ++)
+      {
+        d.nstate_f[c][idx] = state[c];
+        d.nfrc_f[c][idx] = f[c];
+        d.narm_f[c][idx] = armj[c];
+      }
+      fs[0] += f[0]; fs[1] += f[1]; fs[2] += f[2];
+      ts[0] += armi[1]*f[2] - armi[2]*f[1];
+      ts[1] += armi[2]*f[0] - armi[0]*f[2];
+      ts[2] += armi[0]*f[1] - armi[1]*f[0];
     }
   }
   for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
@@ -445,82 +403,6 @@ __global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_contacts_mx(PgDev d, 
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool more = false;
   if (i < d.ellnum) more = mx_contacts_item<MX_SPHERES>(d, i, step_d);
-  pgk::tri_queue_push(d, more, i);
-}
-
-// The sphere partners in three passes, so that the evaluations run on full
-// warps (one thread per sphere walks a list whose lengths differ across a
-// warp): the probe queues every sphere-partner entry (one atomic per warp),
-// a grid-stride loop evaluates the queued entries (mx_sphere_entry, as
-// above), and one thread per sphere sums its active entries in list order
-// (mx_accumulate, as above) and queues the spheres with triangles.  The
-// same operations in the same order as k_contacts_mx: the same bits.
-__global__ void __launch_bounds__(TPB) k_mx_probe(PgDev d)
-{
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cnt = i < d.ellnum ? d.ncnt[i] : 0;
-  int kmax = cnt;
-  for (int o = 16; o > 0; o >>= 1)
-  {
-    const int other = __shfl_xor_sync(0xffffffffu, kmax, o);
-    kmax = other > kmax ? other : kmax;
-  }
-  bool spheres = true;
-  for (int k = 0; k < kmax; k ++)
-  {
-    const size_t idx = (size_t)k * d.estride + i;
-    bool push = false;
-    if (spheres && k < cnt)
-    {
-      push = d.ncode[idx] >= 0;
-      spheres = push;
-    }
-    const unsigned mk = __ballot_sync(0xffffffffu, push);
-    if (!mk) continue;
-    const int lane = threadIdx.x & 31, lead = __ffs(mk) - 1;
-    int base = 0;
-    if (lane == lead) base = atomicAdd(d.cwork_n, __popc(mk));
-    base = __shfl_sync(0xffffffffu, base, lead);
-    if (push) d.cwork[base + __popc(mk & ((1u << lane) - 1u))] = (int)idx;
-  }
-}
-
-__global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_mx_eval(PgDev d, double step_d)
-{
-  const int n = *d.cwork_n;
-  const float step = (float)step_d;
-  const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
-  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
-  {
-    const size_t idx = (size_t)d.cwork[w];
-    const int i = (int)(idx % (size_t)d.estride);
-    MxSphere m;
-    mx_sphere_load(d, i, m);
-    float f[3];
-    mx_sphere_entry(d, i, idx, d.ncode[idx], m, step, obsc, f);
-  }
-}
-
-__global__ void __launch_bounds__(TPB, PG_MX_MIN_BLOCKS) k_mx_sum(PgDev d)
-{
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool more = false;
-  if (i < d.ellnum)
-  {
-    const int pi = d.part[i];
-    const int cnt = d.ncnt[i];
-    float fs[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
-    for (int k = 0; k < cnt; k ++)
-    {
-      const size_t idx = (size_t)k * d.estride + i;
-      if (d.ncode[idx] < 0) { more = true; break; }
-      if (!d.nflag[idx]) continue;
-      const float f[3] = {d.nfrc_f[0][idx], d.nfrc_f[1][idx], d.nfrc_f[2][idx]};
-      const float armi[3] = {-d.narm_f[0][idx], -d.narm_f[1][idx], -d.narm_f[2][idx]};
-      mx_accumulate(fs, ts, armi, f);
-    }
-    for (int c = 0; c < 3; c ++) { d.fm_f[c][pi] = fs[c]; d.tm_f[c][pi] = ts[c]; }
-  }
   pgk::tri_queue_push(d, more, i);
 }
 
@@ -819,39 +701,12 @@ void pg_launch_mx_centres(const PgDev &d, cudaStream_t s)
   if (d.ellnum) k_mx_centres<<<nblk(d.ellnum), TPB, 0, s>>>(d);
 }
 
-// resident blocks of the queued evaluation over every SM
-static int mx_eval_blocks()
-{
-  static int nb = 0;
-  if (!nb)
-  {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_eval, TPB, 0);
-    nb = (sms > 0 ? sms : 152) * (per > 0 ? per : 8);
-  }
-  return nb;
-}
-
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)
 {
   if (!d.ellnum) return;
+  k_contacts_mx<<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
   const int nb = nblk(d.ellnum);
-  if (d.cwork && d.cwork_n)
-  {
-    cudaMemsetAsync(d.cwork_n, 0, sizeof(int), s);
-    k_mx_probe<<<nb, TPB, 0, s>>>(d);
-    k_mx_eval<<<mx_eval_blocks(), TPB, 0, s>>>(d, step);
-    k_mx_sum<<<nb, TPB, 0, s>>>(d);
-  }
-  else k_contacts_mx<<<nb, TPB, 0, s>>>(d, step);
   k_tri_mx<<<nb < pgk::TRI_PASS_BLOCKS ? nb : pgk::TRI_PASS_BLOCKS, TPB, 0, s>>>(d, step);
-}
-
-int pg_contacts_mx_kernel_count(const PgDev &d)
-{
-  return d.ellnum ? ((d.cwork && d.cwork_n) ? 4 : 2) : 0;
 }
 
 void pg_launch_integrate_mx(const PgDev &d, cudaStream_t s, double step)

@@ -742,8 +742,6 @@ int slot_buffers(pg_session *s)
       TRY(dalloc(s, &d.nfrc_f[k], slots));
       TRY(dalloc(s, &d.narm_f[k], slots));
     }
-    TRY(dalloc(s, &d.cwork, slots));
-    TRY(dalloc(s, &d.cwork_n, 1));
   }
   // slave-list entries: at most kn per sphere
   const size_t ent = slots;

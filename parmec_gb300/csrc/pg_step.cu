@@ -2452,12 +2452,11 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
 }
 
 // the FP64 form evaluates the lists in three passes (one when no work queue
-// is allocated); the mixed form in three sphere passes and a triangle pass
-// (pg_mixed.cu)
+// is allocated); the mixed form in a sphere and a triangle pass (pg_mixed.cu)
 int pg_contacts_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
-  if (d.form == PG_FORM_MIXED) return pg_contacts_mx_kernel_count(d);
+  if (d.form == PG_FORM_MIXED) return 2;
   return (d.cwork && d.cwork_n) ? 3 : 1;
 }
 
