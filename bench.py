@@ -184,12 +184,22 @@ def mixed_form(args, ref64):
     eng.download()
     n = m.parnum
     dx = float(np.max(np.abs(m.P.position[0:3, :n] - ref64["x"])))
+    # per kernel group, on K more steps with CUDA events around each group
+    # (after the state above was read)
+    times2, end2 = driver.step_times(m.curtime, args.steps * dt - 0.5 * dt, dt)
+    tabs2 = driver.StepTables(m, times2, dt, [1e9, 1e9], [None, None], [-1, -1])
+    eng.profile(True)
+    eng.run(tabs2.ctab(0, len(times2)), dt)
+    torch.cuda.synchronize()
+    prof = eng.profile_read()
+    eng.profile(False)
+    kernel_ms = {k: round(v[0] / args.steps, 4) for k, v in prof.items() if v[1] > 0}
     fmax = float(np.max(np.abs(ref64["f"])))
     df = float(np.max(np.abs(m.P.force[:, :n] - ref64["f"]))) / fmax
     E = energy.total(m)
     out = {"form": "mixed: FP32 contact geometry and forces, compensated FP32 pairs for x, v, L, radii and gaps",
            "value": n * args.steps / (el_ms * 1e-3), "unit": "particle-steps/s",
-           "ms_per_step": el_ms / args.steps,
+           "ms_per_step": el_ms / args.steps, "kernel_ms": kernel_ms,
            "errors_vs_fp64": {"steps": args.warmup + args.steps, "position_max_abs_m": dx,
                               "force_max_abs_rel_to_max": df,
                               "energy_rel": abs(E - ref64["E"]) / abs(ref64["E"]),
