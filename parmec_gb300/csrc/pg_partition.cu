@@ -92,6 +92,9 @@ extern "C" int pg_cell_order(const double *x, const double *y, const double *z, 
 // entries per tile (tile = the sort's SORT_TILE keys, 2048 when this was
 // written); the call checks pg_sort_blocks(n) against this bound
 #define PG_CELL_ORDER_STATIC_BLOCKS 32
+// the histogram of a sort this small is scanned by one block, so the
+// scratch needs no room for the grid scan's tile sums (pg_sort_hist_len)
+static_assert(PG_CELL_ORDER_STATIC_BLOCKS <= PG_SORT_SCAN_ONE_BLOCK, "static scratch too small for the grid scan");
 
 namespace {
 
