@@ -256,6 +256,15 @@ def batched_form(args, scenes):
             n = P.parnum
             snap[key] = {"x": P.P.position[0:3, :n].copy(), "f": P.P.force[:, :n].copy(),
                          "E": [range_energy(P, r[0], r[1], sc[2][0:3]) for r, sc in zip(P.scene_ranges, scenes)]}
+            # per kernel group, on K more steps with CUDA events around each group
+            times2, _ = driver.step_times(end_time, steps * dt - 0.5 * dt, dt)
+            tabs2 = driver.StepTables(P, times2, dt, [1e9, 1e9], [None, None], [-1, -1])
+            eng.profile(True)
+            eng.run(tabs2.ctab(0, len(times2)), dt)
+            torch.cuda.synchronize()
+            prof = eng.profile_read()
+            eng.profile(False)
+            out[key]["kernel_ms"] = {g: round(v[0] / steps, 4) for g, v in prof.items() if v[1] > 0}
         if fused:
             threads, blocks, tuned, graph = eng.fused_config()
             out[key]["kernel"] = {"fused_step": True, "threads": threads, "blocks": blocks,
