@@ -226,7 +226,7 @@ bool restart_lists(int P, int E, int T)
   d.estride = E;
   d.sbits = pg_rebuild_entry_bits(P);
   bool ok = zeros(d.ncnt, E) && zeros(d.rcnt, P) && grow(d.soff, (size_t)P + 1) && grow(d.eorder, E) &&
-            grow(d.eoff, (size_t)E + 1) && grow(d.smeta, 4) && grow(d.gbar, 4) && slot_arrays(0);
+            grow(d.eoff, (size_t)E + 1) && grow(d.smeta, 5) && grow(d.gbar, 4) && slot_arrays(0);
   for (int k = 0; ok && k < 3; k ++) ok = grow(d.cref[k], E) && grow(d.fm[k], P) && grow(d.tm[k], P);
   ok = ok && grow(d.cfs, E) && grow(d.pfs, E) && grow(d.ekey, E);
   for (int k = 0; ok && k < 9; k ++) ok = grow(d.tref[k], T);

@@ -598,10 +598,48 @@ __device__ __forceinline__ void rb_soff_item(const PgDev &d, int p)
 {
   const int n = d.rcnt[p];
   d.soff[p] = n;
-  // one atomic per warp for the largest slave count
+  d.rcnt[p] = 0;                 // the placement cursor of the entry scatter
+  // one atomic per warp for the largest slave count (of the session and of
+  // this rebuild)
   const unsigned am = __activemask();
   const int wmax = __reduce_max_sync(am, n);
-  if ((threadIdx.x & 31) == __ffs(am) - 1 && wmax > 0) atomicMax(&d.stats[2], wmax);
+  if ((threadIdx.x & 31) == __ffs(am) - 1 && wmax > 0)
+  {
+    atomicMax(&d.stats[2], wmax);
+    atomicMax(&d.smeta[4], wmax);
+  }
+}
+
+// Slave lists whose longest list has at most PG_SLAVE_PLACE_MAX entries are
+// built without the entry sort: every entry goes to its partner's next free
+// position (an atomic cursor), then each particle orders its few entries by
+// emit position, the order the stable sort by partner gives them.
+constexpr int PG_SLAVE_PLACE_MAX = 64;
+
+__device__ __forceinline__ void rb_place_item(const PgDev &d, int e)
+{
+  const unsigned pj = d.skey[0][e];
+  if (pj == 0xffffffffu) return;
+  const int at = d.soff[pj] + atomicAdd(&d.rcnt[pj], 1);
+  d.skey[1][at] = (unsigned)e;
+  d.sval[1][at] = d.sval[0][e];
+}
+
+__device__ __forceinline__ void rb_order_item(const PgDev &d, int p, int *dst)
+{
+  const int b = d.soff[p], n = d.soff[p+1] - b;
+  unsigned key[PG_SLAVE_PLACE_MAX];
+  int val[PG_SLAVE_PLACE_MAX];
+  for (int a = 0; a < n; a ++)
+  {
+    const unsigned k = d.skey[1][b + a];
+    const int v = d.sval[1][b + a];
+    int c = a - 1;
+    while (c >= 0 && key[c] > k) { key[c+1] = key[c]; val[c+1] = val[c]; c --; }
+    key[c+1] = k;
+    val[c+1] = v;
+  }
+  for (int a = 0; a < n; a ++) dst[b + a] = val[a];
 }
 
 // sizes of the entry sort (one thread): entries, tiles, histogram length and
@@ -755,7 +793,7 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   if (!grid_barrier(d)) return false;
   for (int p = g0; p < P; p += gsz) rb_rzero_item(d, p);
   for (int q = g0; q < E; q += gsz) rb_count_item(d, q);
-  if (g0 == 0) d.eoff[E] = 0;
+  if (g0 == 0) { d.eoff[E] = 0; d.smeta[4] = 0; }
   if (!grid_barrier(d)) return false;
   if (!grid_scan(d, d.eoff, E + 1, (int *)d.sbs, (int *)sm.part)) return false;
   for (int q = g0; q < E; q += gsz) rb_emit_item(d, q);
@@ -764,6 +802,17 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   if (g0 == 0) { d.soff[P] = 0; rb_meta_item(d); }
   if (!grid_barrier(d)) return false;
   if (!grid_scan(d, d.soff, P + 1, (int *)d.sbs, (int *)sm.part)) return false;
+  if (d.smeta[4] <= PG_SLAVE_PLACE_MAX)
+  {
+    // short lists: placement and per-particle ordering, the result where
+    // the entry sort would leave it (sval[epasses & 1])
+    const int n = d.smeta[0];
+    for (int e = g0; e < n; e += gsz) rb_place_item(d, e);
+    if (!grid_barrier(d)) return false;
+    int *dst = d.sval[epasses & 1];
+    for (int p = g0; p < P; p += gsz) rb_order_item(d, p, dst);
+  }
+  else
   {
     const int n = d.smeta[0], nbe = d.smeta[1];
     for (int p = 0; p < epasses; p ++)

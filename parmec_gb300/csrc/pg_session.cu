@@ -792,7 +792,7 @@ int contact_buffers(pg_session *s)
   TRY(dalloc(s, &d.eorder, E));
   s->h_part.clear();                              // eorder is rebuilt at the next upload
   TRY(dalloc(s, &d.eoff, E + 1));
-  TRY(dalloc(s, &d.smeta, 4));
+  TRY(dalloc(s, &d.smeta, 5));
   d.sbits = pg_rebuild_entry_bits((int)P);
   for (int k = 0; k < 9; k ++) TRY(dalloc(s, &d.tref[k], T));
   TRY(dalloc(s, &d.tbox, 6 * std::max<size_t>(T, 1)));

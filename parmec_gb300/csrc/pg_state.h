@@ -138,7 +138,7 @@ struct PgDev
   unsigned *skey[2];        // [kn*ellnum] entry sort: partner particle (0xffffffff: none)
   int *sval[2];             // [kn*ellnum] entry sort: entry index
   unsigned *shist;          // entry-sort tile histograms
-  int *smeta;               // [4]: entries, tiles, histogram length, scan tiles of it
+  int *smeta;               // [5]: entries, tiles, histogram length, scan tiles of it, longest slave list
   unsigned *sbs;            // scan block sums
   int sbits;                // bits of the entry-sort keys
 
