@@ -30,7 +30,7 @@ constexpr int TPB = 128;
 #define PG_INTEGRATE_MINB 1
 #endif
 #ifndef PG_EVAL_MINB
-#define PG_EVAL_MINB 6
+#define PG_EVAL_MINB 8
 #endif
 #if PG_INTEGRATE_MINB
 #define PG_LB_INTEGRATE __launch_bounds__(TPB, PG_INTEGRATE_MINB)
@@ -541,13 +541,20 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
 // Every slot takes the same operations as in k_contacts and the sums the
 // same order, so the results are the same bits; the list's order plays no
 // part.
-// the evaluation of one candidate entry (slot idx0 = k * estride + i)
 template <bool GEOM, bool ADAPT>
-__device__ __forceinline__ void contact_entry(const PgDev &d, int idx0, double step, bool obsc)
+__global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
 {
+  if (ADAPT) step = d.hs[0];
+  const int n = *d.cwork_n;
+  const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
   {
+    const int idx0 = d.cwork[w];
     const size_t idx = (size_t)idx0;
     const int i = idx0 % d.estride;
+    // an entry past its sphere's list (a range whose lists restarted since
+    // the list was made) is no longer a candidate
+    if (idx0 / d.estride >= d.ncnt[i]) continue;
     const int pi = d.part[i];
     double c[3];
     for (int k = 0; k < 3; k ++) c[k] = d.center[k][i];
@@ -604,7 +611,7 @@ __device__ __forceinline__ void contact_entry(const PgDev &d, int idx0, double s
         d.nflag[idx] = 0;
         d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
       }
-      return;
+      continue;
     }
     // the rest of sphere i's state, for the contacts that are active
     double x[3], v[3], oi[3];
@@ -732,82 +739,6 @@ __device__ __forceinline__ void contact_entry(const PgDev &d, int idx0, double s
     }
     if (GEOM) d.ndep[idx] = depth;
   }
-}
-
-// Is entry idx0 worth the evaluation?  Not when it is past its sphere's
-// list (a range whose lists restarted since the work list was made), nor
-// when it is a sphere partner clearly apart: the squared-distance test
-// before the square root, an existing contact ending there.  Triangle
-// partners are always evaluated.
-__device__ __forceinline__ bool entry_near(const PgDev &d, int idx0)
-{
-  const size_t idx = (size_t)idx0;
-  const int i = idx0 % d.estride;
-  if (idx0 / d.estride >= d.ncnt[i]) return false;
-  const int code = d.ncode[idx];
-  if (code < 0) return true;
-  double q[3];
-  q[0] = d.center[0][i]-d.center[0][code];
-  q[1] = d.center[1][i]-d.center[1][code];
-  q[2] = d.center[2][i]-d.center[2][code];
-  const double d2 = dot3(q, q);
-  const double sr = d.radii[0][i]+d.radii[0][code];
-  if (d2 > (sr*sr) * (1.0 + 1e-12))
-  {
-    if (d.nflag[idx])
-    {
-      d.nflag[idx] = 0;
-      d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
-    }
-    return false;
-  }
-  return true;
-}
-
-// Each block walks tiles of the work list: every thread tests its entry
-// (entry_near), the near ones go to a queue in shared memory, and whenever
-// the queue holds a block's worth the whole block evaluates them, so the
-// FP64 evaluation runs on full warps.
-template <bool GEOM, bool ADAPT>
-__global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
-{
-  if (ADAPT) step = d.hs[0];
-  const int n = *d.cwork_n;
-  const bool obsc = (d.compat & PG_COMPAT_OBSIDX) != 0;
-  __shared__ int queue[2 * TPB];
-  __shared__ int qn;
-  if (threadIdx.x == 0) qn = 0;
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  for (int base = blockIdx.x * TPB; base < n; base += gridDim.x * TPB)
-  {
-    const int w = base + threadIdx.x;
-    int idx0 = 0;
-    bool push = false;
-    if (w < n)
-    {
-      idx0 = d.cwork[w];
-      push = entry_near(d, idx0);
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, push);
-    int wb = 0;
-    if (lane == 0 && m) wb = atomicAdd(&qn, __popc(m));
-    wb = __shfl_sync(0xffffffffu, wb, 0);
-    if (push) queue[wb + __popc(m & ((1u << lane) - 1u))] = idx0;
-    __syncthreads();
-    if (qn >= TPB)
-    {
-      contact_entry<GEOM, ADAPT>(d, queue[threadIdx.x], step, obsc);
-      __syncthreads();
-      const int rest = qn - TPB;
-      const int moved = threadIdx.x < rest ? queue[TPB + threadIdx.x] : 0;
-      __syncthreads();
-      if (threadIdx.x < rest) queue[threadIdx.x] = moved;
-      if (threadIdx.x == 0) qn = rest;
-      __syncthreads();
-    }
-  }
-  if (threadIdx.x < qn) contact_entry<GEOM, ADAPT>(d, queue[threadIdx.x], step, obsc);
 }
 
 template <bool ADAPT>
