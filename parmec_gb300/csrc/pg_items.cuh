@@ -800,15 +800,6 @@ __device__ bool rebuild_all(const PgDev &d, int passes, int epasses, RebuildSmem
   if (!grid_barrier(d)) return false;
   for (int p = g0; p < P; p += gsz) rb_soff_item(d, p);
   if (g0 == 0) { d.soff[P] = 0; rb_meta_item(d); }
-  if (d.cwork)
-  {
-    // the FP64 contact evaluation's work list until the next rebuild: every
-    // candidate entry, in emit order (spheres in particle order, each
-    // sphere's entries in list order)
-    const int n = d.eoff[E];
-    for (int e = g0; e < n; e += gsz) d.cwork[e] = d.sval[0][e];
-    if (g0 == 0) *d.cwork_n = n;
-  }
   if (!grid_barrier(d)) return false;
   if (!grid_scan(d, d.soff, P + 1, (int *)d.sbs, (int *)sm.part)) return false;
   if (d.smeta[4] <= PG_SLAVE_PLACE_MAX)

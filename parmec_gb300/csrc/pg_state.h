@@ -123,7 +123,7 @@ struct PgDev
   double *npnt[3];          // [kn][ellnum]: contact point
   double *nen;              // [kn][ellnum]: normal damping of the pair, damper*2*sqrt(kn*m) (FP64 session)
   double *nnrm[3], *ndep;   // normal and depth (depth: parity exports only)
-  int *cwork, *cwork_n;     // [kn][ellnum] work list of the FP64 contact evaluation (every candidate entry, made by the rebuild), and its length
+  int *cwork, *cwork_n;     // [kn][ellnum] work queue of the FP64 contact evaluation, and its length
   int record_geometry;
   double *fm[3], *tm[3];    // [parnum] master-side partial force and torque sums
   int kr;                   // (unused: slave lists have no per-particle limit)

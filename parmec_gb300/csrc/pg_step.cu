@@ -524,23 +524,85 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
   }
 }
 
-// ---------------------------------------------------------------- contacts in two passes
+// ---------------------------------------------------------------- contacts in three passes
 // The same evaluation as k_contacts, split so that the FP64 work runs on
 // full warps: one thread per sphere walks a list whose active contacts sit
 // at different slots, so its warp's FP64 instructions ran with a fraction of
 // the lanes.
-//   k_contacts_eval   one thread per candidate entry (a grid-stride loop
-//                     over the work list the rebuild leaves in cwork: every
-//                     entry, spheres in particle order, each list in order):
-//                     geometry, the creation/persistence rule, contact
-//                     velocities and the granular law, written to the slot;
-//                     an entry apart ends an existing contact;
+//   k_contacts_probe  one thread per sphere: the squared-distance test of
+//                     every sphere candidate; a candidate clearly apart is
+//                     settled there (an existing contact ends), every other
+//                     slot goes to the work queue (one atomic per warp);
+//   k_contacts_eval   one thread per queued slot (a grid-stride loop over
+//                     the queue): geometry, the creation/persistence rule,
+//                     contact velocities and the granular law, written to
+//                     the slot;
 //   k_contacts_sum    one thread per sphere: the master-side force, torque
 //                     and (adaptive) stiffness sums over its slots in slot
 //                     order, as k_contacts sums them.
 // Every slot takes the same operations as in k_contacts and the sums the
-// same order, so the results are the same bits; the list's order plays no
+// same order, so the results are the same bits; the queue's order plays no
 // part.
+__device__ __forceinline__ void queue_push(int *work, int *count, bool push, int idx)
+{
+  const unsigned m = __ballot_sync(__activemask(), push);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(__activemask(), base, leader);
+  if (push) work[base + __popc(m & ((1u << lane) - 1u))] = idx;
+}
+
+__global__ void __launch_bounds__(TPB) k_contacts_probe(PgDev d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = i < d.ellnum ? d.ncnt[i] : 0;
+  double c[3] = {0.0, 0.0, 0.0}, ri = 0.0;
+  if (cnt > 0)
+  {
+    c[0] = d.center[0][i]; c[1] = d.center[1][i]; c[2] = d.center[2][i];
+    ri = d.radii[0][i];
+  }
+  // every lane of the warp takes part in each round's vote
+  int kmax = cnt;
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    const int other = __shfl_xor_sync(0xffffffffu, kmax, o);
+    kmax = other > kmax ? other : kmax;
+  }
+  for (int k = 0; k < kmax; k ++)
+  {
+    bool push = false;
+    size_t idx = 0;
+    if (k < cnt)
+    {
+      idx = (size_t)k * d.estride + i;
+      const int code = d.ncode[idx];
+      push = true;
+      if (code >= 0)
+      {
+        double q[3];
+        q[0] = c[0]-d.center[0][code];
+        q[1] = c[1]-d.center[1][code];
+        q[2] = c[2]-d.center[2][code];
+        const double d2 = dot3(q, q);
+        const double sr = ri+d.radii[0][code];
+        if (d2 > (sr*sr) * (1.0 + 1e-12))
+        {
+          push = false;
+          if (d.nflag[idx])
+          {
+            d.nflag[idx] = 0;
+            d.nstate[0][idx] = 0.0; d.nstate[1][idx] = 0.0; d.nstate[2][idx] = 0.0;
+          }
+        }
+      }
+    }
+    queue_push(d.cwork, d.cwork_n, push, (int)idx);
+  }
+}
+
 template <bool GEOM, bool ADAPT>
 __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
 {
@@ -552,13 +614,18 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
     const int idx0 = d.cwork[w];
     const size_t idx = (size_t)idx0;
     const int i = idx0 % d.estride;
-    // an entry past its sphere's list (a range whose lists restarted since
-    // the list was made) is no longer a candidate
-    if (idx0 / d.estride >= d.ncnt[i]) continue;
     const int pi = d.part[i];
-    double c[3];
-    for (int k = 0; k < 3; k ++) c[k] = d.center[k][i];
+    double x[3], v[3], oi[3], c[3];
+    for (int k = 0; k < 3; k ++)
+    {
+      x[k] = d.position[k][pi];
+      v[k] = d.linear[k][pi];
+      oi[k] = d.angular[3+k][pi];
+      c[k] = d.center[k][i];
+    }
     const double ri = d.radii[0][i];
+    const int coli = d.ellcol[i];
+    const double invmi = d.invm[pi], massi = d.mass[pi];
     const int code = d.ncode[idx];
     const bool existing = d.nflag[idx] != 0;
     double point[3], normal[3], depth = 0.0, q[3], len = 0.0;
@@ -613,16 +680,6 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
       }
       continue;
     }
-    // the rest of sphere i's state, for the contacts that are active
-    double x[3], v[3], oi[3];
-    for (int k = 0; k < 3; k ++)
-    {
-      x[k] = d.position[k][pi];
-      v[k] = d.linear[k][pi];
-      oi[k] = d.angular[3+k][pi];
-    }
-    const int coli = d.ellcol[i];
-    const double invmi = d.invm[pi], massi = d.mass[pi];
     if (sphere)
     {
       double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
@@ -2367,7 +2424,9 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   if (!d.ellnum) return;
   if (d.cwork && d.cwork_n)
   {
-    // two passes (evaluation over the rebuild's work list, sums): the same bits as k_contacts
+    // three passes (probe, queued evaluation, sums): the same bits as k_contacts
+    cudaMemsetAsync(d.cwork_n, 0, sizeof(int), s);
+    k_contacts_probe<<<nblk(d.ellnum), TPB, 0, s>>>(d);
     const int nb = eval_blocks();
     if (d.hs)
     {
@@ -2392,13 +2451,13 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   else k_contacts<false, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
 }
 
-// the FP64 form evaluates the lists in two passes (one when no work list
+// the FP64 form evaluates the lists in three passes (one when no work queue
 // is allocated); the mixed form in a sphere and a triangle pass (pg_mixed.cu)
 int pg_contacts_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
   if (d.form == PG_FORM_MIXED) return 2;
-  return (d.cwork && d.cwork_n) ? 2 : 1;
+  return (d.cwork && d.cwork_n) ? 3 : 1;
 }
 
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
