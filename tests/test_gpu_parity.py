@@ -103,3 +103,29 @@ def test_graph_and_stream_launches_identical(gpu_lib):
         m.dem(80 * dt, dt, interval=1e9, engine=GpuEngine(graph=graph))
         out.append(m)
     assert_bitwise(out[0], out[1])
+
+
+def test_run_async_equals_run(gpu_lib):
+    """pg_session_run_async enqueues the same steps as pg_session_run: after
+    pg_session_sync the state is the same bits; the step tables may be
+    rebuilt on the host while the steps run."""
+    from parmec_gb300 import driver
+    from parmec_gb300.engine import GpuEngine
+    out = []
+    for asynchronous in (False, True):
+        m, dt = make_collision_scene(n_side=5, seed=37, moving=True)
+        eng = GpuEngine()
+        m.dem(10 * dt - 0.5 * dt, dt, interval=1e9, engine=eng)
+        times, end = driver.step_times(m.curtime, 50 * dt - 0.5 * dt, dt)
+        tabs = driver.StepTables(m, times, dt, [1e9, 1e9], [None, None], [-1, -1])
+        tab = tabs.ctab(0, len(times))
+        if asynchronous:
+            eng.run_async(tab, dt)
+            tabs = driver.StepTables(m, times, dt, [1e9, 1e9], [None, None], [-1, -1])   # host work meanwhile
+            eng.sync()
+        else:
+            eng.run(tab, dt)
+        m.curtime = end
+        eng.download()
+        out.append(m)
+    assert_bitwise(out[0], out[1])
