@@ -180,8 +180,12 @@ class GpuEngine:
         d = np.ascontiguousarray(dims, dtype=np.int32)
         abi.check(self.lib.pg_session_set_grid(self.sess, float(cell), abi.iptr(d)), "pg_session_set_grid")
 
-    def upload_range(self, r):
-        self.scene_refresh()
+    def upload_range(self, r, refresh=True):
+        """Upload pool ranges r (pg_session_upload_range); refresh=False keeps
+        the scene structure of the last call, for a model whose arrays are
+        the same objects (a serving pool's)."""
+        if refresh or self.scene is None:
+            self.scene_refresh()
         rr = np.ascontiguousarray(r, dtype=np.int32)
         abi.check(self.lib.pg_session_upload_range(self.sess, ctypes.byref(self.scene), abi.iptr(rr)),
                   "pg_session_upload_range")

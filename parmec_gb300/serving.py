@@ -208,7 +208,7 @@ class Server:
         e0, e1, _, _, t0, t1, _, _ = r
         self.P.pscene[e0:e1] = slot
         self.P.tscene[t0:t1] = slot
-        self.eng.upload_range(r)
+        self.eng.upload_range(r, refresh=False)      # the pool's arrays never move
         lo = m.E.center[0:3, :m.parnum].min(axis=1)
         self.eng.set_scene(slot, True, origin=lo - 4.0 * self.cell, excitation=req.excitation, start=-1)
 
