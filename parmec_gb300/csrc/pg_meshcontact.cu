@@ -204,7 +204,6 @@ __global__ void __launch_bounds__(TPB) k_tt_cull(PgDev d, PgTT g, int np)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   bool near = false;
-  int cls = 0;
   if (k < np)
   {
     double va[3][3], vb[3][3];
@@ -217,51 +216,24 @@ __global__ void __launch_bounds__(TPB) k_tt_cull(PgDev d, PgTT g, int np)
       g.act[k] = 0;
       for (int c = 0; c < 3; c ++) { g.st[c][k] = 0.0; g.f[c][k] = 0.0; g.p[c][k] = 0.0; }
     }
-    else
-    {
-      // the pair's class: the angle between the two planes, in quarters of
-      // |cos| (FP32; it only groups pairs whose narrow phases take alike
-      // branches, so that a warp evaluates alike pairs)
-      float e1[3], e2[3], f1[3], f2[3];
-      for (int c = 0; c < 3; c ++)
-      {
-        e1[c] = (float)(va[1][c] - va[0][c]); e2[c] = (float)(va[2][c] - va[0][c]);
-        f1[c] = (float)(vb[1][c] - vb[0][c]); f2[c] = (float)(vb[2][c] - vb[0][c]);
-      }
-      const float na[3] = {e1[1]*e2[2] - e1[2]*e2[1], e1[2]*e2[0] - e1[0]*e2[2], e1[0]*e2[1] - e1[1]*e2[0]};
-      const float nb[3] = {f1[1]*f2[2] - f1[2]*f2[1], f1[2]*f2[0] - f1[0]*f2[2], f1[0]*f2[1] - f1[1]*f2[0]};
-      const float dn = fabsf(na[0]*nb[0] + na[1]*nb[1] + na[2]*nb[2]);
-      const float ln = sqrtf((na[0]*na[0] + na[1]*na[1] + na[2]*na[2]) * (nb[0]*nb[0] + nb[1]*nb[1] + nb[2]*nb[2]));
-      const float cs = ln > 0.0f ? dn / ln : 0.0f;
-      cls = cs >= 0.75f ? 3 : (cs >= 0.5f ? 2 : (cs >= 0.25f ? 1 : 0));
-    }
   }
-  // warp-aggregated push of the near pairs into their class's queue
-  for (int q = 0; q < PG_TT_CLASSES; q ++)
-  {
-    const bool push = near && cls == q;
-    const unsigned m = __ballot_sync(0xffffffffu, push);
-    if (!m) continue;
-    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&g.qn[q], __popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (push) g.queue[(size_t)q * g.cap + base + __popc(m & ((1u << lane) - 1u))] = k;
-  }
+  // warp-aggregated push of the near pairs
+  const unsigned m = __ballot_sync(0xffffffffu, near);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(g.qn, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (near) g.queue[base + __popc(m & ((1u << lane) - 1u))] = k;
 }
 
 // 5b. contact and granular force of each queued pair
 __global__ void __launch_bounds__(TPB) k_tt_pairs(PgDev d, PgTT g, double step)
 {
-  int qoff[PG_TT_CLASSES + 1];
-  qoff[0] = 0;
-  for (int q = 0; q < PG_TT_CLASSES; q ++) qoff[q + 1] = qoff[q] + g.qn[q];
-  const int nq = qoff[PG_TT_CLASSES];
+  const int nq = *g.qn;
   for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nq; w += gridDim.x * blockDim.x)
   {
-  int q = 0;
-  while (w >= qoff[q + 1]) q ++;
-  const int k = g.queue[(size_t)q * g.cap + (w - qoff[q])];
+  const int k = g.queue[w];
   const int f = g.pf[k], u = g.pu[k];
   double va[3][3], vb[3][3];
   tri_vertices(d, f, va);
@@ -447,7 +419,7 @@ void pg_tt_forces(const PgDev &d, PgTT &g, cudaStream_t s, int np, double step)
   if (np > 0)
   {
     k_tt_emit<<<nblk(T), TPB, 0, s>>>(d, g);
-    cudaMemsetAsync(g.qn, 0, PG_TT_CLASSES * sizeof(int), s);
+    cudaMemsetAsync(g.qn, 0, sizeof(int), s);
     k_tt_cull<<<nblk(np), TPB, 0, s>>>(d, g, np);
     k_tt_pairs<<<pairs_blocks(), TPB, 0, s>>>(d, g, step);
     k_tt_entries<<<nblk(np), TPB, 0, s>>>(d, g, np);

@@ -25,7 +25,7 @@ struct PgTT
   int cap = 0;                    // pair capacity
   int np_last = 0;                // pairs of the last step
   int *pf = nullptr, *pu = nullptr;         // [cap] finder and partner of each pair
-  int *queue = nullptr, *qn = nullptr;      // [PG_TT_CLASSES][cap] pairs not plainly apart, by class; counts
+  int *queue = nullptr, *qn = nullptr;      // [cap] pairs that are not plainly apart, their count
   unsigned char *act = nullptr;
   double *st[3] = {}, *f[3] = {}, *p[3] = {};   // tangential state, force on the finder's particle, point
   // the previous step's pairs (state carried by (finder, partner))
@@ -42,7 +42,6 @@ struct PgTT
 };
 
 #define PG_TT_CHUNK 1024          // entries one warp sums into one chunk sum
-#define PG_TT_CLASSES 4           // classes of near pairs (angle between their planes)
 
 int pg_tt_key_bits(int ncells);
 void pg_tt_find(const PgDev &d, PgTT &g, cudaStream_t s);                 // steps 1-4a; total in g.np_dev

@@ -1096,7 +1096,7 @@ int tt_stage(pg_session *s, double step)
     int *pf = nullptr, *pu = nullptr; unsigned char *act = nullptr; double *st[3] = {}, *f[3] = {}, *p[3] = {};
     int *queue = nullptr;
     TRY(dalloc(s, &pf, cap)); TRY(dalloc(s, &pu, cap)); TRY(dalloc(s, &act, cap)); TRY(dalloc(s, &ppu, cap));
-    TRY(dalloc(s, &queue, (size_t)PG_TT_CLASSES * cap));
+    TRY(dalloc(s, &queue, cap));
     TRY(dalloc(s, &pact, cap));
     for (int c = 0; c < 3; c ++)
     {
@@ -1664,7 +1664,7 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
     TRY(dalloc(s, &g.nch, P));
     TRY(dalloc(s, &g.choff, (size_t)P + 1));
     TRY(dalloc(s, &g.nchunks, 1));
-    TRY(dalloc(s, &g.qn, PG_TT_CLASSES));
+    TRY(dalloc(s, &g.qn, 1));
     for (int c = 0; c < 3; c ++) { TRY(dalloc(s, &d.ttF[c], P)); TRY(dalloc(s, &d.ttT[c], P)); }
   }
   release(s, g.cstart);
