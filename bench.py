@@ -11,9 +11,11 @@ steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 N > 1 (under torchrun) runs independent replicas, one per GPU ("replicas
-only": scenes do not exchange data), and reports the aggregate.
---impl reference times the CPU restatement of the reference's ISPC path
-(the reference itself cannot be built: no ispc) on all host cores.
+only": scenes do not exchange data), and reports the aggregate: every
+rank's particle-steps over the slowest rank's time.
+--impl reference times the reference's own hot path on all host cores: its
+ISPC sources translated to C++ at gang size one (oracle/ispc_ref.py; the
+ispc compiler is not installed), driven by parmec.cpp's dem() call sequence.
 """
 import argparse
 import json
@@ -31,6 +33,22 @@ import numpy as np  # noqa: E402
 
 WORKLOAD = ("rotating drum: 1,048,576 spheres, radii log-uniform [0.5,2] mm, 4,096-triangle cylinder "
             "R=0.5 m L=0.3 m at 2 rad/s, GRANULAR kn=1e6 damping 0.2 friction 0.3, dt=0.1 critical")
+
+
+def max_over_ranks(x, dist, device):
+    """The largest x over the ranks (a job's time is its slowest rank's);
+    x itself without a process group."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank, world, seconds):
+    """Whole-job throughput: the units every rank processed over the job's time."""
+    return units_per_rank * world / seconds
 
 
 def env_int(name, default):
@@ -513,11 +531,8 @@ def main():
     clk = clocks.stop()
     launches = eng.kernel_launches() - launches0
     m.curtime = end_time
-    el_ms = ev0.elapsed_time(ev1)
+    el_ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     if dist:
-        t = torch.tensor([el_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_ms = float(t.item())
         dist.barrier()
     # FP64 reference state after W + K steps, for the mixed form's error report
     eng.download()
@@ -560,11 +575,7 @@ def main():
             print(json.dumps({"e2e_failure_diagnostics": eng.diagnostics()}), file=sys.stderr)
             raise
         e2e_runs.append(time.perf_counter() - t0)
-    e2e_s = float(np.median(e2e_runs))
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(float(np.median(e2e_runs)), dist, "cuda")
     up, down = state_bytes(m)
 
     if rank != 0:
@@ -572,8 +583,7 @@ def main():
             dist.destroy_process_group()
         return 0
 
-    total_ps = m.parnum * args.steps * world
-    value = total_ps / (el_ms * 1e-3)
+    value = job_value(m.parnum * args.steps, world, el_ms * 1e-3)
     hbm, peak_kind = peaks()
     # roofline of the dominant kernel group: the step's compulsory bytes per
     # particle, B = 420 + 56 c (c = contact pairs per particle, measured on
@@ -615,7 +625,7 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": arm_config(args, info, world),
         "contacts_per_particle": round(c_pair, 3),
-        "e2e": {"value": m.parnum * args.steps * world / e2e_s, "unit": "particle-steps/s",
+        "e2e": {"value": job_value(m.parnum * args.steps, world, e2e_s), "unit": "particle-steps/s",
                 "h2d_bytes_per_step": up // args.steps, "d2h_bytes_per_step": down // args.steps,
                 "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
                         "full host->device upload, K steps, device->host download; host SoA arrays "
