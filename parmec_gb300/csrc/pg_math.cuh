@@ -14,8 +14,16 @@ PG_DEV double dot3(const double *a, const double *b) { return a[0]*b[0] + a[1]*b
 
 // Comparisons on the integer pipe.  GB300 issues FP64 instructions, DSETP
 // included, at 2 lanes per clock per SM; these give the truth values of the
-// FP64 comparisons they stand for, from the bit patterns.
-PG_DEV unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+// FP64 comparisons they stand for, from the bit patterns.  The bits are
+// taken by a move the compiler cannot see through: with a plain bitcast it
+// folds tests such as "bits << 1 != 0" or "exponent != 0x7ff" back into
+// FP64 comparisons (DSETP), which issue on the FP64 pipe again.
+PG_DEV unsigned long long dbits(double x)
+{
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
 PG_DEV bool nan_bits(unsigned long long b) { return (b & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
 PG_DEV bool finite_d(double x) { return ((dbits(x) >> 52) & 0x7ff) != 0x7ff; }
 // x != 0.0 (true for NaN, as the FP64 comparison)
@@ -26,6 +34,21 @@ PG_DEV bool gt_nonneg(double a, double b)
 {
   const unsigned long long ua = dbits(a), ub = dbits(b);
   return !nan_bits(ua) && !nan_bits(ub) && ua > ub;
+}
+// x < 0.0 and x > 0.0: false for NaN and for either zero
+PG_DEV bool lt_zero_d(double x) { return dbits(x) - 0x8000000000000001ULL < 0x7ff0000000000000ULL; }
+PG_DEV bool gt_zero_d(double x) { return dbits(x) - 1ULL < 0x7ff0000000000000ULL; }
+// the IEEE order of non-NaN values as unsigned order, -0 and +0 one key
+PG_DEV unsigned long long order_key(unsigned long long b)
+{
+  if ((b << 1) == 0) b = 0;
+  return (long long)b < 0 ? ~b : b | 0x8000000000000000ULL;
+}
+// a > b for any a and b (false when either is NaN)
+PG_DEV bool gt_d(double a, double b)
+{
+  const unsigned long long ua = dbits(a), ub = dbits(b);
+  return !nan_bits(ua) && !nan_bits(ub) && order_key(ua) > order_key(ub);
 }
 
 // NVMUL: C = A*B, A column-major 3x3

@@ -89,23 +89,23 @@ __global__ void k_excite(PgDev d, double step)
 __device__ __forceinline__ void set_piso(const PgDev &d, int i)
 {
   if (!d.piso) return;
-  const long long j = __double_as_longlong(d.inertia[0][i]), ij = __double_as_longlong(d.inverse[0][i]);
-  bool iso = __double_as_longlong(d.inertia[4][i]) == j && __double_as_longlong(d.inertia[8][i]) == j &&
-             __double_as_longlong(d.inverse[4][i]) == ij && __double_as_longlong(d.inverse[8][i]) == ij;
+  const unsigned long long j = dbits(d.inertia[0][i]), ij = dbits(d.inverse[0][i]);
+  bool iso = dbits(d.inertia[4][i]) == j && dbits(d.inertia[8][i]) == j &&
+             dbits(d.inverse[4][i]) == ij && dbits(d.inverse[8][i]) == ij;
   const int off[6] = {1, 2, 3, 5, 6, 7};
   for (int k = 0; k < 6; k ++)
-    iso = iso && __double_as_longlong(d.inertia[off[k]][i]) == 0 && __double_as_longlong(d.inverse[off[k]][i]) == 0;
+    iso = iso && dbits(d.inertia[off[k]][i]) == 0 && dbits(d.inverse[off[k]][i]) == 0;
   d.piso[i] = iso ? 1 : 0;
 }
 
-__device__ __forceinline__ bool finite_bits(double x) { return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff; }
+__device__ __forceinline__ bool finite_bits(double x) { return finite_d(x); }
 
 // p + 0*a + 0*b as the full product sums them, for finite a and b
 __device__ __forceinline__ double zero_terms(double p, double a, double b)
 {
-  const long long bp = __double_as_longlong(p);
+  const long long bp = (long long)dbits(p);
   if ((bp << 1) != 0) return p;
-  const bool neg = bp < 0 && __double_as_longlong(a) < 0 && __double_as_longlong(b) < 0;
+  const bool neg = bp < 0 && (long long)dbits(a) < 0 && (long long)dbits(b) < 0;
   return __longlong_as_double(neg ? (long long)0x8000000000000000ull : 0ll);
 }
 
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
         q[2] = c[2]-cj[2];
         const double d2 = dot3(q, q);
         const double sr = ri+d.radii[0][j];
-        apart = d2 > (sr*sr) * (1.0 + 1e-12);
+        apart = gt_nonneg(d2, (sr*sr) * (1.0 + 1e-12));
         if (!apart)
         {
           len = sqrt(d2);
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
         q[1] = c[1]-point[1];
         q[2] = c[2]-point[2];
         const double d2 = dot3(q, q);
-        apart = d2 > (ri*ri) * (1.0 + 1e-12);
+        apart = gt_nonneg(d2, (ri*ri) * (1.0 + 1e-12));
         if (!apart)
         {
           len = sqrt(d2);
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
         pj = d.triobs[t];
         colj = d.tricol[t];
       }
-      const bool active = !apart && (existing ? !(depth < 0.0) : (depth > 0.0));
+      const bool active = !apart && (existing ? !lt_zero_d(depth) : gt_zero_d(depth));
       if (!active)
       {
         if (existing)
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       }
       if (cjp)
       {
-        double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
+        double ilen = existing ? 1.0/len : (gt_zero_d(len) ? 1.0/len : 1.0);
         point[0] = 0.5*(c[0]+cj[0]);
         point[1] = 0.5*(c[1]+cj[1]);
         point[2] = 0.5*(c[2]+cj[2]);
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
       ft[2] = kt*state[2] + et*vt[2];
       double flen = sqrt(dot3(ft, ft));
       double lim = mus*fn;
-      if (flen > lim)
+      if (gt_d(flen, lim))
       {
         lim = mud*fn/flen;
         ft[0] *= lim;
@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(TPB) k_contacts_probe(PgDev d)
         q[2] = c[2]-d.center[2][code];
         const double d2 = dot3(q, q);
         const double sr = ri+d.radii[0][code];
-        if (d2 > (sr*sr) * (1.0 + 1e-12))
+        if (gt_nonneg(d2, (sr*sr) * (1.0 + 1e-12)))
         {
           push = false;
           if (d.nflag[idx])
@@ -644,7 +644,7 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
       q[2] = c[2]-cj[2];
       const double d2 = dot3(q, q);
       const double sr = ri+d.radii[0][j];
-      apart = d2 > (sr*sr) * (1.0 + 1e-12);
+      apart = gt_nonneg(d2, (sr*sr) * (1.0 + 1e-12));
       if (!apart)
       {
         len = sqrt(d2);
@@ -661,7 +661,7 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
       q[1] = c[1]-point[1];
       q[2] = c[2]-point[2];
       const double d2 = dot3(q, q);
-      apart = d2 > (ri*ri) * (1.0 + 1e-12);
+      apart = gt_nonneg(d2, (ri*ri) * (1.0 + 1e-12));
       if (!apart)
       {
         len = sqrt(d2);
@@ -670,7 +670,7 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
       pj = d.triobs[t];
       colj = d.tricol[t];
     }
-    const bool active = !apart && (existing ? !(depth < 0.0) : (depth > 0.0));
+    const bool active = !apart && (existing ? !lt_zero_d(depth) : gt_zero_d(depth));
     if (!active)
     {
       if (existing)
@@ -682,7 +682,7 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
     }
     if (sphere)
     {
-      double ilen = existing ? 1.0/len : (len > 0.0 ? 1.0/len : 1.0);
+      double ilen = existing ? 1.0/len : (gt_zero_d(len) ? 1.0/len : 1.0);
       point[0] = 0.5*(c[0]+cj[0]);
       point[1] = 0.5*(c[1]+cj[1]);
       point[2] = 0.5*(c[2]+cj[2]);
@@ -775,7 +775,7 @@ __global__ void PG_LB_EVAL k_contacts_eval(PgDev d, double step)
     ft[2] = kt*state[2] + et*vt[2];
     double flen = sqrt(dot3(ft, ft));
     double lim = mus*fn;
-    if (flen > lim)
+    if (gt_d(flen, lim))
     {
       lim = mud*fn/flen;
       ft[0] *= lim;
