@@ -391,7 +391,7 @@ def serving_form(args, count):
            "requests_built_s": t_gen}
     energies = {}
     for form, key in ((abi.PG_FORM_MIXED, "mixed_pool"), (abi.PG_FORM_FP64, "fp64_pool")):
-        srv = Server(reqs[0].model, reqs[0].dt, form=form, budget_bytes=150e9, max_scenes=256,
+        srv = Server(reqs[0].model, reqs[0].dt, form=form, budget_bytes=150e9, max_scenes=args.scene_slots,
                      max_scene_extent=4.0)
         torch.cuda.synchronize()
         res, st = srv.serve(reqs, realtime=True)
@@ -474,6 +474,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=512, help="scenes of the batched leg")
     ap.add_argument("--serving", type=int, default=500, help="requests in the serving stream (0: skip)")
+    ap.add_argument("--scene-slots", type=int, default=256,
+                    help="scene slots of each serving pool (the 150 GB budget bounds its spheres)")
     ap.add_argument("--lattice", type=int, default=256, help="side of the spring lattice (0: skip)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -432,6 +432,11 @@ int pg_session_upload_range(pg_session *s, const pg_scene *scene, const int rang
 /* Copy the same ranges of the dynamic state back to the host scene. */
 int pg_session_download_range(pg_session *s, pg_scene *scene, const int range[8]);
 
+/* The motion state of the particle range alone (position, linear and angular
+ * velocity rows): what a finished request of a serving pool hands back.  The
+ * scene's other host arrays are left as they were. */
+int pg_session_download_range_motion(pg_session *s, pg_scene *scene, const int range[8]);
+
 /* Free the same ranges in a pool: their particles, spheres, triangles and
  * obstacles get scene id -1, which every kernel skips, and the spheres'
  * candidate lists restart empty.  Only device scene ids change: the state

@@ -179,6 +179,7 @@ def load_library():
         "pg_session_scene": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, D, D, ctypes.c_longlong]),
         "pg_session_upload_range": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I]),
         "pg_session_download_range": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I]),
+        "pg_session_download_range_motion": (ctypes.c_int, [P, ctypes.POINTER(PgScene), I]),
         "pg_session_release_range": (ctypes.c_int, [P, I]),
         "pg_session_global_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
         "pg_session_use_graph": (ctypes.c_int, [P, ctypes.c_int]),

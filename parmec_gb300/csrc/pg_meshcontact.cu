@@ -51,11 +51,16 @@ __device__ __forceinline__ void tri_vertices(const PgDev &d, int t, double v[3][
     for (int c = 0; c < 3; c ++) v[a][c] = d.tri[3*a + c][t];
 }
 
-__device__ __forceinline__ bool boxes_overlap(const PgTT &g, int t, int u)
+// box keys: lo < hi on the keys is the FP64 comparison lo < hi
+__device__ __forceinline__ unsigned long long lo_key(double x)
 {
-  for (int c = 0; c < 3; c ++)
-    if (!(g.box[c][t] < g.box[3+c][u] && g.box[c][u] < g.box[3+c][t])) return false;
-  return true;
+  const unsigned long long b = pgtt::bits(x);
+  return pgtt::nan_b(b) ? ~0ULL : pgtt::okey(b);
+}
+__device__ __forceinline__ unsigned long long hi_key(double x)
+{
+  const unsigned long long b = pgtt::bits(x);
+  return pgtt::nan_b(b) ? 0ULL : pgtt::okey(b);
 }
 
 // 1. boxes and cell keys
@@ -75,8 +80,8 @@ __global__ void __launch_bounds__(TPB) k_tt_keys(PgDev d, PgTT g)
       h = h > e ? h : e;
       lo[c] = l - g.r;
       hi[c] = h + g.r;
-      g.box[c][t] = lo[c];
-      g.box[3+c][t] = hi[c];
+      g.box[c][t] = lo_key(lo[c]);
+      g.box[3+c][t] = hi_key(hi[c]);
     }
     if (g.big[t]) key = (unsigned)g.ncells;
     else
@@ -90,6 +95,7 @@ __global__ void __launch_bounds__(TPB) k_tt_keys(PgDev d, PgTT g)
       }
       key = (unsigned)((ix[2]*g.dim[1] + ix[1])*g.dim[0] + ix[0]);
     }
+    g.cell[t] = (int)key;
   }
   g.keys[0][t] = key;
   g.vals[0][t] = t;
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(TPB) k_tt_find(PgDev d, PgTT g)
   {
     const int owner = d.triobs[t];
     const bool big = g.big[t] != 0;
-    double lo[3], hi[3];
+    unsigned long long lo[3], hi[3];
     for (int c = 0; c < 3; c ++) { lo[c] = g.box[c][t]; hi[c] = g.box[3+c][t]; }
     auto take = [&](int u) {
       if (u == t || !mesh_tri(d, u) || d.triobs[u] == owner) return;
@@ -135,12 +141,8 @@ __global__ void __launch_bounds__(TPB) k_tt_find(PgDev d, PgTT g)
     };
     if (!big)
     {
-      int ix[3];
-      for (int c = 0; c < 3; c ++)
-      {
-        const double q = floor((0.5*(g.box[c][t] + g.box[3+c][t]) - g.org[c]) / g.h);
-        ix[c] = q < 0.0 ? 0 : (q > (double)(g.dim[c]-1) ? g.dim[c]-1 : (int)q);
-      }
+      const int cell = g.cell[t];
+      const int ix[3] = {cell % g.dim[0], (cell / g.dim[0]) % g.dim[1], cell / (g.dim[0] * g.dim[1])};
       for (int z = ix[2]-1; z <= ix[2]+1; z ++)
       {
         if (z < 0 || z >= g.dim[2]) continue;

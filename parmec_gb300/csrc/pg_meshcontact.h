@@ -16,7 +16,11 @@ struct PgTT
   int passes = 2, epasses = 2;    // radix-sort passes of the two sorts
   int kmax = PG_TT_KMAX;          // partners one triangle may find
   unsigned char *big = nullptr;   // [trinum] 1: larger than a cell
-  double *box[6] = {};            // [trinum] box widened by r: min xyz, max xyz
+  // [trinum] box widened by r, as keys whose unsigned order is the IEEE
+  // order of the coordinates (-0 = +0): min xyz (NaN: above every key),
+  // max xyz (NaN: 0), so that a NaN fails every overlap test
+  unsigned long long *box[6] = {};
+  int *cell = nullptr;            // [trinum] grid cell of a small triangle's box centre
   unsigned *keys[2] = {}; int *vals[2] = {}; unsigned *hist = nullptr;
   int *cstart = nullptr, *cend = nullptr;   // [ncells + 1]: the last range holds the big triangles
   int *cand = nullptr;            // [kmax][trinum] partners found, sorted

@@ -1652,6 +1652,7 @@ int pg_session_mesh_contact(pg_session *s, double radius, double cell, const uns
   {
     TRY(dalloc(s, &g.big, T));
     for (int c = 0; c < 6; c ++) TRY(dalloc(s, &g.box[c], T));
+    TRY(dalloc(s, &g.cell, T));
     for (int k = 0; k < 2; k ++) { TRY(dalloc(s, &g.keys[k], T)); TRY(dalloc(s, &g.vals[k], T)); }
     TRY(dalloc(s, &g.hist, pg_sort_hist_len(T)));
     TRY(dalloc(s, &g.cand, (size_t)g.kmax * T));
@@ -1925,6 +1926,21 @@ int pg_session_download_range(pg_session *s, pg_scene *sc, const int range[8])
   Ranges r;
   TRY(ranges_of(s->d, range, &r));
   TRY(download_ranges(s, sc, r));
+  CK(cudaStreamSynchronize(s->stream));
+  int e = read_err(s);
+  return e ? e : PG_OK;
+}
+
+int pg_session_download_range_motion(pg_session *s, pg_scene *sc, const int range[8])
+{
+  if (!s || !sc) return PG_ERR_ARGUMENT;
+  Ranges r;
+  TRY(ranges_of(s->d, range, &r));
+  PgDev &d = s->d;
+  if (d.form == PG_FORM_MIXED) pg_launch_mx_to64(d, s->stream, (int)r.p0, (int)r.p1);
+  for (int k = 0; k < 6; k ++) TRY(d2hr(s, sc->angular[k], d.angular[k], r.p0, r.p1));
+  for (int k = 0; k < 3; k ++) TRY(d2hr(s, sc->linear[k], d.linear[k], r.p0, r.p1));
+  for (int k = 0; k < 6; k ++) TRY(d2hr(s, sc->position[k], d.position[k], r.p0, r.p1));
   CK(cudaStreamSynchronize(s->stream));
   int e = read_err(s);
   return e ? e : PG_OK;

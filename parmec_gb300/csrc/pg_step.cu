@@ -1478,14 +1478,35 @@ __global__ void k_restrain_forces(PgDev d, const int *first, const int *list, in
 // from d.hs.
 enum { INT_FUSED = 0, INT_FORCES = 1, INT_DYNAMICS = 2, INT_FORCES_ADAPT = 3, INT_DYN_FUSED = 4 };
 
+// F + m*g on the integer pipe when g is a zero and m and F are finite: m*g
+// is then a zero of sign sign(m) xor sign(g), and F plus a zero is F, except
+// that two zeros sum to -0 only when both are -0 (the gravity components of
+// a scene that are zero)
+__device__ __forceinline__ double add_times_zero(double F, double m, double g)
+{
+  const unsigned long long bg = dbits(g);
+  if ((bg << 1) != 0 || !finite_d(m) || !finite_d(F)) return F + m*g;
+  const unsigned long long bF = dbits(F);
+  if ((bF << 1) != 0) return F;
+  const bool neg = (bF >> 63) && ((dbits(m) ^ bg) >> 63);
+  return __longlong_as_double(neg ? (long long)0x8000000000000000ull : 0ll);
+}
+
+// half = step/2 and hstep = (step + step1)/2 come from the host (the same
+// IEEE operations), except where the step is chosen on the device
 template <int MODE>
-__global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double step1)
+__global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double half, double hstep)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
   constexpr bool ADAPT = MODE == INT_FORCES_ADAPT;
   constexpr bool FUSED = MODE == INT_FUSED || MODE == INT_DYN_FUSED;
-  if (MODE == INT_FORCES_ADAPT || MODE == INT_DYN_FUSED) { step = d.hs[0]; step1 = d.hs[1]; }
+  if (MODE == INT_FORCES_ADAPT || MODE == INT_DYN_FUSED)
+  {
+    step = d.hs[0];
+    half = 0.5*step;
+    hstep = 0.5*(step+d.hs[1]);
+  }
   if (i < d.parnum && d.pscene[i] >= 0 && d.sactive[d.pscene[i]])
   {
     const int row = *d.stepno;
@@ -1569,9 +1590,9 @@ __global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double step1)
         }
       }
     }
-    F[0] = F[0] + ma * grav[0];
-    F[1] = F[1] + ma * grav[1];
-    F[2] = F[2] + ma * grav[2];
+    F[0] = add_times_zero(F[0], ma, grav[0]);
+    F[1] = add_times_zero(F[1], ma, grav[1]);
+    F[2] = add_times_zero(F[2], ma, grav[2]);
     if (d.tt_on)
     {
       // mesh-mesh contacts (pg_meshcontact.cu), summed per particle beforehand
@@ -1753,8 +1774,6 @@ __global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double step1)
     double x[3] = {po[0], po[1], po[2]};
     if (!(d.flags[i] & PG_FLAG_SKIP))
     {
-      const double half = 0.5*step;
-      const double hstep = 0.5*(step+step1);
       for (int k = 0; k < 3; k ++) { O[k] = d.angular[k][i]; v[k] = d.linear[k][i]; }
       const bool iso = d.piso && d.piso[i];
       const double js = iso ? d.inertia[0][i] : 0.0, is = iso ? d.inverse[0][i] : 0.0;
@@ -2400,7 +2419,7 @@ void pg_launch_shapes(const PgDev &d, cudaStream_t s, bool skip_analytical)
 
 void pg_launch_obstacles_state(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.obsnum && d.trinum) k_obstacles<<<nblk(d.trinum), TPB, 0, s>>>(d, step, 0);
+  if (d.obsnum && d.trinum) k_obstacles<<<(d.trinum + 31) / 32, 32, 0, s>>>(d, step, 0);
   if (d.obsnum) k_tail<<<1, 32, 0, s>>>(d, step, 0);
 }
 
@@ -2498,22 +2517,22 @@ void pg_launch_spring_runs(const PgDev &d, cudaStream_t s)
 
 void pg_launch_integrate(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.parnum) k_integrate<INT_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, step, step);
+  if (d.parnum) k_integrate<INT_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, step, 0.5*step, 0.5*(step+step));
 }
 
 void pg_launch_force_sums(const PgDev &d, cudaStream_t s)
 {
-  if (d.parnum) k_integrate<INT_FORCES><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+  if (d.parnum) k_integrate<INT_FORCES><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0, 0.0);
 }
 
 void pg_launch_dynamics(const PgDev &d, cudaStream_t s, double step0, double step1)
 {
-  if (d.parnum) k_integrate<INT_DYNAMICS><<<nblk(d.parnum), TPB, 0, s>>>(d, step0, step1);
+  if (d.parnum) k_integrate<INT_DYNAMICS><<<nblk(d.parnum), TPB, 0, s>>>(d, step0, 0.5*step0, 0.5*(step0+step1));
 }
 
 void pg_launch_force_sums_adapt(const PgDev &d, cudaStream_t s)
 {
-  if (d.parnum) k_integrate<INT_FORCES_ADAPT><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+  if (d.parnum) k_integrate<INT_FORCES_ADAPT><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0, 0.0);
 }
 
 void pg_launch_adapt_step(const PgDev &d, cudaStream_t s)
@@ -2541,7 +2560,7 @@ void pg_launch_eqm_one(const PgDev &d, cudaStream_t s, int part2, const double *
 
 void pg_launch_dynamics_fused(const PgDev &d, cudaStream_t s)
 {
-  if (d.parnum) k_integrate<INT_DYN_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0);
+  if (d.parnum) k_integrate<INT_DYN_FUSED><<<nblk(d.parnum), TPB, 0, s>>>(d, 0.0, 0.0, 0.0);
 }
 
 void pg_launch_restrain_velocities(const PgDev &d, cudaStream_t s)
@@ -2562,7 +2581,9 @@ void pg_launch_mesh(const PgDev &d, cudaStream_t s)
 
 void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step)
 {
-  if (d.obsnum && d.trinum) k_obstacles<<<nblk(d.trinum), TPB, 0, s>>>(d, step, 1);
+  // one warp per block: a few thousand triangles then spread over most SMs,
+  // each triangle's update being a chain of FP64 work
+  if (d.obsnum && d.trinum) k_obstacles<<<(d.trinum + 31) / 32, 32, 0, s>>>(d, step, 1);
 }
 
 void pg_launch_excite(const PgDev &d, cudaStream_t s, double step)

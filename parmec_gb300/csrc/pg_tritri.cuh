@@ -17,6 +17,7 @@
 // contraction on both), which therefore evaluate the same operations.
 #pragma once
 #include <math.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define PG_TT __host__ __device__ __forceinline__
@@ -33,6 +34,43 @@ PG_TT void cross(const double *a, const double *b, double *c)
   c[0] = a[1]*b[2] - a[2]*b[1];
   c[1] = a[2]*b[0] - a[0]*b[2];
   c[2] = a[0]*b[1] - a[1]*b[0];
+}
+
+// Comparisons taken from the bit patterns, on the integer pipe of the
+// device (the FP64 pipe, which issues comparisons too, is the narrow one);
+// each gives the truth value of the IEEE comparison it stands for, NaN
+// operands included.  On the device the bits are taken by a move the
+// compiler cannot fold back into an FP64 comparison.  The plane test and
+// the box keys of the candidate search use them; in the narrow phase, whose
+// branches they reshape, plain comparisons measured faster.
+PG_TT unsigned long long bits(double x)
+{
+  unsigned long long b;
+#ifdef __CUDA_ARCH__
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+#else
+  memcpy(&b, &x, sizeof b);
+#endif
+  return b;
+}
+PG_TT bool nan_b(unsigned long long b) { return (b & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
+// non-NaN values in IEEE order as unsigned order, -0 and +0 one key
+PG_TT unsigned long long okey(unsigned long long b)
+{
+  if ((b << 1) == 0) b = 0;
+  return (long long)b < 0 ? ~b : b | 0x8000000000000000ULL;
+}
+PG_TT bool lt(double x, double y)
+{
+  const unsigned long long a = bits(x), b = bits(y);
+  return !nan_b(a) && !nan_b(b) && okey(a) < okey(b);
+}
+PG_TT bool gt(double x, double y) { return lt(y, x); }
+// x < -y, the sign of y flipped on its bits
+PG_TT bool lt_neg(double x, double y)
+{
+  const unsigned long long a = bits(x), b = bits(y) ^ 0x8000000000000000ULL;
+  return !nan_b(a) && !nan_b(b) && okey(a) < okey(b);
 }
 PG_TT double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
 
@@ -227,8 +265,8 @@ PG_TT bool beyond_plane(const double *const P[3], const double *const Q[3], doub
     double w[3];
     sub(Q[k], P[0], w);
     const double h = dot(n, w);
-    above += h > lim ? 1 : 0;
-    below += h < -lim ? 1 : 0;
+    above += gt(h, lim) ? 1 : 0;
+    below += lt_neg(h, lim) ? 1 : 0;
   }
   return above == 3 || below == 3;
 }

@@ -196,6 +196,13 @@ class GpuEngine:
                   "pg_session_download_range")
         self.model.pull_obstacles()
 
+    def download_range_motion(self, r):
+        """Positions, linear and angular velocities of pool range r alone
+        (pg_session_download_range_motion)."""
+        rr = np.ascontiguousarray(r, dtype=np.int32)
+        abi.check(self.lib.pg_session_download_range_motion(self.sess, ctypes.byref(self.scene), abi.iptr(rr)),
+                  "pg_session_download_range_motion")
+
     def release_range(self, r):
         """Free pool ranges on the device: scene id -1 for their entries."""
         rr = np.ascontiguousarray(r, dtype=np.int32)

@@ -221,7 +221,7 @@ class Server:
     def _unload(self, slot):
         req, r, _, _ = self.active.pop(slot)
         e0, e1, _, _, t0, t1, _, _ = r
-        self.eng.download_range(r)
+        self.eng.download_range_motion(r)          # mass and inertia are the request's own
         P = self.P
         pos = P.P.position[0:3, e0:e1].copy()
         lin = P.P.linear[:, e0:e1].copy()
@@ -321,8 +321,11 @@ class Server:
             c = min(self.chunk, min(v[2] for v in self.active.values()))
             self.eng.run_async(self._tab(c), self.dt)
             # while the chunk runs, copy arrived requests into free ranges of
-            # the host arrays; they go to the device after the wait
-            while pending and (not realtime or pending[0].arrival <= now()) and len(staged) < len(self.slots):
+            # the host arrays, as many as there will be free slots after it
+            # (the free ones and those of the scenes it finishes); they go to
+            # the device after the wait
+            room = len(self.slots) + sum(1 for v in self.active.values() if v[2] == c)
+            while pending and (not realtime or pending[0].arrival <= now()) and len(staged) < room:
                 r = self._stage(pending[0])
                 if r is None:
                     break

@@ -73,3 +73,31 @@ def test_small_pool_queues_and_rejects_malformed(gpu_lib):
             assert r.rid == 99
             continue
         assert np.array_equal(bits(r.position), bits(by[r.rid].position))
+
+
+@pytest.mark.parametrize("form", [1, 0])
+def test_motion_download_equals_full_download(gpu_lib, form):
+    """pg_session_download_range_motion brings back the same position and
+    velocity rows as the full range download."""
+    from parmec_gb300.serving import Server
+    reqs = small_stream(seed=5, count=2)
+    srv = Server(reqs[0].model, reqs[0].dt, form=form, budget_bytes=2e9, max_scenes=2, max_scene_extent=1.0)
+    try:
+        r = srv._load(reqs[1], 0)
+        srv.active[0] = (reqs[1], r, 30, 0.0)
+        srv._update_live()
+        srv.eng.run_async(srv._tab(30), srv.dt)
+        srv.eng.sync()
+        e0, e1 = r[0], r[1]
+        P = srv.P.P
+        srv.eng.download_range_motion(r)
+        got = [P.position[:, e0:e1].copy(), P.linear[:, e0:e1].copy(), P.angular[:, e0:e1].copy()]
+        for a in (P.position, P.linear, P.angular):
+            a[:, e0:e1] = np.nan
+        srv.eng.download_range(r)
+        want = [P.position[:, e0:e1], P.linear[:, e0:e1], P.angular[:, e0:e1]]
+        for g, w in zip(got, want):
+            assert np.array_equal(bits(g), bits(w))
+        assert not np.array_equal(bits(got[0]), bits(reqs[1].model.P.position[:, :e1 - e0]))   # the scene moved
+    finally:
+        srv.close()
