@@ -608,7 +608,7 @@ def main():
     # launch divided by the spheres), scaled to the full drum; the contact
     # group is its three passes (probe, evaluation, sums) together
     traffic_per_unit = {"integrate": 464.0, "contacts": 338.0}
-    fp64_per_unit = {"integrate": 289.0, "contacts": 174.0}
+    fp64_per_unit = {"integrate": 279.0, "contacts": 174.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     fp64 = None
     if dom in fp64_per_unit:
