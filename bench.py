@@ -599,16 +599,18 @@ def main():
     step_bytes = P * (420.0 + 56.0 * c_pair)
     achieved = step_bytes / avg_s / 1e9
     # the kernel's own data (each datum it reads or writes, counted once):
-    # 696 + 53 c_s bytes per particle for the integration (c_s: slave
-    # contacts), 172 + 96 c per sphere for the contacts
-    kernel_model = {"integrate": P * (696.0 + 53.0 * c_pair), "contacts": P * (172.0 + 96.0 * c_pair)}
+    # 652 + 53 c_s + 48 c bytes per particle for the integration (c_s: slave
+    # contacts, c: master contacts, whose force and point it sums), 92 + 48 c
+    # per sphere for the probe and evaluation passes
+    kernel_model = {"integrate": P * (652.0 + 101.0 * c_pair), "contacts": P * (92.0 + 48.0 * c_pair)}
     # DRAM bytes per unit and FP64 instructions per unit of each kernel group,
     # from ncu captures of the 262,144-sphere drum (dram__bytes_read.sum +
     # dram__bytes_write.sum, and DADD + DMUL + DFMA thread instructions, per
     # launch divided by the spheres), scaled to the full drum; the contact
-    # group is its three passes (probe, evaluation, sums) together
-    traffic_per_unit = {"integrate": 464.0, "contacts": 338.0}
-    fp64_per_unit = {"integrate": 279.0, "contacts": 174.0}
+    # group is its probe and evaluation passes, the integration takes the
+    # master-side contact sums
+    traffic_per_unit = {"integrate": 404.0, "contacts": 251.0}
+    fp64_per_unit = {"integrate": 298.0, "contacts": 155.0}
     traffic = traffic_per_unit[dom] * P if dom in traffic_per_unit else None
     fp64 = None
     if dom in fp64_per_unit:

@@ -539,7 +539,9 @@ __global__ void __launch_bounds__(TPB) k_contacts(PgDev d, double step)
 //                     the slot;
 //   k_contacts_sum    one thread per sphere: the master-side force, torque
 //                     and (adaptive) stiffness sums over its slots in slot
-//                     order, as k_contacts sums them.
+//                     order, as k_contacts sums them.  Without adaptive
+//                     stepping k_integrate takes the force and torque sums
+//                     itself, in the same order, and this pass is not run.
 // Every slot takes the same operations as in k_contacts and the sums the
 // same order, so the results are the same bits; the queue's order plays no
 // part.
@@ -1539,7 +1541,27 @@ __global__ void PG_LB_INTEGRATE k_integrate(PgDev d, double step, double half, d
     {
     double grav[3];
     scene_gravity(d, d.pscene[i], step, d.t_gravity + 3*(size_t)row, grav);
-    if (e >= 0)
+    if (e >= 0 && !ADAPT && d.cwork)
+    {
+      // the master side of the sphere's contacts, summed here in slot order
+      // as k_contacts_sum sums them into fm and tm in the adaptive mode
+      double fs[3] = {0.0, 0.0, 0.0}, ts[3] = {0.0, 0.0, 0.0};
+      const int cnt = d.ncnt[e];
+      for (int k = 0; k < cnt; k ++)
+      {
+        const size_t idx = (size_t)k * d.estride + e;
+        if (!d.nflag[idx]) continue;
+        const double f[3] = {d.nfrc[0][idx], d.nfrc[1][idx], d.nfrc[2][idx]};
+        const double a[3] = {d.npnt[0][idx]-po[0], d.npnt[1][idx]-po[1], d.npnt[2][idx]-po[2]};
+        fs[0] += f[0]; fs[1] += f[1]; fs[2] += f[2];
+        ts[0] += a[1]*f[2] - a[2]*f[1];
+        ts[1] += a[2]*f[0] - a[0]*f[2];
+        ts[2] += a[0]*f[1] - a[1]*f[0];
+      }
+      F[0] = fs[0]; F[1] = fs[1]; F[2] = fs[2];
+      T[0] = ts[0]; T[1] = ts[1]; T[2] = ts[2];
+    }
+    else if (e >= 0)
     {
       F[0] = d.fm[0][i]; F[1] = d.fm[1][i]; F[2] = d.fm[2][i];
       T[0] = d.tm[0][i]; T[1] = d.tm[1][i]; T[2] = d.tm[2][i];
@@ -2443,7 +2465,8 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   if (!d.ellnum) return;
   if (d.cwork && d.cwork_n)
   {
-    // three passes (probe, queued evaluation, sums): the same bits as k_contacts
+    // three passes (probe, queued evaluation, sums; the sums in k_integrate
+    // unless adaptive): the same bits as k_contacts
     cudaMemsetAsync(d.cwork_n, 0, sizeof(int), s);
     k_contacts_probe<<<nblk(d.ellnum), TPB, 0, s>>>(d);
     const int nb = eval_blocks();
@@ -2455,9 +2478,9 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
     }
     else
     {
+      // the master-side sums are taken by k_integrate (INT_FUSED, INT_FORCES)
       if (d.record_geometry) k_contacts_eval<true, false><<<nb, TPB, 0, s>>>(d, step);
       else k_contacts_eval<false, false><<<nb, TPB, 0, s>>>(d, step);
-      k_contacts_sum<false><<<nblk(d.ellnum), TPB, 0, s>>>(d);
     }
     return;
   }
@@ -2470,13 +2493,14 @@ void pg_launch_contacts(const PgDev &d, cudaStream_t s, double step)
   else k_contacts<false, false><<<nblk(d.ellnum), TPB, 0, s>>>(d, step);
 }
 
-// the FP64 form evaluates the lists in three passes (one when no work queue
-// is allocated); the mixed form in a sphere and a triangle pass (pg_mixed.cu)
+// the FP64 form evaluates the lists in three passes with adaptive stepping,
+// two otherwise (one when no work queue is allocated); the mixed form in a
+// sphere and a triangle pass (pg_mixed.cu)
 int pg_contacts_kernel_count(const PgDev &d)
 {
   if (!d.ellnum) return 0;
   if (d.form == PG_FORM_MIXED) return 2;
-  return (d.cwork && d.cwork_n) ? 3 : 1;
+  return (d.cwork && d.cwork_n) ? (d.hs ? 3 : 2) : 1;
 }
 
 void pg_launch_springs(const PgDev &d, cudaStream_t s, double step)
