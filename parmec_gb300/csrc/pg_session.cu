@@ -16,6 +16,8 @@
 #include "pg_meshcontact.h"
 #include "../../include/parmec_gb300.h"
 
+#define PG_GRAPH_STEPS 8          // steps per replay of the multi-step graph
+
 struct pg_session
 {
   PgDev d;
@@ -42,6 +44,10 @@ struct pg_session
   double graph_step = 0.0;
   int graph_adapt = 0;                     // the captured step is the adaptive one
   int use_graph = 1;
+  // PG_GRAPH_STEPS copies of the same step in one graph (fewer graph
+  // launches for long runs); dropped with the one-step graph
+  cudaGraph_t graphn = nullptr;
+  cudaGraphExec_t graphn_exec = nullptr;
   // adaptive stepping: device step pair, per-step records and the minimum
   // (PgDev.hs points at hs_buf only while an adaptive run is enqueued)
   double *hs_buf = nullptr;
@@ -905,6 +911,10 @@ void drop_graph(pg_session *s)
   if (s->graph) cudaGraphDestroy(s->graph);
   s->graph_exec = nullptr;
   s->graph = nullptr;
+  if (s->graphn_exec) cudaGraphExecDestroy(s->graphn_exec);
+  if (s->graphn) cudaGraphDestroy(s->graphn);
+  s->graphn_exec = nullptr;
+  s->graphn = nullptr;
   if (s->fgraph_exec) cudaGraphExecDestroy(s->fgraph_exec);
   if (s->fgraph) cudaGraphDestroy(s->fgraph);
   s->fgraph_exec = nullptr;
@@ -1158,6 +1168,18 @@ int capture_step(pg_session *s, double step)
   CK(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
   s->graph_step = step;
   s->graph_adapt = 0;
+  return PG_OK;
+}
+
+// PG_GRAPH_STEPS steps as one graph, for the step of the current one-step graph
+int capture_steps(pg_session *s, double step)
+{
+  TRY(capture_step(s, step));
+  if (s->graphn_exec) return PG_OK;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < PG_GRAPH_STEPS; k ++) enqueue_step(s, step);
+  CK(cudaStreamEndCapture(s->stream, &s->graphn));
+  CK(cudaGraphInstantiate(&s->graphn_exec, s->graphn, 0));
   return PG_OK;
 }
 
@@ -1443,7 +1465,13 @@ static int run_steps(pg_session *s, const pg_steptab *tab, double step, bool wai
   if (!s->profile && s->use_graph && !d.tt_on)
   {
     TRY(capture_step(s, step));
-    for (int k = 0; k < n; k ++) CK(cudaGraphLaunch(s->graph_exec, s->stream));
+    int k = 0;
+    if (n >= PG_GRAPH_STEPS)
+    {
+      TRY(capture_steps(s, step));
+      for (; k + PG_GRAPH_STEPS <= n; k += PG_GRAPH_STEPS) CK(cudaGraphLaunch(s->graphn_exec, s->stream));
+    }
+    for (; k < n; k ++) CK(cudaGraphLaunch(s->graph_exec, s->stream));
   }
   else if (!s->profile)
   {
