@@ -873,43 +873,48 @@ __device__ __forceinline__ void excite_item(const PgDev &d, int sc, double step)
 // Returns whether a vertex left its rebuild neighbourhood.
 __device__ __forceinline__ bool obstacles_item(const PgDev &d, int t, double step, int use_row)
 {
-  bool need = false;
-  int o = d.triown[t];
-  if (o >= 0 && d.tscene[t] >= 0 && d.sactive[d.tscene[t]])
+  const int o = d.triown[t];
+  if (o < 0) return false;
+  // every load that needs only t and o is issued before the scene test, so
+  // that one memory latency covers them (the update is a short chain)
+  const int sc = d.tscene[t];
+  const double *ang, *lin;
+  if (use_row)
   {
-    const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
-    const double *ang, *lin;
-    if (use_row)
-    {
-      int row = *d.stepno;
-      ang = d.t_obs_ang + (size_t)row * d.tab_obs_stride + 3*o;
-      lin = d.t_obs_lin + (size_t)row * d.tab_obs_stride + 3*o;
-    }
-    else
-    {
-      ang = d.obsang + 3*o;
-      lin = d.obslin + 3*o;
-    }
-    const double *x = d.obspnt + 3*o;
-    double y[3], DL[9], z[3];
-    y[0] = x[0] + step*lin[0];
-    y[1] = x[1] + step*lin[1];
-    y[2] = x[2] + step*lin[2];
-    pg::expmap(step*ang[0], step*ang[1], step*ang[2], DL, typo);
-    for (int v = 0; v < 3; v ++)
-    {
-      z[0] = d.tri[3*v+0][t] - x[0];
-      z[1] = d.tri[3*v+1][t] - x[1];
-      z[2] = d.tri[3*v+2][t] - x[2];
-      double n0 = DL[0]*z[0]+DL[3]*z[1]+DL[6]*z[2] + y[0];
-      double n1 = DL[1]*z[0]+DL[4]*z[1]+DL[7]*z[2] + y[1];
-      double n2 = DL[2]*z[0]+DL[5]*z[1]+DL[8]*z[2] + y[2];
-      d.tri[3*v+0][t] = n0;
-      d.tri[3*v+1][t] = n1;
-      d.tri[3*v+2][t] = n2;
-      double r0 = n0 - d.tref[3*v+0][t], r1 = n1 - d.tref[3*v+1][t], r2 = n2 - d.tref[3*v+2][t];
-      need |= (r0*r0 + r1*r1 + r2*r2) > d.half_skin_sq;
-    }
+    const int row = *d.stepno;
+    ang = d.t_obs_ang + (size_t)row * d.tab_obs_stride + 3*o;
+    lin = d.t_obs_lin + (size_t)row * d.tab_obs_stride + 3*o;
+  }
+  else
+  {
+    ang = d.obsang + 3*o;
+    lin = d.obslin + 3*o;
+  }
+  const double *x = d.obspnt + 3*o;
+  double V[9], R[9];
+  for (int k = 0; k < 9; k ++) { V[k] = d.tri[k][t]; R[k] = d.tref[k][t]; }
+  const double a[3] = {ang[0], ang[1], ang[2]}, l[3] = {lin[0], lin[1], lin[2]}, p[3] = {x[0], x[1], x[2]};
+  if (sc < 0 || !d.sactive[sc]) return false;
+  const bool typo = (d.compat & PG_COMPAT_EXPMAP) != 0;
+  bool need = false;
+  double y[3], DL[9], z[3];
+  y[0] = p[0] + step*l[0];
+  y[1] = p[1] + step*l[1];
+  y[2] = p[2] + step*l[2];
+  pg::expmap(step*a[0], step*a[1], step*a[2], DL, typo);
+  for (int v = 0; v < 3; v ++)
+  {
+    z[0] = V[3*v+0] - p[0];
+    z[1] = V[3*v+1] - p[1];
+    z[2] = V[3*v+2] - p[2];
+    double n0 = DL[0]*z[0]+DL[3]*z[1]+DL[6]*z[2] + y[0];
+    double n1 = DL[1]*z[0]+DL[4]*z[1]+DL[7]*z[2] + y[1];
+    double n2 = DL[2]*z[0]+DL[5]*z[1]+DL[8]*z[2] + y[2];
+    d.tri[3*v+0][t] = n0;
+    d.tri[3*v+1][t] = n1;
+    d.tri[3*v+2][t] = n2;
+    double r0 = n0 - R[3*v+0], r1 = n1 - R[3*v+1], r2 = n2 - R[3*v+2];
+    need |= pg::gt_nonneg(r0*r0 + r1*r1 + r2*r2, d.half_skin_sq);
   }
   return need;
 }
@@ -918,25 +923,32 @@ __device__ __forceinline__ bool obstacles_item(const PgDev &d, int t, double ste
 // velocity state, and the step counters (one thread)
 __device__ __forceinline__ void tail_item(const PgDev &d, double step, int use_row)
 {
-  int row = use_row ? *d.stepno : 0;
+  const int row = use_row ? *d.stepno : 0;
+  const long long gs = use_row ? *d.gstep : 0;
   for (int o = 0; o < d.obsnum; o ++)
   {
-    if (d.oscene[o] < 0 || !d.sactive[d.oscene[o]]) continue;
+    // the obstacle's loads first, then its scene test (one memory latency)
+    const int sc = d.oscene[o];
+    double *x = d.obspnt + 3*o;
+    const double p[3] = {x[0], x[1], x[2]};
+    double a[3], v[3];
     if (use_row)
       for (int k = 0; k < 3; k ++)
       {
-        d.obsang[3*o+k] = d.t_obs_ang[(size_t)row * d.tab_obs_stride + 3*o + k];
-        d.obslin[3*o+k] = d.t_obs_lin[(size_t)row * d.tab_obs_stride + 3*o + k];
+        a[k] = d.t_obs_ang[(size_t)row * d.tab_obs_stride + 3*o + k];
+        v[k] = d.t_obs_lin[(size_t)row * d.tab_obs_stride + 3*o + k];
       }
-    double *x = d.obspnt + 3*o;
-    const double *v = d.obslin + 3*o;
-    double y0 = x[0] + step*v[0], y1 = x[1] + step*v[1], y2 = x[2] + step*v[2];
-    x[0] = y0; x[1] = y1; x[2] = y2;
+    else
+      for (int k = 0; k < 3; k ++) v[k] = d.obslin[3*o+k];
+    if (sc < 0 || !d.sactive[sc]) continue;
+    if (use_row)
+      for (int k = 0; k < 3; k ++) { d.obsang[3*o+k] = a[k]; d.obslin[3*o+k] = v[k]; }
+    x[0] = p[0] + step*v[0]; x[1] = p[1] + step*v[1]; x[2] = p[2] + step*v[2];
   }
   if (use_row)
   {
     *d.stepno = row + 1;
-    *d.gstep += 1;
+    *d.gstep = gs + 1;
   }
 }
 

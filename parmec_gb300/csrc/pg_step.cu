@@ -240,7 +240,7 @@ __global__ void k_faces(PgDev d)
           dd += r*r;
         }
       }
-      need |= dd > d.half_skin_sq;
+      need |= gt_nonneg(dd, d.half_skin_sq);
     }
   }
   if (d.ellnum) flag_rebuild(d, need);
