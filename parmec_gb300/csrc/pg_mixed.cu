@@ -194,11 +194,13 @@ __device__ __forceinline__ void mx_centres_item(const PgDev &d, int e)
   }
 }
 
+// launched every step and idle unless a rebuild is due: a grid-stride loop
+// over a grid of a few blocks per SM, so that the idle launch is short
 __global__ void k_mx_centres(PgDev d)
 {
   if (!*d.rebuild) return;
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < d.ellnum) mx_centres_item(d, e);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.ellnum; e += gridDim.x * blockDim.x)
+    mx_centres_item(d, e);
 }
 
 __global__ void k_mx_to64(PgDev d, int p0, int p1)
@@ -698,7 +700,16 @@ void pg_launch_mx_to64(const PgDev &d, cudaStream_t s, int p0, int p1)
 
 void pg_launch_mx_centres(const PgDev &d, cudaStream_t s)
 {
-  if (d.ellnum) k_mx_centres<<<nblk(d.ellnum), TPB, 0, s>>>(d);
+  static int cap = 0;
+  if (!cap)
+  {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cap = 4 * (sms > 0 ? sms : 152);
+  }
+  const int nb = nblk(d.ellnum);
+  if (d.ellnum) k_mx_centres<<<nb < cap ? nb : cap, TPB, 0, s>>>(d);
 }
 
 void pg_launch_contacts_mx(const PgDev &d, cudaStream_t s, double step)
