@@ -34,6 +34,8 @@ void pg_launch_restrain_forces(const PgDev &d, cudaStream_t s);       // drop-in
 void pg_launch_mesh(const PgDev &d, cudaStream_t s);
 void pg_launch_obstacles_row(const PgDev &d, cudaStream_t s, double step);     // velocities from the step table
 void pg_launch_tail(const PgDev &d, cudaStream_t s, double step);
+void pg_launch_obstacles_tail(const PgDev &d, cudaStream_t s, double step);  // both, one launch when it can
+int pg_obstacles_kernel_count(const PgDev &d);
 void pg_launch_excite(const PgDev &d, cudaStream_t s, double step);
 int  pg_step_kernel_count(const PgDev &d);
 

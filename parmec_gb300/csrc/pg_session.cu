@@ -1070,8 +1070,7 @@ void enqueue_step(pg_session *s, double step)
   {
     pg_launch_contacts_mx(d, s->stream, step);
     pg_launch_integrate_mx(d, s->stream, step);
-    pg_launch_obstacles_row(d, s->stream, step);
-    pg_launch_tail(d, s->stream, step);
+    pg_launch_obstacles_tail(d, s->stream, step);
     return;
   }
   pg_launch_contacts(d, s->stream, step);
@@ -1082,8 +1081,7 @@ void enqueue_step(pg_session *s, double step)
   if (d.tt_on) tt_stage(s, step);
   pg_launch_integrate(d, s->stream, step);
   pg_launch_mesh(d, s->stream);
-  pg_launch_obstacles_row(d, s->stream, step);
-  pg_launch_tail(d, s->stream, step);
+  pg_launch_obstacles_tail(d, s->stream, step);
 }
 
 // the mesh-contact stage of one step: pairs, forces and per-particle sums;
@@ -1254,8 +1252,7 @@ void enqueue_step_adaptive(pg_session *s)
   pg_launch_adapt_step(d, s->stream);
   pg_launch_dynamics_fused(d, s->stream);
   pg_launch_mesh(d, s->stream);
-  pg_launch_obstacles_row(d, s->stream, 0.0);
-  pg_launch_tail(d, s->stream, 0.0);
+  pg_launch_obstacles_tail(d, s->stream, 0.0);
 }
 
 int adaptive_kernel_count(const PgDev &d)
@@ -1345,6 +1342,7 @@ int pg_session_create(const pg_scene *sc, int form, pg_session **out)
   if ((r = allocate(s, sc)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.stepno, 1)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.rebuild, 1)) != PG_OK) goto fail;
+  if ((r = dalloc(s, &d.obs_done, 1)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.err, 4)) != PG_OK) goto fail;
   if ((r = dalloc(s, &d.stats, 8)) != PG_OK) goto fail;
   if ((r = contact_buffers(s)) != PG_OK) goto fail;
@@ -1509,13 +1507,12 @@ static int run_steps(pg_session *s, const pg_steptab *tab, double step, bool wai
       CK(cudaEventRecord(ev[4], s->stream));
       pg_launch_mesh(d, s->stream);
       CK(cudaEventRecord(ev[5], s->stream));
-      pg_launch_obstacles_row(d, s->stream, step);
-      pg_launch_tail(d, s->stream, step);
+      pg_launch_obstacles_tail(d, s->stream, step);
       CK(cudaEventRecord(ev[6], s->stream));
     }
     CK(cudaStreamSynchronize(s->stream));
     const int counts[6] = {pg_rebuild_kernel_count(d), pg_contacts_kernel_count(d), d.sprnum ? 1 : 0, d.parnum ? 1 : 0,
-                           (d.nodnum ? 1 : 0) + (d.facnum ? 1 : 0), 1 + ((d.obsnum && d.trinum) ? 1 : 0)};
+                           (d.nodnum ? 1 : 0) + (d.facnum ? 1 : 0), pg_obstacles_kernel_count(d)};
     for (int k = 0; k < n; k ++)
     {
       cudaEvent_t *ev = &s->ring[(size_t)k * (G + 1)];

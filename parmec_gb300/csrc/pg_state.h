@@ -144,6 +144,7 @@ struct PgDev
 
   // ---- rebuild machinery
   int *rebuild;             // 1 when the candidate lists must be rebuilt
+  int *obs_done;            // [1]: blocks of the step's obstacle update that finished (the last runs the tail)
   int *err;                 // [4]: first device error (PG_ERR_*), site, index, value; 0 when fine
   unsigned *gbar;           // [4]: grid barrier of the fused step kernel: arrivals, generation, abort
   int *stats;               // [8]: rebuilds, max candidates, max slave entries, max triangles per sphere

@@ -276,6 +276,40 @@ __global__ void k_tail(PgDev d, double step, int use_row)
   pgk::tail_item(d, step, use_row);
 }
 
+// The row-mode obstacle update with the tail in the same launch: the last
+// block to finish (a counter that it resets) runs the tail, after every
+// block has read the old obstacle points and the step pair.
+__global__ void k_obstacles_tail(PgDev d, double step)
+{
+  const double step0 = step;
+  if (d.hs) step = 0.5*(d.hs[0] + d.hs[1]);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (t < d.trinum) need = pgk::obstacles_item(d, t, step, 1);
+  if (d.ellnum) flag_rebuild(d, need);
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    __threadfence();
+    last = atomicAdd(d.obs_done, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  *d.obs_done = 0;
+  if (d.hs)
+  {
+    const double h1 = d.hs[1];
+    const double st = 0.5*(d.hs[0] + h1);
+    d.hrec[*d.stepno] = h1;
+    pgk::tail_item(d, st, 1);
+    d.hs[0] = h1;
+    return;
+  }
+  pgk::tail_item(d, step0, 1);
+}
+
 using pgk::pairing;
 
 // ---------------------------------------------------------------- contacts
@@ -2620,15 +2654,32 @@ void pg_launch_tail(const PgDev &d, cudaStream_t s, double step)
   k_tail<<<1, 32, 0, s>>>(d, step, 1);
 }
 
+// the obstacle update and the tail of a step: one launch when the session
+// has the completion counter, else the two kernels
+void pg_launch_obstacles_tail(const PgDev &d, cudaStream_t s, double step)
+{
+  if (d.obsnum && d.trinum && d.obs_done) k_obstacles_tail<<<(d.trinum + 31) / 32, 32, 0, s>>>(d, step);
+  else
+  {
+    pg_launch_obstacles_row(d, s, step);
+    pg_launch_tail(d, s, step);
+  }
+}
+
+int pg_obstacles_kernel_count(const PgDev &d)
+{
+  return 1 + ((d.obsnum && d.trinum && !d.obs_done) ? 1 : 0);
+}
+
 int pg_step_kernel_count(const PgDev &d)
 {
-  int n = 2;                                   // excite, tail
+  int n = 1;                                   // excite
   n += pg_contacts_kernel_count(d);            // contacts: sphere and triangle passes
   if (d.sprnum) n += 1 + (d.nbig > 0 ? 2 : 0) + (d.unsprnum ? 1 : 0);
   if (d.trqsprnum) n += 1;                     // torsion springs
   if (d.parnum) n += 1;                        // integrate
   if (d.nodnum) n += 1;
   if (d.facnum) n += 1;
-  if (d.obsnum && d.trinum) n += 1;
+  n += pg_obstacles_kernel_count(d);           // obstacles and tail
   return n;
 }
