@@ -634,7 +634,10 @@ def main():
                 "path": "Model.dem() through the pg_session C ABI: per-step host tables (Python callbacks), "
                         "full host->device upload, K steps, device->host download; host SoA arrays "
                         "page-locked by the engine (cudaHostRegister)",
-                "runs_s": [round(x, 4) for x in e2e_runs], "statistic": "median of five DEM calls"},
+                "runs_s": [round(x, 4) for x in e2e_runs], "statistic": "median of five DEM calls",
+                "segment": f"the five calls continue the same drum from step {2 * args.warmup + 2 * args.steps + 1}, "
+                           f"after the timed steps (from step {args.warmup + 1}) and the profiled ones; "
+                           "each call includes its upload, its first list rebuild and its download"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
