@@ -100,3 +100,19 @@ def test_every_request_runs_its_own_steps(monkeypatch, slots, chunk):
     assert adm == sorted(adm)
     assert stats["pool"]["peak_scenes"] <= slots
     assert not srv.eng.active
+
+
+def test_ranges_first_fit_and_merge():
+    from parmec_gb300.serving import _Ranges
+    r = _Ranges(100)
+    a, b, c = r.take(30), r.take(30), r.take(30)
+    assert (a, b, c) == (0, 30, 60)
+    assert r.take(20) is None                      # 10 left
+    r.give(b, 30)
+    assert r.take(40) is None                      # holes of 30 and 10
+    assert r.take(25) == 30                        # first fit, inside the hole
+    r.give(a, 30)
+    r.give(30, 25)
+    r.give(c, 30)
+    assert r.free == [(0, 100)]                    # everything merged back
+    assert r.take(0) == 0 and r.free == [(0, 100)]
